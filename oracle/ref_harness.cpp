@@ -1,0 +1,201 @@
+// Golden-vector harness: drives the UNMODIFIED reference TwoChNRG routines
+// (linked from the reference sources by oracle/build_ref.sh) through the
+// NRG_main iteration order (src/Main/NRG_main.cpp:282-427) and prints every
+// per-iteration quantity at full precision, so that the CPU oracle
+// restatement and the GPU path can be pinned against the real reference.
+//
+// Test infrastructure only: this file never ships in the product.
+//
+// Usage:
+//   ref_harness <model> <Nsites> <Ncutoff> <Lambda> <U> <ed> <Gamma1> <Gamma2|B>
+//   model: 1chQS   one-channel Anderson, (Q,S) basis   (ModelSwitch SymNo 0 / ModelNo 0)
+//          1chQSz  one-channel Anderson, (Q,Sz) basis  (SymNo 2 / ModelNo 0); last arg = B
+//          2chQS   two-channel Anderson, (Q,S) basis: the impurity H_{-1} of
+//                  OneChQS_SetAnderson_Hm1 coupled to both channels through
+//                  TwoChQS_HN_MatEl with f_ch1 = f_ch2 = d; last arg = Gamma2
+// Output: line records "ITER", "BLK", "EN", "CUT", "THERMO", "OPAVG" (see
+// tests/golden/make_golden.py for the parser).
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <unistd.h>
+#include <vector>
+
+#include "NRGclasses.hpp"
+#include "NRGfunctions.hpp"
+#include "NRGOpMatRules.hpp"
+#include "NRG_main.hpp"
+#include "TwoChQS.hpp"
+
+#ifndef pi
+#define pi 3.141592653589793238462643383279502884197169
+#endif
+
+int OneChQS_SetSingleSite(CNRGbasisarray& SingleSite);
+int OneChQSz_SetSingleSite(CNRGbasisarray& SingleSite);
+int TwoChQS_SetSingleSite(CNRGbasisarray* pSingleSite);
+
+static void print_iter(int N, const std::vector<double>& ParamsHN, CNRGarray& Aeig, double Ecut,
+                       int nkept) {
+  printf("ITER %d", N);
+  for (size_t k = 0; k < ParamsHN.size(); ++k) printf(" %.17g", ParamsHN[k]);
+  printf("\n");
+  printf("BLK %d %d", Aeig.NumBlocks(), Aeig.NQNumbers);
+  for (int b = 0; b < Aeig.NumBlocks(); ++b) {
+    for (int q = 0; q < Aeig.NQNumbers; ++q) printf(" %.17g", Aeig.GetQNumber(b, q));
+    printf(" %d", Aeig.GetBlockSize(b));
+  }
+  printf("\n");
+  printf("EN %d", (int)Aeig.dEn.size());
+  for (size_t k = 0; k < Aeig.dEn.size(); ++k) printf(" %.17g", Aeig.dEn[k]);
+  printf("\n");
+  printf("CUT %.17g %d\n", Ecut, nkept);
+}
+
+int main(int argc, char** argv) {
+  if (argc < 9) {
+    fprintf(stderr, "usage: %s model Nsites Ncutoff Lambda U ed Gamma1 Gamma2|B\n", argv[0]);
+    return 2;
+  }
+  std::string model = argv[1];
+  int Nsites = atoi(argv[2]);
+  int Ncutoff = atoi(argv[3]);
+  double Lambda = atof(argv[4]);
+  double U = atof(argv[5]);
+  double ed = atof(argv[6]);
+  double Gamma1 = atof(argv[7]);
+  double extra = atof(argv[8]);
+
+  // Silence the reference's chatter on stdout: all of it goes to stderr.
+  FILE* real_out = fdopen(dup(fileno(stdout)), "w");
+  fflush(stdout);
+  dup2(fileno(stderr), fileno(stdout));
+  stdout = real_out;
+
+  double HalfLambdaFactor = 0.5 * (1.0 + 1.0 / Lambda);  // NRGcodehandlerClass.cpp:142-146, z=1
+  CNRGchain chain(Lambda);
+  chain.SetChainWilson(Nsites > 100 ? Nsites : 100);      // NRGcodehandlerClass.cpp:222-227
+  double ALambda = sqrt(0.5 * log(Lambda) * (Lambda + 1) / (Lambda - 1));  // NRG_main.cpp:205-207
+
+  CNRGarray Aeig;
+  CNRGbasisarray AeigCut, Abasis, SingleSite;
+  CNRGmatrix HN;
+  HN.NeedOld = false;
+  HN.UpperTriangular = true;
+  HN.CheckForMatEl = Diag_check;
+  std::vector<CNRGmatrix> Mats;
+  std::vector<int> CommonQNs, totSpos;
+  std::vector<double> ParamsHN;
+  bool totalS = true;
+  int sqnumber = 1;
+  int nchan = 1;
+
+  CNRGmatrix aux;
+  if (model == "1chQS") {
+    OneChQS_SetSingleSite(SingleSite);
+    for (int i = 0; i < 4; ++i) Mats.push_back(aux);
+    Mats[0].NeedOld = false; Mats[0].UpperTriangular = false;
+    Mats[0].CheckForMatEl = OneChQS_cd_check; Mats[0].CalcMatEl = OneChQS_fN_MatEl;
+    CNRGmatrix avg; avg.NeedOld = true; avg.UpperTriangular = false; avg.CalcAvg = true;
+    avg.CheckForMatEl = Diag_check; avg.CalcMatEl = ImpOnly_MatEl;
+    Mats[1] = avg; Mats[2] = avg; Mats[3] = avg;
+    strcpy(Mats[1].MatName, "Ndot"); strcpy(Mats[2].MatName, "NdSq"); strcpy(Mats[3].MatName, "SdSq");
+    double chi_m1 = sqrt(2.0 * Gamma1 / pi) / (sqrt(Lambda) * HalfLambdaFactor) * ALambda;
+    std::vector<double> P = {Lambda, HalfLambdaFactor, U, ed, chi_m1};
+    OneChQS_SetAnderson_Hm1(P, &Aeig, Mats);
+    CommonQNs = {2, 0, 1, 0, 1}; totSpos = {1};
+    HN.CalcHNMatEl = OneChQS_HN_MatEl;
+    ParamsHN = {Lambda, chi_m1, 0.0, 0.0};
+  } else if (model == "1chQSz") {
+    OneChQSz_SetSingleSite(SingleSite);
+    for (int i = 0; i < 4; ++i) Mats.push_back(aux);
+    Mats[0].NeedOld = false; Mats[0].CheckForMatEl = OneChQ_cd_check; Mats[0].CalcMatEl = OneChQ_fNup_MatEl;
+    Mats[1].NeedOld = false; Mats[1].CheckForMatEl = OneChQ_cd_check; Mats[1].CalcMatEl = OneChQ_fNdn_MatEl;
+    CNRGmatrix avg; avg.NeedOld = true; avg.UpperTriangular = false; avg.CalcAvg = true;
+    avg.CheckForMatEl = Diag_check; avg.CalcMatEl = ImpOnly_MatEl;
+    Mats[2] = avg; Mats[3] = avg;
+    strcpy(Mats[2].MatName, "Ndot"); strcpy(Mats[3].MatName, "Szdot");
+    std::vector<double> P = {U, ed, Lambda, HalfLambdaFactor, extra};
+    OneChQSz_SetAnderson_Hm1(P, &Aeig, Mats);
+    CommonQNs = {2, 0, 1, 0, 1}; totSpos.clear();
+    HN.CalcHNMatEl = OneChQSz_HN_MatEl;
+    double chi_m1 = sqrt(2.0 * Gamma1 / pi) / (sqrt(Lambda) * HalfLambdaFactor) * ALambda;
+    ParamsHN = {Lambda, chi_m1, 0.0, 0.0};
+    totalS = false;
+  } else if (model == "2chQS") {
+    TwoChQS_SetSingleSite(&SingleSite);
+    // Impurity H_{-1} and its reduced <||d||> from the one-channel set-up.
+    std::vector<CNRGmatrix> M1(4, aux);
+    strcpy(M1[1].MatName, "Ndot"); strcpy(M1[2].MatName, "NdSq"); strcpy(M1[3].MatName, "SdSq");
+    double chi1 = sqrt(2.0 * Gamma1 / pi) / (sqrt(Lambda) * HalfLambdaFactor) * ALambda;
+    double chi2 = sqrt(2.0 * extra / pi) / (sqrt(Lambda) * HalfLambdaFactor) * ALambda;
+    std::vector<double> P = {Lambda, HalfLambdaFactor, U, ed, chi1};
+    OneChQS_SetAnderson_Hm1(P, &Aeig, M1);
+    Mats.push_back(M1[0]);  // f_ch1 = d
+    Mats.push_back(M1[0]);  // f_ch2 = d
+    Mats.push_back(M1[1]); Mats.push_back(M1[2]); Mats.push_back(M1[3]);
+    for (int i = 0; i < 2; ++i) {
+      Mats[i].NeedOld = false; Mats[i].UpperTriangular = false;
+      Mats[i].CheckForMatEl = TwoChQS_cd_check;
+      Mats[i].CalcMatEl = (i == 0) ? TwoChQS_fNch1_MatEl : TwoChQS_fNch2_MatEl;
+    }
+    for (int i = 2; i < 5; ++i) {
+      Mats[i].NeedOld = true; Mats[i].UpperTriangular = false; Mats[i].CalcAvg = true;
+      Mats[i].CheckForMatEl = Diag_check; Mats[i].CalcMatEl = ImpOnly_MatEl;
+    }
+    CommonQNs = {2, 0, 1, 0, 1}; totSpos = {1};
+    HN.CalcHNMatEl = TwoChQS_HN_MatEl;
+    ParamsHN = {Lambda, chi1, chi2, 0.0, 0.0};
+    nchan = 2;
+  } else {
+    fprintf(stderr, "unknown model %s\n", model.c_str());
+    return 2;
+  }
+
+  double betabar = 0.727;  // NRG_main.cpp:96
+  CutStates(Aeig, AeigCut, Ncutoff);  // NRG_main.cpp:239
+  // Op averages for H_{-1} (CalcStuff at NRG_main.cpp:262)
+  {
+    std::vector<double> Pb = {betabar};
+    printf("OPAVG -1");
+    for (size_t i = 0; i < Mats.size(); ++i)
+      if (Mats[i].CalcAvg) printf(" %s %.17g", Mats[i].MatName, CalcOpAvg(Pb, &AeigCut, &Mats[i], totalS, sqnumber));
+    printf("\n");
+  }
+
+  for (int N = 0; N < Nsites; ++N) {
+    double DN = HalfLambdaFactor * pow(Lambda, (-(N - 1) / 2.0));  // NRG_main.cpp:283
+    BuildBasis(CommonQNs, totSpos, &AeigCut, &Abasis, &SingleSite, 0);
+    HN.DiagHN(ParamsHN, &Abasis, &SingleSite, &Mats[0], &Aeig, false);
+    Aeig.SetKept(Ncutoff);
+    int nk = 0;
+    for (size_t k = 0; k < Aeig.Kept.size(); ++k) nk += Aeig.Kept[k] ? 1 : 0;
+    double Ecut = Aeig.Ecut(Ncutoff);
+    print_iter(N, ParamsHN, Aeig, Ecut, nk);
+    // Thermodynamics at the four betabar values of CNRGCodeHandler::CalcThermo
+    // (NRGcodehandlerClass.cpp:643-672), raw Calc values.
+    for (int nc = 1; nc <= 4; ++nc) {
+      double bN = betabar * pow(Lambda, (nc - 4) / (2.0 * 4));
+      std::vector<double> Pb = {bN};
+      printf("THERMO %d %.17g %.17g %.17g %.17g\n", nc, bN, DN / bN,
+             CalcSuscep(Pb, &Aeig, sqnumber, totalS), CalcEntropy(Pb, &Aeig, sqnumber, totalS));
+    }
+    CutStates(Aeig, AeigCut, Ncutoff);
+    UpdateMatrices(&SingleSite, &AeigCut, &Abasis, &Mats[0], (int)Mats.size(), false);
+    {
+      std::vector<double> Pb = {betabar};
+      printf("OPAVG %d", N);
+      for (size_t i = 0; i < Mats.size(); ++i)
+        if (Mats[i].CalcAvg) printf(" %s %.17g", Mats[i].MatName, CalcOpAvg(Pb, &AeigCut, &Mats[i], totalS, sqnumber));
+      printf("\n");
+    }
+    printf("KEPTBLK %d", AeigCut.NumBlocks());
+    for (int b = 0; b < AeigCut.NumBlocks(); ++b) printf(" %d", AeigCut.GetBlockSize(b));
+    printf("\n");
+    for (int ich = 0; ich < nchan; ++ich) ParamsHN[ich + 1] = chain.GetChin(N);  // NRG_main.cpp:402-405
+  }
+  fflush(stdout);
+  return 0;
+}
