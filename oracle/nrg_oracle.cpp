@@ -1,0 +1,1073 @@
+// CPU oracle: a plain C++ restatement of the TwoChNRG iterative
+// diagonalization (the NRG_main sweep) used ONLY as the checker by tests/,
+// __graft_entry__.smoke() and bench.py's CPU baseline.  It is test
+// infrastructure, never part of the product path.
+//
+// Every routine follows the reference function it cites (paths relative to
+// the TwoChNRG source tree).  The restatement keeps the reference's data
+// model (block-concatenated state vectors, BlockBegEnd pairs, row-wise
+// per-block eigenvectors, MatBlockMap/MatBlockBegEnd/MatEl operators), its
+// element-by-element Hamiltonian and operator rules and its LAPACK dspev /
+// CBLAS dgemm calls, so its arithmetic is that of the reference.  LAPACK and
+// BLAS come from the OpenBLAS bundled with scipy, loaded at run time.
+//
+// Parity pin: the outputs of this file are compared against (a) the
+// reference's own golden log Runs/run1/output_NRG_test.txt and (b) full-
+// precision fixtures produced by the unmodified reference through
+// oracle/ref_harness.cpp (tests/golden/).
+#include "nrg_oracle.h"
+
+#include <dlfcn.h>
+
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <thread>
+#include <utility>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------- LAPACK/BLAS
+typedef void (*dspev_t)(const char*, const char*, const int*, double*, double*, double*,
+                        const int*, double*, int*, size_t, size_t);
+typedef void (*dgemm_t)(int, int, int, int, int, int, double, const double*, int, const double*,
+                        int, double, double*, int);
+typedef void (*setthreads_t)(int);
+dspev_t g_dspev = nullptr;
+dgemm_t g_dgemm = nullptr;
+setthreads_t g_setthreads = nullptr;
+std::string g_err;
+
+const int kRowMajor = 101, kNoTrans = 111, kTrans = 112;
+
+// ---------------------------------------------------------------- helpers
+// dEqual.cpp:6 — absolute 1e-20 comparison used for quantum numbers.
+inline bool dEq(double a, double b) { return std::fabs(a - b) < 1.e-20; }
+// dEqual.cpp:17 — A<B or |A-B|<1e-20.
+inline bool dLEq(double a, double b) { return (a < b) || (std::fabs(a - b) < 1.e-20); }
+
+// gsl_sf_fact(n): n! rounded once to double (exact integer product in 128 bits).
+double fact(int n) {
+  if (n < 0) return 0.0;
+  unsigned __int128 p = 1;
+  for (int k = 2; k <= n; ++k) p *= (unsigned)k;
+  return (double)p;
+}
+
+// CGordan.cpp:34-120 — Clebsch-Gordan <J1 M1; J2 M2 | J M> (Landau-Lifshitz form).
+double cgordan(double J1, double M1, double J2, double M2, double J, double M) {
+  if ((J1 < 0.0) || (J2 < 0.0) || (J < 0.0)) return 0.0;
+  if ((std::fabs(M1) > J1) || (std::fabs(M2) > J2) || (std::fabs(M) > J)) return 0.0;
+  if (std::fabs(M - (M1 + M2)) > 1.0e-10) return 0.0;
+  if ((J > (J1 + J2)) || (J < std::fabs(J1 - J2))) return 0.0;
+  double a0 = fact((int)(J1 + J2 - J)), a1 = fact((int)(J1 - J2 + J)), a2 = fact((int)(-J1 + J2 + J));
+  double a3 = 2 * J + 1, a4 = fact((int)(J1 + J2 + J + 1));
+  double a5 = a0 * a1 * a2 * a3 / a4;
+  double rho = a5 > 0.0 ? std::sqrt(a5) : 0.0;
+  double s0 = fact((int)(J + M)), s1 = fact((int)(J - M)), s2 = fact((int)(J1 + M1));
+  double s3 = fact((int)(J1 - M1)), s4 = fact((int)(J2 + M2)), s5 = fact((int)(J2 - M2));
+  double s6 = s0 * s1 * s2 * s3 * s4 * s5;
+  double sigma = s6 > 0.0 ? std::sqrt(s6) : 0.0;
+  int b1[] = {(int)(J1 - M1), (int)(J2 + M2), (int)(J1 + J2 - J)};
+  int rmax = *std::min_element(b1, b1 + 3);
+  int b2[] = {-(int)(J - J2 + M1), -(int)(J - J1 - M2), 0};
+  int rmin = *std::max_element(b2, b2 + 3);
+  double tau = 0.0;
+  for (int r = rmin; r <= rmax; r++) {
+    double t0 = fact((int)(J1 - M1) - r), t1 = fact((int)(J2 + M2) - r), t2 = fact((int)(J - J2 + M1) + r);
+    double t3 = fact((int)(J - J1 - M2) + r), t4 = fact((int)(J1 + J2 - J) - r), t5 = fact(r);
+    double t6 = 1.0 / (t0 * t1 * t2 * t3 * t4 * t5);
+    tau += std::pow(-1.0, r) * t6;
+  }
+  return rho * sigma * tau;
+}
+
+// CGordan.cpp:13 — triangle inequality with a 1e-10 tolerance.
+bool triang(double J1, double J2, double J) {
+  return !((J - (J1 + J2) > 1.0e-10) || (J - std::fabs(J1 - J2) < -1.0e-10));
+}
+
+// Memoised CG: the reference calls CGordan ~1e7 times per sweep; the value is
+// a pure function of its six arguments, so caching it changes no result.
+struct CGCache {
+  std::map<std::array<double, 6>, double> m;
+  double operator()(double a, double b, double c, double d, double e, double f) {
+    std::array<double, 6> k{a, b, c, d, e, f};
+    auto it = m.find(k);
+    if (it != m.end()) return it->second;
+    double v = cgordan(a, b, c, d, e, f);
+    m.emplace(k, v);
+    return v;
+  }
+};
+
+// ---------------------------------------------------------------- containers
+// CNRGarray (include/NRGclasses.hpp:47-200).
+struct Arr {
+  int nshell = 0, nqn = 0;
+  std::vector<double> qn;
+  std::vector<int> bbe;         // BlockBegEnd pairs
+  std::vector<double> en;       // dEn
+  std::vector<double> evec;     // dEigVec, block-concatenated, row = eigenvector
+  std::vector<char> kept;       // Kept
+  bool totalS = false;
+  std::vector<int> sqn;         // Sqnumbers
+  int nblocks() const { return nqn ? (int)qn.size() / nqn : 0; }
+  int beg(int b) const { return b < 0 ? 0 : bbe[2 * b]; }
+  int end(int b) const { return b < 0 ? 0 : bbe[2 * b + 1]; }
+  int bsize(int b) const { return bbe[2 * b + 1] - bbe[2 * b] + 1; }
+  int nstates() const { return bbe.empty() ? 0 : bbe.back() - bbe.front() + 1; }
+  double q(int b, int k) const { return qn.empty() ? 0.0 : qn[(size_t)b * nqn + k]; }
+  // GetBlockFromSt (NRGarrayClass.cpp:374): first block whose end >= ist.
+  int block_of(int ist, int& pos) const {
+    int lo = 0, hi = nblocks() - 1;
+    while (lo < hi) {
+      int mid = (lo + hi) / 2;
+      if (ist > bbe[2 * mid + 1]) lo = mid + 1; else hi = mid;
+    }
+    pos = ist - bbe[2 * lo];
+    return lo;
+  }
+  // GetBlockFromQNumbers (NRGarrayClass.cpp:514): first block whose QNs all
+  // match within 1e-20, -1 if none.
+  int block_of_qn(const double* q) const {
+    for (int b = 0; b < nblocks(); ++b) {
+      bool ok = true;
+      for (int k = 0; k < nqn && ok; ++k) ok = dEq(qn[(size_t)b * nqn + k], q[k]);
+      if (ok) return b;
+    }
+    return -1;
+  }
+};
+
+// CNRGbasisarray (NRGclasses.hpp:215-349).
+struct Basis : Arr {
+  std::vector<int> itype, stcf, bbe_bc, bbe_eig;
+  int bsize_bc(int b) const { return bbe_bc[2 * b + 1] - bbe_bc[2 * b] + 1; }
+};
+
+// CNRGmatrix (NRGclasses.hpp:365-759) for real, non-packed operators.
+struct Mat {
+  Arr blk;                         // the synced block structure it acts on
+  std::vector<int> map, mbe;
+  std::vector<double> el;
+  std::map<std::pair<int, int>, int> index;  // FindMatBlock (NRGmatrixClass.cpp:33)
+  bool need_old = false, calc_avg = false;
+  std::string name;
+  int rule = 0;  // operator rule id (see OpRule)
+  void clear_data() { map.clear(); mbe.clear(); el.clear(); index.clear(); }
+  void push_block(int i, int j, const double* v, int n) {
+    index.emplace(std::make_pair(i, j), (int)map.size() / 2);
+    map.push_back(i); map.push_back(j);
+    int b = (int)el.size();
+    mbe.push_back(b); mbe.push_back(b + n - 1);
+    el.insert(el.end(), v, v + n);
+  }
+  // GetMatEl (NRGmatrixClass.cpp:174) -> GetBlockMatEl (:131).
+  double get(int ist, int jst) const {
+    int pi, pj;
+    int bi = blk.block_of(ist, pi), bj = blk.block_of(jst, pj);
+    auto it = index.find(std::make_pair(bi, bj));
+    if (it == index.end() || pi < 0 || pj < 0) return 0.0;
+    int n2 = blk.bsize(bj);
+    return el[(size_t)mbe[2 * it->second] + (size_t)pi * n2 + pj];
+  }
+};
+
+// ---------------------------------------------------------------- site tables
+// OneCh_fd_table (OpTables.cpp:8-33): <type_i| f^dagger_sigma |type_j>.
+double onech_fd(int sigma, int ti, int tj) {
+  if (sigma == 1) { if (ti == 1 && tj == 0) return 1.0; if (ti == 3 && tj == 2) return 1.0; return 0.0; }
+  if (sigma == -1) { if (ti == 2 && tj == 0) return 1.0; if (ti == 3 && tj == 1) return -1.0; return 0.0; }
+  return 0.0;
+}
+
+// TwoChQS_fd_table (TwoChQS_OpTables.cpp:20-130) in the 16-state site basis
+// of TwoChQS_SetSingleSite.  The table entries are the reference's.
+double twoch_fd(int ch, int sigma, int ti, int tj) {
+  if (ti < 0 || tj < 0 || ti > 15 || tj > 15) return 0.0;
+  double M[16][16] = {{0.0}};
+  const double r = 1.0 / std::sqrt(2.0), mr = -1.0 / std::sqrt(2.0);
+  if (ch == 1 && sigma == 1) {
+    M[2][0] = 1; M[10][1] = 1; M[9][3] = r; M[11][6] = 1; M[5][3] = r;
+    M[7][4] = 1; M[12][9] = r; M[12][5] = mr; M[14][8] = 1; M[15][13] = 1;
+  } else if (ch == 1 && sigma == -1) {
+    M[4][0] = 1; M[9][1] = r; M[5][1] = mr; M[8][3] = 1; M[13][6] = 1;
+    M[7][2] = -1; M[12][10] = -1; M[14][9] = mr; M[14][5] = mr; M[15][11] = -1;
+  } else if (ch == 2 && sigma == 1) {
+    M[1][0] = 1; M[6][3] = 1; M[10][2] = -1; M[11][9] = mr; M[11][5] = mr;
+    M[9][4] = mr; M[5][4] = r; M[13][8] = -1; M[12][7] = 1; M[15][14] = 1;
+  } else if (ch == 2 && sigma == -1) {
+    M[3][0] = 1; M[6][1] = -1; M[9][2] = mr; M[11][10] = 1; M[5][2] = mr;
+    M[8][4] = -1; M[13][9] = r; M[13][5] = mr; M[14][7] = 1; M[15][12] = -1;
+  } else {
+    return 0.0;
+  }
+  return M[ti][tj];
+}
+
+// TwoChQS_SpSm_table (TwoChQS_OpTables.cpp:140-185): 1 on the diagonal and on
+// the pairs connected by S+/S- within a channel, else 0.
+double twoch_spsm(int ti, int tj) {
+  if (ti == tj) return 1.0;
+  static const int pairs[][2] = {{1, 3}, {2, 4}, {11, 13}, {12, 14}, {8, 9}, {9, 10}, {8, 10}};
+  for (auto& p : pairs)
+    if ((p[0] == ti && p[1] == tj) || (p[1] == ti && p[0] == tj)) return 1.0;
+  return 0.0;
+}
+
+void add_site_block(Basis& s, std::initializer_list<double> q, int b, int e) {
+  for (double v : q) s.qn.push_back(v);
+  s.bbe.push_back(b); s.bbe.push_back(e);
+}
+
+// OneChQS_SetSingleSite (OneChQS_SetSingleSite.cpp:5-44).
+Basis site_1chQS() {
+  Basis s; s.nqn = 3; s.totalS = true; s.sqn = {1};
+  add_site_block(s, {-1, 0, 0}, 0, 0); add_site_block(s, {0, 0.5, 0.5}, 1, 1);
+  add_site_block(s, {0, 0.5, -0.5}, 2, 2); add_site_block(s, {1, 0, 0}, 3, 3);
+  for (int i = 0; i < 4; ++i) s.itype.push_back(i);
+  return s;
+}
+// OneChQSz_SetSingleSite (Main/Main_SetSingleSite.cpp:347-380).
+Basis site_1chQSz() {
+  Basis s; s.nqn = 2; s.totalS = false;
+  add_site_block(s, {-1, 0}, 0, 0); add_site_block(s, {0, 0.5}, 1, 1);
+  add_site_block(s, {0, -0.5}, 2, 2); add_site_block(s, {1, 0}, 3, 3);
+  for (int i = 0; i < 4; ++i) s.itype.push_back(i);
+  return s;
+}
+// TwoChQS_SetSingleSite (TwoChQS_SetSingleSite.cpp:5-124): 16 states in 10 blocks.
+Basis site_2chQS() {
+  Basis s; s.nqn = 3; s.totalS = true; s.sqn = {1};
+  add_site_block(s, {-2, 0, 0}, 0, 0);
+  add_site_block(s, {-1, 0.5, 0.5}, 1, 2);
+  add_site_block(s, {-1, 0.5, -0.5}, 3, 4);
+  add_site_block(s, {0, 0, 0}, 5, 7);
+  add_site_block(s, {0, 1, -1}, 8, 8);
+  add_site_block(s, {0, 1, 0}, 9, 9);
+  add_site_block(s, {0, 1, 1}, 10, 10);
+  add_site_block(s, {1, 0.5, 0.5}, 11, 12);
+  add_site_block(s, {1, 0.5, -0.5}, 13, 14);
+  add_site_block(s, {2, 0, 0}, 15, 15);
+  for (int i = 0; i < 16; ++i) s.itype.push_back(i);
+  return s;
+}
+
+// ---------------------------------------------------------------- rules
+enum OpRule { R_F_QS = 1, R_FUP_QSZ, R_FDN_QSZ, R_F1_2CH, R_F2_2CH, R_IMPONLY };
+enum Check { C_DIAG = 1, C_QS_CD, C_Q_CD, C_2CH_CD };
+
+struct Model {
+  int kind;          // ORACLE_MODEL_*
+  Basis site;
+  std::vector<int> common{2, 0, 1, 0, 1}, totS;
+  int nchan = 1;
+  std::vector<int> op_rule, op_check;  // per operator
+};
+
+// CheckForMatEl rules: Diag_check OpMatRules.cpp:12, OneChQS_cd_check :106,
+// OneChQ_cd_check :92, TwoChQS_cd_check TwoChQS_OpMatRules.cpp:16.
+bool check(int c, const Arr& a, int i, int j) {
+  switch (c) {
+    case C_DIAG: return i == j;
+    case C_QS_CD: return dEq(a.q(j, 0), a.q(i, 0) + 1.0) &&
+                         (dEq(a.q(j, 1), a.q(i, 1) + 0.5) || dEq(a.q(j, 1), a.q(i, 1) - 0.5));
+    case C_Q_CD: return dEq(a.q(j, 0), a.q(i, 0) + 1.0);
+    case C_2CH_CD: return dEq(a.q(j, 0), a.q(i, 0) + 1.0) &&
+                          (dEq(a.q(j, 1), a.q(i, 1) + 0.5) || dEq(a.q(j, 1), a.q(i, 1) - 0.5));
+  }
+  return false;
+}
+
+struct Ctx {
+  Model m;
+  CGCache cg;
+};
+
+double qn_from_st(const Arr& a, int ist, int k) { int p; int b = a.block_of(ist, p); return a.q(b, k); }
+
+// OneChQS_HN_MatEl (OpMatRules.cpp:1410-1535).
+double hn_1chQS(Ctx& c, const std::vector<double>& P, const Basis& ab, const std::vector<Mat>& M,
+                int ist, int jst) {
+  const Basis& ss = c.m.site;
+  double Lambda = P[0], chi_N = P[1], eN = P[2];
+  double Qi = qn_from_st(ab, ist, 0), Si = qn_from_st(ab, ist, 1);
+  double Qj = qn_from_st(ab, jst, 0), Sj = qn_from_st(ab, jst, 1);
+  if (!dEq(Qi, Qj) || !dEq(Si, Sj)) return 0.0;
+  if (ist == jst) {
+    double v = std::sqrt(Lambda) * ab.en[ist];
+    double Qt = qn_from_st(ss, ab.itype[ist], 0);
+    return v + eN * (Qt + 1.0);
+  }
+  int ti = ab.itype[ist], tj = ab.itype[jst];
+  double Old = M[0].get(ab.stcf[ist], ab.stcf[jst]);
+  int typep = ti, type = tj;
+  if (dEq(Old, 0.0)) { Old = M[0].get(ab.stcf[jst], ab.stcf[ist]); typep = tj; type = ti; }
+  double Qtp = ss.q(typep, 0), Stp = ss.q(typep, 1), Sztp = ss.q(typep, 2);
+  double Qt = ss.q(type, 0), St = ss.q(type, 1), Szt = ss.q(type, 2);
+  double Scfp = Si - Sztp, Scf = Si - Szt;
+  double FermiSign = dEq(Qt, 0.0) ? -1.0 : 1.0;
+  double Coef = 0.0;
+  double sqp[3] = {Qtp, Stp, Sztp}, sq[3] = {Qt, St, Szt};
+  for (double Sz = -St; Sz <= St; Sz += 1.0) {
+    sq[2] = Sz;
+    int sst = ss.block_of_qn(sq);
+    for (int sigma = -1; sigma <= 1; sigma += 2) {
+      double dS = 0.5 * (double)sigma;
+      double Szcf = Si - Sz, Szcfp = Szcf - dS, Szp = Sz + dS;
+      sqp[2] = Sz + dS;
+      int sstp = ss.block_of_qn(sqp);
+      double a0 = c.cg(Scf, Szcf, St, Sz, Si, Si);
+      double a1 = c.cg(Scfp, Szcfp, Stp, Szp, Si, Si);
+      double a2 = c.cg(Scfp, Szcfp, 0.5, dS, Scf, Szcf);
+      double a3 = onech_fd(sigma, sstp, sst);
+      Coef += a0 * a1 * a2 * a3;
+    }
+  }
+  return chi_N * Old * Coef * FermiSign;
+}
+
+// OneChQSz_HN_MatEl (OpMatRules.cpp:431-537).
+double hn_1chQSz(Ctx& c, const std::vector<double>& P, const Basis& ab, const std::vector<Mat>& M,
+                 int ist, int jst) {
+  const Basis& ss = c.m.site;
+  double Lambda = P[0], chi_N = P[1], eN = P[2];
+  double Qi = qn_from_st(ab, ist, 0), Szi = qn_from_st(ab, ist, 1);
+  double Qj = qn_from_st(ab, jst, 0), Szj = qn_from_st(ab, jst, 1);
+  if (!dEq(Qi, Qj) || !dEq(Szi, Szj)) return 0.0;
+  if (ist == jst) {
+    double v = std::sqrt(Lambda) * ab.en[ist];
+    double Qt = qn_from_st(ss, ab.itype[ist], 0);
+    return v + eN * (Qt + 1.0);
+  }
+  int ti = ab.itype[ist], tj = ab.itype[jst];
+  double v = 0.0;
+  int imat = 0;
+  for (int isigma = 1; isigma >= -1; isigma -= 2) {
+    int typep = ti, type = tj;
+    double Old = M[imat].get(ab.stcf[ist], ab.stcf[jst]);
+    if (dEq(Old, 0.0)) { Old = M[imat].get(ab.stcf[jst], ab.stcf[ist]); typep = tj; type = ti; }
+    double Qt = qn_from_st(ss, type, 0);
+    double FermiSign = dEq(Qt, 0.0) ? -1.0 : 1.0;
+    v += FermiSign * Old * onech_fd(isigma, typep, type);
+    imat++;
+  }
+  return v * chi_N;
+}
+
+// TwoChQS_HN_MatEl (TwoChQS_OpMatRules.cpp:794-986).
+double hn_2chQS(Ctx& c, const std::vector<double>& P, const Basis& ab, const std::vector<Mat>& M,
+                int ist, int jst) {
+  const Basis& ss = c.m.site;
+  double Lambda = P[0], chi[2] = {P[1], P[2]};
+  double Qi = qn_from_st(ab, ist, 0), Si = qn_from_st(ab, ist, 1);
+  double Qj = qn_from_st(ab, jst, 0), Sj = qn_from_st(ab, jst, 1);
+  if (!dEq(Qi, Qj) || !dEq(Si, Sj)) return 0.0;
+  if (ist == jst) return std::sqrt(Lambda) * ab.en[ist];
+  double v = 0.0;
+  int ti = ab.itype[ist], tj = ab.itype[jst];
+  int ci = ab.stcf[ist], cj = ab.stcf[jst];
+  for (int ich = 1; ich <= 2; ich++) {
+    double Old = M[ich - 1].get(ci, cj);
+    int typep = ti, type = tj;
+    if (dEq(std::fabs(Old), 0.0)) { Old = M[ich - 1].get(cj, ci); typep = tj; type = ti; }
+    int pos;
+    int bp = ss.block_of(typep, pos), b = ss.block_of(type, pos);
+    double Stp = ss.q(bp, 1), Sztp = ss.q(bp, 2);
+    double St = ss.q(b, 1), Szt = ss.q(b, 2);
+    double Soldp = Si - Sztp, Sold = Si - Szt;
+    double FermiSign = (dEq(Szt, 0.5) || dEq(Szt, -0.5)) ? -1.0 : 1.0;
+    double sqp[3] = {ss.q(bp, 0), ss.q(bp, 1), ss.q(bp, 2)};
+    double sq[3] = {ss.q(b, 0), ss.q(b, 1), ss.q(b, 2)};
+    for (int sigma = -1; sigma <= 1; sigma += 2) {
+      double dS = 0.5 * (double)sigma;
+      double Full = 0.0;
+      for (double Szold = Sold; Szold >= -Sold; Szold -= 1.0) {
+        double Szoldp = Szold - dS;
+        double Sz = Si - Szold, Szp = Sz + dS;
+        sqp[2] = Szp; sq[2] = Sz;
+        int sbp = ss.block_of_qn(sqp), sb = ss.block_of_qn(sq);
+        if (dLEq(std::fabs(Szp), Stp) && dLEq(std::fabs(Szold), Sold) && dLEq(std::fabs(Szoldp), Soldp)) {
+          double a0 = c.cg(Sold, Szold, St, Sz, Si, Si);
+          double a1 = c.cg(Soldp, Szoldp, Stp, Szp, Si, Si);
+          double a2 = c.cg(Soldp, Szoldp, 0.5, dS, Sold, Szold);
+          for (int sp = ss.beg(sbp); sp <= ss.end(sbp); sp++)
+            for (int s = ss.beg(sb); s <= ss.end(sb); s++) {
+              double x0 = twoch_spsm(s, type), x1 = twoch_spsm(sp, typep);
+              double a3 = twoch_fd(ich, sigma, sp, s);
+              Full += a0 * a1 * a2 * a3 * FermiSign * x0 * x1;
+            }
+        }
+      }
+      v += chi[ich - 1] * Old * Full;
+    }
+  }
+  return v;
+}
+
+// OneChQS_fN_MatEl (OpMatRules.cpp:1167-1244).
+double op_f_QS(Ctx& c, const Basis& ab, int ist, int jst) {
+  const Basis& ss = c.m.site;
+  double Si = qn_from_st(ab, ist, 1), Sj = qn_from_st(ab, jst, 1);
+  int ti = ab.itype[ist], tj = ab.itype[jst];
+  if (ab.stcf[ist] != ab.stcf[jst]) return 0.0;
+  double Qti = ss.q(ti, 0), Sti = ss.q(ti, 1), Szti = ss.q(ti, 2);
+  double Qtj = ss.q(tj, 0), Stj = ss.q(tj, 1), Sztj = ss.q(tj, 2);
+  double sqi[3] = {Qti, Sti, Szti}, sqj[3] = {Qtj, Stj, Sztj};
+  double Scfi = Si - Szti, Scfj = Sj - Sztj;
+  double aux0 = 0.0, cg0 = 0.0, cg1 = 0.0;
+  double sigma = Sj - Si;
+  for (double Sz = -Stj; Sz <= Stj; Sz += 1.0) {
+    sqj[2] = Sz;
+    int ssj = ss.block_of_qn(sqj);
+    sqi[2] = Sz - sigma;
+    int ssi = ss.block_of_qn(sqi);
+    cg0 = c.cg(Scfi, Si - Sz + sigma, Sti, Sz - sigma, Si, Si);
+    cg1 = c.cg(Scfj, Sj - Sz, Stj, Sz, Sj, Sj);
+    aux0 += onech_fd((int)(sigma / 0.5), ssj, ssi) * cg0 * cg1;
+  }
+  double n0 = c.cg(Si, Si, 0.5, sigma, Sj, Sj);
+  if (!dEq(n0, 0.0)) return aux0 / n0;
+  if (!dEq(cg1, 0.0)) return 0.0 / cg1;
+  return 0.0;
+}
+
+// OneChQ_fN_MatEl (OpMatRules.cpp:1003-1033), sigma = +1 (up) / -1 (dn).
+double op_f_QSz(const Basis& ab, int ist, int jst, int isigma) {
+  if (ab.stcf[ist] == ab.stcf[jst]) return onech_fd(isigma, ab.itype[jst], ab.itype[ist]);
+  return 0.0;
+}
+
+// TwoChQS_fN_MatEl (TwoChQS_OpMatRules.cpp:1205-1352).
+double op_f_2ch(Ctx& c, const Basis& ab, int ist, int jst, int ich) {
+  const Basis& ss = c.m.site;
+  double Si = qn_from_st(ab, ist, 1), Sj = qn_from_st(ab, jst, 1);
+  int ti = ab.itype[ist], tj = ab.itype[jst];
+  if (ab.stcf[ist] != ab.stcf[jst]) return 0.0;
+  int pos;
+  int bi = ss.block_of(ti, pos), bj = ss.block_of(tj, pos);
+  double Sti = ss.q(bi, 1), Szti = ss.q(bi, 2), Stj = ss.q(bj, 1), Sztj = ss.q(bj, 2);
+  (void)Sti; (void)Stj;
+  double sqi[3] = {ss.q(bi, 0), ss.q(bi, 1), ss.q(bi, 2)};
+  double sqj[3] = {ss.q(bj, 0), ss.q(bj, 1), ss.q(bj, 2)};
+  double Scfi = Si - Szti, Scfj = Sj - Sztj;
+  double aux = 0.0, CGnorm = 1.0;
+  int sigma = 0;
+  double c0 = c.cg(Si, Si, 0.5, -0.5, Sj, Sj), c1 = c.cg(Si, Si, 0.5, 0.5, Sj, Sj);
+  if (!dEq(c0, 0.0)) { sigma = -1; CGnorm = c0; }
+  else if (!dEq(c1, 0.0)) { sigma = 1; CGnorm = c1; }
+  if (sigma == 0) return 0.0;
+  for (double Szcfj = Scfj; Szcfj >= -Scfj; Szcfj -= 1.0) {
+    double Szi = Si - Szcfj, Szj = Sj - Szcfj;
+    sqi[2] = Szi; int bsi = ss.block_of_qn(sqi);
+    sqj[2] = Szj; int bsj = ss.block_of_qn(sqj);
+    double a0 = c.cg(Scfi, Szcfj, ss.q(bi, 1), Szi, Si, Si);
+    double a1 = c.cg(Scfj, Szcfj, ss.q(bj, 1), Szj, Sj, Sj);
+    for (int si = ss.beg(bsi); si <= ss.end(bsi); si++)
+      for (int sj = ss.beg(bsj); sj <= ss.end(bsj); sj++)
+        aux += twoch_fd(ich, sigma, sj, si) * a0 * a1 * twoch_spsm(si, ti) * twoch_spsm(sj, tj);
+  }
+  return aux / CGnorm;
+}
+
+double op_rule(Ctx& c, int rule, const Basis& ab, int ist, int jst) {
+  switch (rule) {
+    case R_F_QS: return op_f_QS(c, ab, ist, jst);
+    case R_FUP_QSZ: return op_f_QSz(ab, ist, jst, 1);
+    case R_FDN_QSZ: return op_f_QSz(ab, ist, jst, -1);
+    case R_F1_2CH: return op_f_2ch(c, ab, ist, jst, 1);
+    case R_F2_2CH: return op_f_2ch(c, ab, ist, jst, 2);
+    case R_IMPONLY: return ab.itype[ist] == ab.itype[jst] ? 1.0 : 0.0;  // ImpOnly_MatEl OpMatRules.cpp:265
+  }
+  return 0.0;
+}
+
+// ---------------------------------------------------------------- BuildBasis
+// BuildBasis (BuildBasis.cpp:8-432) for the Q,S / Q,Sz cases (no parity,
+// no symmetry reduction, BefCut=0).
+void build_basis(const Model& m, const Basis& cut, Basis& ab) {
+  const Basis& ss = m.site;
+  int NC = m.common[0];
+  std::vector<int> posold(NC), possite(NC), totS(NC, 0), match(NC);
+  int its = 0;
+  for (int i = 0; i < NC; ++i) {
+    posold[i] = m.common[i + 1];
+    possite[i] = m.common[i + 1 + NC];
+    if (its < (int)m.totS.size() && posold[i] == m.totS[its]) { totS[i] = 1; its++; }
+    match[i] = (possite[i] >= 0 && possite[i] < ss.nqn) ? 1 : 0;
+  }
+  ab = Basis();
+  ab.nshell = cut.nshell + 1;
+  ab.nqn = NC;
+  ab.totalS = !m.totS.empty();
+  ab.sqn = m.totS;
+  std::vector<double> qo(NC), qs(NC), qnew(NC);
+  std::vector<double> cand;
+  for (int b = 0; b < cut.nblocks(); ++b) {
+    for (int i = 0; i < NC; ++i) qo[i] = cut.q(b, posold[i]);
+    for (int s = 0; s < ss.nblocks(); ++s) {
+      for (int i = 0; i < NC; ++i) {
+        qs[i] = match[i] ? ss.q(s, possite[i]) : 0.0;
+        qnew[i] = qs[i] + qo[i];
+        cand.push_back(qnew[i]);
+      }
+      if (!m.totS.empty()) {
+        for (int i = 0; i < NC; ++i) {
+          if (totS[i] == 1) {
+            double Snew = qo[i] + qs[i] - 1.0;
+            while (Snew >= std::fabs(qo[i] - qs[i])) {
+              qnew[i] = Snew;
+              for (int k = 0; k < NC; ++k) cand.push_back(qnew[k]);
+              Snew -= 1.0;
+            }
+          }
+        }
+      }
+    }
+  }
+  // FilterQNumbers (NRGarrayClass.cpp:271-309): stable removal of exact duplicates.
+  std::vector<double>& Q = ab.qn;
+  for (size_t k = 0; k < cand.size(); k += NC) {
+    bool dup = false;
+    for (size_t j = 0; j < Q.size() && !dup; j += NC) {
+      bool eq = true;
+      for (int i = 0; i < NC && eq; ++i) eq = (Q[j + i] == cand[k + i]);
+      dup = eq;
+    }
+    if (!dup) Q.insert(Q.end(), cand.begin() + k, cand.begin() + k + NC);
+  }
+  int ist = 0;
+  for (int b = 0; b < ab.nblocks(); ++b) {
+    for (int i = 0; i < NC; ++i) qnew[i] = ab.q(b, i);
+    ab.bbe.push_back(ist);
+    for (int bo = 0; bo < cut.nblocks(); ++bo) {
+      for (int i = 0; i < NC; ++i) qo[i] = cut.q(bo, posold[i]);
+      for (int s = 0; s < ss.nblocks(); ++s) {
+        bool ok = true;
+        for (int i = 0; i < NC; ++i) {
+          qs[i] = match[i] ? ss.q(s, possite[i]) : 0.0;
+          if (totS[i] == 0) {
+            if (!dEq(qnew[i], qs[i] + qo[i])) ok = false;
+          } else {
+            double Sold = qo[i], Ssite = ss.q(s, possite[i]), Szsite = ss.q(s, possite[i] + 1);
+            if (!dEq(qnew[i], Szsite + Sold) || !triang(Sold, Ssite, qnew[i])) ok = false;
+          }
+        }
+        if (!ok) continue;
+        for (int so = cut.bbe[2 * bo]; so <= cut.bbe[2 * bo + 1]; so++)
+          for (int st = ss.beg(s); st <= ss.end(s); st++) {
+            ab.itype.push_back(ss.itype[st]);
+            ab.en.push_back(cut.en[so]);
+            ab.stcf.push_back(so);
+            ist++;
+          }
+      }
+    }
+    ab.bbe.push_back(ist - 1);
+  }
+}
+
+// ---------------------------------------------------------------- DiagHN
+struct Sweep;
+double hn_el(Ctx& c, const std::vector<double>& P, const Basis& ab, const std::vector<Mat>& M,
+             int i, int j) {
+  switch (c.m.kind) {
+    case ORACLE_MODEL_1CHQS: return hn_1chQS(c, P, ab, M, i, j);
+    case ORACLE_MODEL_1CHQSZ: return hn_1chQSz(c, P, ab, M, i, j);
+    case ORACLE_MODEL_2CHQS: return hn_2chQS(c, P, ab, M, i, j);
+  }
+  return 0.0;
+}
+
+template <class F>
+void parallel_for(int n, int nthreads, F f) {
+  if (nthreads <= 1 || n <= 1) { for (int i = 0; i < n; ++i) f(i); return; }
+  std::atomic<int> next(0);
+  std::vector<std::thread> th;
+  for (int t = 0; t < std::min(n, nthreads); ++t)
+    th.emplace_back([&]() { for (int i; (i = next.fetch_add(1)) < n;) f(i); });
+  for (auto& t : th) t.join();
+}
+
+// CNRGmatrix::DiagHN (DiagHN.cpp:6-119) with DiagBlock (NRGmatrixClass.cpp:566-696):
+// packed upper triangle, row-major (j >= i), handed to dspev('V','L'); row k
+// of the returned Z is eigenvector k.  Optionally keeps the packed blocks.
+void diag_hn(Ctx& c, const std::vector<double>& P, const Basis& ab, const std::vector<Mat>& M,
+             Arr& eig, int nthreads, std::vector<std::vector<double>>* keepH, double* emin_out) {
+  int nb = ab.nblocks();
+  std::vector<std::vector<double>> ev(nb), vec(nb), packed(nb);
+  // The CG cache is not thread safe: warm it serially on the first row of
+  // every block pair type by evaluating the blocks' first element rows.
+  auto work = [&](int b, Ctx& cc) {
+    int n = ab.bsize(b), b0 = ab.beg(b);
+    std::vector<double> A;
+    A.reserve((size_t)n * (n + 1) / 2);
+    for (int i = 0; i < n; ++i)
+      for (int j = i; j < n; ++j) A.push_back(hn_el(cc, P, ab, M, b0 + i, b0 + j));
+    if (keepH) packed[b] = A;
+    std::vector<double> w(n), Z((size_t)n * n), work3(3 * (size_t)n);
+    int info = 0, ldz = n;
+    const char jobz = 'V', uplo = 'L';
+    g_dspev(&jobz, &uplo, &n, A.data(), w.data(), Z.data(), &ldz, work3.data(), &info, 1, 1);
+    ev[b] = w;
+    vec[b] = Z;
+  };
+  if (nthreads <= 1) {
+    for (int b = 0; b < nb; ++b) work(b, c);
+  } else {
+    std::vector<Ctx> ctxs(nthreads, c);
+    std::atomic<int> next(0);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthreads; ++t)
+      th.emplace_back([&, t]() { for (int b; (b = next.fetch_add(1)) < nb;) work(b, ctxs[t]); });
+    for (auto& t : th) t.join();
+  }
+  eig = Arr();
+  eig.nshell = ab.nshell; eig.nqn = ab.nqn; eig.qn = ab.qn; eig.bbe = ab.bbe;
+  eig.totalS = ab.totalS; eig.sqn = ab.sqn;
+  for (int b = 0; b < nb; ++b) {
+    eig.en.insert(eig.en.end(), ev[b].begin(), ev[b].end());
+    eig.evec.insert(eig.evec.end(), vec[b].begin(), vec[b].end());
+  }
+  if (keepH) *keepH = packed;
+  // SetE0zero (NRGarrayClass.cpp:234-241).
+  double emin = *std::min_element(eig.en.begin(), eig.en.end());
+  for (double& e : eig.en) e -= emin;
+  if (emin_out) *emin_out = emin;
+}
+
+// SetDegen (NRGarrayClass.cpp:244-268): pairwise merge of levels closer than
+// MyEPS (1e-18), in the reference's order.  Only values with a neighbour
+// within MyEPS can change, so the O(n^2) loop runs on those alone.
+void set_degen(std::vector<double>& en, double eps) {
+  int n = (int)en.size();
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  std::sort(idx.begin(), idx.end(), [&](int a, int b) { return en[a] < en[b]; });
+  std::vector<char> cand(n, 0);
+  for (int k = 0; k + 1 < n; ++k)
+    if (std::fabs(en[idx[k + 1]] - en[idx[k]]) < eps) { cand[idx[k]] = 1; cand[idx[k + 1]] = 1; }
+  std::vector<int> list;
+  for (int i = 0; i < n; ++i) if (cand[i]) list.push_back(i);
+  for (size_t a = 0; a < list.size(); ++a)
+    for (size_t b = a + 1; b < list.size(); ++b) {
+      int ii = list[a], jj = list[b];
+      if (std::fabs(en[jj] - en[ii]) < eps) {
+        if (en[jj] > en[ii]) en[jj] = en[ii]; else en[ii] = en[jj];
+      }
+    }
+}
+
+// CNRGarray::Ecut (NRGarrayClass.cpp:661-691).  The window walk stops at the
+// end of the spectrum (the reference would read past it).
+double ecut(const std::vector<double>& en, int Ncut) {
+  std::vector<double> E = en;
+  std::sort(E.begin(), E.end());
+  size_t sz = E.size();
+  if ((size_t)Ncut >= sz - 1) return E.back();
+  double aux = E[Ncut - 1], aux2 = E[Ncut];
+  size_t ii = 1;
+  while ((aux2 > 0.0) && (std::fabs((aux2 - aux) / aux) < 0.01) && (ii < sz) && (Ncut + ii < sz)) {
+    aux2 = E[Ncut + ii];
+    ii++;
+  }
+  if (ii > 1) aux = E[Ncut + ii - 2];
+  return aux;
+}
+
+// SetKept (NRGarrayClass.cpp:461-491).
+double set_kept(Arr& a, int Ncut, double eps, int* nkept) {
+  set_degen(a.en, eps);
+  double ec = ecut(a.en, Ncut);
+  a.kept.assign(a.en.size(), 0);
+  int nk = 0;
+  for (size_t i = 0; i < a.en.size(); ++i) if (a.en[i] <= ec) { a.kept[i] = 1; nk++; }
+  if (nkept) *nkept = nk;
+  return ec;
+}
+
+// CutStates (CutStates.cpp:10-95) with RemoveBlock (NRGarrayClass.cpp:1307)
+// and RemoveStatesFromBlock (:1467): whole blocks with E_min > E_cut go, then
+// each block loses everything from its first level above E_cut.
+void cut_states(const Arr& ain, Basis& acut, int Ncut, double eps) {
+  Basis out;
+  out.nshell = ain.nshell; out.nqn = ain.nqn; out.totalS = ain.totalS; out.sqn = ain.sqn;
+  std::vector<int> eoff(ain.nblocks() + 1, 0);
+  for (int b = 0; b < ain.nblocks(); ++b) eoff[b + 1] = eoff[b] + ain.bsize(b) * ain.bsize(b);
+  if (Ncut >= ain.nstates()) {
+    out.qn = ain.qn; out.bbe = ain.bbe; out.en = ain.en; out.evec = ain.evec; out.kept = ain.kept;
+    for (int i = 0; i < ain.nstates(); ++i) out.stcf.push_back(i);
+    out.bbe_bc = ain.bbe;
+    for (int b = 0; b < ain.nblocks(); ++b) { out.bbe_eig.push_back(eoff[b]); out.bbe_eig.push_back(eoff[b + 1] - 1); }
+    acut = out;
+    return;
+  }
+  double ec = ecut(ain.en, Ncut);
+  std::vector<double> en = ain.en;  // Acut.SetKept on its own copy
+  set_degen(en, eps);
+  double ec2 = ecut(en, Ncut);
+  std::vector<char> kept(en.size());
+  for (size_t i = 0; i < en.size(); ++i) kept[i] = en[i] <= ec2;
+  int ist = 0, eig = 0;
+  for (int b = 0; b < ain.nblocks(); ++b) {
+    int b0 = ain.beg(b), b1 = ain.end(b), n = ain.bsize(b);
+    double emin = *std::min_element(en.begin() + b0, en.begin() + b1 + 1);
+    if (emin > ec) continue;
+    int p = b0;
+    while (p <= b1 && en[p] <= ec) p++;   // GetBlockEcutPos (NRGarrayClass.cpp:439-457)
+    int k = p - b0;
+    for (int q = 0; q < ain.nqn; ++q) out.qn.push_back(ain.q(b, q));
+    out.bbe.push_back(ist); out.bbe.push_back(ist + k - 1);
+    out.bbe_bc.push_back(b0); out.bbe_bc.push_back(b1);
+    for (int i = 0; i < k; ++i) {
+      out.en.push_back(en[b0 + i]);
+      out.kept.push_back(kept[b0 + i]);
+      out.stcf.push_back(b0 + i);
+    }
+    out.evec.insert(out.evec.end(), ain.evec.begin() + eoff[b], ain.evec.begin() + eoff[b] + (size_t)k * n);
+    out.bbe_eig.push_back(eig); out.bbe_eig.push_back(eig + k * n - 1);
+    eig += k * n;
+    ist += k;
+  }
+  acut = out;
+}
+
+// ---------------------------------------------------------------- UpdateMatrices
+// UpdateMatrices (UpdateMatrices.cpp:272-568): for every kept block pair
+// allowed by CheckForMatEl and every operator, build fnbasis element by
+// element (times the old operator through StCameFrom when NeedOld) and form
+// Z_i . fnbasis . Z_j^T with two dgemm calls.
+void update_matrices(Ctx& c, const Basis& acut, const Basis& ab, std::vector<Mat>& mats, int nthreads) {
+  std::vector<Mat> old = mats;
+  // FindMatchBlock (FindMatchBlock.cpp:5-24).
+  std::vector<int> bc(acut.nblocks());
+  for (int b = 0; b < acut.nblocks(); ++b) bc[b] = ab.block_of_qn(&acut.qn[(size_t)b * acut.nqn]);
+  for (size_t im = 0; im < mats.size(); ++im) {
+    Mat& M = mats[im];
+    M.clear_data();
+    M.blk = acut;
+    M.blk.evec.clear();
+    struct Job { int i, j; };
+    std::vector<Job> jobs;
+    for (int i = 0; i < acut.nblocks(); ++i)
+      for (int j = 0; j < acut.nblocks(); ++j)
+        if (check(c.m.op_check[im], acut, i, j)) jobs.push_back({i, j});
+    std::vector<std::vector<double>> res(jobs.size());
+    auto work = [&](int k, Ctx& cc) {
+      int i = jobs[k].i, j = jobs[k].j;
+      int ni = acut.bsize(i), nj = acut.bsize(j);
+      int ib = bc[i], jb = bc[j];
+      int niBC = ab.bsize(ib), njBC = ab.bsize(jb);
+      std::vector<double> F((size_t)niBC * njBC);
+      size_t r = 0;
+      for (int ist = ab.beg(ib); ist <= ab.end(ib); ist++)
+        for (int jst = ab.beg(jb); jst <= ab.end(jb); jst++) {
+          double v = op_rule(cc, c.m.op_rule[im], ab, ist, jst);
+          if (M.need_old) v = v * old[im].get(ab.stcf[ist], ab.stcf[jst]);
+          F[r++] = v;
+        }
+      const double* Zi = &acut.evec[acut.bbe_eig[2 * i]];
+      const double* Zj = &acut.evec[acut.bbe_eig[2 * j]];
+      std::vector<double> T((size_t)niBC * nj), O((size_t)ni * nj);
+      g_dgemm(kRowMajor, kNoTrans, kTrans, niBC, nj, njBC, 1.0, F.data(), njBC, Zj, njBC, 0.0, T.data(), nj);
+      g_dgemm(kRowMajor, kNoTrans, kNoTrans, ni, nj, niBC, 1.0, Zi, niBC, T.data(), nj, 0.0, O.data(), nj);
+      res[k] = O;
+    };
+    if (nthreads <= 1) {
+      for (size_t k = 0; k < jobs.size(); ++k) work((int)k, c);
+    } else {
+      std::vector<Ctx> ctxs(nthreads, c);
+      std::atomic<int> next(0);
+      std::vector<std::thread> th;
+      for (int t = 0; t < nthreads; ++t)
+        th.emplace_back([&, t]() { for (int k; (k = next.fetch_add(1)) < (int)jobs.size();) work(k, ctxs[t]); });
+      for (auto& t : th) t.join();
+    }
+    for (size_t k = 0; k < jobs.size(); ++k)
+      M.push_block(jobs[k].i, jobs[k].j, res[k].data(), (int)res[k].size());
+  }
+}
+
+// ---------------------------------------------------------------- observables
+// CalcSuscep (CalcThermo.cpp:16-74): returns <Sz^2>/Z (the <Sz>^2 term is
+// multiplied by 0 in the reference).
+double calc_suscep(const Arr& a, double beta, int sq, bool totalS) {
+  double s0 = 0, s1 = 0, s2 = 0;
+  for (int b = 0; b < a.nblocks(); ++b) {
+    double Si = a.q(b, sq);
+    for (int i = a.beg(b); i <= a.end(b); i++) {
+      double auxS, SzSq, Sz;
+      if (totalS) { auxS = 2.0 * Si + 1.0; SzSq = (1.0 / 12.0) * auxS * (auxS * auxS - 1.0); Sz = 0.0; }
+      else { auxS = 1.0; SzSq = Si * Si; Sz = Si; }
+      double e = std::exp(-beta * a.en[i]);
+      s0 += auxS * e; s1 += SzSq * e; s2 += Sz * e;
+    }
+  }
+  return (s1 - 0.0 * s1 * s2) / s0;
+}
+// CalcEntropy (CalcThermo.cpp:80-121).
+double calc_entropy(const Arr& a, double beta, int sq, bool totalS) {
+  double Z = 0, s = 0;
+  for (int b = 0; b < a.nblocks(); ++b) {
+    double deg = totalS ? 2.0 * a.q(b, sq) + 1.0 : 1.0;
+    for (int i = a.beg(b); i <= a.end(b); i++) {
+      double E = a.en[i], e = std::exp(-beta * E);
+      s += deg * E * e; Z += deg * e;
+    }
+  }
+  return beta * (s / Z) + std::log(Z);
+}
+// CalcOpAvg (CalcOpAvg.cpp:13-84): Boltzmann average of a diagonal operator
+// over the kept states.
+double calc_opavg(const Arr& a, const Mat& M, double beta, bool totalS, int sq) {
+  double s = 0, Z = 0;
+  for (int b = 0; b < a.nblocks(); ++b) {
+    double deg = totalS ? 2.0 * a.q(b, sq) + 1.0 : 1.0;
+    for (int i = a.beg(b); i <= a.end(b); i++) {
+      double e = std::exp(-beta * a.en[i]);
+      s += deg * M.get(i, i) * e; Z += deg * e;
+    }
+  }
+  if (!(std::fabs(Z - 0.0) < 1.e-20)) s = s / Z;
+  return s;
+}
+
+// ---------------------------------------------------------------- model set-up
+// Operator matrix on one-state-per-block arrays.
+Mat diag_op(const Arr& a, const std::vector<double>& vals, const char* name) {
+  Mat M; M.blk = a; M.blk.evec.clear(); M.need_old = true; M.calc_avg = true; M.name = name;
+  M.rule = R_IMPONLY;
+  for (int b = 0; b < a.nblocks(); ++b) { double v = vals[b]; M.push_block(b, b, &v, 1); }
+  return M;
+}
+
+// OneChQS_SetAnderson_Hm1 (Main/Main_SetH0.cpp:1794-1969): three impurity
+// multiplets, reduced <||d||> = (1, -sqrt 2), n_d, n_d^2 and S^2.
+void hm1_QS(double Lambda, double HLF, double U, double ed, Arr& a, Mat& f, std::vector<Mat>& avg) {
+  a = Arr(); a.nqn = 2; a.nshell = -1; a.totalS = true; a.sqn = {1};
+  a.qn = {-1, 0, 0, 0.5, 1, 0};
+  a.bbe = {0, 0, 1, 1, 2, 2};
+  a.en = {0.5 * U / (Lambda * HLF), (ed + 0.5 * U) / (Lambda * HLF), (2.0 * ed + 1.5 * U) / (Lambda * HLF)};
+  a.evec = {1, 1, 1};
+  f = Mat(); f.blk = a; f.blk.evec.clear();
+  double one = 1.0, m2 = -std::sqrt(2.0);
+  f.push_block(0, 1, &one, 1); f.push_block(1, 2, &m2, 1);
+  std::vector<double> nd, nd2, s2;
+  for (int b = 0; b < 3; ++b) {
+    double n = a.q(b, 0) + 1.0, S = a.q(b, 1);
+    nd.push_back(n); nd2.push_back(n * n); s2.push_back(S * (S + 1.0));
+  }
+  avg = {diag_op(a, nd, "Ndot"), diag_op(a, nd2, "NdSq"), diag_op(a, s2, "SdSq")};
+}
+
+// OneChQSz_SetAnderson_Hm1 (Main/Main_SetH0.cpp:421-660): four impurity
+// states, f_up, f_dn, n_d and S_z.
+void hm1_QSz(double Lambda, double HLF, double U, double ed, double B, Arr& a, Mat& fu, Mat& fd,
+             std::vector<Mat>& avg) {
+  double hz = 0.5 * B;
+  a = Arr(); a.nqn = 2; a.nshell = -1; a.totalS = false;
+  a.qn = {-1, 0, 0, 0.5, 0, -0.5, 1, 0};
+  a.bbe = {0, 0, 1, 1, 2, 2, 3, 3};
+  a.en = {0.5 * U / (Lambda * HLF), (ed + 0.5 * U - hz) / (Lambda * HLF), (ed + 0.5 * U + hz) / (Lambda * HLF),
+          (2.0 * ed + 1.5 * U) / (Lambda * HLF)};
+  a.evec = {1, 1, 1, 1};
+  double one = 1.0, mone = -1.0;
+  fu = Mat(); fu.blk = a; fu.blk.evec.clear();
+  fu.push_block(0, 1, &one, 1); fu.push_block(2, 3, &one, 1);
+  fd = Mat(); fd.blk = a; fd.blk.evec.clear();
+  fd.push_block(0, 2, &one, 1); fd.push_block(1, 3, &mone, 1);
+  std::vector<double> nd, sz;
+  for (int b = 0; b < 4; ++b) { nd.push_back(a.q(b, 0) + 1.0); sz.push_back(a.q(b, 1)); }
+  avg = {diag_op(a, nd, "Ndot"), diag_op(a, sz, "Szdot")};
+}
+
+}  // namespace
+
+// ================================================================ C ABI
+struct OracleIter {
+  std::vector<double> params;     // ParamsHN used for this iteration
+  std::vector<double> qn;         // block QNs
+  std::vector<int> bsize;         // block sizes
+  std::vector<double> en;         // energies after SetE0zero + SetDegen
+  double emin = 0, ecut = 0;
+  int nkept = 0;
+  std::vector<double> thermo;     // 4 x (beta, T, suscep, entropy)
+  std::vector<double> opavg;      // CalcAvg operators over AeigCut
+  std::vector<int> kept_bsize;    // AeigCut block sizes
+  // Optional capture of the DiagHN inputs/outputs for drop-in tests.
+  std::vector<double> basis_qn, basis_en;
+  std::vector<int> basis_bbe, basis_itype, basis_stcf;
+  std::vector<double> H;          // packed upper triangles, block-concatenated
+};
+
+struct OracleRun {
+  int nqn = 2;
+  std::vector<double> opavg_m1;
+  std::vector<std::string> opnames;
+  std::vector<OracleIter> it;
+  double seconds = 0;
+};
+
+extern "C" {
+
+int oracle_load_lapack(const char* path) {
+  void* h = dlopen(path, RTLD_NOW | RTLD_LOCAL);
+  if (!h) { g_err = dlerror(); return -1; }
+  g_dspev = (dspev_t)dlsym(h, "scipy_dspev_");
+  if (!g_dspev) g_dspev = (dspev_t)dlsym(h, "dspev_");
+  g_dgemm = (dgemm_t)dlsym(h, "scipy_cblas_dgemm");
+  if (!g_dgemm) g_dgemm = (dgemm_t)dlsym(h, "cblas_dgemm");
+  g_setthreads = (setthreads_t)dlsym(h, "scipy_openblas_set_num_threads");
+  if (!g_setthreads) g_setthreads = (setthreads_t)dlsym(h, "openblas_set_num_threads");
+  if (!g_dspev || !g_dgemm) { g_err = "dspev/dgemm symbols not found"; return -2; }
+  return 0;
+}
+
+const char* oracle_last_error(void) { return g_err.c_str(); }
+
+void oracle_blas_threads(int n) { if (g_setthreads) g_setthreads(n); }
+
+double oracle_cgordan(double j1, double m1, double j2, double m2, double j, double m) {
+  return cgordan(j1, m1, j2, m2, j, m);
+}
+
+void* oracle_run(const oracle_config* cfg) {
+  if (!g_dspev) { g_err = "LAPACK not loaded"; return nullptr; }
+  auto t0 = std::chrono::steady_clock::now();
+  OracleRun* R = new OracleRun();
+  Ctx c;
+  const double pi = 3.141592653589793238462643383279502884197169;
+  double Lambda = cfg->lambda;
+  double HLF = 0.5 * (1.0 + 1.0 / Lambda);
+  double ALambda = std::sqrt(0.5 * std::log(Lambda) * (Lambda + 1) / (Lambda - 1));
+  double eps = cfg->degen_eps > 0 ? cfg->degen_eps : 1.0e-18;
+  int nthreads = cfg->nthreads > 0 ? cfg->nthreads : 1;
+  // SetChainWilson (NRGchainClass.cpp:132-155).
+  auto chin = [&](int N) {
+    double d0 = 1.0 - std::pow(Lambda, -((double)N + 1.0));
+    double d1 = std::sqrt(1.0 - std::pow(Lambda, -(2.0 * (double)N + 1.0)));
+    double d2 = std::sqrt(1.0 - std::pow(Lambda, -(2.0 * (double)N + 3.0)));
+    return d0 / (d1 * d2);
+  };
+  c.m.kind = cfg->model;
+  Arr eig;
+  std::vector<Mat> mats;
+  std::vector<double> P;
+  int sq = 1;
+  bool totalS = true;
+  int nchan = 1;
+  double chi1 = std::sqrt(2.0 * cfg->gamma1 / pi) / (std::sqrt(Lambda) * HLF) * ALambda;
+  if (cfg->model == ORACLE_MODEL_1CHQS) {
+    c.m.site = site_1chQS(); c.m.totS = {1};
+    Mat f; std::vector<Mat> avg;
+    hm1_QS(Lambda, HLF, cfg->U, cfg->ed, eig, f, avg);
+    mats.push_back(f); for (auto& x : avg) mats.push_back(x);
+    c.m.op_rule = {R_F_QS, R_IMPONLY, R_IMPONLY, R_IMPONLY};
+    c.m.op_check = {C_QS_CD, C_DIAG, C_DIAG, C_DIAG};
+    P = {Lambda, chi1, 0.0, 0.0};
+  } else if (cfg->model == ORACLE_MODEL_1CHQSZ) {
+    c.m.site = site_1chQSz(); c.m.totS = {};
+    Mat fu, fd; std::vector<Mat> avg;
+    hm1_QSz(Lambda, HLF, cfg->U, cfg->ed, cfg->gamma2_or_B, eig, fu, fd, avg);
+    mats.push_back(fu); mats.push_back(fd); for (auto& x : avg) mats.push_back(x);
+    c.m.op_rule = {R_FUP_QSZ, R_FDN_QSZ, R_IMPONLY, R_IMPONLY};
+    c.m.op_check = {C_Q_CD, C_Q_CD, C_DIAG, C_DIAG};
+    P = {Lambda, chi1, 0.0, 0.0};
+    totalS = false;
+  } else if (cfg->model == ORACLE_MODEL_2CHQS) {
+    c.m.site = site_2chQS(); c.m.totS = {1};
+    Mat f; std::vector<Mat> avg;
+    hm1_QS(Lambda, HLF, cfg->U, cfg->ed, eig, f, avg);
+    mats.push_back(f); mats.push_back(f); for (auto& x : avg) mats.push_back(x);
+    c.m.op_rule = {R_F1_2CH, R_F2_2CH, R_IMPONLY, R_IMPONLY, R_IMPONLY};
+    c.m.op_check = {C_2CH_CD, C_2CH_CD, C_DIAG, C_DIAG, C_DIAG};
+    double chi2 = std::sqrt(2.0 * cfg->gamma2_or_B / pi) / (std::sqrt(Lambda) * HLF) * ALambda;
+    P = {Lambda, chi1, chi2, 0.0, 0.0};
+    nchan = 2;
+  } else {
+    g_err = "unknown model"; delete R; return nullptr;
+  }
+  for (size_t i = 0; i < mats.size(); ++i) {
+    if (c.m.op_rule[i] == R_IMPONLY) { mats[i].need_old = true; mats[i].calc_avg = true; }
+    else { mats[i].need_old = false; mats[i].calc_avg = false; }
+  }
+  R->nqn = 2;
+  for (auto& m : mats) if (m.calc_avg) R->opnames.push_back(m.name);
+  const double betabar = 0.727;
+  Basis cut, ab;
+  cut_states(eig, cut, cfg->ncutoff, eps);
+  for (auto& m : mats) if (m.calc_avg) R->opavg_m1.push_back(calc_opavg(cut, m, betabar, totalS, sq));
+  for (int N = 0; N < cfg->nsites; ++N) {
+    OracleIter I;
+    I.params = P;
+    double DN = HLF * std::pow(Lambda, (-(N - 1) / 2.0));
+    build_basis(c.m, cut, ab);
+    bool cap = (cfg->capture_iter == N);
+    if (cap) {
+      I.basis_qn = ab.qn; I.basis_en = ab.en; I.basis_bbe = ab.bbe;
+      I.basis_itype = ab.itype; I.basis_stcf = ab.stcf;
+    }
+    std::vector<std::vector<double>> H;
+    diag_hn(c, P, ab, mats, eig, nthreads, cap ? &H : nullptr, &I.emin);
+    if (cap) for (auto& h : H) I.H.insert(I.H.end(), h.begin(), h.end());
+    I.ecut = set_kept(eig, cfg->ncutoff, eps, &I.nkept);
+    I.qn = eig.qn;
+    for (int b = 0; b < eig.nblocks(); ++b) I.bsize.push_back(eig.bsize(b));
+    I.en = eig.en;
+    for (int nc = 1; nc <= 4; ++nc) {
+      double bN = betabar * std::pow(Lambda, (nc - 4) / (2.0 * 4));
+      I.thermo.push_back(bN); I.thermo.push_back(DN / bN);
+      I.thermo.push_back(calc_suscep(eig, bN, sq, totalS));
+      I.thermo.push_back(calc_entropy(eig, bN, sq, totalS));
+    }
+    cut_states(eig, cut, cfg->ncutoff, eps);
+    update_matrices(c, cut, ab, mats, nthreads);
+    for (auto& m : mats) if (m.calc_avg) I.opavg.push_back(calc_opavg(cut, m, betabar, totalS, sq));
+    for (int b = 0; b < cut.nblocks(); ++b) I.kept_bsize.push_back(cut.bsize(b));
+    for (int ich = 0; ich < nchan; ++ich) P[ich + 1] = chin(N);
+    R->it.push_back(std::move(I));
+  }
+  R->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return R;
+}
+
+void oracle_free(void* h) { delete (OracleRun*)h; }
+
+int oracle_num_iters(void* h) { return (int)((OracleRun*)h)->it.size(); }
+double oracle_seconds(void* h) { return ((OracleRun*)h)->seconds; }
+int oracle_num_ops(void* h) { return (int)((OracleRun*)h)->opnames.size(); }
+const char* oracle_op_name(void* h, int k) { return ((OracleRun*)h)->opnames[k].c_str(); }
+const double* oracle_opavg_m1(void* h) { return ((OracleRun*)h)->opavg_m1.data(); }
+
+#define ITER(h, n) (((OracleRun*)h)->it[n])
+int oracle_iter_nblocks(void* h, int n) { return (int)ITER(h, n).bsize.size(); }
+const double* oracle_iter_qn(void* h, int n) { return ITER(h, n).qn.data(); }
+const int* oracle_iter_bsize(void* h, int n) { return ITER(h, n).bsize.data(); }
+int oracle_iter_nstates(void* h, int n) { return (int)ITER(h, n).en.size(); }
+const double* oracle_iter_en(void* h, int n) { return ITER(h, n).en.data(); }
+double oracle_iter_emin(void* h, int n) { return ITER(h, n).emin; }
+double oracle_iter_ecut(void* h, int n) { return ITER(h, n).ecut; }
+int oracle_iter_nkept(void* h, int n) { return ITER(h, n).nkept; }
+const double* oracle_iter_thermo(void* h, int n) { return ITER(h, n).thermo.data(); }
+const double* oracle_iter_opavg(void* h, int n) { return ITER(h, n).opavg.data(); }
+int oracle_iter_nparams(void* h, int n) { return (int)ITER(h, n).params.size(); }
+const double* oracle_iter_params(void* h, int n) { return ITER(h, n).params.data(); }
+int oracle_iter_nkeptblocks(void* h, int n) { return (int)ITER(h, n).kept_bsize.size(); }
+const int* oracle_iter_kept_bsize(void* h, int n) { return ITER(h, n).kept_bsize.data(); }
+int oracle_iter_H_size(void* h, int n) { return (int)ITER(h, n).H.size(); }
+const double* oracle_iter_H(void* h, int n) { return ITER(h, n).H.data(); }
+const int* oracle_iter_basis_itype(void* h, int n) { return ITER(h, n).basis_itype.data(); }
+const int* oracle_iter_basis_stcf(void* h, int n) { return ITER(h, n).basis_stcf.data(); }
+const double* oracle_iter_basis_en(void* h, int n) { return ITER(h, n).basis_en.data(); }
+
+}  // extern "C"

@@ -1,0 +1,33 @@
+/* C interface of the CPU oracle (test infrastructure only; see nrg_oracle.cpp). */
+#ifndef NRG_ORACLE_H
+#define NRG_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORACLE_MODEL_1CHQS 0  /* one-channel Anderson, (Q,S) basis  */
+#define ORACLE_MODEL_1CHQSZ 1 /* one-channel Anderson, (Q,Sz) basis */
+#define ORACLE_MODEL_2CHQS 2  /* two-channel Anderson, (Q,S) basis  */
+
+typedef struct {
+  int model;          /* ORACLE_MODEL_* */
+  int nsites;         /* Wilson iterations N = 0 .. nsites-1 */
+  int ncutoff;        /* kept multiplets (states in Q,Sz) */
+  double lambda, U, ed, gamma1;
+  double gamma2_or_B; /* Gamma2 for 2chQS, magnetic field B for 1chQSz */
+  double degen_eps;   /* SetDegen tolerance, <=0 -> 1e-18 */
+  int nthreads;       /* host threads over blocks / block pairs */
+  int capture_iter;   /* iteration whose DiagHN inputs/H are kept, -1 none */
+} oracle_config;
+
+int oracle_load_lapack(const char* path);
+const char* oracle_last_error(void);
+void oracle_blas_threads(int n);
+double oracle_cgordan(double j1, double m1, double j2, double m2, double j, double m);
+void* oracle_run(const oracle_config* cfg);
+void oracle_free(void* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,152 @@
+"""ctypes wrapper of the C++ oracle restatement (oracle/nrg_oracle.cpp).
+
+Test infrastructure only.  ``build()`` compiles the oracle in-tree with g++;
+``run()`` executes one NRG sweep and returns per-iteration numpy arrays.
+"""
+from __future__ import annotations
+
+import ctypes
+import glob
+import os
+import subprocess
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SO = os.path.join(HERE, "_build", "libnrg_oracle.so")
+
+MODEL_1CHQS, MODEL_1CHQSZ, MODEL_2CHQS = 0, 1, 2
+MODELS = {"1chQS": MODEL_1CHQS, "1chQSz": MODEL_1CHQSZ, "2chQS": MODEL_2CHQS}
+
+
+class _Cfg(ctypes.Structure):
+    _fields_ = [("model", ctypes.c_int), ("nsites", ctypes.c_int), ("ncutoff", ctypes.c_int),
+                ("lambda_", ctypes.c_double), ("U", ctypes.c_double), ("ed", ctypes.c_double),
+                ("gamma1", ctypes.c_double), ("gamma2_or_B", ctypes.c_double),
+                ("degen_eps", ctypes.c_double), ("nthreads", ctypes.c_int),
+                ("capture_iter", ctypes.c_int)]
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "nrg_oracle.cpp")
+    if force or not os.path.exists(SO) or os.path.getmtime(SO) < os.path.getmtime(src):
+        os.makedirs(os.path.dirname(SO), exist_ok=True)
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", src, "-o", SO,
+                               "-ldl", "-lpthread"])
+    return SO
+
+
+def openblas_path() -> str:
+    """OpenBLAS bundled with scipy (LP64, symbols prefixed ``scipy_``)."""
+    import scipy
+    root = os.path.dirname(os.path.dirname(scipy.__file__))
+    libs = sorted(glob.glob(os.path.join(root, "scipy.libs", "libscipy_openblas*.so")))
+    if not libs:
+        raise RuntimeError("scipy's bundled OpenBLAS not found")
+    return libs[0]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(SO)
+        L.oracle_run.restype = ctypes.c_void_p
+        L.oracle_run.argtypes = [ctypes.POINTER(_Cfg)]
+        L.oracle_last_error.restype = ctypes.c_char_p
+        L.oracle_cgordan.restype = ctypes.c_double
+        L.oracle_cgordan.argtypes = [ctypes.c_double] * 6
+        L.oracle_seconds.restype = ctypes.c_double
+        L.oracle_op_name.restype = ctypes.c_char_p
+        for name in ("oracle_iter_emin", "oracle_iter_ecut"):
+            getattr(L, name).restype = ctypes.c_double
+        for name in ("oracle_iter_qn", "oracle_iter_en", "oracle_iter_thermo", "oracle_iter_opavg",
+                     "oracle_iter_params", "oracle_iter_H", "oracle_iter_basis_en", "oracle_opavg_m1"):
+            getattr(L, name).restype = ctypes.POINTER(ctypes.c_double)
+        for name in ("oracle_iter_bsize", "oracle_iter_kept_bsize", "oracle_iter_basis_itype",
+                     "oracle_iter_basis_stcf"):
+            getattr(L, name).restype = ctypes.POINTER(ctypes.c_int)
+        for name in [n for n in dir(L) if False]:
+            pass
+        rc = L.oracle_load_lapack(openblas_path().encode())
+        if rc != 0:
+            raise RuntimeError("oracle: " + L.oracle_last_error().decode())
+        _lib = L
+    return _lib
+
+
+@dataclass
+class Iteration:
+    params: np.ndarray
+    qn: np.ndarray          # (nblocks, 2)
+    bsize: np.ndarray       # (nblocks,)
+    en: np.ndarray          # (nstates,)
+    emin: float
+    ecut: float
+    nkept: int
+    thermo: np.ndarray      # (4, 4): beta, T, suscep, entropy
+    opavg: np.ndarray
+    kept_bsize: np.ndarray
+    H: np.ndarray | None = None
+    basis_itype: np.ndarray | None = None
+    basis_stcf: np.ndarray | None = None
+    basis_en: np.ndarray | None = None
+
+
+@dataclass
+class Sweep:
+    iters: list = field(default_factory=list)
+    opnames: list = field(default_factory=list)
+    opavg_m1: np.ndarray | None = None
+    seconds: float = 0.0
+
+
+def _arr(ptr, n, dtype):
+    if n == 0:
+        return np.zeros(0, dtype=dtype)
+    return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+
+
+def run(model: str, nsites: int, ncutoff: int, lam: float, U: float, ed: float, gamma1: float,
+        gamma2_or_B: float = 0.0, nthreads: int = 1, capture_iter: int = -1,
+        degen_eps: float = 0.0, blas_threads: int = 1) -> Sweep:
+    L = lib()
+    L.oracle_blas_threads(int(blas_threads))
+    cfg = _Cfg(MODELS[model], nsites, ncutoff, lam, U, ed, gamma1, gamma2_or_B, degen_eps,
+               nthreads, capture_iter)
+    h = L.oracle_run(ctypes.byref(cfg))
+    if not h:
+        raise RuntimeError("oracle: " + L.oracle_last_error().decode())
+    h = ctypes.c_void_p(h)
+    try:
+        out = Sweep()
+        nops = L.oracle_num_ops(h)
+        out.opnames = [L.oracle_op_name(h, k).decode() for k in range(nops)]
+        out.opavg_m1 = _arr(L.oracle_opavg_m1(h), nops, np.float64)
+        out.seconds = L.oracle_seconds(h)
+        for n in range(L.oracle_num_iters(h)):
+            nb = L.oracle_iter_nblocks(h, n)
+            ns = L.oracle_iter_nstates(h, n)
+            it = Iteration(
+                params=_arr(L.oracle_iter_params(h, n), L.oracle_iter_nparams(h, n), np.float64),
+                qn=_arr(L.oracle_iter_qn(h, n), 2 * nb, np.float64).reshape(nb, 2),
+                bsize=_arr(L.oracle_iter_bsize(h, n), nb, np.int64),
+                en=_arr(L.oracle_iter_en(h, n), ns, np.float64),
+                emin=L.oracle_iter_emin(h, n), ecut=L.oracle_iter_ecut(h, n),
+                nkept=L.oracle_iter_nkept(h, n),
+                thermo=_arr(L.oracle_iter_thermo(h, n), 16, np.float64).reshape(4, 4),
+                opavg=_arr(L.oracle_iter_opavg(h, n), nops, np.float64),
+                kept_bsize=_arr(L.oracle_iter_kept_bsize(h, n), L.oracle_iter_nkeptblocks(h, n), np.int64))
+            if n == capture_iter:
+                it.H = _arr(L.oracle_iter_H(h, n), L.oracle_iter_H_size(h, n), np.float64)
+                it.basis_itype = _arr(L.oracle_iter_basis_itype(h, n), ns, np.int64)
+                it.basis_stcf = _arr(L.oracle_iter_basis_stcf(h, n), ns, np.int64)
+                it.basis_en = _arr(L.oracle_iter_basis_en(h, n), ns, np.float64)
+            out.iters.append(it)
+        return out
+    finally:
+        L.oracle_free(h)
