@@ -1,0 +1,209 @@
+/*
+ * twochnrg_gb300.h — C ABI of the GB300-native TwoChNRG iterative-
+ * diagonalization engine.
+ *
+ * The engine replaces the hot path of the TwoChNRG NRG_main loop
+ * (src/Main/NRG_main.cpp:282-427): block-Hamiltonian assembly and block
+ * diagonalization (CNRGmatrix::DiagHN, src/DiagHN.cpp:6-119 and
+ * src/NRGmatrixClass.cpp:566-696), truncation (CNRGarray::SetKept,
+ * src/NRGarrayClass.cpp:461-491, and CutStates, src/CutStates.cpp:10-95),
+ * operator rotation (UpdateMatrices, src/UpdateMatrices.cpp:272-568) and the
+ * per-iteration observables (CalcSuscep/CalcEntropy, src/CalcThermo.cpp:16-121;
+ * CalcOpAvg, src/CalcOpAvg.cpp:13-84).
+ *
+ * Data cross this boundary as plain host arrays laid out like the
+ * reference's containers (include/NRGclasses.hpp:47-759):
+ *   - blocks:      QNumbers[nblocks*nqn], BlockBegEnd[2*nblocks] (inclusive)
+ *   - states:      dEn[nstates], iType[nstates], StCameFrom[nstates]
+ *   - eigenvectors: dEigVec, per block a row-major (rows x cols) matrix whose
+ *                  row k is eigenvector k
+ *   - operators:   MatBlockMap[2*npairs], MatBlockBegEnd[2*npairs], MatEl
+ *                  (dense row-major block per pair, block-pair order as the
+ *                  reference produces it: ibl major, jbl minor).
+ * Every call returns an nrg_status.  Nothing calls exit(); no call falls back
+ * to the CPU: without a usable sm_103 device, nrg_create() fails with
+ * NRG_ERR_CUDA.  Output arrays are owned by the context and stay valid until
+ * the next call on the same context.  One context drives one CUDA stream;
+ * distinct contexts may be used from distinct host threads.
+ */
+#ifndef TWOCHNRG_GB300_H
+#define TWOCHNRG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  NRG_OK = 0,
+  NRG_ERR_ARG = 1,          /* bad argument / unsupported model            */
+  NRG_ERR_CUDA = 2,         /* CUDA runtime error or no usable device      */
+  NRG_ERR_NOMEM = 3,        /* device or host allocation failed            */
+  NRG_ERR_NOT_CONVERGED = 4,/* eigensolver iteration limit reached         */
+  NRG_ERR_SIZE = 5,         /* a block exceeds the compiled size limits    */
+  NRG_ERR_SYNC = 6,         /* block structures out of sync (ChkSync)      */
+  NRG_ERR_TIMEOUT = 7,      /* a bounded device-side wait gave up          */
+  NRG_ERR_STATE = 8         /* call order violated (e.g. no sweep loaded)  */
+} nrg_status;
+
+/* Model families (CNRGCodeHandler::ModelSwitch, src/CodeHandler_ModelSwitch.cpp). */
+typedef enum {
+  NRG_MODEL_1CH_QS = 0,  /* one-channel Anderson, |Q S> basis   (SymNo 0, ModelNo 0) */
+  NRG_MODEL_1CH_QSZ = 1, /* one-channel Anderson, |Q Sz> basis  (SymNo 2, ModelNo 0) */
+  NRG_MODEL_2CH_QS = 2   /* two-channel Anderson, |Q S> basis   (SymNo 1)            */
+} nrg_model;
+
+/* Arithmetic of the dense steps. */
+typedef enum {
+  NRG_PREC_FP64 = 0      /* plain FP64 everywhere */
+} nrg_precision;
+
+typedef struct nrg_ctx nrg_ctx;
+
+/* Sweep parameters: the input_nrg.dat quantities NRG_main reads
+ * (CNRGCodeHandler::ReadParams, src/NRGcodehandlerClass.cpp:104-149). */
+typedef struct {
+  int model;          /* nrg_model */
+  int nsites;         /* Wilson iterations N = 0 .. nsites-1 */
+  int ncutoff;        /* Ncutoff: kept multiplets (Q,S) or states (Q,Sz) */
+  double lambda;      /* Lambda */
+  double U, ed;       /* impurity interaction and level */
+  double gamma1;      /* hybridization Gamma (channel 1) */
+  double gamma2_or_B; /* Gamma2 for NRG_MODEL_2CH_QS, field B for NRG_MODEL_1CH_QSZ */
+  double degen_eps;   /* CNRGarray::MyEPS (-E flag); <= 0 selects 1e-18 */
+  int precision;      /* nrg_precision */
+} nrg_sweep_config;
+
+/* Per-iteration results of a sweep (what NRG_main prints / writes). */
+typedef struct {
+  int nblocks;             /* blocks of H_N */
+  const double* qnumbers;  /* [nblocks*2] (Q,S) or (Q,Sz) */
+  const int* block_size;   /* [nblocks] */
+  int nstates;
+  const double* en;        /* [nstates] rescaled energies after SetE0zero/SetDegen */
+  double emin;             /* ground energy subtracted by SetE0zero */
+  double ecut;             /* CNRGarray::Ecut(Ncutoff) */
+  int nkept;               /* states with E <= Ecut */
+  int nkept_blocks;
+  const int* kept_block_size; /* [nkept_blocks] block sizes of AeigCut */
+  const double* thermo;    /* [4*4]: (betabar_n, T_M, T chi (CalcSuscep), S (CalcEntropy)) */
+  int nops;
+  const double* opavg;     /* [nops] CalcOpAvg of the averaged operators at betabar */
+  const double* params;    /* [4] ParamsHN used: Lambda, chi_1, chi_2 (0 if 1ch), eN */
+} nrg_iteration;
+
+/* Phase timing of the last sweep (device time from CUDA events). */
+typedef struct {
+  double total_ms;        /* host wall time of nrg_sweep_run                   */
+  double assemble_ms;     /* H_N assembly kernels                               */
+  double tridiag_ms;      /* Householder tridiagonalization                     */
+  double tridiag_eig_ms;  /* bisection + inverse iteration on the tridiagonals  */
+  double backtransform_ms;/* eigenvector back-transformation                    */
+  double cut_ms;          /* SetE0zero/SetDegen/Ecut/CutStates + observables    */
+  double update_ms;       /* operator rotation (UpdateMatrices)                 */
+  double tridiag_flops;   /* algorithmic FP64 flops of the tridiagonalization   */
+  double update_flops;    /* algorithmic flops of the rotation GEMMs            */
+  double backtransform_flops;
+  int64_t kernel_launches;/* kernels launched by the sweep                      */
+  int64_t tridiag_launches;
+} nrg_timing;
+
+/* ---- context ---------------------------------------------------------- */
+nrg_status nrg_create(int device, nrg_ctx** out);
+void nrg_destroy(nrg_ctx* ctx);
+const char* nrg_last_error(const nrg_ctx* ctx);
+const char* nrg_status_string(nrg_status s);
+/* Number of kernels this library has launched on the context so far. */
+int64_t nrg_kernel_count(const nrg_ctx* ctx);
+
+/* ---- whole sweep (NRG_main main loop, src/Main/NRG_main.cpp:282-427) ----
+ * Runs the Wilson chain from the impurity H_{-1} through nsites iterations
+ * with all state (kept eigenvectors, operator blocks) resident in HBM. */
+nrg_status nrg_sweep_run(nrg_ctx* ctx, const nrg_sweep_config* cfg);
+int nrg_sweep_num_iterations(const nrg_ctx* ctx);
+nrg_status nrg_sweep_iteration(const nrg_ctx* ctx, int n, nrg_iteration* out);
+nrg_status nrg_sweep_opavg_initial(const nrg_ctx* ctx, int* nops, const double** vals);
+nrg_status nrg_sweep_timing(const nrg_ctx* ctx, nrg_timing* out);
+
+/* ---- drop-in replacements --------------------------------------------- */
+
+/* Basis array as produced by BuildBasis (CNRGbasisarray, NRGclasses.hpp:215). */
+typedef struct {
+  int nqn;                   /* QNumbers per block (2) */
+  int nblocks;
+  const double* qnumbers;    /* [nblocks*nqn] */
+  const int* block_beg_end;  /* [2*nblocks] */
+  const double* en;          /* [nstates] dEn: energies of the states they came from */
+  const int* itype;          /* [nstates] iType */
+  const int* st_came_from;   /* [nstates] StCameFrom (index into the old kept array) */
+} nrg_basis;
+
+/* Operator in the old kept basis (CNRGmatrix, NRGclasses.hpp:365). */
+typedef struct {
+  int npairs;
+  const int* mat_block_map;      /* [2*npairs] */
+  const int* mat_block_beg_end;  /* [2*npairs] */
+  const double* mat_el;
+  /* block structure of the old kept array the operator lives on */
+  int nblocks;
+  const int* block_beg_end;      /* [2*nblocks] */
+} nrg_operator;
+
+/* Eigen array as DiagHN leaves it in Aeig (CNRGarray). */
+typedef struct {
+  int nblocks;
+  const double* qnumbers;    /* [nblocks*2] */
+  const int* block_beg_end;  /* [2*nblocks] */
+  int nstates;
+  const double* en;          /* [nstates] ascending per block, E_min shifted out */
+  const double* eigvec;      /* [sum n_b^2] row k of block b = eigenvector k */
+  double emin;               /* subtracted ground energy */
+} nrg_eig;
+
+/* CNRGmatrix::DiagHN replacement (src/DiagHN.cpp:6-119): assemble every
+ * (Q,S)/(Q,Sz) block of H_N on the device from the basis, the single-site
+ * rules of `model` and the old operators f_N (ops[0..nchan*nsigma-1] in the
+ * order of the model's MatArray), diagonalize all blocks in one batched
+ * launch series and return ascending energies with SetE0zero applied and
+ * all eigenvectors.  params = ParamsHN: {Lambda, chi_1[, chi_2], eN}. */
+nrg_status nrg_diag_hn(nrg_ctx* ctx, int model, const double* params, int nparams,
+                       const nrg_basis* abasis, const nrg_operator* ops, int nops,
+                       nrg_eig* out);
+
+/* Truncated array as CutStates leaves it in AeigCut (CNRGbasisarray). */
+typedef struct {
+  int nblocks;
+  const double* qnumbers;       /* [nblocks*2] */
+  const int* block_beg_end;     /* [2*nblocks] kept states */
+  const int* block_beg_end_bc;  /* [2*nblocks] the same blocks before the cut */
+  int nstates;
+  const double* en;             /* [nstates] kept energies (after SetDegen) */
+  const int* st_came_from;      /* [nstates] index in the uncut array */
+  const double* eigvec;         /* per block (kept x n_bc) rows = eigenvectors */
+  double ecut;
+  int nkept;                    /* states with E <= Ecut in the uncut array */
+} nrg_cut;
+
+/* CNRGarray::SetKept + CutStates replacement (src/NRGarrayClass.cpp:461-491,
+ * src/CutStates.cpp:10-95): SetDegen, Ecut with the 1% window, Kept flags,
+ * block removal and per-block tail removal, computed on the device.
+ * `in` energies are SetDegen-merged in place semantics (returned in out). */
+nrg_status nrg_cut_states(nrg_ctx* ctx, const nrg_eig* in, int ncutoff, double degen_eps,
+                          nrg_cut* out);
+
+/* UpdateMatrices replacement (src/UpdateMatrices.cpp:272-568) for the
+ * operators of `model` (index op_index in the model's MatArray order):
+ * O_new(i,j) = Z_i . F(i,j) . Z_j^T for every kept block pair the model's
+ * CheckForMatEl admits.  `old_op` is needed by NeedOld operators (n_d ...)
+ * and ignored otherwise. */
+nrg_status nrg_update_matrix(nrg_ctx* ctx, int model, int op_index, const nrg_cut* acut,
+                             const nrg_basis* abasis, const nrg_operator* old_op,
+                             int* npairs, const int** mat_block_map,
+                             const int** mat_block_beg_end, const double** mat_el);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TWOCHNRG_GB300_H */

@@ -1,0 +1,773 @@
+// Host driver of the GB300 NRG engine and the C ABI (include/twochnrg_gb300.h).
+//
+// nrg_sweep_run follows the iteration order of NRG_main
+// (src/Main/NRG_main.cpp:282-427): BuildBasis -> DiagHN -> SetKept ->
+// CalcThermo -> CutStates -> UpdateMatrices -> CalcStuff -> next chi_N.
+// The host does the block bookkeeping (a few hundred blocks) and builds the
+// small tables the kernels read; everything per state and per matrix element
+// runs on the device, and the kept eigenvectors and operator blocks stay in
+// HBM from one iteration to the next.  Two host synchronisations per
+// iteration remain: after the cut (the kept counts shape the next launches)
+// and after the operator averages.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/twochnrg_gb300.h"
+#include "nrg_device.cuh"
+#include "nrg_model.h"
+
+namespace nrg {
+
+// ------------------------------------------------------------------ errors
+struct NrgError : std::runtime_error {
+  nrg_status st;
+  NrgError(nrg_status s, const std::string& m) : std::runtime_error(m), st(s) {}
+};
+
+#define CU(x)                                                                                   \
+  do {                                                                                          \
+    cudaError_t _e = (x);                                                                       \
+    if (_e != cudaSuccess)                                                                      \
+      throw NrgError(_e == cudaErrorMemoryAllocation ? NRG_ERR_NOMEM : NRG_ERR_CUDA,            \
+                     std::string(#x) + ": " + cudaGetErrorString(_e));                          \
+  } while (0)
+
+// ------------------------------------------------------------------ device buffers
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  ~DevBuf() { if (p) cudaFree(p); }
+  void ensure(size_t bytes) {
+    if (bytes <= cap) return;
+    if (p) { CU(cudaFree(p)); p = nullptr; cap = 0; }
+    size_t want = std::max(bytes, cap + cap / 2);
+    CU(cudaMalloc(&p, want));
+    cap = want;
+  }
+  template <class T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+// Packs host arrays into one staging buffer and one device buffer so a table
+// set costs a single host-to-device copy.
+struct Packer {
+  std::vector<char> host;
+  struct Item { size_t off; };
+  size_t add(const void* src, size_t bytes) {
+    size_t off = (host.size() + 255) & ~size_t(255);
+    host.resize(off + bytes);
+    if (bytes) std::memcpy(host.data() + off, src, bytes);
+    return off;
+  }
+  template <class T> size_t add(const std::vector<T>& v) { return add(v.data(), v.size() * sizeof(T)); }
+};
+
+struct IterResult {
+  std::vector<double> params, qn, en, thermo, opavg;
+  std::vector<int> bsize, kept_bsize;
+  double emin = 0, ecut = 0;
+  int nkept = 0;
+};
+
+}  // namespace nrg
+
+struct nrg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int64_t launches = 0;
+  int num_sms = 0;
+  // sweep results
+  std::vector<nrg::IterResult> iters;
+  std::vector<double> opavg_m1;
+  nrg_timing timing{};
+  // device buffers
+  nrg::DevBuf meta, vmeta, H, d, e, tau, ev, en, flag, scal, Y, scratch, Z, Zt, T, partial, red, gpart;
+  nrg::DevBuf ops_a[6], ops_b[6], opptr;
+  cudaEvent_t ev_a[8];
+  // drop-in outputs (host)
+  std::vector<double> out_qn, out_en, out_vec, out_el;
+  std::vector<int> out_bbe, out_bbe_bc, out_stcf, out_map, out_mbe;
+};
+
+namespace nrg {
+
+namespace {
+
+const double kPi = 3.141592653589793238462643383279502884197169;
+
+// Chain hoppings of CNRGchain::SetChainWilson (NRGchainClass.cpp:132-155).
+double chin(double lambda, int N) {
+  double d0 = 1.0 - std::pow(lambda, -((double)N + 1.0));
+  double d1 = std::sqrt(1.0 - std::pow(lambda, -(2.0 * (double)N + 1.0)));
+  double d2 = std::sqrt(1.0 - std::pow(lambda, -(2.0 * (double)N + 3.0)));
+  return d0 / (d1 * d2);
+}
+
+// chi_{-1} of NRG_main.cpp:194-207 with the sqrt(A_Lambda) factor.
+double chi_m1(double lambda, double gamma) {
+  double HLF = 0.5 * (1.0 + 1.0 / lambda);
+  double c = std::sqrt(2.0 * gamma / kPi) / (std::sqrt(lambda) * HLF);
+  return c * std::sqrt(0.5 * std::log(lambda) * (lambda + 1) / (lambda - 1));
+}
+
+struct Timer {
+  nrg_ctx* c;
+  std::vector<std::pair<double*, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  explicit Timer(nrg_ctx* ctx) : c(ctx) {}
+  ~Timer() { for (auto e : pool) cudaEventDestroy(e); }
+  cudaEvent_t get() {
+    if (used == pool.size()) { cudaEvent_t e; CU(cudaEventCreate(&e)); pool.push_back(e); }
+    return pool[used++];
+  }
+  cudaEvent_t start() { cudaEvent_t e = get(); CU(cudaEventRecord(e, c->stream)); return e; }
+  void stop(cudaEvent_t s, double* acc) {
+    cudaEvent_t e = get();
+    CU(cudaEventRecord(e, c->stream));
+    pending.push_back({acc, {s, e}});
+  }
+  void collect() {  // stream must be synchronised
+    for (auto& p : pending) {
+      float ms = 0.f;
+      CU(cudaEventElapsedTime(&ms, p.second.first, p.second.second));
+      *p.first += ms;
+    }
+    pending.clear();
+    used = 0;
+  }
+};
+
+void check_flag(nrg_ctx* c) {
+  int f = 0;
+  CU(cudaMemcpy(&f, c->flag.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (f & DEV_SIZE) throw NrgError(NRG_ERR_SIZE, "a block exceeds the eigensolver size limit");
+  if (f & DEV_DEGEN_OVERFLOW) throw NrgError(NRG_ERR_SIZE, "too many near-degenerate levels for SetDegen");
+  if (f & DEV_BAD_INPUT) throw NrgError(NRG_ERR_ARG, "non-finite value met in an eigenvalue solve");
+  if (f & DEV_NOT_CONVERGED) throw NrgError(NRG_ERR_NOT_CONVERGED, "inverse iteration did not converge");
+}
+
+// ------------------------------------------------------------------ eigensolve
+// Tridiagonalize all blocks, eigenvalues of all, eigenvectors of the first
+// nvec[b] of each block (Z: nvec x n row-major, Zt: n x nvec), all on device.
+struct EigPlan {
+  std::vector<int> bsize, soff, nvec;
+  std::vector<int64_t> hoff, yoff;
+  int nstates = 0, maxn = 0;
+  int64_t hsize = 0, ysize = 0;
+};
+
+void plan_blocks(EigPlan& P, const std::vector<int>& bsize) {
+  P.bsize = bsize;
+  P.soff.assign(bsize.size(), 0);
+  P.hoff.assign(bsize.size(), 0);
+  int s = 0;
+  int64_t h = 0;
+  P.maxn = 0;
+  for (size_t b = 0; b < bsize.size(); ++b) {
+    P.soff[b] = s; P.hoff[b] = h;
+    s += bsize[b];
+    h += (int64_t)bsize[b] * bsize[b];
+    P.maxn = std::max(P.maxn, bsize[b]);
+  }
+  P.nstates = s;
+  P.hsize = h;
+}
+
+int choose_cluster(int maxn) { return maxn >= 256 ? 16 : 8; }
+
+// Blocks at least this large are tridiagonalized by the whole GPU (one
+// after the other); smaller ones by one thread-block cluster each.
+int big_block_threshold() {
+  const char* s = std::getenv("NRG_BIG_N");
+  return s ? std::atoi(s) : 1200;
+}
+
+// `order`: all blocks, largest first (host copy `order_h`); the big blocks
+// form its prefix.
+void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::vector<int>& order_h,
+                            const int* d_order, const int* d_bsize, const int64_t* d_hoff, const int* d_soff,
+                            const int* d_state_block) {
+  const int nb = (int)P.bsize.size();
+  const int thr = big_block_threshold();
+  int nbig = 0;
+  while (nbig < nb && P.bsize[order_h[nbig]] >= thr) ++nbig;
+  CU(cudaMemsetAsync(c->red.p, 0, sizeof(int), c->stream));
+  TridiagArgs ta{};
+  ta.nblocks = nb; ta.order = d_order; ta.bsize = d_bsize; ta.hoff = d_hoff; ta.soff = d_soff;
+  ta.H = c->H.as<double>(); ta.d = c->d.as<double>(); ta.e = c->e.as<double>(); ta.tau = c->tau.as<double>();
+  ta.queue = c->red.as<int>(); ta.flag = c->flag.as<int>(); ta.maxn = std::max(P.maxn, 2);
+  cudaEvent_t t0 = tm.start();
+  if (nbig > 0) {
+    const int G = tridiag_grid_size(ta.maxn);
+    if (G <= 0) throw NrgError(NRG_ERR_SIZE, "whole-GPU tridiagonalization does not fit");
+    c->gpart.ensure(sizeof(double) * ((size_t)G * ta.maxn + ta.maxn + G + 64));
+    double* part = c->gpart.as<double>();
+    double* pvec = part + (size_t)G * ta.maxn;
+    double* dots = pvec + ta.maxn;
+    CU(launch_tridiag_grid(ta, d_order, nbig, part, pvec, dots, G, c->stream));
+    c->launches++; c->timing.tridiag_launches++;
+  }
+  if (nbig < nb) {
+    int maxs = P.bsize[order_h[nbig]];
+    TridiagArgs ts = ta;
+    ts.order = d_order + nbig;
+    ts.nblocks = nb - nbig;
+    ts.maxn = std::max(maxs, 2);
+    int cluster = choose_cluster(maxs);
+    int ncl = tridiag_max_clusters(cluster, ts.maxn);
+    if (ncl <= 0) { cluster = 8; ncl = tridiag_max_clusters(cluster, ts.maxn); }
+    if (ncl <= 0) throw NrgError(NRG_ERR_SIZE, "tridiagonalization does not fit on the device");
+    ncl = std::min(ncl, nb - nbig);
+    CU(launch_tridiag(ts, cluster, ncl, c->stream));
+    c->launches++; c->timing.tridiag_launches++;
+  }
+  tm.stop(t0, &c->timing.tridiag_ms);
+  double fl = 0.0;
+  for (int n : P.bsize) fl += 4.0 / 3.0 * (double)n * n * n;
+  c->timing.tridiag_flops += fl;
+  TdEigArgs ea{};
+  ea.nblocks = nb; ea.bsize = d_bsize; ea.soff = d_soff; ea.d = c->d.as<double>(); ea.e = c->e.as<double>();
+  ea.ev = c->ev.as<double>(); ea.nstates = P.nstates; ea.flag = c->flag.as<int>();
+  cudaEvent_t t1 = tm.start();
+  launch_bisect(ea, d_state_block, c->stream);
+  c->launches++;
+  tm.stop(t1, &c->timing.tridiag_eig_ms);
+}
+
+// Eigenvectors for the lowest nvec[b] levels of every block (host has the
+// eigenvalues `ev` to form clusters).
+void run_vectors(nrg_ctx* c, Timer& tm, EigPlan& P, const std::vector<double>& ev_host, const int* d_bsize,
+                 const int64_t* d_hoff, const int* d_soff) {
+  const int nb = (int)P.bsize.size();
+  P.yoff.assign(nb, 0);
+  int64_t y = 0;
+  for (int b = 0; b < nb; ++b) { P.yoff[b] = y; y += (int64_t)P.bsize[b] * P.nvec[b]; }
+  P.ysize = y;
+  if (y == 0) return;
+  std::vector<int> vb, vi, cb, cf, cn, ctab, ctaf;
+  const int bw = backtransform_warps(std::max(P.maxn, 1));
+  for (int b = 0; b < nb; ++b) {
+    const int n = P.bsize[b], k = P.nvec[b];
+    if (k == 0) continue;
+    double onenrm = 0.0;
+    for (int i = 0; i < n; ++i) onenrm = std::max(onenrm, std::fabs(ev_host[P.soff[b] + i]));
+    const double ortol = 1e-4 * std::max(onenrm, 1e-300);
+    int start = 0;
+    for (int x = 0; x < k; ++x) {
+      vb.push_back(b); vi.push_back(x);
+      if (x > 0 && ev_host[P.soff[b] + x] - ev_host[P.soff[b] + x - 1] > ortol) {
+        cb.push_back(b); cf.push_back(start); cn.push_back(x - start); start = x;
+      }
+    }
+    cb.push_back(b); cf.push_back(start); cn.push_back(k - start);
+    for (int x = 0; x < k; x += bw) { ctab.push_back(b); ctaf.push_back(x); }
+  }
+  Packer pk;
+  size_t o_nvec = pk.add(P.nvec), o_yoff = pk.add(P.yoff), o_vb = pk.add(vb), o_vi = pk.add(vi), o_cb = pk.add(cb),
+         o_cf = pk.add(cf), o_cn = pk.add(cn), o_tb = pk.add(ctab), o_tf = pk.add(ctaf);
+  DevBuf& mb = c->vmeta;
+  mb.ensure(pk.host.size() + 256);
+  CU(cudaMemcpyAsync(mb.p, pk.host.data(), pk.host.size(), cudaMemcpyHostToDevice, c->stream));
+  char* base = mb.as<char>();
+  c->Y.ensure(sizeof(double) * y);
+  c->scratch.ensure(sizeof(double) * 5 * y);
+  c->Z.ensure(sizeof(double) * y);
+  c->Zt.ensure(sizeof(double) * y);
+  InvIterArgs ia{};
+  ia.nblocks = nb; ia.bsize = d_bsize; ia.soff = d_soff; ia.d = c->d.as<double>(); ia.e = c->e.as<double>();
+  ia.ev = c->ev.as<double>(); ia.nvec = (const int*)(base + o_nvec); ia.yoff = (const int64_t*)(base + o_yoff);
+  ia.Y = c->Y.as<double>(); ia.scratch = c->scratch.as<double>();
+  ia.cl_block = (const int*)(base + o_cb); ia.cl_first = (const int*)(base + o_cf); ia.cl_count = (const int*)(base + o_cn);
+  ia.nclusters = (int)cb.size(); ia.flag = c->flag.as<int>();
+  cudaEvent_t t0 = tm.start();
+  launch_inviter(ia, (const int*)(base + o_vb), (const int*)(base + o_vi), (int)vb.size(), c->stream);
+  c->launches += 2;
+  tm.stop(t0, &c->timing.tridiag_eig_ms);
+  BackArgs ba{};
+  ba.bsize = d_bsize; ba.hoff = d_hoff; ba.H_const = c->H.as<double>(); ba.soff = d_soff; ba.tau = c->tau.as<double>();
+  ba.nvec = ia.nvec; ba.yoff = ia.yoff; ba.Y = c->Y.as<double>(); ba.Z = c->Z.as<double>(); ba.Zt = c->Zt.as<double>();
+  ba.zoff = ia.yoff; ba.maxn = std::max(P.maxn, 1);
+  cudaEvent_t t1 = tm.start();
+  CU(launch_backtransform(ba, (const int*)(base + o_tb), (const int*)(base + o_tf), (int)ctab.size(), c->stream));
+  c->launches++;
+  tm.stop(t1, &c->timing.backtransform_ms);
+  double fl = 0.0;
+  for (int b = 0; b < nb; ++b) fl += 2.0 * (double)P.bsize[b] * P.bsize[b] * P.nvec[b];
+  c->timing.backtransform_flops += fl;
+}
+
+// ------------------------------------------------------------------ sweep state
+struct OpMeta {
+  std::vector<int> bi, bj;
+  std::vector<int64_t> off;
+  int64_t size = 0;
+  int find(int i, int j) const {
+    for (size_t k = 0; k < bi.size(); ++k) if (bi[k] == i && bj[k] == j) return (int)k;
+    return -1;
+  }
+};
+
+struct Kept {
+  BlockArray blk;        // kept blocks: QNs, kept sizes, offsets
+  std::vector<int> src;  // index of the block in the previous iteration's basis
+};
+
+struct Sweep {
+  nrg_ctx* c;
+  ModelSpec m;
+  nrg_sweep_config cfg;
+  Kept kept;
+  std::vector<OpMeta> ops;
+  int cur = 0;           // which of ops_a / ops_b holds the current operators
+  DevBuf* opbuf(int which, int o) { return which == 0 ? &c->ops_a[o] : &c->ops_b[o]; }
+};
+
+double opavg_host(const BlockArray& a, const std::vector<double>& en, const std::vector<double>& diag, bool totalS,
+                  double beta) {
+  // CalcOpAvg (CalcOpAvg.cpp:13-84) on a one-state-per-block array.
+  double s = 0, Z = 0;
+  for (int b = 0; b < a.nblocks(); ++b) {
+    double deg = totalS ? 2.0 * a.q(b, 1) + 1.0 : 1.0;
+    for (int i = a.offset[b]; i < a.offset[b] + a.size[b]; ++i) {
+      double w = std::exp(-beta * en[i]);
+      s += deg * diag[i] * w; Z += deg * w;
+    }
+  }
+  if (!(std::fabs(Z) < 1.e-20)) s = s / Z;
+  return s;
+}
+
+void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
+  using clock = std::chrono::steady_clock;
+  auto t_begin = clock::now();
+  if (cfg->model < 0 || cfg->model > 2) throw NrgError(NRG_ERR_ARG, "unknown model");
+  if (cfg->nsites < 1 || cfg->ncutoff < 4 || !(cfg->lambda > 1.0)) throw NrgError(NRG_ERR_ARG, "bad sweep parameters");
+  if (cfg->precision != NRG_PREC_FP64) throw NrgError(NRG_ERR_ARG, "unsupported precision");
+  c->iters.clear();
+  c->opavg_m1.clear();
+  std::memset(&c->timing, 0, sizeof(c->timing));
+  const int64_t launches0 = c->launches;
+  Sweep S;
+  S.c = c;
+  S.m = make_model((ModelKind)cfg->model);
+  S.cfg = *cfg;
+  const ModelSpec& m = S.m;
+  const double eps = cfg->degen_eps > 0 ? cfg->degen_eps : 1.0e-18;
+  const double lambda = cfg->lambda;
+  const double HLF = 0.5 * (1.0 + 1.0 / lambda);
+  const double betabar = 0.727;
+  const int nops = (int)m.op_kind.size();
+  const int nops_h = m.kind == MODEL_1CHQS ? 1 : 2;  // old operators entering H_N
+  Timer tm(c);
+  c->flag.ensure(sizeof(int) * 4);
+  CU(cudaMemsetAsync(c->flag.p, 0, sizeof(int), c->stream));
+  c->scal.ensure(sizeof(double) * 32);
+  c->partial.ensure(sizeof(double) * 64 * 16);
+  c->opptr.ensure(sizeof(double*) * 32);
+
+  // H_{-1} (the initial CutStates keeps everything: Ncutoff >= 4 states).
+  StartState st = make_start(m, lambda, cfg->U, cfg->ed, cfg->gamma2_or_B);
+  S.kept.blk = st.blk;
+  std::vector<double> kept_en = st.en;
+  for (int o = 0; o < nops; ++o) {
+    OpMeta om;
+    om.bi = st.ops[o].bi; om.bj = st.ops[o].bj; om.off = st.ops[o].off; om.size = (int64_t)st.ops[o].el.size();
+    S.ops.push_back(om);
+    DevBuf* b = S.opbuf(0, o);
+    b->ensure(sizeof(double) * std::max<int64_t>(om.size, 1));
+    CU(cudaMemcpyAsync(b->p, st.ops[o].el.data(), sizeof(double) * om.size, cudaMemcpyHostToDevice, c->stream));
+    if (m.op_avg[o]) {
+      std::vector<double> diag(st.en.size(), 0.0);
+      for (size_t k = 0; k < st.ops[o].bi.size(); ++k)
+        if (st.ops[o].bi[k] == st.ops[o].bj[k]) diag[st.blk.offset[st.ops[o].bi[k]]] = st.ops[o].el[st.ops[o].off[k]];
+      c->opavg_m1.push_back(opavg_host(st.blk, st.en, diag, m.totalS, betabar));
+    }
+  }
+
+  double chi[2] = {chi_m1(lambda, cfg->gamma1), 0.0};
+  if (m.nchan == 2) chi[1] = chi_m1(lambda, cfg->gamma2_or_B);
+  const double eN = 0.0;  // flat band (CNRGchain::GetEn of SetChainWilson)
+
+  for (int N = 0; N < cfg->nsites; ++N) {
+    IterResult R;
+    R.params = {lambda, chi[0], chi[1], eN};
+    const double DN = HLF * std::pow(lambda, (-(N - 1) / 2.0));
+    // ---------------- BuildBasis + tables (host)
+    Basis B;
+    build_basis(m, S.kept.blk, B);
+    HNTables tabs;
+    build_hn_tables(m, B, tabs);
+    const int nb = B.blk.nblocks();
+    EigPlan P;
+    plan_blocks(P, B.blk.size);
+    std::vector<int> order(nb);
+    for (int b = 0; b < nb; ++b) order[b] = b;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return P.bsize[x] > P.bsize[y]; });
+    std::vector<int> state_block(P.nstates), row_index(P.nstates), st_seg(P.nstates), st_a(P.nstates),
+        st_type(P.nstates);
+    std::vector<double> st_eold(P.nstates);
+    for (int b = 0; b < nb; ++b)
+      for (int i = 0; i < P.bsize[b]; ++i) {
+        int g = P.soff[b] + i;
+        state_block[g] = b; row_index[g] = i;
+        st_seg[g] = B.seg_of[g]; st_a[g] = B.a_of[g]; st_type[g] = B.itype[g];
+        st_eold[g] = kept_en[B.stcf[g]];
+      }
+    std::vector<int> nseg(nb);
+    std::vector<int64_t> pair_base(nb), pair_fwd, pair_bwd;
+    std::vector<int> pair_fwd_ld, pair_bwd_ld;
+    for (int b = 0; b < nb; ++b) {
+      const auto& sg = B.seg[b];
+      nseg[b] = (int)sg.size();
+      pair_base[b] = (int64_t)pair_fwd.size();
+      for (size_t p = 0; p < sg.size(); ++p)
+        for (size_t q = 0; q < sg.size(); ++q)
+          for (int o = 0; o < nops_h; ++o) {
+            const OpMeta& om = S.ops[o];
+            int kf = om.find(sg[p].old_block, sg[q].old_block);
+            int kb = om.find(sg[q].old_block, sg[p].old_block);
+            pair_fwd.push_back(kf >= 0 ? om.off[kf] : -1);
+            pair_fwd_ld.push_back(kf >= 0 ? S.kept.blk.size[om.bj[kf]] : 0);
+            pair_bwd.push_back(kb >= 0 ? om.off[kb] : -1);
+            pair_bwd_ld.push_back(kb >= 0 ? S.kept.blk.size[om.bj[kb]] : 0);
+          }
+    }
+    std::vector<double> site_q(m.site.nstates);
+    for (int t = 0; t < m.site.nstates; ++t) site_q[t] = m.site.blk.q(m.site.block_of_state(t), 0);
+    Packer pk;
+    size_t o_bsize = pk.add(P.bsize), o_soff = pk.add(P.soff), o_hoff = pk.add(P.hoff), o_order = pk.add(order),
+           o_sb = pk.add(state_block), o_ri = pk.add(row_index), o_seg = pk.add(st_seg), o_a = pk.add(st_a),
+           o_type = pk.add(st_type), o_eold = pk.add(st_eold), o_nseg = pk.add(nseg), o_pb = pk.add(pair_base),
+           o_pf = pk.add(pair_fwd), o_pfl = pk.add(pair_fwd_ld), o_pbw = pk.add(pair_bwd), o_pbl = pk.add(pair_bwd_ld),
+           o_coef = pk.add(tabs.coef), o_sq = pk.add(site_q), o_bq = pk.add(B.blk.qn);
+    c->meta.ensure(pk.host.size() + 256);
+    CU(cudaMemcpyAsync(c->meta.p, pk.host.data(), pk.host.size(), cudaMemcpyHostToDevice, c->stream));
+    char* mb = c->meta.as<char>();
+    c->H.ensure(sizeof(double) * std::max<int64_t>(P.hsize, 1));
+    c->d.ensure(sizeof(double) * P.nstates); c->e.ensure(sizeof(double) * P.nstates);
+    c->tau.ensure(sizeof(double) * P.nstates); c->ev.ensure(sizeof(double) * P.nstates);
+    c->en.ensure(sizeof(double) * P.nstates);
+    c->red.ensure(sizeof(int) * (nb + 8));
+    // operator pointer table
+    std::vector<const double*> hops(8, nullptr);
+    for (int o = 0; o < nops; ++o) hops[o] = S.opbuf(S.cur, o)->as<double>();
+    CU(cudaMemcpyAsync(c->opptr.p, hops.data(), sizeof(double*) * hops.size(), cudaMemcpyHostToDevice, c->stream));
+    // ---------------- assembly
+    AssembleArgs aa{};
+    aa.nblocks = nb; aa.bsize = (const int*)(mb + o_bsize); aa.bstate = (const int*)(mb + o_soff);
+    aa.hoff = (const int64_t*)(mb + o_hoff); aa.seg_nseg = (const int*)(mb + o_nseg);
+    aa.st_seg = (const int*)(mb + o_seg); aa.st_a = (const int*)(mb + o_a); aa.st_type = (const int*)(mb + o_type);
+    aa.st_eold = (const double*)(mb + o_eold); aa.pair_base = (const int64_t*)(mb + o_pb);
+    aa.pair_fwd = (const int64_t*)(mb + o_pf); aa.pair_fwd_ld = (const int*)(mb + o_pfl);
+    aa.pair_bwd = (const int64_t*)(mb + o_pbw); aa.pair_bwd_ld = (const int*)(mb + o_pbl);
+    aa.coef = (const double*)(mb + o_coef); aa.ntypes = tabs.ntypes; aa.nchan = tabs.nchan; aa.nsigma = tabs.nsigma;
+    aa.nops_h = nops_h; aa.model = (int)m.kind; aa.ops = (const double* const*)c->opptr.p;
+    aa.sqrt_lambda = std::sqrt(lambda); aa.eN = eN; aa.chi[0] = chi[0]; aa.chi[1] = chi[1];
+    aa.site_q = (const double*)(mb + o_sq); aa.H = c->H.as<double>();
+    cudaEvent_t ta = tm.start();
+    launch_assemble(aa, P.nstates, (const int*)(mb + o_sb), (const int*)(mb + o_ri), c->stream);
+    c->launches++;
+    tm.stop(ta, &c->timing.assemble_ms);
+    // ---------------- tridiagonalization + eigenvalues
+    run_tridiag_and_bisect(c, tm, P, order, (const int*)(mb + o_order), (const int*)(mb + o_bsize),
+                           (const int64_t*)(mb + o_hoff), (const int*)(mb + o_soff), (const int*)(mb + o_sb));
+    // ---------------- SetE0zero / SetDegen / Ecut / Kept / CutStates bookkeeping
+    cudaEvent_t tc = tm.start();
+    CutArgs ca{};
+    ca.nstates = P.nstates; ca.ev = c->ev.as<double>(); ca.en = c->en.as<double>(); ca.ncutoff = cfg->ncutoff; ca.eps = eps;
+    ca.out_scalars = c->scal.as<double>(); ca.flag = c->flag.as<int>();
+    launch_cut(ca, c->stream);
+    std::vector<int> keptb(nb);
+    BlockStatsArgs bs{};
+    bs.nblocks = nb; bs.bsize = aa.bsize; bs.soff = aa.bstate; bs.en = c->en.as<double>(); bs.scalars = ca.out_scalars;
+    bs.kept = c->red.as<int>() + 4;
+    launch_block_stats(bs, c->stream);
+    ThermoArgs th{};
+    std::vector<double> betas(4);
+    for (int nc = 1; nc <= 4; ++nc) betas[nc - 1] = betabar * std::pow(lambda, (nc - 4) / (2.0 * 4));
+    th.bq = (const double*)(mb + o_bq); th.en = c->en.as<double>(); th.totalS = m.totalS ? 1 : 0;
+    for (int t = 0; t < 4; ++t) th.beta[t] = betas[t];
+    th.out = c->scal.as<double>() + 8;
+    launch_thermo(th, (const int*)(mb + o_sb), P.nstates, c->partial.as<double>(), c->stream);
+    c->launches += 4;
+    std::vector<double> scal(20);
+    R.en.resize(P.nstates);
+    CU(cudaMemcpyAsync(scal.data(), c->scal.p, sizeof(double) * 20, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemcpyAsync(keptb.data(), bs.kept, sizeof(int) * nb, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemcpyAsync(R.en.data(), c->en.p, sizeof(double) * P.nstates, cudaMemcpyDeviceToHost, c->stream));
+    tm.stop(tc, &c->timing.cut_ms);
+    CU(cudaStreamSynchronize(c->stream));
+    check_flag(c);
+    R.emin = scal[0]; R.ecut = scal[1]; R.nkept = (int)scal[2];
+    R.qn = B.blk.qn; R.bsize = P.bsize;
+    for (int t = 0; t < 4; ++t) {
+      const double Z = scal[8 + 3 * t], s1 = scal[8 + 3 * t + 1], sE = scal[8 + 3 * t + 2];
+      R.thermo.push_back(betas[t]);
+      R.thermo.push_back(DN / betas[t]);
+      R.thermo.push_back((s1 - 0.0 * s1) / Z);
+      R.thermo.push_back(betas[t] * (sE / Z) + std::log(Z));
+    }
+    // ---------------- new kept array (CutStates)
+    Kept K;
+    K.blk.nqn = 2;
+    std::vector<double> new_kept_en;
+    for (int b = 0; b < nb; ++b) {
+      if (keptb[b] <= 0) continue;
+      K.blk.push(&B.blk.qn[2 * b], keptb[b]);
+      K.src.push_back(b);
+      for (int x = 0; x < keptb[b]; ++x) new_kept_en.push_back(R.en[P.soff[b] + x]);
+    }
+    for (int x : K.blk.size) R.kept_bsize.push_back(x);
+    // ---------------- kept eigenvectors
+    P.nvec.assign(nb, 0);
+    for (int b = 0; b < nb; ++b) P.nvec[b] = keptb[b];
+    // eigenvalues for clustering: shifted energies have the same gaps
+    run_vectors(c, tm, P, R.en, aa.bsize, aa.hoff, aa.bstate);
+    // ---------------- UpdateMatrices
+    cudaEvent_t tu = tm.start();
+    std::vector<OpMeta> newops(nops);
+    std::vector<RotJob> jobs;
+    std::vector<GatherTerm> terms;
+    std::vector<int> gfirst, gcount, tjob, tmn;
+    int64_t tsize = 0;
+    const int nk = K.blk.nblocks();
+    for (int o = 0; o < nops; ++o) {
+      OpMeta& no = newops[o];
+      for (int i = 0; i < nk; ++i)
+        for (int j = 0; j < nk; ++j) {
+          if (!op_check(m.op_check[o], K.blk, i, j)) continue;
+          const int bI = K.src[i], bJ = K.src[j];
+          RotJob J{};
+          J.ki = K.blk.size[i]; J.kj = K.blk.size[j]; J.nI = P.bsize[bI];
+          J.z_off = P.yoff[bI]; J.zt_off = P.yoff[bJ]; J.t_off = tsize; J.o_off = no.size; J.op = o;
+          no.bi.push_back(i); no.bj.push_back(j); no.off.push_back(no.size);
+          no.size += (int64_t)J.ki * J.kj;
+          tsize += (int64_t)J.nI * J.kj;
+          const int jid = (int)jobs.size();
+          jobs.push_back(J);
+          const double SI = B.blk.q(bI, 1), SJ = B.blk.q(bJ, 1);
+          const auto& segI = B.seg[bI];
+          const auto& segJ = B.seg[bJ];
+          for (const Segment& p : segI)
+            for (int u = 0; u < p.nsite; ++u) {
+              const int tu_ = m.site.blk.offset[p.site_block] + u;
+              const int first = (int)terms.size();
+              for (const Segment& q : segJ)
+                for (int v = 0; v < q.nsite; ++v) {
+                  const int tv = m.site.blk.offset[q.site_block] + v;
+                  GatherTerm G{};
+                  G.job = jid; G.dst_base = p.offset + u; G.dst_stride = p.nsite; G.rows = p.count;
+                  G.src_base = q.offset + v; G.src_stride = q.nsite; G.srows = q.count;
+                  if (m.op_kind[o] == OP_IMPONLY) {
+                    if (tu_ != tv) continue;
+                    const OpMeta& om = S.ops[o];
+                    int kx = om.find(p.old_block, q.old_block);
+                    if (kx < 0) continue;
+                    G.mode = 1; G.coef = 1.0; G.old_off = om.off[kx]; G.op = o;
+                  } else {
+                    if (p.old_block != q.old_block) continue;
+                    double g = op_site_factor(m, m.op_kind[o], SI, SJ, tu_, tv);
+                    if (g == 0.0) continue;
+                    G.mode = 0; G.coef = g;
+                  }
+                  terms.push_back(G);
+                }
+              if ((int)terms.size() > first) { gfirst.push_back(first); gcount.push_back((int)terms.size() - first); }
+            }
+          for (int mt = 0; mt * 64 < J.ki; ++mt)
+            for (int nt = 0; nt * 64 < J.kj; ++nt) { tjob.push_back(jid); tmn.push_back((mt << 16) | nt); }
+        }
+    }
+    int nxt = 1 - S.cur;
+    std::vector<double*> newptr(8, nullptr), oldptr(8, nullptr);
+    for (int o = 0; o < nops; ++o) {
+      DevBuf* b = S.opbuf(nxt, o);
+      b->ensure(sizeof(double) * std::max<int64_t>(newops[o].size, 1));
+      newptr[o] = b->as<double>();
+      oldptr[o] = S.opbuf(S.cur, o)->as<double>();
+    }
+    Packer up;
+    size_t o_terms = up.add(terms), o_gf = up.add(gfirst), o_gc = up.add(gcount), o_jobs = up.add(jobs),
+           o_tj = up.add(tjob), o_tm = up.add(tmn), o_old = up.add(oldptr), o_new = up.add(newptr),
+           o_ken = up.add(new_kept_en);
+    // kept-state tables for the operator averages
+    std::vector<int> kstate_block, ksz = K.blk.size, koff = K.blk.offset;
+    for (int i = 0; i < nk; ++i) for (int x = 0; x < K.blk.size[i]; ++x) kstate_block.push_back(i);
+    std::vector<int64_t> diag_off;
+    std::vector<int> avg_ops;
+    for (int o = 0; o < nops; ++o) if (m.op_avg[o]) avg_ops.push_back(o);
+    std::vector<const double*> avgptr;
+    for (int o : avg_ops) {
+      avgptr.push_back(newptr[o]);
+      for (int i = 0; i < nk; ++i) { int k = newops[o].find(i, i); diag_off.push_back(k >= 0 ? newops[o].off[k] : -1); }
+    }
+    size_t o_ksb = up.add(kstate_block), o_ksz = up.add(ksz), o_koff = up.add(koff), o_doff = up.add(diag_off),
+           o_avp = up.add(avgptr), o_kq = up.add(K.blk.qn);
+    c->T.ensure(sizeof(double) * std::max<int64_t>(tsize, 1) + up.host.size() + 512);
+    char* ub = c->T.as<char>() + ((sizeof(double) * std::max<int64_t>(tsize, 1) + 255) & ~size_t(255));
+    CU(cudaMemcpyAsync(ub, up.host.data(), up.host.size(), cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemsetAsync(c->T.p, 0, sizeof(double) * std::max<int64_t>(tsize, 1), c->stream));
+    UpdateArgs ua{};
+    ua.terms = (const GatherTerm*)(ub + o_terms); ua.group_first = (const int*)(ub + o_gf);
+    ua.group_count = (const int*)(ub + o_gc); ua.ngroups = (int)gfirst.size(); ua.jobs = (const RotJob*)(ub + o_jobs);
+    ua.Z = c->Z.as<double>(); ua.Zt = c->Zt.as<double>(); ua.T = c->T.as<double>();
+    ua.old_ops = (const double* const*)(ub + o_old); ua.new_ops = (double* const*)(ub + o_new);
+    ua.tile_job = (const int*)(ub + o_tj); ua.tile_mn = (const int*)(ub + o_tm); ua.ntiles = (int)tjob.size();
+    launch_update(ua, c->stream);
+    c->launches += 2;
+    for (const RotJob& J : jobs) c->timing.update_flops += 2.0 * J.ki * (double)J.nI * J.kj;
+    tm.stop(tu, &c->timing.update_ms);
+    // ---------------- CalcStuff: operator averages over the kept states
+    cudaEvent_t to = tm.start();
+    OpDiagArgs od{};
+    od.nblocks = nk; od.ksize = (const int*)(ub + o_ksz); od.koff = (const int*)(ub + o_koff);
+    od.ken = (const double*)(ub + o_ken); od.bq = (const double*)(ub + o_kq); od.totalS = m.totalS ? 1 : 0;
+    od.beta = betabar; od.nops = (int)avg_ops.size(); od.ops = (const double* const*)(ub + o_avp);
+    od.diag_off = (const int64_t*)(ub + o_doff); od.out = c->scal.as<double>() + 24;
+    launch_opdiag(od, (const int*)(ub + o_ksb), (int)kstate_block.size(), c->partial.as<double>(), c->stream);
+    c->launches += 2;
+    std::vector<double> avg(8);
+    CU(cudaMemcpyAsync(avg.data(), c->scal.as<double>() + 24, sizeof(double) * 8, cudaMemcpyDeviceToHost, c->stream));
+    tm.stop(to, &c->timing.cut_ms);
+    CU(cudaStreamSynchronize(c->stream));
+    check_flag(c);
+    tm.collect();
+    const double Zk = avg[avg_ops.size()];
+    for (size_t k = 0; k < avg_ops.size(); ++k) {
+      double s = avg[k];
+      if (!(std::fabs(Zk) < 1.e-20)) s = s / Zk;
+      R.opavg.push_back(s);
+    }
+    // ---------------- next iteration
+    S.kept = K;
+    kept_en = new_kept_en;
+    S.ops = newops;
+    S.cur = nxt;
+    for (int ich = 0; ich < m.nchan; ++ich) chi[ich] = chin(lambda, N);
+    c->iters.push_back(std::move(R));
+  }
+  c->timing.kernel_launches = c->launches - launches0;
+  c->timing.total_ms = std::chrono::duration<double, std::milli>(clock::now() - t_begin).count();
+}
+
+}  // namespace
+}  // namespace nrg
+
+// ================================================================== C ABI
+using namespace nrg;
+
+#define GUARD(ctx, body)                                   \
+  try {                                                    \
+    body;                                                  \
+  } catch (const NrgError& ex) {                           \
+    if (ctx) (ctx)->err = ex.what();                       \
+    return ex.st;                                          \
+  } catch (const std::exception& ex) {                     \
+    if (ctx) (ctx)->err = ex.what();                       \
+    return NRG_ERR_ARG;                                    \
+  }
+
+extern "C" {
+
+const char* nrg_status_string(nrg_status s) {
+  switch (s) {
+    case NRG_OK: return "ok";
+    case NRG_ERR_ARG: return "bad argument";
+    case NRG_ERR_CUDA: return "CUDA error";
+    case NRG_ERR_NOMEM: return "out of memory";
+    case NRG_ERR_NOT_CONVERGED: return "not converged";
+    case NRG_ERR_SIZE: return "size limit exceeded";
+    case NRG_ERR_SYNC: return "block structures out of sync";
+    case NRG_ERR_TIMEOUT: return "device wait timed out";
+    case NRG_ERR_STATE: return "bad call order";
+  }
+  return "unknown";
+}
+
+nrg_status nrg_create(int device, nrg_ctx** out) {
+  if (!out) return NRG_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return NRG_ERR_CUDA;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return NRG_ERR_CUDA;
+  if (prop.major < 10) return NRG_ERR_CUDA;  // built for sm_103a only
+  if (cudaSetDevice(device) != cudaSuccess) return NRG_ERR_CUDA;
+  nrg_ctx* c = new nrg_ctx();
+  c->device = device;
+  c->num_sms = prop.multiProcessorCount;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return NRG_ERR_CUDA; }
+  *out = c;
+  return NRG_OK;
+}
+
+void nrg_destroy(nrg_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char* nrg_last_error(const nrg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int64_t nrg_kernel_count(const nrg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+nrg_status nrg_sweep_run(nrg_ctx* ctx, const nrg_sweep_config* cfg) {
+  if (!ctx || !cfg) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    sweep_run(ctx, cfg);
+  });
+  return NRG_OK;
+}
+
+int nrg_sweep_num_iterations(const nrg_ctx* ctx) { return ctx ? (int)ctx->iters.size() : 0; }
+
+nrg_status nrg_sweep_iteration(const nrg_ctx* ctx, int n, nrg_iteration* out) {
+  if (!ctx || !out || n < 0 || n >= (int)ctx->iters.size()) return NRG_ERR_ARG;
+  const IterResult& R = ctx->iters[n];
+  out->nblocks = (int)R.bsize.size();
+  out->qnumbers = R.qn.data();
+  out->block_size = R.bsize.data();
+  out->nstates = (int)R.en.size();
+  out->en = R.en.data();
+  out->emin = R.emin;
+  out->ecut = R.ecut;
+  out->nkept = R.nkept;
+  out->nkept_blocks = (int)R.kept_bsize.size();
+  out->kept_block_size = R.kept_bsize.data();
+  out->thermo = R.thermo.data();
+  out->nops = (int)R.opavg.size();
+  out->opavg = R.opavg.data();
+  out->params = R.params.data();
+  return NRG_OK;
+}
+
+nrg_status nrg_sweep_opavg_initial(const nrg_ctx* ctx, int* nops, const double** vals) {
+  if (!ctx || !nops || !vals) return NRG_ERR_ARG;
+  *nops = (int)ctx->opavg_m1.size();
+  *vals = ctx->opavg_m1.data();
+  return NRG_OK;
+}
+
+nrg_status nrg_sweep_timing(const nrg_ctx* ctx, nrg_timing* out) {
+  if (!ctx || !out) return NRG_ERR_ARG;
+  *out = ctx->timing;
+  return NRG_OK;
+}
+
+}  // extern "C"

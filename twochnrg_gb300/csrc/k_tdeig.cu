@@ -1,0 +1,284 @@
+// Eigenpairs of the tridiagonal matrices left by the tridiagonalization, and
+// the back-transformation to eigenvectors of the H_N blocks (FP64).
+//
+// Together with k_tridiag.cu this replaces the per-block dspev call of
+// CNRGmatrix::DiagBlock (NRGmatrixClass.cpp:566-696).  Eigenvalues come from
+// Sturm-count bisection (one thread per eigenvalue, all blocks in one grid);
+// eigenvectors are only formed for the states that survive the cut (the
+// reference keeps only those rows of dEigVec, CutStates.cpp:10-95 and
+// RemoveStatesFromBlock NRGarrayClass.cpp:1467-1548): inverse iteration per
+// wanted eigenvalue (one thread per vector), a modified Gram-Schmidt pass over
+// clusters of close eigenvalues, then the Householder reflectors are applied
+// in reverse order with one warp per eigenvector.
+#include <cfloat>
+
+#include "nrg_device.cuh"
+
+namespace nrg {
+
+namespace {
+
+constexpr double kEps = 2.220446049250313e-16;
+
+__device__ __forceinline__ int sturm_count(const double* d, const double* e, int n, double x, double pivmin) {
+  int cnt = 0;
+  double q = d[0] - x;
+  if (fabs(q) < pivmin) q = -pivmin;
+  if (q < 0.0) cnt++;
+  for (int i = 1; i < n; ++i) {
+    const double ei = e[i - 1];
+    q = (d[i] - x) - (ei * ei) / q;
+    if (fabs(q) < pivmin) q = -pivmin;
+    if (q < 0.0) cnt++;
+  }
+  return cnt;
+}
+
+__global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= A.nstates) return;
+  const int b = state_block[g];
+  const int n = A.bsize[b];
+  const int so = A.soff[b];
+  const int k = g - so;
+  const double* d = A.d + so;
+  const double* e = A.e + so;
+  double gl = DBL_MAX, gu = -DBL_MAX, emax2 = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
+    gl = fmin(gl, d[i] - r);
+    gu = fmax(gu, d[i] + r);
+    if (i + 1 < n) emax2 = fmax(emax2, e[i] * e[i]);
+  }
+  const double tnorm = fmax(fabs(gl), fabs(gu));
+  const double pivmin = DBL_MIN * fmax(1.0, emax2);
+  double lo = gl - 2.0 * kEps * tnorm * n - 2.0 * pivmin;
+  double hi = gu + 2.0 * kEps * tnorm * n + 2.0 * pivmin;
+  const double atol = 1e-3 * kEps * fmax(tnorm, DBL_MIN);
+  for (int it = 0; it < 200; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (mid <= lo || mid >= hi) break;
+    if (hi - lo <= fmax(2.0 * kEps * fmax(fabs(lo), fabs(hi)), atol)) break;
+    if (sturm_count(d, e, n, mid, pivmin) > k) hi = mid; else lo = mid;
+  }
+  const double v = 0.5 * (lo + hi);
+  if (!isfinite(v)) atomicOr(A.flag, DEV_BAD_INPUT);
+  A.ev[g] = v;
+}
+
+// Deterministic pseudo-random start vector component in (-1, 1).
+__device__ __forceinline__ double start_component(int k, int i) {
+  uint64_t z = ((uint64_t)(uint32_t)k << 32) ^ (uint64_t)(uint32_t)i ^ 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return 2.0 * ((double)(z >> 11) * (1.0 / 9007199254740992.0)) - 1.0;
+}
+
+// One thread per wanted eigenvector.  Scratch per block: five interleaved
+// n x nv arrays (l, 1/u1, u2, u3, pivot flag); Y is interleaved n x nv.
+__global__ void inviter_kernel(InvIterArgs A, const int* vec_block, const int* vec_index, int nvecs) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nvecs) return;
+  const int b = vec_block[g];
+  const int k = vec_index[g];
+  const int n = A.bsize[b];
+  const int so = A.soff[b];
+  const int nv = A.nvec[b];
+  const double* d = A.d + so;
+  const double* e = A.e + so;
+  const double* ev = A.ev + so;
+  double* Y = A.Y + A.yoff[b];
+  double* L = A.scratch + 5 * A.yoff[b];
+  double* IU1 = L + (int64_t)n * nv;
+  double* U2 = IU1 + (int64_t)n * nv;
+  double* U3 = U2 + (int64_t)n * nv;
+  double* PV = U3 + (int64_t)n * nv;
+#define AT(arr, i) arr[(int64_t)(i) * nv + k]
+  double onenrm = 0.0;
+  for (int i = 0; i < n; ++i)
+    onenrm = fmax(onenrm, fabs(d[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0));
+  onenrm = fmax(onenrm, DBL_MIN);
+  // Shift: separate numerically equal eigenvalues as LAPACK dstein does.
+  double sigma = ev[k];
+  {
+    int run = 0;
+    for (int kk = k - 1; kk >= 0 && ev[k] - ev[kk] < 10.0 * kEps * fmax(fabs(ev[k]), onenrm * 1e-3); --kk) run++;
+    sigma += run * 10.0 * kEps * fmax(fabs(ev[k]), onenrm * 1e-3);
+  }
+  if (n == 1) { AT(Y, 0) = 1.0; return; }
+  // LU with partial pivoting of T - sigma I (rows i, i+1 may swap).
+  const double tiny = kEps * onenrm;
+  double u1 = d[0] - sigma, u2 = e[0];
+  for (int i = 0; i + 1 < n; ++i) {
+    const double c = e[i];                  // sub-diagonal below row i
+    const double an = d[i + 1] - sigma;     // next diagonal
+    const double bn = (i + 2 < n) ? e[i + 1] : 0.0;
+    double l, nu1, nu2, r1, r2, r3;
+    if (fabs(c) > fabs(u1)) {               // swap rows i and i+1
+      l = u1 / c;
+      r1 = c; r2 = an; r3 = bn;
+      nu1 = u2 - l * an; nu2 = -l * bn;
+      AT(PV, i) = 1.0;
+    } else {
+      if (fabs(u1) < tiny) u1 = copysign(tiny, u1);
+      l = c / u1;
+      r1 = u1; r2 = u2; r3 = 0.0;
+      nu1 = an - l * u2; nu2 = bn;
+      AT(PV, i) = 0.0;
+    }
+    if (fabs(r1) < tiny) r1 = copysign(tiny, r1);
+    AT(L, i) = l; AT(IU1, i) = 1.0 / r1; AT(U2, i) = r2; AT(U3, i) = r3;
+    u1 = nu1; u2 = nu2;
+  }
+  if (fabs(u1) < tiny) u1 = copysign(tiny, u1);
+  AT(IU1, n - 1) = 1.0 / u1; AT(U2, n - 1) = 0.0; AT(U3, n - 1) = 0.0; AT(L, n - 1) = 0.0; AT(PV, n - 1) = 0.0;
+  const double last = fabs(u1);
+  for (int i = 0; i < n; ++i) AT(Y, i) = start_component(k, i);
+  const double dtpcrt = sqrt(0.1 / n);
+  int extra = 0;
+  bool conv = false;
+  for (int it = 0; it < 8; ++it) {
+    double asum = 0.0;
+    for (int i = 0; i < n; ++i) asum += fabs(AT(Y, i));
+    const double scl = n * onenrm * fmax(kEps, last) / fmax(asum, DBL_MIN);
+    // forward: P and L, in place
+    double xi = AT(Y, 0) * scl;
+    for (int i = 0; i + 1 < n; ++i) {
+      double xn = AT(Y, i + 1) * scl;
+      if (AT(PV, i) != 0.0) { const double t = xi; xi = xn; xn = t - AT(L, i) * xn; }
+      else xn = xn - AT(L, i) * xi;
+      AT(Y, i) = xi;
+      xi = xn;
+    }
+    AT(Y, n - 1) = xi;
+    // backward: U
+    double x2 = 0.0, x1 = 0.0;
+    double nrmmax = 0.0;
+    for (int i = n - 1; i >= 0; --i) {
+      const double x = (AT(Y, i) - AT(U2, i) * x1 - AT(U3, i) * x2) * AT(IU1, i);
+      AT(Y, i) = x;
+      x2 = x1; x1 = x;
+      nrmmax = fmax(nrmmax, fabs(x));
+    }
+    // normalise to max 1 to keep the next scaling in range
+    const double inv = 1.0 / fmax(nrmmax, DBL_MIN);
+    for (int i = 0; i < n; ++i) AT(Y, i) *= inv;
+    if (nrmmax >= dtpcrt) { conv = true; if (++extra >= 2) break; }
+  }
+  if (!conv) atomicOr(A.flag, DEV_NOT_CONVERGED);
+  double s2 = 0.0, big = 0.0;
+  int jmax = 0;
+  for (int i = 0; i < n; ++i) {
+    const double x = AT(Y, i);
+    s2 += x * x;
+    if (fabs(x) > big) { big = fabs(x); jmax = i; }
+  }
+  double nrm = 1.0 / sqrt(s2);
+  if (AT(Y, jmax) < 0.0) nrm = -nrm;
+  for (int i = 0; i < n; ++i) AT(Y, i) *= nrm;
+#undef AT
+}
+
+// Modified Gram-Schmidt over each cluster of close eigenvalues (one warp per
+// cluster, vectors in ascending order, two passes).
+__global__ void mgs_kernel(InvIterArgs A) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= A.nclusters) return;
+  const int b = A.cl_block[warp], k0 = A.cl_first[warp], cnt = A.cl_count[warp];
+  if (cnt < 2) return;
+  const int n = A.bsize[b], nv = A.nvec[b];
+  double* Y = A.Y + A.yoff[b];
+  for (int kk = 1; kk < cnt; ++kk) {
+    const int k = k0 + kk;
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int jj = 0; jj < kk; ++jj) {
+        const int j = k0 + jj;
+        double dot = 0.0;
+        for (int i = lane; i < n; i += 32) dot = fma(Y[(int64_t)i * nv + j], Y[(int64_t)i * nv + k], dot);
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+        for (int i = lane; i < n; i += 32) Y[(int64_t)i * nv + k] = fma(-dot, Y[(int64_t)i * nv + j], Y[(int64_t)i * nv + k]);
+      }
+      double s2 = 0.0;
+      for (int i = lane; i < n; i += 32) { const double x = Y[(int64_t)i * nv + k]; s2 = fma(x, x, s2); }
+      for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+      const double inv = 1.0 / sqrt(s2);
+      for (int i = lane; i < n; i += 32) Y[(int64_t)i * nv + k] *= inv;
+    }
+  }
+}
+
+constexpr int kBackWarps = 8;
+
+// Apply H_0 H_1 ... H_{n-3} to the eigenvectors of T.  One CTA takes up to
+// eight eigenvectors of one block; each reflector is staged once in shared
+// memory for all of them.
+__global__ void __launch_bounds__(kBackWarps * 32) backtransform_kernel(BackArgs A, const int* cta_block,
+                                                                       const int* cta_first) {
+  extern __shared__ double sm[];
+  const int b = cta_block[blockIdx.x];
+  const int k0 = cta_first[blockIdx.x];
+  const int n = A.bsize[b];
+  const int nv = A.nvec[b];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = k0 + warp;
+  const bool active = k < nv;
+  double* vbuf = sm;                       // n
+  double* y = sm + A.maxn * (1 + warp);    // n per warp
+  const double* Yb = A.Y + A.yoff[b];
+  if (active)
+    for (int i = lane; i < n; i += 32) y[i] = Yb[(int64_t)i * nv + k];
+  const double* H = A.H_const;
+  const double* tau = A.tau + A.soff[b];
+  for (int j = n - 3; j >= 0; --j) {
+    __syncthreads();
+    const double* vrow = H + A.hoff[b] + (int64_t)j * n;
+    for (int c = j + 1 + threadIdx.x; c < n; c += blockDim.x) vbuf[c] = vrow[c];
+    __syncthreads();
+    const double t = tau[j];
+    if (!active || t == 0.0) continue;
+    double dot = 0.0;
+    for (int c = j + 1 + lane; c < n; c += 32) dot = fma(vbuf[c], y[c], dot);
+    for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+    const double s = t * dot;
+    for (int c = j + 1 + lane; c < n; c += 32) y[c] = fma(-s, vbuf[c], y[c]);
+  }
+  if (!active) return;
+  double* Zb = A.Z + A.zoff[b] + (int64_t)k * n;
+  for (int i = lane; i < n; i += 32) Zb[i] = y[i];
+  if (A.Zt) {
+    double* Ztb = A.Zt + A.zoff[b];
+    for (int i = lane; i < n; i += 32) Ztb[(int64_t)i * nv + k] = y[i];
+  }
+}
+
+}  // namespace
+
+void launch_bisect(const TdEigArgs& a, const int* state_block, cudaStream_t s) {
+  if (a.nstates <= 0) return;
+  bisect_kernel<<<(a.nstates + 127) / 128, 128, 0, s>>>(a, state_block);
+}
+
+void launch_inviter(const InvIterArgs& a, const int* vec_block, const int* vec_index, int nvecs, cudaStream_t s) {
+  if (nvecs > 0) inviter_kernel<<<(nvecs + 63) / 64, 64, 0, s>>>(a, vec_block, vec_index, nvecs);
+  if (a.nclusters > 0) mgs_kernel<<<(a.nclusters * 32 + 127) / 128, 128, 0, s>>>(a);
+}
+
+int backtransform_warps(int maxn) {
+  int w = (int)((220 * 1024) / (sizeof(double) * (size_t)maxn)) - 1;
+  return w < 1 ? 1 : (w > kBackWarps ? kBackWarps : w);
+}
+size_t backtransform_smem_bytes(int maxn) { return sizeof(double) * (size_t)maxn * (1 + backtransform_warps(maxn)); }
+
+cudaError_t launch_backtransform(const BackArgs& a, const int* cta_block, const int* cta_first, int nctas,
+                                 cudaStream_t s) {
+  if (nctas <= 0) return cudaSuccess;
+  size_t smem = backtransform_smem_bytes(a.maxn);
+  cudaError_t err = cudaFuncSetAttribute(backtransform_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  backtransform_kernel<<<nctas, backtransform_warps(a.maxn) * 32, smem, s>>>(a, cta_block, cta_first);
+  return cudaGetLastError();
+}
+
+}  // namespace nrg

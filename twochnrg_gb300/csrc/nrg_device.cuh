@@ -1,0 +1,209 @@
+// Device-side declarations shared by the GB300 NRG kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nrg {
+
+// Error flags a kernel can raise without trapping; the host reads the word
+// after the launch series and turns it into an nrg_status.
+enum DeviceFlag : int {
+  DEV_OK = 0,
+  DEV_SIZE = 1,           // a block exceeded a compiled / shared-memory limit
+  DEV_NOT_CONVERGED = 2,  // inverse iteration did not converge
+  DEV_BAD_INPUT = 4,      // NaN / Inf met in an input
+  DEV_DEGEN_OVERFLOW = 8  // too many near-zero levels for the SetDegen pass
+};
+
+// ---------------------------------------------------------------- assembly
+// One H_N block (dense n x n row-major at hoff) per new (Q,S)/(Q,Sz) sector.
+struct AssembleArgs {
+  int nblocks;
+  const int* bsize;          // [nblocks]
+  const int* bstate;         // [nblocks] first global state of the block
+  const int64_t* hoff;       // [nblocks] offset of the block in H
+  const int* seg_nseg;       // [nblocks] segments in the block
+  // per global state
+  const int* st_seg;         // local segment index
+  const int* st_a;           // old state inside the old block
+  const int* st_type;        // site type
+  const double* st_eold;     // energy of the old state it came from
+  // per (block, p, q, old operator): old-operator block for the pair of old
+  // blocks of segments p and q, forward (p,q) and backward (q,p)
+  const int64_t* pair_base;  // [nblocks] offset of the block's pair table
+  const int64_t* pair_fwd;   // element offset or -1
+  const int* pair_fwd_ld;    // columns of the forward block
+  const int64_t* pair_bwd;
+  const int* pair_bwd_ld;
+  // coefficient tables (see nrg_model.h HNTables)
+  const double* coef;        // [nblocks * per_block]
+  int ntypes, nchan, nsigma;
+  int nops_h;                // old operators entering H_N (pair-table stride)
+  int model;                 // ModelKind
+  const double* const* ops;  // [nops_h] old operator element arrays
+  double sqrt_lambda, eN;
+  double chi[2];
+  const double* site_q;      // [ntypes] site charge Q~ of each type
+  double* H;
+};
+void launch_assemble(const AssembleArgs& a, int64_t total_rows, const int* row_block,
+                     const int* row_index, cudaStream_t s);
+
+// ---------------------------------------------------------------- eigensolver
+struct TridiagArgs {
+  int nblocks;
+  const int* order;      // processing order (largest first)
+  const int* bsize;
+  const int64_t* hoff;   // matrix offsets; on exit row j holds v_j in cols j+1..n-1
+  const int* soff;       // state offsets for d/e/tau
+  double* H;
+  double* d;
+  double* e;
+  double* tau;
+  int* queue;            // work counter (reset to 0 before launch)
+  int* flag;
+  int maxn;
+};
+cudaError_t launch_tridiag(const TridiagArgs& a, int cluster, int nclusters, cudaStream_t s);
+size_t tridiag_smem_bytes(int maxn);
+int tridiag_max_clusters(int cluster, int maxn);
+// Whole-GPU cooperative variant for the largest blocks (processed in turn).
+int tridiag_grid_size(int maxn);
+cudaError_t launch_tridiag_grid(const TridiagArgs& a, const int* big, int nbig, double* part, double* pvec,
+                                double* dots, int grid, cudaStream_t s);
+
+struct TdEigArgs {
+  int nblocks;
+  const int* bsize;
+  const int* soff;       // state offset of each block
+  const double* d;
+  const double* e;
+  double* ev;            // [nstates] ascending per block
+  int nstates;
+  int* flag;
+};
+void launch_bisect(const TdEigArgs& a, const int* state_block, cudaStream_t s);
+
+struct InvIterArgs {
+  int nblocks;
+  const int* bsize;
+  const int* soff;
+  const double* d;
+  const double* e;
+  const double* ev;       // eigenvalues of T
+  const int* nvec;        // [nblocks] eigenvectors wanted (lowest ones)
+  const int64_t* yoff;    // [nblocks] offset of the block's Y (n x nvec, row-major)
+  double* Y;              // eigenvectors of T: Y[yoff + i*nvec + k]
+  double* scratch;        // 5 interleaved n x nvec arrays per block at 5*yoff
+  const int* cl_block;    // per cluster of close eigenvalues: block
+  const int* cl_first;    // first eigenvalue index in block
+  const int* cl_count;    // eigenvalues in the cluster
+  int nclusters;
+  int* flag;
+};
+void launch_inviter(const InvIterArgs& a, const int* vec_block, const int* vec_index, int nvecs,
+                    cudaStream_t s);
+
+struct BackArgs {
+  const int* bsize;
+  const int64_t* hoff;    // Householder vectors in rows of H
+  const double* H_const;
+  const int* soff;        // tau offsets
+  const double* tau;
+  const int* nvec;
+  const int64_t* yoff;
+  const double* Y;        // eigenvectors of T (n x nvec, interleaved)
+  double* Z;              // row k = eigenvector k (nvec x n) at zoff
+  double* Zt;             // transposed (n x nvec) at zoff, may be null
+  const int64_t* zoff;
+  int maxn;
+};
+cudaError_t launch_backtransform(const BackArgs& a, const int* cta_block, const int* cta_first, int nctas,
+                                 cudaStream_t s);
+size_t backtransform_smem_bytes(int maxn);
+int backtransform_warps(int maxn);  // eigenvectors per CTA
+
+// ---------------------------------------------------------------- cut
+struct CutArgs {
+  int nstates;
+  const double* ev;      // raw eigenvalues (left untouched)
+  double* en;            // out: shifted + SetDegen-merged energies
+  int ncutoff;
+  double eps;            // SetDegen tolerance
+  double* out_scalars;   // [0]=emin [1]=ecut [2]=nkept
+  int* flag;
+};
+void launch_cut(const CutArgs& a, cudaStream_t s);
+
+struct BlockStatsArgs {   // per block: kept count (leading run <= ecut) or 0 if removed
+  int nblocks;
+  const int* bsize;
+  const int* soff;
+  const double* en;
+  const double* scalars;  // ecut in [1]
+  int* kept;
+};
+void launch_block_stats(const BlockStatsArgs& a, cudaStream_t s);
+
+struct ThermoArgs {
+  const double* bq;       // [nblocks*2] block quantum numbers
+  const double* en;
+  int totalS;
+  double beta[4];
+  double* out;            // [4*3]: per beta  Z, sum SzSq e^{-bE}, sum deg E e^{-bE}
+};
+void launch_thermo(const ThermoArgs& a, const int* state_block, int n, double* partial, cudaStream_t s);
+
+// ---------------------------------------------------------------- update
+struct GatherTerm {       // T[dst rows] += coef * M . Zt[src rows]
+  int job;                // rotation job
+  int dst_base, dst_stride, rows;   // rows of T (local to the job's T)
+  int src_base, src_stride, srows;  // rows of Zt_J (local to block J)
+  int mode;               // 0: identity (srows == rows); 1: old block (rows x srows)
+  double coef;
+  int64_t old_off;        // element offset of the old block (mode 1)
+  int op;                 // old operator index (mode 1)
+};
+struct RotJob {           // O (ki x kj) = Z_I (ki x nI) . T (nI x kj)
+  int ki, kj, nI;
+  int64_t z_off;          // Z_I (row-major ki x nI)
+  int64_t zt_off;         // Zt_J (row-major nJ x kj)
+  int64_t t_off;          // T scratch (nI x kj)
+  int64_t o_off;          // output in the new operator's element array
+  int op;                 // operator index
+};
+struct UpdateArgs {
+  const GatherTerm* terms;
+  const int* group_first; // terms grouped by destination rows
+  const int* group_count;
+  int ngroups;
+  const RotJob* jobs;
+  const double* Z;
+  const double* Zt;
+  double* T;
+  const double* const* old_ops;
+  double* const* new_ops;
+  const int* tile_job;    // GEMM tiles: job
+  const int* tile_mn;     // GEMM tiles: (mtile << 16) | ntile
+  int ntiles;
+};
+void launch_update(const UpdateArgs& a, cudaStream_t s);
+
+struct OpDiagArgs {       // Boltzmann sums of diagonal elements over kept states
+  int nblocks;
+  const int* ksize;       // kept states per block
+  const int* koff;        // kept state offsets
+  const double* ken;      // kept energies
+  const double* bq;
+  int totalS;
+  double beta;
+  int nops;
+  const double* const* ops;
+  const int64_t* diag_off; // [nops*nblocks] element offset of diagonal block, -1 if none
+  double* out;            // [nops+1]: sums, last = Z
+};
+void launch_opdiag(const OpDiagArgs& a, const int* kstate_block, int nk, double* partial, cudaStream_t s);
+int reduce_partial_count();
+
+}  // namespace nrg

@@ -1,0 +1,451 @@
+// Host-side model tables of the GB300 NRG engine (see nrg_model.h).
+#include "nrg_model.h"
+
+#include <algorithm>
+#include <cmath>
+#include <stdexcept>
+
+namespace nrg {
+
+namespace {
+// dEqual.cpp:6 and :17.
+inline bool deq(double a, double b) { return std::fabs(a - b) < 1.e-20; }
+inline bool dleq(double a, double b) { return (a < b) || (std::fabs(a - b) < 1.e-20); }
+
+double factorial(int n) {
+  if (n < 0) return 0.0;
+  unsigned __int128 p = 1;
+  for (int k = 2; k <= n; ++k) p *= (unsigned)k;
+  return (double)p;  // n! rounded once, as a table of factorials holds it
+}
+
+// CGordan.cpp:13.
+bool triangle(double J1, double J2, double J) {
+  return !((J - (J1 + J2) > 1.0e-10) || (J - std::fabs(J1 - J2) < -1.0e-10));
+}
+
+// Single-site operator tables.  OneCh_fd_table (OpTables.cpp:8-33) gives
+// <t_i| f^dagger_sigma |t_j> in the basis |0>,|up>,|dn>,|up dn>.
+double fd_onech(int sigma, int ti, int tj) {
+  if (sigma == 1) return ((ti == 1 && tj == 0) || (ti == 3 && tj == 2)) ? 1.0 : 0.0;
+  if (sigma == -1) { if (ti == 2 && tj == 0) return 1.0; if (ti == 3 && tj == 1) return -1.0; }
+  return 0.0;
+}
+
+// TwoChQS_fd_table (TwoChQS_OpTables.cpp:20-130): the reference's table of
+// f^dagger_{ch,sigma} in the 16-state two-channel site basis.
+struct TwoChTables {
+  double fd[2][2][16][16];  // [ch-1][sigma==+1][ti][tj]
+  double spsm[16][16];      // TwoChQS_SpSm_table (:140-185)
+  TwoChTables() {
+    for (auto& a : fd) for (auto& b : a) for (auto& c : b) for (double& x : c) x = 0.0;
+    const double r = 1.0 / std::sqrt(2.0), mr = -1.0 / std::sqrt(2.0);
+    auto& u1 = fd[0][1]; auto& d1 = fd[0][0]; auto& u2 = fd[1][1]; auto& d2 = fd[1][0];
+    u1[2][0] = 1; u1[10][1] = 1; u1[9][3] = r; u1[11][6] = 1; u1[5][3] = r;
+    u1[7][4] = 1; u1[12][9] = r; u1[12][5] = mr; u1[14][8] = 1; u1[15][13] = 1;
+    d1[4][0] = 1; d1[9][1] = r; d1[5][1] = mr; d1[8][3] = 1; d1[13][6] = 1;
+    d1[7][2] = -1; d1[12][10] = -1; d1[14][9] = mr; d1[14][5] = mr; d1[15][11] = -1;
+    u2[1][0] = 1; u2[6][3] = 1; u2[10][2] = -1; u2[11][9] = mr; u2[11][5] = mr;
+    u2[9][4] = mr; u2[5][4] = r; u2[13][8] = -1; u2[12][7] = 1; u2[15][14] = 1;
+    d2[3][0] = 1; d2[6][1] = -1; d2[9][2] = mr; d2[11][10] = 1; d2[5][2] = mr;
+    d2[8][4] = -1; d2[13][9] = r; d2[13][5] = mr; d2[14][7] = 1; d2[15][12] = -1;
+    for (int i = 0; i < 16; ++i) for (int j = 0; j < 16; ++j) spsm[i][j] = (i == j) ? 1.0 : 0.0;
+    const int pairs[][2] = {{1, 3}, {2, 4}, {11, 13}, {12, 14}, {8, 9}, {9, 10}, {8, 10}};
+    for (auto& p : pairs) { spsm[p[0]][p[1]] = 1.0; spsm[p[1]][p[0]] = 1.0; }
+  }
+  double f(int ch, int sigma, int ti, int tj) const {
+    if (ti < 0 || tj < 0 || ti > 15 || tj > 15 || (ch != 1 && ch != 2) || (sigma != 1 && sigma != -1)) return 0.0;
+    return fd[ch - 1][sigma == 1][ti][tj];
+  }
+};
+const TwoChTables& twoch() { static TwoChTables t; return t; }
+
+void site_block(Site& s, std::initializer_list<double> q, int n) {
+  std::vector<double> v(q);
+  s.blk.push(v.data(), n);
+  s.nstates += n;
+}
+}  // namespace
+
+double clebsch(double J1, double M1, double J2, double M2, double J, double M) {
+  if ((J1 < 0.0) || (J2 < 0.0) || (J < 0.0)) return 0.0;
+  if ((std::fabs(M1) > J1) || (std::fabs(M2) > J2) || (std::fabs(M) > J)) return 0.0;
+  if (std::fabs(M - (M1 + M2)) > 1.0e-10) return 0.0;
+  if ((J > (J1 + J2)) || (J < std::fabs(J1 - J2))) return 0.0;
+  double a = factorial((int)(J1 + J2 - J)) * factorial((int)(J1 - J2 + J)) * factorial((int)(-J1 + J2 + J)) *
+             (2 * J + 1) / factorial((int)(J1 + J2 + J + 1));
+  double rho = a > 0.0 ? std::sqrt(a) : 0.0;
+  double s = factorial((int)(J + M)) * factorial((int)(J - M)) * factorial((int)(J1 + M1)) *
+             factorial((int)(J1 - M1)) * factorial((int)(J2 + M2)) * factorial((int)(J2 - M2));
+  double sigma = s > 0.0 ? std::sqrt(s) : 0.0;
+  int rmax = std::min(std::min((int)(J1 - M1), (int)(J2 + M2)), (int)(J1 + J2 - J));
+  int rmin = std::max(std::max(-(int)(J - J2 + M1), -(int)(J - J1 - M2)), 0);
+  double tau = 0.0;
+  for (int r = rmin; r <= rmax; r++) {
+    double d = factorial((int)(J1 - M1) - r) * factorial((int)(J2 + M2) - r) * factorial((int)(J - J2 + M1) + r) *
+               factorial((int)(J - J1 - M2) + r) * factorial((int)(J1 + J2 - J) - r) * factorial(r);
+    tau += std::pow(-1.0, r) * (1.0 / d);
+  }
+  return rho * sigma * tau;
+}
+
+namespace {
+// Memoised Clebsch-Gordan: pure function of six half-integers.
+double cg(double a, double b, double c, double d, double e, double f) {
+  static std::map<std::array<double, 6>, double> memo;
+  std::array<double, 6> k{a, b, c, d, e, f};
+  auto it = memo.find(k);
+  if (it != memo.end()) return it->second;
+  double v = clebsch(a, b, c, d, e, f);
+  memo.emplace(k, v);
+  return v;
+}
+}  // namespace
+
+void BlockArray::push(const double* q, int n) {
+  for (int k = 0; k < nqn; ++k) qn.push_back(q[k]);
+  offset.push_back(nstates());
+  size.push_back(n);
+}
+
+int BlockArray::find(const double* q) const {
+  for (int b = 0; b < nblocks(); ++b) {
+    bool ok = true;
+    for (int k = 0; k < nqn && ok; ++k) ok = deq(qn[(size_t)b * nqn + k], q[k]);
+    if (ok) return b;
+  }
+  return -1;
+}
+
+int Site::block_of_state(int t) const {
+  for (int b = 0; b < blk.nblocks(); ++b)
+    if (t >= blk.offset[b] && t < blk.offset[b] + blk.size[b]) return b;
+  return -1;
+}
+
+int OpBlocks::find(int i, int j) const {
+  for (size_t k = 0; k < bi.size(); ++k)
+    if (bi[k] == i && bj[k] == j) return (int)k;
+  return -1;
+}
+
+ModelSpec make_model(ModelKind kind) {
+  ModelSpec m;
+  m.kind = kind;
+  if (kind == MODEL_1CHQS) {
+    // OneChQS_SetSingleSite (OneChQS_SetSingleSite.cpp:5-44): (Q,S,Sz), one state per block.
+    m.site.blk.nqn = 3;
+    site_block(m.site, {-1, 0, 0}, 1); site_block(m.site, {0, 0.5, 0.5}, 1);
+    site_block(m.site, {0, 0.5, -0.5}, 1); site_block(m.site, {1, 0, 0}, 1);
+    m.totalS = true; m.nchan = 1; m.nsigma = 1;
+    m.op_kind = {OP_F_QS, OP_IMPONLY, OP_IMPONLY, OP_IMPONLY};
+    m.op_check = {CHK_QS_CD, CHK_DIAG, CHK_DIAG, CHK_DIAG};
+    m.op_name = {"fN", "Ndot", "NdSq", "SdSq"};
+  } else if (kind == MODEL_1CHQSZ) {
+    // OneChQSz_SetSingleSite (Main/Main_SetSingleSite.cpp:347-380).
+    m.site.blk.nqn = 2;
+    site_block(m.site, {-1, 0}, 1); site_block(m.site, {0, 0.5}, 1);
+    site_block(m.site, {0, -0.5}, 1); site_block(m.site, {1, 0}, 1);
+    m.totalS = false; m.nchan = 1; m.nsigma = 2;
+    m.op_kind = {OP_FUP_QSZ, OP_FDN_QSZ, OP_IMPONLY, OP_IMPONLY};
+    m.op_check = {CHK_Q_CD, CHK_Q_CD, CHK_DIAG, CHK_DIAG};
+    m.op_name = {"fNup", "fNdn", "Ndot", "Szdot"};
+  } else if (kind == MODEL_2CHQS) {
+    // TwoChQS_SetSingleSite (TwoChQS_SetSingleSite.cpp:5-124): 16 states in 10 blocks.
+    m.site.blk.nqn = 3;
+    site_block(m.site, {-2, 0, 0}, 1); site_block(m.site, {-1, 0.5, 0.5}, 2);
+    site_block(m.site, {-1, 0.5, -0.5}, 2); site_block(m.site, {0, 0, 0}, 3);
+    site_block(m.site, {0, 1, -1}, 1); site_block(m.site, {0, 1, 0}, 1);
+    site_block(m.site, {0, 1, 1}, 1); site_block(m.site, {1, 0.5, 0.5}, 2);
+    site_block(m.site, {1, 0.5, -0.5}, 2); site_block(m.site, {2, 0, 0}, 1);
+    m.totalS = true; m.nchan = 2; m.nsigma = 2;
+    m.op_kind = {OP_F1_2CH, OP_F2_2CH, OP_IMPONLY, OP_IMPONLY, OP_IMPONLY};
+    m.op_check = {CHK_2CH_CD, CHK_2CH_CD, CHK_DIAG, CHK_DIAG, CHK_DIAG};
+    m.op_name = {"fNch1", "fNch2", "Ndot", "NdSq", "SdSq"};
+  } else {
+    throw std::runtime_error("unknown model");
+  }
+  for (int k : m.op_kind) m.op_avg.push_back(k == OP_IMPONLY ? 1 : 0);
+  return m;
+}
+
+namespace {
+void diag_op(const BlockArray& a, const std::vector<double>& v, OpBlocks& o) {
+  for (int b = 0; b < a.nblocks(); ++b) {
+    o.bi.push_back(b); o.bj.push_back(b); o.off.push_back((int64_t)o.el.size()); o.el.push_back(v[b]);
+  }
+}
+void single(OpBlocks& o, int i, int j, double v) {
+  o.bi.push_back(i); o.bj.push_back(j); o.off.push_back((int64_t)o.el.size()); o.el.push_back(v);
+}
+}  // namespace
+
+StartState make_start(const ModelSpec& m, double lambda, double U, double ed, double B) {
+  StartState s;
+  double HLF = 0.5 * (1.0 + 1.0 / lambda);
+  double scale = lambda * HLF;
+  s.blk.nqn = 2;
+  if (m.kind == MODEL_1CHQS || m.kind == MODEL_2CHQS) {
+    // OneChQS_SetAnderson_Hm1 (Main/Main_SetH0.cpp:1794-1969): the impurity
+    // multiplets |0>, |sigma>, |up dn> in units of Lambda*HLF, reduced
+    // <||d||> = (1, -sqrt 2), and n_d, n_d^2, S^2 on the diagonal.
+    const double q[3][2] = {{-1, 0}, {0, 0.5}, {1, 0}};
+    for (auto& x : q) s.blk.push(x, 1);
+    s.en = {0.5 * U / scale, (ed + 0.5 * U) / scale, (2.0 * ed + 1.5 * U) / scale};
+    OpBlocks f;
+    single(f, 0, 1, 1.0);
+    single(f, 1, 2, -std::sqrt(2.0));
+    std::vector<double> nd, nd2, s2;
+    for (int b = 0; b < 3; ++b) {
+      double n = s.blk.q(b, 0) + 1.0, S = s.blk.q(b, 1);
+      nd.push_back(n); nd2.push_back(n * n); s2.push_back(S * (S + 1.0));
+    }
+    OpBlocks o1, o2, o3;
+    diag_op(s.blk, nd, o1); diag_op(s.blk, nd2, o2); diag_op(s.blk, s2, o3);
+    s.ops.push_back(f);
+    if (m.kind == MODEL_2CHQS) s.ops.push_back(f);  // f_ch1 = f_ch2 = d
+    s.ops.push_back(o1); s.ops.push_back(o2); s.ops.push_back(o3);
+  } else {
+    // OneChQSz_SetAnderson_Hm1 (Main/Main_SetH0.cpp:421-660) with the Zeeman
+    // term -hz S_z, hz = B/2.
+    double hz = 0.5 * B;
+    const double q[4][2] = {{-1, 0}, {0, 0.5}, {0, -0.5}, {1, 0}};
+    for (auto& x : q) s.blk.push(x, 1);
+    s.en = {0.5 * U / scale, (ed + 0.5 * U - hz) / scale, (ed + 0.5 * U + hz) / scale, (2.0 * ed + 1.5 * U) / scale};
+    OpBlocks fu, fd, nd, sz;
+    single(fu, 0, 1, 1.0); single(fu, 2, 3, 1.0);
+    single(fd, 0, 2, 1.0); single(fd, 1, 3, -1.0);
+    std::vector<double> vn, vs;
+    for (int b = 0; b < 4; ++b) { vn.push_back(s.blk.q(b, 0) + 1.0); vs.push_back(s.blk.q(b, 1)); }
+    diag_op(s.blk, vn, nd); diag_op(s.blk, vs, sz);
+    s.ops = {fu, fd, nd, sz};
+  }
+  return s;
+}
+
+void build_basis(const ModelSpec& m, const BlockArray& kept, Basis& out) {
+  // BuildBasis (BuildBasis.cpp:8-432) with CommonQNs = {2, 0,1, 0,1} and,
+  // for SU(2) models, totSpos = {1}.
+  const BlockArray& ss = m.site.blk;
+  out = Basis();
+  out.blk.nqn = 2;
+  std::vector<double> cand;
+  for (int b = 0; b < kept.nblocks(); ++b) {
+    double Qo = kept.q(b, 0), So = kept.q(b, 1);
+    for (int s = 0; s < ss.nblocks(); ++s) {
+      double Qs = ss.q(s, 0), Ss = ss.q(s, 1);
+      cand.push_back(Qs + Qo); cand.push_back(Ss + So);
+      if (m.totalS) {
+        for (double Sn = So + Ss - 1.0; Sn >= std::fabs(So - Ss); Sn -= 1.0) {
+          cand.push_back(Qs + Qo); cand.push_back(Sn);
+        }
+      }
+    }
+  }
+  // FilterQNumbers (NRGarrayClass.cpp:271-309): keep first occurrences.
+  std::vector<double> qn;
+  for (size_t k = 0; k < cand.size(); k += 2) {
+    bool dup = false;
+    for (size_t j = 0; j < qn.size() && !dup; j += 2) dup = (qn[j] == cand[k] && qn[j + 1] == cand[k + 1]);
+    if (!dup) { qn.push_back(cand[k]); qn.push_back(cand[k + 1]); }
+  }
+  int nb = (int)qn.size() / 2;
+  out.seg.resize(nb);
+  for (int b = 0; b < nb; ++b) {
+    double Qn = qn[2 * b], Sn = qn[2 * b + 1];
+    int local = 0;
+    for (int bo = 0; bo < kept.nblocks(); ++bo) {
+      double Qo = kept.q(bo, 0), So = kept.q(bo, 1);
+      for (int s = 0; s < ss.nblocks(); ++s) {
+        bool ok = deq(Qn, ss.q(s, 0) + Qo);
+        if (m.totalS) ok = ok && deq(Sn, ss.q(s, 2) + So) && triangle(So, ss.q(s, 1), Sn);
+        else ok = ok && deq(Sn, ss.q(s, 1) + So);
+        if (!ok) continue;
+        Segment g{bo, s, local, kept.size[bo], ss.size[s]};
+        int sidx = (int)out.seg[b].size();
+        out.seg[b].push_back(g);
+        for (int a = 0; a < g.count; ++a)
+          for (int u = 0; u < g.nsite; ++u) {
+            out.itype.push_back(ss.offset[s] + u);
+            out.stcf.push_back(kept.offset[bo] + a);
+            out.seg_of.push_back(sidx);
+            out.a_of.push_back(a);
+          }
+        local += g.count * g.nsite;
+      }
+    }
+    out.blk.push(&qn[2 * b], local);
+  }
+}
+
+namespace {
+// Coefficient of OneChQS_HN_MatEl (OpMatRules.cpp:1473-1523) for the site
+// pair (typep, type) in a new multiplet of spin Si, times the fermion sign.
+double hn_coef_1chQS(const Site& st, double Si, int typep, int type) {
+  const BlockArray& ss = st.blk;
+  double Qtp = ss.q(typep, 0), Stp = ss.q(typep, 1), Sztp = ss.q(typep, 2);
+  double Qt = ss.q(type, 0), Stt = ss.q(type, 1), Szt = ss.q(type, 2);
+  double Scfp = Si - Sztp, Scf = Si - Szt;
+  double fermi = deq(Qt, 0.0) ? -1.0 : 1.0;
+  double coef = 0.0;
+  double qp[3] = {Qtp, Stp, Sztp}, qq[3] = {Qt, Stt, Szt};
+  for (double Sz = -Stt; Sz <= Stt; Sz += 1.0) {
+    qq[2] = Sz;
+    int sst = ss.find(qq);
+    for (int sigma = -1; sigma <= 1; sigma += 2) {
+      double dS = 0.5 * (double)sigma;
+      double Szcf = Si - Sz, Szcfp = Szcf - dS, Szp = Sz + dS;
+      qp[2] = Sz + dS;
+      int sstp = ss.find(qp);
+      double a0 = cg(Scf, Szcf, Stt, Sz, Si, Si);
+      double a1 = cg(Scfp, Szcfp, Stp, Szp, Si, Si);
+      double a2 = cg(Scfp, Szcfp, 0.5, dS, Scf, Szcf);
+      double a3 = fd_onech(sigma, sstp, sst);
+      coef += a0 * a1 * a2 * a3;
+    }
+  }
+  return coef * fermi;  // fermi = +-1: multiplying first or last is exact
+}
+
+// Per-(channel, sigma) sum FullMatEl of TwoChQS_HN_MatEl
+// (TwoChQS_OpMatRules.cpp:843-957) for the site pair (typep, type).
+double hn_full_2chQS(const Site& st, double Si, int typep, int type, int ich, int sigma) {
+  const BlockArray& ss = st.blk;
+  const TwoChTables& T = twoch();
+  int bp = st.block_of_state(typep), b = st.block_of_state(type);
+  double Stp = ss.q(bp, 1), Sztp = ss.q(bp, 2), Stt = ss.q(b, 1), Szt = ss.q(b, 2);
+  double Soldp = Si - Sztp, Sold = Si - Szt;
+  double fermi = (deq(Szt, 0.5) || deq(Szt, -0.5)) ? -1.0 : 1.0;
+  double qp[3] = {ss.q(bp, 0), ss.q(bp, 1), ss.q(bp, 2)}, qq[3] = {ss.q(b, 0), ss.q(b, 1), ss.q(b, 2)};
+  double dS = 0.5 * (double)sigma;
+  double full = 0.0;
+  for (double Szold = Sold; Szold >= -Sold; Szold -= 1.0) {
+    double Szoldp = Szold - dS, Sz = Si - Szold, Szp = Sz + dS;
+    qp[2] = Szp; qq[2] = Sz;
+    int sbp = ss.find(qp), sb = ss.find(qq);
+    if (!(dleq(std::fabs(Szp), Stp) && dleq(std::fabs(Szold), Sold) && dleq(std::fabs(Szoldp), Soldp))) continue;
+    double a0 = cg(Sold, Szold, Stt, Sz, Si, Si);
+    double a1 = cg(Soldp, Szoldp, Stp, Szp, Si, Si);
+    double a2 = cg(Soldp, Szoldp, 0.5, dS, Sold, Szold);
+    // GetBlockLimit of a missing block (-1) is state 0 (NRGarrayClass.cpp:335).
+    int p0 = sbp < 0 ? 0 : ss.offset[sbp], p1 = sbp < 0 ? 0 : ss.offset[sbp] + ss.size[sbp] - 1;
+    int s0 = sb < 0 ? 0 : ss.offset[sb], s1 = sb < 0 ? 0 : ss.offset[sb] + ss.size[sb] - 1;
+    for (int sp = p0; sp <= p1; sp++)
+      for (int s = s0; s <= s1; s++) {
+        double x0 = T.spsm[s][type], x1 = T.spsm[sp][typep];
+        double a3 = T.f(ich, sigma, sp, s);
+        full += a0 * a1 * a2 * a3 * fermi * x0 * x1;
+      }
+  }
+  return full;
+}
+}  // namespace
+
+void build_hn_tables(const ModelSpec& m, const Basis& b, HNTables& t) {
+  int NT = m.site.nstates;
+  t.ntypes = NT; t.nchan = m.nchan; t.nsigma = m.nsigma;
+  size_t pb = t.per_block();
+  t.coef.assign(pb * b.blk.nblocks(), 0.0);
+  std::map<double, size_t> done;  // tables depend on the block's S (or Sz) only
+  for (int blk = 0; blk < b.blk.nblocks(); ++blk) {
+    double Si = b.blk.q(blk, 1);
+    double* c = &t.coef[pb * blk];
+    auto it = done.find(Si);
+    if (it != done.end()) { std::copy(t.coef.begin() + it->second, t.coef.begin() + it->second + pb, c); continue; }
+    done.emplace(Si, pb * blk);
+    for (int ti = 0; ti < NT; ++ti)
+      for (int tj = 0; tj < NT; ++tj) {
+        size_t base = ((size_t)ti * NT + tj) * t.nchan * t.nsigma;
+        if (m.kind == MODEL_1CHQS) {
+          c[base * 2 + 0] = hn_coef_1chQS(m.site, Si, ti, tj);
+          c[base * 2 + 1] = hn_coef_1chQS(m.site, Si, tj, ti);
+        } else if (m.kind == MODEL_1CHQSZ) {
+          // OneChQSz_HN_MatEl (OpMatRules.cpp:468-531): per spin, the fermion
+          // sign of the "type" state times <typep|f^dagger_sigma|type>.
+          for (int s = 0; s < 2; ++s) {
+            int isigma = s == 0 ? 1 : -1;
+            double fq = deq(m.site.blk.q(tj, 0), 0.0) ? -1.0 : 1.0;
+            double bq = deq(m.site.blk.q(ti, 0), 0.0) ? -1.0 : 1.0;
+            c[(base + s) * 2 + 0] = fq * fd_onech(isigma, ti, tj);
+            c[(base + s) * 2 + 1] = bq * fd_onech(isigma, tj, ti);
+          }
+        } else {
+          for (int ch = 0; ch < 2; ++ch)
+            for (int s = 0; s < 2; ++s) {
+              int sigma = s == 0 ? -1 : 1;
+              size_t k = base + (size_t)ch * 2 + s;
+              c[k * 2 + 0] = hn_full_2chQS(m.site, Si, ti, tj, ch + 1, sigma);
+              c[k * 2 + 1] = hn_full_2chQS(m.site, Si, tj, ti, ch + 1, sigma);
+            }
+        }
+      }
+  }
+}
+
+double op_site_factor(const ModelSpec& m, int op, double Si, double Sj, int ti, int tj) {
+  const BlockArray& ss = m.site.blk;
+  if (op == OP_FUP_QSZ) return fd_onech(1, tj, ti);   // OneChQ_fN_MatEl (OpMatRules.cpp:1003-1033)
+  if (op == OP_FDN_QSZ) return fd_onech(-1, tj, ti);
+  if (op == OP_IMPONLY) return ti == tj ? 1.0 : 0.0;
+  if (op == OP_F_QS) {
+    // OneChQS_fN_MatEl (OpMatRules.cpp:1167-1244).
+    double qi[3] = {ss.q(ti, 0), ss.q(ti, 1), ss.q(ti, 2)}, qj[3] = {ss.q(tj, 0), ss.q(tj, 1), ss.q(tj, 2)};
+    double Sti = qi[1], Szti = qi[2], Stj = qj[1], Sztj = qj[2];
+    double Scfi = Si - Szti, Scfj = Sj - Sztj;
+    double acc = 0.0, c1 = 0.0;
+    double sigma = Sj - Si;
+    for (double Sz = -Stj; Sz <= Stj; Sz += 1.0) {
+      qj[2] = Sz; int sj = ss.find(qj);
+      qi[2] = Sz - sigma; int si = ss.find(qi);
+      double c0 = cg(Scfi, Si - Sz + sigma, Sti, Sz - sigma, Si, Si);
+      c1 = cg(Scfj, Sj - Sz, Stj, Sz, Sj, Sj);
+      acc += fd_onech((int)(sigma / 0.5), sj, si) * c0 * c1;
+    }
+    double n0 = cg(Si, Si, 0.5, sigma, Sj, Sj);
+    if (!deq(n0, 0.0)) return acc / n0;
+    return 0.0;
+  }
+  if (op == OP_F1_2CH || op == OP_F2_2CH) {
+    // TwoChQS_fN_MatEl (TwoChQS_OpMatRules.cpp:1205-1352).
+    int ich = op == OP_F1_2CH ? 1 : 2;
+    const TwoChTables& T = twoch();
+    int bi = m.site.block_of_state(ti), bj = m.site.block_of_state(tj);
+    double qi[3] = {ss.q(bi, 0), ss.q(bi, 1), ss.q(bi, 2)}, qj[3] = {ss.q(bj, 0), ss.q(bj, 1), ss.q(bj, 2)};
+    double Scfi = Si - qi[2], Scfj = Sj - qj[2];
+    double c0 = cg(Si, Si, 0.5, -0.5, Sj, Sj), c1 = cg(Si, Si, 0.5, 0.5, Sj, Sj);
+    int sigma = 0; double norm = 1.0;
+    if (!deq(c0, 0.0)) { sigma = -1; norm = c0; }
+    else if (!deq(c1, 0.0)) { sigma = 1; norm = c1; }
+    if (sigma == 0) return 0.0;
+    double acc = 0.0;
+    for (double Szcfj = Scfj; Szcfj >= -Scfj; Szcfj -= 1.0) {
+      double Szi = Si - Szcfj, Szj = Sj - Szcfj;
+      qi[2] = Szi; int bsi = ss.find(qi);
+      qj[2] = Szj; int bsj = ss.find(qj);
+      double a0 = cg(Scfi, Szcfj, ss.q(bi, 1), Szi, Si, Si);
+      double a1 = cg(Scfj, Szcfj, ss.q(bj, 1), Szj, Sj, Sj);
+      int i0 = bsi < 0 ? 0 : ss.offset[bsi], i1 = bsi < 0 ? 0 : ss.offset[bsi] + ss.size[bsi] - 1;
+      int j0 = bsj < 0 ? 0 : ss.offset[bsj], j1 = bsj < 0 ? 0 : ss.offset[bsj] + ss.size[bsj] - 1;
+      for (int si = i0; si <= i1; si++)
+        for (int sj = j0; sj <= j1; sj++)
+          acc += T.f(ich, sigma, sj, si) * a0 * a1 * T.spsm[si][ti] * T.spsm[sj][tj];
+    }
+    return acc / norm;
+  }
+  return 0.0;
+}
+
+bool op_check(int chk, const BlockArray& a, int i, int j) {
+  // Diag_check (OpMatRules.cpp:12), OneChQS_cd_check (:106), OneChQ_cd_check
+  // (:92), TwoChQS_cd_check (TwoChQS_OpMatRules.cpp:16).
+  switch (chk) {
+    case CHK_DIAG: return i == j;
+    case CHK_Q_CD: return deq(a.q(j, 0), a.q(i, 0) + 1.0);
+    case CHK_QS_CD:
+    case CHK_2CH_CD:
+      return deq(a.q(j, 0), a.q(i, 0) + 1.0) && (deq(a.q(j, 1), a.q(i, 1) + 0.5) || deq(a.q(j, 1), a.q(i, 1) - 0.5));
+  }
+  return false;
+}
+
+}  // namespace nrg

@@ -1,0 +1,124 @@
+// Host-side model description for the GB300 NRG engine: single-site tables,
+// impurity start-up (H_{-1}), basis construction and the coefficient tables
+// that let the device assemble H_N and update operators block by block.
+//
+// The arithmetic of every coefficient follows the reference rule it cites, in
+// the same evaluation order, so that the device-assembled Hamiltonian equals
+// the reference's element by element.
+#pragma once
+
+#include <array>
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+namespace nrg {
+
+enum ModelKind { MODEL_1CHQS = 0, MODEL_1CHQSZ = 1, MODEL_2CHQS = 2 };
+
+// Operator rule ids (how the operator acts on a new site; see build_op_terms).
+enum OpKind {
+  OP_F_QS = 1,      // OneChQS_fN_MatEl      (OpMatRules.cpp:1167)
+  OP_FUP_QSZ = 2,   // OneChQ_fNup_MatEl     (OpMatRules.cpp:1037)
+  OP_FDN_QSZ = 3,   // OneChQ_fNdn_MatEl     (OpMatRules.cpp:1046)
+  OP_F1_2CH = 4,    // TwoChQS_fNch1_MatEl   (TwoChQS_OpMatRules.cpp:1355)
+  OP_F2_2CH = 5,    // TwoChQS_fNch2_MatEl   (TwoChQS_OpMatRules.cpp:1362)
+  OP_IMPONLY = 6,   // ImpOnly_MatEl x old   (OpMatRules.cpp:265)
+};
+// CheckForMatEl rule ids.
+enum CheckKind { CHK_DIAG = 1, CHK_QS_CD = 2, CHK_Q_CD = 3, CHK_2CH_CD = 4 };
+
+// Block-structured array: the common part of CNRGarray / CNRGbasisarray
+// (include/NRGclasses.hpp:47-349).
+struct BlockArray {
+  int nqn = 2;
+  std::vector<double> qn;       // nblocks * nqn
+  std::vector<int> size;        // states per block
+  std::vector<int> offset;      // first state of each block
+  int nblocks() const { return (int)size.size(); }
+  int nstates() const { return offset.empty() ? 0 : offset.back() + size.back(); }
+  double q(int b, int k) const { return qn[(size_t)b * nqn + k]; }
+  void push(const double* q, int n);
+  int find(const double* q) const;  // GetBlockFromQNumbers semantics, -1 if absent
+};
+
+// One single-site basis: blocks by (Q,S,Sz) or (Q,Sz); each state has a type.
+struct Site {
+  BlockArray blk;               // blocks of the site
+  int nstates = 0;
+  int block_of_state(int t) const;
+};
+
+// A contiguous run of new-basis states that share one old kept block and one
+// site block (BuildBasis.cpp:292-403 order: old state major, site state minor).
+struct Segment {
+  int old_block;   // index in the previous kept array
+  int site_block;  // index in Site::blk
+  int offset;      // first state inside the new block
+  int count;       // kept states of the old block
+  int nsite;       // states in the site block (stride)
+};
+
+// New basis (CNRGbasisarray after BuildBasis).
+struct Basis {
+  BlockArray blk;
+  std::vector<std::vector<Segment>> seg;  // per new block
+  // Per state, over all blocks (global state index):
+  std::vector<int> itype;     // iType
+  std::vector<int> stcf;      // StCameFrom (old kept state, global)
+  std::vector<int> seg_of;    // segment index inside its block
+  std::vector<int> a_of;      // old state index inside the old block
+};
+
+struct ModelSpec {
+  ModelKind kind;
+  Site site;
+  bool totalS;           // SU(2) multiplet basis
+  int nchan;             // Wilson channels
+  int nsigma;            // spin components summed in H_N (QSz: 2)
+  std::vector<int> op_kind, op_check;
+  std::vector<std::string> op_name;
+  std::vector<char> op_avg;  // CalcAvg operators
+};
+
+ModelSpec make_model(ModelKind kind);
+
+// Initial impurity data (H_{-1}): kept array with energies and operators in
+// dense per-block-pair form (reference MatBlockMap order).
+struct OpBlocks {
+  std::vector<int> bi, bj;         // block pairs
+  std::vector<int64_t> off;        // offset of each pair in el
+  std::vector<double> el;          // row-major blocks, concatenated
+  int find(int i, int j) const;
+};
+struct StartState {
+  BlockArray blk;
+  std::vector<double> en;
+  std::vector<OpBlocks> ops;
+};
+StartState make_start(const ModelSpec& m, double lambda, double U, double ed, double B);
+
+// BuildBasis (BuildBasis.cpp:8-432) from a kept array.
+void build_basis(const ModelSpec& m, const BlockArray& kept, Basis& out);
+
+// Coefficient tables for H_N assembly, per new block:
+//   coef[((ti*NT + tj)*nchan*nsigma + ch*nsigma + s)*2 + dir]
+// dir 0: the old operator is read as (stcf_i, stcf_j); dir 1: as (stcf_j,
+// stcf_i) after the reference's zero test.
+struct HNTables {
+  int ntypes, nchan, nsigma;
+  std::vector<double> coef;  // nblocks * ntypes^2 * nchan * nsigma * 2
+  size_t per_block() const { return (size_t)ntypes * ntypes * nchan * nsigma * 2; }
+};
+void build_hn_tables(const ModelSpec& m, const Basis& b, HNTables& t);
+
+// Site factor of an operator between two new-basis states that came from the
+// same old state (f-type operators), g(S_i, S_j, t_i, t_j).
+double op_site_factor(const ModelSpec& m, int op, double Si, double Sj, int ti, int tj);
+bool op_check(int chk, const BlockArray& kept, int i, int j);
+
+// Clebsch-Gordan <J1 M1; J2 M2 | J M>  (CGordan.cpp:34-120).
+double clebsch(double J1, double M1, double J2, double M2, double J, double M);
+
+}  // namespace nrg
