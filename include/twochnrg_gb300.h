@@ -108,6 +108,9 @@ typedef struct {
   double backtransform_flops;
   int64_t kernel_launches;/* kernels launched by the sweep                      */
   int64_t tridiag_launches;
+  double device_ms;       /* CUDA-event span of the sweep on the engine stream  */
+  int64_t h2d_bytes;      /* host-to-device bytes copied by the sweep           */
+  int64_t d2h_bytes;      /* device-to-host bytes copied by the sweep           */
 } nrg_timing;
 
 /* ---- context ---------------------------------------------------------- */
@@ -126,6 +129,10 @@ int nrg_sweep_num_iterations(const nrg_ctx* ctx);
 nrg_status nrg_sweep_iteration(const nrg_ctx* ctx, int n, nrg_iteration* out);
 nrg_status nrg_sweep_opavg_initial(const nrg_ctx* ctx, int* nops, const double** vals);
 nrg_status nrg_sweep_timing(const nrg_ctx* ctx, nrg_timing* out);
+
+/* Measured FP64 FMA throughput of the device (TFLOP/s), from a register-only
+ * DFMA loop over all SMs: the roofline denominator of the FP64 kernels. */
+nrg_status nrg_fp64_peak(nrg_ctx* ctx, double* tflops);
 
 /* ---- drop-in replacements --------------------------------------------- */
 

@@ -57,7 +57,8 @@ class Timing(ctypes.Structure):
                 ("backtransform_ms", ctypes.c_double), ("cut_ms", ctypes.c_double),
                 ("update_ms", ctypes.c_double), ("tridiag_flops", ctypes.c_double),
                 ("update_flops", ctypes.c_double), ("backtransform_flops", ctypes.c_double),
-                ("kernel_launches", ctypes.c_int64), ("tridiag_launches", ctypes.c_int64)]
+                ("kernel_launches", ctypes.c_int64), ("tridiag_launches", ctypes.c_int64),
+                ("device_ms", ctypes.c_double), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -89,6 +90,7 @@ def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     L.nrg_sweep_opavg_initial.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
                                           ctypes.POINTER(ctypes.POINTER(ctypes.c_double))]
     L.nrg_sweep_timing.argtypes = [ctypes.c_void_p, ctypes.POINTER(Timing)]
+    L.nrg_fp64_peak.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]
     _lib = L
     return L
 
@@ -149,6 +151,12 @@ class Engine:
     @property
     def kernel_count(self) -> int:
         return int(self.L.nrg_kernel_count(self.h))
+
+    def fp64_peak(self) -> float:
+        """Measured FP64 FMA throughput of the device, TFLOP/s."""
+        v = ctypes.c_double()
+        self._check(self.L.nrg_fp64_peak(self.h, ctypes.byref(v)))
+        return v.value
 
     def sweep(self, model: str, nsites: int, ncutoff: int, lam: float, U: float, ed: float,
               gamma1: float, gamma2_or_B: float = 0.0, degen_eps: float = 0.0,

@@ -149,6 +149,18 @@ struct Timer {
   }
 };
 
+// Stream-ordered copies that also count the bytes crossing the host boundary.
+void h2d(nrg_ctx* c, void* dst, const void* src, size_t bytes) {
+  if (!bytes) return;
+  CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream));
+  c->timing.h2d_bytes += (int64_t)bytes;
+}
+void d2h(nrg_ctx* c, void* dst, const void* src, size_t bytes) {
+  if (!bytes) return;
+  CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
+  c->timing.d2h_bytes += (int64_t)bytes;
+}
+
 void check_flag(nrg_ctx* c) {
   int f = 0;
   CU(cudaMemcpy(&f, c->flag.p, sizeof(int), cudaMemcpyDeviceToHost));
@@ -279,7 +291,7 @@ void run_vectors(nrg_ctx* c, Timer& tm, EigPlan& P, const std::vector<double>& e
          o_cf = pk.add(cf), o_cn = pk.add(cn), o_tb = pk.add(ctab), o_tf = pk.add(ctaf);
   DevBuf& mb = c->vmeta;
   mb.ensure(pk.host.size() + 256);
-  CU(cudaMemcpyAsync(mb.p, pk.host.data(), pk.host.size(), cudaMemcpyHostToDevice, c->stream));
+  h2d(c, mb.p, pk.host.data(), pk.host.size());
   char* base = mb.as<char>();
   c->Y.ensure(sizeof(double) * y);
   c->scratch.ensure(sizeof(double) * 5 * y);
@@ -371,6 +383,11 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
   const int nops = (int)m.op_kind.size();
   const int nops_h = m.kind == MODEL_1CHQS ? 1 : 2;  // old operators entering H_N
   Timer tm(c);
+  cudaEvent_t span0, span1;
+  CU(cudaEventCreate(&span0));
+  CU(cudaEventCreate(&span1));
+  struct EvGuard { cudaEvent_t a, b; ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); } } evg{span0, span1};
+  CU(cudaEventRecord(span0, c->stream));
   c->flag.ensure(sizeof(int) * 4);
   CU(cudaMemsetAsync(c->flag.p, 0, sizeof(int), c->stream));
   c->scal.ensure(sizeof(double) * 32);
@@ -387,7 +404,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
     S.ops.push_back(om);
     DevBuf* b = S.opbuf(0, o);
     b->ensure(sizeof(double) * std::max<int64_t>(om.size, 1));
-    CU(cudaMemcpyAsync(b->p, st.ops[o].el.data(), sizeof(double) * om.size, cudaMemcpyHostToDevice, c->stream));
+    h2d(c, b->p, st.ops[o].el.data(), sizeof(double) * om.size);
     if (m.op_avg[o]) {
       std::vector<double> diag(st.en.size(), 0.0);
       for (size_t k = 0; k < st.ops[o].bi.size(); ++k)
@@ -453,7 +470,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
            o_pf = pk.add(pair_fwd), o_pfl = pk.add(pair_fwd_ld), o_pbw = pk.add(pair_bwd), o_pbl = pk.add(pair_bwd_ld),
            o_coef = pk.add(tabs.coef), o_sq = pk.add(site_q), o_bq = pk.add(B.blk.qn);
     c->meta.ensure(pk.host.size() + 256);
-    CU(cudaMemcpyAsync(c->meta.p, pk.host.data(), pk.host.size(), cudaMemcpyHostToDevice, c->stream));
+    h2d(c, c->meta.p, pk.host.data(), pk.host.size());
     char* mb = c->meta.as<char>();
     c->H.ensure(sizeof(double) * std::max<int64_t>(P.hsize, 1));
     c->d.ensure(sizeof(double) * P.nstates); c->e.ensure(sizeof(double) * P.nstates);
@@ -463,7 +480,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
     // operator pointer table
     std::vector<const double*> hops(8, nullptr);
     for (int o = 0; o < nops; ++o) hops[o] = S.opbuf(S.cur, o)->as<double>();
-    CU(cudaMemcpyAsync(c->opptr.p, hops.data(), sizeof(double*) * hops.size(), cudaMemcpyHostToDevice, c->stream));
+    h2d(c, c->opptr.p, hops.data(), sizeof(double*) * hops.size());
     // ---------------- assembly
     AssembleArgs aa{};
     aa.nblocks = nb; aa.bsize = (const int*)(mb + o_bsize); aa.bstate = (const int*)(mb + o_soff);
@@ -504,9 +521,9 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
     c->launches += 4;
     std::vector<double> scal(20);
     R.en.resize(P.nstates);
-    CU(cudaMemcpyAsync(scal.data(), c->scal.p, sizeof(double) * 20, cudaMemcpyDeviceToHost, c->stream));
-    CU(cudaMemcpyAsync(keptb.data(), bs.kept, sizeof(int) * nb, cudaMemcpyDeviceToHost, c->stream));
-    CU(cudaMemcpyAsync(R.en.data(), c->en.p, sizeof(double) * P.nstates, cudaMemcpyDeviceToHost, c->stream));
+    d2h(c, scal.data(), c->scal.p, sizeof(double) * 20);
+    d2h(c, keptb.data(), bs.kept, sizeof(int) * nb);
+    d2h(c, R.en.data(), c->en.p, sizeof(double) * P.nstates);
     tm.stop(tc, &c->timing.cut_ms);
     CU(cudaStreamSynchronize(c->stream));
     check_flag(c);
@@ -617,7 +634,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
            o_avp = up.add(avgptr), o_kq = up.add(K.blk.qn);
     c->T.ensure(sizeof(double) * std::max<int64_t>(tsize, 1) + up.host.size() + 512);
     char* ub = c->T.as<char>() + ((sizeof(double) * std::max<int64_t>(tsize, 1) + 255) & ~size_t(255));
-    CU(cudaMemcpyAsync(ub, up.host.data(), up.host.size(), cudaMemcpyHostToDevice, c->stream));
+    h2d(c, ub, up.host.data(), up.host.size());
     CU(cudaMemsetAsync(c->T.p, 0, sizeof(double) * std::max<int64_t>(tsize, 1), c->stream));
     UpdateArgs ua{};
     ua.terms = (const GatherTerm*)(ub + o_terms); ua.group_first = (const int*)(ub + o_gf);
@@ -639,7 +656,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
     launch_opdiag(od, (const int*)(ub + o_ksb), (int)kstate_block.size(), c->partial.as<double>(), c->stream);
     c->launches += 2;
     std::vector<double> avg(8);
-    CU(cudaMemcpyAsync(avg.data(), c->scal.as<double>() + 24, sizeof(double) * 8, cudaMemcpyDeviceToHost, c->stream));
+    d2h(c, avg.data(), c->scal.as<double>() + 24, sizeof(double) * 8);
     tm.stop(to, &c->timing.cut_ms);
     CU(cudaStreamSynchronize(c->stream));
     check_flag(c);
@@ -658,8 +675,49 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
     for (int ich = 0; ich < m.nchan; ++ich) chi[ich] = chin(lambda, N);
     c->iters.push_back(std::move(R));
   }
+  CU(cudaEventRecord(span1, c->stream));
+  CU(cudaEventSynchronize(span1));
+  float span_ms = 0.f;
+  CU(cudaEventElapsedTime(&span_ms, span0, span1));
+  c->timing.device_ms = span_ms;
   c->timing.kernel_launches = c->launches - launches0;
   c->timing.total_ms = std::chrono::duration<double, std::milli>(clock::now() - t_begin).count();
+}
+
+// Register-only DFMA loop: eight independent chains per thread.
+__global__ void fp64_peak_kernel(double* out, int iters, double seed) {
+  double a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = seed + k + threadIdx.x * 1e-3;
+  const double m = 0.999999999, s = 1e-9;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fma(a[k], m, s);
+  }
+  double t = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) t += a[k];
+  if (t == 12345.678) out[0] = t;  // keeps the loop alive
+}
+
+double fp64_peak(nrg_ctx* c) {
+  c->scal.ensure(sizeof(double) * 32);
+  const int threads = 256, blocks = c->num_sms * 8, iters = 1 << 14;
+  cudaEvent_t a, b;
+  CU(cudaEventCreate(&a));
+  CU(cudaEventCreate(&b));
+  fp64_peak_kernel<<<blocks, threads, 0, c->stream>>>(c->scal.as<double>(), 256, 1.0);  // warm-up
+  CU(cudaEventRecord(a, c->stream));
+  fp64_peak_kernel<<<blocks, threads, 0, c->stream>>>(c->scal.as<double>(), iters, 1.0);
+  CU(cudaEventRecord(b, c->stream));
+  CU(cudaEventSynchronize(b));
+  c->launches += 2;
+  float ms = 0.f;
+  CU(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  const double flops = 2.0 * 8.0 * (double)iters * threads * blocks;
+  return flops / (ms * 1e-3) / 1e12;
 }
 
 }  // namespace
@@ -767,6 +825,15 @@ nrg_status nrg_sweep_opavg_initial(const nrg_ctx* ctx, int* nops, const double**
 nrg_status nrg_sweep_timing(const nrg_ctx* ctx, nrg_timing* out) {
   if (!ctx || !out) return NRG_ERR_ARG;
   *out = ctx->timing;
+  return NRG_OK;
+}
+
+nrg_status nrg_fp64_peak(nrg_ctx* ctx, double* tflops) {
+  if (!ctx || !tflops) return NRG_ERR_ARG;
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    *tflops = fp64_peak(ctx);
+  });
   return NRG_OK;
 }
 
