@@ -136,6 +136,18 @@ nrg_status nrg_fp64_peak(nrg_ctx* ctx, double* tflops);
 
 /* ---- drop-in replacements --------------------------------------------- */
 
+/* CNRGmatrix::DiagBlock replacement for a batch of blocks
+ * (src/NRGmatrixClass.cpp:566-696, dspev_ at :645).  Block b (size
+ * sizes[b]) is given as the reference hands it to dspev: its upper triangle
+ * packed row by row (element (i,j), j >= i, at i*n - i*(i-1)/2 + (j-i),
+ * ij2rUpTr src/ij2r.cpp:63-68), blocks concatenated.  On return eigvals
+ * holds each block's eigenvalues in ascending order (concatenated) and
+ * eigvecs each block's n x n eigenvector matrix, row k = eigenvector k
+ * (concatenated), exactly the dEn / dEigVec layout DiagBlock appends.
+ * All blocks are diagonalized in one batched launch series. */
+nrg_status nrg_diag_blocks(nrg_ctx* ctx, int nblocks, const int* sizes, const double* packed_upper,
+                           double* eigvals, double* eigvecs);
+
 /* Basis array as produced by BuildBasis (CNRGbasisarray, NRGclasses.hpp:215). */
 typedef struct {
   int nqn;                   /* QNumbers per block (2) */

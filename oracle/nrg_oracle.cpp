@@ -941,6 +941,17 @@ double oracle_cgordan(double j1, double m1, double j2, double m2, double j, doub
   return cgordan(j1, m1, j2, m2, j, m);
 }
 
+// CNRGmatrix::DiagBlock (NRGmatrixClass.cpp:566-656): dspev('V','L') on the
+// row-major packed upper triangle; row k of Z is eigenvector k.
+int oracle_diag_block(int n, const double* packed, double* w, double* Z) {
+  if (!g_dspev) { g_err = "LAPACK not loaded"; return -1; }
+  std::vector<double> A(packed, packed + (size_t)n * (n + 1) / 2), work(3 * (size_t)n);
+  int info = 0, ldz = n;
+  const char jobz = 'V', uplo = 'L';
+  g_dspev(&jobz, &uplo, &n, A.data(), w, Z, &ldz, work.data(), &info, 1, 1);
+  return info;
+}
+
 void* oracle_run(const oracle_config* cfg) {
   if (!g_dspev) { g_err = "LAPACK not loaded"; return nullptr; }
   auto t0 = std::chrono::steady_clock::now();

@@ -24,6 +24,7 @@ int oracle_load_lapack(const char* path);
 const char* oracle_last_error(void);
 void oracle_blas_threads(int n);
 double oracle_cgordan(double j1, double m1, double j2, double m2, double j, double m);
+int oracle_diag_block(int n, const double* packed, double* w, double* Z);
 void* oracle_run(const oracle_config* cfg);
 void oracle_free(void* h);
 

@@ -70,8 +70,8 @@ def lib():
         for name in ("oracle_iter_bsize", "oracle_iter_kept_bsize", "oracle_iter_basis_itype",
                      "oracle_iter_basis_stcf"):
             getattr(L, name).restype = ctypes.POINTER(ctypes.c_int)
-        for name in [n for n in dir(L) if False]:
-            pass
+        L.oracle_diag_block.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         rc = L.oracle_load_lapack(openblas_path().encode())
         if rc != 0:
             raise RuntimeError("oracle: " + L.oracle_last_error().decode())
@@ -150,3 +150,22 @@ def run(model: str, nsites: int, ncutoff: int, lam: float, U: float, ed: float, 
         return out
     finally:
         L.oracle_free(h)
+
+
+def diag_block(packed: np.ndarray, n: int):
+    """The reference's DiagBlock: LAPACK dspev on the packed upper triangle."""
+    L = lib()
+    packed = np.ascontiguousarray(packed, dtype=np.float64)
+    w = np.empty(n, dtype=np.float64)
+    Z = np.empty(n * n, dtype=np.float64)
+    P = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+    info = L.oracle_diag_block(n, P(packed), P(w), P(Z))
+    if info != 0:
+        raise RuntimeError(f"dspev info={info}")
+    return w, Z.reshape(n, n)
+
+
+def pack_upper(A: np.ndarray) -> np.ndarray:
+    """Row-major packed upper triangle (ij2rUpTr order)."""
+    n = A.shape[0]
+    return np.concatenate([A[i, i:] for i in range(n)]) if n else np.zeros(0)

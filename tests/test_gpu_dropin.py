@@ -1,0 +1,67 @@
+"""Drop-in DiagBlock replacement (nrg_diag_blocks) against LAPACK dspev as the
+reference calls it, on random blocks and on real NRG blocks.
+
+Tolerances: eigenvalues 1e-12 relative to the block norm; eigenvectors by
+residual and orthogonality (1e-12), and against dspev's up to sign where the
+level is isolated.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def _check_block(A, w, Z, wr, Zr):
+    nrm = max(1.0, float(np.max(np.abs(wr))))
+    assert np.max(np.abs(w - wr)) / nrm < 1e-12
+    n = A.shape[0]
+    R = A @ Z.T - Z.T * w
+    assert np.max(np.abs(R)) / nrm < 1e-12
+    assert np.max(np.abs(Z @ Z.T - np.eye(n))) < 1e-12
+    gaps = np.diff(wr)
+    for k in range(n):
+        iso = (k == 0 or gaps[k - 1] > 1e-6 * nrm) and (k == n - 1 or gaps[k] > 1e-6 * nrm)
+        if iso:
+            s = np.sign(Z[k] @ Zr[k])
+            assert np.max(np.abs(s * Z[k] - Zr[k])) < 1e-9
+
+
+def test_random_blocks(engine):
+    rng = np.random.default_rng(7)
+    sizes = [1, 2, 3, 17, 64, 130, 333]
+    mats = []
+    for n in sizes:
+        X = rng.standard_normal((n, n))
+        A = 0.5 * (X + X.T)
+        if n > 20:  # planted exact degeneracy
+            A[:3, :] = 0.0; A[:, :3] = 0.0
+            A[0, 0] = A[1, 1] = A[2, 2] = 0.25
+        mats.append(A)
+    packed = np.concatenate([orc.pack_upper(A) for A in mats])
+    ws, Zs = engine.diag_blocks(sizes, packed)
+    for A, w, Z in zip(mats, ws, Zs):
+        wr, Zr = orc.diag_block(orc.pack_upper(A), A.shape[0])
+        _check_block(A, w, Z, wr, Zr)
+
+
+def test_large_block_whole_gpu_path(engine):
+    rng = np.random.default_rng(11)
+    n = 1300  # above the whole-GPU threshold
+    X = rng.standard_normal((n, n))
+    A = (X + X.T) / np.sqrt(n)
+    ws, Zs = engine.diag_blocks([n], orc.pack_upper(A))
+    wr, Zr = orc.diag_block(orc.pack_upper(A), n)
+    _check_block(A, ws[0], Zs[0], wr, Zr)
+
+
+def test_nrg_blocks_from_a_real_iteration(engine):
+    """The H_N blocks the reference assembles (two-channel, N=2) diagonalized
+    through the drop-in must give the oracle's levels (before SetE0zero)."""
+    s = orc.run("2chQS", 3, 120, 2.5, 0.3, -0.15, 0.01, 0.01, capture_iter=2)
+    it = s.iters[2]
+    ws, _ = engine.diag_blocks(it.bsize, it.H)
+    w = np.concatenate(ws) - it.emin
+    # the oracle's levels went through SetDegen (MyEPS = 1e-18): compare to 1e-12
+    assert np.max(np.abs(w - it.en)) < 1e-12 * max(1.0, float(np.max(np.abs(it.en))))

@@ -91,6 +91,9 @@ def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
                                           ctypes.POINTER(ctypes.POINTER(ctypes.c_double))]
     L.nrg_sweep_timing.argtypes = [ctypes.c_void_p, ctypes.POINTER(Timing)]
     L.nrg_fp64_peak.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]
+    _dp = ctypes.POINTER(ctypes.c_double)
+    _ip = ctypes.POINTER(ctypes.c_int)
+    L.nrg_diag_blocks.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp, _dp, _dp]
     _lib = L
     return L
 
@@ -151,6 +154,28 @@ class Engine:
     @property
     def kernel_count(self) -> int:
         return int(self.L.nrg_kernel_count(self.h))
+
+    def diag_blocks(self, sizes, packed_upper):
+        """DiagBlock for a batch of blocks in the reference's packed-upper
+        storage.  Returns (eigenvalues per block, eigenvector matrices per
+        block with row k = eigenvector k)."""
+        sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+        packed = np.ascontiguousarray(packed_upper, dtype=np.float64)
+        need = int(sum(int(n) * (int(n) + 1) // 2 for n in sizes))
+        if packed.size != need:
+            raise ValueError(f"packed storage has {packed.size} elements, expected {need}")
+        ev = np.empty(int(sizes.sum()), dtype=np.float64)
+        vec = np.empty(int((sizes.astype(np.int64) ** 2).sum()), dtype=np.float64)
+        P = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))  # noqa: E731
+        self._check(self.L.nrg_diag_blocks(self.h, len(sizes), P(sizes, ctypes.c_int),
+                                           P(packed, ctypes.c_double), P(ev, ctypes.c_double),
+                                           P(vec, ctypes.c_double)))
+        out_e, out_v, so, vo = [], [], 0, 0
+        for n in sizes:
+            n = int(n)
+            out_e.append(ev[so:so + n]); out_v.append(vec[vo:vo + n * n].reshape(n, n))
+            so += n; vo += n * n
+        return out_e, out_v
 
     def fp64_peak(self) -> float:
         """Measured FP64 FMA throughput of the device, TFLOP/s."""

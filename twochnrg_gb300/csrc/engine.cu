@@ -684,6 +684,56 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
   c->timing.total_ms = std::chrono::duration<double, std::milli>(clock::now() - t_begin).count();
 }
 
+// DiagBlock for a batch of blocks given in the reference's packed upper
+// storage: same device pipeline as the sweep, all eigenvectors kept.
+void diag_blocks_impl(nrg_ctx* c, int nb, const int* sizes, const double* packed, double* evals, double* evecs) {
+  if (nb <= 0 || !sizes || !packed || !evals || !evecs) throw NrgError(NRG_ERR_ARG, "bad arguments");
+  std::vector<int> bs(sizes, sizes + nb);
+  for (int n : bs) if (n <= 0) throw NrgError(NRG_ERR_ARG, "block size must be positive");
+  std::memset(&c->timing, 0, sizeof(c->timing));
+  Timer tm(c);
+  EigPlan P;
+  plan_blocks(P, bs);
+  std::vector<double> Hh((size_t)P.hsize);
+  size_t pos = 0;
+  for (int b = 0; b < nb; ++b) {
+    const int n = bs[b];
+    double* h = Hh.data() + P.hoff[b];
+    for (int i = 0; i < n; ++i)
+      for (int j = i; j < n; ++j) { const double v = packed[pos++]; h[(size_t)i * n + j] = v; h[(size_t)j * n + i] = v; }
+  }
+  std::vector<int> order(nb), state_block(P.nstates);
+  for (int b = 0; b < nb; ++b) order[b] = b;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return bs[x] > bs[y]; });
+  for (int b = 0; b < nb; ++b) for (int i = 0; i < bs[b]; ++i) state_block[P.soff[b] + i] = b;
+  Packer pk;
+  size_t o_bsize = pk.add(P.bsize), o_soff = pk.add(P.soff), o_hoff = pk.add(P.hoff), o_order = pk.add(order),
+         o_sb = pk.add(state_block);
+  c->meta.ensure(pk.host.size() + 256);
+  c->H.ensure(sizeof(double) * (size_t)P.hsize);
+  c->d.ensure(sizeof(double) * P.nstates); c->e.ensure(sizeof(double) * P.nstates);
+  c->tau.ensure(sizeof(double) * P.nstates); c->ev.ensure(sizeof(double) * P.nstates);
+  c->red.ensure(sizeof(int) * 8);
+  c->flag.ensure(sizeof(int) * 4);
+  CU(cudaMemsetAsync(c->flag.p, 0, sizeof(int), c->stream));
+  h2d(c, c->meta.p, pk.host.data(), pk.host.size());
+  h2d(c, c->H.p, Hh.data(), sizeof(double) * (size_t)P.hsize);
+  char* mb = c->meta.as<char>();
+  run_tridiag_and_bisect(c, tm, P, order, (const int*)(mb + o_order), (const int*)(mb + o_bsize),
+                         (const int64_t*)(mb + o_hoff), (const int*)(mb + o_soff), (const int*)(mb + o_sb));
+  std::vector<double> ev(P.nstates);
+  d2h(c, ev.data(), c->ev.p, sizeof(double) * P.nstates);
+  CU(cudaStreamSynchronize(c->stream));
+  check_flag(c);
+  P.nvec = bs;
+  run_vectors(c, tm, P, ev, (const int*)(mb + o_bsize), (const int64_t*)(mb + o_hoff), (const int*)(mb + o_soff));
+  d2h(c, evecs, c->Z.p, sizeof(double) * (size_t)P.ysize);
+  CU(cudaStreamSynchronize(c->stream));
+  check_flag(c);
+  tm.collect();
+  std::memcpy(evals, ev.data(), sizeof(double) * P.nstates);
+}
+
 // Register-only DFMA loop: eight independent chains per thread.
 __global__ void fp64_peak_kernel(double* out, int iters, double seed) {
   double a[8];
@@ -825,6 +875,17 @@ nrg_status nrg_sweep_opavg_initial(const nrg_ctx* ctx, int* nops, const double**
 nrg_status nrg_sweep_timing(const nrg_ctx* ctx, nrg_timing* out) {
   if (!ctx || !out) return NRG_ERR_ARG;
   *out = ctx->timing;
+  return NRG_OK;
+}
+
+nrg_status nrg_diag_blocks(nrg_ctx* ctx, int nblocks, const int* sizes, const double* packed_upper,
+                           double* eigvals, double* eigvecs) {
+  if (!ctx) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    diag_blocks_impl(ctx, nblocks, sizes, packed_upper, eigvals, eigvecs);
+  });
   return NRG_OK;
 }
 
