@@ -148,6 +148,28 @@ nrg_status nrg_fp64_peak(nrg_ctx* ctx, double* tflops);
 nrg_status nrg_diag_blocks(nrg_ctx* ctx, int nblocks, const int* sizes, const double* packed_upper,
                            double* eigvals, double* eigvecs);
 
+/* Largest block nrg_diag_block_noalloc accepts. */
+#define NRG_NOALLOC_MAX_N 256
+
+/* Eigenvalues and eigenvectors of ONE symmetric block with no device memory
+ * allocated by the call.  This entry point has no counterpart in the
+ * reference; it exists for callers that cannot allocate device memory when
+ * they need the solve (all memory carved out at start-up, or an allocation's
+ * implicit device synchronisation not acceptable on their code path).
+ *   n        block size, 1 <= n <= NRG_NOALLOC_MAX_N (larger: NRG_ERR_SIZE)
+ *   a        device pointer, the full symmetric n x n matrix, row-major (read only)
+ *   eigvals  device pointer, n ascending eigenvalues (written)
+ *   eigvecs  device pointer, n x n row-major, row k = eigenvector k (written)
+ *   stream   cudaStream_t to run on (NULL = default stream); the call returns
+ *            after the stream has reached the end of the solve
+ * The solver's scratch is one fixed array of about 3.7 MB in device memory,
+ * reserved when the library is loaded and kept by every GPU that loads it
+ * until the process exits.  The first call on a device looks up the array's
+ * device address with that device current; call on the device you want to
+ * use.  All calls share the array: calls that overlap on the GPU (other host
+ * threads, other streams) race and must not be issued. */
+nrg_status nrg_diag_block_noalloc(int n, const double* a, double* eigvals, double* eigvecs, void* stream);
+
 /* Basis array as produced by BuildBasis (CNRGbasisarray, NRGclasses.hpp:215). */
 typedef struct {
   int nqn;                   /* QNumbers per block (2) */
