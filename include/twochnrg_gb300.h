@@ -170,80 +170,6 @@ nrg_status nrg_diag_blocks(nrg_ctx* ctx, int nblocks, const int* sizes, const do
  * threads, other streams) race and must not be issued. */
 nrg_status nrg_diag_block_noalloc(int n, const double* a, double* eigvals, double* eigvecs, void* stream);
 
-/* Basis array as produced by BuildBasis (CNRGbasisarray, NRGclasses.hpp:215). */
-typedef struct {
-  int nqn;                   /* QNumbers per block (2) */
-  int nblocks;
-  const double* qnumbers;    /* [nblocks*nqn] */
-  const int* block_beg_end;  /* [2*nblocks] */
-  const double* en;          /* [nstates] dEn: energies of the states they came from */
-  const int* itype;          /* [nstates] iType */
-  const int* st_came_from;   /* [nstates] StCameFrom (index into the old kept array) */
-} nrg_basis;
-
-/* Operator in the old kept basis (CNRGmatrix, NRGclasses.hpp:365). */
-typedef struct {
-  int npairs;
-  const int* mat_block_map;      /* [2*npairs] */
-  const int* mat_block_beg_end;  /* [2*npairs] */
-  const double* mat_el;
-  /* block structure of the old kept array the operator lives on */
-  int nblocks;
-  const int* block_beg_end;      /* [2*nblocks] */
-} nrg_operator;
-
-/* Eigen array as DiagHN leaves it in Aeig (CNRGarray). */
-typedef struct {
-  int nblocks;
-  const double* qnumbers;    /* [nblocks*2] */
-  const int* block_beg_end;  /* [2*nblocks] */
-  int nstates;
-  const double* en;          /* [nstates] ascending per block, E_min shifted out */
-  const double* eigvec;      /* [sum n_b^2] row k of block b = eigenvector k */
-  double emin;               /* subtracted ground energy */
-} nrg_eig;
-
-/* CNRGmatrix::DiagHN replacement (src/DiagHN.cpp:6-119): assemble every
- * (Q,S)/(Q,Sz) block of H_N on the device from the basis, the single-site
- * rules of `model` and the old operators f_N (ops[0..nchan*nsigma-1] in the
- * order of the model's MatArray), diagonalize all blocks in one batched
- * launch series and return ascending energies with SetE0zero applied and
- * all eigenvectors.  params = ParamsHN: {Lambda, chi_1[, chi_2], eN}. */
-nrg_status nrg_diag_hn(nrg_ctx* ctx, int model, const double* params, int nparams,
-                       const nrg_basis* abasis, const nrg_operator* ops, int nops,
-                       nrg_eig* out);
-
-/* Truncated array as CutStates leaves it in AeigCut (CNRGbasisarray). */
-typedef struct {
-  int nblocks;
-  const double* qnumbers;       /* [nblocks*2] */
-  const int* block_beg_end;     /* [2*nblocks] kept states */
-  const int* block_beg_end_bc;  /* [2*nblocks] the same blocks before the cut */
-  int nstates;
-  const double* en;             /* [nstates] kept energies (after SetDegen) */
-  const int* st_came_from;      /* [nstates] index in the uncut array */
-  const double* eigvec;         /* per block (kept x n_bc) rows = eigenvectors */
-  double ecut;
-  int nkept;                    /* states with E <= Ecut in the uncut array */
-} nrg_cut;
-
-/* CNRGarray::SetKept + CutStates replacement (src/NRGarrayClass.cpp:461-491,
- * src/CutStates.cpp:10-95): SetDegen, Ecut with the 1% window, Kept flags,
- * block removal and per-block tail removal, computed on the device.
- * `in` energies are SetDegen-merged in place semantics (returned in out). */
-nrg_status nrg_cut_states(nrg_ctx* ctx, const nrg_eig* in, int ncutoff, double degen_eps,
-                          nrg_cut* out);
-
-/* UpdateMatrices replacement (src/UpdateMatrices.cpp:272-568) for the
- * operators of `model` (index op_index in the model's MatArray order):
- * O_new(i,j) = Z_i . F(i,j) . Z_j^T for every kept block pair the model's
- * CheckForMatEl admits.  `old_op` is needed by NeedOld operators (n_d ...)
- * and ignored otherwise. */
-nrg_status nrg_update_matrix(nrg_ctx* ctx, int model, int op_index, const nrg_cut* acut,
-                             const nrg_basis* abasis, const nrg_operator* old_op,
-                             int* npairs, const int** mat_block_map,
-                             const int** mat_block_beg_end, const double** mat_el);
-
 #ifdef __cplusplus
 }
 #endif
