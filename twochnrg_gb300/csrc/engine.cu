@@ -556,7 +556,8 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
     cudaEvent_t tu = tm.start();
     std::vector<OpMeta> newops(nops);
     std::vector<RotJob> jobs;
-    std::vector<GatherTerm> terms;
+    std::vector<GatherTerm> terms, terms1;
+    std::vector<int> t1term, t1mn;
     std::vector<int> gfirst, gcount, tjob, tmn;
     int64_t tsize = 0;
     const int nk = K.blk.nblocks();
@@ -599,6 +600,13 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
                     if (g == 0.0) continue;
                     G.mode = 0; G.coef = g;
                   }
+                  if (G.mode == 1) {  // old block x Zt rows: tiled GEMM, one destination per term
+                    const int tid1 = (int)terms1.size();
+                    terms1.push_back(G);
+                    for (int mt = 0; mt * 64 < G.rows; ++mt)
+                      for (int nt = 0; nt * 64 < J.kj; ++nt) { t1term.push_back(tid1); t1mn.push_back((mt << 16) | nt); }
+                    continue;
+                  }
                   terms.push_back(G);
                 }
               if ((int)terms.size() > first) { gfirst.push_back(first); gcount.push_back((int)terms.size() - first); }
@@ -616,6 +624,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
       oldptr[o] = S.opbuf(S.cur, o)->as<double>();
     }
     Packer up;
+    size_t o_t1 = up.add(terms1), o_t1t = up.add(t1term), o_t1m = up.add(t1mn);
     size_t o_terms = up.add(terms), o_gf = up.add(gfirst), o_gc = up.add(gcount), o_jobs = up.add(jobs),
            o_tj = up.add(tjob), o_tm = up.add(tmn), o_old = up.add(oldptr), o_new = up.add(newptr),
            o_ken = up.add(new_kept_en);
@@ -642,7 +651,10 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
     ua.Z = c->Z.as<double>(); ua.Zt = c->Zt.as<double>(); ua.T = c->T.as<double>();
     ua.old_ops = (const double* const*)(ub + o_old); ua.new_ops = (double* const*)(ub + o_new);
     ua.tile_job = (const int*)(ub + o_tj); ua.tile_mn = (const int*)(ub + o_tm); ua.ntiles = (int)tjob.size();
+    ua.terms1 = (const GatherTerm*)(ub + o_t1); ua.tile1_term = (const int*)(ub + o_t1t);
+    ua.tile1_mn = (const int*)(ub + o_t1m); ua.ntiles1 = (int)t1term.size();
     launch_update(ua, c->stream);
+    if (ua.ntiles1 > 0) c->launches++;
     c->launches += 2;
     for (const RotJob& J : jobs) c->timing.update_flops += 2.0 * J.ki * (double)J.nI * J.kj;
     tm.stop(tu, &c->timing.update_ms);

@@ -34,6 +34,49 @@ __device__ __forceinline__ int sturm_count(const double* d, const double* e, int
   return cnt;
 }
 
+__device__ __forceinline__ int sturm_count_f32(const double* d, const double* e, int n, float x, float pivmin) {
+  int cnt = 0;
+  float q = (float)d[0] - x;
+  if (fabsf(q) < pivmin) q = -pivmin;
+  if (q < 0.0f) cnt++;
+  for (int i = 1; i < n; ++i) {
+    const float ei = (float)e[i - 1];
+    q = ((float)d[i] - x) - __fdividef(ei * ei, q);
+    if (fabsf(q) < pivmin) q = -pivmin;
+    if (q < 0.0f) cnt++;
+  }
+  return cnt;
+}
+
+// One FP64 pass: Sturm count of T - x and the Newton step -f/f' of
+// f(x) = det(T - x) from the pivot recurrence q_i and its derivative.
+__device__ __forceinline__ int sturm_newton(const double* d, const double* e, int n, double x, double pivmin,
+                                            double* step) {
+  int cnt = 0;
+  double q = d[0] - x, dq = -1.0;
+  if (fabs(q) < pivmin) q = -pivmin;
+  if (q < 0.0) cnt++;
+  double r = 1.0 / q;
+  double s = dq * r;  // sum of q_i'/q_i = f'/f
+  for (int i = 1; i < n; ++i) {
+    const double e2r = e[i - 1] * e[i - 1] * r;
+    const double qn = (d[i] - x) - e2r;
+    dq = fma(e2r * r, dq, -1.0);
+    q = fabs(qn) < pivmin ? -pivmin : qn;
+    if (q < 0.0) cnt++;
+    r = 1.0 / q;
+    s = fma(dq, r, s);
+  }
+  *step = -1.0 / s;
+  return cnt;
+}
+
+// The k-th eigenvalue (ascending) of each tridiagonal block: FP32 bisection
+// to about 1e-6 of the spectral radius, the bracket checked in FP64, then
+// safeguarded Newton steps in FP64 (a bisection step whenever Newton leaves
+// the bracket or stalls) until the bracket is a few ulps wide.  Every FP64
+// pass also updates the bracket with its Sturm count, so the result is the
+// k-th eigenvalue whatever the clustering.
 __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= A.nstates) return;
@@ -55,13 +98,51 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
   double lo = gl - 2.0 * kEps * tnorm * n - 2.0 * pivmin;
   double hi = gu + 2.0 * kEps * tnorm * n + 2.0 * pivmin;
   const double atol = 1e-3 * kEps * fmax(tnorm, DBL_MIN);
-  for (int it = 0; it < 200; ++it) {
-    const double mid = 0.5 * (lo + hi);
-    if (mid <= lo || mid >= hi) break;
-    if (hi - lo <= fmax(2.0 * kEps * fmax(fabs(lo), fabs(hi)), atol)) break;
-    if (sturm_count(d, e, n, mid, pivmin) > k) hi = mid; else lo = mid;
+  // FP32 bracket
+  if (tnorm > 1e-30 && tnorm < 1e30) {
+    float flo = (float)lo, fhi = (float)hi;
+    const float fpiv = 1e-30f;
+    for (int it = 0; it < 40 && (fhi - flo) > 1e-6f * (float)tnorm; ++it) {
+      const float mid = 0.5f * (flo + fhi);
+      if (sturm_count_f32(d, e, n, mid, fpiv) > k) fhi = mid; else flo = mid;
+    }
+    const double margin = 1e-5 * tnorm;
+    const double tlo = (double)flo - margin, thi = (double)fhi + margin;
+    double st;
+    if (tlo > lo && sturm_newton(d, e, n, tlo, pivmin, &st) <= k) lo = tlo;
+    if (thi < hi && sturm_newton(d, e, n, thi, pivmin, &st) > k) hi = thi;
   }
-  const double v = 0.5 * (lo + hi);
+  double x = 0.5 * (lo + hi);
+  double v = x;
+  bool newton = true, done = false;
+  for (int it = 0; it < 200 && !done; ++it) {
+    if (hi - lo <= fmax(2.0 * kEps * fmax(fabs(lo), fabs(hi)), atol)) break;
+    double step;
+    const int c = sturm_newton(d, e, n, x, pivmin, &step);
+    if (c > k) hi = x; else lo = x;
+    double xn = 0.5 * (lo + hi);
+    if (newton && isfinite(step)) {
+      // round-off floor of the recurrence: a few ulps of the spectral radius
+      const double small = 4.0 * kEps * fabs(x) + 16.0 * kEps * tnorm;
+      if (fabs(step) <= small) {
+        // converged: accept only if the k-th level is within reach of x
+        const double del = 2.0 * fabs(step) + small;
+        double t;
+        if (sturm_newton(d, e, n, x - del, pivmin, &t) <= k && sturm_newton(d, e, n, x + del, pivmin, &t) > k) {
+          v = x + step;
+          done = true;
+          break;
+        } else {
+          newton = false;
+        }
+      } else if (x + step > lo && x + step < hi && fabs(step) < 0.5 * (hi - lo)) {
+        xn = x + step;
+      }
+    }
+    x = xn;
+    v = x;
+  }
+  if (!done) v = (hi - lo <= fmax(2.0 * kEps * fmax(fabs(lo), fabs(hi)), atol)) ? 0.5 * (lo + hi) : x;
   if (!isfinite(v)) atomicOr(A.flag, DEV_BAD_INPUT);
   A.ev[g] = v;
 }

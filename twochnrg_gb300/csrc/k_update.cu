@@ -106,10 +106,70 @@ __global__ void __launch_bounds__(256) gemm_kernel(UpdateArgs A) {
   }
 }
 
+// Impurity-operator terms (old block x rows of Zt) as 64x64 GEMM tiles:
+// T[dst(a)] += coef * sum_b M[a][b] Zt[src(b)].  Each term owns its
+// destination rows, so tiles of different terms never overlap.
+__global__ void __launch_bounds__(256) imp_gemm_kernel(UpdateArgs A) {
+  __shared__ double As[TK][TM + 1];
+  __shared__ double Bs[TK][TN];
+  const GatherTerm G = A.terms1[A.tile1_term[blockIdx.x]];
+  const int mn = A.tile1_mn[blockIdx.x];
+  const RotJob J = A.jobs[G.job];
+  const int m0 = (mn >> 16) * TM, n0 = (mn & 0xffff) * TN;
+  const int M = G.rows, N = J.kj, K = G.srows;
+  const double* Am = A.old_ops[G.op] + G.old_off;  // rows x srows
+  const double* Zt = A.Zt + J.zt_off;
+  double* T = A.T + J.t_off;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+  for (int k0 = 0; k0 < K; k0 += TK) {
+    for (int idx = threadIdx.x; idx < TM * TK; idx += 256) {
+      const int r = idx / TK, c = idx - r * TK;
+      const int gr = m0 + r, gc = k0 + c;
+      As[c][r] = (gr < M && gc < K) ? Am[(int64_t)gr * K + gc] : 0.0;
+    }
+    for (int idx = threadIdx.x; idx < TK * TN; idx += 256) {
+      const int r = idx / TN, c = idx - r * TN;
+      const int gr = k0 + r, gc = n0 + c;
+      Bs[r][c] = (gr < K && gc < N) ? Zt[(int64_t)(G.src_base + gr * G.src_stride) * N + gc] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TK; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = m0 + ty + 16 * i;
+    if (r >= M) continue;
+    double* Trow = T + (int64_t)(G.dst_base + r * G.dst_stride) * N;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = n0 + tx + 16 * j;
+      if (c < N) Trow[c] = fma(G.coef, acc[i][j], Trow[c]);
+    }
+  }
+}
+
 }  // namespace
 
 void launch_update(const UpdateArgs& a, cudaStream_t s) {
   if (a.ngroups > 0) gather_kernel<<<a.ngroups, 256, 0, s>>>(a);
+  if (a.ntiles1 > 0) imp_gemm_kernel<<<a.ntiles1, 256, 0, s>>>(a);
   if (a.ntiles > 0) gemm_kernel<<<a.ntiles, 256, 0, s>>>(a);
 }
 

@@ -187,6 +187,11 @@ struct UpdateArgs {
   const int* tile_job;    // GEMM tiles: job
   const int* tile_mn;     // GEMM tiles: (mtile << 16) | ntile
   int ntiles;
+  // impurity-operator terms (mode 1), one destination per term, as tiles
+  const GatherTerm* terms1;
+  const int* tile1_term;
+  const int* tile1_mn;
+  int ntiles1;
 };
 void launch_update(const UpdateArgs& a, cudaStream_t s);
 
