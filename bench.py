@@ -147,7 +147,43 @@ def run_reference_arm(args, rank: int):
             "config": {"workload": WORKLOAD_NAME, "parallelism": "host threads over blocks"},
             "cpu_baseline": {"value": value, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    cbs, cdt, cn = cpu_batch_sample(cores)
+    line["batched"] = {"metric": "batched solves/s", "value": cbs, "unit": "solves/s",
+                       "instances": cn, "seconds": cdt, "workload": BATCH_NAME,
+                       "sample": f"oracle port on the first {cn} of {BATCH_INSTANCES} instances, one per thread"}
     print(json.dumps(line), flush=True)
+
+
+BATCH_INSTANCES = 256
+BATCH_SEED = 2024
+BATCH_NAME = ("independent one-channel Anderson solves, (Q,Sz) basis: U~U[0.1,1], ed=-U/2+U[-0.1,0.1], "
+              "Gamma log-U[1e-3,5e-2], B log-U[1e-8,1e-3], kept U{200..1000}, Lambda=2.5, 40 iterations, "
+              f"seed {BATCH_SEED}")
+
+
+def cpu_batch_sample(cores: int):
+    """Oracle port on the first `cores` instances, one per host thread."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as orc
+    from twochnrg_gb300.workloads import batched_qsz
+    inst = batched_qsz(BATCH_INSTANCES, seed=BATCH_SEED)[:cores]
+    orc.lib()
+    t = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=cores) as ex:
+        list(ex.map(lambda c: orc.run(c["model"], c["nsites"], c["ncutoff"], c["lam"], c["U"], c["ed"],
+                                      c["gamma1"], c["gamma2_or_B"], nthreads=1), inst))
+    dt = time.perf_counter() - t
+    return len(inst) / dt, dt, len(inst)
+
+
+def gpu_batch(workers: int, device: int):
+    import twochnrg_gb300 as tg
+    from twochnrg_gb300.workloads import batched_qsz
+    inst = batched_qsz(BATCH_INSTANCES, seed=BATCH_SEED)
+    tg.sweep_batch(inst[:workers], nworkers=workers, device=device)  # warm-up
+    res = tg.sweep_batch(inst, nworkers=workers, device=device)
+    return BATCH_INSTANCES / res.seconds, res.seconds
 
 
 # Fixed by the workload: sum over the 50 iterations of n_b^3 for the block
@@ -163,6 +199,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-workers", type=int, default=16)
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
@@ -231,6 +268,11 @@ def main():
                                           "cut_ms", "update_ms")},
         "sum_n3": w_full,
     }
+    # second half of the metric: batched independent solves per second
+    bs, bsec = gpu_batch(args.batch_workers, local)
+    line["batched"] = {"metric": "batched solves/s", "value": bs * (ws if dist else 1), "unit": "solves/s",
+                       "instances": BATCH_INSTANCES, "seconds": bsec, "workers": args.batch_workers,
+                       "workload": BATCH_NAME, "timing": "host wall time of nrg_sweep_batch"}
     if not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         dt, w_s = cpu_sample(cores)
@@ -238,6 +280,10 @@ def main():
             "value": dt * w_full / w_s, "unit": "s", "cores": cores, "kind": "port",
             "sample": (f"oracle port, same model/parameters with 600 kept and 8 iterations: {dt:.2f} s on "
                        f"{cores} threads, scaled by the sum n^3 ratio {w_full / w_s:.1f}")}
+        cbs, cdt, cn = cpu_batch_sample(cores)
+        line["batched"]["cpu_baseline"] = {
+            "value": cbs, "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": f"oracle port on the first {cn} instances, one per thread: {cdt:.2f} s"}
     print(json.dumps(line), flush=True)
     eng.close()
     if dist:

@@ -130,6 +130,20 @@ nrg_status nrg_sweep_iteration(const nrg_ctx* ctx, int n, nrg_iteration* out);
 nrg_status nrg_sweep_opavg_initial(const nrg_ctx* ctx, int* nops, const double** vals);
 nrg_status nrg_sweep_timing(const nrg_ctx* ctx, nrg_timing* out);
 
+/* ---- batched independent sweeps ----------------------------------------
+ * The reference's only batching is one process per parameter point
+ * (src/Scripts/RunNRGcluster.perl:18-122).  nrg_sweep_batch runs `ninst`
+ * independent sweeps on one GPU with `nworkers` host threads, each owning
+ * its own context and CUDA stream, so the instances' launches overlap on the
+ * device.  Per instance i and iteration n (n < cfgs[i].nsites, row stride
+ * `max_sites`) it writes
+ *   thermo[(i*max_sites + n)*16 .. +16]  as nrg_iteration.thermo,
+ *   opavg [(i*max_sites + n)*4  .. +4]   CalcOpAvg values (unused slots 0),
+ *   nkept [i*max_sites + n]              states with E <= Ecut.
+ * *seconds receives the wall time of the whole batch. */
+nrg_status nrg_sweep_batch(int device, int ninst, const nrg_sweep_config* cfgs, int nworkers, int max_sites,
+                           double* thermo, double* opavg, int* nkept, double* seconds);
+
 /* Measured FP64 FMA throughput of the device (TFLOP/s), from a register-only
  * DFMA loop over all SMs: the roofline denominator of the FP64 kernels. */
 nrg_status nrg_fp64_peak(nrg_ctx* ctx, double* tflops);

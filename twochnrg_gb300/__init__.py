@@ -94,6 +94,8 @@ def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     _dp = ctypes.POINTER(ctypes.c_double)
     _ip = ctypes.POINTER(ctypes.c_int)
     L.nrg_diag_blocks.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp, _dp, _dp]
+    L.nrg_sweep_batch.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(SweepConfig), ctypes.c_int,
+                                  ctypes.c_int, _dp, _dp, _ip, _dp]
     _lib = L
     return L
 
@@ -214,4 +216,36 @@ class Engine:
         return out
 
 
-__all__ = ["Engine", "NRGError", "SweepResult", "Iteration", "load_library", "MODELS"]
+@dataclass
+class BatchResult:
+    thermo: np.ndarray   # (ninst, max_sites, 4, 4)
+    opavg: np.ndarray    # (ninst, max_sites, 4)
+    nkept: np.ndarray    # (ninst, max_sites)
+    seconds: float
+
+
+def sweep_batch(instances, nworkers: int = 16, device: int = 0, precision: int = PREC_FP64) -> BatchResult:
+    """Run independent sweeps (dicts with the Engine.sweep keywords) on one
+    GPU through nrg_sweep_batch."""
+    L = load_library()
+    n = len(instances)
+    cfgs = (SweepConfig * max(n, 1))()
+    max_sites = max([int(c["nsites"]) for c in instances] + [1])
+    for i, c in enumerate(instances):
+        cfgs[i] = SweepConfig(MODELS[c["model"]], int(c["nsites"]), int(c["ncutoff"]), float(c["lam"]),
+                              float(c["U"]), float(c["ed"]), float(c["gamma1"]),
+                              float(c.get("gamma2_or_B", 0.0)), float(c.get("degen_eps", 0.0)), precision)
+    thermo = np.zeros((n, max_sites, 16))
+    opavg = np.zeros((n, max_sites, 4))
+    nkept = np.zeros((n, max_sites), dtype=np.int32)
+    sec = ctypes.c_double()
+    P = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))  # noqa: E731
+    st = L.nrg_sweep_batch(int(device), n, cfgs, int(nworkers), max_sites, P(thermo, ctypes.c_double),
+                           P(opavg, ctypes.c_double), P(nkept, ctypes.c_int), ctypes.byref(sec))
+    if st != 0:
+        raise NRGError(st, "nrg_sweep_batch: " + L.nrg_last_error(None).decode())
+    return BatchResult(thermo.reshape(n, max_sites, 4, 4), opavg, nkept, sec.value)
+
+
+__all__ = ["Engine", "NRGError", "SweepResult", "Iteration", "BatchResult", "load_library", "sweep_batch",
+           "MODELS"]

@@ -21,6 +21,9 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <atomic>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "../../include/twochnrg_gb300.h"
@@ -799,6 +802,9 @@ using namespace nrg;
     return NRG_ERR_ARG;                                    \
   }
 
+static std::mutex g_batch_mu;
+static std::string g_batch_err;
+
 extern "C" {
 
 const char* nrg_status_string(nrg_status s) {
@@ -841,7 +847,11 @@ void nrg_destroy(nrg_ctx* ctx) {
   delete ctx;
 }
 
-const char* nrg_last_error(const nrg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+const char* nrg_last_error(const nrg_ctx* ctx) {
+  if (ctx) return ctx->err.c_str();
+  std::lock_guard<std::mutex> lock(g_batch_mu);  // without a context: the last nrg_sweep_batch error
+  return g_batch_err.c_str();
+}
 
 int64_t nrg_kernel_count(const nrg_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
@@ -899,6 +909,54 @@ nrg_status nrg_diag_blocks(nrg_ctx* ctx, int nblocks, const int* sizes, const do
     diag_blocks_impl(ctx, nblocks, sizes, packed_upper, eigvals, eigvecs);
   });
   return NRG_OK;
+}
+
+nrg_status nrg_sweep_batch(int device, int ninst, const nrg_sweep_config* cfgs, int nworkers, int max_sites,
+                           double* thermo, double* opavg, int* nkept, double* seconds) {
+  if (ninst < 0 || !cfgs || nworkers < 1 || max_sites < 1 || !thermo || !opavg || !nkept) return NRG_ERR_ARG;
+  for (int i = 0; i < ninst; ++i)
+    if (cfgs[i].nsites > max_sites) return NRG_ERR_ARG;
+  auto t0 = std::chrono::steady_clock::now();
+  {
+    std::lock_guard<std::mutex> lock(g_batch_mu);
+    g_batch_err.clear();
+  }
+  std::atomic<int> next(0);
+  std::atomic<int> status(NRG_OK);
+  std::vector<std::thread> th;
+  const int nw = std::min(nworkers, std::max(ninst, 1));
+  for (int w = 0; w < nw; ++w) {
+    th.emplace_back([&]() {
+      nrg_ctx* c = nullptr;
+      nrg_status st = nrg_create(device, &c);
+      if (st != NRG_OK) {
+        status.store(st);
+        std::lock_guard<std::mutex> lock(g_batch_mu);
+        if (g_batch_err.empty()) g_batch_err = "nrg_create failed in a batch worker";
+        return;
+      }
+      for (int i; (i = next.fetch_add(1)) < ninst;) {
+        st = nrg_sweep_run(c, &cfgs[i]);
+        if (st != NRG_OK) {
+          status.store(st);
+          std::lock_guard<std::mutex> lock(g_batch_mu);
+          if (g_batch_err.empty()) g_batch_err = "instance " + std::to_string(i) + ": " + c->err;
+          break;
+        }
+        for (int n = 0; n < (int)c->iters.size(); ++n) {
+          const IterResult& R = c->iters[n];
+          const size_t row = (size_t)i * max_sites + n;
+          std::copy(R.thermo.begin(), R.thermo.end(), thermo + row * 16);
+          for (int k = 0; k < 4; ++k) opavg[row * 4 + k] = k < (int)R.opavg.size() ? R.opavg[k] : 0.0;
+          nkept[row] = R.nkept;
+        }
+      }
+      nrg_destroy(c);
+    });
+  }
+  for (auto& t : th) t.join();
+  if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return (nrg_status)status.load();
 }
 
 nrg_status nrg_fp64_peak(nrg_ctx* ctx, double* tflops) {

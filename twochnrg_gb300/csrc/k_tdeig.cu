@@ -112,11 +112,15 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
     if (tlo > lo && sturm_newton(d, e, n, tlo, pivmin, &st) <= k) lo = tlo;
     if (thi < hi && sturm_newton(d, e, n, thi, pivmin, &st) > k) hi = thi;
   }
+  // Stop at a few ulps of the spectral radius: below that the Sturm counts
+  // are at the round-off of the recurrence.
+  const double floor_w = fmax(8.0 * kEps * tnorm, atol);
   double x = 0.5 * (lo + hi);
   double v = x;
   bool newton = true, done = false;
   for (int it = 0; it < 200 && !done; ++it) {
-    if (hi - lo <= fmax(2.0 * kEps * fmax(fabs(lo), fabs(hi)), atol)) break;
+    if (hi - lo <= fmax(2.0 * kEps * fmax(fabs(lo), fabs(hi)), floor_w)) break;
+    if (it >= 12) newton = false;  // Newton that has not converged by now: bisect
     double step;
     const int c = sturm_newton(d, e, n, x, pivmin, &step);
     if (c > k) hi = x; else lo = x;
@@ -142,7 +146,7 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
     x = xn;
     v = x;
   }
-  if (!done) v = (hi - lo <= fmax(2.0 * kEps * fmax(fabs(lo), fabs(hi)), atol)) ? 0.5 * (lo + hi) : x;
+  if (!done) v = 0.5 * (lo + hi);  // the bracket always holds the k-th level
   if (!isfinite(v)) atomicOr(A.flag, DEV_BAD_INPUT);
   A.ev[g] = v;
 }
@@ -356,7 +360,7 @@ cudaError_t launch_backtransform(const BackArgs& a, const int* cta_block, const 
                                  cudaStream_t s) {
   if (nctas <= 0) return cudaSuccess;
   size_t smem = backtransform_smem_bytes(a.maxn);
-  cudaError_t err = cudaFuncSetAttribute(backtransform_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t err = cudaFuncSetAttribute(backtransform_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem());
   if (err != cudaSuccess) return err;
   backtransform_kernel<<<nctas, backtransform_warps(a.maxn) * 32, smem, s>>>(a, cta_block, cta_first);
   return cudaGetLastError();

@@ -333,7 +333,8 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_grid_kernel(TridiagArgs A
 
 int tridiag_grid_size(int maxn) {
   size_t smem = sizeof(double) * (5 * (size_t)maxn + kWarps + 4) + 16;
-  if (cudaFuncSetAttribute(tridiag_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (cudaFuncSetAttribute(tridiag_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()) !=
+      cudaSuccess)
     return 0;
   int per_sm = 0, dev = 0, sms = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tridiag_grid_kernel, kThreads, smem) != cudaSuccess)
@@ -346,7 +347,8 @@ int tridiag_grid_size(int maxn) {
 cudaError_t launch_tridiag_grid(const TridiagArgs& a, const int* big, int nbig, double* part, double* pvec,
                                 double* dots, int grid, cudaStream_t s) {
   size_t smem = sizeof(double) * (5 * (size_t)a.maxn + kWarps + 4) + 16;
-  cudaError_t err = cudaFuncSetAttribute(tridiag_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t err =
+      cudaFuncSetAttribute(tridiag_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem());
   if (err != cudaSuccess) return err;
   TridiagArgs aa = a;
   void* args[] = {(void*)&aa, (void*)&big, (void*)&nbig, (void*)&part, (void*)&pvec, (void*)&dots};
@@ -359,7 +361,7 @@ size_t tridiag_smem_bytes(int maxn) {
 
 cudaError_t launch_tridiag(const TridiagArgs& a, int cluster, int nclusters, cudaStream_t s) {
   size_t smem = tridiag_smem_bytes(a.maxn);
-  cudaError_t err = cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t err = cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem());
   if (err != cudaSuccess) return err;
   if (cluster > 8) {
     err = cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -382,7 +384,7 @@ cudaError_t launch_tridiag(const TridiagArgs& a, int cluster, int nclusters, cud
 
 int tridiag_max_clusters(int cluster, int maxn) {
   size_t smem = tridiag_smem_bytes(maxn);
-  if (cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()) != cudaSuccess)
     return 0;
   if (cluster > 8) cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   cudaLaunchConfig_t cfg = {};

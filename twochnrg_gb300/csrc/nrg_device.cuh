@@ -6,6 +6,17 @@
 
 namespace nrg {
 
+// Largest opt-in dynamic shared memory per block of the current device.
+// Kernels get this one value as their MaxDynamicSharedMemorySize attribute
+// (never a per-launch size), so concurrent host threads cannot lower the
+// limit between another thread's attribute call and its launch.
+inline int max_dyn_smem() {
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return v;
+}
+
 // Error flags a kernel can raise without trapping; the host reads the word
 // after the launch series and turns it into an nrg_status.
 enum DeviceFlag : int {

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <stdexcept>
 
 namespace nrg {
@@ -90,13 +91,19 @@ double clebsch(double J1, double M1, double J2, double M2, double J, double M) {
 }
 
 namespace {
-// Memoised Clebsch-Gordan: pure function of six half-integers.
+// Memoised Clebsch-Gordan: pure function of six half-integers.  Shared by
+// the host threads of batched sweeps, hence the lock.
 double cg(double a, double b, double c, double d, double e, double f) {
   static std::map<std::array<double, 6>, double> memo;
+  static std::mutex mu;
   std::array<double, 6> k{a, b, c, d, e, f};
-  auto it = memo.find(k);
-  if (it != memo.end()) return it->second;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = memo.find(k);
+    if (it != memo.end()) return it->second;
+  }
   double v = clebsch(a, b, c, d, e, f);
+  std::lock_guard<std::mutex> lock(mu);
   memo.emplace(k, v);
   return v;
 }
