@@ -163,10 +163,19 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
       cl.sync();
 
       // Phase 3: p = tau * A v (sum of the CTAs' shares), w = p - (tau/2)(p.v) v.
-      for (int c = j + 1 + tid; c < n; c += kThreads) {
-        double p = 0.0;
-        for (int q = 0; q < CL; ++q) p += cl.map_shared_rank(yp, q)[c];
-        W[c] = tau * p;
+      {
+        const double* rem[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) rem[q] = q < CL ? cl.map_shared_rank(yp, q) : yp;
+        for (int c = j + 1 + tid; c < n; c += kThreads) {
+          double sh[16];
+#pragma unroll
+          for (int q = 0; q < 16; ++q) sh[q] = q < CL ? rem[q][c] : 0.0;  // all loads in flight
+          double p = 0.0;
+#pragma unroll
+          for (int q = 0; q < 16; ++q) p += sh[q];
+          W[c] = tau * p;
+        }
       }
       __syncthreads();
       double dt = 0.0;
@@ -285,13 +294,18 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_grid_kernel(TridiagArgs A
       // reduce-scatter: this CTA owns columns [q0, q1)
       const int cols_per = (m + G - 1) / G;
       const int q0 = j + 1 + rank * cols_per, q1 = min(n, q0 + cols_per);
+      // one warp per column: lanes stride over the G shares, then a fixed-order
+      // shuffle tree (every CTA sums its columns the same way)
       double dpart = 0.0;
-      for (int c = q0 + tid; c < q1; c += kThreads) {
+      for (int c = q0 + warp; c < q1; c += kWarps) {
         double p = 0.0;
-        for (int q = 0; q < G; ++q) p += __ldcg(part + (int64_t)q * maxn + c);
+        for (int q = lane; q < G; q += 32) p += __ldcg(part + (int64_t)q * maxn + c);
+        for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
         p *= tau;
-        __stcg(pvec + c, p);
-        dpart = fma(p, vnew[c], dpart);
+        if (lane == 0) {
+          __stcg(pvec + c, p);
+          dpart = fma(p, vnew[c], dpart);
+        }
       }
       dpart = block_sum(dpart, red);
       if (tid == 0) __stcg(dots + rank, dpart);
