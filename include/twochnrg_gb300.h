@@ -162,6 +162,111 @@ nrg_status nrg_fp64_peak(nrg_ctx* ctx, double* tflops);
 nrg_status nrg_diag_blocks(nrg_ctx* ctx, int nblocks, const int* sizes, const double* packed_upper,
                            double* eigvals, double* eigvecs);
 
+/* ---- per-step drop-ins for the NRG_main call sites ----------------------
+ * Block structure of a CNRGarray (include/NRGclasses.hpp:47-200).  All
+ * models here carry two quantum numbers per block: (Q,S) for the |Q S>
+ * models, (Q,Sz) for NRG_MODEL_1CH_QSZ.  States are numbered from 0 and the
+ * blocks tile them in order. */
+typedef struct {
+  int nblocks;
+  int nqn;                       /* must be 2 */
+  const double* qnumbers;        /* [nblocks*nqn] QNumbers */
+  const int* block_beg_end;      /* [2*nblocks] BlockBegEnd: first, last state (inclusive) */
+} nrg_blocks;
+
+/* CNRGbasisarray as BuildBasis leaves it (src/BuildBasis.cpp:8-432). */
+typedef struct {
+  nrg_blocks blocks;
+  const int* itype;              /* [nstates] iType: single-site state type */
+  const int* st_came_from;       /* [nstates] StCameFrom: state of the previous AeigCut */
+  const double* en;              /* [nstates] dEn: energy of that previous kept state */
+} nrg_basis;
+
+/* One real operator, CNRGmatrix (include/NRGclasses.hpp:365-434): dense
+ * row-major (size_i x size_j) blocks for the listed block pairs, in the block
+ * structure the operator is synced with. */
+typedef struct {
+  int nmatblocks;
+  const int* mat_block_map;      /* [2*nmatblocks] MatBlockMap: (iblock, jblock) */
+  const int* mat_block_beg_end;  /* [2*nmatblocks] MatBlockBegEnd: first, last index in mat_el */
+  const double* mat_el;          /* MatEl */
+} nrg_matrix;
+
+/* AeigCut as CutStates leaves it (src/CutStates.cpp:10-95, CNRGbasisarray). */
+typedef struct {
+  nrg_blocks blocks;               /* kept blocks; BlockBegEnd over the kept states */
+  const int* block_beg_end_bc;     /* [2*nblocks] BlockBegEndBC: the block's state range before the cut */
+  const int* block_beg_end_eigvec; /* [2*nblocks] BlockBegEndEigVec: range of its rows in eigvec */
+  const int* st_came_from;         /* [nstates] StCameFrom: state of the uncut array */
+  const double* en;                /* [nstates] dEn */
+  const unsigned char* kept;       /* [nstates] Kept */
+  const double* eigvec;            /* dEigVec: per block, kept rows x n_BC, row-major */
+} nrg_eigcut;
+
+/* Result of nrg_cut_states; all arrays are owned by the context. */
+typedef struct {
+  const double* en;              /* [nstates] Aeig.dEn after SetKept (SetDegen applied) */
+  const unsigned char* kept;     /* [nstates] Aeig.Kept */
+  int nkept;                     /* states with E <= Ecut */
+  double ecut;                   /* CNRGarray::Ecut(Ncutoff) */
+  nrg_eigcut cut;                /* AeigCut (cut.eigvec NULL when no eigvec was given) */
+} nrg_cut_result;
+
+/* Operators, in this order, that nrg_diag_hn and nrg_update_ops take and
+ * return (the NRGMats of CNRGCodeHandler::ModelSwitch,
+ * src/CodeHandler_ModelSwitch.cpp:136-157, 748-780):
+ *   NRG_MODEL_1CH_QS : f_N, n_d, n_d^2, S_d^2
+ *   NRG_MODEL_1CH_QSZ: f_N,up, f_N,dn, n_d, S_z
+ *   NRG_MODEL_2CH_QS : f_N,ch1, f_N,ch2, n_d, n_d^2, S_d^2
+ * The f operators (the first one, or two) enter H_N; n_d, n_d^2, S_d^2 and S_z
+ * are the impurity operators CalcOpAvg averages. */
+
+/* CNRGmatrix::DiagHN (src/DiagHN.cpp:6-119, declared include/NRGclasses.hpp:642-646),
+ * including its closing SetE0zero (DiagHN.cpp:116, src/NRGarrayClass.cpp:234-241);
+ * called by NRG_main at src/Main/NRG_main.cpp:313.
+ *   params_hn  ParamsHN as NRG_main builds it (NRG_main.cpp:264-276):
+ *              Lambda, chi_1 [, chi_2], e_N, Delta_SC; nparams >= nchannels + 2,
+ *              Delta_SC (if given) must be 0
+ *   old_kept   block structure of the previous AeigCut (the operators' sync)
+ *   ops        the model's operators (order above) in that structure; the
+ *              f operators are read
+ *   abasis     the basis BuildBasis made from old_kept; a basis that does not
+ *              match BuildBasis's layout returns NRG_ERR_SYNC
+ * Outputs (caller-owned): en[nstates] each block's eigenvalues ascending,
+ * E_min subtracted; eigvec, per block its n x n eigenvector matrix (row k =
+ * eigenvector k), blocks concatenated (sum of n_b^2); *emin the subtracted
+ * ground energy.  H_N is assembled and diagonalized on the device. */
+nrg_status nrg_diag_hn(nrg_ctx* ctx, int model, const double* params_hn, int nparams, const nrg_blocks* old_kept,
+                       int nops, const nrg_matrix* ops, const nrg_basis* abasis, double* en, double* eigvec,
+                       double* emin);
+
+/* CNRGarray::SetKept (src/NRGarrayClass.cpp:461-491: SetDegen and Ecut)
+ * then CutStates (src/CutStates.cpp:10-95) on Aeig as DiagHN leaves it.
+ *   aeig, en    block structure and dEn of Aeig (E_min-shifted: min(en) == 0,
+ *               else NRG_ERR_ARG)
+ *   eigvec      Aeig.dEigVec (per block n x n, row = eigenvector) or NULL
+ *   ncutoff     Ncutoff; degen_eps MyEPS (<= 0 selects 1e-18)
+ * Kept flags, Nkept, BlockBegEnd, BlockBegEndBC, BlockBegEndEigVec and
+ * StCameFrom equal the reference's; `out` points into context storage. */
+nrg_status nrg_cut_states(nrg_ctx* ctx, const nrg_blocks* aeig, const double* en, const double* eigvec,
+                          int ncutoff, double degen_eps, nrg_cut_result* out);
+
+/* UpdateMatrices (src/UpdateMatrices.cpp:272-568) for all of the model's
+ * operators: O_new(i,j) = Z_i F Z_j^T for every pair of kept blocks allowed
+ * by CheckForMatEl, F from the single-site rules (times the old operator for
+ * the impurity operators).
+ *   old_kept  block structure the old operators are synced with
+ *   abasis    the basis BuildBasis made from old_kept (NRG_ERR_SYNC otherwise)
+ *   acut      AeigCut of this iteration (blocks, eigvec, block_beg_end_eigvec
+ *             are read; kept blocks are matched to abasis blocks by their
+ *             quantum numbers, FindMatchBlock src/FindMatchBlock.cpp:5-24)
+ *   old_ops   [nops] the model's operators (order above), nops = the model's count
+ * new_ops[o] receives MatBlockMap/MatBlockBegEnd/MatEl in the reference's
+ * block-pair order (iblock major, jblock minor), pointing into context
+ * storage. */
+nrg_status nrg_update_ops(nrg_ctx* ctx, int model, const nrg_blocks* old_kept, const nrg_basis* abasis,
+                          const nrg_eigcut* acut, int nops, const nrg_matrix* old_ops, nrg_matrix* new_ops);
+
 /* Largest block nrg_diag_block_noalloc accepts. */
 #define NRG_NOALLOC_MAX_N 256
 

@@ -908,6 +908,10 @@ struct OracleIter {
   std::vector<double> basis_qn, basis_en;
   std::vector<int> basis_bbe, basis_itype, basis_stcf;
   std::vector<double> H;          // packed upper triangles, block-concatenated
+  // Every input and output of the iteration's DiagHN / SetKept / CutStates /
+  // UpdateMatrices steps, by name (see oracle_run).
+  std::map<std::string, std::vector<double>> capd;
+  std::map<std::string, std::vector<int>> capi;
 };
 
 struct OracleRun {
@@ -1027,11 +1031,21 @@ void* oracle_run(const oracle_config* cfg) {
     if (cap) {
       I.basis_qn = ab.qn; I.basis_en = ab.en; I.basis_bbe = ab.bbe;
       I.basis_itype = ab.itype; I.basis_stcf = ab.stcf;
+      I.capd["old_qn"] = cut.qn; I.capi["old_bbe"] = cut.bbe;
+      for (size_t o = 0; o < mats.size(); ++o) {
+        I.capi["old_map." + std::to_string(o)] = mats[o].map;
+        I.capi["old_mbe." + std::to_string(o)] = mats[o].mbe;
+        I.capd["old_el." + std::to_string(o)] = mats[o].el;
+      }
+      I.capd["basis_qn"] = ab.qn; I.capi["basis_bbe"] = ab.bbe; I.capd["basis_en"] = ab.en;
+      I.capi["basis_itype"] = ab.itype; I.capi["basis_stcf"] = ab.stcf;
     }
     std::vector<std::vector<double>> H;
     diag_hn(c, P, ab, mats, eig, nthreads, cap ? &H : nullptr, &I.emin);
     if (cap) for (auto& h : H) I.H.insert(I.H.end(), h.begin(), h.end());
+    if (cap) { I.capd["eig_en"] = eig.en; I.capd["eig_evec"] = eig.evec; I.capd["params"] = P; }
     I.ecut = set_kept(eig, cfg->ncutoff, eps, &I.nkept);
+    if (cap) { I.capd["kept_en"] = eig.en; I.capi["kept"] = std::vector<int>(eig.kept.begin(), eig.kept.end()); }
     I.qn = eig.qn;
     for (int b = 0; b < eig.nblocks(); ++b) I.bsize.push_back(eig.bsize(b));
     I.en = eig.en;
@@ -1042,7 +1056,18 @@ void* oracle_run(const oracle_config* cfg) {
       I.thermo.push_back(calc_entropy(eig, bN, sq, totalS));
     }
     cut_states(eig, cut, cfg->ncutoff, eps);
+    if (cap) {
+      I.capd["cut_qn"] = cut.qn; I.capi["cut_bbe"] = cut.bbe; I.capi["cut_bbe_bc"] = cut.bbe_bc;
+      I.capi["cut_bbe_eig"] = cut.bbe_eig; I.capi["cut_stcf"] = cut.stcf; I.capd["cut_en"] = cut.en;
+      I.capi["cut_kept"] = std::vector<int>(cut.kept.begin(), cut.kept.end()); I.capd["cut_evec"] = cut.evec;
+    }
     update_matrices(c, cut, ab, mats, nthreads);
+    if (cap)
+      for (size_t o = 0; o < mats.size(); ++o) {
+        I.capi["new_map." + std::to_string(o)] = mats[o].map;
+        I.capi["new_mbe." + std::to_string(o)] = mats[o].mbe;
+        I.capd["new_el." + std::to_string(o)] = mats[o].el;
+      }
     for (auto& m : mats) if (m.calc_avg) I.opavg.push_back(calc_opavg(cut, m, betabar, totalS, sq));
     for (int b = 0; b < cut.nblocks(); ++b) I.kept_bsize.push_back(cut.bsize(b));
     for (int ich = 0; ich < nchan; ++ich) P[ich + 1] = chin(N);
@@ -1080,5 +1105,21 @@ const double* oracle_iter_H(void* h, int n) { return ITER(h, n).H.data(); }
 const int* oracle_iter_basis_itype(void* h, int n) { return ITER(h, n).basis_itype.data(); }
 const int* oracle_iter_basis_stcf(void* h, int n) { return ITER(h, n).basis_stcf.data(); }
 const double* oracle_iter_basis_en(void* h, int n) { return ITER(h, n).basis_en.data(); }
+
+// Named captures of the capture iteration: NULL (and *len = -1) if absent.
+const double* oracle_cap_d(void* h, int n, const char* name, int* len) {
+  auto& m = ITER(h, n).capd;
+  auto it = m.find(name);
+  if (it == m.end()) { *len = -1; return nullptr; }
+  *len = (int)it->second.size();
+  return it->second.data();
+}
+const int* oracle_cap_i(void* h, int n, const char* name, int* len) {
+  auto& m = ITER(h, n).capi;
+  auto it = m.find(name);
+  if (it == m.end()) { *len = -1; return nullptr; }
+  *len = (int)it->second.size();
+  return it->second.data();
+}
 
 }  // extern "C"

@@ -27,6 +27,9 @@ double oracle_cgordan(double j1, double m1, double j2, double m2, double j, doub
 int oracle_diag_block(int n, const double* packed, double* w, double* Z);
 void* oracle_run(const oracle_config* cfg);
 void oracle_free(void* h);
+/* Named arrays of the capture iteration (NULL and *len = -1 if absent). */
+const double* oracle_cap_d(void* h, int n, const char* name, int* len);
+const int* oracle_cap_i(void* h, int n, const char* name, int* len);
 
 #ifdef __cplusplus
 }

@@ -70,6 +70,11 @@ def lib():
         for name in ("oracle_iter_bsize", "oracle_iter_kept_bsize", "oracle_iter_basis_itype",
                      "oracle_iter_basis_stcf"):
             getattr(L, name).restype = ctypes.POINTER(ctypes.c_int)
+        L.oracle_cap_d.restype = ctypes.POINTER(ctypes.c_double)
+        L.oracle_cap_i.restype = ctypes.POINTER(ctypes.c_int)
+        for name in ("oracle_cap_d", "oracle_cap_i"):
+            getattr(L, name).argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p,
+                                         ctypes.POINTER(ctypes.c_int)]
         L.oracle_diag_block.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         rc = L.oracle_load_lapack(openblas_path().encode())
@@ -95,6 +100,10 @@ class Iteration:
     basis_itype: np.ndarray | None = None
     basis_stcf: np.ndarray | None = None
     basis_en: np.ndarray | None = None
+    # capture iteration only: every input/output of DiagHN, SetKept, CutStates
+    # and UpdateMatrices by name (old_*, basis_*, eig_*, kept*, cut_*, new_*;
+    # per-operator arrays end in .<operator index>)
+    cap: dict | None = None
 
 
 @dataclass
@@ -146,10 +155,46 @@ def run(model: str, nsites: int, ncutoff: int, lam: float, U: float, ed: float, 
                 it.basis_itype = _arr(L.oracle_iter_basis_itype(h, n), ns, np.int64)
                 it.basis_stcf = _arr(L.oracle_iter_basis_stcf(h, n), ns, np.int64)
                 it.basis_en = _arr(L.oracle_iter_basis_en(h, n), ns, np.float64)
+                it.cap = _captures(L, h, n)
             out.iters.append(it)
         return out
     finally:
         L.oracle_free(h)
+
+
+_CAP_D = ("old_qn", "basis_qn", "basis_en", "eig_en", "eig_evec", "params", "kept_en", "cut_qn",
+          "cut_en", "cut_evec")
+_CAP_I = ("old_bbe", "basis_bbe", "basis_itype", "basis_stcf", "kept", "cut_bbe", "cut_bbe_bc",
+          "cut_bbe_eig", "cut_stcf", "cut_kept")
+
+
+def _captures(L, h, n) -> dict:
+    out = {}
+    ln = ctypes.c_int(0)
+
+    def get(fn, name, dtype):
+        p = fn(h, n, name.encode(), ctypes.byref(ln))
+        if ln.value < 0:
+            return None
+        return _arr(p, ln.value, dtype)
+
+    for name in _CAP_D:
+        out[name] = get(L.oracle_cap_d, name, np.float64)
+    for name in _CAP_I:
+        out[name] = get(L.oracle_cap_i, name, np.int64)
+    o = 0
+    while True:
+        el = get(L.oracle_cap_d, f"old_el.{o}", np.float64)
+        if el is None:
+            break
+        out[f"old_el.{o}"] = el
+        for pre in ("old", "new"):
+            out[f"{pre}_map.{o}"] = get(L.oracle_cap_i, f"{pre}_map.{o}", np.int64)
+            out[f"{pre}_mbe.{o}"] = get(L.oracle_cap_i, f"{pre}_mbe.{o}", np.int64)
+        out[f"new_el.{o}"] = get(L.oracle_cap_d, f"new_el.{o}", np.float64)
+        o += 1
+    out["nmats"] = o
+    return out
 
 
 def diag_block(packed: np.ndarray, n: int):

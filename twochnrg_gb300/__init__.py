@@ -64,6 +64,59 @@ class Timing(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+_DP = ctypes.POINTER(ctypes.c_double)
+_IP = ctypes.POINTER(ctypes.c_int)
+_UP = ctypes.POINTER(ctypes.c_ubyte)
+
+
+class _Blocks(ctypes.Structure):
+    _fields_ = [("nblocks", ctypes.c_int), ("nqn", ctypes.c_int), ("qnumbers", _DP), ("block_beg_end", _IP)]
+
+
+class _Basis(ctypes.Structure):
+    _fields_ = [("blocks", _Blocks), ("itype", _IP), ("st_came_from", _IP), ("en", _DP)]
+
+
+class _Matrix(ctypes.Structure):
+    _fields_ = [("nmatblocks", ctypes.c_int), ("mat_block_map", _IP), ("mat_block_beg_end", _IP),
+                ("mat_el", _DP)]
+
+
+class _EigCut(ctypes.Structure):
+    _fields_ = [("blocks", _Blocks), ("block_beg_end_bc", _IP), ("block_beg_end_eigvec", _IP),
+                ("st_came_from", _IP), ("en", _DP), ("kept", _UP), ("eigvec", _DP)]
+
+
+class _CutResult(ctypes.Structure):
+    _fields_ = [("en", _DP), ("kept", _UP), ("nkept", ctypes.c_int), ("ecut", ctypes.c_double),
+                ("cut", _EigCut)]
+
+
+class _Keep:
+    """Holds the numpy arrays a ctypes structure points into."""
+
+    def __init__(self):
+        self.refs = []
+
+    def d(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        self.refs.append(a)
+        return a.ctypes.data_as(_DP)
+
+    def i(self, a):
+        a = np.ascontiguousarray(a, dtype=np.int32)
+        self.refs.append(a)
+        return a.ctypes.data_as(_IP)
+
+    def blocks(self, qn, bbe):
+        qn = np.asarray(qn, dtype=np.float64).reshape(-1)
+        return _Blocks(len(qn) // 2, 2, self.d(qn), self.i(bbe))
+
+    def matrix(self, m):
+        mp, mbe, el = m
+        return _Matrix(len(mp) // 2, self.i(mp), self.i(mbe), self.d(el))
+
+
 _lib = None
 
 
@@ -94,6 +147,13 @@ def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     _dp = ctypes.POINTER(ctypes.c_double)
     _ip = ctypes.POINTER(ctypes.c_int)
     L.nrg_diag_blocks.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp, _dp, _dp]
+    L.nrg_diag_hn.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_int, ctypes.POINTER(_Blocks),
+                              ctypes.c_int, ctypes.POINTER(_Matrix), ctypes.POINTER(_Basis), _dp, _dp, _dp]
+    L.nrg_cut_states.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Blocks), _dp, _dp, ctypes.c_int,
+                                 ctypes.c_double, ctypes.POINTER(_CutResult)]
+    L.nrg_update_ops.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(_Blocks), ctypes.POINTER(_Basis),
+                                 ctypes.POINTER(_EigCut), ctypes.c_int, ctypes.POINTER(_Matrix),
+                                 ctypes.POINTER(_Matrix)]
     L.nrg_sweep_batch.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(SweepConfig), ctypes.c_int,
                                   ctypes.c_int, _dp, _dp, _ip, _dp]
     _lib = L
@@ -178,6 +238,76 @@ class Engine:
             out_e.append(ev[so:so + n]); out_v.append(vec[vo:vo + n * n].reshape(n, n))
             so += n; vo += n * n
         return out_e, out_v
+
+    # ---- per-step drop-ins (the NRG_main call sites) ----------------------
+    # Arrays follow the reference containers: qn (nblocks, 2) QNumbers,
+    # bbe [2*nblocks] inclusive BlockBegEnd, operators as (MatBlockMap,
+    # MatBlockBegEnd, MatEl) triples in the model's operator order.
+
+    def diag_hn(self, model: str, params, old_qn, old_bbe, ops, basis_qn, basis_bbe, itype, stcf, basis_en):
+        """CNRGmatrix::DiagHN + SetE0zero.  Returns (en, eigvec, emin): en the
+        E_min-shifted eigenvalues (ascending per block), eigvec the
+        block-concatenated n x n matrices (row k = eigenvector k)."""
+        k = _Keep()
+        params = np.ascontiguousarray(params, dtype=np.float64)
+        old = k.blocks(old_qn, old_bbe)
+        mats = (_Matrix * len(ops))(*[k.matrix(m) for m in ops])
+        basis = _Basis(k.blocks(basis_qn, basis_bbe), k.i(itype), k.i(stcf), k.d(basis_en))
+        bbe = np.asarray(basis_bbe, dtype=np.int64)
+        sizes = bbe[1::2] - bbe[0::2] + 1
+        en = np.empty(int(sizes.sum()), dtype=np.float64)
+        vec = np.empty(int((sizes ** 2).sum()), dtype=np.float64)
+        emin = ctypes.c_double()
+        self._check(self.L.nrg_diag_hn(self.h, MODELS[model], params.ctypes.data_as(_DP), len(params),
+                                       ctypes.byref(old), len(ops), mats, ctypes.byref(basis),
+                                       en.ctypes.data_as(_DP), vec.ctypes.data_as(_DP), ctypes.byref(emin)))
+        return en, vec, emin.value
+
+    def cut_states(self, qn, bbe, en, eigvec, ncutoff: int, degen_eps: float = 0.0) -> dict:
+        """SetKept + CutStates on Aeig.  Returns a dict with en/kept/nkept/ecut
+        (Aeig after SetKept) and AeigCut's qn, bbe, bbe_bc, bbe_eig, stcf,
+        cut_en, cut_kept, eigvec."""
+        k = _Keep()
+        blk = k.blocks(qn, bbe)
+        en = np.ascontiguousarray(en, dtype=np.float64)
+        evp = k.d(eigvec) if eigvec is not None else None
+        r = _CutResult()
+        self._check(self.L.nrg_cut_states(self.h, ctypes.byref(blk), en.ctypes.data_as(_DP), evp,
+                                          int(ncutoff), float(degen_eps), ctypes.byref(r)))
+        ns = len(en)
+        c = r.cut
+        nb = c.blocks.nblocks
+        bbe_c = _arr(c.blocks.block_beg_end, 2 * nb, np.int64)
+        nk = int(bbe_c[-1] + 1) if nb else 0
+        bbe_eig = _arr(c.block_beg_end_eigvec, 2 * nb, np.int64)
+        out = dict(en=_arr(r.en, ns, np.float64), kept=_arr(r.kept, ns, np.int64), nkept=r.nkept, ecut=r.ecut,
+                   qn=_arr(c.blocks.qnumbers, 2 * nb, np.float64), bbe=bbe_c,
+                   bbe_bc=_arr(c.block_beg_end_bc, 2 * nb, np.int64), bbe_eig=bbe_eig,
+                   stcf=_arr(c.st_came_from, nk, np.int64), cut_en=_arr(c.en, nk, np.float64),
+                   cut_kept=_arr(c.kept, nk, np.int64), eigvec=None)
+        if eigvec is not None:
+            out["eigvec"] = _arr(c.eigvec, int(bbe_eig[-1] + 1) if nb else 0, np.float64)
+        return out
+
+    def update_ops(self, model: str, old_qn, old_bbe, basis_qn, basis_bbe, itype, stcf, basis_en,
+                   cut_qn, cut_bbe, cut_bbe_eig, cut_eigvec, ops):
+        """UpdateMatrices for all of the model's operators.  Returns the new
+        operators as (MatBlockMap, MatBlockBegEnd, MatEl) triples."""
+        k = _Keep()
+        old = k.blocks(old_qn, old_bbe)
+        basis = _Basis(k.blocks(basis_qn, basis_bbe), k.i(itype), k.i(stcf), k.d(basis_en))
+        cut = _EigCut(k.blocks(cut_qn, cut_bbe), None, k.i(cut_bbe_eig), None, None, None, k.d(cut_eigvec))
+        mats = (_Matrix * len(ops))(*[k.matrix(m) for m in ops])
+        new = (_Matrix * len(ops))()
+        self._check(self.L.nrg_update_ops(self.h, MODELS[model], ctypes.byref(old), ctypes.byref(basis),
+                                          ctypes.byref(cut), len(ops), mats, new))
+        res = []
+        for m in new:
+            nmb = m.nmatblocks
+            mbe = _arr(m.mat_block_beg_end, 2 * nmb, np.int64)
+            nel = int(mbe.max() + 1) if nmb else 0
+            res.append((_arr(m.mat_block_map, 2 * nmb, np.int64), mbe, _arr(m.mat_el, nel, np.float64)))
+        return res
 
     def fp64_peak(self) -> float:
         """Measured FP64 FMA throughput of the device, TFLOP/s."""

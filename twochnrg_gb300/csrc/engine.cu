@@ -98,9 +98,10 @@ struct nrg_ctx {
   nrg::DevBuf meta, vmeta, H, d, e, tau, ev, en, flag, scal, Y, scratch, Z, Zt, T, partial, red, gpart;
   nrg::DevBuf ops_a[6], ops_b[6], opptr;
   cudaEvent_t ev_a[8];
-  // drop-in outputs (host)
-  std::vector<double> out_qn, out_en, out_vec, out_el;
-  std::vector<int> out_bbe, out_bbe_bc, out_stcf, out_map, out_mbe;
+  // drop-in outputs (host, valid until the next call on the context)
+  std::vector<double> out_en, out_qn, out_cut_en, out_vec, out_el;
+  std::vector<unsigned char> out_kept, out_cut_kept;
+  std::vector<int> out_bbe, out_bbe_bc, out_bbe_eig, out_stcf, out_map, out_mbe;
 };
 
 namespace nrg {
@@ -257,7 +258,7 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
   ea.ev = c->ev.as<double>(); ea.nstates = P.nstates; ea.flag = c->flag.as<int>();
   cudaEvent_t t1 = tm.start();
   launch_bisect(ea, d_state_block, c->stream);
-  c->launches++;
+  c->launches += 2;
   tm.stop(t1, &c->timing.tridiag_eig_ms);
 }
 
@@ -364,6 +365,200 @@ double opavg_host(const BlockArray& a, const std::vector<double>& en, const std:
   return s;
 }
 
+// Device tables of one DiagHN assembly, uploaded to c->meta.
+struct AsmTables {
+  EigPlan P;
+  std::vector<int> order;  // blocks, largest first
+  size_t o_bsize = 0, o_soff = 0, o_hoff = 0, o_order = 0, o_sb = 0, o_ri = 0, o_bq = 0;
+  AssembleArgs aa{};
+};
+
+// Builds and uploads everything the assembly kernel reads for basis B:
+// per-state rows (segment, old state, site type, E_old), per block the
+// (old block pair, operator) -> operator block offsets, the coefficient
+// tables, and sizes H/d/e/tau/ev/en for the blocks.  `oldops` describe the
+// operators (device pointers `hops`) in the old kept structure whose block
+// sizes are `old_size`.
+AsmTables prepare_assembly(nrg_ctx* c, const ModelSpec& m, const Basis& B, const HNTables& tabs,
+                           const std::vector<double>& st_eold, const std::vector<OpMeta>& oldops,
+                           const std::vector<int>& old_size, int nops_h, const std::vector<const double*>& hops,
+                           double lambda, const double chi[2], double eN) {
+  AsmTables T;
+  EigPlan& P = T.P;
+  const int nb = B.blk.nblocks();
+  plan_blocks(P, B.blk.size);
+  T.order.resize(nb);
+  for (int b = 0; b < nb; ++b) T.order[b] = b;
+  std::stable_sort(T.order.begin(), T.order.end(), [&](int x, int y) { return P.bsize[x] > P.bsize[y]; });
+  std::vector<int> state_block(P.nstates), row_index(P.nstates), st_seg(P.nstates), st_a(P.nstates),
+      st_type(P.nstates);
+  for (int b = 0; b < nb; ++b)
+    for (int i = 0; i < P.bsize[b]; ++i) {
+      int g = P.soff[b] + i;
+      state_block[g] = b; row_index[g] = i;
+      st_seg[g] = B.seg_of[g]; st_a[g] = B.a_of[g]; st_type[g] = B.itype[g];
+    }
+  std::vector<int> nseg(nb);
+  std::vector<int64_t> pair_base(nb), pair_fwd, pair_bwd;
+  std::vector<int> pair_fwd_ld, pair_bwd_ld;
+  for (int b = 0; b < nb; ++b) {
+    const auto& sg = B.seg[b];
+    nseg[b] = (int)sg.size();
+    pair_base[b] = (int64_t)pair_fwd.size();
+    for (size_t p = 0; p < sg.size(); ++p)
+      for (size_t q = 0; q < sg.size(); ++q)
+        for (int o = 0; o < nops_h; ++o) {
+          const OpMeta& om = oldops[o];
+          int kf = om.find(sg[p].old_block, sg[q].old_block);
+          int kb = om.find(sg[q].old_block, sg[p].old_block);
+          pair_fwd.push_back(kf >= 0 ? om.off[kf] : -1);
+          pair_fwd_ld.push_back(kf >= 0 ? old_size[om.bj[kf]] : 0);
+          pair_bwd.push_back(kb >= 0 ? om.off[kb] : -1);
+          pair_bwd_ld.push_back(kb >= 0 ? old_size[om.bj[kb]] : 0);
+        }
+  }
+  std::vector<double> site_q(m.site.nstates);
+  for (int t = 0; t < m.site.nstates; ++t) site_q[t] = m.site.blk.q(m.site.block_of_state(t), 0);
+  Packer pk;
+  T.o_bsize = pk.add(P.bsize); T.o_soff = pk.add(P.soff); T.o_hoff = pk.add(P.hoff); T.o_order = pk.add(T.order);
+  T.o_sb = pk.add(state_block); T.o_ri = pk.add(row_index);
+  size_t o_seg = pk.add(st_seg), o_a = pk.add(st_a), o_type = pk.add(st_type), o_eold = pk.add(st_eold),
+         o_nseg = pk.add(nseg), o_pb = pk.add(pair_base), o_pf = pk.add(pair_fwd), o_pfl = pk.add(pair_fwd_ld),
+         o_pbw = pk.add(pair_bwd), o_pbl = pk.add(pair_bwd_ld), o_coef = pk.add(tabs.coef), o_sq = pk.add(site_q);
+  T.o_bq = pk.add(B.blk.qn);
+  c->meta.ensure(pk.host.size() + 256);
+  h2d(c, c->meta.p, pk.host.data(), pk.host.size());
+  char* mb = c->meta.as<char>();
+  c->H.ensure(sizeof(double) * std::max<int64_t>(P.hsize, 1));
+  c->d.ensure(sizeof(double) * P.nstates); c->e.ensure(sizeof(double) * P.nstates);
+  c->tau.ensure(sizeof(double) * P.nstates); c->ev.ensure(sizeof(double) * P.nstates);
+  c->en.ensure(sizeof(double) * P.nstates);
+  c->red.ensure(sizeof(int) * (nb + 8));
+  c->opptr.ensure(sizeof(double*) * 32);
+  std::vector<const double*> ptrs(hops);
+  ptrs.resize(8, nullptr);
+  h2d(c, c->opptr.p, ptrs.data(), sizeof(double*) * ptrs.size());
+  AssembleArgs& aa = T.aa;
+  aa.nblocks = nb; aa.bsize = (const int*)(mb + T.o_bsize); aa.bstate = (const int*)(mb + T.o_soff);
+  aa.hoff = (const int64_t*)(mb + T.o_hoff); aa.seg_nseg = (const int*)(mb + o_nseg);
+  aa.st_seg = (const int*)(mb + o_seg); aa.st_a = (const int*)(mb + o_a); aa.st_type = (const int*)(mb + o_type);
+  aa.st_eold = (const double*)(mb + o_eold); aa.pair_base = (const int64_t*)(mb + o_pb);
+  aa.pair_fwd = (const int64_t*)(mb + o_pf); aa.pair_fwd_ld = (const int*)(mb + o_pfl);
+  aa.pair_bwd = (const int64_t*)(mb + o_pbw); aa.pair_bwd_ld = (const int*)(mb + o_pbl);
+  aa.coef = (const double*)(mb + o_coef); aa.ntypes = tabs.ntypes; aa.nchan = tabs.nchan; aa.nsigma = tabs.nsigma;
+  aa.nops_h = nops_h; aa.model = (int)m.kind; aa.ops = (const double* const*)c->opptr.p;
+  aa.sqrt_lambda = std::sqrt(lambda); aa.eN = eN; aa.chi[0] = chi[0]; aa.chi[1] = chi[1];
+  aa.site_q = (const double*)(mb + o_sq); aa.H = c->H.as<double>();
+  return T;
+}
+
+// UpdateMatrices for all operators: the host lists, per kept block pair
+// (i, j) allowed by CheckForMatEl, one rotation job Z_i F Z_j^T and the terms
+// of F (site factor x identity, or old operator block x identity), packed in
+// `up`.  The caller adds the operator pointer tables (o_old, o_new) and any
+// tables of its own to `up` before launch_update_plan.
+struct UpdatePlan {
+  std::vector<OpMeta> newops;
+  std::vector<RotJob> jobs;
+  std::vector<GatherTerm> terms, terms1;
+  std::vector<int> t1term, t1mn, gfirst, gcount, tjob, tmn;
+  int64_t tsize = 0;
+  Packer up;
+  size_t o_t1 = 0, o_t1t = 0, o_t1m = 0, o_terms = 0, o_gf = 0, o_gc = 0, o_jobs = 0, o_tj = 0, o_tm = 0;
+  size_t o_old = 0, o_new = 0;
+  char* ub = nullptr;  // device copy of `up` once launched
+};
+
+// kept: the new kept structure (K.src = block of B each kept block came
+// from); yoff/bsize: where each B block's kept eigenvector rows sit in c->Z
+// (kept x n, row-major) and c->Zt (n x kept).
+void plan_update(UpdatePlan& U, const ModelSpec& m, const Basis& B, const EigPlan& P, const Kept& K,
+                 const std::vector<OpMeta>& oldops) {
+  const int nops = (int)m.op_kind.size();
+  U.newops.assign(nops, OpMeta());
+  const int nk = K.blk.nblocks();
+  for (int o = 0; o < nops; ++o) {
+    OpMeta& no = U.newops[o];
+    for (int i = 0; i < nk; ++i)
+      for (int j = 0; j < nk; ++j) {
+        if (!op_check(m.op_check[o], K.blk, i, j)) continue;
+        const int bI = K.src[i], bJ = K.src[j];
+        RotJob J{};
+        J.ki = K.blk.size[i]; J.kj = K.blk.size[j]; J.nI = P.bsize[bI];
+        J.z_off = P.yoff[bI]; J.zt_off = P.yoff[bJ]; J.t_off = U.tsize; J.o_off = no.size; J.op = o;
+        no.bi.push_back(i); no.bj.push_back(j); no.off.push_back(no.size);
+        no.size += (int64_t)J.ki * J.kj;
+        U.tsize += (int64_t)J.nI * J.kj;
+        const int jid = (int)U.jobs.size();
+        U.jobs.push_back(J);
+        const double SI = B.blk.q(bI, 1), SJ = B.blk.q(bJ, 1);
+        const auto& segI = B.seg[bI];
+        const auto& segJ = B.seg[bJ];
+        for (const Segment& p : segI)
+          for (int u = 0; u < p.nsite; ++u) {
+            const int tu_ = m.site.blk.offset[p.site_block] + u;
+            const int first = (int)U.terms.size();
+            for (const Segment& q : segJ)
+              for (int v = 0; v < q.nsite; ++v) {
+                const int tv = m.site.blk.offset[q.site_block] + v;
+                GatherTerm G{};
+                G.job = jid; G.dst_base = p.offset + u; G.dst_stride = p.nsite; G.rows = p.count;
+                G.src_base = q.offset + v; G.src_stride = q.nsite; G.srows = q.count;
+                if (m.op_kind[o] == OP_IMPONLY) {
+                  if (tu_ != tv) continue;
+                  const OpMeta& om = oldops[o];
+                  int kx = om.find(p.old_block, q.old_block);
+                  if (kx < 0) continue;
+                  G.mode = 1; G.coef = 1.0; G.old_off = om.off[kx]; G.op = o;
+                } else {
+                  if (p.old_block != q.old_block) continue;
+                  double g = op_site_factor(m, m.op_kind[o], SI, SJ, tu_, tv);
+                  if (g == 0.0) continue;
+                  G.mode = 0; G.coef = g;
+                }
+                if (G.mode == 1) {  // old block x Zt rows: tiled GEMM, one destination per term
+                  const int tid1 = (int)U.terms1.size();
+                  U.terms1.push_back(G);
+                  for (int mt = 0; mt * 64 < G.rows; ++mt)
+                    for (int nt = 0; nt * 64 < J.kj; ++nt) { U.t1term.push_back(tid1); U.t1mn.push_back((mt << 16) | nt); }
+                  continue;
+                }
+                U.terms.push_back(G);
+              }
+            if ((int)U.terms.size() > first) { U.gfirst.push_back(first); U.gcount.push_back((int)U.terms.size() - first); }
+          }
+        for (int mt = 0; mt * 64 < J.ki; ++mt)
+          for (int nt = 0; nt * 64 < J.kj; ++nt) { U.tjob.push_back(jid); U.tmn.push_back((mt << 16) | nt); }
+      }
+  }
+  U.o_t1 = U.up.add(U.terms1); U.o_t1t = U.up.add(U.t1term); U.o_t1m = U.up.add(U.t1mn);
+  U.o_terms = U.up.add(U.terms); U.o_gf = U.up.add(U.gfirst); U.o_gc = U.up.add(U.gcount);
+  U.o_jobs = U.up.add(U.jobs); U.o_tj = U.up.add(U.tjob); U.o_tm = U.up.add(U.tmn);
+}
+
+void launch_update_plan(nrg_ctx* c, Timer& tm, UpdatePlan& U) {
+  cudaEvent_t tu = tm.start();
+  const size_t tbytes = sizeof(double) * std::max<int64_t>(U.tsize, 1);
+  c->T.ensure(tbytes + U.up.host.size() + 512);
+  U.ub = c->T.as<char>() + ((tbytes + 255) & ~size_t(255));
+  h2d(c, U.ub, U.up.host.data(), U.up.host.size());
+  CU(cudaMemsetAsync(c->T.p, 0, tbytes, c->stream));
+  char* ub = U.ub;
+  UpdateArgs ua{};
+  ua.terms = (const GatherTerm*)(ub + U.o_terms); ua.group_first = (const int*)(ub + U.o_gf);
+  ua.group_count = (const int*)(ub + U.o_gc); ua.ngroups = (int)U.gfirst.size(); ua.jobs = (const RotJob*)(ub + U.o_jobs);
+  ua.Z = c->Z.as<double>(); ua.Zt = c->Zt.as<double>(); ua.T = c->T.as<double>();
+  ua.old_ops = (const double* const*)(ub + U.o_old); ua.new_ops = (double* const*)(ub + U.o_new);
+  ua.tile_job = (const int*)(ub + U.o_tj); ua.tile_mn = (const int*)(ub + U.o_tm); ua.ntiles = (int)U.tjob.size();
+  ua.terms1 = (const GatherTerm*)(ub + U.o_t1); ua.tile1_term = (const int*)(ub + U.o_t1t);
+  ua.tile1_mn = (const int*)(ub + U.o_t1m); ua.ntiles1 = (int)U.t1term.size();
+  launch_update(ua, c->stream);
+  if (ua.ntiles1 > 0) c->launches++;
+  c->launches += 2;
+  for (const RotJob& J : U.jobs) c->timing.update_flops += 2.0 * J.ki * (double)J.nI * J.kj;
+  tm.stop(tu, &c->timing.update_ms);
+}
+
 void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
   using clock = std::chrono::steady_clock;
   auto t_begin = clock::now();
@@ -430,74 +625,19 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
     HNTables tabs;
     build_hn_tables(m, B, tabs);
     const int nb = B.blk.nblocks();
-    EigPlan P;
-    plan_blocks(P, B.blk.size);
-    std::vector<int> order(nb);
-    for (int b = 0; b < nb; ++b) order[b] = b;
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return P.bsize[x] > P.bsize[y]; });
-    std::vector<int> state_block(P.nstates), row_index(P.nstates), st_seg(P.nstates), st_a(P.nstates),
-        st_type(P.nstates);
-    std::vector<double> st_eold(P.nstates);
-    for (int b = 0; b < nb; ++b)
-      for (int i = 0; i < P.bsize[b]; ++i) {
-        int g = P.soff[b] + i;
-        state_block[g] = b; row_index[g] = i;
-        st_seg[g] = B.seg_of[g]; st_a[g] = B.a_of[g]; st_type[g] = B.itype[g];
-        st_eold[g] = kept_en[B.stcf[g]];
-      }
-    std::vector<int> nseg(nb);
-    std::vector<int64_t> pair_base(nb), pair_fwd, pair_bwd;
-    std::vector<int> pair_fwd_ld, pair_bwd_ld;
-    for (int b = 0; b < nb; ++b) {
-      const auto& sg = B.seg[b];
-      nseg[b] = (int)sg.size();
-      pair_base[b] = (int64_t)pair_fwd.size();
-      for (size_t p = 0; p < sg.size(); ++p)
-        for (size_t q = 0; q < sg.size(); ++q)
-          for (int o = 0; o < nops_h; ++o) {
-            const OpMeta& om = S.ops[o];
-            int kf = om.find(sg[p].old_block, sg[q].old_block);
-            int kb = om.find(sg[q].old_block, sg[p].old_block);
-            pair_fwd.push_back(kf >= 0 ? om.off[kf] : -1);
-            pair_fwd_ld.push_back(kf >= 0 ? S.kept.blk.size[om.bj[kf]] : 0);
-            pair_bwd.push_back(kb >= 0 ? om.off[kb] : -1);
-            pair_bwd_ld.push_back(kb >= 0 ? S.kept.blk.size[om.bj[kb]] : 0);
-          }
-    }
-    std::vector<double> site_q(m.site.nstates);
-    for (int t = 0; t < m.site.nstates; ++t) site_q[t] = m.site.blk.q(m.site.block_of_state(t), 0);
-    Packer pk;
-    size_t o_bsize = pk.add(P.bsize), o_soff = pk.add(P.soff), o_hoff = pk.add(P.hoff), o_order = pk.add(order),
-           o_sb = pk.add(state_block), o_ri = pk.add(row_index), o_seg = pk.add(st_seg), o_a = pk.add(st_a),
-           o_type = pk.add(st_type), o_eold = pk.add(st_eold), o_nseg = pk.add(nseg), o_pb = pk.add(pair_base),
-           o_pf = pk.add(pair_fwd), o_pfl = pk.add(pair_fwd_ld), o_pbw = pk.add(pair_bwd), o_pbl = pk.add(pair_bwd_ld),
-           o_coef = pk.add(tabs.coef), o_sq = pk.add(site_q), o_bq = pk.add(B.blk.qn);
-    c->meta.ensure(pk.host.size() + 256);
-    h2d(c, c->meta.p, pk.host.data(), pk.host.size());
-    char* mb = c->meta.as<char>();
-    c->H.ensure(sizeof(double) * std::max<int64_t>(P.hsize, 1));
-    c->d.ensure(sizeof(double) * P.nstates); c->e.ensure(sizeof(double) * P.nstates);
-    c->tau.ensure(sizeof(double) * P.nstates); c->ev.ensure(sizeof(double) * P.nstates);
-    c->en.ensure(sizeof(double) * P.nstates);
-    c->red.ensure(sizeof(int) * (nb + 8));
-    // operator pointer table
+    std::vector<double> st_eold(B.stcf.size());
+    for (size_t g = 0; g < B.stcf.size(); ++g) st_eold[g] = kept_en[B.stcf[g]];
     std::vector<const double*> hops(8, nullptr);
     for (int o = 0; o < nops; ++o) hops[o] = S.opbuf(S.cur, o)->as<double>();
-    h2d(c, c->opptr.p, hops.data(), sizeof(double*) * hops.size());
-    // ---------------- assembly
-    AssembleArgs aa{};
-    aa.nblocks = nb; aa.bsize = (const int*)(mb + o_bsize); aa.bstate = (const int*)(mb + o_soff);
-    aa.hoff = (const int64_t*)(mb + o_hoff); aa.seg_nseg = (const int*)(mb + o_nseg);
-    aa.st_seg = (const int*)(mb + o_seg); aa.st_a = (const int*)(mb + o_a); aa.st_type = (const int*)(mb + o_type);
-    aa.st_eold = (const double*)(mb + o_eold); aa.pair_base = (const int64_t*)(mb + o_pb);
-    aa.pair_fwd = (const int64_t*)(mb + o_pf); aa.pair_fwd_ld = (const int*)(mb + o_pfl);
-    aa.pair_bwd = (const int64_t*)(mb + o_pbw); aa.pair_bwd_ld = (const int*)(mb + o_pbl);
-    aa.coef = (const double*)(mb + o_coef); aa.ntypes = tabs.ntypes; aa.nchan = tabs.nchan; aa.nsigma = tabs.nsigma;
-    aa.nops_h = nops_h; aa.model = (int)m.kind; aa.ops = (const double* const*)c->opptr.p;
-    aa.sqrt_lambda = std::sqrt(lambda); aa.eN = eN; aa.chi[0] = chi[0]; aa.chi[1] = chi[1];
-    aa.site_q = (const double*)(mb + o_sq); aa.H = c->H.as<double>();
+    AsmTables AT = prepare_assembly(c, m, B, tabs, st_eold, S.ops, S.kept.blk.size, nops_h, hops, lambda, chi, eN);
+    EigPlan& P = AT.P;
+    std::vector<int>& order = AT.order;
+    char* mb = c->meta.as<char>();
+    const size_t o_order = AT.o_order, o_bsize = AT.o_bsize, o_hoff = AT.o_hoff, o_soff = AT.o_soff,
+                 o_sb = AT.o_sb, o_bq = AT.o_bq;
+    AssembleArgs& aa = AT.aa;
     cudaEvent_t ta = tm.start();
-    launch_assemble(aa, P.nstates, (const int*)(mb + o_sb), (const int*)(mb + o_ri), c->stream);
+    launch_assemble(aa, P.nstates, (const int*)(mb + o_sb), (const int*)(mb + AT.o_ri), c->stream);
     c->launches++;
     tm.stop(ta, &c->timing.assemble_ms);
     // ---------------- tridiagonalization + eigenvalues
@@ -556,68 +696,10 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
     // eigenvalues for clustering: shifted energies have the same gaps
     run_vectors(c, tm, P, R.en, aa.bsize, aa.hoff, aa.bstate);
     // ---------------- UpdateMatrices
-    cudaEvent_t tu = tm.start();
-    std::vector<OpMeta> newops(nops);
-    std::vector<RotJob> jobs;
-    std::vector<GatherTerm> terms, terms1;
-    std::vector<int> t1term, t1mn;
-    std::vector<int> gfirst, gcount, tjob, tmn;
-    int64_t tsize = 0;
+    UpdatePlan U;
+    plan_update(U, m, B, P, K, S.ops);
+    std::vector<OpMeta>& newops = U.newops;
     const int nk = K.blk.nblocks();
-    for (int o = 0; o < nops; ++o) {
-      OpMeta& no = newops[o];
-      for (int i = 0; i < nk; ++i)
-        for (int j = 0; j < nk; ++j) {
-          if (!op_check(m.op_check[o], K.blk, i, j)) continue;
-          const int bI = K.src[i], bJ = K.src[j];
-          RotJob J{};
-          J.ki = K.blk.size[i]; J.kj = K.blk.size[j]; J.nI = P.bsize[bI];
-          J.z_off = P.yoff[bI]; J.zt_off = P.yoff[bJ]; J.t_off = tsize; J.o_off = no.size; J.op = o;
-          no.bi.push_back(i); no.bj.push_back(j); no.off.push_back(no.size);
-          no.size += (int64_t)J.ki * J.kj;
-          tsize += (int64_t)J.nI * J.kj;
-          const int jid = (int)jobs.size();
-          jobs.push_back(J);
-          const double SI = B.blk.q(bI, 1), SJ = B.blk.q(bJ, 1);
-          const auto& segI = B.seg[bI];
-          const auto& segJ = B.seg[bJ];
-          for (const Segment& p : segI)
-            for (int u = 0; u < p.nsite; ++u) {
-              const int tu_ = m.site.blk.offset[p.site_block] + u;
-              const int first = (int)terms.size();
-              for (const Segment& q : segJ)
-                for (int v = 0; v < q.nsite; ++v) {
-                  const int tv = m.site.blk.offset[q.site_block] + v;
-                  GatherTerm G{};
-                  G.job = jid; G.dst_base = p.offset + u; G.dst_stride = p.nsite; G.rows = p.count;
-                  G.src_base = q.offset + v; G.src_stride = q.nsite; G.srows = q.count;
-                  if (m.op_kind[o] == OP_IMPONLY) {
-                    if (tu_ != tv) continue;
-                    const OpMeta& om = S.ops[o];
-                    int kx = om.find(p.old_block, q.old_block);
-                    if (kx < 0) continue;
-                    G.mode = 1; G.coef = 1.0; G.old_off = om.off[kx]; G.op = o;
-                  } else {
-                    if (p.old_block != q.old_block) continue;
-                    double g = op_site_factor(m, m.op_kind[o], SI, SJ, tu_, tv);
-                    if (g == 0.0) continue;
-                    G.mode = 0; G.coef = g;
-                  }
-                  if (G.mode == 1) {  // old block x Zt rows: tiled GEMM, one destination per term
-                    const int tid1 = (int)terms1.size();
-                    terms1.push_back(G);
-                    for (int mt = 0; mt * 64 < G.rows; ++mt)
-                      for (int nt = 0; nt * 64 < J.kj; ++nt) { t1term.push_back(tid1); t1mn.push_back((mt << 16) | nt); }
-                    continue;
-                  }
-                  terms.push_back(G);
-                }
-              if ((int)terms.size() > first) { gfirst.push_back(first); gcount.push_back((int)terms.size() - first); }
-            }
-          for (int mt = 0; mt * 64 < J.ki; ++mt)
-            for (int nt = 0; nt * 64 < J.kj; ++nt) { tjob.push_back(jid); tmn.push_back((mt << 16) | nt); }
-        }
-    }
     int nxt = 1 - S.cur;
     std::vector<double*> newptr(8, nullptr), oldptr(8, nullptr);
     for (int o = 0; o < nops; ++o) {
@@ -626,11 +708,9 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
       newptr[o] = b->as<double>();
       oldptr[o] = S.opbuf(S.cur, o)->as<double>();
     }
-    Packer up;
-    size_t o_t1 = up.add(terms1), o_t1t = up.add(t1term), o_t1m = up.add(t1mn);
-    size_t o_terms = up.add(terms), o_gf = up.add(gfirst), o_gc = up.add(gcount), o_jobs = up.add(jobs),
-           o_tj = up.add(tjob), o_tm = up.add(tmn), o_old = up.add(oldptr), o_new = up.add(newptr),
-           o_ken = up.add(new_kept_en);
+    Packer& up = U.up;
+    U.o_old = up.add(oldptr); U.o_new = up.add(newptr);
+    size_t o_ken = up.add(new_kept_en);
     // kept-state tables for the operator averages
     std::vector<int> kstate_block, ksz = K.blk.size, koff = K.blk.offset;
     for (int i = 0; i < nk; ++i) for (int x = 0; x < K.blk.size[i]; ++x) kstate_block.push_back(i);
@@ -644,23 +724,8 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
     }
     size_t o_ksb = up.add(kstate_block), o_ksz = up.add(ksz), o_koff = up.add(koff), o_doff = up.add(diag_off),
            o_avp = up.add(avgptr), o_kq = up.add(K.blk.qn);
-    c->T.ensure(sizeof(double) * std::max<int64_t>(tsize, 1) + up.host.size() + 512);
-    char* ub = c->T.as<char>() + ((sizeof(double) * std::max<int64_t>(tsize, 1) + 255) & ~size_t(255));
-    h2d(c, ub, up.host.data(), up.host.size());
-    CU(cudaMemsetAsync(c->T.p, 0, sizeof(double) * std::max<int64_t>(tsize, 1), c->stream));
-    UpdateArgs ua{};
-    ua.terms = (const GatherTerm*)(ub + o_terms); ua.group_first = (const int*)(ub + o_gf);
-    ua.group_count = (const int*)(ub + o_gc); ua.ngroups = (int)gfirst.size(); ua.jobs = (const RotJob*)(ub + o_jobs);
-    ua.Z = c->Z.as<double>(); ua.Zt = c->Zt.as<double>(); ua.T = c->T.as<double>();
-    ua.old_ops = (const double* const*)(ub + o_old); ua.new_ops = (double* const*)(ub + o_new);
-    ua.tile_job = (const int*)(ub + o_tj); ua.tile_mn = (const int*)(ub + o_tm); ua.ntiles = (int)tjob.size();
-    ua.terms1 = (const GatherTerm*)(ub + o_t1); ua.tile1_term = (const int*)(ub + o_t1t);
-    ua.tile1_mn = (const int*)(ub + o_t1m); ua.ntiles1 = (int)t1term.size();
-    launch_update(ua, c->stream);
-    if (ua.ntiles1 > 0) c->launches++;
-    c->launches += 2;
-    for (const RotJob& J : jobs) c->timing.update_flops += 2.0 * J.ki * (double)J.nI * J.kj;
-    tm.stop(tu, &c->timing.update_ms);
+    launch_update_plan(c, tm, U);
+    char* ub = U.ub;
     // ---------------- CalcStuff: operator averages over the kept states
     cudaEvent_t to = tm.start();
     OpDiagArgs od{};
@@ -747,6 +812,324 @@ void diag_blocks_impl(nrg_ctx* c, int nb, const int* sizes, const double* packed
   check_flag(c);
   tm.collect();
   std::memcpy(evals, ev.data(), sizeof(double) * P.nstates);
+}
+
+// ------------------------------------------------------------------ per-step drop-ins
+// Reference containers crossing the ABI are checked and turned into the
+// engine's block structures here.
+BlockArray blocks_from_abi(const nrg_blocks* b, const char* what) {
+  if (!b || b->nblocks < 0 || (b->nblocks > 0 && (!b->qnumbers || !b->block_beg_end)))
+    throw NrgError(NRG_ERR_ARG, std::string(what) + ": missing block structure");
+  if (b->nqn != 2) throw NrgError(NRG_ERR_ARG, std::string(what) + ": expected 2 quantum numbers per block");
+  BlockArray a;
+  a.nqn = 2;
+  int next = 0;
+  for (int k = 0; k < b->nblocks; ++k) {
+    const int beg = b->block_beg_end[2 * k], end = b->block_beg_end[2 * k + 1];
+    if (beg != next || end < beg)
+      throw NrgError(NRG_ERR_ARG, std::string(what) + ": BlockBegEnd must tile the states in order");
+    a.push(&b->qnumbers[2 * k], end - beg + 1);
+    next = end + 1;
+  }
+  return a;
+}
+
+ModelSpec model_from_abi(int model) {
+  if (model < 0 || model > 2) throw NrgError(NRG_ERR_ARG, "unknown model");
+  return make_model((ModelKind)model);
+}
+
+// BuildBasis of `kept` must reproduce the caller's basis: the assembly and
+// rotation tables are derived from that layout (BuildBasis.cpp:292-403).
+void check_basis(const Basis& B, const nrg_basis* ab) {
+  if (!ab) throw NrgError(NRG_ERR_ARG, "abasis is NULL");
+  const nrg_blocks& bb = ab->blocks;
+  if (bb.nqn != 2 || bb.nblocks != B.blk.nblocks())
+    throw NrgError(NRG_ERR_SYNC, "abasis blocks differ from BuildBasis of the kept array");
+  for (int k = 0; k < bb.nblocks; ++k) {
+    if (bb.qnumbers[2 * k] != B.blk.qn[2 * k] || bb.qnumbers[2 * k + 1] != B.blk.qn[2 * k + 1] ||
+        bb.block_beg_end[2 * k] != B.blk.offset[k] || bb.block_beg_end[2 * k + 1] != B.blk.offset[k] + B.blk.size[k] - 1)
+      throw NrgError(NRG_ERR_SYNC, "abasis blocks differ from BuildBasis of the kept array");
+  }
+  const int ns = B.blk.nstates();
+  if (ns > 0 && (!ab->itype || !ab->st_came_from || !ab->en)) throw NrgError(NRG_ERR_ARG, "abasis arrays missing");
+  for (int g = 0; g < ns; ++g)
+    if (ab->itype[g] != B.itype[g] || ab->st_came_from[g] != B.stcf[g])
+      throw NrgError(NRG_ERR_SYNC, "abasis iType/StCameFrom differ from BuildBasis of the kept array");
+}
+
+// A reference operator in the engine's storage (same row-major blocks):
+// pair list, offsets and element count, after range checks.
+OpMeta op_from_abi(const nrg_matrix& M, const BlockArray& blk, int64_t* nel) {
+  OpMeta om;
+  if (M.nmatblocks < 0 || (M.nmatblocks > 0 && (!M.mat_block_map || !M.mat_block_beg_end || !M.mat_el)))
+    throw NrgError(NRG_ERR_ARG, "operator arrays missing");
+  int64_t top = 0;
+  for (int k = 0; k < M.nmatblocks; ++k) {
+    const int i = M.mat_block_map[2 * k], j = M.mat_block_map[2 * k + 1];
+    const int beg = M.mat_block_beg_end[2 * k], end = M.mat_block_beg_end[2 * k + 1];
+    if (i < 0 || j < 0 || i >= blk.nblocks() || j >= blk.nblocks())
+      throw NrgError(NRG_ERR_SYNC, "MatBlockMap names a block outside the kept structure");
+    if (beg < 0 || (int64_t)end - beg + 1 != (int64_t)blk.size[i] * blk.size[j])
+      throw NrgError(NRG_ERR_SYNC, "MatBlockBegEnd does not match the block sizes");
+    om.bi.push_back(i); om.bj.push_back(j); om.off.push_back(beg);
+    top = std::max<int64_t>(top, (int64_t)end + 1);
+  }
+  om.size = top;
+  *nel = top;
+  return om;
+}
+
+// DiagHN + SetE0zero for a caller-given basis (all eigenvectors).
+void diag_hn_impl(nrg_ctx* c, int model, const double* params, int nparams, const nrg_blocks* old_kept, int nops,
+                  const nrg_matrix* ops, const nrg_basis* abasis, double* en_out, double* evec_out, double* emin_out) {
+  const ModelSpec m = model_from_abi(model);
+  if (!params || nparams < m.nchan + 2) throw NrgError(NRG_ERR_ARG, "ParamsHN needs Lambda, chi per channel and e_N");
+  if (nparams > m.nchan + 2 && params[m.nchan + 2] != 0.0)
+    throw NrgError(NRG_ERR_ARG, "superconducting leads (Delta_SC != 0) are not supported");
+  if (!(params[0] > 1.0)) throw NrgError(NRG_ERR_ARG, "Lambda must exceed 1");
+  const int nops_h = m.kind == MODEL_1CHQS ? 1 : 2;
+  if (nops < nops_h || !ops) throw NrgError(NRG_ERR_ARG, "the model's f operators are required");
+  if (!en_out || !evec_out) throw NrgError(NRG_ERR_ARG, "output arrays are NULL");
+  std::memset(&c->timing, 0, sizeof(c->timing));
+  const BlockArray K = blocks_from_abi(old_kept, "old_kept");
+  Basis B;
+  build_basis(m, K, B);
+  check_basis(B, abasis);
+  if (B.blk.nblocks() == 0) throw NrgError(NRG_ERR_ARG, "empty basis");
+  HNTables tabs;
+  build_hn_tables(m, B, tabs);
+  std::vector<OpMeta> oldops(nops_h);
+  std::vector<const double*> hops(8, nullptr);
+  for (int o = 0; o < nops_h; ++o) {
+    int64_t nel = 0;
+    oldops[o] = op_from_abi(ops[o], K, &nel);
+    c->ops_a[o].ensure(sizeof(double) * std::max<int64_t>(nel, 1));
+    h2d(c, c->ops_a[o].p, ops[o].mat_el, sizeof(double) * nel);
+    hops[o] = c->ops_a[o].as<double>();
+  }
+  const int ns = B.blk.nstates();
+  std::vector<double> st_eold(abasis->en, abasis->en + ns);
+  const double chi[2] = {params[1], m.nchan == 2 ? params[2] : 0.0};
+  const double eN = params[1 + m.nchan];
+  Timer tm(c);
+  c->flag.ensure(sizeof(int) * 4);
+  CU(cudaMemsetAsync(c->flag.p, 0, sizeof(int), c->stream));
+  AsmTables AT = prepare_assembly(c, m, B, tabs, st_eold, oldops, K.size, nops_h, hops, params[0], chi, eN);
+  EigPlan& P = AT.P;
+  char* mb = c->meta.as<char>();
+  cudaEvent_t ta = tm.start();
+  launch_assemble(AT.aa, P.nstates, (const int*)(mb + AT.o_sb), (const int*)(mb + AT.o_ri), c->stream);
+  c->launches++;
+  tm.stop(ta, &c->timing.assemble_ms);
+  run_tridiag_and_bisect(c, tm, P, AT.order, (const int*)(mb + AT.o_order), (const int*)(mb + AT.o_bsize),
+                         (const int64_t*)(mb + AT.o_hoff), (const int*)(mb + AT.o_soff), (const int*)(mb + AT.o_sb));
+  std::vector<double> ev(P.nstates);
+  d2h(c, ev.data(), c->ev.p, sizeof(double) * P.nstates);
+  CU(cudaStreamSynchronize(c->stream));
+  check_flag(c);
+  P.nvec = P.bsize;
+  run_vectors(c, tm, P, ev, AT.aa.bsize, AT.aa.hoff, AT.aa.bstate);
+  d2h(c, evec_out, c->Z.p, sizeof(double) * (size_t)P.ysize);
+  CU(cudaStreamSynchronize(c->stream));
+  check_flag(c);
+  tm.collect();
+  // SetE0zero (NRGarrayClass.cpp:234-241).
+  const double emin = *std::min_element(ev.begin(), ev.end());
+  for (int g = 0; g < P.nstates; ++g) en_out[g] = ev[g] - emin;
+  if (emin_out) *emin_out = emin;
+}
+
+// SetKept + CutStates on the device cut kernels; the AeigCut bookkeeping is
+// the host loop of CutStates.cpp:10-95 over the per-block kept counts.
+void cut_states_impl(nrg_ctx* c, const nrg_blocks* aeig, const double* en, const double* evec, int ncutoff,
+                     double eps, nrg_cut_result* out) {
+  if (!en || !out) throw NrgError(NRG_ERR_ARG, "en/out is NULL");
+  if (ncutoff < 1) throw NrgError(NRG_ERR_ARG, "Ncutoff must be positive");
+  const BlockArray A = blocks_from_abi(aeig, "aeig");
+  const int nb = A.nblocks(), ns = A.nstates();
+  if (ns == 0) throw NrgError(NRG_ERR_ARG, "no states");
+  double mn = en[0];
+  for (int g = 1; g < ns; ++g) mn = std::min(mn, en[g]);
+  if (mn != 0.0) throw NrgError(NRG_ERR_ARG, "energies must be E_min-shifted (SetE0zero) as DiagHN leaves them");
+  std::memset(&c->timing, 0, sizeof(c->timing));
+  Timer tm(c);
+  EigPlan P;
+  plan_blocks(P, A.size);
+  std::vector<int> state_block(ns);
+  for (int b = 0; b < nb; ++b) for (int i = 0; i < P.bsize[b]; ++i) state_block[P.soff[b] + i] = b;
+  Packer pk;
+  size_t o_bsize = pk.add(P.bsize), o_soff = pk.add(P.soff);
+  c->meta.ensure(pk.host.size() + 256);
+  c->ev.ensure(sizeof(double) * ns); c->en.ensure(sizeof(double) * ns);
+  c->red.ensure(sizeof(int) * (nb + 8));
+  c->scal.ensure(sizeof(double) * 32);
+  c->flag.ensure(sizeof(int) * 4);
+  CU(cudaMemsetAsync(c->flag.p, 0, sizeof(int), c->stream));
+  h2d(c, c->meta.p, pk.host.data(), pk.host.size());
+  h2d(c, c->ev.p, en, sizeof(double) * ns);
+  char* mb = c->meta.as<char>();
+  cudaEvent_t tc = tm.start();
+  CutArgs ca{};
+  ca.nstates = ns; ca.ev = c->ev.as<double>(); ca.en = c->en.as<double>(); ca.ncutoff = ncutoff; ca.eps = eps;
+  ca.out_scalars = c->scal.as<double>(); ca.flag = c->flag.as<int>();
+  launch_cut(ca, c->stream);
+  BlockStatsArgs bs{};
+  bs.nblocks = nb; bs.bsize = (const int*)(mb + o_bsize); bs.soff = (const int*)(mb + o_soff);
+  bs.en = c->en.as<double>(); bs.scalars = ca.out_scalars; bs.kept = c->red.as<int>() + 4;
+  launch_block_stats(bs, c->stream);
+  c->launches += 2;
+  std::vector<double> scal(4);
+  std::vector<int> keptb(nb);
+  c->out_en.resize(ns);
+  d2h(c, scal.data(), c->scal.p, sizeof(double) * 4);
+  d2h(c, keptb.data(), bs.kept, sizeof(int) * nb);
+  d2h(c, c->out_en.data(), c->en.p, sizeof(double) * ns);
+  tm.stop(tc, &c->timing.cut_ms);
+  CU(cudaStreamSynchronize(c->stream));
+  check_flag(c);
+  tm.collect();
+  const double ecut = scal[1];
+  c->out_kept.assign(ns, 0);
+  int nkept = 0;
+  for (int g = 0; g < ns; ++g) if (c->out_en[g] <= ecut) { c->out_kept[g] = 1; ++nkept; }
+  c->out_qn.clear(); c->out_bbe.clear(); c->out_bbe_bc.clear(); c->out_bbe_eig.clear(); c->out_stcf.clear();
+  c->out_cut_en.clear(); c->out_cut_kept.clear(); c->out_vec.clear();
+  int ist = 0;
+  int64_t eig = 0, eoff = 0;
+  for (int b = 0; b < nb; ++b) {
+    const int n = P.bsize[b], k = keptb[b], b0 = P.soff[b];
+    if (k > 0) {
+      c->out_qn.push_back(A.q(b, 0)); c->out_qn.push_back(A.q(b, 1));
+      c->out_bbe.push_back(ist); c->out_bbe.push_back(ist + k - 1);
+      c->out_bbe_bc.push_back(b0); c->out_bbe_bc.push_back(b0 + n - 1);
+      c->out_bbe_eig.push_back((int)eig); c->out_bbe_eig.push_back((int)(eig + (int64_t)k * n - 1));
+      for (int i = 0; i < k; ++i) {
+        c->out_stcf.push_back(b0 + i);
+        c->out_cut_en.push_back(c->out_en[b0 + i]);
+        c->out_cut_kept.push_back(c->out_kept[b0 + i]);
+      }
+      if (evec) c->out_vec.insert(c->out_vec.end(), evec + eoff, evec + eoff + (int64_t)k * n);
+      eig += (int64_t)k * n;
+      ist += k;
+    }
+    eoff += (int64_t)n * n;
+  }
+  out->en = c->out_en.data();
+  out->kept = c->out_kept.data();
+  out->nkept = nkept;
+  out->ecut = ecut;
+  nrg_eigcut& cut = out->cut;
+  cut.blocks.nblocks = (int)c->out_bbe.size() / 2;
+  cut.blocks.nqn = 2;
+  cut.blocks.qnumbers = c->out_qn.data();
+  cut.blocks.block_beg_end = c->out_bbe.data();
+  cut.block_beg_end_bc = c->out_bbe_bc.data();
+  cut.block_beg_end_eigvec = c->out_bbe_eig.data();
+  cut.st_came_from = c->out_stcf.data();
+  cut.en = c->out_cut_en.data();
+  cut.kept = c->out_cut_kept.data();
+  cut.eigvec = evec ? c->out_vec.data() : nullptr;
+}
+
+// UpdateMatrices for a caller-given AeigCut (kept rows of the eigenvectors
+// uploaded as Z and Z^T) and old operators.
+void update_ops_impl(nrg_ctx* c, int model, const nrg_blocks* old_kept, const nrg_basis* abasis, const nrg_eigcut* acut,
+                     int nops, const nrg_matrix* old_ops, nrg_matrix* new_ops) {
+  const ModelSpec m = model_from_abi(model);
+  if (nops != (int)m.op_kind.size() || !old_ops || !new_ops)
+    throw NrgError(NRG_ERR_ARG, "nops must equal the model's operator count");
+  if (!acut) throw NrgError(NRG_ERR_ARG, "acut is NULL");
+  std::memset(&c->timing, 0, sizeof(c->timing));
+  const BlockArray Kold = blocks_from_abi(old_kept, "old_kept");
+  Basis B;
+  build_basis(m, Kold, B);
+  check_basis(B, abasis);
+  Kept K;
+  K.blk = blocks_from_abi(&acut->blocks, "acut");
+  const int nk = K.blk.nblocks(), nb = B.blk.nblocks();
+  if (nk > 0 && (!acut->eigvec || !acut->block_beg_end_eigvec)) throw NrgError(NRG_ERR_ARG, "acut eigvec missing");
+  EigPlan P;
+  plan_blocks(P, B.blk.size);
+  P.nvec.assign(nb, 0);
+  for (int i = 0; i < nk; ++i) {
+    const int b = B.blk.find(&K.blk.qn[2 * i]);  // FindMatchBlock (FindMatchBlock.cpp:5-24)
+    if (b < 0) throw NrgError(NRG_ERR_SYNC, "a kept block has no match in abasis");
+    if (K.blk.size[i] > P.bsize[b]) throw NrgError(NRG_ERR_SYNC, "kept block larger than its basis block");
+    if (P.nvec[b] != 0) throw NrgError(NRG_ERR_SYNC, "two kept blocks match one basis block");
+    const int64_t len = (int64_t)acut->block_beg_end_eigvec[2 * i + 1] - acut->block_beg_end_eigvec[2 * i] + 1;
+    if (acut->block_beg_end_eigvec[2 * i] < 0 || len != (int64_t)K.blk.size[i] * P.bsize[b])
+      throw NrgError(NRG_ERR_SYNC, "BlockBegEndEigVec does not match kept x basis block size");
+    K.src.push_back(b);
+    P.nvec[b] = K.blk.size[i];
+  }
+  P.yoff.assign(nb, 0);
+  int64_t y = 0;
+  for (int b = 0; b < nb; ++b) { P.yoff[b] = y; y += (int64_t)P.bsize[b] * P.nvec[b]; }
+  P.ysize = y;
+  std::vector<double> Zh((size_t)std::max<int64_t>(y, 1)), Zth((size_t)std::max<int64_t>(y, 1));
+  for (int i = 0; i < nk; ++i) {
+    const int b = K.src[i], n = P.bsize[b], k = K.blk.size[i];
+    const double* src = acut->eigvec + acut->block_beg_end_eigvec[2 * i];
+    double* z = Zh.data() + P.yoff[b];
+    double* zt = Zth.data() + P.yoff[b];
+    std::memcpy(z, src, sizeof(double) * (size_t)k * n);
+    for (int r = 0; r < k; ++r)
+      for (int col = 0; col < n; ++col) zt[(size_t)col * k + r] = src[(size_t)r * n + col];
+  }
+  Timer tm(c);
+  c->flag.ensure(sizeof(int) * 4);
+  CU(cudaMemsetAsync(c->flag.p, 0, sizeof(int), c->stream));
+  c->Z.ensure(sizeof(double) * std::max<int64_t>(y, 1));
+  c->Zt.ensure(sizeof(double) * std::max<int64_t>(y, 1));
+  h2d(c, c->Z.p, Zh.data(), sizeof(double) * y);
+  h2d(c, c->Zt.p, Zth.data(), sizeof(double) * y);
+  std::vector<OpMeta> oldops(nops);
+  std::vector<double*> oldptr(8, nullptr), newptr(8, nullptr);
+  for (int o = 0; o < nops; ++o) {
+    int64_t nel = 0;
+    oldops[o] = op_from_abi(old_ops[o], Kold, &nel);
+    c->ops_a[o].ensure(sizeof(double) * std::max<int64_t>(nel, 1));
+    h2d(c, c->ops_a[o].p, old_ops[o].mat_el, sizeof(double) * nel);
+    oldptr[o] = c->ops_a[o].as<double>();
+  }
+  UpdatePlan U;
+  plan_update(U, m, B, P, K, oldops);
+  int64_t total = 0;
+  std::vector<int64_t> obase(nops);
+  for (int o = 0; o < nops; ++o) {
+    c->ops_b[o].ensure(sizeof(double) * std::max<int64_t>(U.newops[o].size, 1));
+    newptr[o] = c->ops_b[o].as<double>();
+    obase[o] = total;
+    total += U.newops[o].size;
+  }
+  U.o_old = U.up.add(oldptr);
+  U.o_new = U.up.add(newptr);
+  launch_update_plan(c, tm, U);
+  c->out_el.resize((size_t)std::max<int64_t>(total, 1));
+  for (int o = 0; o < nops; ++o)
+    d2h(c, c->out_el.data() + obase[o], newptr[o], sizeof(double) * U.newops[o].size);
+  CU(cudaStreamSynchronize(c->stream));
+  check_flag(c);
+  tm.collect();
+  c->out_map.clear(); c->out_mbe.clear();
+  std::vector<size_t> mbase(nops);
+  for (int o = 0; o < nops; ++o) {
+    const OpMeta& no = U.newops[o];
+    mbase[o] = c->out_map.size();
+    for (size_t k = 0; k < no.bi.size(); ++k) {
+      const int64_t len = (int64_t)K.blk.size[no.bi[k]] * K.blk.size[no.bj[k]];
+      if (no.off[k] + len > INT32_MAX) throw NrgError(NRG_ERR_SIZE, "operator exceeds MatBlockBegEnd's int range");
+      c->out_map.push_back(no.bi[k]); c->out_map.push_back(no.bj[k]);
+      c->out_mbe.push_back((int)no.off[k]); c->out_mbe.push_back((int)(no.off[k] + len - 1));
+    }
+  }
+  for (int o = 0; o < nops; ++o) {
+    new_ops[o].nmatblocks = (int)U.newops[o].bi.size();
+    new_ops[o].mat_block_map = c->out_map.data() + mbase[o];
+    new_ops[o].mat_block_beg_end = c->out_mbe.data() + mbase[o];
+    new_ops[o].mat_el = c->out_el.data() + obase[o];
+  }
 }
 
 // Register-only DFMA loop: eight independent chains per thread.
@@ -907,6 +1290,40 @@ nrg_status nrg_diag_blocks(nrg_ctx* ctx, int nblocks, const int* sizes, const do
   GUARD(ctx, {
     CU(cudaSetDevice(ctx->device));
     diag_blocks_impl(ctx, nblocks, sizes, packed_upper, eigvals, eigvecs);
+  });
+  return NRG_OK;
+}
+
+nrg_status nrg_diag_hn(nrg_ctx* ctx, int model, const double* params_hn, int nparams, const nrg_blocks* old_kept,
+                       int nops, const nrg_matrix* ops, const nrg_basis* abasis, double* en, double* eigvec,
+                       double* emin) {
+  if (!ctx) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    diag_hn_impl(ctx, model, params_hn, nparams, old_kept, nops, ops, abasis, en, eigvec, emin);
+  });
+  return NRG_OK;
+}
+
+nrg_status nrg_cut_states(nrg_ctx* ctx, const nrg_blocks* aeig, const double* en, const double* eigvec,
+                          int ncutoff, double degen_eps, nrg_cut_result* out) {
+  if (!ctx) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    cut_states_impl(ctx, aeig, en, eigvec, ncutoff, degen_eps > 0 ? degen_eps : 1.0e-18, out);
+  });
+  return NRG_OK;
+}
+
+nrg_status nrg_update_ops(nrg_ctx* ctx, int model, const nrg_blocks* old_kept, const nrg_basis* abasis,
+                          const nrg_eigcut* acut, int nops, const nrg_matrix* old_ops, nrg_matrix* new_ops) {
+  if (!ctx) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    update_ops_impl(ctx, model, old_kept, abasis, acut, nops, old_ops, new_ops);
   });
   return NRG_OK;
 }

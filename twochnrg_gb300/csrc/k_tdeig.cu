@@ -151,6 +151,26 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
   A.ev[g] = v;
 }
 
+// Each level is found on its own, so two (nearly) equal levels can come out
+// an ulp out of order.  CutStates reads a block's levels as ascending
+// (its first level above E_cut ends the block), so every block is put in
+// order with odd-even transposition passes: one CTA per block, stopping after
+// two passes without a swap; n + 1 passes always suffice.
+__global__ void order_levels_kernel(TdEigArgs A) {
+  const int b = blockIdx.x;
+  const int n = A.bsize[b];
+  double* v = A.ev + A.soff[b];
+  int quiet = 0;
+  for (int pass = 0; pass <= n && quiet < 2; ++pass) {
+    int swapped = 0;
+    for (int i = 2 * threadIdx.x + (pass & 1); i + 1 < n; i += 2 * blockDim.x) {
+      const double x = v[i], y = v[i + 1];
+      if (y < x) { v[i] = y; v[i + 1] = x; swapped = 1; }
+    }
+    quiet = __syncthreads_or(swapped) ? 0 : quiet + 1;
+  }
+}
+
 // Deterministic pseudo-random start vector component in (-1, 1).
 __device__ __forceinline__ double start_component(int k, int i) {
   uint64_t z = ((uint64_t)(uint32_t)k << 32) ^ (uint64_t)(uint32_t)i ^ 0x9E3779B97F4A7C15ull;
@@ -343,6 +363,7 @@ __global__ void __launch_bounds__(kBackWarps * 32) backtransform_kernel(BackArgs
 void launch_bisect(const TdEigArgs& a, const int* state_block, cudaStream_t s) {
   if (a.nstates <= 0) return;
   bisect_kernel<<<(a.nstates + 127) / 128, 128, 0, s>>>(a, state_block);
+  order_levels_kernel<<<a.nblocks, 256, 0, s>>>(a);
 }
 
 void launch_inviter(const InvIterArgs& a, const int* vec_block, const int* vec_index, int nvecs, cudaStream_t s) {
