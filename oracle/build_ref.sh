@@ -52,6 +52,16 @@ for s in $SRCS $MAIN_SRCS OneChQS_SetSingleSite lapack_forward; do LIBOBJS="$LIB
 LDFLAGS="$OPENBLAS -Wl,-rpath,$(dirname "$OPENBLAS") -lm"
 
 "$CXX" $CXXFLAGS "$REF_DIR/src/Main/NRG_main.cpp" $LIBOBJS $LDFLAGS -o "$OUT/NRG_main"
+# DM_NRG (src/DM_NRG/Makefile: OBJS + OBJS_DMNRG) for the spectral-function
+# golden vectors.
+DM_SRCS="DM_NRG_SetChildSt DM_NRG_CalcRhoN DM_NRG_SetRhoNmax DM_NRG_CalcSpecFuncs DM_NRG_CommandLineRead"
+pids=()
+for s in $DM_SRCS; do compile "$REF_DIR/src/DM_NRG/$s.cpp" "$OBJ/$s.o" & pids+=($!); done
+compile "$REF_DIR/src/BroadDelta.cpp" "$OBJ/BroadDelta.o" & pids+=($!)
+for p in "${pids[@]}"; do wait "$p"; done
+DMOBJS=""
+for s in $DM_SRCS BroadDelta; do DMOBJS="$DMOBJS $OBJ/$s.o"; done
+"$CXX" $CXXFLAGS "$REF_DIR/src/DM_NRG/DM_NRG.cpp" $DMOBJS $LIBOBJS $LDFLAGS -o "$OUT/DM_NRG"
 if [ -f "$HERE/ref_harness.cpp" ]; then
   "$CXX" $CXXFLAGS "$HERE/ref_harness.cpp" $LIBOBJS $LDFLAGS -o "$OUT/ref_harness"
 fi

@@ -264,7 +264,7 @@ Basis site_2chQS() {
 }
 
 // ---------------------------------------------------------------- rules
-enum OpRule { R_F_QS = 1, R_FUP_QSZ, R_FDN_QSZ, R_F1_2CH, R_F2_2CH, R_IMPONLY };
+enum OpRule { R_F_QS = 1, R_FUP_QSZ, R_FDN_QSZ, R_F1_2CH, R_F2_2CH, R_IMPONLY, R_CD_QS };
 enum Check { C_DIAG = 1, C_QS_CD, C_Q_CD, C_2CH_CD };
 
 struct Model {
@@ -480,6 +480,44 @@ double op_f_2ch(Ctx& c, const Basis& ab, int ist, int jst, int ich) {
   return aux / CGnorm;
 }
 
+// OneChQS_cd_MatEl (OpMatRules.cpp:1249-1330): the impurity d operator
+// between new-basis states (reduced matrix element, SU(2) recoupling of the
+// old state with the unchanged site state); multiplied by the old operator by
+// UpdateMatrices (NeedOld).  A site state that is not found compares equal to
+// another one that is not found (-1 == -1), as in the reference.
+double op_cd_QS(Ctx& c, const Basis& ab, int ist, int jst) {
+  const Basis& ss = c.m.site;
+  double Si = qn_from_st(ab, ist, 1), Sj = qn_from_st(ab, jst, 1);
+  int ti = ab.itype[ist], tj = ab.itype[jst];
+  double Qti = ss.q(ti, 0), Sti = ss.q(ti, 1), Szti = ss.q(ti, 2);
+  double Qtj = ss.q(tj, 0), Stj = ss.q(tj, 1), Sztj = ss.q(tj, 2);
+  double sqi[3] = {Qti, Sti, Szti}, sqj[3] = {Qtj, Stj, Sztj};
+  double Scfi = Si - Szti, Scfj = Sj - Sztj;
+  double f = 0.0;
+  double sigma = Sj - Si;
+  double a3 = c.cg(Si, Si, 0.5, sigma, Sj, Sj);
+  if (dEq(a3, 0.0)) {
+    sigma = Si - Sj;
+    a3 = c.cg(Si, Si, 0.5, sigma, Sj, Sj);
+    if (dEq(a3, 0.0)) return 0.0;
+  }
+  for (double Szcfj = -Scfj; Szcfj <= Scfj; Szcfj += 1.0) {
+    double Szcfi = Szcfj - sigma;
+    double Sztj_ = Sj - Szcfj, Szti_ = Si - Szcfi;
+    sqj[2] = Sztj_;
+    int sj = ss.block_of_qn(sqj);
+    sqi[2] = Szti_;
+    int si = ss.block_of_qn(sqi);
+    double a0 = c.cg(Scfi, Szcfi, Sti, Szti_, Si, Si);
+    double a1 = c.cg(Scfj, Szcfj, Stj, Sztj_, Sj, Sj);
+    double a2 = c.cg(Scfi, Szcfi, 0.5, sigma, Scfj, Szcfj);
+    double FermiSign = dEq(Qtj, 0.0) ? -1.0 : 1.0;
+    if (si == sj) f += a0 * a1 * a2 * FermiSign;
+  }
+  if (!dEq(a3, 0.0)) f = f / a3; else f = 0.0;
+  return f;
+}
+
 double op_rule(Ctx& c, int rule, const Basis& ab, int ist, int jst) {
   switch (rule) {
     case R_F_QS: return op_f_QS(c, ab, ist, jst);
@@ -488,14 +526,16 @@ double op_rule(Ctx& c, int rule, const Basis& ab, int ist, int jst) {
     case R_F1_2CH: return op_f_2ch(c, ab, ist, jst, 1);
     case R_F2_2CH: return op_f_2ch(c, ab, ist, jst, 2);
     case R_IMPONLY: return ab.itype[ist] == ab.itype[jst] ? 1.0 : 0.0;  // ImpOnly_MatEl OpMatRules.cpp:265
+    case R_CD_QS: return op_cd_QS(c, ab, ist, jst);
   }
   return 0.0;
 }
 
 // ---------------------------------------------------------------- BuildBasis
 // BuildBasis (BuildBasis.cpp:8-432) for the Q,S / Q,Sz cases (no parity,
-// no symmetry reduction, BefCut=0).
-void build_basis(const Model& m, const Basis& cut, Basis& ab) {
+// no symmetry reduction).  befcut: StCameFrom numbers the states before the
+// cut (BuildBasis.cpp:386-391), as NRG_main asks when UpdateBefCut = 1.
+void build_basis(const Model& m, const Basis& cut, Basis& ab, bool befcut = false) {
   const Basis& ss = m.site;
   int NC = m.common[0];
   std::vector<int> posold(NC), possite(NC), totS(NC, 0), match(NC);
@@ -568,7 +608,7 @@ void build_basis(const Model& m, const Basis& cut, Basis& ab) {
           for (int st = ss.beg(s); st <= ss.end(s); st++) {
             ab.itype.push_back(ss.itype[st]);
             ab.en.push_back(cut.en[so]);
-            ab.stcf.push_back(so);
+            ab.stcf.push_back(befcut ? cut.stcf[so] : so);
             ist++;
           }
       }
@@ -891,6 +931,323 @@ void hm1_QSz(double Lambda, double HLF, double U, double ed, double B, Arr& a, M
   avg = {diag_op(a, nd, "Ndot"), diag_op(a, sz, "Szdot")};
 }
 
+// ---------------------------------------------------------------- DM-NRG
+// What NRG_main saves per shell when the spectral density is asked for
+// (calcdens = 1, UpdateBefCut = 1; CNRGCodeHandler::SaveArrays,
+// NRGcodehandlerClass.cpp:887-932): Abasis_N, the uncut eigen-array Acut_N
+// (all states, Kept flags, all eigenvectors) and the c_d operator in it.
+struct DmShell {
+  Basis ab;
+  Basis full;
+  Mat cd;
+};
+
+// CalcDN (CalcDN.cpp) with z = 1.
+double calc_dn(double L, int N) {
+  double hlf = L > 0.0 ? 0.5 * (1.0 + (1.0 / L)) : 1.0;
+  return hlf * std::pow(L, (-(N - 1) / 2.0) - 1.0 + 1.0);
+}
+// LogGaussDelta (BroadDelta.cpp:116-133) and GaussDelta (BroadDelta.cpp:96-106).
+double log_gauss_delta(double omega, double Ep, double b) {
+  if (Ep == 0.0) Ep = 1.0E-100;
+  if ((omega * Ep) < 0.0) return 0.0;
+  double a0 = 1.0 / (b * std::fabs(Ep) * std::sqrt(3.141592653589793238462643383279502884197169));
+  double a1 = std::log(std::fabs(omega / Ep)) / b;
+  return a0 * std::exp(-(a1 - b / 4.0) * (a1 - b / 4.0));
+}
+double gauss_delta(double omega, double Ep, double b) {
+  double a0 = 1.0 / (b * std::sqrt(3.141592653589793238462643383279502884197169));
+  double a1 = (omega - Ep) / b;
+  return a0 * std::exp(-a1 * a1);
+}
+// PartitionFunc / PartitionFuncDisc (NRGarrayClass.cpp:997-1060): (2S+1)
+// weighted Boltzmann sums over all / discarded states.
+double partition(const Arr& a, double beta, bool disc_only) {
+  double sum = 0.0;
+  for (int b = 0; b < a.nblocks(); ++b) {
+    double Si = a.totalS ? a.q(b, a.sqn[0]) : 0.0;
+    for (int i = a.beg(b); i <= a.end(b); ++i)
+      if (!disc_only || !a.kept[i]) sum += (2.0 * Si + 1.0) * std::exp(-beta * a.en[i]);
+  }
+  return sum;
+}
+
+struct DmParams {
+  double lambda, temp, betabar, bbroad, twindow, broadtemp, site_dim;
+  double tempbar0;  // TempBar handed to DM_NRG_SetRhoNmax
+};
+
+// DM_NRG's temperature (DM_NRG.cpp:100-121): Mtemp < Nsitesmax-1 puts T at
+// D_Mtemp/betabar, otherwise at D_{Nsitesmax+199}/betabar; a positive
+// `temp` given by the caller replaces the latter.  SetRhoNmax receives
+// T/D_Mtemp or T/D_{Nsitesmax-1} respectively.
+void dm_temperature(DmParams& p, int nsites, int mtemp, double temp) {
+  const double L = p.lambda;
+  if (mtemp >= 0 && mtemp < nsites - 1) {
+    double DM = calc_dn(L, mtemp);
+    p.temp = DM / p.betabar;
+    p.tempbar0 = p.temp / DM;
+  } else {
+    p.temp = temp > 0.0 ? temp : calc_dn(L, nsites + 199) / p.betabar;
+    p.tempbar0 = p.temp / calc_dn(L, nsites - 1);
+  }
+}
+
+// Dense symmetric density-matrix blocks, one per block of the uncut array.
+typedef std::vector<std::vector<double>> RhoBlocks;
+
+// DM_NRG main (DM_NRG/DM_NRG.cpp:128-383) for the default temperature branch
+// (Mtemp >= Nsitesmax-1) with FDM: partition sums, DM_NRG_SetRhoNmax
+// (DM_NRG_SetRhoNmax.cpp:9-126) and, shell by shell, RotateMatrix
+// (RotateMatrix.cpp:17-99) + DM_NRG_CalcRhoN_withSU2 (DM_NRG_CalcRhoN.cpp:252-449).
+// site_dim is the 4.0 of DM_NRG.cpp:292 (d of one Wilson site).
+void dm_backward(Ctx& c, const std::vector<DmShell>& sh, const DmParams& p, std::vector<RhoBlocks>& rho) {
+  const int nsites = (int)sh.size();
+  const int Nmax = nsites - 1;
+  const double L = p.lambda, Temp = p.temp;
+  const double TempBar0 = p.tempbar0;
+  double DM = calc_dn(L, Nmax - 1);
+  double TempBar = Temp / DM;
+  double ZTot = partition(sh[Nmax].full, 1.0 / TempBar, false);
+  for (int N = Nmax - 1; N >= 0; --N) {
+    DM = calc_dn(L, N - 1);
+    TempBar = Temp / DM;
+    double ZNdisc = partition(sh[N].full, 1.0 / TempBar, true);
+    ZTot += ZNdisc * std::pow(p.site_dim, Nmax - N);
+  }
+  rho.assign(nsites, RhoBlocks());
+  {  // SetRhoNmax
+    const Arr& a = sh[Nmax].full;
+    double beta = dEq(TempBar0, 0.0) ? 1.0e10 : 1.0 / TempBar0;
+    rho[Nmax].resize(a.nblocks());
+    for (int b = 0; b < a.nblocks(); ++b) {
+      int n = a.bsize(b);
+      std::vector<double>& R = rho[Nmax][b];
+      R.assign((size_t)n * n, 0.0);
+      for (int i = 0; i < n; ++i) R[(size_t)i * n + i] = std::exp(-beta * a.en[a.beg(b) + i]) / ZTot;
+    }
+  }
+  for (int N = Nmax - 1; N >= 0; --N) {
+    const Arr& aN = sh[N].full;
+    const Basis& fNp1 = sh[N + 1].full;
+    const Basis& abNp1 = sh[N + 1].ab;
+    DM = calc_dn(L, N - 1);
+    TempBar = Temp / DM;
+    const double ZNdisc = ZTot / std::pow(p.site_dim, Nmax - N);
+    const double beta = 1 / TempBar;
+    // RotateMatrix: rho~ = Z^T rho Z per block, in the before-cut basis.
+    RhoBlocks rot(fNp1.nblocks());
+    for (int b = 0; b < fNp1.nblocks(); ++b) {
+      int n = fNp1.bsize(b), nb = fNp1.bsize_bc(b);
+      const double* Z = &fNp1.evec[fNp1.bbe_eig[2 * b]];
+      const std::vector<double>& R = rho[N + 1][b];
+      std::vector<double> T((size_t)n * nb, 0.0);
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < nb; ++j) {
+          double s = 0.0;
+          for (int k = 0; k < n; ++k) s += R[(size_t)i * n + k] * Z[(size_t)k * nb + j];
+          T[(size_t)i * nb + j] = s;
+        }
+      std::vector<double>& O = rot[b];
+      O.assign((size_t)nb * nb, 0.0);
+      for (int i = 0; i < nb; ++i)
+        for (int j = 0; j < nb; ++j) {
+          double s = 0.0;
+          for (int k = 0; k < n; ++k) s += Z[(size_t)k * nb + i] * T[(size_t)k * nb + j];
+          O[(size_t)i * nb + j] = s;
+        }
+    }
+    // DM_NRG_SetChildSt (DM_NRG_SetChildSt.cpp:11-40).
+    std::vector<std::vector<int>> child(aN.nstates());
+    for (size_t k = 0; k < abNp1.stcf.size(); ++k) child[abNp1.stcf[k]].push_back((int)k);
+    rho[N].resize(aN.nblocks());
+    for (int b = 0; b < aN.nblocks(); ++b) {
+      int n = aN.bsize(b), b0 = aN.beg(b);
+      double Sold = aN.totalS ? aN.q(b, aN.sqn[0]) : 0.0;
+      std::vector<double>& R = rho[N][b];
+      R.assign((size_t)n * n, 0.0);
+      for (int i = 0; i < n; ++i)
+        for (int j = i; j < n; ++j) {
+          int ist = b0 + i, jst = b0 + j;
+          double v = 0.0;
+          // DM_NRG_SetChildSameType (DM_NRG_SetChildSt.cpp:45-113).
+          for (int ci : child[ist]) {
+            int pos;
+            int ib = abNp1.block_of(ci, pos);
+            int ti = abNp1.itype[ci];
+            for (int cj : child[jst]) {
+              int jb = abNp1.block_of(cj, pos);
+              if (ti != abNp1.itype[cj] || ib != jb) continue;
+              double Si = abNp1.totalS ? abNp1.q(ib, abNp1.sqn[0]) : 0.0;
+              double St = c.m.site.totalS ? c.m.site.q(ti, c.m.site.sqn[0]) : 0.0;
+              double cgf = 0.0;
+              for (double Sz = -Si; Sz <= Si; Sz += 1.0) {
+                double x = c.cg(Sold, Sold, St, Sz - Sold, Si, Sz);
+                cgf += x * x;
+              }
+              int nb = fNp1.bsize_bc(ib);
+              int pi = ci - fNp1.bbe_bc[2 * ib], pj = cj - fNp1.bbe_bc[2 * ib];
+              v += cgf * rot[ib][(size_t)pi * nb + pj];
+            }
+          }
+          if (i == j && !aN.kept[ist] && !dEq(ZNdisc, 0.0)) v = std::exp(-beta * (aN.en[ist])) / ZNdisc;
+          R[(size_t)i * n + j] = v;
+          R[(size_t)j * n + i] = v;
+        }
+    }
+  }
+}
+
+// CSpecFunction::MijxBDeltaEij (SpecFunc_allSTL.cpp:132-220 and
+// SpecFuncClass.cpp:934-990): the broadened delta between two levels, the
+// log-Gaussian, or a Gaussian inside the thermal window.
+double broad_delta(const DmParams& p, double omega, double dE, double TempDN) {
+  double BD = log_gauss_delta(omega, dE, p.bbroad);
+  if (std::fabs(dE) < p.twindow * TempDN) BD = gauss_delta(omega, dE, p.broadtemp);
+  return BD;
+}
+
+// Sum_{Sz} <S1 Sz; 1/2 1/2 | S2 Sz+1/2>^2 of the spectral sums
+// (SpecFunc_allSTL.cpp, end of FDM_SpecDens_M_STL; SpecFuncClass.cpp:600-617).
+double spec_cg(Ctx& c, const Arr& a, int b1, int b2) {
+  if (!a.totalS) return 1.0;
+  double S1 = a.q(b1, a.sqn[0]), S2 = a.q(b2, a.sqn[0]), f = 0.0;
+  for (double Sz1 = -S1; Sz1 <= S1; Sz1 += 1.0) {
+    double x = c.cg(S1, Sz1, 0.5, 0.5, S2, Sz1 + 0.5);
+    f += x * x;
+  }
+  return f;
+}
+
+// CSpecFunction::CalcSpecCosti_T_N (SpecFuncClass.cpp:417-650): the last shell.
+double spec_costi(Ctx& c, const DmShell& s, int N, const DmParams& p, double omegabar) {
+  const Arr& a = s.full;
+  const Mat& A = s.cd;
+  const double TempDN = p.temp / calc_dn(p.lambda, N);
+  double rho = 0.0;
+  for (size_t k = 0; k < A.map.size() / 2; ++k) {
+    int b1 = A.map[2 * k], b2 = A.map[2 * k + 1];
+    int n1 = a.bsize(b1), n2 = a.bsize(b2), o1 = a.beg(b1), o2 = a.beg(b2);
+    const double* M = &A.el[A.mbe[2 * k]];
+    double tr = 0.0;
+    for (int bb = 0; bb < n2; ++bb)
+      for (int aa = 0; aa < n1; ++aa) {
+        double E1 = a.en[o1 + aa], E2 = a.en[o2 + bb];
+        double m = M[(size_t)aa * n2 + bb];
+        double sum12 = m * std::exp(-p.betabar * E1) + std::exp(-p.betabar * E2) * m;
+        tr += sum12 * (m * broad_delta(p, omegabar, E2 - E1, TempDN));
+      }
+    rho += spec_cg(c, a, b1, b2) * tr;
+  }
+  return rho / partition(a, p.betabar, false);
+}
+
+// CSpecFunction::FDM_SpecDens_M_STL (SpecFunc_allSTL.cpp:1253-2358), real
+// operators, Op2 = Op1.  Each term is the trace of (B^T rho or rho B^T) times
+// A o delta over one kept/discarded sub-block pair.
+double spec_fdm(Ctx& c, const std::vector<DmShell>& sh, const std::vector<RhoBlocks>& rho, int N,
+                const DmParams& p, double omegabar) {
+  const int nshell = (int)sh.size();
+  if (N > nshell - 1) return 0.0;
+  if (N == nshell - 1) {
+    // FDM_SpecDens_M_STL sets Betabar = 1e10 when Temp is zero within 1e-20.
+    DmParams q = p;
+    if (dEq(p.temp, 0.0)) q.betabar = 1.0e10;
+    return spec_costi(c, sh[N], N, q, omegabar);
+  }
+  const Arr& a = sh[N].full;
+  const Mat& A = sh[N].cd;
+  const double TempDN = p.temp / calc_dn(p.lambda, N);
+  double pos_w = 0.0, neg_w = 0.0;
+  for (size_t k = 0; k < A.map.size() / 2; ++k) {
+    int b1 = A.map[2 * k], b2 = A.map[2 * k + 1];
+    int n1 = a.bsize(b1), n2 = a.bsize(b2), o1 = a.beg(b1), o2 = a.beg(b2);
+    std::vector<int> K1, D1, K2, D2;
+    for (int i = 0; i < n1; ++i) (a.kept[o1 + i] ? K1 : D1).push_back(i);
+    for (int i = 0; i < n2; ++i) (a.kept[o2 + i] ? K2 : D2).push_back(i);
+    if ((K1.empty() && K2.empty()) || (D1.empty() && D2.empty())) continue;
+    const double* M = &A.el[A.mbe[2 * k]];
+    const std::vector<double>& R1 = rho[N][b1];
+    const std::vector<double>& R2 = rho[N][b2];
+    auto el = [&](int i, int j) { return M[(size_t)i * n2 + j]; };
+    auto bd = [&](int i, int j) { return broad_delta(p, omegabar, a.en[o2 + j] - a.en[o1 + i], TempDN); };
+    // trace over b in S2 of sum_{a in S1} (sum_{a' in S1} A[a',b] rho1[a',a]) A[a,b] d(a,b)
+    auto term1 = [&](const std::vector<int>& S1, const std::vector<int>& S2) {
+      double t = 0.0;
+      for (int bb : S2)
+        for (int aa : S1) {
+          double pr = 0.0;
+          for (int ap : S1) pr += el(ap, bb) * R1[(size_t)ap * n1 + aa];
+          t += pr * (el(aa, bb) * bd(aa, bb));
+        }
+      return t;
+    };
+    // trace over b in S2 of sum_{a in S1} (sum_{b' in S2} rho2[b,b'] A[a,b']) A[a,b] d(a,b)
+    auto term2 = [&](const std::vector<int>& S1, const std::vector<int>& S2) {
+      double t = 0.0;
+      for (int bb : S2)
+        for (int aa : S1) {
+          double pr = 0.0;
+          for (int bp : S2) pr += R2[(size_t)bb * n2 + bp] * el(aa, bp);
+          t += pr * (el(aa, bb) * bd(aa, bb));
+        }
+      return t;
+    };
+    double T1KK = 0, T1DDADD = 0, T1DDADK = 0, T2KK = 0, T2DDADD = 0, T2DDAKD = 0;
+    if (!K1.empty() && !D2.empty() && omegabar >= 0.0) T1KK = term1(K1, D2);
+    if (!D1.empty() && !D2.empty()) {
+      T1DDADD = term1(D1, D2);
+      if (!K2.empty()) T1DDADK = term1(D1, K2);
+    }
+    if (!D1.empty() && !K2.empty() && omegabar < 0.0) T2KK = term2(D1, K2);
+    if (!D1.empty() && !D2.empty()) {
+      T2DDADD = term2(D1, D2);
+      if (!K1.empty()) T2DDAKD = term2(K1, D2);
+    }
+    double cgf = spec_cg(c, a, b1, b2);
+    pos_w += cgf * (T1KK + T1DDADD + T2DDADD + T2DDAKD);
+    neg_w += cgf * (T2KK + T1DDADD + T1DDADK + T2DDADD);
+  }
+  return omegabar >= 0.0 ? pos_w : neg_w;
+}
+
+// CSpecFunction::CalcNfromOmega (SpecFuncClass.cpp:41-49) and CalcSpecDM_NRG
+// (SpecFuncClass.cpp:1827-1883): the shells within a window around omega.
+double spec_at(Ctx& c, const std::vector<DmShell>& sh, const std::vector<RhoBlocks>& rho, const DmParams& p,
+               double omega) {
+  const double L = p.lambda, hlf = 0.5 * (1.0 + (1.0 / L));
+  const int nshell = (int)sh.size();
+  int iaux = (int)(2.0 * std::log(2.0 * std::fabs(omega) / hlf) / std::log(L));
+  iaux = 1 - iaux;
+  if (iaux < 0) iaux = 0;
+  int N0 = iaux - 8 > 0 ? iaux - 8 : 0;
+  int N1 = iaux + 14 < nshell ? iaux + 14 : nshell;
+  double s = 0.0;
+  for (int N = N0; N < N1; ++N) {
+    double DN = calc_dn(L, N);
+    s += spec_fdm(c, sh, rho, N, p, omega / DN) / DN;
+  }
+  return s;
+}
+
+// CSpecFunction::CalcSpec_ManyOmegas (SpecFuncClass.cpp:2238-2341), FDM:
+// nw frequencies per shell from shell 2 to the last-but-one, negative side
+// first.
+void spec_grid(double L, int nshell, int nw, std::vector<double>& om) {
+  const double hlf = 0.5 * (1.0 + (1.0 / L)), factorWN = std::pow(L, 1.25);
+  auto dn = [&](int N) { return hlf * std::pow(L, (-(N - 1) / 2.0) - 1.0 + 1.0); };
+  const int Nmax = nshell - 1, N0 = 2;
+  om.clear();
+  for (int N = N0; N <= Nmax; ++N) {
+    double WN = factorWN * dn(N);
+    for (int i = 0; i < nw; ++i) om.push_back(-(std::pow(L, -((double)i / (2.0 * nw))) * WN));
+  }
+  for (int N = Nmax; N >= N0; --N) {
+    double WN = factorWN * dn(N);
+    for (int i = nw - 1; i >= 0; --i) om.push_back(std::pow(L, -((double)i / (2.0 * nw))) * WN);
+  }
+}
+
 }  // namespace
 
 // ================================================================ C ABI
@@ -916,6 +1273,9 @@ struct OracleIter {
 
 struct OracleRun {
   int nqn = 2;
+  int model = 0;
+  double lambda = 2.5;
+  std::vector<DmShell> dm;        // per shell, when cfg->dm is set
   std::vector<double> opavg_m1;
   std::vector<std::string> opnames;
   std::vector<OracleIter> it;
@@ -975,6 +1335,12 @@ void* oracle_run(const oracle_config* cfg) {
     return d0 / (d1 * d2);
   };
   c.m.kind = cfg->model;
+  R->model = cfg->model;
+  R->lambda = Lambda;
+  const bool dm = cfg->dm != 0;
+  if (dm && cfg->model != ORACLE_MODEL_1CHQS) {
+    g_err = "DM-NRG shells are restated for the one-channel |Q S> model only"; delete R; return nullptr;
+  }
   Arr eig;
   std::vector<Mat> mats;
   std::vector<double> P;
@@ -986,9 +1352,18 @@ void* oracle_run(const oracle_config* cfg) {
     c.m.site = site_1chQS(); c.m.totS = {1};
     Mat f; std::vector<Mat> avg;
     hm1_QS(Lambda, HLF, cfg->U, cfg->ed, eig, f, avg);
-    mats.push_back(f); for (auto& x : avg) mats.push_back(x);
-    c.m.op_rule = {R_F_QS, R_IMPONLY, R_IMPONLY, R_IMPONLY};
-    c.m.op_check = {C_QS_CD, C_DIAG, C_DIAG, C_DIAG};
+    if (dm) {
+      // calcdens = 1 (CodeHandler_ModelSwitch.cpp:162-176): fN and cdot1, the
+      // latter a copy of fN at H_{-1} (Main_SetH0.cpp:1958-1961).
+      Mat cd = f; cd.name = "cdot1";
+      mats.push_back(f); mats.push_back(cd);
+      c.m.op_rule = {R_F_QS, R_CD_QS};
+      c.m.op_check = {C_QS_CD, C_QS_CD};
+    } else {
+      mats.push_back(f); for (auto& x : avg) mats.push_back(x);
+      c.m.op_rule = {R_F_QS, R_IMPONLY, R_IMPONLY, R_IMPONLY};
+      c.m.op_check = {C_QS_CD, C_DIAG, C_DIAG, C_DIAG};
+    }
     P = {Lambda, chi1, 0.0, 0.0};
   } else if (cfg->model == ORACLE_MODEL_1CHQSZ) {
     c.m.site = site_1chQSz(); c.m.totS = {};
@@ -1014,6 +1389,7 @@ void* oracle_run(const oracle_config* cfg) {
   }
   for (size_t i = 0; i < mats.size(); ++i) {
     if (c.m.op_rule[i] == R_IMPONLY) { mats[i].need_old = true; mats[i].calc_avg = true; }
+    else if (c.m.op_rule[i] == R_CD_QS) { mats[i].need_old = true; mats[i].calc_avg = false; }
     else { mats[i].need_old = false; mats[i].calc_avg = false; }
   }
   R->nqn = 2;
@@ -1026,7 +1402,7 @@ void* oracle_run(const oracle_config* cfg) {
     OracleIter I;
     I.params = P;
     double DN = HLF * std::pow(Lambda, (-(N - 1) / 2.0));
-    build_basis(c.m, cut, ab);
+    build_basis(c.m, cut, ab, dm);
     bool cap = (cfg->capture_iter == N);
     if (cap) {
       I.basis_qn = ab.qn; I.basis_en = ab.en; I.basis_bbe = ab.bbe;
@@ -1055,13 +1431,23 @@ void* oracle_run(const oracle_config* cfg) {
       I.thermo.push_back(calc_suscep(eig, bN, sq, totalS));
       I.thermo.push_back(calc_entropy(eig, bN, sq, totalS));
     }
+    if (dm) {
+      // UpdateBefCut = 1 (NRG_main.cpp:334-343, 393-396): operators are
+      // updated in the uncut basis, then the shell is saved, then the cut.
+      Basis full;
+      cut_states(eig, full, 2 * eig.nstates(), eps);
+      update_matrices(c, full, ab, mats, nthreads);
+      DmShell shl;
+      shl.ab = ab; shl.full = full; shl.cd = mats[1];
+      R->dm.push_back(std::move(shl));
+    }
     cut_states(eig, cut, cfg->ncutoff, eps);
     if (cap) {
       I.capd["cut_qn"] = cut.qn; I.capi["cut_bbe"] = cut.bbe; I.capi["cut_bbe_bc"] = cut.bbe_bc;
       I.capi["cut_bbe_eig"] = cut.bbe_eig; I.capi["cut_stcf"] = cut.stcf; I.capd["cut_en"] = cut.en;
       I.capi["cut_kept"] = std::vector<int>(cut.kept.begin(), cut.kept.end()); I.capd["cut_evec"] = cut.evec;
     }
-    update_matrices(c, cut, ab, mats, nthreads);
+    if (!dm) update_matrices(c, cut, ab, mats, nthreads);
     if (cap)
       for (size_t o = 0; o < mats.size(); ++o) {
         I.capi["new_map." + std::to_string(o)] = mats[o].map;
@@ -1105,6 +1491,59 @@ const double* oracle_iter_H(void* h, int n) { return ITER(h, n).H.data(); }
 const int* oracle_iter_basis_itype(void* h, int n) { return ITER(h, n).basis_itype.data(); }
 const int* oracle_iter_basis_stcf(void* h, int n) { return ITER(h, n).basis_stcf.data(); }
 const double* oracle_iter_basis_en(void* h, int n) { return ITER(h, n).basis_en.data(); }
+
+// DM-NRG on the shells of a run made with cfg->dm: the backward sweep of the
+// density matrix and the FDM spectral function of c_d at the given
+// frequencies, or (omegas == NULL) on CalcSpec_ManyOmegas's grid with nw
+// points per shell.  Returns the number of frequencies written (at most cap),
+// or -1.  rho_trace, if not NULL, receives sum_b (2S_b+1) Tr rho_N(b) per shell.
+int oracle_dm_spectral(void* h, const oracle_dm_params* prm, const double* omegas, int nomega, double* omega_out,
+                       double* a_out, int cap, double* rho_trace) {
+  OracleRun* R = (OracleRun*)h;
+  if (R->dm.empty()) { g_err = "run has no DM-NRG shells"; return -1; }
+  Ctx c;
+  c.m.kind = R->model;
+  c.m.site = site_1chQS();
+  DmParams p{R->lambda, prm->temp, prm->betabar, prm->bbroad, prm->twindow, prm->broadtemp, prm->site_dim, 0.0};
+  dm_temperature(p, (int)R->dm.size(), prm->mtemp, prm->temp);
+  std::vector<RhoBlocks> rho;
+  dm_backward(c, R->dm, p, rho);
+  if (rho_trace)
+    for (size_t N = 0; N < rho.size(); ++N) {
+      const Arr& a = R->dm[N].full;
+      double t = 0.0;
+      for (int b = 0; b < a.nblocks(); ++b) {
+        int n = a.bsize(b);
+        double deg = a.totalS ? 2.0 * a.q(b, a.sqn[0]) + 1.0 : 1.0;
+        for (int i = 0; i < n; ++i) t += deg * rho[N][b][(size_t)i * n + i];
+      }
+      rho_trace[N] = t;
+    }
+  std::vector<double> om;
+  if (omegas) om.assign(omegas, omegas + nomega);
+  else spec_grid(R->lambda, (int)R->dm.size(), prm->nw, om);
+  int n = std::min<int>((int)om.size(), cap);
+  for (int k = 0; k < n; ++k) {
+    omega_out[k] = om[k];
+    a_out[k] = spec_at(c, R->dm, rho, p, om[k]);
+  }
+  return n;
+}
+
+// One shell's term of the sum over shells: FDM_SpecDens_M_STL(omegabar, N)
+// (the last shell: CalcSpecCosti_T_N).
+double oracle_dm_shell_term(void* h, const oracle_dm_params* prm, int N, double omegabar) {
+  OracleRun* R = (OracleRun*)h;
+  if (R->dm.empty() || N < 0 || N >= (int)R->dm.size()) return 0.0;
+  Ctx c;
+  c.m.kind = R->model;
+  c.m.site = site_1chQS();
+  DmParams p{R->lambda, prm->temp, prm->betabar, prm->bbroad, prm->twindow, prm->broadtemp, prm->site_dim, 0.0};
+  dm_temperature(p, (int)R->dm.size(), prm->mtemp, prm->temp);
+  std::vector<RhoBlocks> rho;
+  dm_backward(c, R->dm, p, rho);
+  return spec_fdm(c, R->dm, rho, N, p, omegabar);
+}
 
 // Named captures of the capture iteration: NULL (and *len = -1) if absent.
 const double* oracle_cap_d(void* h, int n, const char* name, int* len) {

@@ -18,7 +18,20 @@ typedef struct {
   double degen_eps;   /* SetDegen tolerance, <=0 -> 1e-18 */
   int nthreads;       /* host threads over blocks / block pairs */
   int capture_iter;   /* iteration whose DiagHN inputs/H are kept, -1 none */
+  int dm;             /* keep DM-NRG shells (UpdateBefCut = 1, c_d); 1chQS only */
 } oracle_config;
+
+/* DM-NRG parameters (DM_NRG command line, DM_NRG_CommandLineRead.cpp). */
+typedef struct {
+  double temp;        /* temperature in units of the half-bandwidth (> 0), or 0 for DM_NRG's choice */
+  double betabar;     /* -b, default 0.727 */
+  double bbroad;      /* -e, log-Gaussian width */
+  double twindow;     /* -w, default 2 */
+  double broadtemp;   /* -B, default 0.8 */
+  double site_dim;    /* states per Wilson site in the FDM weights (4 in DM_NRG.cpp) */
+  int nw;             /* -n, frequencies per shell for the default grid */
+  int mtemp;          /* -M: T = D_Mtemp/betabar when Mtemp < nsites-1; -1 otherwise */
+} oracle_dm_params;
 
 int oracle_load_lapack(const char* path);
 const char* oracle_last_error(void);
@@ -30,6 +43,8 @@ void oracle_free(void* h);
 /* Named arrays of the capture iteration (NULL and *len = -1 if absent). */
 const double* oracle_cap_d(void* h, int n, const char* name, int* len);
 const int* oracle_cap_i(void* h, int n, const char* name, int* len);
+int oracle_dm_spectral(void* h, const oracle_dm_params* prm, const double* omegas, int nomega, double* omega_out,
+                       double* a_out, int cap, double* rho_trace);
 
 #ifdef __cplusplus
 }

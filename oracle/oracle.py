@@ -25,7 +25,13 @@ class _Cfg(ctypes.Structure):
                 ("lambda_", ctypes.c_double), ("U", ctypes.c_double), ("ed", ctypes.c_double),
                 ("gamma1", ctypes.c_double), ("gamma2_or_B", ctypes.c_double),
                 ("degen_eps", ctypes.c_double), ("nthreads", ctypes.c_int),
-                ("capture_iter", ctypes.c_int)]
+                ("capture_iter", ctypes.c_int), ("dm", ctypes.c_int)]
+
+
+class _DmParams(ctypes.Structure):
+    _fields_ = [("temp", ctypes.c_double), ("betabar", ctypes.c_double), ("bbroad", ctypes.c_double),
+                ("twindow", ctypes.c_double), ("broadtemp", ctypes.c_double), ("site_dim", ctypes.c_double),
+                ("nw", ctypes.c_int), ("mtemp", ctypes.c_int)]
 
 
 def build(force: bool = False) -> str:
@@ -75,6 +81,10 @@ def lib():
         for name in ("oracle_cap_d", "oracle_cap_i"):
             getattr(L, name).argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p,
                                          ctypes.POINTER(ctypes.c_int)]
+        L.oracle_dm_spectral.argtypes = [ctypes.c_void_p, ctypes.POINTER(_DmParams),
+                                          ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                          ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                          ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         L.oracle_diag_block.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         rc = L.oracle_load_lapack(openblas_path().encode())
@@ -126,7 +136,7 @@ def run(model: str, nsites: int, ncutoff: int, lam: float, U: float, ed: float, 
     L = lib()
     L.oracle_blas_threads(int(blas_threads))
     cfg = _Cfg(MODELS[model], nsites, ncutoff, lam, U, ed, gamma1, gamma2_or_B, degen_eps,
-               nthreads, capture_iter)
+               nthreads, capture_iter, 0)
     h = L.oracle_run(ctypes.byref(cfg))
     if not h:
         raise RuntimeError("oracle: " + L.oracle_last_error().decode())
@@ -195,6 +205,45 @@ def _captures(L, h, n) -> dict:
         o += 1
     out["nmats"] = o
     return out
+
+
+def dm_temp_default(lam: float, nsites: int, betabar: float = 0.727) -> float:
+    """DM_NRG's temperature when Mtemp >= Nsitesmax-1 (DM_NRG.cpp:112-121):
+    D_{Nsitesmax+199} / betabar."""
+    hlf = 0.5 * (1.0 + 1.0 / lam)
+    return hlf * lam ** ((-(nsites + 199 - 1) / 2.0) - 1.0 + 1.0) / betabar
+
+
+def dm_spectral(nsites: int, ncutoff: int, lam: float, U: float, ed: float, gamma: float, temp: float,
+                bbroad: float, nw: int = 4, omegas=None, betabar: float = 0.727, twindow: float = 2.0,
+                broadtemp: float = 0.8, site_dim: float = 4.0, nthreads: int = 1, mtemp: int = -1):
+    """One-channel |Q S> Anderson model: forward sweep saving the DM-NRG
+    shells (UpdateBefCut = 1, c_d), then the FDM density-matrix backward sweep
+    and the c_d spectral function.  Returns (omega, A, rho_trace per shell)."""
+    L = lib()
+    cfg = _Cfg(MODEL_1CHQS, nsites, ncutoff, lam, U, ed, gamma, 0.0, 0.0, nthreads, -1, 1)
+    h = L.oracle_run(ctypes.byref(cfg))
+    if not h:
+        raise RuntimeError("oracle: " + L.oracle_last_error().decode())
+    h = ctypes.c_void_p(h)
+    try:
+        prm = _DmParams(temp, betabar, bbroad, twindow, broadtemp, site_dim, nw, mtemp)
+        P = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+        if omegas is None:
+            cap = 2 * nw * nsites + 8
+            om_in, n_in = None, 0
+        else:
+            om_arr = np.ascontiguousarray(omegas, dtype=np.float64)
+            cap, om_in, n_in = len(om_arr), P(om_arr), len(om_arr)
+        om = np.zeros(cap)
+        A = np.zeros(cap)
+        tr = np.zeros(nsites)
+        n = L.oracle_dm_spectral(h, ctypes.byref(prm), om_in, n_in, P(om), P(A), cap, P(tr))
+        if n < 0:
+            raise RuntimeError("oracle: " + L.oracle_last_error().decode())
+        return om[:n], A[:n], tr
+    finally:
+        L.oracle_free(h)
 
 
 def diag_block(packed: np.ndarray, n: int):
