@@ -111,6 +111,11 @@ typedef struct {
   double device_ms;       /* CUDA-event span of the sweep on the engine stream  */
   int64_t h2d_bytes;      /* host-to-device bytes copied by the sweep           */
   int64_t d2h_bytes;      /* device-to-host bytes copied by the sweep           */
+  double dm_backprop_ms;  /* nrg_dm_backprop: rotations + partial traces        */
+  double dm_spectral_ms;  /* nrg_lehmann: pair weights + Lehmann sums           */
+  double lehmann_ms;      /* nrg_lehmann: the Lehmann-sum kernels alone         */
+  int64_t lehmann_pairs;  /* (E_j - E_i, weight) pairs over all shells          */
+  int64_t lehmann_evals;  /* pair x frequency evaluations of the broadened delta */
 } nrg_timing;
 
 /* ---- context ---------------------------------------------------------- */
@@ -266,6 +271,47 @@ nrg_status nrg_cut_states(nrg_ctx* ctx, const nrg_blocks* aeig, const double* en
  * storage. */
 nrg_status nrg_update_ops(nrg_ctx* ctx, int model, const nrg_blocks* old_kept, const nrg_basis* abasis,
                           const nrg_eigcut* acut, int nops, const nrg_matrix* old_ops, nrg_matrix* new_ops);
+
+/* ---- DM-NRG spectral function (src/DM_NRG/DM_NRG.cpp) --------------------
+ * Parameters of DM_NRG's command line (DM_NRG_CommandLineRead.cpp). */
+typedef struct {
+  double temp;        /* T in units of the half-bandwidth; <= 0: DM_NRG's own
+                         choice, D_{nsites+199}/betabar (or see mtemp) */
+  int mtemp;          /* -M: T = D_Mtemp/betabar when 0 <= mtemp < nsites-1 (else -1) */
+  double betabar;     /* -b, 0.727 */
+  double bbroad;      /* -e, log-Gaussian width b */
+  double twindow;     /* -w, 2: |E_j - E_i| < twindow T/D_N uses the Gaussian */
+  double broadtemp;   /* -B, 0.8: width of that Gaussian */
+  double site_dim;    /* states per Wilson site in the FDM weights (4, DM_NRG.cpp:292) */
+  int nw;             /* -n, frequencies per shell of the default grid */
+} nrg_dm_params;
+
+/* NRG_main with the spectral density of the impurity d operator switched on
+ * (input_nrg.dat calc_density = 1, UpdateBefCut = 1; NRG_main.cpp:334-396):
+ * the sweep of nrg_sweep_run, but the operators f_N and c_d are rotated into
+ * every shell's full eigenbasis, and each shell's energies, Kept flags,
+ * eigenvectors, basis and c_d stay on the device (what SaveArrays writes,
+ * NRGcodehandlerClass.cpp:887-932).  NRG_MODEL_1CH_QS only. */
+nrg_status nrg_sweep_run_dm(nrg_ctx* ctx, const nrg_sweep_config* cfg);
+int nrg_dm_num_shells(const nrg_ctx* ctx);
+
+/* The FDM density-matrix backward sweep of DM_NRG (DM_NRG.cpp:195-383):
+ * partition sums, DM_NRG_SetRhoNmax (DM_NRG_SetRhoNmax.cpp:9-126), then shell
+ * by shell RotateMatrix (RotateMatrix.cpp:17-99) and DM_NRG_CalcRhoN_withSU2
+ * (DM_NRG_CalcRhoN.cpp:252-449).  rho_trace (optional, [nshells]) receives
+ * sum_b (2S_b+1) Tr rho_N(b) per shell. */
+nrg_status nrg_dm_backprop(nrg_ctx* ctx, const nrg_dm_params* prm, double* rho_trace);
+
+/* The c_d spectral function after nrg_dm_backprop (same parameters):
+ * CalcSpecDM_NRG (SpecFuncClass.cpp:1827-1883) over FDM_SpecDens_M_STL
+ * (SpecFunc_allSTL.cpp:1253-2358) and, for the last shell, CalcSpecCosti_T_N
+ * (SpecFuncClass.cpp:417-650).  With omegas != NULL the nomega given
+ * frequencies are used; with omegas == NULL the grid of CalcSpec_ManyOmegas
+ * (SpecFuncClass.cpp:2238-2341, prm->nw points per shell), which must fit in
+ * nomega.  Writes Omega_Rhow: omega_rhow[k] = omega_k and
+ * omega_rhow[nomega + k] = A(omega_k) for k < *nout. */
+nrg_status nrg_lehmann(nrg_ctx* ctx, const nrg_dm_params* prm, int nomega, const double* omegas, double* omega_rhow,
+                       int* nout);
 
 /* Largest block nrg_diag_block_noalloc accepts. */
 #define NRG_NOALLOC_MAX_N 256

@@ -58,10 +58,21 @@ class Timing(ctypes.Structure):
                 ("update_ms", ctypes.c_double), ("tridiag_flops", ctypes.c_double),
                 ("update_flops", ctypes.c_double), ("backtransform_flops", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int64), ("tridiag_launches", ctypes.c_int64),
-                ("device_ms", ctypes.c_double), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
+                ("device_ms", ctypes.c_double), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64),
+                ("dm_backprop_ms", ctypes.c_double), ("dm_spectral_ms", ctypes.c_double),
+                ("lehmann_ms", ctypes.c_double), ("lehmann_pairs", ctypes.c_int64),
+                ("lehmann_evals", ctypes.c_int64)]
+
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class DmParams(ctypes.Structure):
+    """DM_NRG's command-line parameters (nrg_dm_params)."""
+    _fields_ = [("temp", ctypes.c_double), ("mtemp", ctypes.c_int), ("betabar", ctypes.c_double),
+                ("bbroad", ctypes.c_double), ("twindow", ctypes.c_double), ("broadtemp", ctypes.c_double),
+                ("site_dim", ctypes.c_double), ("nw", ctypes.c_int)]
 
 
 _DP = ctypes.POINTER(ctypes.c_double)
@@ -154,6 +165,10 @@ def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     L.nrg_update_ops.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(_Blocks), ctypes.POINTER(_Basis),
                                  ctypes.POINTER(_EigCut), ctypes.c_int, ctypes.POINTER(_Matrix),
                                  ctypes.POINTER(_Matrix)]
+    L.nrg_sweep_run_dm.argtypes = [ctypes.c_void_p, ctypes.POINTER(SweepConfig)]
+    L.nrg_dm_num_shells.argtypes = [ctypes.c_void_p]
+    L.nrg_dm_backprop.argtypes = [ctypes.c_void_p, ctypes.POINTER(DmParams), _dp]
+    L.nrg_lehmann.argtypes = [ctypes.c_void_p, ctypes.POINTER(DmParams), ctypes.c_int, _dp, _dp, _ip]
     L.nrg_sweep_batch.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(SweepConfig), ctypes.c_int,
                                   ctypes.c_int, _dp, _dp, _ip, _dp]
     _lib = L
@@ -308,6 +323,50 @@ class Engine:
             nel = int(mbe.max() + 1) if nmb else 0
             res.append((_arr(m.mat_block_map, 2 * nmb, np.int64), mbe, _arr(m.mat_el, nel, np.float64)))
         return res
+
+    # ---- DM-NRG spectral function ---------------------------------------
+    def sweep_dm(self, nsites: int, ncutoff: int, lam: float, U: float, ed: float, gamma: float,
+                 degen_eps: float = 0.0) -> int:
+        """Forward sweep of the one-channel |Q S> Anderson model keeping the
+        DM-NRG shells on the device; returns the number of shells."""
+        cfg = SweepConfig(MODEL_1CH_QS, nsites, ncutoff, lam, U, ed, gamma, 0.0, degen_eps, PREC_FP64)
+        self._check(self.L.nrg_sweep_run_dm(self.h, ctypes.byref(cfg)))
+        return int(self.L.nrg_dm_num_shells(self.h))
+
+    @staticmethod
+    def dm_params(temp: float = 0.0, mtemp: int = -1, betabar: float = 0.727, bbroad: float = 0.6,
+                  twindow: float = 2.0, broadtemp: float = 0.8, site_dim: float = 4.0, nw: int = 4) -> DmParams:
+        return DmParams(temp, mtemp, betabar, bbroad, twindow, broadtemp, site_dim, nw)
+
+    def dm_backprop(self, prm: DmParams) -> np.ndarray:
+        """Density-matrix backward sweep; returns the trace per shell."""
+        n = int(self.L.nrg_dm_num_shells(self.h))
+        tr = np.zeros(max(n, 1))
+        self._check(self.L.nrg_dm_backprop(self.h, ctypes.byref(prm), tr.ctypes.data_as(_DP)))
+        return tr[:n]
+
+    def lehmann(self, prm: DmParams, omegas=None, capacity: int = 0):
+        """A(omega) of c_d; omegas=None uses the reference's grid.
+        Returns (omega, A)."""
+        n_sh = int(self.L.nrg_dm_num_shells(self.h))
+        if omegas is None:
+            cap = capacity or 2 * prm.nw * n_sh + 8
+            om_ptr = None
+        else:
+            om = np.ascontiguousarray(omegas, dtype=np.float64)
+            cap = len(om)
+            om_ptr = om.ctypes.data_as(_DP)
+        out = np.zeros(2 * max(cap, 1))
+        nout = ctypes.c_int(0)
+        self._check(self.L.nrg_lehmann(self.h, ctypes.byref(prm), cap, om_ptr, out.ctypes.data_as(_DP),
+                                       ctypes.byref(nout)))
+        n = nout.value
+        return out[:n].copy(), out[cap:cap + n].copy()
+
+    def timing(self) -> dict:
+        t = Timing()
+        self._check(self.L.nrg_sweep_timing(self.h, ctypes.byref(t)))
+        return t.as_dict()
 
     def fp64_peak(self) -> float:
         """Measured FP64 FMA throughput of the device, TFLOP/s."""

@@ -75,6 +75,36 @@ struct Packer {
   template <class T> size_t add(const std::vector<T>& v) { return add(v.data(), v.size() * sizeof(T)); }
 };
 
+// Block pairs of an operator and where each dense row-major block starts.
+struct OpMeta {
+  std::vector<int> bi, bj;
+  std::vector<int64_t> off;
+  int64_t size = 0;
+  int find(int i, int j) const {
+    for (size_t k = 0; k < bi.size(); ++k) if (bi[k] == i && bj[k] == j) return (int)k;
+    return -1;
+  }
+};
+
+// One Wilson shell as the DM-NRG backward sweep needs it (what NRG_main
+// saves with UpdateBefCut = 1: Abasis_N, the uncut eigen-array Acut_N and
+// c_d in it), kept on the device between the forward and backward sweeps.
+struct DmShell {
+  std::vector<int> bsize, boff;        // blocks of H_N (all states)
+  std::vector<double> qn;              // (Q,S) per block
+  std::vector<double> en;              // energies after SetE0zero / SetDegen
+  std::vector<unsigned char> kept;     // Kept (E <= Ecut)
+  std::vector<int> kept_src;           // block of each kept block (AeigCut -> Aeig)
+  Basis basis;                         // Abasis_N (segments over shell N-1's kept blocks)
+  OpMeta cd;                           // c_d blocks in this shell's full basis
+  std::vector<int64_t> zoff;           // each block's n x n eigenvector matrix in Z
+  int64_t zsize = 0;
+  DevBuf Z, cdel;                      // eigenvectors (row = eigenvector) and c_d elements
+  DevBuf rho;                          // reduced density matrix, dense blocks laid out like Z
+  DevBuf pairs;                        // Lehmann pairs: dE, W(omega >= 0), W(omega < 0)
+  int64_t npairs = 0;
+};
+
 struct IterResult {
   std::vector<double> params, qn, en, thermo, opavg;
   std::vector<int> bsize, kept_bsize;
@@ -102,6 +132,11 @@ struct nrg_ctx {
   std::vector<double> out_en, out_qn, out_cut_en, out_vec, out_el;
   std::vector<unsigned char> out_kept, out_cut_kept;
   std::vector<int> out_bbe, out_bbe_bc, out_bbe_eig, out_stcf, out_map, out_mbe;
+  // DM-NRG shells of the last nrg_sweep_run_dm, and the density matrices
+  double dm_lambda = 0.0;
+  std::vector<std::unique_ptr<nrg::DmShell>> dm;
+  bool dm_rho_valid = false;
+  double dm_temp = 0.0;                // temperature the density matrices were built for
 };
 
 namespace nrg {
@@ -325,15 +360,6 @@ void run_vectors(nrg_ctx* c, Timer& tm, EigPlan& P, const std::vector<double>& e
 }
 
 // ------------------------------------------------------------------ sweep state
-struct OpMeta {
-  std::vector<int> bi, bj;
-  std::vector<int64_t> off;
-  int64_t size = 0;
-  int find(int i, int j) const {
-    for (size_t k = 0; k < bi.size(); ++k) if (bi[k] == i && bj[k] == j) return (int)k;
-    return -1;
-  }
-};
 
 struct Kept {
   BlockArray blk;        // kept blocks: QNs, kept sizes, offsets
@@ -377,12 +403,17 @@ struct AsmTables {
 // per-state rows (segment, old state, site type, E_old), per block the
 // (old block pair, operator) -> operator block offsets, the coefficient
 // tables, and sizes H/d/e/tau/ev/en for the blocks.  `oldops` describe the
-// operators (device pointers `hops`) in the old kept structure whose block
-// sizes are `old_size`.
+// operators (device pointers `hops`) in the block structure whose block
+// sizes are `old_size`; opblock maps a block of the previous kept array to
+// that structure's block (NULL: the operators live in the kept array itself).
+// Kept states are the leading states of their block, so a state's row is the
+// same in both.
 AsmTables prepare_assembly(nrg_ctx* c, const ModelSpec& m, const Basis& B, const HNTables& tabs,
                            const std::vector<double>& st_eold, const std::vector<OpMeta>& oldops,
                            const std::vector<int>& old_size, int nops_h, const std::vector<const double*>& hops,
-                           double lambda, const double chi[2], double eN) {
+                           double lambda, const double chi[2], double eN,
+                           const std::vector<int>* opblock = nullptr) {
+  auto ob = [&](int k) { return opblock ? (*opblock)[k] : k; };
   AsmTables T;
   EigPlan& P = T.P;
   const int nb = B.blk.nblocks();
@@ -409,8 +440,8 @@ AsmTables prepare_assembly(nrg_ctx* c, const ModelSpec& m, const Basis& B, const
       for (size_t q = 0; q < sg.size(); ++q)
         for (int o = 0; o < nops_h; ++o) {
           const OpMeta& om = oldops[o];
-          int kf = om.find(sg[p].old_block, sg[q].old_block);
-          int kb = om.find(sg[q].old_block, sg[p].old_block);
+          int kf = om.find(ob(sg[p].old_block), ob(sg[q].old_block));
+          int kb = om.find(ob(sg[q].old_block), ob(sg[p].old_block));
           pair_fwd.push_back(kf >= 0 ? om.off[kf] : -1);
           pair_fwd_ld.push_back(kf >= 0 ? old_size[om.bj[kf]] : 0);
           pair_bwd.push_back(kb >= 0 ? om.off[kb] : -1);
@@ -461,19 +492,24 @@ struct UpdatePlan {
   std::vector<OpMeta> newops;
   std::vector<RotJob> jobs;
   std::vector<GatherTerm> terms, terms1;
-  std::vector<int> t1term, t1mn, gfirst, gcount, tjob, tmn;
+  std::vector<int> g1first, g1count, t1group, t1mn, gfirst, gcount, tjob, tmn;
   int64_t tsize = 0;
   Packer up;
-  size_t o_t1 = 0, o_t1t = 0, o_t1m = 0, o_terms = 0, o_gf = 0, o_gc = 0, o_jobs = 0, o_tj = 0, o_tm = 0;
+  size_t o_t1 = 0, o_g1f = 0, o_g1c = 0, o_t1g = 0, o_t1m = 0, o_terms = 0, o_gf = 0, o_gc = 0, o_jobs = 0,
+         o_tj = 0, o_tm = 0;
   size_t o_old = 0, o_new = 0;
   char* ub = nullptr;  // device copy of `up` once launched
 };
 
 // kept: the new kept structure (K.src = block of B each kept block came
 // from); yoff/bsize: where each B block's kept eigenvector rows sit in c->Z
-// (kept x n, row-major) and c->Zt (n x kept).
+// (kept x n, row-major) and c->Zt (n x kept).  opblock maps a block of the
+// previous kept array (a segment's old_block) to the block the old operators
+// are stored by (NULL: the same block).
 void plan_update(UpdatePlan& U, const ModelSpec& m, const Basis& B, const EigPlan& P, const Kept& K,
-                 const std::vector<OpMeta>& oldops) {
+                 const std::vector<OpMeta>& oldops, const std::vector<int>* opblock = nullptr,
+                 const std::vector<int>* opsize = nullptr) {
+  auto ob = [&](int k) { return opblock ? (*opblock)[k] : k; };
   const int nops = (int)m.op_kind.size();
   U.newops.assign(nops, OpMeta());
   const int nk = K.blk.nblocks();
@@ -498,40 +534,52 @@ void plan_update(UpdatePlan& U, const ModelSpec& m, const Basis& B, const EigPla
           for (int u = 0; u < p.nsite; ++u) {
             const int tu_ = m.site.blk.offset[p.site_block] + u;
             const int first = (int)U.terms.size();
+            const int first1 = (int)U.terms1.size();
             for (const Segment& q : segJ)
               for (int v = 0; v < q.nsite; ++v) {
                 const int tv = m.site.blk.offset[q.site_block] + v;
                 GatherTerm G{};
                 G.job = jid; G.dst_base = p.offset + u; G.dst_stride = p.nsite; G.rows = p.count;
                 G.src_base = q.offset + v; G.src_stride = q.nsite; G.srows = q.count;
-                if (m.op_kind[o] == OP_IMPONLY) {
-                  if (tu_ != tv) continue;
+                if (m.op_kind[o] == OP_IMPONLY || m.op_kind[o] == OP_CD_QS) {
+                  double g = 1.0;
+                  if (m.op_kind[o] == OP_IMPONLY) {
+                    if (tu_ != tv) continue;
+                  } else {
+                    g = op_site_factor(m, m.op_kind[o], SI, SJ, tu_, tv);
+                    if (g == 0.0) continue;
+                  }
                   const OpMeta& om = oldops[o];
-                  int kx = om.find(p.old_block, q.old_block);
+                  int kx = om.find(ob(p.old_block), ob(q.old_block));
                   if (kx < 0) continue;
-                  G.mode = 1; G.coef = 1.0; G.old_off = om.off[kx]; G.op = o;
+                  G.mode = 1; G.coef = g; G.old_off = om.off[kx]; G.op = o;
+                  G.old_ld = opsize ? (*opsize)[ob(q.old_block)] : q.count;
                 } else {
                   if (p.old_block != q.old_block) continue;
                   double g = op_site_factor(m, m.op_kind[o], SI, SJ, tu_, tv);
                   if (g == 0.0) continue;
                   G.mode = 0; G.coef = g;
                 }
-                if (G.mode == 1) {  // old block x Zt rows: tiled GEMM, one destination per term
-                  const int tid1 = (int)U.terms1.size();
+                if (G.mode == 1) {  // old block x Zt rows: tiled GEMM over the row group's terms
                   U.terms1.push_back(G);
-                  for (int mt = 0; mt * 64 < G.rows; ++mt)
-                    for (int nt = 0; nt * 64 < J.kj; ++nt) { U.t1term.push_back(tid1); U.t1mn.push_back((mt << 16) | nt); }
                   continue;
                 }
                 U.terms.push_back(G);
               }
             if ((int)U.terms.size() > first) { U.gfirst.push_back(first); U.gcount.push_back((int)U.terms.size() - first); }
+            if ((int)U.terms1.size() > first1) {
+              const int gid = (int)U.g1first.size();
+              U.g1first.push_back(first1); U.g1count.push_back((int)U.terms1.size() - first1);
+              for (int mt = 0; mt * 64 < p.count; ++mt)
+                for (int nt = 0; nt * 64 < J.kj; ++nt) { U.t1group.push_back(gid); U.t1mn.push_back((mt << 16) | nt); }
+            }
           }
         for (int mt = 0; mt * 64 < J.ki; ++mt)
           for (int nt = 0; nt * 64 < J.kj; ++nt) { U.tjob.push_back(jid); U.tmn.push_back((mt << 16) | nt); }
       }
   }
-  U.o_t1 = U.up.add(U.terms1); U.o_t1t = U.up.add(U.t1term); U.o_t1m = U.up.add(U.t1mn);
+  U.o_t1 = U.up.add(U.terms1); U.o_g1f = U.up.add(U.g1first); U.o_g1c = U.up.add(U.g1count);
+  U.o_t1g = U.up.add(U.t1group); U.o_t1m = U.up.add(U.t1mn);
   U.o_terms = U.up.add(U.terms); U.o_gf = U.up.add(U.gfirst); U.o_gc = U.up.add(U.gcount);
   U.o_jobs = U.up.add(U.jobs); U.o_tj = U.up.add(U.tjob); U.o_tm = U.up.add(U.tmn);
 }
@@ -550,8 +598,9 @@ void launch_update_plan(nrg_ctx* c, Timer& tm, UpdatePlan& U) {
   ua.Z = c->Z.as<double>(); ua.Zt = c->Zt.as<double>(); ua.T = c->T.as<double>();
   ua.old_ops = (const double* const*)(ub + U.o_old); ua.new_ops = (double* const*)(ub + U.o_new);
   ua.tile_job = (const int*)(ub + U.o_tj); ua.tile_mn = (const int*)(ub + U.o_tm); ua.ntiles = (int)U.tjob.size();
-  ua.terms1 = (const GatherTerm*)(ub + U.o_t1); ua.tile1_term = (const int*)(ub + U.o_t1t);
-  ua.tile1_mn = (const int*)(ub + U.o_t1m); ua.ntiles1 = (int)U.t1term.size();
+  ua.terms1 = (const GatherTerm*)(ub + U.o_t1); ua.group1_first = (const int*)(ub + U.o_g1f);
+  ua.group1_count = (const int*)(ub + U.o_g1c); ua.tile1_group = (const int*)(ub + U.o_t1g);
+  ua.tile1_mn = (const int*)(ub + U.o_t1m); ua.ntiles1 = (int)U.t1group.size();
   launch_update(ua, c->stream);
   if (ua.ntiles1 > 0) c->launches++;
   c->launches += 2;
@@ -559,10 +608,17 @@ void launch_update_plan(nrg_ctx* c, Timer& tm, UpdatePlan& U) {
   tm.stop(tu, &c->timing.update_ms);
 }
 
-void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
+// dm: NRG_main with the spectral density switched on (calcdens = 1,
+// UpdateBefCut = 1; CodeHandler_ModelSwitch.cpp:162-176, NRG_main.cpp:334-396):
+// the operators are f_N and c_d, they are rotated into the full (uncut)
+// eigenbasis of every shell, and each shell's eigen-array, eigenvectors and
+// c_d stay on the device for the DM-NRG backward sweep.
+void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false) {
   using clock = std::chrono::steady_clock;
   auto t_begin = clock::now();
   if (cfg->model < 0 || cfg->model > 2) throw NrgError(NRG_ERR_ARG, "unknown model");
+  if (dm && cfg->model != NRG_MODEL_1CH_QS)
+    throw NrgError(NRG_ERR_ARG, "DM-NRG shells are available for the one-channel |Q S> model");
   if (cfg->nsites < 1 || cfg->ncutoff < 4 || !(cfg->lambda > 1.0)) throw NrgError(NRG_ERR_ARG, "bad sweep parameters");
   if (cfg->precision != NRG_PREC_FP64) throw NrgError(NRG_ERR_ARG, "unsupported precision");
   c->iters.clear();
@@ -573,6 +629,15 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
   S.c = c;
   S.m = make_model((ModelKind)cfg->model);
   S.cfg = *cfg;
+  if (dm) {
+    S.m.op_kind = {OP_F_QS, OP_CD_QS};
+    S.m.op_check = {CHK_QS_CD, CHK_QS_CD};
+    S.m.op_name = {"fN", "cdot1"};
+    S.m.op_avg = {0, 0};
+    c->dm.clear();
+    c->dm_rho_valid = false;
+    c->dm_lambda = cfg->lambda;
+  }
   const ModelSpec& m = S.m;
   const double eps = cfg->degen_eps > 0 ? cfg->degen_eps : 1.0e-18;
   const double lambda = cfg->lambda;
@@ -594,7 +659,11 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
 
   // H_{-1} (the initial CutStates keeps everything: Ncutoff >= 4 states).
   StartState st = make_start(m, lambda, cfg->U, cfg->ed, cfg->gamma2_or_B);
+  if (dm) st.ops = {st.ops[0], st.ops[0]};  // c_d at H_{-1} is a copy of f (Main_SetH0.cpp:1958-1961)
   S.kept.blk = st.blk;
+  // Operators are stored by the blocks of `opsize`; opblock maps a kept
+  // block to that structure (empty: the kept array itself).
+  std::vector<int> opsize = st.blk.size, opblock;
   std::vector<double> kept_en = st.en;
   for (int o = 0; o < nops; ++o) {
     OpMeta om;
@@ -629,7 +698,8 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
     for (size_t g = 0; g < B.stcf.size(); ++g) st_eold[g] = kept_en[B.stcf[g]];
     std::vector<const double*> hops(8, nullptr);
     for (int o = 0; o < nops; ++o) hops[o] = S.opbuf(S.cur, o)->as<double>();
-    AsmTables AT = prepare_assembly(c, m, B, tabs, st_eold, S.ops, S.kept.blk.size, nops_h, hops, lambda, chi, eN);
+    AsmTables AT = prepare_assembly(c, m, B, tabs, st_eold, S.ops, opsize, nops_h, hops, lambda, chi, eN,
+                                    opblock.empty() ? nullptr : &opblock);
     EigPlan& P = AT.P;
     std::vector<int>& order = AT.order;
     char* mb = c->meta.as<char>();
@@ -692,12 +762,17 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
     for (int x : K.blk.size) R.kept_bsize.push_back(x);
     // ---------------- kept eigenvectors
     P.nvec.assign(nb, 0);
-    for (int b = 0; b < nb; ++b) P.nvec[b] = keptb[b];
+    for (int b = 0; b < nb; ++b) P.nvec[b] = dm ? P.bsize[b] : keptb[b];
     // eigenvalues for clustering: shifted energies have the same gaps
     run_vectors(c, tm, P, R.en, aa.bsize, aa.hoff, aa.bstate);
     // ---------------- UpdateMatrices
     UpdatePlan U;
-    plan_update(U, m, B, P, K, S.ops);
+    Kept Kfull;  // UpdateBefCut: rotate into every state of H_N
+    if (dm) {
+      Kfull.blk = B.blk;
+      for (int b = 0; b < nb; ++b) Kfull.src.push_back(b);
+    }
+    plan_update(U, m, B, P, dm ? Kfull : K, S.ops, opblock.empty() ? nullptr : &opblock, &opsize);
     std::vector<OpMeta>& newops = U.newops;
     const int nk = K.blk.nblocks();
     int nxt = 1 - S.cur;
@@ -747,6 +822,27 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
       if (!(std::fabs(Zk) < 1.e-20)) s = s / Zk;
       R.opavg.push_back(s);
     }
+    // ---------------- DM-NRG shell (SaveArrays, NRGcodehandlerClass.cpp:887-932)
+    if (dm) {
+      auto sh = std::make_unique<DmShell>();
+      sh->bsize = P.bsize; sh->boff = P.soff; sh->qn = B.blk.qn; sh->en = R.en;
+      sh->kept.resize(P.nstates);
+      for (int g = 0; g < P.nstates; ++g) sh->kept[g] = R.en[g] <= R.ecut ? 1 : 0;
+      sh->kept_src = K.src;
+      sh->cd = newops[1];
+      sh->zoff = P.yoff; sh->zsize = P.ysize;
+      sh->Z.ensure(sizeof(double) * std::max<int64_t>(P.ysize, 1));
+      CU(cudaMemcpyAsync(sh->Z.p, c->Z.p, sizeof(double) * P.ysize, cudaMemcpyDeviceToDevice, c->stream));
+      sh->cdel.ensure(sizeof(double) * std::max<int64_t>(newops[1].size, 1));
+      CU(cudaMemcpyAsync(sh->cdel.p, newptr[1], sizeof(double) * newops[1].size, cudaMemcpyDeviceToDevice,
+                         c->stream));
+      sh->basis = std::move(B);
+      c->dm.push_back(std::move(sh));
+      opsize = P.bsize;
+      opblock = K.src;
+    } else {
+      opsize = K.blk.size;
+    }
     // ---------------- next iteration
     S.kept = K;
     kept_en = new_kept_en;
@@ -762,6 +858,341 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg) {
   c->timing.device_ms = span_ms;
   c->timing.kernel_launches = c->launches - launches0;
   c->timing.total_ms = std::chrono::duration<double, std::milli>(clock::now() - t_begin).count();
+}
+
+// ------------------------------------------------------------------ DM-NRG
+// CalcDN (CalcDN.cpp) with z = 1: the energy scale of shell N.
+double calc_dn(double L, int N) {
+  const double hlf = L > 0.0 ? 0.5 * (1.0 + (1.0 / L)) : 1.0;
+  return hlf * std::pow(L, (-(N - 1) / 2.0) - 1.0 + 1.0);
+}
+
+struct DmResolved {
+  double temp, tempbar0, betabar, bbroad, twindow, broadtemp, site_dim;
+};
+
+// The temperature logic of DM_NRG.cpp:100-121: Mtemp < Nsitesmax-1 puts T at
+// D_Mtemp/betabar (and SetRhoNmax gets T/D_Mtemp); otherwise T is
+// D_{Nsitesmax+199}/betabar, or the caller's positive temp, and SetRhoNmax
+// gets T/D_{Nsitesmax-1}.
+DmResolved dm_resolve(const nrg_dm_params* p, double L, int nsites) {
+  if (!p) throw NrgError(NRG_ERR_ARG, "DM-NRG parameters are NULL");
+  if (!(p->betabar > 0.0) || !(p->bbroad > 0.0) || !(p->broadtemp > 0.0) || !(p->site_dim > 0.0) ||
+      p->twindow < 0.0)
+    throw NrgError(NRG_ERR_ARG, "betabar, bbroad, broadtemp and site_dim must be positive");
+  DmResolved r{0, 0, p->betabar, p->bbroad, p->twindow, p->broadtemp, p->site_dim};
+  if (p->mtemp >= 0 && p->mtemp < nsites - 1) {
+    const double DM = calc_dn(L, p->mtemp);
+    r.temp = DM / p->betabar;
+    r.tempbar0 = r.temp / DM;
+  } else {
+    r.temp = p->temp > 0.0 ? p->temp : calc_dn(L, nsites + 199) / p->betabar;
+    r.tempbar0 = r.temp / calc_dn(L, nsites - 1);
+  }
+  return r;
+}
+
+// (2S+1)-weighted Boltzmann sums over all / discarded states of a shell
+// (PartitionFunc / PartitionFuncDisc, NRGarrayClass.cpp:997-1060).
+double dm_partition(const DmShell& s, double beta, bool disc_only) {
+  double sum = 0.0;
+  for (size_t b = 0; b < s.bsize.size(); ++b) {
+    const double Si = s.qn[2 * b + 1];
+    for (int i = s.boff[b]; i < s.boff[b] + s.bsize[b]; ++i)
+      if (!disc_only || !s.kept[i]) sum += (2.0 * Si + 1.0) * std::exp(-beta * s.en[i]);
+  }
+  return sum;
+}
+
+struct GemmPlan {
+  std::vector<GemmJob> jobs;
+  std::vector<int> tjob, tmn;
+  void add(const GemmJob& J) {
+    const int id = (int)jobs.size();
+    jobs.push_back(J);
+    for (int mt = 0; mt * 64 < J.m; ++mt)
+      for (int nt = 0; nt * 64 < J.n; ++nt) { tjob.push_back(id); tmn.push_back((mt << 16) | nt); }
+  }
+};
+
+void run_gemm_plan(nrg_ctx* c, const GemmPlan& G) {
+  if (G.jobs.empty()) return;
+  Packer pk;
+  size_t oj = pk.add(G.jobs), ot = pk.add(G.tjob), om = pk.add(G.tmn);
+  c->vmeta.ensure(pk.host.size() + 256);
+  h2d(c, c->vmeta.p, pk.host.data(), pk.host.size());
+  char* b = c->vmeta.as<char>();
+  launch_gemm_jobs((const GemmJob*)(b + oj), (const int*)(b + ot), (const int*)(b + om), (int)G.tjob.size(), c->stream);
+  c->launches++;
+}
+
+// DM_NRG_SetRhoNmax + (RotateMatrix, DM_NRG_CalcRhoN_withSU2) per shell, FDM.
+void dm_backprop_impl(nrg_ctx* c, const nrg_dm_params* prm, double* rho_trace) {
+  if (c->dm.empty()) throw NrgError(NRG_ERR_STATE, "no DM-NRG shells: run nrg_sweep_run_dm first");
+  const int nsh = (int)c->dm.size(), Nmax = nsh - 1;
+  const double L = c->dm_lambda;
+  const DmResolved p = dm_resolve(prm, L, nsh);
+  Timer tm(c);
+  cudaEvent_t t0 = tm.start();
+  // Partition sums (DM_NRG.cpp:201-257).
+  double TempBar = p.temp / calc_dn(L, Nmax - 1);
+  double ZTot = dm_partition(*c->dm[Nmax], 1.0 / TempBar, false);
+  for (int N = Nmax - 1; N >= 0; --N) {
+    TempBar = p.temp / calc_dn(L, N - 1);
+    ZTot += dm_partition(*c->dm[N], 1.0 / TempBar, true) * std::pow(p.site_dim, Nmax - N);
+  }
+  {  // SetRhoNmax (DM_NRG_SetRhoNmax.cpp:9-126): diagonal Boltzmann weights.
+    DmShell& s = *c->dm[Nmax];
+    const double beta = std::fabs(p.tempbar0) < 1.e-20 ? 1.0e10 : 1.0 / p.tempbar0;
+    std::vector<double> R((size_t)std::max<int64_t>(s.zsize, 1), 0.0);
+    for (size_t b = 0; b < s.bsize.size(); ++b) {
+      const int n = s.bsize[b];
+      for (int i = 0; i < n; ++i) R[s.zoff[b] + (int64_t)i * n + i] = std::exp(-beta * s.en[s.boff[b] + i]) / ZTot;
+    }
+    s.rho.ensure(sizeof(double) * R.size());
+    h2d(c, s.rho.p, R.data(), sizeof(double) * s.zsize);
+  }
+  for (int N = Nmax - 1; N >= 0; --N) {
+    DmShell& sN = *c->dm[N];
+    DmShell& s1 = *c->dm[N + 1];
+    // RotateMatrix: rho~_b = Z_b^T (rho_b Z_b), Z_b rows = eigenvectors.
+    const size_t zs = sizeof(double) * std::max<int64_t>(s1.zsize, 1);
+    c->T.ensure(2 * zs + 512);
+    double* Tm = c->T.as<double>();
+    double* rot = (double*)((char*)c->T.p + ((zs + 255) & ~size_t(255)));
+    GemmPlan g1, g2;
+    for (size_t b = 0; b < s1.bsize.size(); ++b) {
+      const int n = s1.bsize[b];
+      const double* Z = s1.Z.as<double>() + s1.zoff[b];
+      g1.add(GemmJob{n, n, n, 0, s1.rho.as<double>() + s1.zoff[b], n, Z, n, Tm + s1.zoff[b], n});
+      g2.add(GemmJob{n, n, n, 1, Z, n, Tm + s1.zoff[b], n, rot + s1.zoff[b], n});
+    }
+    run_gemm_plan(c, g1);
+    run_gemm_plan(c, g2);
+    // Partial trace over the child states (DM_NRG_SetChildSt, SetChildSameType).
+    const Basis& B1 = s1.basis;
+    const int nbN = (int)sN.bsize.size();
+    const ModelSpec ms = make_model(MODEL_1CHQS);
+    std::vector<std::vector<DmTraceTerm>> per(nbN);
+    for (int nb1 = 0; nb1 < B1.blk.nblocks(); ++nb1) {
+      const double Si = B1.blk.q(nb1, 1);
+      for (const Segment& sg : B1.seg[nb1]) {
+        const int fb = sN.kept_src[sg.old_block];
+        const double Sold = sN.qn[2 * fb + 1];
+        for (int u = 0; u < sg.nsite; ++u) {
+          // S of the site state.
+          const int t = ms.site.blk.offset[sg.site_block] + u;
+          const double St = ms.site.blk.q(ms.site.block_of_state(t), 1);
+          double cgf = 0.0;
+          for (double Sz = -Si; Sz <= Si; Sz += 1.0) {
+            const double x = clebsch(Sold, Sold, St, Sz - Sold, Si, Sz);
+            cgf += x * x;
+          }
+          per[fb].push_back(DmTraceTerm{s1.zoff[nb1], s1.bsize[nb1], sg.offset + u, sg.nsite, sg.count, cgf});
+        }
+      }
+    }
+    std::vector<DmTraceTerm> terms;
+    std::vector<int> tfirst(nbN), tcount(nbN), nkept(nbN, 0);
+    for (int b = 0; b < nbN; ++b) {
+      tfirst[b] = (int)terms.size();
+      tcount[b] = (int)per[b].size();
+      terms.insert(terms.end(), per[b].begin(), per[b].end());
+      while (nkept[b] < sN.bsize[b] && sN.kept[sN.boff[b] + nkept[b]]) nkept[b]++;
+    }
+    Packer pk;
+    size_t o_bs = pk.add(sN.bsize), o_so = pk.add(sN.boff), o_ro = pk.add(sN.zoff), o_nk = pk.add(nkept),
+           o_tf = pk.add(tfirst), o_tc = pk.add(tcount), o_t = pk.add(terms), o_en = pk.add(sN.en),
+           o_kp = pk.add(sN.kept);
+    c->meta.ensure(pk.host.size() + 256);
+    h2d(c, c->meta.p, pk.host.data(), pk.host.size());
+    char* mb = c->meta.as<char>();
+    sN.rho.ensure(sizeof(double) * std::max<int64_t>(sN.zsize, 1));
+    TempBar = p.temp / calc_dn(L, N - 1);
+    DmTraceArgs ta{};
+    ta.bsize = (const int*)(mb + o_bs); ta.soff = (const int*)(mb + o_so); ta.roff = (const int64_t*)(mb + o_ro);
+    ta.nkept = (const int*)(mb + o_nk); ta.term_first = (const int*)(mb + o_tf); ta.term_count = (const int*)(mb + o_tc);
+    ta.terms = (const DmTraceTerm*)(mb + o_t); ta.rot = rot; ta.en = (const double*)(mb + o_en);
+    ta.kept = (const unsigned char*)(mb + o_kp); ta.beta = 1 / TempBar;
+    ta.zdisc = ZTot / std::pow(p.site_dim, Nmax - N); ta.rho = sN.rho.as<double>();
+    launch_dm_trace(ta, nbN, c->stream);
+    c->launches++;
+    CU(cudaStreamSynchronize(c->stream));  // meta and T are reused by the next shell
+  }
+  tm.stop(t0, &c->timing.dm_backprop_ms);
+  CU(cudaStreamSynchronize(c->stream));
+  check_flag(c);
+  tm.collect();
+  c->dm_rho_valid = true;
+  c->dm_temp = p.temp;
+  if (rho_trace) {
+    for (int N = 0; N < nsh; ++N) {
+      const DmShell& s = *c->dm[N];
+      std::vector<double> R((size_t)std::max<int64_t>(s.zsize, 1));
+      d2h(c, R.data(), s.rho.p, sizeof(double) * s.zsize);
+      CU(cudaStreamSynchronize(c->stream));
+      double t = 0.0;
+      for (size_t b = 0; b < s.bsize.size(); ++b) {
+        const int n = s.bsize[b];
+        for (int i = 0; i < n; ++i) t += (2.0 * s.qn[2 * b + 1] + 1.0) * R[s.zoff[b] + (int64_t)i * n + i];
+      }
+      rho_trace[N] = t;
+    }
+  }
+}
+
+// CalcSpec_ManyOmegas's frequency grid (SpecFuncClass.cpp:2238-2341), FDM:
+// nw points per shell from shell 2 to the last-but-one, negative side first.
+std::vector<double> dm_grid(double L, int nsh, int nw) {
+  const double factorWN = std::pow(L, 1.25);
+  const int Nmax = nsh - 1, N0 = 2;
+  std::vector<double> om;
+  for (int N = N0; N <= Nmax; ++N) {
+    const double WN = factorWN * calc_dn(L, N);
+    for (int i = 0; i < nw; ++i) om.push_back(-(std::pow(L, -((double)i / (2.0 * nw))) * WN));
+  }
+  for (int N = Nmax; N >= N0; --N) {
+    const double WN = factorWN * calc_dn(L, N);
+    for (int i = nw - 1; i >= 0; --i) om.push_back(std::pow(L, -((double)i / (2.0 * nw))) * WN);
+  }
+  return om;
+}
+
+// CalcSpecDM_NRG (SpecFuncClass.cpp:1827-1883) with FDM_SpecDens_M_STL /
+// CalcSpecCosti_T_N for every shell of the window, for all frequencies.
+void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double* omegas, double* omega_rhow,
+                  int* nout) {
+  if (!c->dm_rho_valid) throw NrgError(NRG_ERR_STATE, "no density matrices: run nrg_dm_backprop first");
+  if (!omega_rhow || !nout || nomega < 0) throw NrgError(NRG_ERR_ARG, "bad output arguments");
+  const int nsh = (int)c->dm.size(), Nmax = nsh - 1;
+  const double L = c->dm_lambda, hlf = 0.5 * (1.0 + (1.0 / L));
+  const DmResolved p = dm_resolve(prm, L, nsh);
+  if (p.temp != c->dm_temp) throw NrgError(NRG_ERR_STATE, "temperature differs from the one of nrg_dm_backprop");
+  std::vector<double> om;
+  if (omegas) om.assign(omegas, omegas + nomega);
+  else {
+    if (prm->nw < 1) throw NrgError(NRG_ERR_ARG, "nw must be positive");
+    om = dm_grid(L, nsh, prm->nw);
+    if ((int)om.size() > nomega) throw NrgError(NRG_ERR_SIZE, "omega_rhow holds fewer frequencies than the grid");
+  }
+  const int nw_ = (int)om.size();
+  Timer tm(c);
+  cudaEvent_t t0 = tm.start();
+  // Lehmann pairs of every shell.
+  std::vector<int64_t> shell_off(nsh + 1, 0);
+  for (int N = 0; N < nsh; ++N) {
+    const DmShell& s = *c->dm[N];
+    int64_t np = 0;
+    for (size_t k = 0; k < s.cd.bi.size(); ++k) np += (int64_t)s.bsize[s.cd.bi[k]] * s.bsize[s.cd.bj[k]];
+    shell_off[N + 1] = shell_off[N] + np;
+  }
+  const int64_t ptot = std::max<int64_t>(shell_off[nsh], 1);
+  c->ev.ensure(sizeof(double) * 3 * ptot);  // dE | Wp | Wn for all shells
+  double* dE = c->ev.as<double>();
+  double* Wp = dE + ptot;
+  double* Wn = Wp + ptot;
+  const double beta_last = std::fabs(p.temp) < 1.e-20 ? 1.0e10 : p.betabar;
+  for (int N = 0; N < nsh; ++N) {
+    DmShell& s = *c->dm[N];
+    const bool last = N == Nmax;
+    std::vector<DmPair> pairs;
+    GemmPlan g;
+    int64_t poff = 0;
+    std::vector<int> nk(s.bsize.size(), 0), nd(s.bsize.size(), 0);
+    for (size_t b = 0; b < s.bsize.size(); ++b)
+      for (int i = 0; i < s.bsize[b]; ++i) (s.kept[s.boff[b] + i] ? nk[b] : nd[b])++;
+    const int64_t pbytes = shell_off[N + 1] - shell_off[N];
+    c->Y.ensure(sizeof(double) * std::max<int64_t>(2 * pbytes, 1));
+    double* P1 = c->Y.as<double>();
+    double* P2 = P1 + pbytes;
+    for (size_t k = 0; k < s.cd.bi.size(); ++k) {
+      const int b1 = s.cd.bi[k], b2 = s.cd.bj[k];
+      DmPair P{};
+      P.n1 = s.bsize[b1]; P.n2 = s.bsize[b2]; P.s1 = s.boff[b1]; P.s2 = s.boff[b2];
+      P.a_off = s.cd.off[k]; P.p_off = poff; P.out_off = shell_off[N] + poff;
+      const double S1 = s.qn[2 * b1 + 1], S2 = s.qn[2 * b2 + 1];
+      double cgf = 0.0;
+      for (double Sz1 = -S1; Sz1 <= S1; Sz1 += 1.0) {
+        const double x = clebsch(S1, Sz1, 0.5, 0.5, S2, Sz1 + 0.5);
+        cgf += x * x;
+      }
+      P.cg = cgf;
+      P.skip = ((nk[b1] == 0 && nk[b2] == 0) || (nd[b1] == 0 && nd[b2] == 0)) ? 1 : 0;
+      if (!last && !P.skip) {
+        const double* Acd = s.cdel.as<double>() + P.a_off;
+        g.add(GemmJob{P.n1, P.n2, P.n1, 0, s.rho.as<double>() + s.zoff[b1], P.n1, Acd, P.n2, P1 + poff, P.n2});
+        g.add(GemmJob{P.n1, P.n2, P.n2, 0, Acd, P.n2, s.rho.as<double>() + s.zoff[b2], P.n2, P2 + poff, P.n2});
+      }
+      pairs.push_back(P);
+      poff += (int64_t)P.n1 * P.n2;
+    }
+    run_gemm_plan(c, g);
+    Packer pk;
+    size_t o_p = pk.add(pairs), o_en = pk.add(s.en), o_kp = pk.add(s.kept);
+    c->meta.ensure(pk.host.size() + 256);
+    h2d(c, c->meta.p, pk.host.data(), pk.host.size());
+    char* mb = c->meta.as<char>();
+    DmPairArgs a{};
+    a.pairs = (const DmPair*)(mb + o_p); a.cd = s.cdel.as<double>(); a.P1 = P1; a.P2 = P2;
+    a.en = (const double*)(mb + o_en); a.kept = (const unsigned char*)(mb + o_kp);
+    a.last = last ? 1 : 0;
+    a.beta_last = beta_last;
+    if (last) {
+      double z = 0.0;
+      for (size_t b = 0; b < s.bsize.size(); ++b)
+        for (int i = s.boff[b]; i < s.boff[b] + s.bsize[b]; ++i)
+          z += (2.0 * s.qn[2 * b + 1] + 1.0) * std::exp(-beta_last * s.en[i]);
+      a.inv_z_last = 1.0 / z;
+    }
+    a.dE = dE; a.Wp = Wp; a.Wn = Wn;
+    launch_dm_pairs(a, (int)pairs.size(), c->stream);
+    c->launches++;
+    CU(cudaStreamSynchronize(c->stream));  // meta, vmeta and Y are reused by the next shell
+  }
+  // Windows of shells per frequency (CalcNfromOmega, SpecFuncClass.cpp:41-49).
+  const int window = 22;
+  std::vector<int> wfirst(nw_), wcount(nw_);
+  for (int k = 0; k < nw_; ++k) {
+    int iaux = (int)(2.0 * std::log(2.0 * std::fabs(om[k]) / hlf) / std::log(L));
+    iaux = 1 - iaux;
+    if (iaux < 0) iaux = 0;
+    const int N0 = iaux - 8 > 0 ? iaux - 8 : 0;
+    const int N1 = iaux + 14 < nsh ? iaux + 14 : nsh;
+    wfirst[k] = N0;
+    wcount[k] = std::max(0, N1 - N0);
+  }
+  std::vector<double> dn(nsh), tdn(nsh);
+  for (int N = 0; N < nsh; ++N) { dn[N] = calc_dn(L, N); tdn[N] = p.temp / dn[N]; }
+  Packer pk;
+  size_t o_om = pk.add(om), o_wf = pk.add(wfirst), o_wc = pk.add(wcount), o_so = pk.add(shell_off), o_dn = pk.add(dn),
+         o_td = pk.add(tdn);
+  c->meta.ensure(pk.host.size() + 256);
+  h2d(c, c->meta.p, pk.host.data(), pk.host.size());
+  char* mb = c->meta.as<char>();
+  c->partial.ensure(sizeof(double) * std::max<size_t>((size_t)nw_ * window + nw_, 64 * 16));
+  LehmannArgs la{};
+  la.nomega = nw_; la.omega = (const double*)(mb + o_om); la.win_first = (const int*)(mb + o_wf);
+  la.win_count = (const int*)(mb + o_wc); la.window = window; la.shell_off = (const int64_t*)(mb + o_so);
+  la.dE = dE; la.Wp = Wp; la.Wn = Wn; la.dn = (const double*)(mb + o_dn); la.tempdn = (const double*)(mb + o_td);
+  la.b = p.bbroad; la.twindow = p.twindow; la.broadtemp = p.broadtemp;
+  la.partial = c->partial.as<double>(); la.out = la.partial + (size_t)nw_ * window;
+  cudaEvent_t t1 = tm.start();
+  launch_lehmann(la, c->stream);
+  c->launches += 2;
+  tm.stop(t1, &c->timing.lehmann_ms);
+  std::vector<double> A(nw_);
+  d2h(c, A.data(), la.out, sizeof(double) * nw_);
+  tm.stop(t0, &c->timing.dm_spectral_ms);
+  CU(cudaStreamSynchronize(c->stream));
+  check_flag(c);
+  tm.collect();
+  int64_t evals = 0;
+  for (int k = 0; k < nw_; ++k)
+    for (int s = 0; s < wcount[k]; ++s) evals += shell_off[wfirst[k] + s + 1] - shell_off[wfirst[k] + s];
+  c->timing.lehmann_pairs = shell_off[nsh];
+  c->timing.lehmann_evals = evals;
+  for (int k = 0; k < nw_; ++k) { omega_rhow[k] = om[k]; omega_rhow[nomega + k] = A[k]; }
+  *nout = nw_;
 }
 
 // DiagBlock for a batch of blocks given in the reference's packed upper
@@ -1324,6 +1755,41 @@ nrg_status nrg_update_ops(nrg_ctx* ctx, int model, const nrg_blocks* old_kept, c
   GUARD(ctx, {
     CU(cudaSetDevice(ctx->device));
     update_ops_impl(ctx, model, old_kept, abasis, acut, nops, old_ops, new_ops);
+  });
+  return NRG_OK;
+}
+
+nrg_status nrg_sweep_run_dm(nrg_ctx* ctx, const nrg_sweep_config* cfg) {
+  if (!ctx || !cfg) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    sweep_run(ctx, cfg, true);
+  });
+  return NRG_OK;
+}
+
+int nrg_dm_num_shells(const nrg_ctx* ctx) { return ctx ? (int)ctx->dm.size() : 0; }
+
+nrg_status nrg_dm_backprop(nrg_ctx* ctx, const nrg_dm_params* prm, double* rho_trace) {
+  if (!ctx) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    std::memset(&ctx->timing, 0, sizeof(ctx->timing));
+    dm_backprop_impl(ctx, prm, rho_trace);
+  });
+  return NRG_OK;
+}
+
+nrg_status nrg_lehmann(nrg_ctx* ctx, const nrg_dm_params* prm, int nomega, const double* omegas, double* omega_rhow,
+                       int* nout) {
+  if (!ctx) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    std::memset(&ctx->timing, 0, sizeof(ctx->timing));
+    lehmann_impl(ctx, prm, nomega, omegas, omega_rhow, nout);
   });
   return NRG_OK;
 }

@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(256) gather_kernel(UpdateArgs A) {
       for (int idx = threadIdx.x; idx < G.rows * kj; idx += blockDim.x) {
         const int a = idx / kj, c = idx - a * kj;
         double acc = 0.0;
-        const double* Ma = M + (int64_t)a * G.srows;
+        const double* Ma = M + (int64_t)a * G.old_ld;
         for (int bb = 0; bb < G.srows; ++bb)
           acc = fma(Ma[bb], Zt[(int64_t)(G.src_base + bb * G.src_stride) * kj + c], acc);
         double* dst = T + (int64_t)(G.dst_base + a * G.dst_stride) * kj + c;
@@ -107,17 +107,19 @@ __global__ void __launch_bounds__(256) gemm_kernel(UpdateArgs A) {
 }
 
 // Impurity-operator terms (old block x rows of Zt) as 64x64 GEMM tiles:
-// T[dst(a)] += coef * sum_b M[a][b] Zt[src(b)].  Each term owns its
-// destination rows, so tiles of different terms never overlap.
+// T[dst(a)] += sum_terms coef * sum_b M[a][b] Zt[src(b)].  The terms of one
+// group share their destination rows (one row group of one job) and are
+// summed inside the tile, so tiles of different groups never overlap.
 __global__ void __launch_bounds__(256) imp_gemm_kernel(UpdateArgs A) {
   __shared__ double As[TK][TM + 1];
   __shared__ double Bs[TK][TN];
-  const GatherTerm G = A.terms1[A.tile1_term[blockIdx.x]];
+  const int grp = A.tile1_group[blockIdx.x];
+  const int t0 = A.group1_first[grp], nt = A.group1_count[grp];
   const int mn = A.tile1_mn[blockIdx.x];
-  const RotJob J = A.jobs[G.job];
+  const GatherTerm G0 = A.terms1[t0];
+  const RotJob J = A.jobs[G0.job];
   const int m0 = (mn >> 16) * TM, n0 = (mn & 0xffff) * TN;
-  const int M = G.rows, N = J.kj, K = G.srows;
-  const double* Am = A.old_ops[G.op] + G.old_off;  // rows x srows
+  const int M = G0.rows, N = J.kj;
   const double* Zt = A.Zt + J.zt_off;
   double* T = A.T + J.t_off;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -126,41 +128,46 @@ __global__ void __launch_bounds__(256) imp_gemm_kernel(UpdateArgs A) {
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
-  for (int k0 = 0; k0 < K; k0 += TK) {
-    for (int idx = threadIdx.x; idx < TM * TK; idx += 256) {
-      const int r = idx / TK, c = idx - r * TK;
-      const int gr = m0 + r, gc = k0 + c;
-      As[c][r] = (gr < M && gc < K) ? Am[(int64_t)gr * K + gc] : 0.0;
+  for (int t = t0; t < t0 + nt; ++t) {
+    const GatherTerm G = A.terms1[t];
+    const int K = G.srows;
+    const double* Am = A.old_ops[G.op] + G.old_off;  // rows x srows, row stride old_ld
+    for (int k0 = 0; k0 < K; k0 += TK) {
+      for (int idx = threadIdx.x; idx < TM * TK; idx += 256) {
+        const int r = idx / TK, c = idx - r * TK;
+        const int gr = m0 + r, gc = k0 + c;
+        As[c][r] = (gr < M && gc < K) ? G.coef * Am[(int64_t)gr * G.old_ld + gc] : 0.0;
+      }
+      for (int idx = threadIdx.x; idx < TK * TN; idx += 256) {
+        const int r = idx / TN, c = idx - r * TN;
+        const int gr = k0 + r, gc = n0 + c;
+        Bs[r][c] = (gr < K && gc < N) ? Zt[(int64_t)(G.src_base + gr * G.src_stride) * N + gc] : 0.0;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int kk = 0; kk < TK; ++kk) {
+        double a[4], b[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+      }
+      __syncthreads();
     }
-    for (int idx = threadIdx.x; idx < TK * TN; idx += 256) {
-      const int r = idx / TN, c = idx - r * TN;
-      const int gr = k0 + r, gc = n0 + c;
-      Bs[r][c] = (gr < K && gc < N) ? Zt[(int64_t)(G.src_base + gr * G.src_stride) * N + gc] : 0.0;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < TK; ++kk) {
-      double a[4], b[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
-    }
-    __syncthreads();
   }
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int r = m0 + ty + 16 * i;
     if (r >= M) continue;
-    double* Trow = T + (int64_t)(G.dst_base + r * G.dst_stride) * N;
+    double* Trow = T + (int64_t)(G0.dst_base + r * G0.dst_stride) * N;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int c = n0 + tx + 16 * j;
-      if (c < N) Trow[c] = fma(G.coef, acc[i][j], Trow[c]);
+      if (c < N) Trow[c] += acc[i][j];
     }
   }
 }

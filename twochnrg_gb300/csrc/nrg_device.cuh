@@ -174,6 +174,7 @@ struct GatherTerm {       // T[dst rows] += coef * M . Zt[src rows]
   int mode;               // 0: identity (srows == rows); 1: old block (rows x srows)
   double coef;
   int64_t old_off;        // element offset of the old block (mode 1)
+  int old_ld;             // its row stride (columns of the stored old block)
   int op;                 // old operator index (mode 1)
 };
 struct RotJob {           // O (ki x kj) = Z_I (ki x nI) . T (nI x kj)
@@ -198,9 +199,12 @@ struct UpdateArgs {
   const int* tile_job;    // GEMM tiles: job
   const int* tile_mn;     // GEMM tiles: (mtile << 16) | ntile
   int ntiles;
-  // impurity-operator terms (mode 1), one destination per term, as tiles
+  // impurity-operator terms (mode 1) as GEMM tiles; the terms of one group
+  // share their destination rows and are summed inside one tile
   const GatherTerm* terms1;
-  const int* tile1_term;
+  const int* group1_first;
+  const int* group1_count;
+  const int* tile1_group;
   const int* tile1_mn;
   int ntiles1;
 };
@@ -221,5 +225,85 @@ struct OpDiagArgs {       // Boltzmann sums of diagonal elements over kept state
 };
 void launch_opdiag(const OpDiagArgs& a, const int* kstate_block, int nk, double* partial, cudaStream_t s);
 int reduce_partial_count();
+
+// ---------------------------------------------------------------- DM-NRG
+struct GemmJob {          // C (m x n) = op(A) (m x k) . B (k x n), row-major, FP64
+  int m, n, k;
+  int transA;             // 0: A stored m x k; 1: A stored k x m and used transposed
+  const double* A;
+  int lda;
+  const double* B;
+  int ldb;
+  double* C;
+  int ldc;
+};
+// One 64x64 tile of C per CTA: tile t belongs to job tile_job[t] at
+// (tile_mn[t] >> 16, tile_mn[t] & 0xffff).
+void launch_gemm_jobs(const GemmJob* jobs, const int* tile_job, const int* tile_mn, int ntiles, cudaStream_t s);
+
+struct DmTraceTerm {      // rho_N(i,j) += cg * rot[(base + i*stride) * nb + base + j*stride]
+  int64_t rot_off;        // the child block of the rotated rho_{N+1} (dense nb x nb)
+  int nb, base, stride;
+  int count;              // i, j < count (kept states of the parent block in this segment)
+  double cg;
+};
+struct DmTraceArgs {      // DM_NRG_CalcRhoN_withSU2 for all blocks of shell N
+  const int* bsize;
+  const int* soff;        // first state of each block
+  const int64_t* roff;    // each block's dense n x n matrix in rho
+  const int* nkept;       // kept states of each block (a prefix)
+  const int* term_first;
+  const int* term_count;
+  const DmTraceTerm* terms;
+  const double* rot;
+  const double* en;
+  const unsigned char* kept;
+  double beta;            // FDM diagonal of discarded states: exp(-beta E) / zdisc
+  double zdisc;
+  double* rho;
+};
+void launch_dm_trace(const DmTraceArgs& a, int nblocks, cudaStream_t s);
+
+struct DmPair {           // one block pair (b1, b2) of c_d
+  int n1, n2;
+  int s1, s2;             // first states of the blocks
+  int64_t a_off;          // c_d block (n1 x n2) in cd
+  int64_t p_off;          // rho1 . A and A . rho2 (each n1 x n2) in scratch
+  int64_t out_off;        // first Lehmann pair of this block pair
+  double cg;              // sum_Sz CG^2 of the spectral sum
+  int skip;               // both blocks without kept or without discarded states
+};
+struct DmPairArgs {
+  const DmPair* pairs;
+  const double* cd;
+  const double* P1;
+  const double* P2;
+  const double* en;
+  const unsigned char* kept;
+  int last;               // last shell: CalcSpecCosti_T_N weights
+  double beta_last, inv_z_last;
+  double* dE;             // E(b2) - E(b1)
+  double* Wp;             // weight for omega >= 0
+  double* Wn;             // weight for omega < 0
+};
+void launch_dm_pairs(const DmPairArgs& a, int npairs_blocks, cudaStream_t s);
+
+struct LehmannArgs {      // A(omega) = sum_N sum_p W_p BD(omega/D_N, dE_p) / D_N
+  int nomega;
+  const double* omega;
+  const int* win_first;   // first shell of each frequency's window
+  const int* win_count;   // shells in the window (<= window)
+  int window;
+  const int64_t* shell_off;  // Lehmann pairs of shell N: [shell_off[N], shell_off[N+1])
+  const double* dE;
+  const double* Wp;
+  const double* Wn;
+  const double* dn;       // D_N
+  const double* tempdn;   // T / D_N
+  double b, twindow, broadtemp;
+  double* partial;        // [nomega * window], divided by D_N
+  double* out;            // [nomega]
+};
+void launch_lehmann(const LehmannArgs& a, cudaStream_t s);
 
 }  // namespace nrg

@@ -394,6 +394,33 @@ double op_site_factor(const ModelSpec& m, int op, double Si, double Sj, int ti, 
   if (op == OP_FUP_QSZ) return fd_onech(1, tj, ti);   // OneChQ_fN_MatEl (OpMatRules.cpp:1003-1033)
   if (op == OP_FDN_QSZ) return fd_onech(-1, tj, ti);
   if (op == OP_IMPONLY) return ti == tj ? 1.0 : 0.0;
+  if (op == OP_CD_QS) {
+    // OneChQS_cd_MatEl (OpMatRules.cpp:1249-1330): the impurity d operator
+    // recoupled with a site state it leaves unchanged.  A site state that is
+    // not found matches another one that is not found, as in the reference.
+    double qi[3] = {ss.q(ti, 0), ss.q(ti, 1), ss.q(ti, 2)}, qj[3] = {ss.q(tj, 0), ss.q(tj, 1), ss.q(tj, 2)};
+    const double Sti = qi[1], Stj = qj[1];
+    const double Scfi = Si - qi[2], Scfj = Sj - qj[2];
+    const double fermi = deq(qj[0], 0.0) ? -1.0 : 1.0;
+    double sigma = Sj - Si;
+    double norm = cg(Si, Si, 0.5, sigma, Sj, Sj);
+    if (deq(norm, 0.0)) {
+      sigma = Si - Sj;
+      norm = cg(Si, Si, 0.5, sigma, Sj, Sj);
+      if (deq(norm, 0.0)) return 0.0;
+    }
+    double f = 0.0;
+    for (double Szcfj = -Scfj; Szcfj <= Scfj; Szcfj += 1.0) {
+      const double Szcfi = Szcfj - sigma;
+      qj[2] = Sj - Szcfj; const int sj = ss.find(qj);
+      qi[2] = Si - Szcfi; const int si = ss.find(qi);
+      const double a0 = cg(Scfi, Szcfi, Sti, qi[2], Si, Si);
+      const double a1 = cg(Scfj, Szcfj, Stj, qj[2], Sj, Sj);
+      const double a2 = cg(Scfi, Szcfi, 0.5, sigma, Scfj, Szcfj);
+      if (si == sj) f += a0 * a1 * a2 * fermi;
+    }
+    return f / norm;
+  }
   if (op == OP_F_QS) {
     // OneChQS_fN_MatEl (OpMatRules.cpp:1167-1244).
     double qi[3] = {ss.q(ti, 0), ss.q(ti, 1), ss.q(ti, 2)}, qj[3] = {ss.q(tj, 0), ss.q(tj, 1), ss.q(tj, 2)};

@@ -25,6 +25,7 @@ enum OpKind {
   OP_F1_2CH = 4,    // TwoChQS_fNch1_MatEl   (TwoChQS_OpMatRules.cpp:1355)
   OP_F2_2CH = 5,    // TwoChQS_fNch2_MatEl   (TwoChQS_OpMatRules.cpp:1362)
   OP_IMPONLY = 6,   // ImpOnly_MatEl x old   (OpMatRules.cpp:265)
+  OP_CD_QS = 7,     // OneChQS_cd_MatEl x old (OpMatRules.cpp:1249)
 };
 // CheckForMatEl rule ids.
 enum CheckKind { CHK_DIAG = 1, CHK_QS_CD = 2, CHK_Q_CD = 3, CHK_2CH_CD = 4 };
@@ -113,8 +114,10 @@ struct HNTables {
 };
 void build_hn_tables(const ModelSpec& m, const Basis& b, HNTables& t);
 
-// Site factor of an operator between two new-basis states that came from the
-// same old state (f-type operators), g(S_i, S_j, t_i, t_j).
+// Site factor of an operator between two new-basis states, g(S_i, S_j, t_i,
+// t_j): for f-type operators the states came from the same old state; for
+// impurity operators (OP_IMPONLY, OP_CD_QS) g multiplies the old operator
+// element between the states they came from.
 double op_site_factor(const ModelSpec& m, int op, double Si, double Sj, int ti, int tj);
 bool op_check(int chk, const BlockArray& kept, int i, int j);
 
