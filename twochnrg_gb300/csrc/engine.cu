@@ -128,6 +128,12 @@ struct nrg_ctx {
   nrg::DevBuf meta, vmeta, H, d, e, tau, ev, en, flag, scal, Y, scratch, Z, Zt, T, partial, red, gpart;
   nrg::DevBuf ops_a[6], ops_b[6], opptr;
   cudaEvent_t ev_a[8];
+  // concurrent whole-GPU tridiagonalizations: side streams, fork/join events,
+  // per-stream scratch and the block lists
+  static constexpr int kMaxSplit = 4;
+  cudaStream_t aux[kMaxSplit] = {};
+  cudaEvent_t fork = nullptr, join[kMaxSplit] = {};
+  nrg::DevBuf gpart_k[kMaxSplit], gbig;
   // drop-in outputs (host, valid until the next call on the context)
   std::vector<double> out_en, out_qn, out_cut_en, out_vec, out_el;
   std::vector<unsigned char> out_kept, out_cut_kept;
@@ -238,11 +244,23 @@ void plan_blocks(EigPlan& P, const std::vector<int>& bsize) {
 
 int choose_cluster(int maxn) { return maxn >= 256 ? 16 : 8; }
 
-// Blocks at least this large are tridiagonalized by the whole GPU (one
-// after the other); smaller ones by one thread-block cluster each.
+// Blocks at least this large are tridiagonalized by a cooperative grid of
+// many SMs (one block after the other per grid); smaller ones by one
+// thread-block cluster each.
 int big_block_threshold() {
   const char* s = std::getenv("NRG_BIG_N");
   return s ? std::atoi(s) : 1200;
+}
+
+// The large blocks are dealt (by n^3, largest first) to this many concurrent
+// cooperative grids, each with an equal share of the SMs: a Householder step
+// is latency-bound (two grid barriers and a reduce-scatter), so independent
+// blocks on fewer SMs each overlap those latencies.
+int grid_split(int nbig) {
+  const char* s = std::getenv("NRG_GRID_SPLIT");
+  int k = s ? std::atoi(s) : 2;
+  k = std::max(1, std::min(k, nrg_ctx::kMaxSplit));
+  return std::min(k, nbig);
 }
 
 // `order`: all blocks, largest first (host copy `order_h`); the big blocks
@@ -259,8 +277,24 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
   ta.nblocks = nb; ta.order = d_order; ta.bsize = d_bsize; ta.hoff = d_hoff; ta.soff = d_soff;
   ta.H = c->H.as<double>(); ta.d = c->d.as<double>(); ta.e = c->e.as<double>(); ta.tau = c->tau.as<double>();
   ta.queue = c->red.as<int>(); ta.flag = c->flag.as<int>(); ta.maxn = std::max(P.maxn, 2);
+  const int K = nbig > 0 ? grid_split(nbig) : 0;
+  std::vector<std::vector<int>> bins(std::max(K, 1));
+  size_t o_bins[nrg_ctx::kMaxSplit] = {};
+  if (K > 1) {  // deal the large blocks by n^3 and upload the lists before the fork
+    std::vector<double> load(K, 0.0);
+    for (int q = 0; q < nbig; ++q) {
+      const int b = order_h[q];
+      const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      bins[k].push_back(b);
+      load[k] += (double)P.bsize[b] * P.bsize[b] * P.bsize[b];
+    }
+    Packer pk;
+    for (int k = 0; k < K; ++k) o_bins[k] = pk.add(bins[k]);
+    c->gbig.ensure(pk.host.size() + 256);
+    h2d(c, c->gbig.p, pk.host.data(), pk.host.size());
+  }
   cudaEvent_t t0 = tm.start();
-  if (nbig > 0) {
+  if (K == 1) {
     const int G = tridiag_grid_size(ta.maxn);
     if (G <= 0) throw NrgError(NRG_ERR_SIZE, "whole-GPU tridiagonalization does not fit");
     c->gpart.ensure(sizeof(double) * ((size_t)G * ta.maxn + ta.maxn + G + 64));
@@ -269,6 +303,25 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
     double* dots = pvec + ta.maxn;
     CU(launch_tridiag_grid(ta, d_order, nbig, part, pvec, dots, G, c->stream));
     c->launches++; c->timing.tridiag_launches++;
+  } else if (K > 1) {
+    const int G = tridiag_grid_size(ta.maxn);
+    if (G <= 0) throw NrgError(NRG_ERR_SIZE, "whole-GPU tridiagonalization does not fit");
+    const int Gk = G / K;
+    if (!c->fork) CU(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
+    CU(cudaEventRecord(c->fork, c->stream));
+    for (int k = 0; k < K; ++k) {
+      if (!c->aux[k]) CU(cudaStreamCreateWithFlags(&c->aux[k], cudaStreamNonBlocking));
+      if (!c->join[k]) CU(cudaEventCreateWithFlags(&c->join[k], cudaEventDisableTiming));
+      c->gpart_k[k].ensure(sizeof(double) * ((size_t)Gk * ta.maxn + ta.maxn + Gk + 64));
+      double* part = c->gpart_k[k].as<double>();
+      double* pvec = part + (size_t)Gk * ta.maxn;
+      double* dots = pvec + ta.maxn;
+      CU(cudaStreamWaitEvent(c->aux[k], c->fork, 0));
+      CU(launch_tridiag_grid(ta, (const int*)(c->gbig.as<char>() + o_bins[k]), (int)bins[k].size(), part, pvec,
+                             dots, Gk, c->aux[k]));
+      CU(cudaEventRecord(c->join[k], c->aux[k]));
+      c->launches++; c->timing.tridiag_launches++;
+    }
   }
   if (nbig < nb) {
     int maxs = P.bsize[order_h[nbig]];
@@ -284,13 +337,14 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
     CU(launch_tridiag(ts, cluster, ncl, c->stream));
     c->launches++; c->timing.tridiag_launches++;
   }
+  for (int k = 0; K > 1 && k < K; ++k) CU(cudaStreamWaitEvent(c->stream, c->join[k], 0));
   tm.stop(t0, &c->timing.tridiag_ms);
   double fl = 0.0;
   for (int n : P.bsize) fl += 4.0 / 3.0 * (double)n * n * n;
   c->timing.tridiag_flops += fl;
   TdEigArgs ea{};
   ea.nblocks = nb; ea.bsize = d_bsize; ea.soff = d_soff; ea.d = c->d.as<double>(); ea.e = c->e.as<double>();
-  ea.ev = c->ev.as<double>(); ea.nstates = P.nstates; ea.flag = c->flag.as<int>();
+  ea.ev = c->ev.as<double>(); ea.nstates = P.nstates; ea.flag = c->flag.as<int>(); ea.maxn = std::max(P.maxn, 1);
   cudaEvent_t t1 = tm.start();
   launch_bisect(ea, d_state_block, c->stream);
   c->launches += 2;
@@ -1657,6 +1711,11 @@ void nrg_destroy(nrg_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  for (int k = 0; k < nrg_ctx::kMaxSplit; ++k) {
+    if (ctx->aux[k]) { cudaStreamSynchronize(ctx->aux[k]); cudaStreamDestroy(ctx->aux[k]); }
+    if (ctx->join[k]) cudaEventDestroy(ctx->join[k]);
+  }
+  if (ctx->fork) cudaEventDestroy(ctx->fork);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
 }

@@ -71,21 +71,44 @@ __device__ __forceinline__ int sturm_newton(const double* d, const double* e, in
   return cnt;
 }
 
-// The k-th eigenvalue (ascending) of each tridiagonal block: FP32 bisection
-// to about 1e-6 of the spectral radius, the bracket checked in FP64, then
-// safeguarded Newton steps in FP64 (a bisection step whenever Newton leaves
-// the bracket or stalls) until the bracket is a few ulps wide.  Every FP64
-// pass also updates the bracket with its Sturm count, so the result is the
-// k-th eigenvalue whatever the clustering.
+// e_i is negligible next to its diagonal neighbours (the splitting test of
+// LAPACK's tridiagonal solvers): the block then falls apart into unreduced
+// pieces whose eigenvalues are simple.
+__device__ __forceinline__ bool split_at(const double* d, const double* e, int i) {
+  return fabs(e[i]) <= kEps * sqrt(fabs(d[i])) * sqrt(fabs(d[i + 1])) || e[i] == 0.0;
+}
+
+// One thread per diagonal position k of each tridiagonal block: the piece
+// (unreduced sub-block) containing position k is found, and thread k
+// computes that piece's (k - start)-th eigenvalue.  Over all threads this is
+// every eigenvalue of the block exactly once; sort_levels orders them.  On a
+// piece the levels are simple, so after an FP32 Sturm bisection to about
+// 1e-6 of the piece's spectral radius, safeguarded FP64 Newton steps on the
+// pivot recurrence converge quadratically (a bisection step whenever Newton
+// leaves the bracket or stalls); every FP64 pass also tightens the bracket
+// with its Sturm count.  Dropping the negligible e_i moves the levels by at
+// most one ulp of the neighbouring diagonal.
 __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= A.nstates) return;
   const int b = state_block[g];
-  const int n = A.bsize[b];
+  const int nb = A.bsize[b];
   const int so = A.soff[b];
-  const int k = g - so;
-  const double* d = A.d + so;
-  const double* e = A.e + so;
+  const int pos = g - so;
+  const double* db = A.d + so;
+  const double* eb = A.e + so;
+  int s0 = pos, s1 = pos;
+  while (s0 > 0 && !split_at(db, eb, s0 - 1)) --s0;
+  while (s1 < nb - 1 && !split_at(db, eb, s1)) ++s1;
+  const int n = s1 - s0 + 1;
+  const int k = pos - s0;
+  const double* d = db + s0;
+  const double* e = eb + s0;
+  if (n == 1) {
+    if (!isfinite(d[0])) atomicOr(A.flag, DEV_BAD_INPUT);
+    A.ev[g] = d[0];
+    return;
+  }
   double gl = DBL_MAX, gu = -DBL_MAX, emax2 = 0.0;
   for (int i = 0; i < n; ++i) {
     const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
@@ -108,9 +131,8 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
     }
     const double margin = 1e-5 * tnorm;
     const double tlo = (double)flo - margin, thi = (double)fhi + margin;
-    double st;
-    if (tlo > lo && sturm_newton(d, e, n, tlo, pivmin, &st) <= k) lo = tlo;
-    if (thi < hi && sturm_newton(d, e, n, thi, pivmin, &st) > k) hi = thi;
+    if (tlo > lo && sturm_count(d, e, n, tlo, pivmin) <= k) lo = tlo;
+    if (thi < hi && sturm_count(d, e, n, thi, pivmin) > k) hi = thi;
   }
   // Stop at a few ulps of the spectral radius: below that the Sturm counts
   // are at the round-off of the recurrence.
@@ -131,8 +153,7 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
       if (fabs(step) <= small) {
         // converged: accept only if the k-th level is within reach of x
         const double del = 2.0 * fabs(step) + small;
-        double t;
-        if (sturm_newton(d, e, n, x - del, pivmin, &t) <= k && sturm_newton(d, e, n, x + del, pivmin, &t) > k) {
+        if (sturm_count(d, e, n, x - del, pivmin) <= k && sturm_count(d, e, n, x + del, pivmin) > k) {
           v = x + step;
           done = true;
           break;
@@ -151,10 +172,37 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
   A.ev[g] = v;
 }
 
-// Each level is found on its own, so two (nearly) equal levels can come out
-// an ulp out of order.  CutStates reads a block's levels as ascending
-// (its first level above E_cut ends the block), so every block is put in
-// order with odd-even transposition passes: one CTA per block, stopping after
+// Levels come out piece by piece (and two close levels of one piece can come
+// out an ulp out of order); CutStates reads a block's levels as ascending
+// (its first level above E_cut ends the block).  Each block is sorted in
+// shared memory with a bitonic network, one CTA per block, padded with +inf
+// to a power of two.
+__global__ void sort_levels_kernel(TdEigArgs A, int pmax) {
+  extern __shared__ double sv[];
+  const int b = blockIdx.x;
+  const int n = A.bsize[b];
+  double* v = A.ev + A.soff[b];
+  int P = 1;
+  while (P < n) P <<= 1;
+  if (P > pmax) return;  // launched only when every block fits
+  for (int i = threadIdx.x; i < P; i += blockDim.x) sv[i] = i < n ? v[i] : DBL_MAX;
+  for (int size = 2; size <= P; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      __syncthreads();
+      for (int i = threadIdx.x; i < (P >> 1); i += blockDim.x) {
+        const int lo = 2 * i - (i & (stride - 1));
+        const int hi = lo + stride;
+        const bool asc = (lo & size) == 0;
+        const double x = sv[lo], y = sv[hi];
+        if ((x > y) == asc) { sv[lo] = y; sv[hi] = x; }
+      }
+    }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) v[i] = sv[i];
+}
+
+// Fallback for blocks too large for the shared-memory sort: odd-even
+// transposition passes in global memory, one CTA per block, stopping after
 // two passes without a swap; n + 1 passes always suffice.
 __global__ void order_levels_kernel(TdEigArgs A) {
   const int b = blockIdx.x;
@@ -363,7 +411,16 @@ __global__ void __launch_bounds__(kBackWarps * 32) backtransform_kernel(BackArgs
 void launch_bisect(const TdEigArgs& a, const int* state_block, cudaStream_t s) {
   if (a.nstates <= 0) return;
   bisect_kernel<<<(a.nstates + 127) / 128, 128, 0, s>>>(a, state_block);
-  order_levels_kernel<<<a.nblocks, 256, 0, s>>>(a);
+  int P = 1;
+  while (P < a.maxn) P <<= 1;
+  const size_t smem = sizeof(double) * (size_t)P;
+  if (smem <= (size_t)max_dyn_smem() &&
+      cudaFuncSetAttribute(sort_levels_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()) ==
+          cudaSuccess) {
+    sort_levels_kernel<<<a.nblocks, 512, smem, s>>>(a, P);
+  } else {
+    order_levels_kernel<<<a.nblocks, 256, 0, s>>>(a);
+  }
 }
 
 void launch_inviter(const InvIterArgs& a, const int* vec_block, const int* vec_index, int nvecs, cudaStream_t s) {

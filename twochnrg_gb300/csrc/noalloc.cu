@@ -122,7 +122,7 @@ extern "C" nrg_status nrg_diag_block_noalloc(int n, const double* a, double* eig
   if (launch_tridiag(ta, 8, 1, s) != cudaSuccess) return NRG_ERR_CUDA;
   TdEigArgs ea{};
   ea.nblocks = 1; ea.bsize = L.bsize; ea.soff = L.soff; ea.d = L.d; ea.e = L.e; ea.ev = L.ev; ea.nstates = n;
-  ea.flag = L.flag;
+  ea.flag = L.flag; ea.maxn = n;
   launch_bisect(ea, L.state_block, s);
   cluster_kernel<<<1, 32, 0, s>>>(L, n);
   InvIterArgs ia{};

@@ -93,6 +93,7 @@ struct TdEigArgs {
   double* ev;            // [nstates] ascending per block
   int nstates;
   int* flag;
+  int maxn;              // largest block (sizes the sort's shared memory)
 };
 void launch_bisect(const TdEigArgs& a, const int* state_block, cudaStream_t s);
 
