@@ -99,7 +99,7 @@ typedef struct {
   double total_ms;        /* host wall time of nrg_sweep_run                   */
   double assemble_ms;     /* H_N assembly kernels                               */
   double tridiag_ms;      /* Householder tridiagonalization                     */
-  double tridiag_eig_ms;  /* bisection + inverse iteration on the tridiagonals  */
+  double tridiag_eig_ms;  /* eigenvalues of the tridiagonals (bisection, sort)  */
   double backtransform_ms;/* eigenvector back-transformation                    */
   double cut_ms;          /* SetE0zero/SetDegen/Ecut/CutStates + observables    */
   double update_ms;       /* operator rotation (UpdateMatrices)                 */
@@ -116,6 +116,7 @@ typedef struct {
   double lehmann_ms;      /* nrg_lehmann: the Lehmann-sum kernels alone         */
   int64_t lehmann_pairs;  /* (E_j - E_i, weight) pairs over all shells          */
   int64_t lehmann_evals;  /* pair x frequency evaluations of the broadened delta */
+  double vectors_ms;      /* inverse iteration + reorthogonalization            */
 } nrg_timing;
 
 /* ---- context ---------------------------------------------------------- */

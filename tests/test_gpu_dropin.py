@@ -46,14 +46,33 @@ def test_random_blocks(engine):
         _check_block(A, w, Z, wr, Zr)
 
 
-def test_large_block_whole_gpu_path(engine):
+def test_large_block_whole_gpu_path(engine, monkeypatch):
     rng = np.random.default_rng(11)
-    n = 1300  # above the whole-GPU threshold
+    n = 1300
+    monkeypatch.setenv("NRG_BIG_N", "1000")  # route the block to the cooperative-grid kernel
     X = rng.standard_normal((n, n))
     A = (X + X.T) / np.sqrt(n)
     ws, Zs = engine.diag_blocks([n], orc.pack_upper(A))
     wr, Zr = orc.diag_block(orc.pack_upper(A), n)
     _check_block(A, ws[0], Zs[0], wr, Zr)
+
+
+@pytest.mark.parametrize("split", ["1", "2", "3"])
+def test_concurrent_grids_path(engine, monkeypatch, split):
+    """Several large blocks dealt to concurrent cooperative grids, next to
+    small blocks on the cluster kernel."""
+    rng = np.random.default_rng(12)
+    monkeypatch.setenv("NRG_BIG_N", "1000")
+    monkeypatch.setenv("NRG_GRID_SPLIT", split)
+    sizes = [1100, 300, 1250, 1020, 64]
+    mats = []
+    for n in sizes:
+        X = rng.standard_normal((n, n))
+        mats.append((X + X.T) / np.sqrt(n))
+    ws, Zs = engine.diag_blocks(sizes, np.concatenate([orc.pack_upper(A) for A in mats]))
+    for A, w, Z in zip(mats, ws, Zs):
+        wr, Zr = orc.diag_block(orc.pack_upper(A), A.shape[0])
+        _check_block(A, w, Z, wr, Zr)
 
 
 def test_nrg_blocks_from_a_real_iteration(engine):

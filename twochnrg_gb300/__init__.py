@@ -61,7 +61,7 @@ class Timing(ctypes.Structure):
                 ("device_ms", ctypes.c_double), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64),
                 ("dm_backprop_ms", ctypes.c_double), ("dm_spectral_ms", ctypes.c_double),
                 ("lehmann_ms", ctypes.c_double), ("lehmann_pairs", ctypes.c_int64),
-                ("lehmann_evals", ctypes.c_int64)]
+                ("lehmann_evals", ctypes.c_int64), ("vectors_ms", ctypes.c_double)]
 
 
     def as_dict(self) -> dict:

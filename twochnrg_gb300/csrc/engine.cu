@@ -249,7 +249,7 @@ int choose_cluster(int maxn) { return maxn >= 256 ? 16 : 8; }
 // thread-block cluster each.
 int big_block_threshold() {
   const char* s = std::getenv("NRG_BIG_N");
-  return s ? std::atoi(s) : 1200;
+  return s ? std::atoi(s) : 2400;
 }
 
 // The large blocks are dealt (by n^3, largest first) to this many concurrent
@@ -399,7 +399,7 @@ void run_vectors(nrg_ctx* c, Timer& tm, EigPlan& P, const std::vector<double>& e
   cudaEvent_t t0 = tm.start();
   launch_inviter(ia, (const int*)(base + o_vb), (const int*)(base + o_vi), (int)vb.size(), c->stream);
   c->launches += 2;
-  tm.stop(t0, &c->timing.tridiag_eig_ms);
+  tm.stop(t0, &c->timing.vectors_ms);
   BackArgs ba{};
   ba.bsize = d_bsize; ba.hoff = d_hoff; ba.H_const = c->H.as<double>(); ba.soff = d_soff; ba.tau = c->tau.as<double>();
   ba.nvec = ia.nvec; ba.yoff = ia.yoff; ba.Y = c->Y.as<double>(); ba.Z = c->Z.as<double>(); ba.Zt = c->Zt.as<double>();

@@ -48,34 +48,68 @@ __device__ __forceinline__ int sturm_count_f32(const double* d, const double* e,
   return cnt;
 }
 
-// One FP64 pass: Sturm count of T - x and the Newton step -f/f' of
-// f(x) = det(T - x) from the pivot recurrence q_i and its derivative.
-__device__ __forceinline__ int sturm_newton(const double* d, const double* e, int n, double x, double pivmin,
-                                            double* step) {
+// One FP64 pass: Sturm count of T - x and, from the pivot recurrence q_i
+// and its first two derivatives, S1 = sum q_i'/q_i = f'/f and
+// S2 = sum (q_i''/q_i - (q_i'/q_i)^2) = (log f)'' of f(x) = det(T - x).
+__device__ __forceinline__ int sturm_sums(const double* d, const double* e, int n, double x, double pivmin,
+                                          double* S1, double* S2) {
   int cnt = 0;
-  double q = d[0] - x, dq = -1.0;
+  double q = d[0] - x, dq = -1.0, ddq = 0.0;
   if (fabs(q) < pivmin) q = -pivmin;
   if (q < 0.0) cnt++;
   double r = 1.0 / q;
-  double s = dq * r;  // sum of q_i'/q_i = f'/f
+  double u = dq * r;
+  double s1 = u, s2 = -u * u;
   for (int i = 1; i < n; ++i) {
-    const double e2r = e[i - 1] * e[i - 1] * r;
-    const double qn = (d[i] - x) - e2r;
-    dq = fma(e2r * r, dq, -1.0);
+    const double e2 = e[i - 1] * e[i - 1];
+    const double qn = (d[i] - x) - e2 * r;
+    const double e2rr = e2 * r * r;
+    const double ddqn = e2rr * fma(-2.0 * dq * dq, r, ddq);
+    dq = fma(e2rr, dq, -1.0);
+    ddq = ddqn;
     q = fabs(qn) < pivmin ? -pivmin : qn;
     if (q < 0.0) cnt++;
     r = 1.0 / q;
-    s = fma(dq, r, s);
+    u = dq * r;
+    s1 += u;
+    s2 = fma(ddq, r, fma(-u, u, s2));
   }
-  *step = -1.0 / s;
+  *S1 = s1;
+  *S2 = s2;
   return cnt;
+}
+
+// Step towards the wanted level from a local two-level model
+// f ~ C (x-a)(x-b): 1/(x-a) + 1/(x-b) = S1 and 1/(x-a)^2 + 1/(x-b)^2 = -S2
+// (Laguerre's step for degree 2).  `above` tells on which side of x the
+// level lies and `rank` how many levels of that side come first (both from
+// the Sturm count at x).  A level with a close partner (the channel doublets
+// of the two-channel model) is then reached in a few steps, where Newton on f
+// converges only linearly; without a real two-level fit the Newton step on
+// f/f' (S1/S2) is taken.
+__device__ __forceinline__ double pair_step(double S1, double S2, bool above, int rank) {
+  const double disc = -2.0 * S2 - S1 * S1;
+  if (disc >= 0.0) {
+    const double sq = sqrt(disc);
+    const double t1 = 0.5 * (S1 + sq), t2 = 0.5 * (S1 - sq);
+    const double d1 = t1 != 0.0 ? -1.0 / t1 : 0.0, d2 = t2 != 0.0 ? -1.0 / t2 : 0.0;
+    const bool ok1 = t1 != 0.0 && ((d1 > 0.0) == above), ok2 = t2 != 0.0 && ((d2 > 0.0) == above);
+    if (ok1 && ok2) {
+      const double nearer = fabs(d1) <= fabs(d2) ? d1 : d2, farther = fabs(d1) <= fabs(d2) ? d2 : d1;
+      return rank == 0 ? nearer : farther;
+    }
+    if (ok1) return d1;
+    if (ok2) return d2;
+  }
+  return S1 / S2;
 }
 
 // e_i is negligible next to its diagonal neighbours (the splitting test of
 // LAPACK's tridiagonal solvers): the block then falls apart into unreduced
 // pieces whose eigenvalues are simple.
 __device__ __forceinline__ bool split_at(const double* d, const double* e, int i) {
-  return fabs(e[i]) <= kEps * sqrt(fabs(d[i])) * sqrt(fabs(d[i + 1])) || e[i] == 0.0;
+  const double ei = e[i];
+  return ei * ei <= (kEps * kEps) * fabs(d[i] * d[i + 1]) || ei == 0.0;
 }
 
 // One thread per diagonal position k of each tridiagonal block: the piece
@@ -83,10 +117,11 @@ __device__ __forceinline__ bool split_at(const double* d, const double* e, int i
 // computes that piece's (k - start)-th eigenvalue.  Over all threads this is
 // every eigenvalue of the block exactly once; sort_levels orders them.  On a
 // piece the levels are simple, so after an FP32 Sturm bisection to about
-// 1e-6 of the piece's spectral radius, safeguarded FP64 Newton steps on the
-// pivot recurrence converge quadratically (a bisection step whenever Newton
-// leaves the bracket or stalls); every FP64 pass also tightens the bracket
-// with its Sturm count.  Dropping the negligible e_i moves the levels by at
+// 1e-6 of the piece's spectral radius, safeguarded FP64 steps from a local
+// two-level model (pair_step) converge in a few passes also next to a
+// near-degenerate partner (a bisection step whenever the model step leaves
+// the bracket); every FP64 pass also tightens the bracket with its Sturm
+// count.  Dropping the negligible e_i moves the levels by at
 // most one ulp of the neighbouring diagonal.
 __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -109,18 +144,23 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
     A.ev[g] = d[0];
     return;
   }
-  double gl = DBL_MAX, gu = -DBL_MAX, emax2 = 0.0;
+  // Gershgorin bounds in FP32, widened past their rounding: they only seed
+  // the bracket.
+  float fgl = FLT_MAX, fgu = -FLT_MAX, femax = 0.0f;
   for (int i = 0; i < n; ++i) {
-    const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
-    gl = fmin(gl, d[i] - r);
-    gu = fmax(gu, d[i] + r);
-    if (i + 1 < n) emax2 = fmax(emax2, e[i] * e[i]);
+    const float fe0 = i > 0 ? fabsf((float)e[i - 1]) : 0.0f, fe1 = i + 1 < n ? fabsf((float)e[i]) : 0.0f;
+    const float fd = (float)d[i];
+    fgl = fminf(fgl, fd - (fe0 + fe1));
+    fgu = fmaxf(fgu, fd + (fe0 + fe1));
+    femax = fmaxf(femax, fe1);
   }
-  const double tnorm = fmax(fabs(gl), fabs(gu));
+  const double tnorm = fmax(fabs((double)fgl), fabs((double)fgu));
+  const double emax2 = (double)femax * (double)femax;
   const double pivmin = DBL_MIN * fmax(1.0, emax2);
-  double lo = gl - 2.0 * kEps * tnorm * n - 2.0 * pivmin;
-  double hi = gu + 2.0 * kEps * tnorm * n + 2.0 * pivmin;
+  double lo = (double)fgl - 1e-6 * tnorm - 2.0 * kEps * tnorm * n - 2.0 * pivmin;
+  double hi = (double)fgu + 1e-6 * tnorm + 2.0 * kEps * tnorm * n + 2.0 * pivmin;
   const double atol = 1e-3 * kEps * fmax(tnorm, DBL_MIN);
+  int clo = -1, chi = -1;  // Sturm counts at lo / hi once checked in FP64
   // FP32 bracket
   if (tnorm > 1e-30 && tnorm < 1e30) {
     float flo = (float)lo, fhi = (float)hi;
@@ -131,9 +171,18 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
     }
     const double margin = 1e-5 * tnorm;
     const double tlo = (double)flo - margin, thi = (double)fhi + margin;
-    if (tlo > lo && sturm_count(d, e, n, tlo, pivmin) <= k) lo = tlo;
-    if (thi < hi && sturm_count(d, e, n, thi, pivmin) > k) hi = thi;
+    if (tlo > lo) {
+      const int c = sturm_count(d, e, n, tlo, pivmin);
+      if (c <= k) { lo = tlo; clo = c; }
+    }
+    if (thi < hi) {
+      const int c = sturm_count(d, e, n, thi, pivmin);
+      if (c > k) { hi = thi; chi = c; }
+    }
   }
+  // The bracket holds the k-th level alone: Newton kept inside it can only
+  // converge to that level.
+  const bool unique = clo == k && chi == k + 1;
   // Stop at a few ulps of the spectral radius: below that the Sturm counts
   // are at the round-off of the recurrence.
   const double floor_w = fmax(8.0 * kEps * tnorm, atol);
@@ -142,25 +191,32 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
   bool newton = true, done = false;
   for (int it = 0; it < 200 && !done; ++it) {
     if (hi - lo <= fmax(2.0 * kEps * fmax(fabs(lo), fabs(hi)), floor_w)) break;
-    if (it >= 12) newton = false;  // Newton that has not converged by now: bisect
-    double step;
-    const int c = sturm_newton(d, e, n, x, pivmin, &step);
+    if (it >= 16) newton = false;  // a model step that has not converged by now: bisect
+    double S1, S2;
+    const int c = sturm_sums(d, e, n, x, pivmin, &S1, &S2);
     if (c > k) hi = x; else lo = x;
+    const bool above = c <= k;
+    const double step = pair_step(S1, S2, above, above ? k - c : c - 1 - k);
     double xn = 0.5 * (lo + hi);
     if (newton && isfinite(step)) {
       // round-off floor of the recurrence: a few ulps of the spectral radius
       const double small = 4.0 * kEps * fabs(x) + 16.0 * kEps * tnorm;
       if (fabs(step) <= small) {
-        // converged: accept only if the k-th level is within reach of x
-        const double del = 2.0 * fabs(step) + small;
-        if (sturm_count(d, e, n, x - del, pivmin) <= k && sturm_count(d, e, n, x + del, pivmin) > k) {
-          v = x + step;
+        // converged: accept only if the k-th level is within reach of x + step;
+        // the count at x already settles the side x is on
+        const double xc = x + step, del = 2.0 * fabs(step) + small;
+        bool ok;
+        if (unique && xc >= lo && xc <= hi) ok = true;
+        else if (above && step >= 0.0) ok = sturm_count(d, e, n, xc + del, pivmin) > k;
+        else if (!above && step <= 0.0) ok = sturm_count(d, e, n, xc - del, pivmin) <= k;
+        else ok = sturm_count(d, e, n, xc - del, pivmin) <= k && sturm_count(d, e, n, xc + del, pivmin) > k;
+        if (ok) {
+          v = xc;
           done = true;
           break;
-        } else {
-          newton = false;
         }
-      } else if (x + step > lo && x + step < hi && fabs(step) < 0.5 * (hi - lo)) {
+        newton = false;
+      } else if (x + step > lo && x + step < hi) {
         xn = x + step;
       }
     }
@@ -410,7 +466,9 @@ __global__ void __launch_bounds__(kBackWarps * 32) backtransform_kernel(BackArgs
 
 void launch_bisect(const TdEigArgs& a, const int* state_block, cudaStream_t s) {
   if (a.nstates <= 0) return;
-  bisect_kernel<<<(a.nstates + 127) / 128, 128, 0, s>>>(a, state_block);
+  // One warp per CTA: the long-running threads of the largest blocks then
+  // spread over all SMs instead of crowding a few.
+  bisect_kernel<<<(a.nstates + 31) / 32, 32, 0, s>>>(a, state_block);
   int P = 1;
   while (P < a.maxn) P <<= 1;
   const size_t smem = sizeof(double) * (size_t)P;

@@ -31,17 +31,19 @@ namespace {
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 
-// Deterministic block-wide sum (same tree in every CTA of the cluster).
+// Deterministic block-wide sum (same tree in every CTA of the cluster): a
+// shuffle tree per warp, then one over the warp sums (FP64 latency is long,
+// so no serial chains).
 __device__ double block_sum(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   __syncthreads();
   if (lane == 0) red[warp] = v;
   __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x == 0) {
-    for (int w = 0; w < kWarps; ++w) s += red[w];
-    red[kWarps] = s;
+  if (warp == 0) {
+    double t = lane < kWarps ? red[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (lane == 0) red[kWarps] = t;
   }
   __syncthreads();
   return red[kWarps];
@@ -85,16 +87,15 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
     bool have_old = false;
     for (int j = 0; j + 2 < n; ++j) {
       // Phase 1: row j of A^(j) (pending rank-2 update applied) -> x.
+      double s = 0.0;
       for (int c = j + tid; c < n; c += kThreads) {
         double a = __ldcg(H + (int64_t)j * n + c);
         if (have_old) a = fma(-vold[j], W[c], fma(-W[j], vold[c], a));
         vnew[c] = a;
+        if (c >= j + 2) s = fma(a, a, s);
       }
       if (have_old && rank == 0)
         for (int c = j + tid; c < n; c += kThreads) H[(int64_t)(j - 1) * n + c] = vold[c];
-      __syncthreads();
-      double s = 0.0;
-      for (int c = j + 2 + tid; c < n; c += kThreads) s = fma(vnew[c], vnew[c], s);
       s = block_sum(s, red);
       const double dj = vnew[j], alpha = vnew[j + 1];
       double tau, beta, scal;
