@@ -177,6 +177,34 @@ def cpu_batch_sample(cores: int):
     return len(inst) / dt, dt, len(inst)
 
 
+DM_WORKLOAD = dict(nsites=40, ncutoff=500, lam=2.5, U=0.5, ed=-0.25, gamma=0.02)
+DM_TEMP, DM_BROAD, DM_NOMEGA = 1e-8, 0.6, 2000
+DM_NAME = ("DM-NRG (FDM) spectral function of c_d, one-channel Anderson (Q,S): Lambda=2.5, U=0.5, ed=-0.25, "
+           "Gamma=0.02, 40 iterations, 500 kept; T=1e-8, log-Gaussian b=0.6, 2000 frequencies "
+           "+-logspace(-10, 0, 1000)")
+DM_SAMPLE = dict(nsites=16, ncutoff=150, lam=2.5, U=0.5, ed=-0.25, gamma=0.02)
+DM_SAMPLE_NOMEGA = 200
+
+
+def dm_omegas(n):
+    import numpy as np
+    h = n // 2
+    return np.concatenate([-np.logspace(0, -10, h), np.logspace(-10, 0, h)])
+
+
+def gpu_dm(eng, W, nomega):
+    """Forward sweep keeping the DM-NRG shells, backward sweep, Lehmann sums;
+    device times of each phase (CUDA events on the engine stream)."""
+    eng.sweep_dm(**W)
+    fwd = eng.timing()["device_ms"]
+    prm = eng.dm_params(temp=DM_TEMP, bbroad=DM_BROAD)
+    eng.dm_backprop(prm)
+    back = eng.timing()["dm_backprop_ms"]
+    om, A = eng.lehmann(prm, omegas=dm_omegas(nomega))
+    t = eng.timing()
+    return fwd, back, t["dm_spectral_ms"], t["lehmann_ms"], t["lehmann_pairs"], t["lehmann_evals"], A
+
+
 def gpu_batch(workers: int, device: int):
     import twochnrg_gb300 as tg
     from twochnrg_gb300.workloads import batched_qsz
@@ -264,8 +292,8 @@ def main():
                                     "entry in MEASURED_PEAKS.json)",
                      "algorithmic": "4/3 sum_b n_b^3 flops per iteration"},
         "clocks": ck,
-        "phases_ms": {k: T[k] for k in ("assemble_ms", "tridiag_ms", "tridiag_eig_ms", "backtransform_ms",
-                                          "cut_ms", "update_ms")},
+        "phases_ms": {k: T[k] for k in ("assemble_ms", "tridiag_ms", "tridiag_eig_ms", "vectors_ms",
+                                          "backtransform_ms", "cut_ms", "update_ms")},
         "sum_n3": w_full,
     }
     # second half of the metric: batched independent solves per second
@@ -273,6 +301,14 @@ def main():
     line["batched"] = {"metric": "batched solves/s", "value": bs * (ws if dist else 1), "unit": "solves/s",
                        "instances": BATCH_INSTANCES, "seconds": bsec, "workers": args.batch_workers,
                        "workload": BATCH_NAME, "timing": "host wall time of nrg_sweep_batch"}
+    # DM-NRG spectral function (one-channel: the reference's DM_NRG is d = 4 only)
+    gpu_dm(eng, DM_WORKLOAD, 200)  # warm-up
+    fwd, back, spec, leh, pairs, evals, _ = gpu_dm(eng, DM_WORKLOAD, DM_NOMEGA)
+    line["dm_spectral"] = {
+        "workload": DM_NAME, "unit": "ms", "forward_sweep_ms": fwd, "backprop_ms": back, "spectral_ms": spec,
+        "total_ms": fwd + back + spec, "lehmann_kernel_ms": leh, "lehmann_pairs": pairs,
+        "lehmann_evals": evals, "lehmann_evals_per_s": evals / (leh * 1e-3) if leh > 0 else None,
+        "lehmann_bound": "fp64 (one log and one exp per pair and frequency)"}
     if not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         dt, w_s = cpu_sample(cores)
@@ -284,6 +320,19 @@ def main():
         line["batched"]["cpu_baseline"] = {
             "value": cbs, "unit": "solves/s", "cores": cores, "kind": "port",
             "sample": f"oracle port on the first {cn} instances, one per thread: {cdt:.2f} s"}
+        # DM-NRG: GPU and the oracle port on the same reduced case (the port
+        # evaluates every frequency with dense products, as DM_NRG does)
+        from oracle import oracle as orc
+        g = gpu_dm(eng, DM_SAMPLE, DM_SAMPLE_NOMEGA)
+        t = time.perf_counter()
+        orc.dm_spectral(DM_SAMPLE["nsites"], DM_SAMPLE["ncutoff"], DM_SAMPLE["lam"], DM_SAMPLE["U"],
+                        DM_SAMPLE["ed"], DM_SAMPLE["gamma"], DM_TEMP, DM_BROAD, omegas=dm_omegas(DM_SAMPLE_NOMEGA))
+        cdm = (time.perf_counter() - t) * 1e3
+        line["dm_spectral"]["cpu_baseline"] = {
+            "value": cdm, "unit": "ms", "cores": 1, "kind": "port",
+            "sample": (f"oracle port (single thread) on {DM_SAMPLE['nsites']} iterations, {DM_SAMPLE['ncutoff']} "
+                       f"kept, {DM_SAMPLE_NOMEGA} frequencies, same T and b; GPU on that case: "
+                       f"{g[0] + g[1] + g[2]:.1f} ms")}
     print(json.dumps(line), flush=True)
     eng.close()
     if dist:
