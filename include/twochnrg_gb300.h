@@ -314,6 +314,33 @@ nrg_status nrg_dm_backprop(nrg_ctx* ctx, const nrg_dm_params* prm, double* rho_t
 nrg_status nrg_lehmann(nrg_ctx* ctx, const nrg_dm_params* prm, int nomega, const double* omegas, double* omega_rhow,
                        int* nout);
 
+/* ---- .bin snapshots in the reference's layout ---------------------------
+ * One DM-NRG shell as NRG_main saves it with UpdateBefCut = 1
+ * (CNRGCodeHandler::SaveArrays, NRGcodehandlerClass.cpp:887-932). */
+typedef struct {
+  int nshell;                    /* N */
+  nrg_basis basis;               /* Abasis_N: blocks, iType, StCameFrom, dEn (old energies) */
+  nrg_blocks blocks;             /* Acut_N: the blocks of all states of H_N */
+  const double* en;              /* [nstates] dEn (SetE0zero, SetDegen) */
+  const unsigned char* kept;     /* [nstates] Kept */
+  const double* eigvec;          /* dEigVec: per block n x n, row = eigenvector */
+  nrg_matrix cd;                 /* c_d between all states of H_N */
+} nrg_dm_shell;
+
+/* Writes Abasis_<name>_N<n>.bin, Acut_<name>_N<n>.bin and Mat0_<name>_N<n>.bin
+ * into `dir` in the byte layout of CNRGbasisarray::SaveBin / CNRGmatrix::SaveBin
+ * (NRGarrayClass.cpp:780-868, 1947-2003; NRGmatrixClass.cpp:957-1015), for the
+ * one-channel |Q S> model; needs no device. */
+nrg_status nrg_write_dm_shell(const char* dir, const char* name, const nrg_dm_shell* s);
+
+/* ThisCodePars.dat as CNRGCodeHandler::SaveGenPars writes it
+ * (NRGcodehandlerClass.cpp): what DM_NRG reads before the shells. */
+nrg_status nrg_write_code_pars(const char* dir, double lambda, int nsites, const char* name);
+
+/* The shells of the last nrg_sweep_run_dm written with nrg_write_dm_shell,
+ * plus ThisCodePars.dat: the reference's DM_NRG can then run on them. */
+nrg_status nrg_dm_save_bin(nrg_ctx* ctx, const char* dir, const char* name);
+
 /* Largest block nrg_diag_block_noalloc accepts. */
 #define NRG_NOALLOC_MAX_N 256
 

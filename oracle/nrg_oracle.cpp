@@ -1545,6 +1545,39 @@ double oracle_dm_shell_term(void* h, const oracle_dm_params* prm, int N, double 
   return spec_fdm(c, R->dm, rho, N, p, omegabar);
 }
 
+// The DM-NRG shells of a run made with cfg->dm, field by field (NULL and
+// *len = -1 if absent): basis_qn/bbe/itype/stcf/en (Abasis_N), qn/bbe/en/
+// kept/evec (Acut_N), cd_map/cd_mbe/cd_el (c_d).
+const double* oracle_dm_d(void* h, int N, const char* name, int* len) {
+  OracleRun* R = (OracleRun*)h;
+  *len = -1;
+  if (N < 0 || N >= (int)R->dm.size()) return nullptr;
+  const DmShell& s = R->dm[N];
+  const std::string k(name);
+  const std::vector<double>* v = nullptr;
+  if (k == "basis_qn") v = &s.ab.qn; else if (k == "basis_en") v = &s.ab.en; else if (k == "qn") v = &s.full.qn;
+  else if (k == "en") v = &s.full.en; else if (k == "evec") v = &s.full.evec; else if (k == "cd_el") v = &s.cd.el;
+  if (!v) return nullptr;
+  *len = (int)v->size();
+  return v->data();
+}
+const int* oracle_dm_i(void* h, int N, const char* name, int* len) {
+  OracleRun* R = (OracleRun*)h;
+  *len = -1;
+  if (N < 0 || N >= (int)R->dm.size()) return nullptr;
+  static thread_local std::vector<int> kept;
+  const DmShell& s = R->dm[N];
+  const std::string k(name);
+  const std::vector<int>* v = nullptr;
+  if (k == "basis_bbe") v = &s.ab.bbe; else if (k == "basis_itype") v = &s.ab.itype;
+  else if (k == "basis_stcf") v = &s.ab.stcf; else if (k == "bbe") v = &s.full.bbe;
+  else if (k == "cd_map") v = &s.cd.map; else if (k == "cd_mbe") v = &s.cd.mbe;
+  else if (k == "kept") { kept.assign(s.full.kept.begin(), s.full.kept.end()); v = &kept; }
+  if (!v) return nullptr;
+  *len = (int)v->size();
+  return v->data();
+}
+
 // Named captures of the capture iteration: NULL (and *len = -1) if absent.
 const double* oracle_cap_d(void* h, int n, const char* name, int* len) {
   auto& m = ITER(h, n).capd;

@@ -43,6 +43,8 @@ void oracle_free(void* h);
 /* Named arrays of the capture iteration (NULL and *len = -1 if absent). */
 const double* oracle_cap_d(void* h, int n, const char* name, int* len);
 const int* oracle_cap_i(void* h, int n, const char* name, int* len);
+const double* oracle_dm_d(void* h, int N, const char* name, int* len);
+const int* oracle_dm_i(void* h, int N, const char* name, int* len);
 int oracle_dm_spectral(void* h, const oracle_dm_params* prm, const double* omegas, int nomega, double* omega_out,
                        double* a_out, int cap, double* rho_trace);
 

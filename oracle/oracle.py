@@ -85,6 +85,11 @@ def lib():
                                           ctypes.POINTER(ctypes.c_double), ctypes.c_int,
                                           ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                           ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        L.oracle_dm_d.restype = ctypes.POINTER(ctypes.c_double)
+        L.oracle_dm_i.restype = ctypes.POINTER(ctypes.c_int)
+        for name in ("oracle_dm_d", "oracle_dm_i"):
+            getattr(L, name).argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p,
+                                         ctypes.POINTER(ctypes.c_int)]
         L.oracle_diag_block.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         rc = L.oracle_load_lapack(openblas_path().encode())
@@ -242,6 +247,37 @@ def dm_spectral(nsites: int, ncutoff: int, lam: float, U: float, ed: float, gamm
         if n < 0:
             raise RuntimeError("oracle: " + L.oracle_last_error().decode())
         return om[:n], A[:n], tr
+    finally:
+        L.oracle_free(h)
+
+
+_DM_D = ("basis_qn", "basis_en", "qn", "en", "evec", "cd_el")
+_DM_I = ("basis_bbe", "basis_itype", "basis_stcf", "bbe", "kept", "cd_map", "cd_mbe")
+
+
+def dm_shells(nsites: int, ncutoff: int, lam: float, U: float, ed: float, gamma: float, nthreads: int = 1):
+    """The DM-NRG shells of the one-channel |Q S> Anderson sweep (UpdateBefCut
+    = 1, c_d), one dict of arrays per shell (Abasis_N: basis_*; Acut_N: qn,
+    bbe, en, kept, evec; c_d: cd_*)."""
+    L = lib()
+    cfg = _Cfg(MODEL_1CHQS, nsites, ncutoff, lam, U, ed, gamma, 0.0, 0.0, nthreads, -1, 1)
+    h = L.oracle_run(ctypes.byref(cfg))
+    if not h:
+        raise RuntimeError("oracle: " + L.oracle_last_error().decode())
+    h = ctypes.c_void_p(h)
+    try:
+        out = []
+        ln = ctypes.c_int(0)
+        for N in range(nsites):
+            d = {}
+            for k in _DM_D:
+                p = L.oracle_dm_d(h, N, k.encode(), ctypes.byref(ln))
+                d[k] = _arr(p, ln.value, np.float64)
+            for k in _DM_I:
+                p = L.oracle_dm_i(h, N, k.encode(), ctypes.byref(ln))
+                d[k] = _arr(p, ln.value, np.int64)
+            out.append(d)
+        return out
     finally:
         L.oracle_free(h)
 

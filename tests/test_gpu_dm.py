@@ -65,3 +65,48 @@ def test_dm_call_order_and_model_errors(engine):
     with pytest.raises(tg.NRGError) as e:  # Lehmann sums before the backward sweep
         engine.lehmann(prm)
     assert e.value.status == 8
+
+
+def test_dm_shells_saved_in_reference_layout(engine, tmp_path):
+    """nrg_dm_save_bin: the GPU sweep's shells as the reference's .bin files.
+    Integers (blocks, iType, StCameFrom, Kept, MatBlockMap) equal the oracle's
+    shells exactly; energies within 1e-12.  From shell 1 on, the product basis
+    carries each implementation's own eigenvector signs (H_N agrees up to
+    that gauge), so eigenvectors are checked by orthonormality (and against
+    the oracle's in shell 0), and c_d by the Frobenius norm of each block
+    pair, which the gauge leaves unchanged."""
+    from oracle.binfiles import read_bin
+    ns, nc = 8, 60
+    engine.sweep_dm(ns, nc, 2.5, 0.5, -0.25, 0.02)
+    engine.dm_save_bin(str(tmp_path), "1chQSAnderson")
+    ref = orc.dm_shells(ns, nc, 2.5, 0.5, -0.25, 0.02)
+    pars = open(tmp_path / "ThisCodePars.dat").read().split()
+    assert float(pars[0]) == 2.5 and int(pars[2]) == ns and pars[4] == "1chQSAnderson"
+    for N, s in enumerate(ref):
+        ab = read_bin(str(tmp_path / f"Abasis_1chQSAnderson_N{N}.bin"), "basis")
+        ac = read_bin(str(tmp_path / f"Acut_1chQSAnderson_N{N}.bin"), "basis")
+        m = read_bin(str(tmp_path / f"Mat0_1chQSAnderson_N{N}.bin"), "matrix")
+        np.testing.assert_array_equal(ab["QNumbers"], s["basis_qn"])
+        np.testing.assert_array_equal(ab["BlockBegEnd"], s["basis_bbe"])
+        np.testing.assert_array_equal(ab["iType"], s["basis_itype"])
+        np.testing.assert_array_equal(ab["StCameFrom"], s["basis_stcf"])
+        np.testing.assert_allclose(ab["dEn"], s["basis_en"], rtol=0, atol=1e-12 * max(1, np.abs(s["basis_en"]).max()))
+        np.testing.assert_array_equal(ac["BlockBegEnd"], s["bbe"])
+        np.testing.assert_array_equal(ac["Kept"], s["kept"])
+        np.testing.assert_allclose(ac["dEn"], s["en"], rtol=0, atol=1e-12 * max(1, np.abs(s["en"]).max()))
+        np.testing.assert_array_equal(m["MatBlockMap"], s["cd_map"])
+        np.testing.assert_array_equal(m["MatBlockBegEnd"], s["cd_mbe"])
+        bbe = s["bbe"]
+        off = 0
+        for b in range(len(bbe) // 2):
+            n = int(bbe[2 * b + 1] - bbe[2 * b] + 1)
+            Z = ac["dEigVec"][off:off + n * n].reshape(n, n)
+            Zr = s["evec"][off:off + n * n].reshape(n, n)
+            off += n * n
+            assert np.abs(Z @ Z.T - np.eye(n)).max() < 1e-11
+            if N == 0:
+                np.testing.assert_allclose(np.abs(Z @ Zr.T), np.eye(n), atol=1e-9)
+        for k in range(len(s["cd_map"]) // 2):
+            lo, hi = s["cd_mbe"][2 * k], s["cd_mbe"][2 * k + 1] + 1
+            a, r = m["MatEl"][lo:hi], s["cd_el"][lo:hi]
+            assert abs(np.linalg.norm(a) - np.linalg.norm(r)) < 1e-10 * max(1.0, np.linalg.norm(r))

@@ -103,6 +103,11 @@ class _CutResult(ctypes.Structure):
                 ("cut", _EigCut)]
 
 
+class DmShell(ctypes.Structure):
+    _fields_ = [("nshell", ctypes.c_int), ("basis", _Basis), ("blocks", _Blocks), ("en", _DP), ("kept", _UP),
+                ("eigvec", _DP), ("cd", _Matrix)]
+
+
 class _Keep:
     """Holds the numpy arrays a ctypes structure points into."""
 
@@ -129,6 +134,30 @@ class _Keep:
 
 
 _lib = None
+
+
+def write_dm_shell(directory: str, name: str, nshell: int, shell: dict) -> None:
+    """Write one DM-NRG shell (dict with basis_qn/bbe/itype/stcf/en, qn, bbe, en,
+    kept, evec, cd_map/cd_mbe/cd_el) as the reference's Abasis/Acut/Mat0 .bin
+    files.  Needs no device."""
+    L = load_library()
+    k = _Keep()
+    kept = np.ascontiguousarray(shell["kept"], dtype=np.uint8)
+    k.refs.append(kept)
+    s = DmShell(nshell,
+                _Basis(k.blocks(shell["basis_qn"], shell["basis_bbe"]), k.i(shell["basis_itype"]),
+                       k.i(shell["basis_stcf"]), k.d(shell["basis_en"])),
+                k.blocks(shell["qn"], shell["bbe"]), k.d(shell["en"]), kept.ctypes.data_as(_UP),
+                k.d(shell["evec"]), k.matrix((shell["cd_map"], shell["cd_mbe"], shell["cd_el"])))
+    st = L.nrg_write_dm_shell(directory.encode(), name.encode(), ctypes.byref(s))
+    if st != 0:
+        raise NRGError(st, f"cannot write shell {nshell} into {directory}")
+
+
+def write_code_pars(directory: str, lam: float, nsites: int, name: str) -> None:
+    st = load_library().nrg_write_code_pars(directory.encode(), float(lam), int(nsites), name.encode())
+    if st != 0:
+        raise NRGError(st, f"cannot write ThisCodePars.dat into {directory}")
 
 
 def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
@@ -169,6 +198,9 @@ def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     L.nrg_dm_num_shells.argtypes = [ctypes.c_void_p]
     L.nrg_dm_backprop.argtypes = [ctypes.c_void_p, ctypes.POINTER(DmParams), _dp]
     L.nrg_lehmann.argtypes = [ctypes.c_void_p, ctypes.POINTER(DmParams), ctypes.c_int, _dp, _dp, _ip]
+    L.nrg_write_dm_shell.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(DmShell)]
+    L.nrg_write_code_pars.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_int, ctypes.c_char_p]
+    L.nrg_dm_save_bin.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]
     L.nrg_sweep_batch.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(SweepConfig), ctypes.c_int,
                                   ctypes.c_int, _dp, _dp, _ip, _dp]
     _lib = L
@@ -362,6 +394,10 @@ class Engine:
                                        ctypes.byref(nout)))
         n = nout.value
         return out[:n].copy(), out[cap:cap + n].copy()
+
+    def dm_save_bin(self, directory: str, name: str) -> None:
+        """The DM-NRG shells as the reference's .bin files plus ThisCodePars.dat."""
+        self._check(self.L.nrg_dm_save_bin(self.h, directory.encode(), name.encode()))
 
     def timing(self) -> dict:
         t = Timing()

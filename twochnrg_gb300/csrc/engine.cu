@@ -143,6 +143,7 @@ struct nrg_ctx {
   std::vector<std::unique_ptr<nrg::DmShell>> dm;
   bool dm_rho_valid = false;
   double dm_temp = 0.0;                // temperature the density matrices were built for
+  std::vector<double> dm_hm1_en;       // H_{-1} energies (what shell 0's basis came from)
 };
 
 namespace nrg {
@@ -242,7 +243,11 @@ void plan_blocks(EigPlan& P, const std::vector<int>& bsize) {
   P.hsize = h;
 }
 
-int choose_cluster(int maxn) { return maxn >= 256 ? 16 : 8; }
+int choose_cluster(int maxn) {
+  const char* s = std::getenv("NRG_CLUSTER");
+  if (s) return std::atoi(s);
+  return maxn >= 256 ? 16 : 8;
+}
 
 // Blocks at least this large are tridiagonalized by a cooperative grid of
 // many SMs (one block after the other per grid); smaller ones by one
@@ -713,7 +718,10 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false) {
 
   // H_{-1} (the initial CutStates keeps everything: Ncutoff >= 4 states).
   StartState st = make_start(m, lambda, cfg->U, cfg->ed, cfg->gamma2_or_B);
-  if (dm) st.ops = {st.ops[0], st.ops[0]};  // c_d at H_{-1} is a copy of f (Main_SetH0.cpp:1958-1961)
+  if (dm) {
+    st.ops = {st.ops[0], st.ops[0]};  // c_d at H_{-1} is a copy of f (Main_SetH0.cpp:1958-1961)
+    c->dm_hm1_en = st.en;
+  }
   S.kept.blk = st.blk;
   // Operators are stored by the blocks of `opsize`; opblock maps a kept
   // block to that structure (empty: the kept array itself).
@@ -1247,6 +1255,73 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
   c->timing.lehmann_evals = evals;
   for (int k = 0; k < nw_; ++k) { omega_rhow[k] = om[k]; omega_rhow[nomega + k] = A[k]; }
   *nout = nw_;
+}
+
+// The DM-NRG shells as the reference's .bin snapshots.  Abasis_N's
+// StCameFrom numbers the states of the uncut array of shell N-1 (UpdateBefCut,
+// BuildBasis.cpp:386-391): a state that came from state a of kept block k came
+// from state a of that kept block's uncut block.
+void dm_save_bin_impl(nrg_ctx* c, const char* dir, const char* name) {
+  if (c->dm.empty()) throw NrgError(NRG_ERR_STATE, "no DM-NRG shells: run nrg_sweep_run_dm first");
+  if (!dir || !name) throw NrgError(NRG_ERR_ARG, "directory or name is NULL");
+  for (size_t N = 0; N < c->dm.size(); ++N) {
+    const DmShell& s = *c->dm[N];
+    const Basis& B = s.basis;
+    const int ns = B.blk.nstates();
+    std::vector<int> bbbe, stcf(ns), bbe;
+    std::vector<double> ben(ns);
+    for (int b = 0; b < B.blk.nblocks(); ++b) {
+      bbbe.push_back(B.blk.offset[b]);
+      bbbe.push_back(B.blk.offset[b] + B.blk.size[b] - 1);
+      for (int i = 0; i < B.blk.size[b]; ++i) {
+        const int g = B.blk.offset[b] + i;
+        const Segment& sg = B.seg[b][B.seg_of[g]];
+        int full;
+        double e;
+        if (N == 0) {
+          full = B.stcf[g];
+          e = c->dm_hm1_en[full];
+        } else {
+          const DmShell& p = *c->dm[N - 1];
+          full = p.boff[p.kept_src[sg.old_block]] + B.a_of[g];
+          e = p.en[full];
+        }
+        stcf[g] = full;
+        ben[g] = e;
+      }
+    }
+    for (size_t b = 0; b < s.bsize.size(); ++b) {
+      bbe.push_back(s.boff[b]);
+      bbe.push_back(s.boff[b] + s.bsize[b] - 1);
+    }
+    std::vector<double> Z((size_t)std::max<int64_t>(s.zsize, 1)), el((size_t)std::max<int64_t>(s.cd.size, 1));
+    d2h(c, Z.data(), s.Z.p, sizeof(double) * s.zsize);
+    d2h(c, el.data(), s.cdel.p, sizeof(double) * s.cd.size);
+    CU(cudaStreamSynchronize(c->stream));
+    std::vector<int> map, mbe;
+    for (size_t k = 0; k < s.cd.bi.size(); ++k) {
+      map.push_back(s.cd.bi[k]);
+      map.push_back(s.cd.bj[k]);
+      const int64_t len = (int64_t)s.bsize[s.cd.bi[k]] * s.bsize[s.cd.bj[k]];
+      mbe.push_back((int)s.cd.off[k]);
+      mbe.push_back((int)(s.cd.off[k] + len - 1));
+    }
+    nrg_dm_shell v{};
+    v.nshell = (int)N;
+    v.basis.blocks = nrg_blocks{B.blk.nblocks(), 2, B.blk.qn.data(), bbbe.data()};
+    v.basis.itype = B.itype.data();
+    v.basis.st_came_from = stcf.data();
+    v.basis.en = ben.data();
+    v.blocks = nrg_blocks{(int)s.bsize.size(), 2, s.qn.data(), bbe.data()};
+    v.en = s.en.data();
+    v.kept = s.kept.data();
+    v.eigvec = Z.data();
+    v.cd = nrg_matrix{(int)s.cd.bi.size(), map.data(), mbe.data(), el.data()};
+    const nrg_status st = nrg_write_dm_shell(dir, name, &v);
+    if (st != NRG_OK) throw NrgError(st, std::string("cannot write the shell files into ") + dir);
+  }
+  const nrg_status st = nrg_write_code_pars(dir, c->dm_lambda, (int)c->dm.size(), name);
+  if (st != NRG_OK) throw NrgError(st, std::string("cannot write ThisCodePars.dat into ") + dir);
 }
 
 // DiagBlock for a batch of blocks given in the reference's packed upper
@@ -1849,6 +1924,16 @@ nrg_status nrg_lehmann(nrg_ctx* ctx, const nrg_dm_params* prm, int nomega, const
     CU(cudaSetDevice(ctx->device));
     std::memset(&ctx->timing, 0, sizeof(ctx->timing));
     lehmann_impl(ctx, prm, nomega, omegas, omega_rhow, nout);
+  });
+  return NRG_OK;
+}
+
+nrg_status nrg_dm_save_bin(nrg_ctx* ctx, const char* dir, const char* name) {
+  if (!ctx) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    dm_save_bin_impl(ctx, dir, name);
   });
   return NRG_OK;
 }
