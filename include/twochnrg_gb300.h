@@ -314,6 +314,50 @@ nrg_status nrg_dm_backprop(nrg_ctx* ctx, const nrg_dm_params* prm, double* rho_t
 nrg_status nrg_lehmann(nrg_ctx* ctx, const nrg_dm_params* prm, int nomega, const double* omegas, double* omega_rhow,
                        int* nout);
 
+/* ---- thermodynamics with the free-chain subtraction --------------------
+ * The reference computes the impurity T chi and S in two NRG_main runs
+ * (calcdens = 3, then 2): the free Wilson chain first, written to
+ * SuscepChain*.dat / EntropyChain*.dat, then the impurity sweep, which reads
+ * those files back (CNRGthermo::ReadNChainValue, NRGthermoClass.cpp:66-103)
+ * and writes T, value, chain value, value - chain
+ * (CNRGthermo::SaveNValue, NRGthermoClass.cpp:109-150).
+ *
+ * nrg_sweep_run_chain: the calcdens = 3 sweep (ModelNo 3,
+ * CodeHandler_ModelSwitch.cpp:377-420, 667-720, 940-1000).  H_0 is the first
+ * Wilson site alone (iteration 0, thermodynamics at D_0 as NRG_main.cpp:242-255
+ * takes them); iterations 1 .. nsites-1 add one site each.  U, ed, gamma1 and
+ * gamma2_or_B are ignored (ZeroParams).  Results through nrg_sweep_iteration. */
+nrg_status nrg_sweep_run_chain(nrg_ctx* ctx, const nrg_sweep_config* cfg);
+
+typedef struct {
+  int nvalues;                 /* 4*nsites: value k = 4N + nc - 1, N the iteration, nc = 1..4 */
+  const double* temp;          /* [nvalues] T_M = D_N / betabar_nc (both sweeps agree bit for bit) */
+  const double* suscep;        /* T chi (CalcSuscep) of the impurity sweep */
+  const double* suscep_chain;  /* T chi of the free chain */
+  const double* suscep_imp;    /* suscep - suscep_chain */
+  const double* entropy;       /* S (CalcEntropy) of the impurity sweep */
+  const double* entropy_chain;
+  const double* entropy_imp;
+  int chain_reused;            /* 1: the chain values came from an earlier call */
+  double chain_ms, imp_ms, total_ms; /* host wall times of the chain sweep, the impurity sweep, the call */
+} nrg_thermo;
+
+/* Both sweeps for one parameter set: the chain sweep runs on a second
+ * context (own stream, own host thread) beside the impurity sweep on `ctx`.
+ * With reuse_chain != 0 and the chain parameters (model, nsites, ncutoff,
+ * lambda, degen_eps, precision) equal to the last call's, the stored chain
+ * values are used instead, as the reference reuses its chain files.  The
+ * impurity sweep's iterations stay readable with nrg_sweep_iteration.
+ * Returns NRG_ERR_SYNC if the two sweeps' temperatures differ. */
+nrg_status nrg_thermo_run(nrg_ctx* ctx, const nrg_sweep_config* cfg, int reuse_chain, nrg_thermo* out);
+
+/* One thermodynamics file in the layout of CNRGthermo::SaveNValue: per line
+ * T value chain value-chain, each "%.20e" (ofstream precision 20,
+ * scientific).  chain == NULL writes a chain file (third column 0).  Needs
+ * no device. */
+nrg_status nrg_write_thermo(const char* path, int nvalues, const double* temp, const double* value,
+                            const double* chain);
+
 /* ---- .bin snapshots in the reference's layout ---------------------------
  * One DM-NRG shell as NRG_main saves it with UpdateBefCut = 1
  * (CNRGCodeHandler::SaveArrays, NRGcodehandlerClass.cpp:887-932). */

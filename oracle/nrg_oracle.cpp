@@ -931,6 +931,39 @@ void hm1_QSz(double Lambda, double HLF, double U, double ed, double B, Arr& a, M
   avg = {diag_op(a, nd, "Ndot"), diag_op(a, sz, "Szdot")};
 }
 
+// TwoChQS_SetH0Chain (Main/Main_SetH0.cpp:3472-3560): the two-channel first
+// site in its multiplet basis (QNumbers, BlockBegEnd and iType as listed
+// there, StCameFrom 0, all energies 0, identity eigenvectors), and f_ch1,
+// f_ch2 by CNRGmatrix::SetMatrix (NRGmatrixClass.cpp:1836-1877): every block
+// pair passing CheckForMatEl, every state pair through CalcMatEl.
+void h0_chain_2chQS(Ctx& c, Arr& a, Mat& f1, Mat& f2) {
+  Basis b; b.nqn = 2; b.nshell = 0;
+  b.qn = {-2, 0, -1, 0.5, 0, 0, 0, 1, 1, 0.5, 2, 0};
+  b.bbe = {0, 0, 1, 2, 3, 5, 6, 6, 7, 8, 9, 9};
+  b.itype = {0, 1, 2, 5, 6, 7, 10, 11, 12, 15};
+  b.stcf.assign(10, 0);
+  a = Arr(); a.nqn = 2; a.nshell = 0; a.totalS = true; a.sqn = {1};
+  a.qn = b.qn; a.bbe = b.bbe;
+  a.en.assign(10, 0.0);
+  for (int k = 0; k < a.nblocks(); ++k)
+    for (int i = 0; i < a.bsize(k); ++i)
+      for (int j = 0; j < a.bsize(k); ++j) a.evec.push_back(i == j ? 1.0 : 0.0);
+  Mat* out[2] = {&f1, &f2};
+  const int rules[2] = {R_F1_2CH, R_F2_2CH};
+  for (int o = 0; o < 2; ++o) {
+    Mat& M = *out[o];
+    M = Mat(); M.blk = a; M.blk.evec.clear();
+    for (int i = 0; i < b.nblocks(); ++i)
+      for (int j = 0; j < b.nblocks(); ++j) {
+        if (!check(C_2CH_CD, b, i, j)) continue;
+        std::vector<double> v;
+        for (int ist = b.beg(i); ist <= b.end(i); ++ist)
+          for (int jst = b.beg(j); jst <= b.end(j); ++jst) v.push_back(op_rule(c, rules[o], b, ist, jst));
+        M.push_block(i, j, v.data(), (int)v.size());
+      }
+  }
+}
+
 // ---------------------------------------------------------------- DM-NRG
 // What NRG_main saves per shell when the spectral density is asked for
 // (calcdens = 1, UpdateBefCut = 1; CNRGCodeHandler::SaveArrays,
@@ -1341,6 +1374,11 @@ void* oracle_run(const oracle_config* cfg) {
   if (dm && cfg->model != ORACLE_MODEL_1CHQS) {
     g_err = "DM-NRG shells are restated for the one-channel |Q S> model only"; delete R; return nullptr;
   }
+  // calcdens = 3: the free Wilson chain (ModelNo 3 with ZeroParams,
+  // NRGcodehandlerClass.cpp:85-91; CodeHandler_ModelSwitch.cpp:377-420,
+  // 667-720, 940-1000).  H_0 is the first site alone and only f_N is kept.
+  const bool chain = cfg->chain != 0;
+  if (chain && dm) { g_err = "chain and DM-NRG runs are exclusive"; delete R; return nullptr; }
   Arr eig;
   std::vector<Mat> mats;
   std::vector<double> P;
@@ -1348,7 +1386,38 @@ void* oracle_run(const oracle_config* cfg) {
   bool totalS = true;
   int nchan = 1;
   double chi1 = std::sqrt(2.0 * cfg->gamma1 / pi) / (std::sqrt(Lambda) * HLF) * ALambda;
-  if (cfg->model == ORACLE_MODEL_1CHQS) {
+  if (chain) {
+    // OneChQS_SetChainH0 / OneChQSz_SetChainH0 (Main/Main_SetH0.cpp:3322-3465)
+    // are the impurity start-ups' blocks and f elements at U = ed = B = 0.
+    const double chi0 = chin(0);
+    if (cfg->model == ORACLE_MODEL_1CHQS) {
+      c.m.site = site_1chQS(); c.m.totS = {1};
+      Mat f; std::vector<Mat> avg;
+      hm1_QS(Lambda, HLF, 0.0, 0.0, eig, f, avg);
+      mats.push_back(f);
+      c.m.op_rule = {R_F_QS}; c.m.op_check = {C_QS_CD};
+      P = {Lambda, chi0, 0.0, 0.0};
+    } else if (cfg->model == ORACLE_MODEL_1CHQSZ) {
+      c.m.site = site_1chQSz(); c.m.totS = {};
+      Mat fu, fd; std::vector<Mat> avg;
+      hm1_QSz(Lambda, HLF, 0.0, 0.0, 0.0, eig, fu, fd, avg);
+      mats.push_back(fu); mats.push_back(fd);
+      c.m.op_rule = {R_FUP_QSZ, R_FDN_QSZ}; c.m.op_check = {C_Q_CD, C_Q_CD};
+      P = {Lambda, chi0, 0.0, 0.0};
+      totalS = false;
+    } else if (cfg->model == ORACLE_MODEL_2CHQS) {
+      c.m.site = site_2chQS(); c.m.totS = {1};
+      Mat f1, f2;
+      h0_chain_2chQS(c, eig, f1, f2);
+      mats.push_back(f1); mats.push_back(f2);
+      c.m.op_rule = {R_F1_2CH, R_F2_2CH}; c.m.op_check = {C_2CH_CD, C_2CH_CD};
+      P = {Lambda, chi0, chi0, 0.0, 0.0};
+      nchan = 2;
+    } else {
+      g_err = "unknown model"; delete R; return nullptr;
+    }
+    eig.nshell = 0;
+  } else if (cfg->model == ORACLE_MODEL_1CHQS) {
     c.m.site = site_1chQS(); c.m.totS = {1};
     Mat f; std::vector<Mat> avg;
     hm1_QS(Lambda, HLF, cfg->U, cfg->ed, eig, f, avg);
@@ -1398,7 +1467,27 @@ void* oracle_run(const oracle_config* cfg) {
   Basis cut, ab;
   cut_states(eig, cut, cfg->ncutoff, eps);
   for (auto& m : mats) if (m.calc_avg) R->opavg_m1.push_back(calc_opavg(cut, m, betabar, totalS, sq));
-  for (int N = 0; N < cfg->nsites; ++N) {
+  int N0 = 0;
+  if (chain) {
+    // Nsites0 = 1: CalcThermo on H_0 before the loop, at D = HLF
+    // Lambda^(-(Nsites0-2)/2) (NRG_main.cpp:242-255).
+    OracleIter I;
+    I.params = P;
+    const double D0 = HLF * std::pow(Lambda, 0.5);
+    I.qn = eig.qn;
+    for (int b = 0; b < eig.nblocks(); ++b) { I.bsize.push_back(eig.bsize(b)); I.kept_bsize.push_back(eig.bsize(b)); }
+    I.en = eig.en;
+    I.nkept = eig.nstates();
+    for (int nc = 1; nc <= 4; ++nc) {
+      double bN = betabar * std::pow(Lambda, (nc - 4) / (2.0 * 4));
+      I.thermo.push_back(bN); I.thermo.push_back(D0 / bN);
+      I.thermo.push_back(calc_suscep(eig, bN, sq, totalS));
+      I.thermo.push_back(calc_entropy(eig, bN, sq, totalS));
+    }
+    R->it.push_back(std::move(I));
+    N0 = 1;
+  }
+  for (int N = N0; N < cfg->nsites; ++N) {
     OracleIter I;
     I.params = P;
     double DN = HLF * std::pow(Lambda, (-(N - 1) / 2.0));

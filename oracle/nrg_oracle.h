@@ -19,6 +19,7 @@ typedef struct {
   int nthreads;       /* host threads over blocks / block pairs */
   int capture_iter;   /* iteration whose DiagHN inputs/H are kept, -1 none */
   int dm;             /* keep DM-NRG shells (UpdateBefCut = 1, c_d); 1chQS only */
+  int chain;          /* the free Wilson chain of calcdens = 3 (H_0 = first site, iterations 1..nsites-1) */
 } oracle_config;
 
 /* DM-NRG parameters (DM_NRG command line, DM_NRG_CommandLineRead.cpp). */

@@ -25,7 +25,7 @@ class _Cfg(ctypes.Structure):
                 ("lambda_", ctypes.c_double), ("U", ctypes.c_double), ("ed", ctypes.c_double),
                 ("gamma1", ctypes.c_double), ("gamma2_or_B", ctypes.c_double),
                 ("degen_eps", ctypes.c_double), ("nthreads", ctypes.c_int),
-                ("capture_iter", ctypes.c_int), ("dm", ctypes.c_int)]
+                ("capture_iter", ctypes.c_int), ("dm", ctypes.c_int), ("chain", ctypes.c_int)]
 
 
 class _DmParams(ctypes.Structure):
@@ -137,11 +137,13 @@ def _arr(ptr, n, dtype):
 
 def run(model: str, nsites: int, ncutoff: int, lam: float, U: float, ed: float, gamma1: float,
         gamma2_or_B: float = 0.0, nthreads: int = 1, capture_iter: int = -1,
-        degen_eps: float = 0.0, blas_threads: int = 1) -> Sweep:
+        degen_eps: float = 0.0, blas_threads: int = 1, chain: bool = False) -> Sweep:
+    """One sweep.  chain=True: the free Wilson chain of calcdens = 3 (U, ed and
+    the couplings are ignored; iteration 0 is the first site alone)."""
     L = lib()
     L.oracle_blas_threads(int(blas_threads))
     cfg = _Cfg(MODELS[model], nsites, ncutoff, lam, U, ed, gamma1, gamma2_or_B, degen_eps,
-               nthreads, capture_iter, 0)
+               nthreads, capture_iter, 0, 1 if chain else 0)
     h = L.oracle_run(ctypes.byref(cfg))
     if not h:
         raise RuntimeError("oracle: " + L.oracle_last_error().decode())

@@ -160,6 +160,71 @@ def write_code_pars(directory: str, lam: float, nsites: int, name: str) -> None:
         raise NRGError(st, f"cannot write ThisCodePars.dat into {directory}")
 
 
+class _Thermo(ctypes.Structure):
+    _fields_ = [("nvalues", ctypes.c_int), ("temp", _DP), ("suscep", _DP), ("suscep_chain", _DP),
+                ("suscep_imp", _DP), ("entropy", _DP), ("entropy_chain", _DP), ("entropy_imp", _DP),
+                ("chain_reused", ctypes.c_int), ("chain_ms", ctypes.c_double), ("imp_ms", ctypes.c_double),
+                ("total_ms", ctypes.c_double)]
+
+
+# Thermodynamics file stems of CNRGCodeHandler::ModelSwitch
+# (CodeHandler_ModelSwitch.cpp:202-216, 810-822, 585-593; z = 1 gives "_zEQ1").
+# NRG_main has no two-channel Anderson model; its impurity stem follows the
+# one-channel Anderson pattern.
+THERMO_STEMS = {
+    "1chQS": ("Imp1ChQS_Anderson", "Chain1Ch_QS"),
+    "1chQSz": ("Imp1ChQSz", "Chain1Ch_QSz"),
+    "2chQS": ("Imp2ChQS_Anderson", "Chain2Ch_QS"),
+}
+
+
+def write_thermo(path: str, temp, value, chain=None) -> None:
+    """One file in the layout of CNRGthermo::SaveNValue: T value chain value-chain
+    per line (chain=None: a chain file, third column 0).  Needs no device."""
+    L = load_library()
+    t = np.ascontiguousarray(temp, dtype=np.float64)
+    v = np.ascontiguousarray(value, dtype=np.float64)
+    c = None if chain is None else np.ascontiguousarray(chain, dtype=np.float64)
+    if len(v) != len(t) or (c is not None and len(c) != len(t)):
+        raise NRGError(1, "temp, value and chain must have the same length")
+    st = L.nrg_write_thermo(path.encode(), len(t), t.ctypes.data_as(_DP), v.ctypes.data_as(_DP),
+                            None if c is None else c.ctypes.data_as(_DP))
+    if st != 0:
+        raise NRGError(st, f"cannot write {path}")
+
+
+@dataclass
+class ThermoResult:
+    """T chi and S of the impurity sweep, of the free chain, and their
+    difference, at T_M = D_N / betabar_nc (value k = 4 N + nc - 1)."""
+    temp: np.ndarray
+    suscep: np.ndarray
+    suscep_chain: np.ndarray
+    suscep_imp: np.ndarray
+    entropy: np.ndarray
+    entropy_chain: np.ndarray
+    entropy_imp: np.ndarray
+    chain_reused: bool
+    chain_ms: float
+    imp_ms: float
+    total_ms: float
+    model: str = "1chQS"
+
+    def save(self, directory: str, z: str = "1") -> list:
+        """The reference's four files (SuscepImp*, EntropyImp*, SuscepChain*,
+        EntropyChain*) in `directory`; returns their paths."""
+        imp, chain = THERMO_STEMS[self.model]
+        out = []
+        for kind, val, ch in (("Suscep", self.suscep, self.suscep_chain),
+                              ("Entropy", self.entropy, self.entropy_chain)):
+            p_imp = os.path.join(directory, f"{kind}{imp}_zEQ{z}.dat")
+            p_ch = os.path.join(directory, f"{kind}{chain}_zEQ{z}.dat")
+            write_thermo(p_imp, self.temp, val, ch)
+            write_thermo(p_ch, self.temp, ch, None)
+            out += [p_imp, p_ch]
+        return out
+
+
 def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     """Load the engine library; raise if it is not built (no fallback)."""
     global _lib
@@ -201,6 +266,10 @@ def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     L.nrg_write_dm_shell.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(DmShell)]
     L.nrg_write_code_pars.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_int, ctypes.c_char_p]
     L.nrg_dm_save_bin.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]
+    L.nrg_sweep_run_chain.argtypes = [ctypes.c_void_p, ctypes.POINTER(SweepConfig)]
+    L.nrg_thermo_run.argtypes = [ctypes.c_void_p, ctypes.POINTER(SweepConfig), ctypes.c_int,
+                                 ctypes.POINTER(_Thermo)]
+    L.nrg_write_thermo.argtypes = [ctypes.c_char_p, ctypes.c_int, _dp, _dp, _dp]
     L.nrg_sweep_batch.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(SweepConfig), ctypes.c_int,
                                   ctypes.c_int, _dp, _dp, _ip, _dp]
     _lib = L
@@ -410,12 +479,45 @@ class Engine:
         self._check(self.L.nrg_fp64_peak(self.h, ctypes.byref(v)))
         return v.value
 
+    def sweep_chain(self, model: str, nsites: int, ncutoff: int, lam: float, degen_eps: float = 0.0,
+                    precision: int = PREC_FP64, fetch: bool = True) -> SweepResult:
+        """The free Wilson chain (calcdens = 3): iteration 0 is the first site
+        alone, iterations 1 .. nsites-1 add one site each."""
+        cfg = SweepConfig(MODELS[model], nsites, ncutoff, lam, 0.0, 0.0, 0.0, 0.0, degen_eps, precision)
+        self._check(self.L.nrg_sweep_run_chain(self.h, ctypes.byref(cfg)))
+        return self._fetch(fetch)
+
+    def thermo(self, model: str, nsites: int, ncutoff: int, lam: float, U: float, ed: float,
+               gamma1: float, gamma2_or_B: float = 0.0, degen_eps: float = 0.0,
+               precision: int = PREC_FP64, reuse_chain: bool = True) -> ThermoResult:
+        """Impurity T chi and S with the free chain subtracted (calcdens = 3
+        then 2): the chain sweep runs beside the impurity sweep on a second
+        stream, or is reused from the last call with the same chain
+        parameters.  The impurity sweep stays readable through fetch()."""
+        cfg = SweepConfig(MODELS[model], nsites, ncutoff, lam, U, ed, gamma1, gamma2_or_B,
+                          degen_eps, precision)
+        t = _Thermo()
+        self._check(self.L.nrg_thermo_run(self.h, ctypes.byref(cfg), 1 if reuse_chain else 0, ctypes.byref(t)))
+        n = t.nvalues
+        return ThermoResult(_arr(t.temp, n, np.float64), _arr(t.suscep, n, np.float64),
+                            _arr(t.suscep_chain, n, np.float64), _arr(t.suscep_imp, n, np.float64),
+                            _arr(t.entropy, n, np.float64), _arr(t.entropy_chain, n, np.float64),
+                            _arr(t.entropy_imp, n, np.float64), bool(t.chain_reused), t.chain_ms,
+                            t.imp_ms, t.total_ms, model)
+
     def sweep(self, model: str, nsites: int, ncutoff: int, lam: float, U: float, ed: float,
               gamma1: float, gamma2_or_B: float = 0.0, degen_eps: float = 0.0,
               precision: int = PREC_FP64, fetch: bool = True) -> SweepResult:
         cfg = SweepConfig(MODELS[model], nsites, ncutoff, lam, U, ed, gamma1, gamma2_or_B,
                           degen_eps, precision)
         self._check(self.L.nrg_sweep_run(self.h, ctypes.byref(cfg)))
+        return self._fetch(fetch)
+
+    def fetch(self) -> SweepResult:
+        """The iterations of the last sweep on this context."""
+        return self._fetch(True)
+
+    def _fetch(self, fetch: bool) -> SweepResult:
         out = SweepResult()
         tm = Timing()
         self._check(self.L.nrg_sweep_timing(self.h, ctypes.byref(tm)))

@@ -144,6 +144,17 @@ struct nrg_ctx {
   bool dm_rho_valid = false;
   double dm_temp = 0.0;                // temperature the density matrices were built for
   std::vector<double> dm_hm1_en;       // H_{-1} energies (what shell 0's basis came from)
+  // thermodynamics with the free-chain subtraction (nrg_thermo_run): the
+  // chain sweep runs on a second context beside the impurity sweep, and its
+  // values are kept for later calls with the same chain parameters (the
+  // reference keeps them in its chain files)
+  nrg_ctx* chain_ctx = nullptr;
+  bool chain_valid = false;
+  nrg_sweep_config chain_cfg{};
+  std::vector<double> chain_thermo;    // 16 per iteration, as nrg_iteration.thermo
+  std::vector<double> th_temp, th_sus, th_sus_chain, th_sus_imp, th_ent, th_ent_chain, th_ent_imp;
+  double th_chain_ms = 0.0, th_imp_ms = 0.0, th_total_ms = 0.0;
+  int th_chain_reused = 0;
 };
 
 namespace nrg {
@@ -268,6 +279,15 @@ int grid_split(int nbig) {
   return std::min(k, nbig);
 }
 
+// Cooperative grids of different contexts (the chain sweep beside the
+// impurity sweep, batch workers) never run at the same time: the grids of one
+// context together ask for one CTA per SM, and two contexts' grids, each
+// partly resident and waiting at grid.sync for the rest, could wait on each
+// other.  A context holds this lock from the launch of its grids until they
+// have finished; the launches of other contexts' non-cooperative kernels are
+// not held up.
+std::mutex g_coop_mu;
+
 // `order`: all blocks, largest first (host copy `order_h`); the big blocks
 // form its prefix.
 void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::vector<int>& order_h,
@@ -298,6 +318,12 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
     c->gbig.ensure(pk.host.size() + 256);
     h2d(c, c->gbig.p, pk.host.data(), pk.host.size());
   }
+  std::unique_lock<std::mutex> coop(g_coop_mu, std::defer_lock);
+  if (K >= 1) {
+    coop.lock();
+    for (int k = 0; k < K; ++k)
+      if (!c->join[k]) CU(cudaEventCreateWithFlags(&c->join[k], cudaEventDisableTiming));
+  }
   cudaEvent_t t0 = tm.start();
   if (K == 1) {
     const int G = tridiag_grid_size(ta.maxn);
@@ -307,6 +333,7 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
     double* pvec = part + (size_t)G * ta.maxn;
     double* dots = pvec + ta.maxn;
     CU(launch_tridiag_grid(ta, d_order, nbig, part, pvec, dots, G, c->stream));
+    CU(cudaEventRecord(c->join[0], c->stream));
     c->launches++; c->timing.tridiag_launches++;
   } else if (K > 1) {
     const int G = tridiag_grid_size(ta.maxn);
@@ -316,7 +343,6 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
     CU(cudaEventRecord(c->fork, c->stream));
     for (int k = 0; k < K; ++k) {
       if (!c->aux[k]) CU(cudaStreamCreateWithFlags(&c->aux[k], cudaStreamNonBlocking));
-      if (!c->join[k]) CU(cudaEventCreateWithFlags(&c->join[k], cudaEventDisableTiming));
       c->gpart_k[k].ensure(sizeof(double) * ((size_t)Gk * ta.maxn + ta.maxn + Gk + 64));
       double* part = c->gpart_k[k].as<double>();
       double* pvec = part + (size_t)Gk * ta.maxn;
@@ -343,6 +369,10 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
     c->launches++; c->timing.tridiag_launches++;
   }
   for (int k = 0; K > 1 && k < K; ++k) CU(cudaStreamWaitEvent(c->stream, c->join[k], 0));
+  if (coop.owns_lock()) {
+    for (int k = 0; k < K; ++k) CU(cudaEventSynchronize(c->join[k]));
+    coop.unlock();
+  }
   tm.stop(t0, &c->timing.tridiag_ms);
   double fl = 0.0;
   for (int n : P.bsize) fl += 4.0 / 3.0 * (double)n * n * n;
@@ -448,6 +478,33 @@ double opavg_host(const BlockArray& a, const std::vector<double>& en, const std:
   }
   if (!(std::fabs(Z) < 1.e-20)) s = s / Z;
   return s;
+}
+
+// CalcSuscep / CalcEntropy (CalcThermo.cpp:16-121) at the four betabar_nc of
+// CNRGCodeHandler::CalcThermo (NRGcodehandlerClass.cpp:627-677) for a small
+// host array (the free-chain H_0): (betabar_nc, D/betabar_nc, T chi, S) x 4,
+// the layout the thermo kernel's results are reported in.
+std::vector<double> thermo_host(const BlockArray& a, const std::vector<double>& en, bool totalS, double lambda,
+                                double DN, double betabar) {
+  std::vector<double> out;
+  for (int nc = 1; nc <= 4; ++nc) {
+    const double beta = betabar * std::pow(lambda, (nc - 4) / (2.0 * 4));
+    double Z = 0, s1 = 0, sE = 0;
+    for (int b = 0; b < a.nblocks(); ++b) {
+      const double S = a.q(b, 1);
+      const double deg = totalS ? 2.0 * S + 1.0 : 1.0;
+      const double szsq = totalS ? (1.0 / 12.0) * deg * (deg * deg - 1.0) : S * S;
+      for (int i = a.offset[b]; i < a.offset[b] + a.size[b]; ++i) {
+        const double w = std::exp(-beta * en[i]);
+        Z += deg * w; s1 += szsq * w; sE += deg * en[i] * w;
+      }
+    }
+    out.push_back(beta);
+    out.push_back(DN / beta);
+    out.push_back(s1 / Z);
+    out.push_back(beta * (sE / Z) + std::log(Z));
+  }
+  return out;
 }
 
 // Device tables of one DiagHN assembly, uploaded to c->meta.
@@ -672,7 +729,13 @@ void launch_update_plan(nrg_ctx* c, Timer& tm, UpdatePlan& U) {
 // the operators are f_N and c_d, they are rotated into the full (uncut)
 // eigenbasis of every shell, and each shell's eigen-array, eigenvectors and
 // c_d stay on the device for the DM-NRG backward sweep.
-void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false) {
+//
+// chain: the free Wilson chain of calcdens = 3 (NRGcodehandlerClass.cpp:85-91
+// switches to ModelNo 3; CodeHandler_ModelSwitch.cpp:377-420, 667-720,
+// 940-1000): H_0 is the first site alone (Nsites0 = 1), its thermodynamics
+// are taken before the loop at D_0 (NRG_main.cpp:242-255), and iteration N =
+// 1 .. nsites-1 adds site N with hopping chi_{N-1}.  Only f_N is carried.
+void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool chain = false) {
   using clock = std::chrono::steady_clock;
   auto t_begin = clock::now();
   if (cfg->model < 0 || cfg->model > 2) throw NrgError(NRG_ERR_ARG, "unknown model");
@@ -688,6 +751,10 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false) {
   S.c = c;
   S.m = make_model((ModelKind)cfg->model);
   S.cfg = *cfg;
+  if (chain) {
+    const int nf = S.m.kind == MODEL_1CHQS ? 1 : 2;
+    S.m.op_kind.resize(nf); S.m.op_check.resize(nf); S.m.op_name.resize(nf); S.m.op_avg.resize(nf);
+  }
   if (dm) {
     S.m.op_kind = {OP_F_QS, OP_CD_QS};
     S.m.op_check = {CHK_QS_CD, CHK_QS_CD};
@@ -717,7 +784,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false) {
   c->opptr.ensure(sizeof(double*) * 32);
 
   // H_{-1} (the initial CutStates keeps everything: Ncutoff >= 4 states).
-  StartState st = make_start(m, lambda, cfg->U, cfg->ed, cfg->gamma2_or_B);
+  StartState st = chain ? make_chain_start(m, lambda) : make_start(m, lambda, cfg->U, cfg->ed, cfg->gamma2_or_B);
   if (dm) {
     st.ops = {st.ops[0], st.ops[0]};  // c_d at H_{-1} is a copy of f (Main_SetH0.cpp:1958-1961)
     c->dm_hm1_en = st.en;
@@ -745,8 +812,23 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false) {
   double chi[2] = {chi_m1(lambda, cfg->gamma1), 0.0};
   if (m.nchan == 2) chi[1] = chi_m1(lambda, cfg->gamma2_or_B);
   const double eN = 0.0;  // flat band (CNRGchain::GetEn of SetChainWilson)
+  int N0 = 0;
+  if (chain) {
+    // chi_m1 = chiN(0) for every channel; H_0 is recorded as iteration 0 with
+    // the thermodynamics CalcThermo takes before the loop, at
+    // D = HLF Lambda^(-(Nsites0-2)/2) = D_0.
+    chi[0] = chin(lambda, 0);
+    chi[1] = m.nchan == 2 ? chin(lambda, 0) : 0.0;
+    IterResult R;
+    R.params = {lambda, chi[0], chi[1], eN};
+    R.qn = st.blk.qn; R.bsize = st.blk.size; R.kept_bsize = st.blk.size;
+    R.en = st.en; R.nkept = st.blk.nstates();
+    R.thermo = thermo_host(st.blk, st.en, m.totalS, lambda, HLF * std::pow(lambda, 0.5), betabar);
+    c->iters.push_back(std::move(R));
+    N0 = 1;
+  }
 
-  for (int N = 0; N < cfg->nsites; ++N) {
+  for (int N = N0; N < cfg->nsites; ++N) {
     IterResult R;
     R.params = {lambda, chi[0], chi[1], eN};
     const double DN = HLF * std::pow(lambda, (-(N - 1) / 2.0));
@@ -1326,6 +1408,85 @@ void dm_save_bin_impl(nrg_ctx* c, const char* dir, const char* name) {
 
 // DiagBlock for a batch of blocks given in the reference's packed upper
 // storage: same device pipeline as the sweep, all eigenvectors kept.
+// ------------------------------------------------------------ thermodynamics
+// calcdens = 3 then 2 (NRGthermoClass.cpp:10-150, NRGcodehandlerClass.cpp:
+// 627-677): the free chain's T chi and S at the same temperatures T_M = D_N /
+// betabar_nc as the impurity sweep, and the impurity contribution as the
+// difference.  Value k (= 4 N + nc - 1) of the impurity sweep is paired with
+// value k of the chain, which is what CNRGthermo::ReadNChainValue does with
+// line k of the chain file.  The chain's own CNRGthermo::dImpValue is never
+// set by ModelSwitch for ModelNo 3 and reads as 0 there; it is 0 here.
+bool same_chain(const nrg_sweep_config& a, const nrg_sweep_config& b) {
+  return a.model == b.model && a.nsites == b.nsites && a.ncutoff == b.ncutoff && a.lambda == b.lambda &&
+         a.degen_eps == b.degen_eps && a.precision == b.precision;
+}
+
+void thermo_run_impl(nrg_ctx* c, const nrg_sweep_config* cfg, int reuse_chain) {
+  using clock = std::chrono::steady_clock;
+  const auto t0 = clock::now();
+  const bool reuse = reuse_chain != 0 && c->chain_valid && same_chain(c->chain_cfg, *cfg);
+  double chain_ms = 0.0, imp_ms = 0.0;
+  if (!reuse) {
+    c->chain_valid = false;
+    if (!c->chain_ctx) {
+      const nrg_status st = nrg_create(c->device, &c->chain_ctx);
+      if (st != NRG_OK) throw NrgError(st, "cannot create the free-chain context");
+    }
+    nrg_ctx* cc = c->chain_ctx;
+    nrg_status cst = NRG_OK;
+    std::string cerr;
+    // The chain sweep on its own stream and host thread: the two sweeps'
+    // launches overlap on the device.
+    std::thread th([&]() {
+      const auto a = clock::now();
+      try {
+        CU(cudaSetDevice(cc->device));
+        sweep_run(cc, cfg, false, true);
+      } catch (const NrgError& e) {
+        cst = e.st; cerr = e.what();
+      } catch (const std::exception& e) {
+        cst = NRG_ERR_ARG; cerr = e.what();
+      }
+      chain_ms = std::chrono::duration<double, std::milli>(clock::now() - a).count();
+    });
+    try {
+      const auto a = clock::now();
+      sweep_run(c, cfg);
+      imp_ms = std::chrono::duration<double, std::milli>(clock::now() - a).count();
+    } catch (...) {
+      th.join();
+      throw;
+    }
+    th.join();
+    if (cst != NRG_OK) throw NrgError(cst, "free-chain sweep: " + cerr);
+    c->chain_thermo.clear();
+    for (const IterResult& R : cc->iters) c->chain_thermo.insert(c->chain_thermo.end(), R.thermo.begin(), R.thermo.end());
+    c->chain_cfg = *cfg;
+    c->chain_valid = true;
+  } else {
+    const auto a = clock::now();
+    sweep_run(c, cfg);
+    imp_ms = std::chrono::duration<double, std::milli>(clock::now() - a).count();
+  }
+  const int nv = 4 * (int)c->iters.size();
+  if ((int)c->chain_thermo.size() != 4 * nv) throw NrgError(NRG_ERR_SYNC, "chain and impurity sweeps differ in length");
+  for (auto* v : {&c->th_temp, &c->th_sus, &c->th_sus_chain, &c->th_sus_imp, &c->th_ent, &c->th_ent_chain,
+                  &c->th_ent_imp})
+    v->assign(nv, 0.0);
+  for (int k = 0; k < nv; ++k) {
+    const double* imp = c->iters[k / 4].thermo.data() + 4 * (k % 4);
+    const double* ch = c->chain_thermo.data() + 4 * k;
+    if (imp[1] != ch[1]) throw NrgError(NRG_ERR_SYNC, "chain and impurity temperatures differ");
+    c->th_temp[k] = imp[1];
+    c->th_sus[k] = imp[2]; c->th_sus_chain[k] = ch[2]; c->th_sus_imp[k] = imp[2] - ch[2];
+    c->th_ent[k] = imp[3]; c->th_ent_chain[k] = ch[3]; c->th_ent_imp[k] = imp[3] - ch[3];
+  }
+  c->th_chain_reused = reuse ? 1 : 0;
+  c->th_chain_ms = chain_ms;
+  c->th_imp_ms = imp_ms;
+  c->th_total_ms = std::chrono::duration<double, std::milli>(clock::now() - t0).count();
+}
+
 void diag_blocks_impl(nrg_ctx* c, int nb, const int* sizes, const double* packed, double* evals, double* evecs) {
   if (nb <= 0 || !sizes || !packed || !evals || !evecs) throw NrgError(NRG_ERR_ARG, "bad arguments");
   std::vector<int> bs(sizes, sizes + nb);
@@ -1792,7 +1953,9 @@ void nrg_destroy(nrg_ctx* ctx) {
   }
   if (ctx->fork) cudaEventDestroy(ctx->fork);
   cudaStreamDestroy(ctx->stream);
+  nrg_ctx* chain = ctx->chain_ctx;
   delete ctx;
+  nrg_destroy(chain);
 }
 
 const char* nrg_last_error(const nrg_ctx* ctx) {
@@ -1900,6 +2063,38 @@ nrg_status nrg_sweep_run_dm(nrg_ctx* ctx, const nrg_sweep_config* cfg) {
     CU(cudaSetDevice(ctx->device));
     sweep_run(ctx, cfg, true);
   });
+  return NRG_OK;
+}
+
+nrg_status nrg_sweep_run_chain(nrg_ctx* ctx, const nrg_sweep_config* cfg) {
+  if (!ctx || !cfg) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    sweep_run(ctx, cfg, false, true);
+  });
+  return NRG_OK;
+}
+
+nrg_status nrg_thermo_run(nrg_ctx* ctx, const nrg_sweep_config* cfg, int reuse_chain, nrg_thermo* out) {
+  if (!ctx || !cfg || !out) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    thermo_run_impl(ctx, cfg, reuse_chain);
+  });
+  out->nvalues = (int)ctx->th_temp.size();
+  out->temp = ctx->th_temp.data();
+  out->suscep = ctx->th_sus.data();
+  out->suscep_chain = ctx->th_sus_chain.data();
+  out->suscep_imp = ctx->th_sus_imp.data();
+  out->entropy = ctx->th_ent.data();
+  out->entropy_chain = ctx->th_ent_chain.data();
+  out->entropy_imp = ctx->th_ent_imp.data();
+  out->chain_reused = ctx->th_chain_reused;
+  out->chain_ms = ctx->th_chain_ms;
+  out->imp_ms = ctx->th_imp_ms;
+  out->total_ms = ctx->th_total_ms;
   return NRG_OK;
 }
 

@@ -230,6 +230,44 @@ StartState make_start(const ModelSpec& m, double lambda, double U, double ed, do
   return s;
 }
 
+StartState make_chain_start(const ModelSpec& m, double lambda) {
+  const int nf = m.kind == MODEL_1CHQS ? 1 : 2;  // f_N operators entering H_N
+  if (m.kind != MODEL_2CHQS) {
+    // OneChQS_SetChainH0 / OneChQSz_SetChainH0 (Main/Main_SetH0.cpp:3322-3465):
+    // the site multiplets at zero energy carry the same blocks and reduced f
+    // elements as the impurity start with U = ed = B = 0.
+    StartState s = make_start(m, lambda, 0.0, 0.0, 0.0);
+    s.ops.resize(nf);
+    return s;
+  }
+  // TwoChQS_SetH0Chain (Main/Main_SetH0.cpp:3472-3560): the two-channel site
+  // in its multiplet basis -- the highest-weight state (Sz = S) of every site
+  // block, blocks in order of first appearance, all from one "old" state --
+  // and f_ch = SetMatrix over that basis with the rule UpdateMatrices uses.
+  BlockArray vac;
+  vac.nqn = 2;
+  const double q0[2] = {0.0, 0.0};
+  vac.push(q0, 1);
+  Basis B;
+  build_basis(m, vac, B);
+  StartState s;
+  s.blk = B.blk;
+  s.en.assign(B.blk.nstates(), 0.0);
+  for (int o = 0; o < nf; ++o) {
+    OpBlocks f;
+    for (int i = 0; i < B.blk.nblocks(); ++i)
+      for (int j = 0; j < B.blk.nblocks(); ++j) {
+        if (!op_check(m.op_check[o], B.blk, i, j)) continue;
+        f.bi.push_back(i); f.bj.push_back(j); f.off.push_back((int64_t)f.el.size());
+        for (int a = B.blk.offset[i]; a < B.blk.offset[i] + B.blk.size[i]; ++a)
+          for (int b = B.blk.offset[j]; b < B.blk.offset[j] + B.blk.size[j]; ++b)
+            f.el.push_back(op_site_factor(m, m.op_kind[o], B.blk.q(i, 1), B.blk.q(j, 1), B.itype[a], B.itype[b]));
+      }
+    s.ops.push_back(f);
+  }
+  return s;
+}
+
 void build_basis(const ModelSpec& m, const BlockArray& kept, Basis& out) {
   // BuildBasis (BuildBasis.cpp:8-432) with CommonQNs = {2, 0,1, 0,1} and,
   // for SU(2) models, totSpos = {1}.

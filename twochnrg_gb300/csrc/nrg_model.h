@@ -99,6 +99,10 @@ struct StartState {
   std::vector<OpBlocks> ops;
 };
 StartState make_start(const ModelSpec& m, double lambda, double U, double ed, double B);
+// Free-chain start-up (calcdens = 3, CodeHandler_ModelSwitch.cpp:377-420,
+// 667-720, 940-1000): the first Wilson site alone at zero energy (flat band,
+// e_0 = 0) with only the channel operators f_N that enter H_N.
+StartState make_chain_start(const ModelSpec& m, double lambda);
 
 // BuildBasis (BuildBasis.cpp:8-432) from a kept array.
 void build_basis(const ModelSpec& m, const BlockArray& kept, Basis& out);
