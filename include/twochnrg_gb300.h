@@ -52,7 +52,12 @@ typedef enum {
 typedef enum {
   NRG_MODEL_1CH_QS = 0,  /* one-channel Anderson, |Q S> basis   (SymNo 0, ModelNo 0) */
   NRG_MODEL_1CH_QSZ = 1, /* one-channel Anderson, |Q Sz> basis  (SymNo 2, ModelNo 0) */
-  NRG_MODEL_2CH_QS = 2   /* two-channel Anderson, |Q S> basis   (SymNo 1)            */
+  NRG_MODEL_2CH_QS = 2,  /* two-channel Anderson, |Q S> basis   (SymNo 1)            */
+  NRG_MODEL_1CH_Q = 3    /* one-channel Anderson, |Q> basis     (SymNo 3, ModelNo 0);
+                            whole sweeps only.  Blocks are reported as (Q, 0); the
+                            averaged operators are S_z and S_z^2; the reference takes
+                            only the entropy for this symmetry, and the T chi slot of
+                            nrg_iteration.thermo is 0 */
 } nrg_model;
 
 /* Arithmetic of the dense steps. */

@@ -246,6 +246,13 @@ Basis site_1chQSz() {
   for (int i = 0; i < 4; ++i) s.itype.push_back(i);
   return s;
 }
+// CNRGCodeHandler::SetSingleSite for SymNo 3 (NRGcodehandlerClass.cpp:484-503).
+Basis site_1chQ() {
+  Basis s; s.nqn = 1; s.totalS = false;
+  add_site_block(s, {-1}, 0, 0); add_site_block(s, {0}, 1, 2); add_site_block(s, {1}, 3, 3);
+  for (int i = 0; i < 4; ++i) s.itype.push_back(i);
+  return s;
+}
 // TwoChQS_SetSingleSite (TwoChQS_SetSingleSite.cpp:5-124): 16 states in 10 blocks.
 Basis site_2chQS() {
   Basis s; s.nqn = 3; s.totalS = true; s.sqn = {1};
@@ -350,6 +357,29 @@ double hn_1chQSz(Ctx& c, const std::vector<double>& P, const Basis& ab, const st
     double Qt = qn_from_st(ss, ab.itype[ist], 0);
     return v + eN * (Qt + 1.0);
   }
+  int ti = ab.itype[ist], tj = ab.itype[jst];
+  double v = 0.0;
+  int imat = 0;
+  for (int isigma = 1; isigma >= -1; isigma -= 2) {
+    int typep = ti, type = tj;
+    double Old = M[imat].get(ab.stcf[ist], ab.stcf[jst]);
+    if (dEq(Old, 0.0)) { Old = M[imat].get(ab.stcf[jst], ab.stcf[ist]); typep = tj; type = ti; }
+    double Qt = qn_from_st(ss, type, 0);
+    double FermiSign = dEq(Qt, 0.0) ? -1.0 : 1.0;
+    v += FermiSign * Old * onech_fd(isigma, typep, type);
+    imat++;
+  }
+  return v * chi_N;
+}
+
+// OneChQ_HN_MatEl (OpMatRules.cpp:1065-1147): blocks by Q alone, no e_N term.
+double hn_1chQ(Ctx& c, const std::vector<double>& P, const Basis& ab, const std::vector<Mat>& M,
+               int ist, int jst) {
+  const Basis& ss = c.m.site;
+  double Lambda = P[0], chi_N = P[1];
+  double Qi = qn_from_st(ab, ist, 0), Qj = qn_from_st(ab, jst, 0);
+  if (!dEq(Qi, Qj)) return 0.0;
+  if (ist == jst) return std::sqrt(Lambda) * ab.en[ist];
   int ti = ab.itype[ist], tj = ab.itype[jst];
   double v = 0.0;
   int imat = 0;
@@ -625,6 +655,7 @@ double hn_el(Ctx& c, const std::vector<double>& P, const Basis& ab, const std::v
     case ORACLE_MODEL_1CHQS: return hn_1chQS(c, P, ab, M, i, j);
     case ORACLE_MODEL_1CHQSZ: return hn_1chQSz(c, P, ab, M, i, j);
     case ORACLE_MODEL_2CHQS: return hn_2chQS(c, P, ab, M, i, j);
+    case ORACLE_MODEL_1CHQ: return hn_1chQ(c, P, ab, M, i, j);
   }
   return 0.0;
 }
@@ -842,6 +873,7 @@ void update_matrices(Ctx& c, const Basis& acut, const Basis& ab, std::vector<Mat
 // CalcSuscep (CalcThermo.cpp:16-74): returns <Sz^2>/Z (the <Sz>^2 term is
 // multiplied by 0 in the reference).
 double calc_suscep(const Arr& a, double beta, int sq, bool totalS) {
+  if (sq < 0) return 0.0;  // Sqnumber -1 ("no spin whatsoever"): not taken by the reference
   double s0 = 0, s1 = 0, s2 = 0;
   for (int b = 0; b < a.nblocks(); ++b) {
     double Si = a.q(b, sq);
@@ -962,6 +994,30 @@ void h0_chain_2chQS(Ctx& c, Arr& a, Mat& f1, Mat& f2) {
         M.push_block(i, j, v.data(), (int)v.size());
       }
   }
+}
+
+// OneChQ_SetAnderson_Hm1 (Main/Main_SetH0.cpp:217-352): one quantum number,
+// the Q = 0 block holds |up>, |dn>; f_up, f_dn not reduced; S_z and S_z^2
+// from iDegen/10 on the diagonal.
+void hm1_Q(double Lambda, double HLF, double U, double ed, Arr& a, Mat& fu, Mat& fd, std::vector<Mat>& avg) {
+  a = Arr(); a.nqn = 1; a.nshell = -1; a.totalS = false;
+  a.qn = {-1, 0, 1};
+  a.bbe = {0, 0, 1, 2, 3, 3};
+  a.en = {0.5 * U / (Lambda * HLF), (ed + 0.5 * U) / (Lambda * HLF), (ed + 0.5 * U) / (Lambda * HLF),
+          (2.0 * ed + 1.5 * U) / (Lambda * HLF)};
+  a.evec = {1, 1, 0, 0, 1, 1};
+  fu = Mat(); fu.blk = a; fu.blk.evec.clear();
+  fd = Mat(); fd.blk = a; fd.blk.evec.clear();
+  const double u01[2] = {1, 0}, u12[2] = {0, 1}, d01[2] = {0, 1}, d12[2] = {-1, 0};
+  fu.push_block(0, 1, u01, 2); fu.push_block(1, 2, u12, 2);
+  fd.push_block(0, 1, d01, 2); fd.push_block(1, 2, d12, 2);
+  Mat sz, sz2;
+  sz.blk = a; sz.blk.evec.clear(); sz.name = "Sz";
+  sz2.blk = a; sz2.blk.evec.clear(); sz2.name = "Sz2";
+  const double z0[1] = {0}, z1[4] = {0.5, 0, 0, -0.5}, q1[4] = {0.25, 0, 0, 0.25};
+  sz.push_block(0, 0, z0, 1); sz.push_block(1, 1, z1, 4); sz.push_block(2, 2, z0, 1);
+  sz2.push_block(0, 0, z0, 1); sz2.push_block(1, 1, q1, 4); sz2.push_block(2, 2, z0, 1);
+  avg = {sz, sz2};
 }
 
 // ---------------------------------------------------------------- DM-NRG
@@ -1405,6 +1461,16 @@ void* oracle_run(const oracle_config* cfg) {
       c.m.op_rule = {R_FUP_QSZ, R_FDN_QSZ}; c.m.op_check = {C_Q_CD, C_Q_CD};
       P = {Lambda, chi0, 0.0, 0.0};
       totalS = false;
+    } else if (cfg->model == ORACLE_MODEL_1CHQ) {
+      // ModelSwitch has no chain case for OneChQ; the first site alone is the
+      // impurity start at U = ed = 0, as for the other one-channel symmetries.
+      c.m.site = site_1chQ(); c.m.totS = {}; c.m.common = {1, 0, 0};
+      Mat fu, fd; std::vector<Mat> avg;
+      hm1_Q(Lambda, HLF, 0.0, 0.0, eig, fu, fd, avg);
+      mats.push_back(fu); mats.push_back(fd);
+      c.m.op_rule = {R_FUP_QSZ, R_FDN_QSZ}; c.m.op_check = {C_Q_CD, C_Q_CD};
+      P = {Lambda, chi0, 0.0, 0.0};
+      totalS = false; sq = -1;
     } else if (cfg->model == ORACLE_MODEL_2CHQS) {
       c.m.site = site_2chQS(); c.m.totS = {1};
       Mat f1, f2;
@@ -1443,6 +1509,17 @@ void* oracle_run(const oracle_config* cfg) {
     c.m.op_check = {C_Q_CD, C_Q_CD, C_DIAG, C_DIAG};
     P = {Lambda, chi1, 0.0, 0.0};
     totalS = false;
+  } else if (cfg->model == ORACLE_MODEL_1CHQ) {
+    // SymNo 3 (CodeHandler_ModelSwitch.cpp:1138-1200): f_up, f_dn (OneChQ_fN
+    // rules, OneChQ_cd_check), S_z and S_z^2 averaged; CommonQNs = {1, 0, 0}.
+    c.m.site = site_1chQ(); c.m.totS = {}; c.m.common = {1, 0, 0};
+    Mat fu, fd; std::vector<Mat> avg;
+    hm1_Q(Lambda, HLF, cfg->U, cfg->ed, eig, fu, fd, avg);
+    mats.push_back(fu); mats.push_back(fd); for (auto& x : avg) mats.push_back(x);
+    c.m.op_rule = {R_FUP_QSZ, R_FDN_QSZ, R_IMPONLY, R_IMPONLY};
+    c.m.op_check = {C_Q_CD, C_Q_CD, C_DIAG, C_DIAG};
+    P = {Lambda, chi1, 0.0, 0.0};
+    totalS = false; sq = -1;
   } else if (cfg->model == ORACLE_MODEL_2CHQS) {
     c.m.site = site_2chQS(); c.m.totS = {1};
     Mat f; std::vector<Mat> avg;
@@ -1461,7 +1538,7 @@ void* oracle_run(const oracle_config* cfg) {
     else if (c.m.op_rule[i] == R_CD_QS) { mats[i].need_old = true; mats[i].calc_avg = false; }
     else { mats[i].need_old = false; mats[i].calc_avg = false; }
   }
-  R->nqn = 2;
+  R->nqn = cfg->model == ORACLE_MODEL_1CHQ ? 1 : 2;
   for (auto& m : mats) if (m.calc_avg) R->opnames.push_back(m.name);
   const double betabar = 0.727;
   Basis cut, ab;
@@ -1555,6 +1632,7 @@ void* oracle_run(const oracle_config* cfg) {
 void oracle_free(void* h) { delete (OracleRun*)h; }
 
 int oracle_num_iters(void* h) { return (int)((OracleRun*)h)->it.size(); }
+int oracle_nqn(void* h) { return ((OracleRun*)h)->nqn; }
 double oracle_seconds(void* h) { return ((OracleRun*)h)->seconds; }
 int oracle_num_ops(void* h) { return (int)((OracleRun*)h)->opnames.size(); }
 const char* oracle_op_name(void* h, int k) { return ((OracleRun*)h)->opnames[k].c_str(); }

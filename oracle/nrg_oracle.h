@@ -8,6 +8,7 @@ extern "C" {
 #define ORACLE_MODEL_1CHQS 0  /* one-channel Anderson, (Q,S) basis  */
 #define ORACLE_MODEL_1CHQSZ 1 /* one-channel Anderson, (Q,Sz) basis */
 #define ORACLE_MODEL_2CHQS 2  /* two-channel Anderson, (Q,S) basis  */
+#define ORACLE_MODEL_1CHQ 3   /* one-channel Anderson, (Q) basis    */
 
 typedef struct {
   int model;          /* ORACLE_MODEL_* */

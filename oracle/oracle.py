@@ -16,8 +16,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 SO = os.path.join(HERE, "_build", "libnrg_oracle.so")
 
-MODEL_1CHQS, MODEL_1CHQSZ, MODEL_2CHQS = 0, 1, 2
-MODELS = {"1chQS": MODEL_1CHQS, "1chQSz": MODEL_1CHQSZ, "2chQS": MODEL_2CHQS}
+MODEL_1CHQS, MODEL_1CHQSZ, MODEL_2CHQS, MODEL_1CHQ = 0, 1, 2, 3
+MODELS = {"1chQS": MODEL_1CHQS, "1chQSz": MODEL_1CHQSZ, "2chQS": MODEL_2CHQS, "1chQ": MODEL_1CHQ}
 
 
 class _Cfg(ctypes.Structure):
@@ -154,12 +154,13 @@ def run(model: str, nsites: int, ncutoff: int, lam: float, U: float, ed: float, 
         out.opnames = [L.oracle_op_name(h, k).decode() for k in range(nops)]
         out.opavg_m1 = _arr(L.oracle_opavg_m1(h), nops, np.float64)
         out.seconds = L.oracle_seconds(h)
+        nq = L.oracle_nqn(h)
         for n in range(L.oracle_num_iters(h)):
             nb = L.oracle_iter_nblocks(h, n)
             ns = L.oracle_iter_nstates(h, n)
             it = Iteration(
                 params=_arr(L.oracle_iter_params(h, n), L.oracle_iter_nparams(h, n), np.float64),
-                qn=_arr(L.oracle_iter_qn(h, n), 2 * nb, np.float64).reshape(nb, 2),
+                qn=_arr(L.oracle_iter_qn(h, n), nq * nb, np.float64).reshape(nb, nq),
                 bsize=_arr(L.oracle_iter_bsize(h, n), nb, np.int64),
                 en=_arr(L.oracle_iter_en(h, n), ns, np.float64),
                 emin=L.oracle_iter_emin(h, n), ecut=L.oracle_iter_ecut(h, n),

@@ -10,6 +10,7 @@
 //   ref_harness <model> <Nsites> <Ncutoff> <Lambda> <U> <ed> <Gamma1> <Gamma2|B>
 //   model: 1chQS   one-channel Anderson, (Q,S) basis   (ModelSwitch SymNo 0 / ModelNo 0)
 //          1chQSz  one-channel Anderson, (Q,Sz) basis  (SymNo 2 / ModelNo 0); last arg = B
+//          1chQ    one-channel Anderson, (Q) basis     (SymNo 3 / ModelNo 0)
 //          2chQS   two-channel Anderson, (Q,S) basis: the impurity H_{-1} of
 //                  OneChQS_SetAnderson_Hm1 coupled to both channels through
 //                  TwoChQS_HN_MatEl with f_ch1 = f_ch2 = d; last arg = Gamma2
@@ -124,6 +125,29 @@ int main(int argc, char** argv) {
     double chi_m1 = sqrt(2.0 * Gamma1 / pi) / (sqrt(Lambda) * HalfLambdaFactor) * ALambda;
     ParamsHN = {Lambda, chi_m1, 0.0, 0.0};
     totalS = false;
+  } else if (model == "1chQ") {
+    // CNRGCodeHandler::SetSingleSite, SymNo 3 (NRGcodehandlerClass.cpp:484-503)
+    SingleSite.NQNumbers = 1;
+    SingleSite.Nshell = 0;
+    SingleSite.QNumbers = {-1.0, 0.0, 1.0};
+    SingleSite.BlockBegEnd = {0, 0, 1, 2, 3, 3};
+    for (int ii = 0; ii < 4; ++ii) SingleSite.iType.push_back(ii);
+    // ModelSwitch SymNo 3, ModelNo 0 (CodeHandler_ModelSwitch.cpp:1138-1200)
+    for (int i = 0; i < 4; ++i) Mats.push_back(aux);
+    Mats[0].NeedOld = false; Mats[0].CheckForMatEl = OneChQ_cd_check; Mats[0].CalcMatEl = OneChQ_fNup_MatEl;
+    Mats[1].NeedOld = false; Mats[1].CheckForMatEl = OneChQ_cd_check; Mats[1].CalcMatEl = OneChQ_fNdn_MatEl;
+    CNRGmatrix avg; avg.NeedOld = true; avg.UpperTriangular = false; avg.CalcAvg = true;
+    avg.CheckForMatEl = Diag_check; avg.CalcMatEl = ImpOnly_MatEl;
+    Mats[2] = avg; Mats[3] = avg;
+    strcpy(Mats[2].MatName, "Sz"); strcpy(Mats[3].MatName, "Sz2");
+    std::vector<double> P = {U, ed, Lambda, HalfLambdaFactor};
+    OneChQ_SetAnderson_Hm1(P, &Aeig, Mats);
+    CommonQNs = {1, 0, 0}; totSpos.clear();
+    HN.CalcHNMatEl = OneChQ_HN_MatEl;
+    double chi_m1 = sqrt(2.0 * Gamma1 / pi) / (sqrt(Lambda) * HalfLambdaFactor) * ALambda;
+    ParamsHN = {Lambda, chi_m1, 0.0, 0.0};
+    totalS = false;
+    sqnumber = -1;  // NRGcodehandlerClass.cpp:762-765
   } else if (model == "2chQS") {
     TwoChQS_SetSingleSite(&SingleSite);
     // Impurity H_{-1} and its reduced <||d||> from the one-channel set-up.

@@ -36,6 +36,8 @@ CASES = {
     # Two-channel Anderson at the headline parameters, reduced kept count.
     "cfg1_2chQS_n8_k300": ("2chQS", 8, 300, 2.5, 0.3, -0.15, 0.01, 0.01),
     "small_2chQS_n5_k60": ("2chQS", 5, 60, 2.5, 0.3, -0.15, 0.01, 0.01),
+    # One-channel Anderson in the charge-only |Q> basis (SymNo 3).
+    "q_1chQ_n12_k200": ("1chQ", 12, 200, 2.5, 0.5, -0.25, 0.02, 0.0),
 }
 
 

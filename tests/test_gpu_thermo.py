@@ -89,3 +89,17 @@ def test_gpu_thermo_files(engine, tmp_path):
     for stem, key in (("SuscepImp1ChQS_Anderson", "imp_suscep"), ("EntropyImp1ChQS_Anderson", "imp_entropy"),
                       ("SuscepChain1Ch_QS", "chain_suscep"), ("EntropyChain1Ch_QS", "chain_entropy")):
         _close(np.loadtxt(str(tmp_path / f"{stem}_zEQ1.dat")), g[key])
+
+
+def test_charge_only_symmetry_entropy(engine, tmp_path):
+    """|Q> basis: entropy only (the reference's Sqnumber -1 takes no T chi).
+    ModelSwitch has no free-chain case for this symmetry; its chain is the
+    same physical chain as the |Q Sz> one, so the entropies agree."""
+    r = engine.thermo("1chQ", 10, 150, 2.5, 0.5, -0.25, 0.02)
+    assert not r.suscep.any() and not r.suscep_chain.any()
+    z = np.array([i.thermo for i in engine.sweep_chain("1chQSz", 10, 150, 2.5).iters]).reshape(-1, 4)
+    _close(r.entropy_chain, z[:, 3])
+    o = np.array([i.thermo for i in orc.run("1chQ", 10, 150, 2.5, 0.5, -0.25, 0.02).iters]).reshape(-1, 4)
+    _close(r.entropy, o[:, 3])
+    names = sorted(os.path.basename(p) for p in r.save(str(tmp_path)))
+    assert names == ["EntropyChain1Ch_Q.dat", "EntropyImp1Ch_Anderson_Q.dat"]

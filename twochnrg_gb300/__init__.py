@@ -19,8 +19,8 @@ from . import build as _build
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = _build.LIB
 
-MODEL_1CH_QS, MODEL_1CH_QSZ, MODEL_2CH_QS = 0, 1, 2
-MODELS = {"1chQS": MODEL_1CH_QS, "1chQSz": MODEL_1CH_QSZ, "2chQS": MODEL_2CH_QS}
+MODEL_1CH_QS, MODEL_1CH_QSZ, MODEL_2CH_QS, MODEL_1CH_Q = 0, 1, 2, 3
+MODELS = {"1chQS": MODEL_1CH_QS, "1chQSz": MODEL_1CH_QSZ, "2chQS": MODEL_2CH_QS, "1chQ": MODEL_1CH_Q}
 PREC_FP64 = 0
 
 STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "out of memory", 4: "not converged",
@@ -167,14 +167,20 @@ class _Thermo(ctypes.Structure):
                 ("total_ms", ctypes.c_double)]
 
 
-# Thermodynamics file stems of CNRGCodeHandler::ModelSwitch
-# (CodeHandler_ModelSwitch.cpp:202-216, 810-822, 585-593; z = 1 gives "_zEQ1").
-# NRG_main has no two-channel Anderson model; its impurity stem follows the
-# one-channel Anderson pattern.
-THERMO_STEMS = {
-    "1chQS": ("Imp1ChQS_Anderson", "Chain1Ch_QS"),
-    "1chQSz": ("Imp1ChQSz", "Chain1Ch_QSz"),
-    "2chQS": ("Imp2ChQS_Anderson", "Chain2Ch_QS"),
+# Thermodynamics files of CNRGCodeHandler::ModelSwitch
+# (CodeHandler_ModelSwitch.cpp:202-216, 810-822, 585-593, 1187-1188), as
+# {quantity: (impurity file, chain file)}; "{z}" becomes the z-string ("_zEQ1"
+# for z = 1).  NRG_main has no two-channel Anderson model; its impurity file
+# follows the one-channel Anderson pattern.  The |Q> symmetry has the entropy
+# only, without a z-string.
+THERMO_FILES = {
+    "1chQS": {"Suscep": ("SuscepImp1ChQS_Anderson{z}.dat", "SuscepChain1Ch_QS{z}.dat"),
+              "Entropy": ("EntropyImp1ChQS_Anderson{z}.dat", "EntropyChain1Ch_QS{z}.dat")},
+    "1chQSz": {"Suscep": ("SuscepImp1ChQSz{z}.dat", "SuscepChain1Ch_QSz{z}.dat"),
+               "Entropy": ("EntropyImp1ChQSz{z}.dat", "EntropyChain1Ch_QSz{z}.dat")},
+    "2chQS": {"Suscep": ("SuscepImp2ChQS_Anderson{z}.dat", "SuscepChain2Ch_QS{z}.dat"),
+              "Entropy": ("EntropyImp2ChQS_Anderson{z}.dat", "EntropyChain2Ch_QS{z}.dat")},
+    "1chQ": {"Entropy": ("EntropyImp1Ch_Anderson_Q.dat", "EntropyChain1Ch_Q.dat")},
 }
 
 
@@ -211,14 +217,15 @@ class ThermoResult:
     model: str = "1chQS"
 
     def save(self, directory: str, z: str = "1") -> list:
-        """The reference's four files (SuscepImp*, EntropyImp*, SuscepChain*,
+        """The reference's files (SuscepImp*, EntropyImp*, SuscepChain*,
         EntropyChain*) in `directory`; returns their paths."""
-        imp, chain = THERMO_STEMS[self.model]
         out = []
         for kind, val, ch in (("Suscep", self.suscep, self.suscep_chain),
                               ("Entropy", self.entropy, self.entropy_chain)):
-            p_imp = os.path.join(directory, f"{kind}{imp}_zEQ{z}.dat")
-            p_ch = os.path.join(directory, f"{kind}{chain}_zEQ{z}.dat")
+            names = THERMO_FILES[self.model].get(kind)
+            if names is None:
+                continue
+            p_imp, p_ch = (os.path.join(directory, n.format(z="_zEQ" + z)) for n in names)
             write_thermo(p_imp, self.temp, val, ch)
             write_thermo(p_ch, self.temp, ch, None)
             out += [p_imp, p_ch]

@@ -593,7 +593,9 @@ AsmTables prepare_assembly(nrg_ctx* c, const ModelSpec& m, const Basis& B, const
   aa.pair_fwd = (const int64_t*)(mb + o_pf); aa.pair_fwd_ld = (const int*)(mb + o_pfl);
   aa.pair_bwd = (const int64_t*)(mb + o_pbw); aa.pair_bwd_ld = (const int*)(mb + o_pbl);
   aa.coef = (const double*)(mb + o_coef); aa.ntypes = tabs.ntypes; aa.nchan = tabs.nchan; aa.nsigma = tabs.nsigma;
-  aa.nops_h = nops_h; aa.model = (int)m.kind; aa.ops = (const double* const*)c->opptr.p;
+  // OneChQ_HN_MatEl is OneChQSz_HN_MatEl without the e_N term (zero on the
+  // flat band): the same device arithmetic
+  aa.nops_h = nops_h; aa.model = m.kind == MODEL_1CHQ ? (int)MODEL_1CHQSZ : (int)m.kind; aa.ops = (const double* const*)c->opptr.p;
   aa.sqrt_lambda = std::sqrt(lambda); aa.eN = eN; aa.chi[0] = chi[0]; aa.chi[1] = chi[1];
   aa.site_q = (const double*)(mb + o_sq); aa.H = c->H.as<double>();
   return T;
@@ -738,7 +740,7 @@ void launch_update_plan(nrg_ctx* c, Timer& tm, UpdatePlan& U) {
 void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool chain = false) {
   using clock = std::chrono::steady_clock;
   auto t_begin = clock::now();
-  if (cfg->model < 0 || cfg->model > 2) throw NrgError(NRG_ERR_ARG, "unknown model");
+  if (cfg->model < 0 || cfg->model > 3) throw NrgError(NRG_ERR_ARG, "unknown model");
   if (dm && cfg->model != NRG_MODEL_1CH_QS)
     throw NrgError(NRG_ERR_ARG, "DM-NRG shells are available for the one-channel |Q S> model");
   if (cfg->nsites < 1 || cfg->ncutoff < 4 || !(cfg->lambda > 1.0)) throw NrgError(NRG_ERR_ARG, "bad sweep parameters");
@@ -803,8 +805,11 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
     h2d(c, b->p, st.ops[o].el.data(), sizeof(double) * om.size);
     if (m.op_avg[o]) {
       std::vector<double> diag(st.en.size(), 0.0);
-      for (size_t k = 0; k < st.ops[o].bi.size(); ++k)
-        if (st.ops[o].bi[k] == st.ops[o].bj[k]) diag[st.blk.offset[st.ops[o].bi[k]]] = st.ops[o].el[st.ops[o].off[k]];
+      for (size_t k = 0; k < st.ops[o].bi.size(); ++k) {
+        const int b = st.ops[o].bi[k], n = st.blk.size[b];
+        if (b != st.ops[o].bj[k]) continue;
+        for (int x = 0; x < n; ++x) diag[st.blk.offset[b] + x] = st.ops[o].el[st.ops[o].off[k] + (int64_t)x * n + x];
+      }
       c->opavg_m1.push_back(opavg_host(st.blk, st.en, diag, m.totalS, betabar));
     }
   }

@@ -157,6 +157,16 @@ ModelSpec make_model(ModelKind kind) {
     m.op_kind = {OP_FUP_QSZ, OP_FDN_QSZ, OP_IMPONLY, OP_IMPONLY};
     m.op_check = {CHK_Q_CD, CHK_Q_CD, CHK_DIAG, CHK_DIAG};
     m.op_name = {"fNup", "fNdn", "Ndot", "Szdot"};
+  } else if (kind == MODEL_1CHQ) {
+    // CNRGCodeHandler::SetSingleSite, SymNo 3 (NRGcodehandlerClass.cpp:484-503):
+    // blocks by Q alone, |0> | |up>,|dn> | |up dn> (types 0..3).
+    m.site.blk.nqn = 2;
+    site_block(m.site, {-1, 0}, 1); site_block(m.site, {0, 0}, 2); site_block(m.site, {1, 0}, 1);
+    m.totalS = false; m.nchan = 1; m.nsigma = 2;
+    // CodeHandler_ModelSwitch.cpp:1138-1158: f_up, f_dn, and S_z, S_z^2 averaged.
+    m.op_kind = {OP_FUP_QSZ, OP_FDN_QSZ, OP_IMPONLY, OP_IMPONLY};
+    m.op_check = {CHK_Q_CD, CHK_Q_CD, CHK_DIAG, CHK_DIAG};
+    m.op_name = {"fNup", "fNdn", "Sz", "Sz2"};
   } else if (kind == MODEL_2CHQS) {
     // TwoChQS_SetSingleSite (TwoChQS_SetSingleSite.cpp:5-124): 16 states in 10 blocks.
     m.site.blk.nqn = 3;
@@ -212,6 +222,23 @@ StartState make_start(const ModelSpec& m, double lambda, double U, double ed, do
     s.ops.push_back(f);
     if (m.kind == MODEL_2CHQS) s.ops.push_back(f);  // f_ch1 = f_ch2 = d
     s.ops.push_back(o1); s.ops.push_back(o2); s.ops.push_back(o3);
+  } else if (m.kind == MODEL_1CHQ) {
+    // OneChQ_SetAnderson_Hm1 (Main/Main_SetH0.cpp:217-352): |0> | |up>,|dn> |
+    // |up dn> by Q, the Q = 0 block two-fold; f_up, f_dn not reduced; S_z and
+    // S_z^2 from the states' iDegen/10.
+    const double q[3][2] = {{-1, 0}, {0, 0}, {1, 0}};
+    s.blk.push(q[0], 1); s.blk.push(q[1], 2); s.blk.push(q[2], 1);
+    s.en = {0.5 * U / scale, (ed + 0.5 * U) / scale, (ed + 0.5 * U) / scale, (2.0 * ed + 1.5 * U) / scale};
+    OpBlocks fu, fd, sz, sz2;
+    auto pair = [](OpBlocks& o, int i, int j, std::initializer_list<double> v) {
+      o.bi.push_back(i); o.bj.push_back(j); o.off.push_back((int64_t)o.el.size());
+      o.el.insert(o.el.end(), v);
+    };
+    pair(fu, 0, 1, {1.0, 0.0}); pair(fu, 1, 2, {0.0, 1.0});
+    pair(fd, 0, 1, {0.0, 1.0}); pair(fd, 1, 2, {-1.0, 0.0});
+    pair(sz, 0, 0, {0.0}); pair(sz, 1, 1, {0.5, 0.0, 0.0, -0.5}); pair(sz, 2, 2, {0.0});
+    pair(sz2, 0, 0, {0.0}); pair(sz2, 1, 1, {0.25, 0.0, 0.0, 0.25}); pair(sz2, 2, 2, {0.0});
+    s.ops = {fu, fd, sz, sz2};
   } else {
     // OneChQSz_SetAnderson_Hm1 (Main/Main_SetH0.cpp:421-660) with the Zeeman
     // term -hz S_z, hz = B/2.
@@ -235,7 +262,8 @@ StartState make_chain_start(const ModelSpec& m, double lambda) {
   if (m.kind != MODEL_2CHQS) {
     // OneChQS_SetChainH0 / OneChQSz_SetChainH0 (Main/Main_SetH0.cpp:3322-3465):
     // the site multiplets at zero energy carry the same blocks and reduced f
-    // elements as the impurity start with U = ed = B = 0.
+    // elements as the impurity start with U = ed = B = 0.  (ModelSwitch has no
+    // chain case for OneChQ; the same construction gives its first site.)
     StartState s = make_start(m, lambda, 0.0, 0.0, 0.0);
     s.ops.resize(nf);
     return s;
@@ -404,13 +432,14 @@ void build_hn_tables(const ModelSpec& m, const Basis& b, HNTables& t) {
         if (m.kind == MODEL_1CHQS) {
           c[base * 2 + 0] = hn_coef_1chQS(m.site, Si, ti, tj);
           c[base * 2 + 1] = hn_coef_1chQS(m.site, Si, tj, ti);
-        } else if (m.kind == MODEL_1CHQSZ) {
-          // OneChQSz_HN_MatEl (OpMatRules.cpp:468-531): per spin, the fermion
-          // sign of the "type" state times <typep|f^dagger_sigma|type>.
+        } else if (m.kind == MODEL_1CHQSZ || m.kind == MODEL_1CHQ) {
+          // OneChQSz_HN_MatEl (OpMatRules.cpp:468-531), OneChQ_HN_MatEl
+          // (:1065-1147): per spin, the fermion sign of the "type" state times
+          // <typep|f^dagger_sigma|type>.
           for (int s = 0; s < 2; ++s) {
             int isigma = s == 0 ? 1 : -1;
-            double fq = deq(m.site.blk.q(tj, 0), 0.0) ? -1.0 : 1.0;
-            double bq = deq(m.site.blk.q(ti, 0), 0.0) ? -1.0 : 1.0;
+            double fq = deq(m.site.blk.q(m.site.block_of_state(tj), 0), 0.0) ? -1.0 : 1.0;
+            double bq = deq(m.site.blk.q(m.site.block_of_state(ti), 0), 0.0) ? -1.0 : 1.0;
             c[(base + s) * 2 + 0] = fq * fd_onech(isigma, ti, tj);
             c[(base + s) * 2 + 1] = bq * fd_onech(isigma, tj, ti);
           }

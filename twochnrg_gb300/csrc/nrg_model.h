@@ -15,7 +15,10 @@
 
 namespace nrg {
 
-enum ModelKind { MODEL_1CHQS = 0, MODEL_1CHQSZ = 1, MODEL_2CHQS = 2 };
+// MODEL_1CHQ (SymNo 3) conserves the charge only; its blocks carry the
+// reference's single quantum number Q plus a constant 0 in the second slot,
+// which leaves BuildBasis's block and state order unchanged.
+enum ModelKind { MODEL_1CHQS = 0, MODEL_1CHQSZ = 1, MODEL_2CHQS = 2, MODEL_1CHQ = 3 };
 
 // Operator rule ids (how the operator acts on a new site; see build_op_terms).
 enum OpKind {
