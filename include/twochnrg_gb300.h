@@ -331,7 +331,12 @@ nrg_status nrg_lehmann(nrg_ctx* ctx, const nrg_dm_params* prm, int nomega, const
  * CodeHandler_ModelSwitch.cpp:377-420, 667-720, 940-1000).  H_0 is the first
  * Wilson site alone (iteration 0, thermodynamics at D_0 as NRG_main.cpp:242-255
  * takes them); iterations 1 .. nsites-1 add one site each.  U, ed, gamma1 and
- * gamma2_or_B are ignored (ZeroParams).  Results through nrg_sweep_iteration. */
+ * gamma2_or_B are ignored (ZeroParams).  For NRG_MODEL_1CH_Q, which has no
+ * chain case in ModelSwitch, NRG_main.cpp:215-218 runs the Anderson model with
+ * every parameter zeroed instead: a decoupled impurity beside the chain,
+ * iterations 0 .. nsites-1, its ln 4 of entropy subtracted by nrg_thermo_run
+ * (dImpValue, CodeHandler_ModelSwitch.cpp:1191).  Results through
+ * nrg_sweep_iteration. */
 nrg_status nrg_sweep_run_chain(nrg_ctx* ctx, const nrg_sweep_config* cfg);
 
 typedef struct {

@@ -1462,14 +1462,15 @@ void* oracle_run(const oracle_config* cfg) {
       P = {Lambda, chi0, 0.0, 0.0};
       totalS = false;
     } else if (cfg->model == ORACLE_MODEL_1CHQ) {
-      // ModelSwitch has no chain case for OneChQ; the first site alone is the
-      // impurity start at U = ed = 0, as for the other one-channel symmetries.
+      // ModelSwitch has no chain case for OneChQ: NRG_main.cpp:215-218 runs
+      // the Anderson model with every parameter zeroed instead (a decoupled
+      // impurity, Gamma = 0, from site 0 on; Nsites0 = 0).
       c.m.site = site_1chQ(); c.m.totS = {}; c.m.common = {1, 0, 0};
       Mat fu, fd; std::vector<Mat> avg;
       hm1_Q(Lambda, HLF, 0.0, 0.0, eig, fu, fd, avg);
       mats.push_back(fu); mats.push_back(fd);
       c.m.op_rule = {R_FUP_QSZ, R_FDN_QSZ}; c.m.op_check = {C_Q_CD, C_Q_CD};
-      P = {Lambda, chi0, 0.0, 0.0};
+      P = {Lambda, 0.0, 0.0, 0.0};
       totalS = false; sq = -1;
     } else if (cfg->model == ORACLE_MODEL_2CHQS) {
       c.m.site = site_2chQS(); c.m.totS = {1};
@@ -1545,7 +1546,7 @@ void* oracle_run(const oracle_config* cfg) {
   cut_states(eig, cut, cfg->ncutoff, eps);
   for (auto& m : mats) if (m.calc_avg) R->opavg_m1.push_back(calc_opavg(cut, m, betabar, totalS, sq));
   int N0 = 0;
-  if (chain) {
+  if (chain && cfg->model != ORACLE_MODEL_1CHQ) {
     // Nsites0 = 1: CalcThermo on H_0 before the loop, at D = HLF
     // Lambda^(-(Nsites0-2)/2) (NRG_main.cpp:242-255).
     OracleIter I;

@@ -35,6 +35,9 @@ CASES = {
                                "Chain1Ch_QSz_zEQ1", "Imp1ChQSz_zEQ1"),
     "thermo_2chQS_chain_n8_k300": ("2chQS_Kondo", 8, 300, 0.3, 0.01, -0.15, 2.5, None,
                                    "Chain2Ch_QS_zEQ1", None),
+    # |Q> symmetry: entropy only, files without the z-string
+    "thermo_1chQ_n10_k150": ("1chQ_Anderson", 10, 150, 0.5, 0.02, -0.25, 2.5, None,
+                             "Chain1Ch_Q", "Imp1Ch_Anderson_Q"),
 }
 
 
@@ -53,13 +56,17 @@ def run_case(opt, ns, nc, U, G, ed, lam, extra, chain, imp) -> dict:
     with tempfile.TemporaryDirectory() as d:
         _input(d, ns, nc, U, G, ed, lam, extra, 3)
         subprocess.run([NRG_MAIN, "-m", opt], cwd=d, check=True, capture_output=True, env=env)
-        out["chain_suscep"] = np.loadtxt(os.path.join(d, f"Suscep{chain}.dat"))
-        out["chain_entropy"] = np.loadtxt(os.path.join(d, f"Entropy{chain}.dat"))
+        for kind in ("Suscep", "Entropy"):
+            p = os.path.join(d, f"{kind}{chain}.dat")
+            if os.path.exists(p):
+                out[f"chain_{kind.lower()}"] = np.loadtxt(p)
         if imp is not None:
             _input(d, ns, nc, U, G, ed, lam, extra, 2)
             subprocess.run([NRG_MAIN, "-m", opt], cwd=d, check=True, capture_output=True, env=env)
-            out["imp_suscep"] = np.loadtxt(os.path.join(d, f"Suscep{imp}.dat"))
-            out["imp_entropy"] = np.loadtxt(os.path.join(d, f"Entropy{imp}.dat"))
+            for kind in ("Suscep", "Entropy"):
+                p = os.path.join(d, f"{kind}{imp}.dat")
+                if os.path.exists(p):
+                    out[f"imp_{kind.lower()}"] = np.loadtxt(p)
     return out
 
 

@@ -46,6 +46,19 @@ def test_random_blocks(engine):
         _check_block(A, w, Z, wr, Zr)
 
 
+def test_zero_and_diagonal_blocks(engine):
+    """Blocks whose tridiagonal splits everywhere: the zero matrix (all
+    levels 0, eigenvectors the identity, as dspev returns them) and a diagonal
+    one with a repeated level."""
+    Z0 = np.zeros((6, 6))
+    D = np.diag([0.5, -1.0, 0.5, 2.0, 0.5])
+    ws, Zs = engine.diag_blocks([6, 5], np.concatenate([orc.pack_upper(Z0), orc.pack_upper(D)]))
+    assert not ws[0].any()
+    np.testing.assert_array_equal(Zs[0], np.eye(6))
+    wr, Zr = orc.diag_block(orc.pack_upper(D), 5)
+    _check_block(D, ws[1], Zs[1], wr, Zr)
+
+
 def test_large_block_whole_gpu_path(engine, monkeypatch):
     rng = np.random.default_rng(11)
     n = 1300

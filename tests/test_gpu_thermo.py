@@ -92,14 +92,17 @@ def test_gpu_thermo_files(engine, tmp_path):
 
 
 def test_charge_only_symmetry_entropy(engine, tmp_path):
-    """|Q> basis: entropy only (the reference's Sqnumber -1 takes no T chi).
-    ModelSwitch has no free-chain case for this symmetry; its chain is the
-    same physical chain as the |Q Sz> one, so the entropies agree."""
-    r = engine.thermo("1chQ", 10, 150, 2.5, 0.5, -0.25, 0.02)
+    """|Q> basis: entropy only (the reference's Sqnumber -1 takes no T chi);
+    its chain run is the Anderson model with every parameter zeroed, minus
+    the decoupled impurity's ln 4."""
+    g = np.load(os.path.join(GOLDEN, "thermo_1chQ_n10_k150.npz"))
+    ns, nc, U, G, ed, lam, x = g["config"]
+    r = engine.thermo("1chQ", int(ns), int(nc), lam, U, ed, G)
     assert not r.suscep.any() and not r.suscep_chain.any()
-    z = np.array([i.thermo for i in engine.sweep_chain("1chQSz", 10, 150, 2.5).iters]).reshape(-1, 4)
-    _close(r.entropy_chain, z[:, 3])
-    o = np.array([i.thermo for i in orc.run("1chQ", 10, 150, 2.5, 0.5, -0.25, 0.02).iters]).reshape(-1, 4)
-    _close(r.entropy, o[:, 3])
+    e = g["imp_entropy"]
+    np.testing.assert_array_equal(r.temp, e[:, 0])
+    _close(r.entropy, e[:, 1]); _close(r.entropy_chain, e[:, 2]); _close(r.entropy_imp, e[:, 3])
+    _close(r.entropy_chain, g["chain_entropy"][:, 1])
     names = sorted(os.path.basename(p) for p in r.save(str(tmp_path)))
     assert names == ["EntropyChain1Ch_Q.dat", "EntropyImp1Ch_Anderson_Q.dat"]
+    _close(np.loadtxt(str(tmp_path / "EntropyImp1Ch_Anderson_Q.dat")), e)

@@ -328,11 +328,8 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
   if (K == 1) {
     const int G = tridiag_grid_size(ta.maxn);
     if (G <= 0) throw NrgError(NRG_ERR_SIZE, "whole-GPU tridiagonalization does not fit");
-    c->gpart.ensure(sizeof(double) * ((size_t)G * ta.maxn + ta.maxn + G + 64));
-    double* part = c->gpart.as<double>();
-    double* pvec = part + (size_t)G * ta.maxn;
-    double* dots = pvec + ta.maxn;
-    CU(launch_tridiag_grid(ta, d_order, nbig, part, pvec, dots, G, c->stream));
+    c->gpart.ensure(sizeof(double) * tridiag_grid_work(ta.maxn, G));
+    CU(launch_tridiag_grid(ta, d_order, nbig, c->gpart.as<double>(), G, c->stream));
     CU(cudaEventRecord(c->join[0], c->stream));
     c->launches++; c->timing.tridiag_launches++;
   } else if (K > 1) {
@@ -343,13 +340,10 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
     CU(cudaEventRecord(c->fork, c->stream));
     for (int k = 0; k < K; ++k) {
       if (!c->aux[k]) CU(cudaStreamCreateWithFlags(&c->aux[k], cudaStreamNonBlocking));
-      c->gpart_k[k].ensure(sizeof(double) * ((size_t)Gk * ta.maxn + ta.maxn + Gk + 64));
-      double* part = c->gpart_k[k].as<double>();
-      double* pvec = part + (size_t)Gk * ta.maxn;
-      double* dots = pvec + ta.maxn;
+      c->gpart_k[k].ensure(sizeof(double) * tridiag_grid_work(ta.maxn, Gk));
       CU(cudaStreamWaitEvent(c->aux[k], c->fork, 0));
-      CU(launch_tridiag_grid(ta, (const int*)(c->gbig.as<char>() + o_bins[k]), (int)bins[k].size(), part, pvec,
-                             dots, Gk, c->aux[k]));
+      CU(launch_tridiag_grid(ta, (const int*)(c->gbig.as<char>() + o_bins[k]), (int)bins[k].size(),
+                             c->gpart_k[k].as<double>(), Gk, c->aux[k]));
       CU(cudaEventRecord(c->join[k], c->aux[k]));
       c->launches++; c->timing.tridiag_launches++;
     }
@@ -786,7 +780,15 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
   c->opptr.ensure(sizeof(double*) * 32);
 
   // H_{-1} (the initial CutStates keeps everything: Ncutoff >= 4 states).
-  StartState st = chain ? make_chain_start(m, lambda) : make_start(m, lambda, cfg->U, cfg->ed, cfg->gamma2_or_B);
+  // calcdens = 3 for the |Q> symmetry: NRG_main.cpp:215-218 turns the chain
+  // run back into the Anderson model with every parameter zeroed (U = ed =
+  // Gamma = 0): a decoupled four-state impurity beside the chain from site 0
+  // on (Nsites0 = 0); its ln 4 is CNRGthermo::dImpValue.
+  const bool chain_q = chain && m.kind == MODEL_1CHQ;
+  StartState st = chain && !chain_q ? make_chain_start(m, lambda)
+                                    : make_start(m, lambda, chain ? 0.0 : cfg->U, chain ? 0.0 : cfg->ed,
+                                                 chain ? 0.0 : cfg->gamma2_or_B);
+  if (chain_q) st.ops.resize(nops);
   if (dm) {
     st.ops = {st.ops[0], st.ops[0]};  // c_d at H_{-1} is a copy of f (Main_SetH0.cpp:1958-1961)
     c->dm_hm1_en = st.en;
@@ -814,11 +816,11 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
     }
   }
 
-  double chi[2] = {chi_m1(lambda, cfg->gamma1), 0.0};
-  if (m.nchan == 2) chi[1] = chi_m1(lambda, cfg->gamma2_or_B);
+  double chi[2] = {chi_m1(lambda, chain ? 0.0 : cfg->gamma1), 0.0};
+  if (m.nchan == 2) chi[1] = chi_m1(lambda, chain ? 0.0 : cfg->gamma2_or_B);
   const double eN = 0.0;  // flat band (CNRGchain::GetEn of SetChainWilson)
   int N0 = 0;
-  if (chain) {
+  if (chain && !chain_q) {
     // chi_m1 = chiN(0) for every channel; H_0 is recorded as iteration 0 with
     // the thermodynamics CalcThermo takes before the loop, at
     // D = HLF Lambda^(-(Nsites0-2)/2) = D_0.
@@ -1466,6 +1468,11 @@ void thermo_run_impl(nrg_ctx* c, const nrg_sweep_config* cfg, int reuse_chain) {
     if (cst != NRG_OK) throw NrgError(cst, "free-chain sweep: " + cerr);
     c->chain_thermo.clear();
     for (const IterResult& R : cc->iters) c->chain_thermo.insert(c->chain_thermo.end(), R.thermo.begin(), R.thermo.end());
+    // CNRGthermo::AddValue (NRGthermoClass.cpp:17-18) subtracts dImpValue in
+    // the chain run: 2 ln 2 for the |Q> entropy (CodeHandler_ModelSwitch.cpp:
+    // 1187-1191, the decoupled impurity); never set, and 0, for the others.
+    if (cfg->model == NRG_MODEL_1CH_Q)
+      for (size_t k = 3; k < c->chain_thermo.size(); k += 4) c->chain_thermo[k] -= 2.0 * std::log(2.0);
     c->chain_cfg = *cfg;
     c->chain_valid = true;
   } else {

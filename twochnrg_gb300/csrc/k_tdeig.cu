@@ -307,7 +307,13 @@ __global__ void inviter_kernel(InvIterArgs A, const int* vec_block, const int* v
   double onenrm = 0.0;
   for (int i = 0; i < n; ++i)
     onenrm = fmax(onenrm, fabs(d[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0));
-  onenrm = fmax(onenrm, DBL_MIN);
+  if (onenrm == 0.0) {
+    // T = 0 (a block of exactly degenerate zero levels, e.g. a decoupled
+    // impurity beside an empty chain): every unit vector is an eigenvector,
+    // and the identity is what the reference's dspev returns for it.
+    for (int i = 0; i < n; ++i) AT(Y, i) = (i == k) ? 1.0 : 0.0;
+    return;
+  }
   // Shift: separate numerically equal eigenvalues as LAPACK dstein does.
   double sigma = ev[k];
   {

@@ -208,11 +208,18 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
 }
 
 // Whole-GPU variant for the largest blocks: every CTA of a cooperative grid
-// works on the same block; per step the column shares go to global memory,
-// one grid barrier, a reduce-scatter of the shares, a second grid barrier,
-// then every CTA forms w.  Same arithmetic and outputs as tridiag_kernel.
+// works on the same block and owns a contiguous range of its rows.  Per
+// Householder step each CTA applies the pending rank-2 update to its rows and
+// forms their complete entries of y = tau A v (the rows hold both triangles),
+// writes them and its share of y.v to global memory, and after ONE grid
+// barrier every CTA reads y and the shares and forms w.  y and the shares are
+// double-buffered by step parity: a CTA that runs ahead into the next step
+// writes the other buffer, and cannot run two steps ahead past the barrier.
+// Same outputs as tridiag_kernel.
+constexpr int kSeg = 4;  // column segments per row: warps work on (row, segment) items
+
 __global__ void __launch_bounds__(kThreads, 1) tridiag_grid_kernel(TridiagArgs A, const int* big, int nbig,
-                                                                  double* part, double* pvec, double* dots) {
+                                                                  double* work) {
   extern __shared__ double sm[];
   cg::grid_group grid = cg::this_grid();
   const int G = (int)gridDim.x;
@@ -221,6 +228,7 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_grid_kernel(TridiagArgs A
   double* V0 = sm;
   double* V1 = sm + maxn;
   double* W = sm + 2 * maxn;
+  double* rowp = sm + 3 * maxn;  // (row, segment) partial sums, up to 2 maxn
   double* red = sm + 5 * maxn;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int qb = 0; qb < nbig; ++qb) {
@@ -235,6 +243,7 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_grid_kernel(TridiagArgs A
     double* vnew = V0;
     double* vold = V1;
     bool have_old = false;
+    int par = 0;
     for (int j = 0; j + 2 < n; ++j) {
       for (int c = j + tid; c < n; c += kThreads) {
         double a = __ldcg(H + (int64_t)j * n + c);
@@ -263,67 +272,58 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_grid_kernel(TridiagArgs A
       const int m = n - j - 1;
       const int rows_per = (m + G - 1) / G;
       const int r0 = j + 1 + rank * rows_per;
-      const int r1 = min(n, r0 + rows_per);
-      double* yp = part + (int64_t)rank * maxn;
-      const int nchunks = (m + 63) / 64;
-      for (int chk = warp; chk < nchunks; chk += kWarps) {
-        const int c0 = j + 1 + chk * 64 + lane;
-        const int c1 = c0 + 32;
-        const bool ok0 = c0 < n, ok1 = c1 < n;
-        double vo0 = 0.0, wo0 = 0.0, vo1 = 0.0, wo1 = 0.0;
+      const int nr = max(0, min(n, r0 + rows_per) - r0);
+      int S = kSeg;
+      while (S > 1 && rows_per * S > 2 * maxn) S >>= 1;
+      const int seglen = (((m + S - 1) / S) + 31) & ~31;
+      for (int it = warp; it < nr * S; it += kWarps) {
+        const int rr = it / S, sg = it - rr * S;
+        const int r = r0 + rr;
+        const int cb = j + 1 + sg * seglen, ce = min(n, cb + seglen);
+        double* Hr = H + (int64_t)r * n;
+        double acc = 0.0;
         if (have_old) {
-          if (ok0) { vo0 = vold[c0]; wo0 = W[c0]; }
-          if (ok1) { vo1 = vold[c1]; wo1 = W[c1]; }
-        }
-        double acc0 = 0.0, acc1 = 0.0;
-        for (int r = r0; r < r1; ++r) {
-          const double* Ha = H + (int64_t)r * n;
-          double a0 = ok0 ? __ldcg(Ha + c0) : 0.0, a1 = ok1 ? __ldcg(Ha + c1) : 0.0;
-          if (have_old) {
-            const double vra = vold[r], wra = W[r];
-            a0 = fma(-vra, wo0, fma(-wra, vo0, a0)); a1 = fma(-vra, wo1, fma(-wra, vo1, a1));
-            if (ok0) __stcg((double*)Ha + c0, a0);
-            if (ok1) __stcg((double*)Ha + c1, a1);
+          const double vr = vold[r], wr = W[r];
+          for (int c = cb + lane; c < ce; c += 32) {
+            double a = __ldcg(Hr + c);
+            a = fma(-vr, W[c], fma(-wr, vold[c], a));
+            __stcg(Hr + c, a);
+            acc = fma(a, vnew[c], acc);
           }
-          const double va = vnew[r];
-          acc0 = fma(a0, va, acc0); acc1 = fma(a1, va, acc1);
+        } else {
+          for (int c = cb + lane; c < ce; c += 32) acc = fma(__ldcg(Hr + c), vnew[c], acc);
         }
-        if (ok0) __stcg(yp + c0, acc0);
-        if (ok1) __stcg(yp + c1, acc1);
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) rowp[rr * S + sg] = acc;
       }
-      grid.sync();
-      // reduce-scatter: this CTA owns columns [q0, q1)
-      const int cols_per = (m + G - 1) / G;
-      const int q0 = j + 1 + rank * cols_per, q1 = min(n, q0 + cols_per);
-      // one warp per column: lanes stride over the G shares, then a fixed-order
-      // shuffle tree (every CTA sums its columns the same way)
+      __syncthreads();
+      double* yb = work + (int64_t)par * maxn;
+      double* db = work + 2 * (int64_t)maxn + par * G;
       double dpart = 0.0;
-      for (int c = q0 + warp; c < q1; c += kWarps) {
-        double p = 0.0;
-        for (int q = lane; q < G; q += 32) p += __ldcg(part + (int64_t)q * maxn + c);
-        for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
-        p *= tau;
-        if (lane == 0) {
-          __stcg(pvec + c, p);
-          dpart = fma(p, vnew[c], dpart);
-        }
+      for (int rr = tid; rr < nr; rr += kThreads) {
+        double y = 0.0;
+        for (int sg = 0; sg < S; ++sg) y += rowp[rr * S + sg];
+        y *= tau;
+        __stcg(yb + r0 + rr, y);
+        dpart = fma(y, vnew[r0 + rr], dpart);
       }
       dpart = block_sum(dpart, red);
-      if (tid == 0) __stcg(dots + rank, dpart);
+      if (tid == 0) __stcg(db + rank, dpart);
       grid.sync();
       double dt = 0.0;
       if (tid < 32) {
-        for (int q = lane; q < G; q += 32) dt += __ldcg(dots + q);
+        for (int q = lane; q < G; q += 32) dt += __ldcg(db + q);
         for (int o = 16; o > 0; o >>= 1) dt += __shfl_xor_sync(0xffffffffu, dt, o);
         if (lane == 0) red[kWarps + 1] = dt;
       }
       __syncthreads();
       dt = red[kWarps + 1];
       const double h = 0.5 * tau * dt;
-      for (int c = j + 1 + tid; c < n; c += kThreads) W[c] = fma(-h, vnew[c], __ldcg(pvec + c));
+      for (int c = j + 1 + tid; c < n; c += kThreads) W[c] = fma(-h, vnew[c], __ldcg(yb + c));
       __syncthreads();
       double* t = vnew; vnew = vold; vold = t;
       have_old = true;
+      par ^= 1;
     }
     if (rank == 0) {
       if (have_old)
@@ -359,14 +359,16 @@ int tridiag_grid_size(int maxn) {
   return per_sm >= 1 ? sms : 0;  // one CTA per SM
 }
 
-cudaError_t launch_tridiag_grid(const TridiagArgs& a, const int* big, int nbig, double* part, double* pvec,
-                                double* dots, int grid, cudaStream_t s) {
+size_t tridiag_grid_work(int maxn, int grid) { return 2 * (size_t)maxn + 2 * (size_t)grid + 64; }
+
+cudaError_t launch_tridiag_grid(const TridiagArgs& a, const int* big, int nbig, double* work, int grid,
+                                cudaStream_t s) {
   size_t smem = sizeof(double) * (5 * (size_t)a.maxn + kWarps + 4) + 16;
   cudaError_t err =
       cudaFuncSetAttribute(tridiag_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem());
   if (err != cudaSuccess) return err;
   TridiagArgs aa = a;
-  void* args[] = {(void*)&aa, (void*)&big, (void*)&nbig, (void*)&part, (void*)&pvec, (void*)&dots};
+  void* args[] = {(void*)&aa, (void*)&big, (void*)&nbig, (void*)&work};
   return cudaLaunchCooperativeKernel((const void*)tridiag_grid_kernel, dim3(grid), dim3(kThreads), args, smem, s);
 }
 

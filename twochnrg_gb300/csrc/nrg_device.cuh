@@ -81,8 +81,10 @@ size_t tridiag_smem_bytes(int maxn);
 int tridiag_max_clusters(int cluster, int maxn);
 // Whole-GPU cooperative variant for the largest blocks (processed in turn).
 int tridiag_grid_size(int maxn);
-cudaError_t launch_tridiag_grid(const TridiagArgs& a, const int* big, int nbig, double* part, double* pvec,
-                                double* dots, int grid, cudaStream_t s);
+// work: tridiag_grid_work(maxn, grid) doubles of device memory.
+size_t tridiag_grid_work(int maxn, int grid);
+cudaError_t launch_tridiag_grid(const TridiagArgs& a, const int* big, int nbig, double* work, int grid,
+                                cudaStream_t s);
 
 struct TdEigArgs {
   int nblocks;

@@ -262,8 +262,7 @@ StartState make_chain_start(const ModelSpec& m, double lambda) {
   if (m.kind != MODEL_2CHQS) {
     // OneChQS_SetChainH0 / OneChQSz_SetChainH0 (Main/Main_SetH0.cpp:3322-3465):
     // the site multiplets at zero energy carry the same blocks and reduced f
-    // elements as the impurity start with U = ed = B = 0.  (ModelSwitch has no
-    // chain case for OneChQ; the same construction gives its first site.)
+    // elements as the impurity start with U = ed = B = 0.
     StartState s = make_start(m, lambda, 0.0, 0.0, 0.0);
     s.ops.resize(nf);
     return s;
