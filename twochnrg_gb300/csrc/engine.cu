@@ -130,7 +130,7 @@ struct nrg_ctx {
   cudaEvent_t ev_a[8];
   // concurrent whole-GPU tridiagonalizations: side streams, fork/join events,
   // per-stream scratch and the block lists
-  static constexpr int kMaxSplit = 4;
+  static constexpr int kMaxSplit = 8;
   cudaStream_t aux[kMaxSplit] = {};
   cudaEvent_t fork = nullptr, join[kMaxSplit] = {};
   nrg::DevBuf gpart_k[kMaxSplit], gbig;
@@ -265,16 +265,19 @@ int choose_cluster(int maxn) {
 // thread-block cluster each.
 int big_block_threshold() {
   const char* s = std::getenv("NRG_BIG_N");
-  return s ? std::atoi(s) : 2400;
+  return s ? std::atoi(s) : 1800;
 }
 
 // The large blocks are dealt (by n^3, largest first) to this many concurrent
-// cooperative grids, each with an equal share of the SMs: a Householder step
-// is latency-bound (two grid barriers and a reduce-scatter), so independent
-// blocks on fewer SMs each overlap those latencies.
+// cooperative grids, each with an equal share of the SMs: part of every
+// Householder step is latency (a grid barrier, block reductions, the L2 round
+// trips of the Householder vector and y), so independent blocks on fewer SMs
+// each overlap those latencies.  Four grids of 38 SMs with blocks from 1800
+// states on measured fastest on the two-channel workload (1 to 8 grids and
+// thresholds 1500 to 3200 tried).
 int grid_split(int nbig) {
   const char* s = std::getenv("NRG_GRID_SPLIT");
-  int k = s ? std::atoi(s) : 2;
+  int k = s ? std::atoi(s) : 4;
   k = std::max(1, std::min(k, nrg_ctx::kMaxSplit));
   return std::min(k, nbig);
 }
