@@ -53,11 +53,15 @@ typedef enum {
   NRG_MODEL_1CH_QS = 0,  /* one-channel Anderson, |Q S> basis   (SymNo 0, ModelNo 0) */
   NRG_MODEL_1CH_QSZ = 1, /* one-channel Anderson, |Q Sz> basis  (SymNo 2, ModelNo 0) */
   NRG_MODEL_2CH_QS = 2,  /* two-channel Anderson, |Q S> basis   (SymNo 1)            */
-  NRG_MODEL_1CH_Q = 3    /* one-channel Anderson, |Q> basis     (SymNo 3, ModelNo 0);
+  NRG_MODEL_1CH_Q = 3,   /* one-channel Anderson, |Q> basis     (SymNo 3, ModelNo 0);
                             whole sweeps only.  Blocks are reported as (Q, 0); the
                             averaged operators are S_z and S_z^2; the reference takes
                             only the entropy for this symmetry, and the T chi slot of
                             nrg_iteration.thermo is 0 */
+  NRG_MODEL_1CH_S = 4    /* one-channel Anderson with superconducting leads, |S> basis
+                            (SymNo 7, ModelNo 0); whole sweeps only.  gamma2_or_B carries
+                            Delta_SC; blocks are reported as (0, S); nrg_iteration.params[2]
+                            is the Delta_N of that iteration; no free-chain run */
 } nrg_model;
 
 /* Arithmetic of the dense steps. */
@@ -76,7 +80,8 @@ typedef struct {
   double lambda;      /* Lambda */
   double U, ed;       /* impurity interaction and level */
   double gamma1;      /* hybridization Gamma (channel 1) */
-  double gamma2_or_B; /* Gamma2 for NRG_MODEL_2CH_QS, field B for NRG_MODEL_1CH_QSZ */
+  double gamma2_or_B; /* Gamma2 for NRG_MODEL_2CH_QS, field B for NRG_MODEL_1CH_QSZ,
+                         Delta_SC for NRG_MODEL_1CH_S */
   double degen_eps;   /* CNRGarray::MyEPS (-E flag); <= 0 selects 1e-18 */
   int precision;      /* nrg_precision */
 } nrg_sweep_config;
@@ -96,7 +101,8 @@ typedef struct {
   const double* thermo;    /* [4*4]: (betabar_n, T_M, T chi (CalcSuscep), S (CalcEntropy)) */
   int nops;
   const double* opavg;     /* [nops] CalcOpAvg of the averaged operators at betabar */
-  const double* params;    /* [4] ParamsHN used: Lambda, chi_1, chi_2 (0 if 1ch), eN */
+  const double* params;    /* [4] ParamsHN used: Lambda, chi_1, chi_2 (0 if 1ch; Delta_N for
+                              NRG_MODEL_1CH_S), eN */
 } nrg_iteration;
 
 /* Phase timing of the last sweep (device time from CUDA events). */

@@ -191,6 +191,15 @@ double onech_fd(int sigma, int ti, int tj) {
   return 0.0;
 }
 
+// OneChS_fd_table (OpTables.cpp:419-443) in the basis |0>, |up dn>, |up>, |dn>
+// of the superconducting-lead site, and OneChS_fdupfddn_table (:447-462).
+double onechS_fd(int sigma, int ti, int tj) {
+  if (sigma == 1) { if (ti == 2 && tj == 0) return 1.0; if (ti == 1 && tj == 3) return 1.0; return 0.0; }
+  if (sigma == -1) { if (ti == 3 && tj == 0) return 1.0; if (ti == 1 && tj == 2) return -1.0; return 0.0; }
+  return 0.0;
+}
+double onechS_pair(int ti, int tj) { return (ti == 1 && tj == 0) ? 1.0 : 0.0; }
+
 // TwoChQS_fd_table (TwoChQS_OpTables.cpp:20-130) in the 16-state site basis
 // of TwoChQS_SetSingleSite.  The table entries are the reference's.
 double twoch_fd(int ch, int sigma, int ti, int tj) {
@@ -247,6 +256,14 @@ Basis site_1chQSz() {
   return s;
 }
 // CNRGCodeHandler::SetSingleSite for SymNo 3 (NRGcodehandlerClass.cpp:484-503).
+// CNRGCodeHandler::SetSingleSite for SymNo 7 (NRGcodehandlerClass.cpp:536-560):
+// (S,Sz) blocks |0>,|up dn> | |up> | |dn>.
+Basis site_1chS() {
+  Basis s; s.nqn = 2; s.totalS = true; s.sqn = {0};
+  add_site_block(s, {0, 0}, 0, 1); add_site_block(s, {0.5, 0.5}, 2, 2); add_site_block(s, {0.5, -0.5}, 3, 3);
+  for (int i = 0; i < 4; ++i) s.itype.push_back(i);
+  return s;
+}
 Basis site_1chQ() {
   Basis s; s.nqn = 1; s.totalS = false;
   add_site_block(s, {-1}, 0, 0); add_site_block(s, {0}, 1, 2); add_site_block(s, {1}, 3, 3);
@@ -271,8 +288,8 @@ Basis site_2chQS() {
 }
 
 // ---------------------------------------------------------------- rules
-enum OpRule { R_F_QS = 1, R_FUP_QSZ, R_FDN_QSZ, R_F1_2CH, R_F2_2CH, R_IMPONLY, R_CD_QS };
-enum Check { C_DIAG = 1, C_QS_CD, C_Q_CD, C_2CH_CD };
+enum OpRule { R_F_QS = 1, R_FUP_QSZ, R_FDN_QSZ, R_F1_2CH, R_F2_2CH, R_IMPONLY, R_CD_QS, R_F_S };
+enum Check { C_DIAG = 1, C_QS_CD, C_Q_CD, C_2CH_CD, C_S_CD };
 
 struct Model {
   int kind;          // ORACLE_MODEL_*
@@ -292,6 +309,7 @@ bool check(int c, const Arr& a, int i, int j) {
     case C_Q_CD: return dEq(a.q(j, 0), a.q(i, 0) + 1.0);
     case C_2CH_CD: return dEq(a.q(j, 0), a.q(i, 0) + 1.0) &&
                           (dEq(a.q(j, 1), a.q(i, 1) + 0.5) || dEq(a.q(j, 1), a.q(i, 1) - 0.5));
+    case C_S_CD: return dEq(a.q(j, 0), a.q(i, 0) + 0.5) || dEq(a.q(j, 0), a.q(i, 0) - 0.5);  // OneChS_cd_check :172
   }
   return false;
 }
@@ -370,6 +388,63 @@ double hn_1chQSz(Ctx& c, const std::vector<double>& P, const Basis& ab, const st
     imat++;
   }
   return v * chi_N;
+}
+
+// OneChS_HNsc_MatEl (OpMatRules.cpp:1794-2003): superconducting leads, S
+// blocks.  P = {Lambda, chi_N, e_N, Delta_N}.  The pairing term acts between
+// states from the same old state; the hopping reads the old operator
+// backwards when its element vanishes or the site table has no f^dagger
+// between the two types.
+double hn_1chS(Ctx& c, const std::vector<double>& P, const Basis& ab, const std::vector<Mat>& M,
+               int ist, int jst) {
+  const Basis& ss = c.m.site;
+  double Lambda = P[0], chi_N = P[1], eN = P[2], Delta = P[3];
+  double Si = qn_from_st(ab, ist, 0), Sj = qn_from_st(ab, jst, 0);
+  if (!dEq(Si, Sj)) return 0.0;
+  double v = 0.0;
+  if (ist == jst) {
+    const double auxN[4] = {0.0, 2.0, 1.0, 1.0};
+    v = std::sqrt(Lambda) * ab.en[ist];
+    v += eN * auxN[ab.itype[ist]];
+    return v;
+  }
+  int ti = ab.itype[ist], tj = ab.itype[jst];
+  if (ab.stcf[ist] == ab.stcf[jst]) {
+    v -= Delta * onechS_pair(ti, tj);
+    v -= Delta * onechS_pair(tj, ti);
+    return v;
+  }
+  double Old = M[0].get(ab.stcf[ist], ab.stcf[jst]);
+  int typep = ti, type = tj;
+  if (dEq(Old, 0.0) || (dEq(onechS_fd(1, ti, tj), 0.0) && dEq(onechS_fd(-1, ti, tj), 0.0))) {
+    Old = M[0].get(ab.stcf[jst], ab.stcf[ist]);
+    typep = tj; type = ti;
+  }
+  double Stp = qn_from_st(ss, typep, 0), Sztp = qn_from_st(ss, typep, 1);
+  double St = qn_from_st(ss, type, 0), Szt0 = qn_from_st(ss, type, 1);
+  double Scfp = Si - Sztp, Scf = Si - Szt0;
+  double FermiSign = (type == 2 || type == 3) ? -1.0 : 1.0;
+  double Coef = 0.0;
+  double qp[2] = {Stp, Sztp}, q[2] = {St, Szt0};
+  for (double Szt = -St; Szt <= St; Szt += 1.0) {
+    q[1] = Szt;
+    int sst = type;
+    if (type == 2 || type == 3) sst = ss.block_of_qn(q) + 1;
+    for (int sigma = -1; sigma <= 1; sigma += 2) {
+      double dS = 0.5 * (double)sigma;
+      double Szcf = Si - Szt, Szcfp = Szcf - dS, Sztp_ = Szt + dS;
+      qp[1] = Sztp_;
+      int sstp = ss.block_of_qn(qp) + 1;
+      if (dEq(Sztp_, 0.0)) sstp = typep;
+      double a0 = c.cg(Scf, Szcf, St, Szt, Si, Si);
+      double a1 = c.cg(Scfp, Szcfp, Stp, Sztp_, Si, Si);
+      double a2 = c.cg(Scfp, Szcfp, 0.5, dS, Scf, Szcf);
+      double a3 = onechS_fd(sigma, sstp, sst);
+      Coef += a0 * a1 * a2 * a3;
+    }
+  }
+  v += chi_N * Old * Coef * FermiSign;
+  return v;
 }
 
 // OneChQ_HN_MatEl (OpMatRules.cpp:1065-1147): blocks by Q alone, no e_N term.
@@ -548,6 +623,36 @@ double op_cd_QS(Ctx& c, const Basis& ab, int ist, int jst) {
   return f;
 }
 
+// OneChS_fN_MatEl (OpMatRules.cpp:1555-1654): a spin-1/2 site state is
+// looked up as (its (S,Sz) site block) + 1, a missing one giving 0.
+double op_f_S(Ctx& c, const Basis& ab, int ist, int jst) {
+  const Basis& ss = c.m.site;
+  double Si = qn_from_st(ab, ist, 0), Sj = qn_from_st(ab, jst, 0);
+  int ti = ab.itype[ist], tj = ab.itype[jst];
+  if (ab.stcf[ist] != ab.stcf[jst]) return 0.0;
+  double Sti = qn_from_st(ss, ti, 0), Szti = qn_from_st(ss, ti, 1);
+  double Stj = qn_from_st(ss, tj, 0), Sztj = qn_from_st(ss, tj, 1);
+  double qi[2] = {Sti, Szti}, qj[2] = {Stj, Sztj};
+  double Scfi = Si - Szti, Scfj = Sj - Sztj;
+  double aux = 0.0, cg1 = 0.0;
+  double sigma = Sj - Si;
+  for (double Szt = -Stj; Szt <= Stj; Szt += 1.0) {
+    qj[1] = Szt;
+    int ssj = tj;
+    if (tj == 2 || tj == 3) ssj = ss.block_of_qn(qj) + 1;
+    qi[1] = Szt - sigma;
+    int ssi = ti;
+    if (ti == 2 || ti == 3) ssi = ss.block_of_qn(qi) + 1;
+    double cg0 = c.cg(Scfi, Si - Szt + sigma, Sti, Szt - sigma, Si, Si);
+    cg1 = c.cg(Scfj, Sj - Szt, Stj, Szt, Sj, Sj);
+    aux += onechS_fd((int)(sigma / 0.5), ssj, ssi) * cg0 * cg1;
+  }
+  double n0 = c.cg(Si, Si, 0.5, sigma, Sj, Sj);
+  if (!dEq(n0, 0.0)) return aux / n0;
+  if (!dEq(cg1, 0.0)) return 0.0 / cg1;
+  return 0.0;
+}
+
 double op_rule(Ctx& c, int rule, const Basis& ab, int ist, int jst) {
   switch (rule) {
     case R_F_QS: return op_f_QS(c, ab, ist, jst);
@@ -557,6 +662,7 @@ double op_rule(Ctx& c, int rule, const Basis& ab, int ist, int jst) {
     case R_F2_2CH: return op_f_2ch(c, ab, ist, jst, 2);
     case R_IMPONLY: return ab.itype[ist] == ab.itype[jst] ? 1.0 : 0.0;  // ImpOnly_MatEl OpMatRules.cpp:265
     case R_CD_QS: return op_cd_QS(c, ab, ist, jst);
+    case R_F_S: return op_f_S(c, ab, ist, jst);
   }
   return 0.0;
 }
@@ -656,6 +762,7 @@ double hn_el(Ctx& c, const std::vector<double>& P, const Basis& ab, const std::v
     case ORACLE_MODEL_1CHQSZ: return hn_1chQSz(c, P, ab, M, i, j);
     case ORACLE_MODEL_2CHQS: return hn_2chQS(c, P, ab, M, i, j);
     case ORACLE_MODEL_1CHQ: return hn_1chQ(c, P, ab, M, i, j);
+    case ORACLE_MODEL_1CHS: return hn_1chS(c, P, ab, M, i, j);
   }
   return 0.0;
 }
@@ -994,6 +1101,28 @@ void h0_chain_2chQS(Ctx& c, Arr& a, Mat& f1, Mat& f2) {
         M.push_block(i, j, v.data(), (int)v.size());
       }
   }
+}
+
+// OneChS_SetAnderson_Hm1 (Main/Main_SetH0.cpp:2618-2700): S blocks 0
+// (|0>, |up dn>) and 1/2; reduced f; n_d, n_d^2, S^2 on the diagonal.
+void hm1_S(double Lambda, double HLF, double U, double ed, Arr& a, Mat& f, std::vector<Mat>& avg) {
+  a = Arr(); a.nqn = 1; a.nshell = -1; a.totalS = true; a.sqn = {0};
+  a.qn = {0.0, 0.5};
+  a.bbe = {0, 1, 2, 2};
+  a.en = {0.5 * U / (Lambda * HLF), (2.0 * ed + 1.5 * U) / (Lambda * HLF), (ed + 0.5 * U) / (Lambda * HLF)};
+  a.evec = {1, 0, 0, 1, 1};
+  f = Mat(); f.blk = a; f.blk.evec.clear();
+  const double f01[2] = {1.0, 0.0}, f10[2] = {0.0, -std::sqrt(2.0)};
+  f.push_block(0, 1, f01, 2); f.push_block(1, 0, f10, 2);
+  Mat nd, nd2, s2;
+  for (Mat* m : {&nd, &nd2, &s2}) { m->blk = a; m->blk.evec.clear(); }
+  nd.name = "Ndot"; nd2.name = "NdSq"; s2.name = "SdSq";
+  const double n0[4] = {0, 0, 0, 2}, n1[1] = {1}, q0[4] = {0, 0, 0, 4}, q1[1] = {1}, s0[4] = {0, 0, 0, 0},
+               s1[1] = {0.75};
+  nd.push_block(0, 0, n0, 4); nd.push_block(1, 1, n1, 1);
+  nd2.push_block(0, 0, q0, 4); nd2.push_block(1, 1, q1, 1);
+  s2.push_block(0, 0, s0, 4); s2.push_block(1, 1, s1, 1);
+  avg = {nd, nd2, s2};
 }
 
 // OneChQ_SetAnderson_Hm1 (Main/Main_SetH0.cpp:217-352): one quantum number,
@@ -1435,6 +1564,9 @@ void* oracle_run(const oracle_config* cfg) {
   // 667-720, 940-1000).  H_0 is the first site alone and only f_N is kept.
   const bool chain = cfg->chain != 0;
   if (chain && dm) { g_err = "chain and DM-NRG runs are exclusive"; delete R; return nullptr; }
+  if (chain && cfg->model == ORACLE_MODEL_1CHS) {
+    g_err = "the reference has no free-chain run for the (S) symmetry"; delete R; return nullptr;
+  }
   Arr eig;
   std::vector<Mat> mats;
   std::vector<double> P;
@@ -1510,6 +1642,19 @@ void* oracle_run(const oracle_config* cfg) {
     c.m.op_check = {C_Q_CD, C_Q_CD, C_DIAG, C_DIAG};
     P = {Lambda, chi1, 0.0, 0.0};
     totalS = false;
+  } else if (cfg->model == ORACLE_MODEL_1CHS) {
+    // SymNo 7, ModelNo 0, calcdens 0 (CodeHandler_ModelSwitch.cpp:1681-1814):
+    // fN (OneChS_fN_MatEl, OneChS_cd_check), n_d, n_d^2, S_d^2 averaged;
+    // CommonQNs = {1, 0, 0}, totSpos = {0}; ParamsHN = {Lambda, chi, e_N,
+    // Delta_SC} (NRG_main.cpp:264-276).
+    c.m.site = site_1chS(); c.m.totS = {0}; c.m.common = {1, 0, 0};
+    Mat f; std::vector<Mat> avg;
+    hm1_S(Lambda, HLF, cfg->U, cfg->ed, eig, f, avg);
+    mats.push_back(f); for (auto& x : avg) mats.push_back(x);
+    c.m.op_rule = {R_F_S, R_IMPONLY, R_IMPONLY, R_IMPONLY};
+    c.m.op_check = {C_S_CD, C_DIAG, C_DIAG, C_DIAG};
+    P = {Lambda, chi1, 0.0, cfg->gamma2_or_B};
+    sq = 0;
   } else if (cfg->model == ORACLE_MODEL_1CHQ) {
     // SymNo 3 (CodeHandler_ModelSwitch.cpp:1138-1200): f_up, f_dn (OneChQ_fN
     // rules, OneChQ_cd_check), S_z and S_z^2 averaged; CommonQNs = {1, 0, 0}.
@@ -1539,7 +1684,7 @@ void* oracle_run(const oracle_config* cfg) {
     else if (c.m.op_rule[i] == R_CD_QS) { mats[i].need_old = true; mats[i].calc_avg = false; }
     else { mats[i].need_old = false; mats[i].calc_avg = false; }
   }
-  R->nqn = cfg->model == ORACLE_MODEL_1CHQ ? 1 : 2;
+  R->nqn = (cfg->model == ORACLE_MODEL_1CHQ || cfg->model == ORACLE_MODEL_1CHS) ? 1 : 2;
   for (auto& m : mats) if (m.calc_avg) R->opnames.push_back(m.name);
   const double betabar = 0.727;
   Basis cut, ab;
@@ -1624,6 +1769,9 @@ void* oracle_run(const oracle_config* cfg) {
     for (auto& m : mats) if (m.calc_avg) I.opavg.push_back(calc_opavg(cut, m, betabar, totalS, sq));
     for (int b = 0; b < cut.nblocks(); ++b) I.kept_bsize.push_back(cut.bsize(b));
     for (int ich = 0; ich < nchan; ++ich) P[ich + 1] = chin(N);
+    // Delta_SC rescaled for the next iteration by CNRGchain::ScaleFactor(N)
+    // (NRG_main.cpp:414-419; NRGchainClass.cpp:187-202, z = 1)
+    if (cfg->model == ORACLE_MODEL_1CHS) P[3] = std::pow(Lambda, 0.5 * (double)N) / HLF * cfg->gamma2_or_B;
     R->it.push_back(std::move(I));
   }
   R->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

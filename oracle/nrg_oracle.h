@@ -9,6 +9,8 @@ extern "C" {
 #define ORACLE_MODEL_1CHQSZ 1 /* one-channel Anderson, (Q,Sz) basis */
 #define ORACLE_MODEL_2CHQS 2  /* two-channel Anderson, (Q,S) basis  */
 #define ORACLE_MODEL_1CHQ 3   /* one-channel Anderson, (Q) basis    */
+#define ORACLE_MODEL_1CHS 4   /* one-channel Anderson, superconducting leads, (S) basis;
+                                 gamma2_or_B carries Delta_SC */
 
 typedef struct {
   int model;          /* ORACLE_MODEL_* */

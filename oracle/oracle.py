@@ -16,8 +16,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 SO = os.path.join(HERE, "_build", "libnrg_oracle.so")
 
-MODEL_1CHQS, MODEL_1CHQSZ, MODEL_2CHQS, MODEL_1CHQ = 0, 1, 2, 3
-MODELS = {"1chQS": MODEL_1CHQS, "1chQSz": MODEL_1CHQSZ, "2chQS": MODEL_2CHQS, "1chQ": MODEL_1CHQ}
+MODEL_1CHQS, MODEL_1CHQSZ, MODEL_2CHQS, MODEL_1CHQ, MODEL_1CHS = 0, 1, 2, 3, 4
+MODELS = {"1chQS": MODEL_1CHQS, "1chQSz": MODEL_1CHQSZ, "2chQS": MODEL_2CHQS, "1chQ": MODEL_1CHQ,
+          "1chS": MODEL_1CHS}
 
 
 class _Cfg(ctypes.Structure):

@@ -11,6 +11,8 @@
 //   model: 1chQS   one-channel Anderson, (Q,S) basis   (ModelSwitch SymNo 0 / ModelNo 0)
 //          1chQSz  one-channel Anderson, (Q,Sz) basis  (SymNo 2 / ModelNo 0); last arg = B
 //          1chQ    one-channel Anderson, (Q) basis     (SymNo 3 / ModelNo 0)
+//          1chS    one-channel Anderson with superconducting leads, (S) basis
+//                  (SymNo 7 / ModelNo 0); last arg = Delta_SC
 //          2chQS   two-channel Anderson, (Q,S) basis: the impurity H_{-1} of
 //                  OneChQS_SetAnderson_Hm1 coupled to both channels through
 //                  TwoChQS_HN_MatEl with f_ch1 = f_ch2 = d; last arg = Gamma2
@@ -92,6 +94,7 @@ int main(int argc, char** argv) {
   bool totalS = true;
   int sqnumber = 1;
   int nchan = 1;
+  double deltaSC = 0.0;  // superconducting leads (1chS): rescaled every iteration
 
   CNRGmatrix aux;
   if (model == "1chQS") {
@@ -148,6 +151,32 @@ int main(int argc, char** argv) {
     ParamsHN = {Lambda, chi_m1, 0.0, 0.0};
     totalS = false;
     sqnumber = -1;  // NRGcodehandlerClass.cpp:762-765
+  } else if (model == "1chS") {
+    // CNRGCodeHandler::SetSingleSite, SymNo 7 (NRGcodehandlerClass.cpp:538-562)
+    SingleSite.NQNumbers = 2;
+    SingleSite.Nshell = 0;
+    SingleSite.totalS = true;
+    SingleSite.Sqnumbers.push_back(0);
+    SingleSite.QNumbers = {0.0, 0.0, 0.5, 0.5, 0.5, -0.5};
+    SingleSite.BlockBegEnd = {0, 1, 2, 2, 3, 3};
+    for (int ii = 0; ii < 4; ++ii) SingleSite.iType.push_back(ii);
+    // ModelSwitch SymNo 7, ModelNo 0, calcdens 0 (CodeHandler_ModelSwitch.cpp:1681-1814)
+    for (int i = 0; i < 4; ++i) Mats.push_back(aux);
+    Mats[0].NeedOld = false; Mats[0].UpperTriangular = false;
+    Mats[0].CheckForMatEl = OneChS_cd_check; Mats[0].CalcMatEl = OneChS_fN_MatEl;
+    CNRGmatrix avg; avg.NeedOld = true; avg.UpperTriangular = false; avg.CalcAvg = true;
+    avg.CheckForMatEl = Diag_check; avg.CalcMatEl = ImpOnly_MatEl;
+    Mats[1] = avg; Mats[2] = avg; Mats[3] = avg;
+    strcpy(Mats[1].MatName, "Ndot"); strcpy(Mats[2].MatName, "NdSq"); strcpy(Mats[3].MatName, "SdSq");
+    std::vector<double> P = {Lambda, HalfLambdaFactor, U, ed};
+    OneChS_SetAnderson_Hm1(P, &Aeig, Mats);
+    CommonQNs = {1, 0, 0}; totSpos = {0};
+    HN.CalcHNMatEl = OneChS_HNsc_MatEl;
+    double chi_m1 = sqrt(2.0 * Gamma1 / pi) / (sqrt(Lambda) * HalfLambdaFactor) * ALambda;
+    ParamsHN = {Lambda, chi_m1, 0.0, extra};  // e_N, Delta_SC (NRG_main.cpp:264-276)
+    totalS = true;
+    sqnumber = 0;  // NRGcodehandlerClass.cpp:774-777
+    deltaSC = extra;
   } else if (model == "2chQS") {
     TwoChQS_SetSingleSite(&SingleSite);
     // Impurity H_{-1} and its reduced <||d||> from the one-channel set-up.
@@ -219,6 +248,7 @@ int main(int argc, char** argv) {
     for (int b = 0; b < AeigCut.NumBlocks(); ++b) printf(" %d", AeigCut.GetBlockSize(b));
     printf("\n");
     for (int ich = 0; ich < nchan; ++ich) ParamsHN[ich + 1] = chain.GetChin(N);  // NRG_main.cpp:402-405
+    if (model == "1chS") ParamsHN[nchan + 2] = chain.ScaleFactor(N) * deltaSC;  // NRG_main.cpp:414-419
   }
   fflush(stdout);
   return 0;

@@ -38,6 +38,9 @@ CASES = {
     "small_2chQS_n5_k60": ("2chQS", 5, 60, 2.5, 0.3, -0.15, 0.01, 0.01),
     # One-channel Anderson in the charge-only |Q> basis (SymNo 3).
     "q_1chQ_n12_k200": ("1chQ", 12, 200, 2.5, 0.5, -0.25, 0.02, 0.0),
+    # One-channel Anderson with superconducting leads in the |S> basis
+    # (SymNo 7), Delta_SC = 0.01.
+    "s_1chS_n12_k200": ("1chS", 12, 200, 2.5, 0.5, -0.25, 0.02, 0.01),
 }
 
 

@@ -19,13 +19,15 @@ EIG_TOL = 1e-10
 OBS_TOL = 1e-8
 
 
-def compare(gpu, ref, niters=None):
+def compare(gpu, ref, model=""):
     assert len(gpu.iters) == len(ref.iters)
     for n, (a, b) in enumerate(zip(gpu.iters, ref.iters)):
-        # |Q> blocks: the engine reports (Q, 0), the reference Q alone
+        # one-quantum-number blocks: the engine reports |Q> as (Q, 0) and |S>
+        # as (0, S), the reference the one number
         nq = b.qn.shape[1]
-        np.testing.assert_array_equal(a.qn[:, :nq], b.qn, err_msg=f"N={n} sectors")
-        assert not a.qn[:, nq:].any()
+        qa = a.qn[:, ::-1] if model == "1chS" else a.qn
+        np.testing.assert_array_equal(qa[:, :nq], b.qn, err_msg=f"N={n} sectors")
+        assert not qa[:, nq:].any()
         np.testing.assert_array_equal(a.bsize, b.bsize, err_msg=f"N={n} block sizes")
         assert a.nkept == b.nkept, f"N={n} Nkept {a.nkept} != {b.nkept}"
         np.testing.assert_array_equal(a.kept_bsize, b.kept_bsize, err_msg=f"N={n} kept blocks")
@@ -45,6 +47,7 @@ CASES = [
     ("2chQS", 5, 80, 2.5, 0.3, -0.15, 0.01, 0.01),
     ("2chQS", 4, 40, 2.5, 0.3, -0.15, 0.01, 0.02),
     ("1chQ", 12, 150, 2.5, 0.4, -0.2, 0.015, 0.0),
+    ("1chS", 12, 150, 2.5, 0.4, -0.2, 0.015, 0.02),
 ]
 
 
@@ -52,12 +55,12 @@ CASES = [
 def test_sweep_matches_oracle(engine, case):
     g = engine.sweep(*case)
     o = orc.run(*case, nthreads=min(8, os.cpu_count() or 1))
-    compare(g, o)
+    compare(g, o, case[0])
     np.testing.assert_allclose(g.opavg_m1, o.opavg_m1, rtol=1e-15)
 
 
 @pytest.mark.parametrize("name", ["cfg0_1chQS_n40_k500", "qsz_1chQSz_n14_k300", "cfg1_2chQS_n8_k300",
-                                  "q_1chQ_n12_k200"])
+                                  "q_1chQ_n12_k200", "s_1chS_n12_k200"])
 def test_sweep_matches_reference_fixture(engine, name):
     g = np.load(os.path.join(GOLD, name + ".npz"))
     model, ns, nc, lam, U, ed, g1, x = g["config"]
@@ -74,7 +77,7 @@ def test_sweep_matches_reference_fixture(engine, name):
         it.nkept, it.ecut = int(g[f"nkept_{n}"]), float(g[f"ecut_{n}"])
         it.kept_bsize, it.thermo, it.opavg = g[f"kept_bsize_{n}"], g[f"thermo_{n}"], g[f"opavg_{n}"]
         Ref.iters.append(it)
-    compare(r, Ref)
+    compare(r, Ref, str(model))
 
 
 def test_kernels_launched(engine):

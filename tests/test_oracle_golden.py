@@ -13,7 +13,7 @@ from oracle import oracle as orc
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
 CASES = ["run1_1chQS", "small_2chQS_n5_k60", "qsz_1chQSz_n14_k300", "cfg1_2chQS_n8_k300",
-         "cfg0_1chQS_n40_k500", "q_1chQ_n12_k200"]
+         "cfg0_1chQS_n40_k500", "q_1chQ_n12_k200", "s_1chS_n12_k200"]
 
 
 def _run(name, **kw):

@@ -19,8 +19,9 @@ from . import build as _build
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = _build.LIB
 
-MODEL_1CH_QS, MODEL_1CH_QSZ, MODEL_2CH_QS, MODEL_1CH_Q = 0, 1, 2, 3
-MODELS = {"1chQS": MODEL_1CH_QS, "1chQSz": MODEL_1CH_QSZ, "2chQS": MODEL_2CH_QS, "1chQ": MODEL_1CH_Q}
+MODEL_1CH_QS, MODEL_1CH_QSZ, MODEL_2CH_QS, MODEL_1CH_Q, MODEL_1CH_S = 0, 1, 2, 3, 4
+MODELS = {"1chQS": MODEL_1CH_QS, "1chQSz": MODEL_1CH_QSZ, "2chQS": MODEL_2CH_QS, "1chQ": MODEL_1CH_Q,
+          "1chS": MODEL_1CH_S}
 PREC_FP64 = 0
 
 STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "out of memory", 4: "not converged",

@@ -125,7 +125,7 @@ struct nrg_ctx {
   std::vector<double> opavg_m1;
   nrg_timing timing{};
   // device buffers
-  nrg::DevBuf meta, vmeta, H, d, e, tau, ev, en, flag, scal, Y, scratch, Z, Zt, T, partial, red, gpart;
+  nrg::DevBuf meta, vmeta, H, d, e, tau, ev, en, flag, scal, Y, scratch, Z, Zt, T, partial, red, gpart, fde;
   nrg::DevBuf ops_a[6], ops_b[6], opptr;
   cudaEvent_t ev_a[8];
   // concurrent whole-GPU tridiagonalizations: side streams, fork/join events,
@@ -377,9 +377,11 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
   TdEigArgs ea{};
   ea.nblocks = nb; ea.bsize = d_bsize; ea.soff = d_soff; ea.d = c->d.as<double>(); ea.e = c->e.as<double>();
   ea.ev = c->ev.as<double>(); ea.nstates = P.nstates; ea.flag = c->flag.as<int>(); ea.maxn = std::max(P.maxn, 1);
+  c->fde.ensure(sizeof(float) * 2 * std::max(P.nstates, 1));
+  ea.fde = c->fde.as<float>();
   cudaEvent_t t1 = tm.start();
   launch_bisect(ea, d_state_block, c->stream);
-  c->launches += 2;
+  c->launches += 3;  // FP32 copies, levels, ordering
   tm.stop(t1, &c->timing.tridiag_eig_ms);
 }
 
@@ -525,7 +527,7 @@ AsmTables prepare_assembly(nrg_ctx* c, const ModelSpec& m, const Basis& B, const
                            const std::vector<double>& st_eold, const std::vector<OpMeta>& oldops,
                            const std::vector<int>& old_size, int nops_h, const std::vector<const double*>& hops,
                            double lambda, const double chi[2], double eN,
-                           const std::vector<int>* opblock = nullptr) {
+                           const std::vector<int>* opblock = nullptr, double delta = 0.0) {
   auto ob = [&](int k) { return opblock ? (*opblock)[k] : k; };
   AsmTables T;
   EigPlan& P = T.P;
@@ -563,12 +565,27 @@ AsmTables prepare_assembly(nrg_ctx* c, const ModelSpec& m, const Basis& B, const
   }
   std::vector<double> site_q(m.site.nstates);
   for (int t = 0; t < m.site.nstates; ++t) site_q[t] = m.site.blk.q(m.site.block_of_state(t), 0);
+  // |S> model: the e_N term counts the site's electrons, {0, 2, 1, 1}
+  // (OneChS_HNsc_MatEl's auxN); pairing and h.c.-switch tables
+  const int NT = m.site.nstates;
+  std::vector<double> sc_pair(NT * NT, 0.0);
+  std::vector<int> hc_sw(NT * NT, 0), st_old(P.nstates, 0);
+  if (m.kind == MODEL_1CHS) {
+    site_q = {-1.0, 1.0, 0.0, 0.0};
+    for (int a = 0; a < NT; ++a)
+      for (int b2 = 0; b2 < NT; ++b2) {
+        sc_pair[a * NT + b2] = sc_pair_1chS(a, b2);
+        hc_sw[a * NT + b2] = hc_switch_1chS(a, b2) ? 1 : 0;
+      }
+    for (int g = 0; g < P.nstates; ++g) st_old[g] = B.stcf[g];
+  }
   Packer pk;
   T.o_bsize = pk.add(P.bsize); T.o_soff = pk.add(P.soff); T.o_hoff = pk.add(P.hoff); T.o_order = pk.add(T.order);
   T.o_sb = pk.add(state_block); T.o_ri = pk.add(row_index);
   size_t o_seg = pk.add(st_seg), o_a = pk.add(st_a), o_type = pk.add(st_type), o_eold = pk.add(st_eold),
          o_nseg = pk.add(nseg), o_pb = pk.add(pair_base), o_pf = pk.add(pair_fwd), o_pfl = pk.add(pair_fwd_ld),
-         o_pbw = pk.add(pair_bwd), o_pbl = pk.add(pair_bwd_ld), o_coef = pk.add(tabs.coef), o_sq = pk.add(site_q);
+         o_pbw = pk.add(pair_bwd), o_pbl = pk.add(pair_bwd_ld), o_coef = pk.add(tabs.coef), o_sq = pk.add(site_q),
+         o_scp = pk.add(sc_pair), o_hcs = pk.add(hc_sw), o_sto = pk.add(st_old);
   T.o_bq = pk.add(B.blk.qn);
   c->meta.ensure(pk.host.size() + 256);
   h2d(c, c->meta.p, pk.host.data(), pk.host.size());
@@ -595,6 +612,8 @@ AsmTables prepare_assembly(nrg_ctx* c, const ModelSpec& m, const Basis& B, const
   aa.nops_h = nops_h; aa.model = m.kind == MODEL_1CHQ ? (int)MODEL_1CHQSZ : (int)m.kind; aa.ops = (const double* const*)c->opptr.p;
   aa.sqrt_lambda = std::sqrt(lambda); aa.eN = eN; aa.chi[0] = chi[0]; aa.chi[1] = chi[1];
   aa.site_q = (const double*)(mb + o_sq); aa.H = c->H.as<double>();
+  aa.sc_pair = (const double*)(mb + o_scp); aa.hc_switch = (const int*)(mb + o_hcs);
+  aa.st_old = (const int*)(mb + o_sto); aa.delta = delta;
   return T;
 }
 
@@ -737,7 +756,9 @@ void launch_update_plan(nrg_ctx* c, Timer& tm, UpdatePlan& U) {
 void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool chain = false) {
   using clock = std::chrono::steady_clock;
   auto t_begin = clock::now();
-  if (cfg->model < 0 || cfg->model > 3) throw NrgError(NRG_ERR_ARG, "unknown model");
+  if (cfg->model < 0 || cfg->model > 4) throw NrgError(NRG_ERR_ARG, "unknown model");
+  if (chain && cfg->model == NRG_MODEL_1CH_S)
+    throw NrgError(NRG_ERR_ARG, "the reference has no free-chain run for the |S> symmetry");
   if (dm && cfg->model != NRG_MODEL_1CH_QS)
     throw NrgError(NRG_ERR_ARG, "DM-NRG shells are available for the one-channel |Q S> model");
   if (cfg->nsites < 1 || cfg->ncutoff < 4 || !(cfg->lambda > 1.0)) throw NrgError(NRG_ERR_ARG, "bad sweep parameters");
@@ -751,7 +772,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
   S.m = make_model((ModelKind)cfg->model);
   S.cfg = *cfg;
   if (chain) {
-    const int nf = S.m.kind == MODEL_1CHQS ? 1 : 2;
+    const int nf = (S.m.kind == MODEL_1CHQS || S.m.kind == MODEL_1CHS) ? 1 : 2;
     S.m.op_kind.resize(nf); S.m.op_check.resize(nf); S.m.op_name.resize(nf); S.m.op_avg.resize(nf);
   }
   if (dm) {
@@ -769,7 +790,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
   const double HLF = 0.5 * (1.0 + 1.0 / lambda);
   const double betabar = 0.727;
   const int nops = (int)m.op_kind.size();
-  const int nops_h = m.kind == MODEL_1CHQS ? 1 : 2;  // old operators entering H_N
+  const int nops_h = (m.kind == MODEL_1CHQS || m.kind == MODEL_1CHS) ? 1 : 2;  // old operators entering H_N
   Timer tm(c);
   cudaEvent_t span0, span1;
   CU(cudaEventCreate(&span0));
@@ -838,9 +859,15 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
     N0 = 1;
   }
 
+  // |S> model with superconducting leads: Delta_SC enters H_N unscaled at
+  // N = 0 and as ScaleFactor(N-1) * Delta_SC = Lambda^((N-1)/2) / HLF *
+  // Delta_SC after that (NRG_main.cpp:220-227, 276, 414-419).
+  const bool sc = m.kind == MODEL_1CHS;
   for (int N = N0; N < cfg->nsites; ++N) {
     IterResult R;
-    R.params = {lambda, chi[0], chi[1], eN};
+    const double delta = !sc ? 0.0 : (N == 0 ? cfg->gamma2_or_B
+                                             : std::pow(lambda, 0.5 * (double)(N - 1)) / HLF * cfg->gamma2_or_B);
+    R.params = {lambda, chi[0], sc ? delta : chi[1], eN};
     const double DN = HLF * std::pow(lambda, (-(N - 1) / 2.0));
     // ---------------- BuildBasis + tables (host)
     Basis B;
@@ -853,7 +880,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
     std::vector<const double*> hops(8, nullptr);
     for (int o = 0; o < nops; ++o) hops[o] = S.opbuf(S.cur, o)->as<double>();
     AsmTables AT = prepare_assembly(c, m, B, tabs, st_eold, S.ops, opsize, nops_h, hops, lambda, chi, eN,
-                                    opblock.empty() ? nullptr : &opblock);
+                                    opblock.empty() ? nullptr : &opblock, delta);
     EigPlan& P = AT.P;
     std::vector<int>& order = AT.order;
     char* mb = c->meta.as<char>();

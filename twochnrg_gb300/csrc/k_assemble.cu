@@ -46,7 +46,21 @@ __global__ void __launch_bounds__(256) assemble_kernel(AssembleArgs A, const int
       const int ti = A.st_type[gi], tj = A.st_type[gj];
       const int64_t pt = A.pair_base[b] + ((int64_t)p * nseg + q) * A.nops_h;
       const double* cij = coef + ((size_t)ti * NT + tj) * NO * 2;
-      if (A.model == 0) {
+      if (A.model == 4) {
+        if (A.st_old[gi] == A.st_old[gj]) {
+          // OneChS_HNsc_MatEl: the lead's pairing term on the new site
+          v = __dsub_rn(__dsub_rn(0.0, __dmul_rn(A.delta, A.sc_pair[ti * NT + tj])),
+                        __dmul_rn(A.delta, A.sc_pair[tj * NT + ti]));
+        } else {
+          double old = old_element(A.ops[0], A.pair_fwd[pt], A.pair_fwd_ld[pt], ai, aj);
+          int dir = 0;
+          if (fabs(old) < 1.e-20 || A.hc_switch[ti * NT + tj]) {
+            old = old_element(A.ops[0], A.pair_bwd[pt], A.pair_bwd_ld[pt], aj, ai);
+            dir = 1;
+          }
+          v = __dmul_rn(__dmul_rn(A.chi[0], old), cij[dir]);
+        }
+      } else if (A.model == 0) {
         // ((chi_N*OldEl)*CoefMatEl)*FermiSign, FermiSign folded into the table.
         double old = old_element(A.ops[0], A.pair_fwd[pt], A.pair_fwd_ld[pt], ai, aj);
         int dir = 0;

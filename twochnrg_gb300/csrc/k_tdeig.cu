@@ -34,14 +34,16 @@ __device__ __forceinline__ int sturm_count(const double* d, const double* e, int
   return cnt;
 }
 
-__device__ __forceinline__ int sturm_count_f32(const double* d, const double* e, int n, float x, float pivmin) {
+// FP32 Sturm count over FP32 copies of d and e, made once per call (a
+// double-to-float conversion in the pass itself would run on the FP64 pipe).
+__device__ __forceinline__ int sturm_count_f32(const float* d, const float* e, int n, float x, float pivmin) {
   int cnt = 0;
-  float q = (float)d[0] - x;
+  float q = d[0] - x;
   if (fabsf(q) < pivmin) q = -pivmin;
   if (q < 0.0f) cnt++;
   for (int i = 1; i < n; ++i) {
-    const float ei = (float)e[i - 1];
-    q = ((float)d[i] - x) - __fdividef(ei * ei, q);
+    const float ei = e[i - 1];
+    q = (d[i] - x) - __fdividef(ei * ei, q);
     if (fabsf(q) < pivmin) q = -pivmin;
     if (q < 0.0f) cnt++;
   }
@@ -139,6 +141,8 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
   const int k = pos - s0;
   const double* d = db + s0;
   const double* e = eb + s0;
+  const float* fd32 = A.fde + so + s0;
+  const float* fe32 = A.fde + A.nstates + so + s0;
   if (n == 1) {
     if (!isfinite(d[0])) atomicOr(A.flag, DEV_BAD_INPUT);
     A.ev[g] = d[0];
@@ -148,8 +152,8 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
   // the bracket.
   float fgl = FLT_MAX, fgu = -FLT_MAX, femax = 0.0f;
   for (int i = 0; i < n; ++i) {
-    const float fe0 = i > 0 ? fabsf((float)e[i - 1]) : 0.0f, fe1 = i + 1 < n ? fabsf((float)e[i]) : 0.0f;
-    const float fd = (float)d[i];
+    const float fe0 = i > 0 ? fabsf(fe32[i - 1]) : 0.0f, fe1 = i + 1 < n ? fabsf(fe32[i]) : 0.0f;
+    const float fd = fd32[i];
     fgl = fminf(fgl, fd - (fe0 + fe1));
     fgu = fmaxf(fgu, fd + (fe0 + fe1));
     femax = fmaxf(femax, fe1);
@@ -167,7 +171,7 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
     const float fpiv = 1e-30f;
     for (int it = 0; it < 40 && (fhi - flo) > 1e-6f * (float)tnorm; ++it) {
       const float mid = 0.5f * (flo + fhi);
-      if (sturm_count_f32(d, e, n, mid, fpiv) > k) fhi = mid; else flo = mid;
+      if (sturm_count_f32(fd32, fe32, n, mid, fpiv) > k) fhi = mid; else flo = mid;
     }
     const double margin = 1e-5 * tnorm;
     const double tlo = (double)flo - margin, thi = (double)fhi + margin;
@@ -470,8 +474,17 @@ __global__ void __launch_bounds__(kBackWarps * 32) backtransform_kernel(BackArgs
 
 }  // namespace
 
+__global__ void to_f32_kernel(const double* d, const double* e, float* out, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    out[i] = (float)d[i];
+    out[n + i] = (float)e[i];
+  }
+}
+
 void launch_bisect(const TdEigArgs& a, const int* state_block, cudaStream_t s) {
   if (a.nstates <= 0) return;
+  to_f32_kernel<<<(a.nstates + 255) / 256 < 1024 ? (a.nstates + 255) / 256 : 1024, 256, 0, s>>>(a.d, a.e, a.fde,
+                                                                                                a.nstates);
   // One warp per CTA: the long-running threads of the largest blocks then
   // spread over all SMs instead of crowding a few.
   bisect_kernel<<<(a.nstates + 31) / 32, 32, 0, s>>>(a, state_block);

@@ -57,6 +57,12 @@ struct AssembleArgs {
   double chi[2];
   const double* site_q;      // [ntypes] site charge Q~ of each type
   double* H;
+  // superconducting-lead |S> model (model 4): old state of every state, the
+  // pairing table and the hopping's h.c. switch per type pair, Delta_N
+  const int* st_old;
+  const double* sc_pair;     // [ntypes^2]
+  const int* hc_switch;      // [ntypes^2]
+  double delta;
 };
 void launch_assemble(const AssembleArgs& a, int64_t total_rows, const int* row_block,
                      const int* row_index, cudaStream_t s);
@@ -96,6 +102,7 @@ struct TdEigArgs {
   int nstates;
   int* flag;
   int maxn;              // largest block (sizes the sort's shared memory)
+  float* fde;            // scratch [2*nstates]: FP32 copies of d and e for the FP32 bracket
 };
 void launch_bisect(const TdEigArgs& a, const int* state_block, cudaStream_t s);
 

@@ -33,6 +33,14 @@ double fd_onech(int sigma, int ti, int tj) {
   return 0.0;
 }
 
+// OneChS_fd_table (OpTables.cpp:419-443): <t_i| f^dagger_sigma |t_j> in the
+// basis |0>, |up dn>, |up>, |dn> of the superconducting-lead site.
+double fd_onechS(int sigma, int ti, int tj) {
+  if (sigma == 1) return ((ti == 2 && tj == 0) || (ti == 1 && tj == 3)) ? 1.0 : 0.0;
+  if (sigma == -1) { if (ti == 3 && tj == 0) return 1.0; if (ti == 1 && tj == 2) return -1.0; }
+  return 0.0;
+}
+
 // TwoChQS_fd_table (TwoChQS_OpTables.cpp:20-130): the reference's table of
 // f^dagger_{ch,sigma} in the 16-state two-channel site basis.
 struct TwoChTables {
@@ -167,6 +175,17 @@ ModelSpec make_model(ModelKind kind) {
     m.op_kind = {OP_FUP_QSZ, OP_FDN_QSZ, OP_IMPONLY, OP_IMPONLY};
     m.op_check = {CHK_Q_CD, CHK_Q_CD, CHK_DIAG, CHK_DIAG};
     m.op_name = {"fNup", "fNdn", "Sz", "Sz2"};
+  } else if (kind == MODEL_1CHS) {
+    // CNRGCodeHandler::SetSingleSite, SymNo 7 (NRGcodehandlerClass.cpp:536-560):
+    // (S,Sz) blocks |0>,|up dn> | |up> | |dn> (types 0..3), here (0,S,Sz).
+    m.site.blk.nqn = 3;
+    site_block(m.site, {0, 0, 0}, 2); site_block(m.site, {0, 0.5, 0.5}, 1); site_block(m.site, {0, 0.5, -0.5}, 1);
+    m.totalS = true; m.nchan = 1; m.nsigma = 1;
+    // CodeHandler_ModelSwitch.cpp:1699-1721 (calcdens 0): fN, and n_d, n_d^2,
+    // S_d^2 averaged.
+    m.op_kind = {OP_F_S, OP_IMPONLY, OP_IMPONLY, OP_IMPONLY};
+    m.op_check = {CHK_S_CD, CHK_DIAG, CHK_DIAG, CHK_DIAG};
+    m.op_name = {"fN", "Ndot", "NdSq", "SdSq"};
   } else if (kind == MODEL_2CHQS) {
     // TwoChQS_SetSingleSite (TwoChQS_SetSingleSite.cpp:5-124): 16 states in 10 blocks.
     m.site.blk.nqn = 3;
@@ -222,6 +241,23 @@ StartState make_start(const ModelSpec& m, double lambda, double U, double ed, do
     s.ops.push_back(f);
     if (m.kind == MODEL_2CHQS) s.ops.push_back(f);  // f_ch1 = f_ch2 = d
     s.ops.push_back(o1); s.ops.push_back(o2); s.ops.push_back(o3);
+  } else if (m.kind == MODEL_1CHS) {
+    // OneChS_SetAnderson_Hm1 (Main/Main_SetH0.cpp:2618-2700): blocks S = 0
+    // (|0>, |up dn>) and S = 1/2; reduced <||f||> between them; n_d, n_d^2,
+    // S^2 diagonal.
+    const double q[2][2] = {{0, 0}, {0, 0.5}};
+    s.blk.push(q[0], 2); s.blk.push(q[1], 1);
+    s.en = {0.5 * U / scale, (2.0 * ed + 1.5 * U) / scale, (ed + 0.5 * U) / scale};
+    OpBlocks f, nd, nd2, s2;
+    auto pair = [](OpBlocks& o, int i, int j, std::initializer_list<double> v) {
+      o.bi.push_back(i); o.bj.push_back(j); o.off.push_back((int64_t)o.el.size());
+      o.el.insert(o.el.end(), v);
+    };
+    pair(f, 0, 1, {1.0, 0.0}); pair(f, 1, 0, {0.0, -std::sqrt(2.0)});
+    pair(nd, 0, 0, {0.0, 0.0, 0.0, 2.0}); pair(nd, 1, 1, {1.0});
+    pair(nd2, 0, 0, {0.0, 0.0, 0.0, 4.0}); pair(nd2, 1, 1, {1.0});
+    pair(s2, 0, 0, {0.0, 0.0, 0.0, 0.0}); pair(s2, 1, 1, {0.75});
+    s.ops = {f, nd, nd2, s2};
   } else if (m.kind == MODEL_1CHQ) {
     // OneChQ_SetAnderson_Hm1 (Main/Main_SetH0.cpp:217-352): |0> | |up>,|dn> |
     // |up dn> by Q, the Q = 0 block two-fold; f_up, f_dn not reduced; S_z and
@@ -413,6 +449,38 @@ double hn_full_2chQS(const Site& st, double Si, int typep, int type, int ich, in
 }
 }  // namespace
 
+// Hopping coefficient of OneChS_HNsc_MatEl (OpMatRules.cpp:1846-1998) for
+// the site pair (typep, type) in a new multiplet of spin Si, times its
+// fermion sign.  A spin-1/2 site state is looked up as (its site block) + 1,
+// which is its type, and as type 0 when no block has the wanted (S, Sz) --
+// the reference's lookup, kept.
+double hn_coef_1chS(const Site& st, double Si, int typep, int type) {
+  const BlockArray& ss = st.blk;
+  auto q = [&](int t, int k) { return ss.q(st.block_of_state(t), k); };
+  auto lookup = [&](double S, double Sz) { const double x[3] = {0.0, S, Sz}; return ss.find(x) + 1; };
+  const double Stildep = q(typep, 1), Sztp0 = q(typep, 2);
+  const double Stilde = q(type, 1), Szt0 = q(type, 2);
+  const double Scfp = Si - Sztp0, Scf = Si - Szt0;
+  const double fermi = (type == 2 || type == 3) ? -1.0 : 1.0;
+  double coef = 0.0;
+  for (double Sztilde = -Stilde; Sztilde <= Stilde; Sztilde += 1.0) {
+    int sitestate = type;
+    if (type == 2 || type == 3) sitestate = lookup(Stilde, Sztilde);
+    for (int sigma = -1; sigma <= 1; sigma += 2) {
+      const double dS = 0.5 * (double)sigma;
+      const double Szcf = Si - Sztilde, Szcfp = Szcf - dS, Sztildep = Sztilde + dS;
+      int sitestatep = lookup(Stildep, Sztildep);
+      if (deq(Sztildep, 0.0)) sitestatep = typep;
+      const double a0 = cg(Scf, Szcf, Stilde, Sztilde, Si, Si);
+      const double a1 = cg(Scfp, Szcfp, Stildep, Sztildep, Si, Si);
+      const double a2 = cg(Scfp, Szcfp, 0.5, dS, Scf, Szcf);
+      const double a3 = fd_onechS(sigma, sitestatep, sitestate);
+      coef += a0 * a1 * a2 * a3;
+    }
+  }
+  return coef * fermi;  // fermi = +-1: multiplying here or after chi*old is exact
+}
+
 void build_hn_tables(const ModelSpec& m, const Basis& b, HNTables& t) {
   int NT = m.site.nstates;
   t.ntypes = NT; t.nchan = m.nchan; t.nsigma = m.nsigma;
@@ -431,6 +499,9 @@ void build_hn_tables(const ModelSpec& m, const Basis& b, HNTables& t) {
         if (m.kind == MODEL_1CHQS) {
           c[base * 2 + 0] = hn_coef_1chQS(m.site, Si, ti, tj);
           c[base * 2 + 1] = hn_coef_1chQS(m.site, Si, tj, ti);
+        } else if (m.kind == MODEL_1CHS) {
+          c[base * 2 + 0] = hn_coef_1chS(m.site, Si, ti, tj);
+          c[base * 2 + 1] = hn_coef_1chS(m.site, Si, tj, ti);
         } else if (m.kind == MODEL_1CHQSZ || m.kind == MODEL_1CHQ) {
           // OneChQSz_HN_MatEl (OpMatRules.cpp:468-531), OneChQ_HN_MatEl
           // (:1065-1147): per spin, the fermion sign of the "type" state times
@@ -455,8 +526,32 @@ void build_hn_tables(const ModelSpec& m, const Basis& b, HNTables& t) {
   }
 }
 
+double sc_pair_1chS(int ti, int tj) { return (ti == 1 && tj == 0) ? 1.0 : 0.0; }
+bool hc_switch_1chS(int ti, int tj) { return fd_onechS(1, ti, tj) == 0.0 && fd_onechS(-1, ti, tj) == 0.0; }
+
 double op_site_factor(const ModelSpec& m, int op, double Si, double Sj, int ti, int tj) {
   const BlockArray& ss = m.site.blk;
+  if (op == OP_F_S) {
+    // OneChS_fN_MatEl (OpMatRules.cpp:1555-1654), with its site lookups.
+    auto q = [&](int t, int k) { return ss.q(m.site.block_of_state(t), k); };
+    auto lookup = [&](double S, double Sz) { const double x[3] = {0.0, S, Sz}; return ss.find(x) + 1; };
+    const double Stildei = q(ti, 1), Stildej = q(tj, 1);
+    const double Scfi = Si - q(ti, 2), Scfj = Sj - q(tj, 2);
+    const double sigma = Sj - Si;
+    double aux = 0.0, cg1 = 0.0;
+    for (double Sztj = -Stildej; Sztj <= Stildej; Sztj += 1.0) {
+      int ssj = tj, ssi = ti;
+      if (tj == 2 || tj == 3) ssj = lookup(Stildej, Sztj);
+      if (ti == 2 || ti == 3) ssi = lookup(Stildei, Sztj - sigma);
+      const double cg0 = cg(Scfi, Si - Sztj + sigma, Stildei, Sztj - sigma, Si, Si);
+      cg1 = cg(Scfj, Sj - Sztj, Stildej, Sztj, Sj, Sj);
+      aux += fd_onechS((int)(sigma / 0.5), ssj, ssi) * cg0 * cg1;
+    }
+    const double n0 = cg(Si, Si, 0.5, sigma, Sj, Sj);
+    if (!deq(n0, 0.0)) return aux / n0;
+    if (!deq(cg1, 0.0)) return 0.0 / cg1;
+    return 0.0;
+  }
   if (op == OP_FUP_QSZ) return fd_onech(1, tj, ti);   // OneChQ_fN_MatEl (OpMatRules.cpp:1003-1033)
   if (op == OP_FDN_QSZ) return fd_onech(-1, tj, ti);
   if (op == OP_IMPONLY) return ti == tj ? 1.0 : 0.0;
@@ -536,10 +631,12 @@ double op_site_factor(const ModelSpec& m, int op, double Si, double Sj, int ti, 
 }
 
 bool op_check(int chk, const BlockArray& a, int i, int j) {
+  // OneChS_cd_check (OpMatRules.cpp:172, S in the second slot here),
   // Diag_check (OpMatRules.cpp:12), OneChQS_cd_check (:106), OneChQ_cd_check
   // (:92), TwoChQS_cd_check (TwoChQS_OpMatRules.cpp:16).
   switch (chk) {
     case CHK_DIAG: return i == j;
+    case CHK_S_CD: return deq(a.q(j, 1), a.q(i, 1) + 0.5) || deq(a.q(j, 1), a.q(i, 1) - 0.5);
     case CHK_Q_CD: return deq(a.q(j, 0), a.q(i, 0) + 1.0);
     case CHK_QS_CD:
     case CHK_2CH_CD:

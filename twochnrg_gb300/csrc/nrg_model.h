@@ -18,7 +18,11 @@ namespace nrg {
 // MODEL_1CHQ (SymNo 3) conserves the charge only; its blocks carry the
 // reference's single quantum number Q plus a constant 0 in the second slot,
 // which leaves BuildBasis's block and state order unchanged.
-enum ModelKind { MODEL_1CHQS = 0, MODEL_1CHQSZ = 1, MODEL_2CHQS = 2, MODEL_1CHQ = 3 };
+//
+// MODEL_1CHS (SymNo 7, superconducting leads) conserves the total spin only;
+// its blocks carry a constant 0 in the charge slot and S in the second, so
+// that every SU(2) rule reads S where it does for (Q,S).
+enum ModelKind { MODEL_1CHQS = 0, MODEL_1CHQSZ = 1, MODEL_2CHQS = 2, MODEL_1CHQ = 3, MODEL_1CHS = 4 };
 
 // Operator rule ids (how the operator acts on a new site; see build_op_terms).
 enum OpKind {
@@ -29,9 +33,10 @@ enum OpKind {
   OP_F2_2CH = 5,    // TwoChQS_fNch2_MatEl   (TwoChQS_OpMatRules.cpp:1362)
   OP_IMPONLY = 6,   // ImpOnly_MatEl x old   (OpMatRules.cpp:265)
   OP_CD_QS = 7,     // OneChQS_cd_MatEl x old (OpMatRules.cpp:1249)
+  OP_F_S = 8,       // OneChS_fN_MatEl       (OpMatRules.cpp:1555)
 };
 // CheckForMatEl rule ids.
-enum CheckKind { CHK_DIAG = 1, CHK_QS_CD = 2, CHK_Q_CD = 3, CHK_2CH_CD = 4 };
+enum CheckKind { CHK_DIAG = 1, CHK_QS_CD = 2, CHK_Q_CD = 3, CHK_2CH_CD = 4, CHK_S_CD = 5 };
 
 // Block-structured array: the common part of CNRGarray / CNRGbasisarray
 // (include/NRGclasses.hpp:47-349).
@@ -126,6 +131,14 @@ void build_hn_tables(const ModelSpec& m, const Basis& b, HNTables& t);
 // impurity operators (OP_IMPONLY, OP_CD_QS) g multiplies the old operator
 // element between the states they came from.
 double op_site_factor(const ModelSpec& m, int op, double Si, double Sj, int ti, int tj);
+
+// Superconducting-lead |S> model (OneChS_HNsc_MatEl, OpMatRules.cpp:1794-2003):
+// the pairing table <t_i| f^dagger_up f^dagger_dn |t_j> (OneChS_fdupfddn_table,
+// OpTables.cpp:447-462), and whether the hopping term reads the old operator
+// as (stcf_j, stcf_i) whatever its (stcf_i, stcf_j) element (both
+// OneChS_fd_table(+-1, t_i, t_j) vanish).
+double sc_pair_1chS(int ti, int tj);
+bool hc_switch_1chS(int ti, int tj);
 bool op_check(int chk, const BlockArray& kept, int i, int j);
 
 // Clebsch-Gordan <J1 M1; J2 M2 | J M>  (CGordan.cpp:34-120).
