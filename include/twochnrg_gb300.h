@@ -58,10 +58,13 @@ typedef enum {
                             averaged operators are S_z and S_z^2; the reference takes
                             only the entropy for this symmetry, and the T chi slot of
                             nrg_iteration.thermo is 0 */
-  NRG_MODEL_1CH_S = 4    /* one-channel Anderson with superconducting leads, |S> basis
-                            (SymNo 7, ModelNo 0); whole sweeps only.  gamma2_or_B carries
-                            Delta_SC; blocks are reported as (0, S); nrg_iteration.params[2]
-                            is the Delta_N of that iteration; no free-chain run */
+  NRG_MODEL_1CH_S = 4,   /* one-channel Anderson with superconducting leads, |S> basis
+                            (SymNo 7, ModelNo 0); whole sweeps only.  Blocks are reported
+                            as (0, S); nrg_iteration.params[2] is the Delta_N of that
+                            iteration; no free-chain run */
+  NRG_MODEL_1CH_SZ = 5   /* the same with a Zeeman field, |Sz> basis (SymNo 8, ModelNo 0);
+                            blocks (0, Sz); averaged operators n_d, S_z, S_z^2 (the
+                            reference names them Ndot, NdSq, SdSq) */
 } nrg_model;
 
 /* Arithmetic of the dense steps. */
@@ -80,10 +83,12 @@ typedef struct {
   double lambda;      /* Lambda */
   double U, ed;       /* impurity interaction and level */
   double gamma1;      /* hybridization Gamma (channel 1) */
-  double gamma2_or_B; /* Gamma2 for NRG_MODEL_2CH_QS, field B for NRG_MODEL_1CH_QSZ,
-                         Delta_SC for NRG_MODEL_1CH_S */
+  double gamma2_or_B; /* Gamma2 for NRG_MODEL_2CH_QS, field B for NRG_MODEL_1CH_QSZ and
+                         NRG_MODEL_1CH_SZ */
   double degen_eps;   /* CNRGarray::MyEPS (-E flag); <= 0 selects 1e-18 */
   int precision;      /* nrg_precision */
+  double delta_sc;    /* gap of the superconducting leads, NRG_MODEL_1CH_S / NRG_MODEL_1CH_SZ
+                         (input_nrg.dat model parameter 4, NRG_main.cpp:220-227); else ignored */
 } nrg_sweep_config;
 
 /* Per-iteration results of a sweep (what NRG_main prints / writes). */

@@ -264,6 +264,14 @@ Basis site_1chS() {
   for (int i = 0; i < 4; ++i) s.itype.push_back(i);
   return s;
 }
+// CNRGCodeHandler::SetSingleSite for SymNo 8 (NRGcodehandlerClass.cpp:564-584):
+// Sz blocks |0>,|up dn> | |up> | |dn>.
+Basis site_1chSz() {
+  Basis s; s.nqn = 1; s.totalS = false;
+  add_site_block(s, {0}, 0, 1); add_site_block(s, {0.5}, 2, 2); add_site_block(s, {-0.5}, 3, 3);
+  for (int i = 0; i < 4; ++i) s.itype.push_back(i);
+  return s;
+}
 Basis site_1chQ() {
   Basis s; s.nqn = 1; s.totalS = false;
   add_site_block(s, {-1}, 0, 0); add_site_block(s, {0}, 1, 2); add_site_block(s, {1}, 3, 3);
@@ -288,8 +296,8 @@ Basis site_2chQS() {
 }
 
 // ---------------------------------------------------------------- rules
-enum OpRule { R_F_QS = 1, R_FUP_QSZ, R_FDN_QSZ, R_F1_2CH, R_F2_2CH, R_IMPONLY, R_CD_QS, R_F_S };
-enum Check { C_DIAG = 1, C_QS_CD, C_Q_CD, C_2CH_CD, C_S_CD };
+enum OpRule { R_F_QS = 1, R_FUP_QSZ, R_FDN_QSZ, R_F1_2CH, R_F2_2CH, R_IMPONLY, R_CD_QS, R_F_S, R_FUP_SZ, R_FDN_SZ };
+enum Check { C_DIAG = 1, C_QS_CD, C_Q_CD, C_2CH_CD, C_S_CD, C_SZ_UP, C_SZ_DN };
 
 struct Model {
   int kind;          // ORACLE_MODEL_*
@@ -310,6 +318,8 @@ bool check(int c, const Arr& a, int i, int j) {
     case C_2CH_CD: return dEq(a.q(j, 0), a.q(i, 0) + 1.0) &&
                           (dEq(a.q(j, 1), a.q(i, 1) + 0.5) || dEq(a.q(j, 1), a.q(i, 1) - 0.5));
     case C_S_CD: return dEq(a.q(j, 0), a.q(i, 0) + 0.5) || dEq(a.q(j, 0), a.q(i, 0) - 0.5);  // OneChS_cd_check :172
+    case C_SZ_UP: return dEq(a.q(j, 0), a.q(i, 0) + 0.5);  // OneChSz_cdup_check :188
+    case C_SZ_DN: return dEq(a.q(j, 0), a.q(i, 0) - 0.5);  // OneChSz_cddn_check :199
   }
   return false;
 }
@@ -444,6 +454,44 @@ double hn_1chS(Ctx& c, const std::vector<double>& P, const Basis& ab, const std:
     }
   }
   v += chi_N * Old * Coef * FermiSign;
+  return v;
+}
+
+// OneChSz_HNsc_MatEl (OpMatRules.cpp:2098-2205): superconducting leads, Sz
+// blocks, f_up and f_dn; per spin the old operator is read backwards when
+// its element vanishes or OneChS_fd_table(sigma, t_i, t_j) does.
+double hn_1chSz(Ctx& c, const std::vector<double>& P, const Basis& ab, const std::vector<Mat>& M,
+                int ist, int jst) {
+  (void)c;
+  double Lambda = P[0], chi_N = P[1], eN = P[2], Delta = P[3];
+  double Szi = qn_from_st(ab, ist, 0), Szj = qn_from_st(ab, jst, 0);
+  if (!dEq(Szi, Szj)) return 0.0;
+  double v = 0.0;
+  if (ist == jst) {
+    const double auxN[4] = {0.0, 2.0, 1.0, 1.0};
+    v = std::sqrt(Lambda) * ab.en[ist];
+    v += eN * auxN[ab.itype[ist]];
+    return v;
+  }
+  int ti = ab.itype[ist], tj = ab.itype[jst];
+  if (ab.stcf[ist] == ab.stcf[jst]) {
+    v -= Delta * onechS_pair(ti, tj);
+    v -= Delta * onechS_pair(tj, ti);
+    return v;
+  }
+  int imat = 0;
+  for (int isigma = 1; isigma >= -1; isigma -= 2) {
+    double Old = M[imat].get(ab.stcf[ist], ab.stcf[jst]);
+    int typep = ti, type = tj;
+    if (dEq(Old, 0.0) || dEq(onechS_fd(isigma, ti, tj), 0.0)) {
+      Old = M[imat].get(ab.stcf[jst], ab.stcf[ist]);
+      typep = tj; type = ti;
+    }
+    double FermiSign = (type == 2 || type == 3) ? -1.0 : 1.0;
+    v += FermiSign * Old * onechS_fd(isigma, typep, type);
+    imat++;
+  }
+  v *= chi_N;
   return v;
 }
 
@@ -663,6 +711,9 @@ double op_rule(Ctx& c, int rule, const Basis& ab, int ist, int jst) {
     case R_IMPONLY: return ab.itype[ist] == ab.itype[jst] ? 1.0 : 0.0;  // ImpOnly_MatEl OpMatRules.cpp:265
     case R_CD_QS: return op_cd_QS(c, ab, ist, jst);
     case R_F_S: return op_f_S(c, ab, ist, jst);
+    // OneChSz_fN_MatEl (OpMatRules.cpp:1986-2014)
+    case R_FUP_SZ: return ab.stcf[ist] == ab.stcf[jst] ? onechS_fd(1, ab.itype[jst], ab.itype[ist]) : 0.0;
+    case R_FDN_SZ: return ab.stcf[ist] == ab.stcf[jst] ? onechS_fd(-1, ab.itype[jst], ab.itype[ist]) : 0.0;
   }
   return 0.0;
 }
@@ -763,6 +814,7 @@ double hn_el(Ctx& c, const std::vector<double>& P, const Basis& ab, const std::v
     case ORACLE_MODEL_2CHQS: return hn_2chQS(c, P, ab, M, i, j);
     case ORACLE_MODEL_1CHQ: return hn_1chQ(c, P, ab, M, i, j);
     case ORACLE_MODEL_1CHS: return hn_1chS(c, P, ab, M, i, j);
+    case ORACLE_MODEL_1CHSZ: return hn_1chSz(c, P, ab, M, i, j);
   }
   return 0.0;
 }
@@ -1103,7 +1155,7 @@ void h0_chain_2chQS(Ctx& c, Arr& a, Mat& f1, Mat& f2) {
   }
 }
 
-// OneChS_SetAnderson_Hm1 (Main/Main_SetH0.cpp:2618-2700): S blocks 0
+// OneChS_SetAnderson_Hm1 (Main/Main_SetH0.cpp:2618-2738): S blocks 0
 // (|0>, |up dn>) and 1/2; reduced f; n_d, n_d^2, S^2 on the diagonal.
 void hm1_S(double Lambda, double HLF, double U, double ed, Arr& a, Mat& f, std::vector<Mat>& avg) {
   a = Arr(); a.nqn = 1; a.nshell = -1; a.totalS = true; a.sqn = {0};
@@ -1123,6 +1175,34 @@ void hm1_S(double Lambda, double HLF, double U, double ed, Arr& a, Mat& f, std::
   nd2.push_block(0, 0, q0, 4); nd2.push_block(1, 1, q1, 1);
   s2.push_block(0, 0, s0, 4); s2.push_block(1, 1, s1, 1);
   avg = {nd, nd2, s2};
+}
+
+// OneChSz_SetAnderson_Hm1 (Main/Main_SetH0.cpp:2751-2933): Sz blocks 0
+// (|0>, |up dn>), +1/2, -1/2, Zeeman -hz S_z with hz = B/2; f_up, f_dn;
+// matrices 2..4 named Ndot, NdSq, SdSq hold n_d, S_z, S_z^2.
+void hm1_Sz(double Lambda, double HLF, double U, double ed, double B, Arr& a, Mat& fu, Mat& fd,
+            std::vector<Mat>& avg) {
+  const double hz = 0.5 * B;
+  a = Arr(); a.nqn = 1; a.nshell = -1; a.totalS = false;
+  a.qn = {0.0, 0.5, -0.5};
+  a.bbe = {0, 1, 2, 2, 3, 3};
+  a.en = {0.5 * U / (Lambda * HLF), (2.0 * ed + 1.5 * U) / (Lambda * HLF), (ed + 0.5 * U - hz) / (Lambda * HLF),
+          (ed + 0.5 * U + hz) / (Lambda * HLF)};
+  a.evec = {1, 0, 0, 1, 1, 1};
+  fu = Mat(); fu.blk = a; fu.blk.evec.clear();
+  fd = Mat(); fd.blk = a; fd.blk.evec.clear();
+  const double u01[2] = {1, 0}, u20[2] = {0, 1}, d02[2] = {1, 0}, d10[2] = {0, -1};
+  fu.push_block(0, 1, u01, 2); fu.push_block(2, 0, u20, 2);
+  fd.push_block(0, 2, d02, 2); fd.push_block(1, 0, d10, 2);
+  Mat nd, sz, sz2;
+  for (Mat* m : {&nd, &sz, &sz2}) { m->blk = a; m->blk.evec.clear(); }
+  nd.name = "Ndot"; sz.name = "NdSq"; sz2.name = "SdSq";
+  const double n0[4] = {0, 0, 0, 2}, one[1] = {1}, z0[4] = {0, 0, 0, 0}, zp[1] = {0.5}, zm[1] = {-0.5},
+               q[1] = {0.25};
+  nd.push_block(0, 0, n0, 4); nd.push_block(1, 1, one, 1); nd.push_block(2, 2, one, 1);
+  sz.push_block(0, 0, z0, 4); sz.push_block(1, 1, zp, 1); sz.push_block(2, 2, zm, 1);
+  sz2.push_block(0, 0, z0, 4); sz2.push_block(1, 1, q, 1); sz2.push_block(2, 2, q, 1);
+  avg = {nd, sz, sz2};
 }
 
 // OneChQ_SetAnderson_Hm1 (Main/Main_SetH0.cpp:217-352): one quantum number,
@@ -1564,8 +1644,8 @@ void* oracle_run(const oracle_config* cfg) {
   // 667-720, 940-1000).  H_0 is the first site alone and only f_N is kept.
   const bool chain = cfg->chain != 0;
   if (chain && dm) { g_err = "chain and DM-NRG runs are exclusive"; delete R; return nullptr; }
-  if (chain && cfg->model == ORACLE_MODEL_1CHS) {
-    g_err = "the reference has no free-chain run for the (S) symmetry"; delete R; return nullptr;
+  if (chain && (cfg->model == ORACLE_MODEL_1CHS || cfg->model == ORACLE_MODEL_1CHSZ)) {
+    g_err = "the reference has no free-chain run for the superconducting-lead models"; delete R; return nullptr;
   }
   Arr eig;
   std::vector<Mat> mats;
@@ -1653,8 +1733,20 @@ void* oracle_run(const oracle_config* cfg) {
     mats.push_back(f); for (auto& x : avg) mats.push_back(x);
     c.m.op_rule = {R_F_S, R_IMPONLY, R_IMPONLY, R_IMPONLY};
     c.m.op_check = {C_S_CD, C_DIAG, C_DIAG, C_DIAG};
-    P = {Lambda, chi1, 0.0, cfg->gamma2_or_B};
+    P = {Lambda, chi1, 0.0, cfg->delta_sc};
     sq = 0;
+  } else if (cfg->model == ORACLE_MODEL_1CHSZ) {
+    // SymNo 8, ModelNo 0, calcdens 0 (CodeHandler_ModelSwitch.cpp:1825-1970):
+    // f_up, f_dn (OneChSz_fN rules and checks), three averaged operators;
+    // CommonQNs = {1, 0, 0}, no SU(2); Sqnumber 0.
+    c.m.site = site_1chSz(); c.m.totS = {}; c.m.common = {1, 0, 0};
+    Mat fu, fd; std::vector<Mat> avg;
+    hm1_Sz(Lambda, HLF, cfg->U, cfg->ed, cfg->gamma2_or_B, eig, fu, fd, avg);
+    mats.push_back(fu); mats.push_back(fd); for (auto& x : avg) mats.push_back(x);
+    c.m.op_rule = {R_FUP_SZ, R_FDN_SZ, R_IMPONLY, R_IMPONLY, R_IMPONLY};
+    c.m.op_check = {C_SZ_UP, C_SZ_DN, C_DIAG, C_DIAG, C_DIAG};
+    P = {Lambda, chi1, 0.0, cfg->delta_sc};
+    totalS = false; sq = 0;
   } else if (cfg->model == ORACLE_MODEL_1CHQ) {
     // SymNo 3 (CodeHandler_ModelSwitch.cpp:1138-1200): f_up, f_dn (OneChQ_fN
     // rules, OneChQ_cd_check), S_z and S_z^2 averaged; CommonQNs = {1, 0, 0}.
@@ -1684,7 +1776,8 @@ void* oracle_run(const oracle_config* cfg) {
     else if (c.m.op_rule[i] == R_CD_QS) { mats[i].need_old = true; mats[i].calc_avg = false; }
     else { mats[i].need_old = false; mats[i].calc_avg = false; }
   }
-  R->nqn = (cfg->model == ORACLE_MODEL_1CHQ || cfg->model == ORACLE_MODEL_1CHS) ? 1 : 2;
+  R->nqn = (cfg->model == ORACLE_MODEL_1CHQ || cfg->model == ORACLE_MODEL_1CHS || cfg->model == ORACLE_MODEL_1CHSZ)
+               ? 1 : 2;
   for (auto& m : mats) if (m.calc_avg) R->opnames.push_back(m.name);
   const double betabar = 0.727;
   Basis cut, ab;
@@ -1771,7 +1864,8 @@ void* oracle_run(const oracle_config* cfg) {
     for (int ich = 0; ich < nchan; ++ich) P[ich + 1] = chin(N);
     // Delta_SC rescaled for the next iteration by CNRGchain::ScaleFactor(N)
     // (NRG_main.cpp:414-419; NRGchainClass.cpp:187-202, z = 1)
-    if (cfg->model == ORACLE_MODEL_1CHS) P[3] = std::pow(Lambda, 0.5 * (double)N) / HLF * cfg->gamma2_or_B;
+    if (cfg->model == ORACLE_MODEL_1CHS || cfg->model == ORACLE_MODEL_1CHSZ)
+      P[3] = std::pow(Lambda, 0.5 * (double)N) / HLF * cfg->delta_sc;
     R->it.push_back(std::move(I));
   }
   R->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

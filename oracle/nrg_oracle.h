@@ -9,8 +9,8 @@ extern "C" {
 #define ORACLE_MODEL_1CHQSZ 1 /* one-channel Anderson, (Q,Sz) basis */
 #define ORACLE_MODEL_2CHQS 2  /* two-channel Anderson, (Q,S) basis  */
 #define ORACLE_MODEL_1CHQ 3   /* one-channel Anderson, (Q) basis    */
-#define ORACLE_MODEL_1CHS 4   /* one-channel Anderson, superconducting leads, (S) basis;
-                                 gamma2_or_B carries Delta_SC */
+#define ORACLE_MODEL_1CHS 4   /* one-channel Anderson, superconducting leads, (S) basis */
+#define ORACLE_MODEL_1CHSZ 5  /* the same in the (Sz) basis with a field B (gamma2_or_B) */
 
 typedef struct {
   int model;          /* ORACLE_MODEL_* */
@@ -23,6 +23,7 @@ typedef struct {
   int capture_iter;   /* iteration whose DiagHN inputs/H are kept, -1 none */
   int dm;             /* keep DM-NRG shells (UpdateBefCut = 1, c_d); 1chQS only */
   int chain;          /* the free Wilson chain of calcdens = 3 (H_0 = first site, iterations 1..nsites-1) */
+  double delta_sc;    /* gap of the superconducting leads (1chS, 1chSz) */
 } oracle_config;
 
 /* DM-NRG parameters (DM_NRG command line, DM_NRG_CommandLineRead.cpp). */

@@ -16,9 +16,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 SO = os.path.join(HERE, "_build", "libnrg_oracle.so")
 
-MODEL_1CHQS, MODEL_1CHQSZ, MODEL_2CHQS, MODEL_1CHQ, MODEL_1CHS = 0, 1, 2, 3, 4
+MODEL_1CHQS, MODEL_1CHQSZ, MODEL_2CHQS, MODEL_1CHQ, MODEL_1CHS, MODEL_1CHSZ = 0, 1, 2, 3, 4, 5
 MODELS = {"1chQS": MODEL_1CHQS, "1chQSz": MODEL_1CHQSZ, "2chQS": MODEL_2CHQS, "1chQ": MODEL_1CHQ,
-          "1chS": MODEL_1CHS}
+          "1chS": MODEL_1CHS, "1chSz": MODEL_1CHSZ}
 
 
 class _Cfg(ctypes.Structure):
@@ -26,7 +26,8 @@ class _Cfg(ctypes.Structure):
                 ("lambda_", ctypes.c_double), ("U", ctypes.c_double), ("ed", ctypes.c_double),
                 ("gamma1", ctypes.c_double), ("gamma2_or_B", ctypes.c_double),
                 ("degen_eps", ctypes.c_double), ("nthreads", ctypes.c_int),
-                ("capture_iter", ctypes.c_int), ("dm", ctypes.c_int), ("chain", ctypes.c_int)]
+                ("capture_iter", ctypes.c_int), ("dm", ctypes.c_int), ("chain", ctypes.c_int),
+                ("delta_sc", ctypes.c_double)]
 
 
 class _DmParams(ctypes.Structure):
@@ -138,13 +139,14 @@ def _arr(ptr, n, dtype):
 
 def run(model: str, nsites: int, ncutoff: int, lam: float, U: float, ed: float, gamma1: float,
         gamma2_or_B: float = 0.0, nthreads: int = 1, capture_iter: int = -1,
-        degen_eps: float = 0.0, blas_threads: int = 1, chain: bool = False) -> Sweep:
+        degen_eps: float = 0.0, blas_threads: int = 1, chain: bool = False, delta_sc: float = 0.0) -> Sweep:
     """One sweep.  chain=True: the free Wilson chain of calcdens = 3 (U, ed and
-    the couplings are ignored; iteration 0 is the first site alone)."""
+    the couplings are ignored; iteration 0 is the first site alone).  delta_sc:
+    the leads' gap of the superconducting-lead models."""
     L = lib()
     L.oracle_blas_threads(int(blas_threads))
     cfg = _Cfg(MODELS[model], nsites, ncutoff, lam, U, ed, gamma1, gamma2_or_B, degen_eps,
-               nthreads, capture_iter, 0, 1 if chain else 0)
+               nthreads, capture_iter, 0, 1 if chain else 0, delta_sc)
     h = L.oracle_run(ctypes.byref(cfg))
     if not h:
         raise RuntimeError("oracle: " + L.oracle_last_error().decode())

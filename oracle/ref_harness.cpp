@@ -7,12 +7,14 @@
 // Test infrastructure only: this file never ships in the product.
 //
 // Usage:
-//   ref_harness <model> <Nsites> <Ncutoff> <Lambda> <U> <ed> <Gamma1> <Gamma2|B>
+//   ref_harness <model> <Nsites> <Ncutoff> <Lambda> <U> <ed> <Gamma1> <Gamma2|B> [Delta_SC]
 //   model: 1chQS   one-channel Anderson, (Q,S) basis   (ModelSwitch SymNo 0 / ModelNo 0)
 //          1chQSz  one-channel Anderson, (Q,Sz) basis  (SymNo 2 / ModelNo 0); last arg = B
 //          1chQ    one-channel Anderson, (Q) basis     (SymNo 3 / ModelNo 0)
 //          1chS    one-channel Anderson with superconducting leads, (S) basis
-//                  (SymNo 7 / ModelNo 0); last arg = Delta_SC
+//                  (SymNo 7 / ModelNo 0)
+//          1chSz   the same in the (Sz) basis (SymNo 8 / ModelNo 0); Gamma2|B = B
+//   optional 9th argument: Delta_SC of the superconducting leads
 //          2chQS   two-channel Anderson, (Q,S) basis: the impurity H_{-1} of
 //                  OneChQS_SetAnderson_Hm1 coupled to both channels through
 //                  TwoChQS_HN_MatEl with f_ch1 = f_ch2 = d; last arg = Gamma2
@@ -94,7 +96,8 @@ int main(int argc, char** argv) {
   bool totalS = true;
   int sqnumber = 1;
   int nchan = 1;
-  double deltaSC = 0.0;  // superconducting leads (1chS): rescaled every iteration
+  // superconducting leads (1chS, 1chSz): the gap, rescaled every iteration
+  double deltaSC = argc > 9 ? atof(argv[9]) : 0.0;
 
   CNRGmatrix aux;
   if (model == "1chQS") {
@@ -173,10 +176,35 @@ int main(int argc, char** argv) {
     CommonQNs = {1, 0, 0}; totSpos = {0};
     HN.CalcHNMatEl = OneChS_HNsc_MatEl;
     double chi_m1 = sqrt(2.0 * Gamma1 / pi) / (sqrt(Lambda) * HalfLambdaFactor) * ALambda;
-    ParamsHN = {Lambda, chi_m1, 0.0, extra};  // e_N, Delta_SC (NRG_main.cpp:264-276)
+    ParamsHN = {Lambda, chi_m1, 0.0, deltaSC};  // e_N, Delta_SC (NRG_main.cpp:264-276)
     totalS = true;
     sqnumber = 0;  // NRGcodehandlerClass.cpp:774-777
-    deltaSC = extra;
+  } else if (model == "1chSz") {
+    // CNRGCodeHandler::SetSingleSite, SymNo 8 (NRGcodehandlerClass.cpp:564-584)
+    SingleSite.NQNumbers = 1;
+    SingleSite.Nshell = 0;
+    SingleSite.totalS = false;
+    SingleSite.QNumbers = {0.0, 0.5, -0.5};
+    SingleSite.BlockBegEnd = {0, 1, 2, 2, 3, 3};
+    for (int ii = 0; ii < 4; ++ii) SingleSite.iType.push_back(ii);
+    // ModelSwitch SymNo 8, ModelNo 0, calcdens 0 (CodeHandler_ModelSwitch.cpp:1825-1970)
+    for (int i = 0; i < 5; ++i) Mats.push_back(aux);
+    Mats[0].NeedOld = false; Mats[0].UpperTriangular = false;
+    Mats[0].CheckForMatEl = OneChSz_cdup_check; Mats[0].CalcMatEl = OneChSz_fNup_MatEl;
+    Mats[1].NeedOld = false; Mats[1].UpperTriangular = false;
+    Mats[1].CheckForMatEl = OneChSz_cddn_check; Mats[1].CalcMatEl = OneChSz_fNdn_MatEl;
+    CNRGmatrix avg; avg.NeedOld = true; avg.UpperTriangular = false; avg.CalcAvg = true;
+    avg.CheckForMatEl = Diag_check; avg.CalcMatEl = ImpOnly_MatEl;
+    Mats[2] = avg; Mats[3] = avg; Mats[4] = avg;
+    strcpy(Mats[2].MatName, "Ndot"); strcpy(Mats[3].MatName, "NdSq"); strcpy(Mats[4].MatName, "SdSq");
+    std::vector<double> P = {Lambda, HalfLambdaFactor, U, ed, extra};
+    OneChSz_SetAnderson_Hm1(P, &Aeig, Mats);
+    CommonQNs = {1, 0, 0}; totSpos.clear();
+    HN.CalcHNMatEl = OneChSz_HNsc_MatEl;
+    double chi_m1 = sqrt(2.0 * Gamma1 / pi) / (sqrt(Lambda) * HalfLambdaFactor) * ALambda;
+    ParamsHN = {Lambda, chi_m1, 0.0, deltaSC};
+    totalS = false;
+    sqnumber = 0;  // NRGcodehandlerClass.cpp:778-781
   } else if (model == "2chQS") {
     TwoChQS_SetSingleSite(&SingleSite);
     // Impurity H_{-1} and its reduced <||d||> from the one-channel set-up.
@@ -248,7 +276,8 @@ int main(int argc, char** argv) {
     for (int b = 0; b < AeigCut.NumBlocks(); ++b) printf(" %d", AeigCut.GetBlockSize(b));
     printf("\n");
     for (int ich = 0; ich < nchan; ++ich) ParamsHN[ich + 1] = chain.GetChin(N);  // NRG_main.cpp:402-405
-    if (model == "1chS") ParamsHN[nchan + 2] = chain.ScaleFactor(N) * deltaSC;  // NRG_main.cpp:414-419
+    if (model == "1chS" || model == "1chSz")
+      ParamsHN[nchan + 2] = chain.ScaleFactor(N) * deltaSC;  // NRG_main.cpp:414-419
   }
   fflush(stdout);
   return 0;

@@ -24,7 +24,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 HARNESS = os.path.join(REPO, "oracle", "_ref", "ref_harness")
 REF = os.environ.get("REF_DIR", "/root/reference")
 
-# name: (model, nsites, ncutoff, Lambda, U, ed, Gamma1, Gamma2|B)
+# name: (model, nsites, ncutoff, Lambda, U, ed, Gamma1, Gamma2|B[, Delta_SC])
 CASES = {
     # Runs/run1 inputs with Gamma rescaled by A_Lambda (the log predates the
     # sqrt(A_Lambda) factor of NRG_main.cpp:205-207).
@@ -38,9 +38,10 @@ CASES = {
     "small_2chQS_n5_k60": ("2chQS", 5, 60, 2.5, 0.3, -0.15, 0.01, 0.01),
     # One-channel Anderson in the charge-only |Q> basis (SymNo 3).
     "q_1chQ_n12_k200": ("1chQ", 12, 200, 2.5, 0.5, -0.25, 0.02, 0.0),
-    # One-channel Anderson with superconducting leads in the |S> basis
-    # (SymNo 7), Delta_SC = 0.01.
-    "s_1chS_n12_k200": ("1chS", 12, 200, 2.5, 0.5, -0.25, 0.02, 0.01),
+    # One-channel Anderson with superconducting leads (Delta_SC = 0.01, the
+    # ninth entry) in the |S> basis (SymNo 7) and, with a field, |Sz> (SymNo 8).
+    "s_1chS_n12_k200": ("1chS", 12, 200, 2.5, 0.5, -0.25, 0.02, 0.0, 0.01),
+    "sz_1chSz_n12_k200": ("1chSz", 12, 200, 2.5, 0.5, -0.25, 0.02, 1.0e-3, 0.01),
 }
 
 
@@ -109,14 +110,16 @@ def main() -> None:
         sys.exit("build the reference first: bash oracle/build_ref.sh")
     np.savez_compressed(os.path.join(HERE, "run1_log.npz"), **run1_log())
     only = sys.argv[1:]
-    for name, (model, ns, nc, lam, U, ed, g1, x) in CASES.items():
+    for name, case in CASES.items():
         if only and name not in only:
             continue
+        model, ns, nc, lam, U, ed, g1, x = case[:8]
         args = [HARNESS, model, str(ns), str(nc), repr(lam), repr(U), repr(ed), repr(g1), repr(x)]
+        args += [repr(v) for v in case[8:]]
         env = dict(os.environ, OPENBLAS_NUM_THREADS="1")
         txt = subprocess.run(args, check=True, capture_output=True, text=True, env=env).stdout
         d = parse(txt)
-        d["config"] = np.array([model, ns, nc, lam, U, ed, g1, x], dtype=object).astype(str)
+        d["config"] = np.array(list(case), dtype=object).astype(str)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
         print(name, d["niters"], "iterations")
 

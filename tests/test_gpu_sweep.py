@@ -22,10 +22,10 @@ OBS_TOL = 1e-8
 def compare(gpu, ref, model=""):
     assert len(gpu.iters) == len(ref.iters)
     for n, (a, b) in enumerate(zip(gpu.iters, ref.iters)):
-        # one-quantum-number blocks: the engine reports |Q> as (Q, 0) and |S>
-        # as (0, S), the reference the one number
+        # one-quantum-number blocks: the engine reports |Q> as (Q, 0) and |S>,
+        # |Sz> as (0, S), (0, Sz), the reference the one number
         nq = b.qn.shape[1]
-        qa = a.qn[:, ::-1] if model == "1chS" else a.qn
+        qa = a.qn[:, ::-1] if model in ("1chS", "1chSz") else a.qn
         np.testing.assert_array_equal(qa[:, :nq], b.qn, err_msg=f"N={n} sectors")
         assert not qa[:, nq:].any()
         np.testing.assert_array_equal(a.bsize, b.bsize, err_msg=f"N={n} block sizes")
@@ -47,24 +47,27 @@ CASES = [
     ("2chQS", 5, 80, 2.5, 0.3, -0.15, 0.01, 0.01),
     ("2chQS", 4, 40, 2.5, 0.3, -0.15, 0.01, 0.02),
     ("1chQ", 12, 150, 2.5, 0.4, -0.2, 0.015, 0.0),
-    ("1chS", 12, 150, 2.5, 0.4, -0.2, 0.015, 0.02),
+    ("1chS", 12, 150, 2.5, 0.4, -0.2, 0.015, 0.0, 0.02),
+    ("1chSz", 10, 200, 2.5, 0.4, -0.2, 0.015, 1e-4, 0.02),
 ]
 
 
 @pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}-n{c[1]}-k{c[2]}" for c in CASES])
 def test_sweep_matches_oracle(engine, case):
-    g = engine.sweep(*case)
-    o = orc.run(*case, nthreads=min(8, os.cpu_count() or 1))
+    delta = case[8] if len(case) > 8 else 0.0  # superconducting leads' gap
+    g = engine.sweep(*case[:8], delta_sc=delta)
+    o = orc.run(*case[:8], nthreads=min(8, os.cpu_count() or 1), delta_sc=delta)
     compare(g, o, case[0])
     np.testing.assert_allclose(g.opavg_m1, o.opavg_m1, rtol=1e-15)
 
 
 @pytest.mark.parametrize("name", ["cfg0_1chQS_n40_k500", "qsz_1chQSz_n14_k300", "cfg1_2chQS_n8_k300",
-                                  "q_1chQ_n12_k200", "s_1chS_n12_k200"])
+                                  "q_1chQ_n12_k200", "s_1chS_n12_k200", "sz_1chSz_n12_k200"])
 def test_sweep_matches_reference_fixture(engine, name):
     g = np.load(os.path.join(GOLD, name + ".npz"))
-    model, ns, nc, lam, U, ed, g1, x = g["config"]
-    r = engine.sweep(model, int(ns), int(nc), float(lam), float(U), float(ed), float(g1), float(x))
+    model, ns, nc, lam, U, ed, g1, x = g["config"][:8]
+    delta = float(g["config"][8]) if len(g["config"]) > 8 else 0.0
+    r = engine.sweep(model, int(ns), int(nc), float(lam), float(U), float(ed), float(g1), float(x), delta_sc=delta)
 
     class Ref:  # fixture in the oracle's shape
         iters = []

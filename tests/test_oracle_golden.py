@@ -13,14 +13,15 @@ from oracle import oracle as orc
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
 CASES = ["run1_1chQS", "small_2chQS_n5_k60", "qsz_1chQSz_n14_k300", "cfg1_2chQS_n8_k300",
-         "cfg0_1chQS_n40_k500", "q_1chQ_n12_k200", "s_1chS_n12_k200"]
+         "cfg0_1chQS_n40_k500", "q_1chQ_n12_k200", "s_1chS_n12_k200", "sz_1chSz_n12_k200"]
 
 
 def _run(name, **kw):
     g = np.load(os.path.join(GOLD, name + ".npz"))
-    model, ns, nc, lam, U, ed, g1, x = g["config"]
+    model, ns, nc, lam, U, ed, g1, x = g["config"][:8]
+    delta = float(g["config"][8]) if len(g["config"]) > 8 else 0.0  # superconducting leads' gap
     s = orc.run(model, int(ns), int(nc), float(lam), float(U), float(ed), float(g1), float(x),
-                nthreads=min(8, os.cpu_count() or 1), **kw)
+                nthreads=min(8, os.cpu_count() or 1), delta_sc=delta, **kw)
     return g, s
 
 

@@ -19,9 +19,9 @@ from . import build as _build
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = _build.LIB
 
-MODEL_1CH_QS, MODEL_1CH_QSZ, MODEL_2CH_QS, MODEL_1CH_Q, MODEL_1CH_S = 0, 1, 2, 3, 4
+MODEL_1CH_QS, MODEL_1CH_QSZ, MODEL_2CH_QS, MODEL_1CH_Q, MODEL_1CH_S, MODEL_1CH_SZ = 0, 1, 2, 3, 4, 5
 MODELS = {"1chQS": MODEL_1CH_QS, "1chQSz": MODEL_1CH_QSZ, "2chQS": MODEL_2CH_QS, "1chQ": MODEL_1CH_Q,
-          "1chS": MODEL_1CH_S}
+          "1chS": MODEL_1CH_S, "1chSz": MODEL_1CH_SZ}
 PREC_FP64 = 0
 
 STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "out of memory", 4: "not converged",
@@ -39,7 +39,7 @@ class SweepConfig(ctypes.Structure):
     _fields_ = [("model", ctypes.c_int), ("nsites", ctypes.c_int), ("ncutoff", ctypes.c_int),
                 ("lambda_", ctypes.c_double), ("U", ctypes.c_double), ("ed", ctypes.c_double),
                 ("gamma1", ctypes.c_double), ("gamma2_or_B", ctypes.c_double),
-                ("degen_eps", ctypes.c_double), ("precision", ctypes.c_int)]
+                ("degen_eps", ctypes.c_double), ("precision", ctypes.c_int), ("delta_sc", ctypes.c_double)]
 
 
 class _Iteration(ctypes.Structure):
@@ -515,9 +515,11 @@ class Engine:
 
     def sweep(self, model: str, nsites: int, ncutoff: int, lam: float, U: float, ed: float,
               gamma1: float, gamma2_or_B: float = 0.0, degen_eps: float = 0.0,
-              precision: int = PREC_FP64, fetch: bool = True) -> SweepResult:
+              precision: int = PREC_FP64, fetch: bool = True, delta_sc: float = 0.0) -> SweepResult:
+        """One sweep (nrg_sweep_run).  gamma2_or_B: Gamma2 (2chQS) or the field B
+        (1chQSz, 1chSz); delta_sc: the leads' gap (1chS, 1chSz)."""
         cfg = SweepConfig(MODELS[model], nsites, ncutoff, lam, U, ed, gamma1, gamma2_or_B,
-                          degen_eps, precision)
+                          degen_eps, precision, delta_sc)
         self._check(self.L.nrg_sweep_run(self.h, ctypes.byref(cfg)))
         return self._fetch(fetch)
 

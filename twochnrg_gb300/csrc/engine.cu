@@ -569,13 +569,18 @@ AsmTables prepare_assembly(nrg_ctx* c, const ModelSpec& m, const Basis& B, const
   // (OneChS_HNsc_MatEl's auxN); pairing and h.c.-switch tables
   const int NT = m.site.nstates;
   std::vector<double> sc_pair(NT * NT, 0.0);
-  std::vector<int> hc_sw(NT * NT, 0), st_old(P.nstates, 0);
-  if (m.kind == MODEL_1CHS) {
+  std::vector<int> hc_sw(2 * NT * NT, 0), st_old(P.nstates, 0);
+  if (m.kind == MODEL_1CHS || m.kind == MODEL_1CHSZ) {
     site_q = {-1.0, 1.0, 0.0, 0.0};
     for (int a = 0; a < NT; ++a)
       for (int b2 = 0; b2 < NT; ++b2) {
         sc_pair[a * NT + b2] = sc_pair_1chS(a, b2);
-        hc_sw[a * NT + b2] = hc_switch_1chS(a, b2) ? 1 : 0;
+        if (m.kind == MODEL_1CHS) {
+          hc_sw[a * NT + b2] = hc_switch_1chS(a, b2) ? 1 : 0;
+        } else {  // per spin: sigma = +1 first, as the old operators f_up, f_dn
+          hc_sw[a * NT + b2] = hc_switch_1chSz(1, a, b2) ? 1 : 0;
+          hc_sw[NT * NT + a * NT + b2] = hc_switch_1chSz(-1, a, b2) ? 1 : 0;
+        }
       }
     for (int g = 0; g < P.nstates; ++g) st_old[g] = B.stcf[g];
   }
@@ -756,9 +761,9 @@ void launch_update_plan(nrg_ctx* c, Timer& tm, UpdatePlan& U) {
 void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool chain = false) {
   using clock = std::chrono::steady_clock;
   auto t_begin = clock::now();
-  if (cfg->model < 0 || cfg->model > 4) throw NrgError(NRG_ERR_ARG, "unknown model");
-  if (chain && cfg->model == NRG_MODEL_1CH_S)
-    throw NrgError(NRG_ERR_ARG, "the reference has no free-chain run for the |S> symmetry");
+  if (cfg->model < 0 || cfg->model > 5) throw NrgError(NRG_ERR_ARG, "unknown model");
+  if (chain && (cfg->model == NRG_MODEL_1CH_S || cfg->model == NRG_MODEL_1CH_SZ))
+    throw NrgError(NRG_ERR_ARG, "the reference has no free-chain run for the superconducting-lead models");
   if (dm && cfg->model != NRG_MODEL_1CH_QS)
     throw NrgError(NRG_ERR_ARG, "DM-NRG shells are available for the one-channel |Q S> model");
   if (cfg->nsites < 1 || cfg->ncutoff < 4 || !(cfg->lambda > 1.0)) throw NrgError(NRG_ERR_ARG, "bad sweep parameters");
@@ -862,11 +867,11 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
   // |S> model with superconducting leads: Delta_SC enters H_N unscaled at
   // N = 0 and as ScaleFactor(N-1) * Delta_SC = Lambda^((N-1)/2) / HLF *
   // Delta_SC after that (NRG_main.cpp:220-227, 276, 414-419).
-  const bool sc = m.kind == MODEL_1CHS;
+  const bool sc = m.kind == MODEL_1CHS || m.kind == MODEL_1CHSZ;
   for (int N = N0; N < cfg->nsites; ++N) {
     IterResult R;
-    const double delta = !sc ? 0.0 : (N == 0 ? cfg->gamma2_or_B
-                                             : std::pow(lambda, 0.5 * (double)(N - 1)) / HLF * cfg->gamma2_or_B);
+    const double delta = !sc ? 0.0 : (N == 0 ? cfg->delta_sc
+                                             : std::pow(lambda, 0.5 * (double)(N - 1)) / HLF * cfg->delta_sc);
     R.params = {lambda, chi[0], sc ? delta : chi[1], eN};
     const double DN = HLF * std::pow(lambda, (-(N - 1) / 2.0));
     // ---------------- BuildBasis + tables (host)

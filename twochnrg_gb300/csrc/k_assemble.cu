@@ -46,7 +46,26 @@ __global__ void __launch_bounds__(256) assemble_kernel(AssembleArgs A, const int
       const int ti = A.st_type[gi], tj = A.st_type[gj];
       const int64_t pt = A.pair_base[b] + ((int64_t)p * nseg + q) * A.nops_h;
       const double* cij = coef + ((size_t)ti * NT + tj) * NO * 2;
-      if (A.model == 4) {
+      if (A.model == 5) {
+        if (A.st_old[gi] == A.st_old[gj]) {
+          v = __dsub_rn(__dsub_rn(0.0, __dmul_rn(A.delta, A.sc_pair[ti * NT + tj])),
+                        __dmul_rn(A.delta, A.sc_pair[tj * NT + ti]));
+        } else {
+          // OneChSz_HNsc_MatEl: sum over sigma of FermiSign*OldEl*fd, then
+          // times chi_N (sign and table folded into cij, exact)
+          double acc = 0.0;
+          for (int o = 0; o < 2; ++o) {
+            double old = old_element(A.ops[o], A.pair_fwd[pt + o], A.pair_fwd_ld[pt + o], ai, aj);
+            int dir = 0;
+            if (fabs(old) < 1.e-20 || A.hc_switch[o * NT * NT + ti * NT + tj]) {
+              old = old_element(A.ops[o], A.pair_bwd[pt + o], A.pair_bwd_ld[pt + o], aj, ai);
+              dir = 1;
+            }
+            acc = __dadd_rn(acc, __dmul_rn(cij[o * 2 + dir], old));
+          }
+          v = __dmul_rn(acc, A.chi[0]);
+        }
+      } else if (A.model == 4) {
         if (A.st_old[gi] == A.st_old[gj]) {
           // OneChS_HNsc_MatEl: the lead's pairing term on the new site
           v = __dsub_rn(__dsub_rn(0.0, __dmul_rn(A.delta, A.sc_pair[ti * NT + tj])),

@@ -61,7 +61,7 @@ struct AssembleArgs {
   // pairing table and the hopping's h.c. switch per type pair, Delta_N
   const int* st_old;
   const double* sc_pair;     // [ntypes^2]
-  const int* hc_switch;      // [ntypes^2]
+  const int* hc_switch;      // [ntypes^2]; model 5: [2 * ntypes^2], spin up first
   double delta;
 };
 void launch_assemble(const AssembleArgs& a, int64_t total_rows, const int* row_block,

@@ -186,6 +186,18 @@ ModelSpec make_model(ModelKind kind) {
     m.op_kind = {OP_F_S, OP_IMPONLY, OP_IMPONLY, OP_IMPONLY};
     m.op_check = {CHK_S_CD, CHK_DIAG, CHK_DIAG, CHK_DIAG};
     m.op_name = {"fN", "Ndot", "NdSq", "SdSq"};
+  } else if (kind == MODEL_1CHSZ) {
+    // CNRGCodeHandler::SetSingleSite, SymNo 8 (NRGcodehandlerClass.cpp:564-584):
+    // Sz blocks |0>,|up dn> | |up> | |dn>, here (0,Sz).
+    m.site.blk.nqn = 2;
+    site_block(m.site, {0, 0}, 2); site_block(m.site, {0, 0.5}, 1); site_block(m.site, {0, -0.5}, 1);
+    m.totalS = false; m.nchan = 1; m.nsigma = 2;
+    // CodeHandler_ModelSwitch.cpp:1846-1880 (calcdens 0): f_up, f_dn, and
+    // three averaged operators named Ndot, NdSq, SdSq that OneChSz_SetAnderson_Hm1
+    // fills with n_d, S_z, S_z^2.
+    m.op_kind = {OP_FUP_SZ, OP_FDN_SZ, OP_IMPONLY, OP_IMPONLY, OP_IMPONLY};
+    m.op_check = {CHK_SZ_UP, CHK_SZ_DN, CHK_DIAG, CHK_DIAG, CHK_DIAG};
+    m.op_name = {"fNup", "fNdn", "Ndot", "NdSq", "SdSq"};
   } else if (kind == MODEL_2CHQS) {
     // TwoChQS_SetSingleSite (TwoChQS_SetSingleSite.cpp:5-124): 16 states in 10 blocks.
     m.site.blk.nqn = 3;
@@ -242,7 +254,7 @@ StartState make_start(const ModelSpec& m, double lambda, double U, double ed, do
     if (m.kind == MODEL_2CHQS) s.ops.push_back(f);  // f_ch1 = f_ch2 = d
     s.ops.push_back(o1); s.ops.push_back(o2); s.ops.push_back(o3);
   } else if (m.kind == MODEL_1CHS) {
-    // OneChS_SetAnderson_Hm1 (Main/Main_SetH0.cpp:2618-2700): blocks S = 0
+    // OneChS_SetAnderson_Hm1 (Main/Main_SetH0.cpp:2618-2738): blocks S = 0
     // (|0>, |up dn>) and S = 1/2; reduced <||f||> between them; n_d, n_d^2,
     // S^2 diagonal.
     const double q[2][2] = {{0, 0}, {0, 0.5}};
@@ -258,6 +270,25 @@ StartState make_start(const ModelSpec& m, double lambda, double U, double ed, do
     pair(nd2, 0, 0, {0.0, 0.0, 0.0, 4.0}); pair(nd2, 1, 1, {1.0});
     pair(s2, 0, 0, {0.0, 0.0, 0.0, 0.0}); pair(s2, 1, 1, {0.75});
     s.ops = {f, nd, nd2, s2};
+  } else if (m.kind == MODEL_1CHSZ) {
+    // OneChSz_SetAnderson_Hm1 (Main/Main_SetH0.cpp:2751-2933): Sz blocks 0
+    // (|0>, |up dn>), +1/2, -1/2 with the Zeeman term -hz S_z, hz = B/2;
+    // f_up, f_dn not reduced; n_d, S_z, S_z^2 diagonal.
+    const double hz = 0.5 * B;
+    const double q[3][2] = {{0, 0}, {0, 0.5}, {0, -0.5}};
+    s.blk.push(q[0], 2); s.blk.push(q[1], 1); s.blk.push(q[2], 1);
+    s.en = {0.5 * U / scale, (2.0 * ed + 1.5 * U) / scale, (ed + 0.5 * U - hz) / scale, (ed + 0.5 * U + hz) / scale};
+    OpBlocks fu, fd, nd, sz, sz2;
+    auto pair = [](OpBlocks& o, int i, int j, std::initializer_list<double> v) {
+      o.bi.push_back(i); o.bj.push_back(j); o.off.push_back((int64_t)o.el.size());
+      o.el.insert(o.el.end(), v);
+    };
+    pair(fu, 0, 1, {1.0, 0.0}); pair(fu, 2, 0, {0.0, 1.0});
+    pair(fd, 0, 2, {1.0, 0.0}); pair(fd, 1, 0, {0.0, -1.0});
+    pair(nd, 0, 0, {0.0, 0.0, 0.0, 2.0}); pair(nd, 1, 1, {1.0}); pair(nd, 2, 2, {1.0});
+    pair(sz, 0, 0, {0.0, 0.0, 0.0, 0.0}); pair(sz, 1, 1, {0.5}); pair(sz, 2, 2, {-0.5});
+    pair(sz2, 0, 0, {0.0, 0.0, 0.0, 0.0}); pair(sz2, 1, 1, {0.25}); pair(sz2, 2, 2, {0.25});
+    s.ops = {fu, fd, nd, sz, sz2};
   } else if (m.kind == MODEL_1CHQ) {
     // OneChQ_SetAnderson_Hm1 (Main/Main_SetH0.cpp:217-352): |0> | |up>,|dn> |
     // |up dn> by Q, the Q = 0 block two-fold; f_up, f_dn not reduced; S_z and
@@ -502,6 +533,16 @@ void build_hn_tables(const ModelSpec& m, const Basis& b, HNTables& t) {
         } else if (m.kind == MODEL_1CHS) {
           c[base * 2 + 0] = hn_coef_1chS(m.site, Si, ti, tj);
           c[base * 2 + 1] = hn_coef_1chS(m.site, Si, tj, ti);
+        } else if (m.kind == MODEL_1CHSZ) {
+          // OneChSz_HNsc_MatEl (OpMatRules.cpp:2160-2200): per spin, the fermion
+          // sign of the "type" state (types 2, 3 carry one electron) times
+          // <typep|f^dagger_sigma|type>.
+          for (int s = 0; s < 2; ++s) {
+            const int isigma = s == 0 ? 1 : -1;
+            const double fj = (tj == 2 || tj == 3) ? -1.0 : 1.0, fi = (ti == 2 || ti == 3) ? -1.0 : 1.0;
+            c[(base + s) * 2 + 0] = fj * fd_onechS(isigma, ti, tj);
+            c[(base + s) * 2 + 1] = fi * fd_onechS(isigma, tj, ti);
+          }
         } else if (m.kind == MODEL_1CHQSZ || m.kind == MODEL_1CHQ) {
           // OneChQSz_HN_MatEl (OpMatRules.cpp:468-531), OneChQ_HN_MatEl
           // (:1065-1147): per spin, the fermion sign of the "type" state times
@@ -528,6 +569,7 @@ void build_hn_tables(const ModelSpec& m, const Basis& b, HNTables& t) {
 
 double sc_pair_1chS(int ti, int tj) { return (ti == 1 && tj == 0) ? 1.0 : 0.0; }
 bool hc_switch_1chS(int ti, int tj) { return fd_onechS(1, ti, tj) == 0.0 && fd_onechS(-1, ti, tj) == 0.0; }
+bool hc_switch_1chSz(int sigma, int ti, int tj) { return fd_onechS(sigma, ti, tj) == 0.0; }
 
 double op_site_factor(const ModelSpec& m, int op, double Si, double Sj, int ti, int tj) {
   const BlockArray& ss = m.site.blk;
@@ -552,6 +594,8 @@ double op_site_factor(const ModelSpec& m, int op, double Si, double Sj, int ti, 
     if (!deq(cg1, 0.0)) return 0.0 / cg1;
     return 0.0;
   }
+  if (op == OP_FUP_SZ) return fd_onechS(1, tj, ti);   // OneChSz_fN_MatEl (OpMatRules.cpp:1986-2014)
+  if (op == OP_FDN_SZ) return fd_onechS(-1, tj, ti);
   if (op == OP_FUP_QSZ) return fd_onech(1, tj, ti);   // OneChQ_fN_MatEl (OpMatRules.cpp:1003-1033)
   if (op == OP_FDN_QSZ) return fd_onech(-1, tj, ti);
   if (op == OP_IMPONLY) return ti == tj ? 1.0 : 0.0;
@@ -637,6 +681,8 @@ bool op_check(int chk, const BlockArray& a, int i, int j) {
   switch (chk) {
     case CHK_DIAG: return i == j;
     case CHK_S_CD: return deq(a.q(j, 1), a.q(i, 1) + 0.5) || deq(a.q(j, 1), a.q(i, 1) - 0.5);
+    case CHK_SZ_UP: return deq(a.q(j, 1), a.q(i, 1) + 0.5);  // OneChSz_cdup_check :188
+    case CHK_SZ_DN: return deq(a.q(j, 1), a.q(i, 1) - 0.5);  // OneChSz_cddn_check :199
     case CHK_Q_CD: return deq(a.q(j, 0), a.q(i, 0) + 1.0);
     case CHK_QS_CD:
     case CHK_2CH_CD:

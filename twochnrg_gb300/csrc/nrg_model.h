@@ -22,7 +22,8 @@ namespace nrg {
 // MODEL_1CHS (SymNo 7, superconducting leads) conserves the total spin only;
 // its blocks carry a constant 0 in the charge slot and S in the second, so
 // that every SU(2) rule reads S where it does for (Q,S).
-enum ModelKind { MODEL_1CHQS = 0, MODEL_1CHQSZ = 1, MODEL_2CHQS = 2, MODEL_1CHQ = 3, MODEL_1CHS = 4 };
+// MODEL_1CHSZ (SymNo 8) is its |Sz> form with a Zeeman field: blocks (0, Sz).
+enum ModelKind { MODEL_1CHQS = 0, MODEL_1CHQSZ = 1, MODEL_2CHQS = 2, MODEL_1CHQ = 3, MODEL_1CHS = 4, MODEL_1CHSZ = 5 };
 
 // Operator rule ids (how the operator acts on a new site; see build_op_terms).
 enum OpKind {
@@ -34,9 +35,12 @@ enum OpKind {
   OP_IMPONLY = 6,   // ImpOnly_MatEl x old   (OpMatRules.cpp:265)
   OP_CD_QS = 7,     // OneChQS_cd_MatEl x old (OpMatRules.cpp:1249)
   OP_F_S = 8,       // OneChS_fN_MatEl       (OpMatRules.cpp:1555)
+  OP_FUP_SZ = 9,    // OneChSz_fNup_MatEl    (OpMatRules.cpp:2016)
+  OP_FDN_SZ = 10,   // OneChSz_fNdn_MatEl    (OpMatRules.cpp:2027)
 };
 // CheckForMatEl rule ids.
-enum CheckKind { CHK_DIAG = 1, CHK_QS_CD = 2, CHK_Q_CD = 3, CHK_2CH_CD = 4, CHK_S_CD = 5 };
+enum CheckKind { CHK_DIAG = 1, CHK_QS_CD = 2, CHK_Q_CD = 3, CHK_2CH_CD = 4, CHK_S_CD = 5, CHK_SZ_UP = 6,
+                 CHK_SZ_DN = 7 };
 
 // Block-structured array: the common part of CNRGarray / CNRGbasisarray
 // (include/NRGclasses.hpp:47-349).
@@ -139,6 +143,10 @@ double op_site_factor(const ModelSpec& m, int op, double Si, double Sj, int ti, 
 // OneChS_fd_table(+-1, t_i, t_j) vanish).
 double sc_pair_1chS(int ti, int tj);
 bool hc_switch_1chS(int ti, int tj);
+// |Sz> form (OneChSz_HNsc_MatEl, OpMatRules.cpp:2098-2205): per spin sigma,
+// the old operator is read backwards also when OneChS_fd_table(sigma, t_i,
+// t_j) vanishes.
+bool hc_switch_1chSz(int sigma, int ti, int tj);
 bool op_check(int chk, const BlockArray& kept, int i, int j);
 
 // Clebsch-Gordan <J1 M1; J2 M2 | J M>  (CGordan.cpp:34-120).
