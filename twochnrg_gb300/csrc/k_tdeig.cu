@@ -20,14 +20,15 @@ namespace {
 
 constexpr double kEps = 2.220446049250313e-16;
 
-__device__ __forceinline__ int sturm_count(const double* d, const double* e, int n, double x, double pivmin) {
+// e2: the squared off-diagonal, formed once per call (a square in every
+// pass of every level would cost an FP64 multiply per step).
+__device__ __forceinline__ int sturm_count(const double* d, const double* e2, int n, double x, double pivmin) {
   int cnt = 0;
   double q = d[0] - x;
   if (fabs(q) < pivmin) q = -pivmin;
   if (q < 0.0) cnt++;
   for (int i = 1; i < n; ++i) {
-    const double ei = e[i - 1];
-    q = (d[i] - x) - (ei * ei) / q;
+    q = (d[i] - x) - e2[i - 1] / q;
     if (fabs(q) < pivmin) q = -pivmin;
     if (q < 0.0) cnt++;
   }
@@ -53,7 +54,7 @@ __device__ __forceinline__ int sturm_count_f32(const float* d, const float* e, i
 // One FP64 pass: Sturm count of T - x and, from the pivot recurrence q_i
 // and its first two derivatives, S1 = sum q_i'/q_i = f'/f and
 // S2 = sum (q_i''/q_i - (q_i'/q_i)^2) = (log f)'' of f(x) = det(T - x).
-__device__ __forceinline__ int sturm_sums(const double* d, const double* e, int n, double x, double pivmin,
+__device__ __forceinline__ int sturm_sums(const double* d, const double* e2v, int n, double x, double pivmin,
                                           double* S1, double* S2) {
   int cnt = 0;
   double q = d[0] - x, dq = -1.0, ddq = 0.0;
@@ -63,7 +64,7 @@ __device__ __forceinline__ int sturm_sums(const double* d, const double* e, int 
   double u = dq * r;
   double s1 = u, s2 = -u * u;
   for (int i = 1; i < n; ++i) {
-    const double e2 = e[i - 1] * e[i - 1];
+    const double e2 = e2v[i - 1];
     const double qn = (d[i] - x) - e2 * r;
     const double e2rr = e2 * r * r;
     const double ddqn = e2rr * fma(-2.0 * dq * dq, r, ddq);
@@ -143,6 +144,7 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
   const double* e = eb + s0;
   const float* fd32 = A.fde + so + s0;
   const float* fe32 = A.fde + A.nstates + so + s0;
+  const double* e2 = A.e2 + so + s0;
   if (n == 1) {
     if (!isfinite(d[0])) atomicOr(A.flag, DEV_BAD_INPUT);
     A.ev[g] = d[0];
@@ -165,6 +167,7 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
   double hi = (double)fgu + 1e-6 * tnorm + 2.0 * kEps * tnorm * n + 2.0 * pivmin;
   const double atol = 1e-3 * kEps * fmax(tnorm, DBL_MIN);
   int clo = -1, chi = -1;  // Sturm counts at lo / hi once checked in FP64
+  double x0 = 0.5 * (lo + hi);
   // FP32 bracket
   if (tnorm > 1e-30 && tnorm < 1e30) {
     float flo = (float)lo, fhi = (float)hi;
@@ -173,14 +176,15 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
       const float mid = 0.5f * (flo + fhi);
       if (sturm_count_f32(fd32, fe32, n, mid, fpiv) > k) fhi = mid; else flo = mid;
     }
+    x0 = 0.5 * ((double)flo + (double)fhi);  // within 1e-6 tnorm of the level: the first step lands
     const double margin = 1e-5 * tnorm;
     const double tlo = (double)flo - margin, thi = (double)fhi + margin;
     if (tlo > lo) {
-      const int c = sturm_count(d, e, n, tlo, pivmin);
+      const int c = sturm_count(d, e2, n, tlo, pivmin);
       if (c <= k) { lo = tlo; clo = c; }
     }
     if (thi < hi) {
-      const int c = sturm_count(d, e, n, thi, pivmin);
+      const int c = sturm_count(d, e2, n, thi, pivmin);
       if (c > k) { hi = thi; chi = c; }
     }
   }
@@ -190,14 +194,14 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
   // Stop at a few ulps of the spectral radius: below that the Sturm counts
   // are at the round-off of the recurrence.
   const double floor_w = fmax(8.0 * kEps * tnorm, atol);
-  double x = 0.5 * (lo + hi);
+  double x = (x0 > lo && x0 < hi) ? x0 : 0.5 * (lo + hi);
   double v = x;
   bool newton = true, done = false;
   for (int it = 0; it < 200 && !done; ++it) {
     if (hi - lo <= fmax(2.0 * kEps * fmax(fabs(lo), fabs(hi)), floor_w)) break;
     if (it >= 16) newton = false;  // a model step that has not converged by now: bisect
     double S1, S2;
-    const int c = sturm_sums(d, e, n, x, pivmin, &S1, &S2);
+    const int c = sturm_sums(d, e2, n, x, pivmin, &S1, &S2);
     if (c > k) hi = x; else lo = x;
     const bool above = c <= k;
     const double step = pair_step(S1, S2, above, above ? k - c : c - 1 - k);
@@ -211,9 +215,9 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
         const double xc = x + step, del = 2.0 * fabs(step) + small;
         bool ok;
         if (unique && xc >= lo && xc <= hi) ok = true;
-        else if (above && step >= 0.0) ok = sturm_count(d, e, n, xc + del, pivmin) > k;
-        else if (!above && step <= 0.0) ok = sturm_count(d, e, n, xc - del, pivmin) <= k;
-        else ok = sturm_count(d, e, n, xc - del, pivmin) <= k && sturm_count(d, e, n, xc + del, pivmin) > k;
+        else if (above && step >= 0.0) ok = sturm_count(d, e2, n, xc + del, pivmin) > k;
+        else if (!above && step <= 0.0) ok = sturm_count(d, e2, n, xc - del, pivmin) <= k;
+        else ok = sturm_count(d, e2, n, xc - del, pivmin) <= k && sturm_count(d, e2, n, xc + del, pivmin) > k;
         if (ok) {
           v = xc;
           done = true;
@@ -474,17 +478,19 @@ __global__ void __launch_bounds__(kBackWarps * 32) backtransform_kernel(BackArgs
 
 }  // namespace
 
-__global__ void to_f32_kernel(const double* d, const double* e, float* out, int n) {
+// FP32 copies of d and e for the FP32 bracket, and e^2 for the FP64 passes.
+__global__ void prep_levels_kernel(const double* d, const double* e, float* out, double* e2, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     out[i] = (float)d[i];
     out[n + i] = (float)e[i];
+    e2[i] = e[i] * e[i];
   }
 }
 
 void launch_bisect(const TdEigArgs& a, const int* state_block, cudaStream_t s) {
   if (a.nstates <= 0) return;
-  to_f32_kernel<<<(a.nstates + 255) / 256 < 1024 ? (a.nstates + 255) / 256 : 1024, 256, 0, s>>>(a.d, a.e, a.fde,
-                                                                                                a.nstates);
+  prep_levels_kernel<<<(a.nstates + 255) / 256 < 1024 ? (a.nstates + 255) / 256 : 1024, 256, 0, s>>>(
+      a.d, a.e, a.fde, a.e2, a.nstates);
   // One warp per CTA: the long-running threads of the largest blocks then
   // spread over all SMs instead of crowding a few.
   bisect_kernel<<<(a.nstates + 31) / 32, 32, 0, s>>>(a, state_block);
