@@ -125,7 +125,7 @@ struct nrg_ctx {
   std::vector<double> opavg_m1;
   nrg_timing timing{};
   // device buffers
-  nrg::DevBuf meta, vmeta, H, d, e, tau, ev, en, flag, scal, Y, scratch, Z, Zt, T, partial, red, gpart, fde, e2;
+  nrg::DevBuf meta, vmeta, H, d, e, tau, ev, en, flag, scal, Y, scratch, Z, Zt, T, partial, red, gpart, fde, e2, spl;
   nrg::DevBuf ops_a[6], ops_b[6], opptr;
   cudaEvent_t ev_a[8];
   // concurrent whole-GPU tridiagonalizations: side streams, fork/join events,
@@ -381,6 +381,8 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
   ea.fde = c->fde.as<float>();
   c->e2.ensure(sizeof(double) * std::max(P.nstates, 1));
   ea.e2 = c->e2.as<double>();
+  c->spl.ensure(std::max(P.nstates, 1));
+  ea.split = c->spl.as<unsigned char>();
   cudaEvent_t t1 = tm.start();
   launch_bisect(ea, d_state_block, c->stream);
   c->launches += 3;  // FP32 copies, levels, ordering

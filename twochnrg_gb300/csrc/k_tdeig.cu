@@ -136,8 +136,9 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
   const double* db = A.d + so;
   const double* eb = A.e + so;
   int s0 = pos, s1 = pos;
-  while (s0 > 0 && !split_at(db, eb, s0 - 1)) --s0;
-  while (s1 < nb - 1 && !split_at(db, eb, s1)) ++s1;
+  const unsigned char* spl = A.split + so;  // split_at for every position, formed once per call
+  while (s0 > 0 && !spl[s0 - 1]) --s0;
+  while (s1 < nb - 1 && !spl[s1]) ++s1;
   const int n = s1 - s0 + 1;
   const int k = pos - s0;
   const double* d = db + s0;
@@ -478,19 +479,22 @@ __global__ void __launch_bounds__(kBackWarps * 32) backtransform_kernel(BackArgs
 
 }  // namespace
 
-// FP32 copies of d and e for the FP32 bracket, and e^2 for the FP64 passes.
-__global__ void prep_levels_kernel(const double* d, const double* e, float* out, double* e2, int n) {
+// FP32 copies of d and e for the FP32 bracket, e^2 for the FP64 passes, and
+// the splitting test at every position (the last state of a block has e = 0).
+__global__ void prep_levels_kernel(const double* d, const double* e, float* out, double* e2, unsigned char* spl,
+                                   int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     out[i] = (float)d[i];
     out[n + i] = (float)e[i];
     e2[i] = e[i] * e[i];
+    spl[i] = (i + 1 < n) ? (split_at(d, e, i) ? 1 : 0) : 1;
   }
 }
 
 void launch_bisect(const TdEigArgs& a, const int* state_block, cudaStream_t s) {
   if (a.nstates <= 0) return;
   prep_levels_kernel<<<(a.nstates + 255) / 256 < 1024 ? (a.nstates + 255) / 256 : 1024, 256, 0, s>>>(
-      a.d, a.e, a.fde, a.e2, a.nstates);
+      a.d, a.e, a.fde, a.e2, a.split, a.nstates);
   // One warp per CTA: the long-running threads of the largest blocks then
   // spread over all SMs instead of crowding a few.
   bisect_kernel<<<(a.nstates + 31) / 32, 32, 0, s>>>(a, state_block);

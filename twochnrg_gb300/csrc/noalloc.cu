@@ -26,12 +26,12 @@ namespace {
 
 constexpr int kN = NRG_NOALLOC_MAX_N;
 // doubles: A copy, Y, five LU arrays, d/e/tau/ev, FP32 copies of d and e
-// (2 kN floats), e^2, then an integer area
+// (2 kN floats), e^2, the split flags (kN bytes), then an integer area
 constexpr size_t kOffA = 0;
 constexpr size_t kOffY = (size_t)kN * kN;
 constexpr size_t kOffLU = 2 * (size_t)kN * kN;
 constexpr size_t kOffVec = 7 * (size_t)kN * kN;
-constexpr size_t kOffInt = kOffVec + 6 * (size_t)kN;
+constexpr size_t kOffInt = kOffVec + 6 * (size_t)kN + (size_t)kN / 8 + 1;
 constexpr size_t kIntWords = 16 + 8 * (size_t)kN;  // in 4-byte words
 constexpr size_t kScratchDoubles = kOffInt + (kIntWords + 1) / 2 + 8;
 
@@ -41,6 +41,7 @@ struct Layout {
   double *A, *Y, *LU, *d, *e, *tau, *ev;
   float* fde;
   double* e2;
+  unsigned char* split;
   int *queue, *flag, *bsize, *soff, *order, *nvec;
   int64_t *hoff, *yoff;
   int *state_block, *vec_block, *vec_index, *cl_block, *cl_first, *cl_count, *cta_block, *cta_first;
@@ -52,6 +53,7 @@ Layout layout(double* base) {
   L.d = base + kOffVec; L.e = L.d + kN; L.tau = L.e + kN; L.ev = L.tau + kN;
   L.fde = reinterpret_cast<float*>(L.ev + kN);
   L.e2 = L.ev + 2 * kN;
+  L.split = reinterpret_cast<unsigned char*>(L.e2 + kN);
   int* ip = reinterpret_cast<int*>(base + kOffInt);
   L.queue = ip; L.flag = ip + 1; L.bsize = ip + 2; L.soff = ip + 3; L.order = ip + 4; L.nvec = ip + 5;
   L.hoff = reinterpret_cast<int64_t*>(ip + 8); L.yoff = L.hoff + 1;
@@ -127,7 +129,7 @@ extern "C" nrg_status nrg_diag_block_noalloc(int n, const double* a, double* eig
   if (launch_tridiag(ta, 8, 1, s) != cudaSuccess) return NRG_ERR_CUDA;
   TdEigArgs ea{};
   ea.nblocks = 1; ea.bsize = L.bsize; ea.soff = L.soff; ea.d = L.d; ea.e = L.e; ea.ev = L.ev; ea.nstates = n;
-  ea.flag = L.flag; ea.maxn = n; ea.fde = L.fde; ea.e2 = L.e2;
+  ea.flag = L.flag; ea.maxn = n; ea.fde = L.fde; ea.e2 = L.e2; ea.split = L.split;
   launch_bisect(ea, L.state_block, s);
   cluster_kernel<<<1, 32, 0, s>>>(L, n);
   InvIterArgs ia{};

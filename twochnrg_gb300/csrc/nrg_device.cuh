@@ -104,6 +104,7 @@ struct TdEigArgs {
   int maxn;              // largest block (sizes the sort's shared memory)
   float* fde;            // scratch [2*nstates]: FP32 copies of d and e for the FP32 bracket
   double* e2;            // scratch [nstates]: e^2
+  unsigned char* split;  // scratch [nstates]: e_i negligible (the pieces' ends)
 };
 void launch_bisect(const TdEigArgs& a, const int* state_block, cudaStream_t s);
 
