@@ -379,6 +379,47 @@ nrg_status nrg_thermo_run(nrg_ctx* ctx, const nrg_sweep_config* cfg, int reuse_c
 nrg_status nrg_write_thermo(const char* path, int nvalues, const double* temp, const double* value,
                             const double* chain);
 
+/* ---- Wilson chains of non-flat bands ------------------------------------
+ * The sweep's chain is Wilson's analytic one for the flat band
+ * (CNRGchain::SetChainWilson, NRGchainClass.cpp:132-155) unless the caller
+ * sets another: hoppings chi[N] (CNRGchain::GetChin(N), the hopping from site
+ * N to N+1) and on-site energies en[N] (GetEn(N)), N = 0 .. n-1, in the
+ * rescaled units NRG_main uses.  Iteration N then uses chi[N-1] (the
+ * impurity coupling at N = 0) and e_N = en[N]; the free-chain run starts
+ * from chi[0].  apply_alambda = 0 leaves the impurity coupling without the
+ * sqrt(A_Lambda) factor, as NRG_main does for the Campo-Oliveira scheme
+ * (NRG_main.cpp:204-207).  n = 0 restores the Wilson chain.  A sweep needs
+ * n >= nsites.  The two-channel model uses chi for both channels and has no
+ * e_N term (TwoChQS_HN_MatEl). */
+nrg_status nrg_set_chain(nrg_ctx* ctx, int n, const double* chi, const double* en, int apply_alambda);
+
+/* Band types of CNRGCodeHandler::SetChain (NRGcodehandlerClass.cpp:202-400)
+ * with their hybridization functions (HybFuncDefs.cpp). */
+enum {
+  NRG_BAND_CONST = 0,      /* -b Const: Gamma(w) = params[0] (1 without params) */
+  NRG_BAND_LORENTZIAN = 1, /* -b SideDot: the six lanc.in values; Gamma(w) =
+                              params[4]^2 params[2] / ((w - params[1])^2 + params[2]^2) */
+  NRG_BAND_TABLE = 2       /* -b FromFile: (omega, Gamma(omega)) pairs, ascending
+                              omega, linear in between (HybFunc_FromFile) */
+};
+typedef struct {
+  int kind;                /* NRG_BAND_* */
+  int nparams;
+  const double* params;
+  double lambda;
+  double z;                /* z-trick twist (1: none) */
+  int disc_scheme;         /* 0 usual, 1 Campo-Oliveira (not for NRG_BAND_LORENTZIAN) */
+  double band_offset;      /* the band is [-(1+offset), 1-offset] (ChemPot) */
+} nrg_band;
+
+/* The chain of a band by the reference's Lanczos procedure
+ * (CNRGchain::SetChainLanczos, NRGchainClass.cpp:234-520, with CalcF2 and
+ * CalcFabmEabm): chi[0..nsites), en[0..nsites) and Fsq = int Gamma / Gamma_ref.
+ * The discretization keeps ceil(nsites/2) intervals per side, so the last
+ * coefficients carry its truncation; NRG_main asks for max(Nsitesmax, 100)
+ * sites (NRGcodehandlerClass.cpp:219).  Host code, no device. */
+nrg_status nrg_chain_lanczos(const nrg_band* band, int nsites, double* chi, double* en, double* fsq);
+
 /* ---- .bin snapshots in the reference's layout ---------------------------
  * One DM-NRG shell as NRG_main saves it with UpdateBefCut = 1
  * (CNRGCodeHandler::SaveArrays, NRGcodehandlerClass.cpp:887-932). */

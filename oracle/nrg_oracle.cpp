@@ -1622,16 +1622,24 @@ void* oracle_run(const oracle_config* cfg) {
   const double pi = 3.141592653589793238462643383279502884197169;
   double Lambda = cfg->lambda;
   double HLF = 0.5 * (1.0 + 1.0 / Lambda);
+  // a caller's chain (chi_N, e_N) replaces SetChainWilson's; the impurity
+  // coupling then carries sqrt(A_Lambda) unless chain_alambda is 0
+  // (NRG_main.cpp:204-207)
+  const bool custom = cfg->chain_len > 0;
+  if (custom && cfg->chain_len < cfg->nsites) { g_err = "chain shorter than nsites"; delete R; return nullptr; }
   double ALambda = std::sqrt(0.5 * std::log(Lambda) * (Lambda + 1) / (Lambda - 1));
+  if (custom && !cfg->chain_alambda) ALambda = 1.0;
   double eps = cfg->degen_eps > 0 ? cfg->degen_eps : 1.0e-18;
   int nthreads = cfg->nthreads > 0 ? cfg->nthreads : 1;
   // SetChainWilson (NRGchainClass.cpp:132-155).
   auto chin = [&](int N) {
+    if (custom) return cfg->chain_chi[N];
     double d0 = 1.0 - std::pow(Lambda, -((double)N + 1.0));
     double d1 = std::sqrt(1.0 - std::pow(Lambda, -(2.0 * (double)N + 1.0)));
     double d2 = std::sqrt(1.0 - std::pow(Lambda, -(2.0 * (double)N + 3.0)));
     return d0 / (d1 * d2);
   };
+  auto onsite = [&](int N) { return custom ? cfg->chain_en[N] : 0.0; };
   c.m.kind = cfg->model;
   R->model = cfg->model;
   R->lambda = Lambda;
@@ -1803,8 +1811,10 @@ void* oracle_run(const oracle_config* cfg) {
     R->it.push_back(std::move(I));
     N0 = 1;
   }
+  const int ien = nchan + 1;  // e_N's place in ParamsHN (NRG_main.cpp:272-276)
   for (int N = N0; N < cfg->nsites; ++N) {
     OracleIter I;
+    P[ien] = onsite(N);  // GetEn(Nsites) (NRG_main.cpp:198, 408-413)
     I.params = P;
     double DN = HLF * std::pow(Lambda, (-(N - 1) / 2.0));
     build_basis(c.m, cut, ab, dm);

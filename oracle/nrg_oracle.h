@@ -24,6 +24,10 @@ typedef struct {
   int dm;             /* keep DM-NRG shells (UpdateBefCut = 1, c_d); 1chQS only */
   int chain;          /* the free Wilson chain of calcdens = 3 (H_0 = first site, iterations 1..nsites-1) */
   double delta_sc;    /* gap of the superconducting leads (1chS, 1chSz) */
+  const double* chain_chi; /* a Wilson chain other than the flat band's: chi_N, */
+  const double* chain_en;  /* e_N for N < chain_len (0: the flat band's) */
+  int chain_len;
+  int chain_alambda;       /* sqrt(A_Lambda) on the impurity coupling */
 } oracle_config;
 
 /* DM-NRG parameters (DM_NRG command line, DM_NRG_CommandLineRead.cpp). */

@@ -27,7 +27,9 @@ class _Cfg(ctypes.Structure):
                 ("gamma1", ctypes.c_double), ("gamma2_or_B", ctypes.c_double),
                 ("degen_eps", ctypes.c_double), ("nthreads", ctypes.c_int),
                 ("capture_iter", ctypes.c_int), ("dm", ctypes.c_int), ("chain", ctypes.c_int),
-                ("delta_sc", ctypes.c_double)]
+                ("delta_sc", ctypes.c_double), ("chain_chi", ctypes.POINTER(ctypes.c_double)),
+                ("chain_en", ctypes.POINTER(ctypes.c_double)), ("chain_len", ctypes.c_int),
+                ("chain_alambda", ctypes.c_int)]
 
 
 class _DmParams(ctypes.Structure):
@@ -139,14 +141,23 @@ def _arr(ptr, n, dtype):
 
 def run(model: str, nsites: int, ncutoff: int, lam: float, U: float, ed: float, gamma1: float,
         gamma2_or_B: float = 0.0, nthreads: int = 1, capture_iter: int = -1,
-        degen_eps: float = 0.0, blas_threads: int = 1, chain: bool = False, delta_sc: float = 0.0) -> Sweep:
+        degen_eps: float = 0.0, blas_threads: int = 1, chain: bool = False, delta_sc: float = 0.0,
+        wilson=None, alambda: bool = True) -> Sweep:
     """One sweep.  chain=True: the free Wilson chain of calcdens = 3 (U, ed and
     the couplings are ignored; iteration 0 is the first site alone).  delta_sc:
-    the leads' gap of the superconducting-lead models."""
+    the leads' gap of the superconducting-lead models.  wilson: a chain (chi, en)
+    other than the flat band's."""
     L = lib()
     L.oracle_blas_threads(int(blas_threads))
     cfg = _Cfg(MODELS[model], nsites, ncutoff, lam, U, ed, gamma1, gamma2_or_B, degen_eps,
                nthreads, capture_iter, 0, 1 if chain else 0, delta_sc)
+    if wilson is not None:
+        wc = np.ascontiguousarray(wilson[0], dtype=np.float64)
+        we = np.ascontiguousarray(wilson[1], dtype=np.float64)
+        cfg.chain_chi = wc.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        cfg.chain_en = we.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        cfg.chain_len = len(wc)
+        cfg.chain_alambda = 1 if alambda else 0
     h = L.oracle_run(ctypes.byref(cfg))
     if not h:
         raise RuntimeError("oracle: " + L.oracle_last_error().decode())

@@ -14,7 +14,8 @@
 //          1chS    one-channel Anderson with superconducting leads, (S) basis
 //                  (SymNo 7 / ModelNo 0)
 //          1chSz   the same in the (Sz) basis (SymNo 8 / ModelNo 0); Gamma2|B = B
-//   optional 9th argument: Delta_SC of the superconducting leads
+//   optional 9th argument: Delta_SC of the superconducting leads; optional
+//   10th: a chain file ("chi_N e_N" per line) instead of the flat band's
 //          2chQS   two-channel Anderson, (Q,S) basis: the impurity H_{-1} of
 //                  OneChQS_SetAnderson_Hm1 coupled to both channels through
 //                  TwoChQS_HN_MatEl with f_ch1 = f_ch2 = d; last arg = Gamma2
@@ -33,6 +34,7 @@
 #include "NRGOpMatRules.hpp"
 #include "NRG_main.hpp"
 #include "TwoChQS.hpp"
+#include "NRGbandtypes.hpp"
 
 #ifndef pi
 #define pi 3.141592653589793238462643383279502884197169
@@ -59,7 +61,52 @@ static void print_iter(int N, const std::vector<double>& ParamsHN, CNRGarray& Ae
   printf("CUT %.17g %d\n", Ecut, nkept);
 }
 
+// Wilson chain of a non-flat hybridization by the reference's Lanczos
+// procedure (CNRGchain::SetChainLanczos, NRGchainClass.cpp:234-520), set up as
+// CNRGCodeHandler::SetChain does for the band types (NRGcodehandlerClass.cpp:
+// 202-400):
+//   ref_harness lanczos <kind> <Lambda> <z> <DiscScheme> <BandOffset> <Nsites> [params...]
+//   kind: const (params: Gamma0), lorentzian (the six lanc.in values),
+//         table (omega, Gamma(omega) pairs, ascending omega)
+// Output: "CHAIN n chi_n e_n" lines and "FSQ Fsq".
+static int lanczos_main(int argc, char** argv) {
+  if (argc < 8) { fprintf(stderr, "usage: lanczos kind Lambda z disc offset Nsites [params]\n"); return 2; }
+  std::string kind = argv[2];
+  CNRGchain chain(atof(argv[3]));
+  chain.z_twist = atof(argv[4]);
+  chain.DiscScheme = atoi(argv[5]);
+  chain.BandOffset = atof(argv[6]);
+  int N = atoi(argv[7]);
+  static std::vector<double> prm;
+  for (int k = 8; k < argc; ++k) prm.push_back(atof(argv[k]));
+  chain.HybFuncParams = &prm;
+  if (kind == "const") {
+    chain.HybFunction = HybFunc_Const;
+    chain.HybFuncWithEn = chain.DiscScheme == 1 ? HybFunc_Const_divEn : HybFunc_Const_timesEn;
+  } else if (kind == "lorentzian") {
+    chain.HybFunction = HybFunc_Lorentzian;
+    chain.HybFuncWithEn = HybFunc_Lorentzian_timesEn;
+  } else if (kind == "table") {
+    chain.HybFunction = HybFunc_FromFile;
+    chain.HybFuncWithEn = chain.DiscScheme == 1 ? HybFunc_FromFile_divEn : HybFunc_FromFile_timesEn;
+    if (chain.GetHyb_w(0.0) == 0.0) { chain.HybRef = 1.0; chain.HybRefIsSet = true; }
+  } else {
+    fprintf(stderr, "unknown band kind %s\n", kind.c_str());
+    return 2;
+  }
+  FILE* real_out = fdopen(dup(fileno(stdout)), "w");
+  fflush(stdout);
+  dup2(fileno(stderr), fileno(stdout));
+  stdout = real_out;
+  chain.SetChainLanczos(N);
+  for (int n = 0; n < N; ++n) printf("CHAIN %d %.17g %.17g\n", n, chain.GetChin(n), chain.GetEn(n));
+  printf("FSQ %.17g\n", chain.Fsq);
+  fflush(stdout);
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc > 1 && std::string(argv[1]) == "lanczos") return lanczos_main(argc, argv);
   if (argc < 9) {
     fprintf(stderr, "usage: %s model Nsites Ncutoff Lambda U ed Gamma1 Gamma2|B\n", argv[0]);
     return 2;
@@ -82,6 +129,16 @@ int main(int argc, char** argv) {
   double HalfLambdaFactor = 0.5 * (1.0 + 1.0 / Lambda);  // NRGcodehandlerClass.cpp:142-146, z=1
   CNRGchain chain(Lambda);
   chain.SetChainWilson(Nsites > 100 ? Nsites : 100);      // NRGcodehandlerClass.cpp:222-227
+  // optional 10th argument: a file of "chi_N e_N" lines replacing the chain
+  // (as CNRGCodeHandler::SetChain would for another band type)
+  if (argc > 10) {
+    FILE* cf = fopen(argv[10], "r");
+    if (!cf) { fprintf(stderr, "cannot read %s\n", argv[10]); return 2; }
+    chain.chin.clear(); chain.en.clear();
+    double a, b;
+    while (fscanf(cf, "%lf %lf", &a, &b) == 2) { chain.chin.push_back(a); chain.en.push_back(b); }
+    fclose(cf);
+  }
   double ALambda = sqrt(0.5 * log(Lambda) * (Lambda + 1) / (Lambda - 1));  // NRG_main.cpp:205-207
 
   CNRGarray Aeig;
@@ -246,6 +303,7 @@ int main(int argc, char** argv) {
     printf("\n");
   }
 
+  ParamsHN[nchan + 1] = chain.GetEn(0);  // NRG_main.cpp:198, 272-273
   for (int N = 0; N < Nsites; ++N) {
     double DN = HalfLambdaFactor * pow(Lambda, (-(N - 1) / 2.0));  // NRG_main.cpp:283
     BuildBasis(CommonQNs, totSpos, &AeigCut, &Abasis, &SingleSite, 0);
@@ -276,6 +334,7 @@ int main(int argc, char** argv) {
     for (int b = 0; b < AeigCut.NumBlocks(); ++b) printf(" %d", AeigCut.GetBlockSize(b));
     printf("\n");
     for (int ich = 0; ich < nchan; ++ich) ParamsHN[ich + 1] = chain.GetChin(N);  // NRG_main.cpp:402-405
+    if ((int)ParamsHN.size() > nchan + 2) ParamsHN[nchan + 1] = chain.GetEn(N + 1);  // NRG_main.cpp:408-413
     if (model == "1chS" || model == "1chSz")
       ParamsHN[nchan + 2] = chain.ScaleFactor(N) * deltaSC;  // NRG_main.cpp:414-419
   }

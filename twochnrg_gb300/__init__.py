@@ -161,6 +161,31 @@ def write_code_pars(directory: str, lam: float, nsites: int, name: str) -> None:
         raise NRGError(st, f"cannot write ThisCodePars.dat into {directory}")
 
 
+BAND_CONST, BAND_LORENTZIAN, BAND_TABLE = 0, 1, 2
+BANDS = {"const": BAND_CONST, "lorentzian": BAND_LORENTZIAN, "table": BAND_TABLE}
+
+
+class _Band(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("nparams", ctypes.c_int), ("params", _DP), ("lambda_", ctypes.c_double),
+                ("z", ctypes.c_double), ("disc_scheme", ctypes.c_int), ("band_offset", ctypes.c_double)]
+
+
+def chain_lanczos(kind: str, nsites: int, lam: float, params=(), z: float = 1.0, disc_scheme: int = 0,
+                  band_offset: float = 0.0):
+    """Wilson chain of a band by the reference's Lanczos procedure
+    (nrg_chain_lanczos): returns (chi, en, Fsq).  Needs no device."""
+    L = load_library()
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    chi = np.zeros(int(nsites)); en = np.zeros(int(nsites)); fsq = ctypes.c_double()
+    b = _Band(BANDS[kind], len(p), p.ctypes.data_as(_DP) if len(p) else None, float(lam), float(z),
+              int(disc_scheme), float(band_offset))
+    st = L.nrg_chain_lanczos(ctypes.byref(b), int(nsites), chi.ctypes.data_as(_DP), en.ctypes.data_as(_DP),
+                             ctypes.byref(fsq))
+    if st != 0:
+        raise NRGError(st, "nrg_chain_lanczos failed")
+    return chi, en, fsq.value
+
+
 class _Thermo(ctypes.Structure):
     _fields_ = [("nvalues", ctypes.c_int), ("temp", _DP), ("suscep", _DP), ("suscep_chain", _DP),
                 ("suscep_imp", _DP), ("entropy", _DP), ("entropy_chain", _DP), ("entropy_imp", _DP),
@@ -278,6 +303,8 @@ def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     L.nrg_thermo_run.argtypes = [ctypes.c_void_p, ctypes.POINTER(SweepConfig), ctypes.c_int,
                                  ctypes.POINTER(_Thermo)]
     L.nrg_write_thermo.argtypes = [ctypes.c_char_p, ctypes.c_int, _dp, _dp, _dp]
+    L.nrg_set_chain.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, ctypes.c_int]
+    L.nrg_chain_lanczos.argtypes = [ctypes.POINTER(_Band), ctypes.c_int, _dp, _dp, _dp]
     L.nrg_sweep_batch.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(SweepConfig), ctypes.c_int,
                                   ctypes.c_int, _dp, _dp, _ip, _dp]
     _lib = L
@@ -486,6 +513,19 @@ class Engine:
         v = ctypes.c_double()
         self._check(self.L.nrg_fp64_peak(self.h, ctypes.byref(v)))
         return v.value
+
+    def set_chain(self, chi=None, en=None, alambda: bool = True):
+        """Use the chain (chi_N, e_N) in the following sweeps (nrg_set_chain);
+        no arguments: back to the flat band's Wilson chain."""
+        if chi is None:
+            self._check(self.L.nrg_set_chain(self.h, 0, None, None, 1))
+            return
+        self._chain = (np.ascontiguousarray(chi, dtype=np.float64), np.ascontiguousarray(en, dtype=np.float64))
+        c, e = self._chain
+        if len(c) != len(e):
+            raise ValueError("chi and en must have the same length")
+        self._check(self.L.nrg_set_chain(self.h, len(c), c.ctypes.data_as(_DP), e.ctypes.data_as(_DP),
+                                         1 if alambda else 0))
 
     def sweep_chain(self, model: str, nsites: int, ncutoff: int, lam: float, degen_eps: float = 0.0,
                     precision: int = PREC_FP64, fetch: bool = True) -> SweepResult:

@@ -20,7 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["engine.cu", "k_assemble.cu", "k_tridiag.cu", "k_tdeig.cu", "k_cut.cu", "k_update.cu",
               "k_dm.cu", "noalloc.cu"]
-CXX_SOURCES = ["nrg_model.cpp", "binfile.cpp", "thermofile.cpp"]
+CXX_SOURCES = ["nrg_model.cpp", "binfile.cpp", "thermofile.cpp", "chain.cpp"]
 
 
 def _nvcc() -> str:

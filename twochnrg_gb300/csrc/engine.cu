@@ -155,6 +155,9 @@ struct nrg_ctx {
   std::vector<double> th_temp, th_sus, th_sus_chain, th_sus_imp, th_ent, th_ent_chain, th_ent_imp;
   double th_chain_ms = 0.0, th_imp_ms = 0.0, th_total_ms = 0.0;
   int th_chain_reused = 0;
+  // the Wilson chain set with nrg_set_chain (empty: the flat band's)
+  std::vector<double> chain_chi, chain_en;
+  bool chain_alambda = true;
 };
 
 namespace nrg {
@@ -171,11 +174,12 @@ double chin(double lambda, int N) {
   return d0 / (d1 * d2);
 }
 
-// chi_{-1} of NRG_main.cpp:194-207 with the sqrt(A_Lambda) factor.
-double chi_m1(double lambda, double gamma) {
+// chi_{-1} of NRG_main.cpp:194-207 with the sqrt(A_Lambda) factor (left out
+// for the Campo-Oliveira discretization, :204-207).
+double chi_m1(double lambda, double gamma, bool alambda = true) {
   double HLF = 0.5 * (1.0 + 1.0 / lambda);
   double c = std::sqrt(2.0 * gamma / kPi) / (std::sqrt(lambda) * HLF);
-  return c * std::sqrt(0.5 * std::log(lambda) * (lambda + 1) / (lambda - 1));
+  return alambda ? c * std::sqrt(0.5 * std::log(lambda) * (lambda + 1) / (lambda - 1)) : c;
 }
 
 struct Timer {
@@ -849,16 +853,25 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
     }
   }
 
-  double chi[2] = {chi_m1(lambda, chain ? 0.0 : cfg->gamma1), 0.0};
-  if (m.nchan == 2) chi[1] = chi_m1(lambda, chain ? 0.0 : cfg->gamma2_or_B);
-  const double eN = 0.0;  // flat band (CNRGchain::GetEn of SetChainWilson)
+  // The chain: Wilson's (SetChainWilson: e_N = 0) or the caller's
+  // (nrg_set_chain); iteration N uses hop(N-1) (chi_{-1} at N = 0) and
+  // e_N = onsite(N) (NRG_main.cpp:198, 402-413).
+  const bool custom = !c->chain_chi.empty();
+  if (custom && (int)c->chain_chi.size() < cfg->nsites)
+    throw NrgError(NRG_ERR_ARG, "the chain set with nrg_set_chain is shorter than nsites");
+  auto hop = [&](int n) { return custom ? c->chain_chi[n] : chin(lambda, n); };
+  auto onsite = [&](int n) { return custom ? c->chain_en[n] : 0.0; };
+  const bool alam = !custom || c->chain_alambda;
+  double chi[2] = {chi_m1(lambda, chain ? 0.0 : cfg->gamma1, alam), 0.0};
+  if (m.nchan == 2) chi[1] = chi_m1(lambda, chain ? 0.0 : cfg->gamma2_or_B, alam);
+  double eN = onsite(0);
   int N0 = 0;
   if (chain && !chain_q) {
     // chi_m1 = chiN(0) for every channel; H_0 is recorded as iteration 0 with
     // the thermodynamics CalcThermo takes before the loop, at
     // D = HLF Lambda^(-(Nsites0-2)/2) = D_0.
-    chi[0] = chin(lambda, 0);
-    chi[1] = m.nchan == 2 ? chin(lambda, 0) : 0.0;
+    chi[0] = hop(0);
+    chi[1] = m.nchan == 2 ? hop(0) : 0.0;
     IterResult R;
     R.params = {lambda, chi[0], chi[1], eN};
     R.qn = st.blk.qn; R.bsize = st.blk.size; R.kept_bsize = st.blk.size;
@@ -874,6 +887,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
   const bool sc = m.kind == MODEL_1CHS || m.kind == MODEL_1CHSZ;
   for (int N = N0; N < cfg->nsites; ++N) {
     IterResult R;
+    eN = onsite(N);
     const double delta = !sc ? 0.0 : (N == 0 ? cfg->delta_sc
                                              : std::pow(lambda, 0.5 * (double)(N - 1)) / HLF * cfg->delta_sc);
     R.params = {lambda, chi[0], sc ? delta : chi[1], eN};
@@ -1038,7 +1052,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
     kept_en = new_kept_en;
     S.ops = newops;
     S.cur = nxt;
-    for (int ich = 0; ich < m.nchan; ++ich) chi[ich] = chin(lambda, N);
+    for (int ich = 0; ich < m.nchan; ++ich) chi[ich] = hop(N);
     c->iters.push_back(std::move(R));
   }
   CU(cudaEventRecord(span1, c->stream));
@@ -1478,6 +1492,9 @@ void thermo_run_impl(nrg_ctx* c, const nrg_sweep_config* cfg, int reuse_chain) {
       const nrg_status st = nrg_create(c->device, &c->chain_ctx);
       if (st != NRG_OK) throw NrgError(st, "cannot create the free-chain context");
     }
+    c->chain_ctx->chain_chi = c->chain_chi;
+    c->chain_ctx->chain_en = c->chain_en;
+    c->chain_ctx->chain_alambda = c->chain_alambda;
     nrg_ctx* cc = c->chain_ctx;
     nrg_status cst = NRG_OK;
     std::string cerr;
@@ -2114,6 +2131,16 @@ nrg_status nrg_sweep_run_dm(nrg_ctx* ctx, const nrg_sweep_config* cfg) {
     CU(cudaSetDevice(ctx->device));
     sweep_run(ctx, cfg, true);
   });
+  return NRG_OK;
+}
+
+nrg_status nrg_set_chain(nrg_ctx* ctx, int n, const double* chi, const double* en, int apply_alambda) {
+  if (!ctx || n < 0 || (n > 0 && (!chi || !en))) return NRG_ERR_ARG;
+  ctx->chain_chi.assign(chi, chi + n);
+  ctx->chain_en.assign(en, en + n);
+  ctx->chain_alambda = apply_alambda != 0;
+  ctx->chain_valid = false;  // stored free-chain values were for the previous chain
+  if (ctx->chain_ctx) nrg_set_chain(ctx->chain_ctx, n, chi, en, apply_alambda);
   return NRG_OK;
 }
 
