@@ -299,7 +299,7 @@ typedef struct {
   double bbroad;      /* -e, log-Gaussian width b */
   double twindow;     /* -w, 2: |E_j - E_i| < twindow T/D_N uses the Gaussian */
   double broadtemp;   /* -B, 0.8: width of that Gaussian */
-  double site_dim;    /* states per Wilson site in the FDM weights (4, DM_NRG.cpp:292) */
+  double site_dim;    /* states per Wilson site in the FDM weights (4, DM_NRG.cpp:292; 16 for two channels) */
   int nw;             /* -n, frequencies per shell of the default grid */
 } nrg_dm_params;
 
@@ -308,7 +308,11 @@ typedef struct {
  * the sweep of nrg_sweep_run, but the operators f_N and c_d are rotated into
  * every shell's full eigenbasis, and each shell's energies, Kept flags,
  * eigenvectors, basis and c_d stay on the device (what SaveArrays writes,
- * NRGcodehandlerClass.cpp:887-932).  NRG_MODEL_1CH_QS only. */
+ * NRGcodehandlerClass.cpp:887-932).  NRG_MODEL_1CH_QS, and NRG_MODEL_2CH_QS
+ * (operators f_N1, f_N2 and c_d; the reference has no two-channel c_d rule
+ * and its DM_NRG is one-channel only, so the two-channel shells take the
+ * one-channel recoupling of c_d across the 16-state site and site_dim = 16
+ * in nrg_dm_params; they cannot be written as .bin snapshots). */
 nrg_status nrg_sweep_run_dm(nrg_ctx* ctx, const nrg_sweep_config* cfg);
 int nrg_dm_num_shells(const nrg_ctx* ctx);
 

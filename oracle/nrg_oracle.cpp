@@ -296,7 +296,8 @@ Basis site_2chQS() {
 }
 
 // ---------------------------------------------------------------- rules
-enum OpRule { R_F_QS = 1, R_FUP_QSZ, R_FDN_QSZ, R_F1_2CH, R_F2_2CH, R_IMPONLY, R_CD_QS, R_F_S, R_FUP_SZ, R_FDN_SZ };
+enum OpRule { R_F_QS = 1, R_FUP_QSZ, R_FDN_QSZ, R_F1_2CH, R_F2_2CH, R_IMPONLY, R_CD_QS, R_F_S, R_FUP_SZ, R_FDN_SZ,
+              R_CD_2CH };
 enum Check { C_DIAG = 1, C_QS_CD, C_Q_CD, C_2CH_CD, C_S_CD, C_SZ_UP, C_SZ_DN };
 
 struct Model {
@@ -671,6 +672,43 @@ double op_cd_QS(Ctx& c, const Basis& ab, int ist, int jst) {
   return f;
 }
 
+// The impurity d operator across the 16-state two-channel site.  The
+// reference has no such rule (TwoChQS keeps no c_d); this restates
+// OneChQS_cd_MatEl's recoupling (above) with the site multiplet unchanged:
+// the two types are members of one multiplet (TwoChQS_SpSm_table), the site
+// member is the same on both sides, and the Fermi sign is (-1) to the site's
+// fermion number Q + 2.
+double op_cd_2ch(Ctx& c, const Basis& ab, int ist, int jst) {
+  const Basis& ss = c.m.site;
+  int ti = ab.itype[ist], tj = ab.itype[jst];
+  if (twoch_spsm(ti, tj) == 0.0) return 0.0;
+  double Si = qn_from_st(ab, ist, 1), Sj = qn_from_st(ab, jst, 1);
+  int pos;
+  int bi = ss.block_of(ti, pos), bj = ss.block_of(tj, pos);
+  double Qt = ss.q(bi, 0), St = ss.q(bi, 1);
+  double Scfi = Si - ss.q(bi, 2), Scfj = Sj - ss.q(bj, 2);
+  int nsite = (int)std::lround(Qt) + 2;
+  double FermiSign = (nsite % 2 == 1) ? -1.0 : 1.0;
+  double sigma = Sj - Si;
+  double a3 = c.cg(Si, Si, 0.5, sigma, Sj, Sj);
+  if (dEq(a3, 0.0)) {
+    sigma = Si - Sj;
+    a3 = c.cg(Si, Si, 0.5, sigma, Sj, Sj);
+    if (dEq(a3, 0.0)) return 0.0;
+  }
+  double f = 0.0;
+  for (double Szcfj = -Scfj; Szcfj <= Scfj; Szcfj += 1.0) {
+    double Szcfi = Szcfj - sigma;
+    double Sztj = Sj - Szcfj, Szti = Si - Szcfi;
+    if (!dEq(Szti, Sztj) || std::fabs(Sztj) > St) continue;  // the same member, and it exists
+    double a0 = c.cg(Scfi, Szcfi, St, Szti, Si, Si);
+    double a1 = c.cg(Scfj, Szcfj, St, Sztj, Sj, Sj);
+    double a2 = c.cg(Scfi, Szcfi, 0.5, sigma, Scfj, Szcfj);
+    f += a0 * a1 * a2 * FermiSign;
+  }
+  return f / a3;
+}
+
 // OneChS_fN_MatEl (OpMatRules.cpp:1555-1654): a spin-1/2 site state is
 // looked up as (its (S,Sz) site block) + 1, a missing one giving 0.
 double op_f_S(Ctx& c, const Basis& ab, int ist, int jst) {
@@ -710,6 +748,7 @@ double op_rule(Ctx& c, int rule, const Basis& ab, int ist, int jst) {
     case R_F2_2CH: return op_f_2ch(c, ab, ist, jst, 2);
     case R_IMPONLY: return ab.itype[ist] == ab.itype[jst] ? 1.0 : 0.0;  // ImpOnly_MatEl OpMatRules.cpp:265
     case R_CD_QS: return op_cd_QS(c, ab, ist, jst);
+    case R_CD_2CH: return op_cd_2ch(c, ab, ist, jst);
     case R_F_S: return op_f_S(c, ab, ist, jst);
     // OneChSz_fN_MatEl (OpMatRules.cpp:1986-2014)
     case R_FUP_SZ: return ab.stcf[ist] == ab.stcf[jst] ? onechS_fd(1, ab.itype[jst], ab.itype[ist]) : 0.0;
@@ -1377,7 +1416,8 @@ void dm_backward(Ctx& c, const std::vector<DmShell>& sh, const DmParams& p, std:
               int jb = abNp1.block_of(cj, pos);
               if (ti != abNp1.itype[cj] || ib != jb) continue;
               double Si = abNp1.totalS ? abNp1.q(ib, abNp1.sqn[0]) : 0.0;
-              double St = c.m.site.totalS ? c.m.site.q(ti, c.m.site.sqn[0]) : 0.0;
+              const int tb = c.m.site.block_of(ti, pos);
+              double St = c.m.site.totalS ? c.m.site.q(tb, c.m.site.sqn[0]) : 0.0;
               double cgf = 0.0;
               for (double Sz = -Si; Sz <= Si; Sz += 1.0) {
                 double x = c.cg(Sold, Sold, St, Sz - Sold, Si, Sz);
@@ -1644,8 +1684,8 @@ void* oracle_run(const oracle_config* cfg) {
   R->model = cfg->model;
   R->lambda = Lambda;
   const bool dm = cfg->dm != 0;
-  if (dm && cfg->model != ORACLE_MODEL_1CHQS) {
-    g_err = "DM-NRG shells are restated for the one-channel |Q S> model only"; delete R; return nullptr;
+  if (dm && cfg->model != ORACLE_MODEL_1CHQS && cfg->model != ORACLE_MODEL_2CHQS) {
+    g_err = "DM-NRG shells are restated for the |Q S> models only"; delete R; return nullptr;
   }
   // calcdens = 3: the free Wilson chain (ModelNo 3 with ZeroParams,
   // NRGcodehandlerClass.cpp:85-91; CodeHandler_ModelSwitch.cpp:377-420,
@@ -1770,9 +1810,17 @@ void* oracle_run(const oracle_config* cfg) {
     c.m.site = site_2chQS(); c.m.totS = {1};
     Mat f; std::vector<Mat> avg;
     hm1_QS(Lambda, HLF, cfg->U, cfg->ed, eig, f, avg);
-    mats.push_back(f); mats.push_back(f); for (auto& x : avg) mats.push_back(x);
-    c.m.op_rule = {R_F1_2CH, R_F2_2CH, R_IMPONLY, R_IMPONLY, R_IMPONLY};
-    c.m.op_check = {C_2CH_CD, C_2CH_CD, C_DIAG, C_DIAG, C_DIAG};
+    if (dm) {
+      // f_N of both channels and c_d, all copies of d at H_{-1}.
+      Mat f2 = f, cd = f; cd.name = "cdot1";
+      mats.push_back(f); mats.push_back(f2); mats.push_back(cd);
+      c.m.op_rule = {R_F1_2CH, R_F2_2CH, R_CD_2CH};
+      c.m.op_check = {C_2CH_CD, C_2CH_CD, C_2CH_CD};
+    } else {
+      mats.push_back(f); mats.push_back(f); for (auto& x : avg) mats.push_back(x);
+      c.m.op_rule = {R_F1_2CH, R_F2_2CH, R_IMPONLY, R_IMPONLY, R_IMPONLY};
+      c.m.op_check = {C_2CH_CD, C_2CH_CD, C_DIAG, C_DIAG, C_DIAG};
+    }
     double chi2 = std::sqrt(2.0 * cfg->gamma2_or_B / pi) / (std::sqrt(Lambda) * HLF) * ALambda;
     P = {Lambda, chi1, chi2, 0.0, 0.0};
     nchan = 2;
@@ -1781,7 +1829,7 @@ void* oracle_run(const oracle_config* cfg) {
   }
   for (size_t i = 0; i < mats.size(); ++i) {
     if (c.m.op_rule[i] == R_IMPONLY) { mats[i].need_old = true; mats[i].calc_avg = true; }
-    else if (c.m.op_rule[i] == R_CD_QS) { mats[i].need_old = true; mats[i].calc_avg = false; }
+    else if (c.m.op_rule[i] == R_CD_QS || c.m.op_rule[i] == R_CD_2CH) { mats[i].need_old = true; mats[i].calc_avg = false; }
     else { mats[i].need_old = false; mats[i].calc_avg = false; }
   }
   R->nqn = (cfg->model == ORACLE_MODEL_1CHQ || cfg->model == ORACLE_MODEL_1CHS || cfg->model == ORACLE_MODEL_1CHSZ)
@@ -1853,7 +1901,7 @@ void* oracle_run(const oracle_config* cfg) {
       cut_states(eig, full, 2 * eig.nstates(), eps);
       update_matrices(c, full, ab, mats, nthreads);
       DmShell shl;
-      shl.ab = ab; shl.full = full; shl.cd = mats[1];
+      shl.ab = ab; shl.full = full; shl.cd = mats.back();
       R->dm.push_back(std::move(shl));
     }
     cut_states(eig, cut, cfg->ncutoff, eps);
@@ -1923,7 +1971,7 @@ int oracle_dm_spectral(void* h, const oracle_dm_params* prm, const double* omega
   if (R->dm.empty()) { g_err = "run has no DM-NRG shells"; return -1; }
   Ctx c;
   c.m.kind = R->model;
-  c.m.site = site_1chQS();
+  c.m.site = R->model == ORACLE_MODEL_2CHQS ? site_2chQS() : site_1chQS();
   DmParams p{R->lambda, prm->temp, prm->betabar, prm->bbroad, prm->twindow, prm->broadtemp, prm->site_dim, 0.0};
   dm_temperature(p, (int)R->dm.size(), prm->mtemp, prm->temp);
   std::vector<RhoBlocks> rho;
@@ -1957,7 +2005,7 @@ double oracle_dm_shell_term(void* h, const oracle_dm_params* prm, int N, double 
   if (R->dm.empty() || N < 0 || N >= (int)R->dm.size()) return 0.0;
   Ctx c;
   c.m.kind = R->model;
-  c.m.site = site_1chQS();
+  c.m.site = R->model == ORACLE_MODEL_2CHQS ? site_2chQS() : site_1chQS();
   DmParams p{R->lambda, prm->temp, prm->betabar, prm->bbroad, prm->twindow, prm->broadtemp, prm->site_dim, 0.0};
   dm_temperature(p, (int)R->dm.size(), prm->mtemp, prm->temp);
   std::vector<RhoBlocks> rho;

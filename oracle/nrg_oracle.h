@@ -21,7 +21,7 @@ typedef struct {
   double degen_eps;   /* SetDegen tolerance, <=0 -> 1e-18 */
   int nthreads;       /* host threads over blocks / block pairs */
   int capture_iter;   /* iteration whose DiagHN inputs/H are kept, -1 none */
-  int dm;             /* keep DM-NRG shells (UpdateBefCut = 1, c_d); 1chQS only */
+  int dm;             /* keep DM-NRG shells (UpdateBefCut = 1, c_d); 1chQS and 2chQS */
   int chain;          /* the free Wilson chain of calcdens = 3 (H_0 = first site, iterations 1..nsites-1) */
   double delta_sc;    /* gap of the superconducting leads (1chS, 1chSz) */
   const double* chain_chi; /* a Wilson chain other than the flat band's: chi_N, */

@@ -238,12 +238,21 @@ def dm_temp_default(lam: float, nsites: int, betabar: float = 0.727) -> float:
 
 def dm_spectral(nsites: int, ncutoff: int, lam: float, U: float, ed: float, gamma: float, temp: float,
                 bbroad: float, nw: int = 4, omegas=None, betabar: float = 0.727, twindow: float = 2.0,
-                broadtemp: float = 0.8, site_dim: float = 4.0, nthreads: int = 1, mtemp: int = -1):
-    """One-channel |Q S> Anderson model: forward sweep saving the DM-NRG
-    shells (UpdateBefCut = 1, c_d), then the FDM density-matrix backward sweep
-    and the c_d spectral function.  Returns (omega, A, rho_trace per shell)."""
+                broadtemp: float = 0.8, site_dim: float | None = None, nthreads: int = 1, mtemp: int = -1,
+                model: str = "1chQS", gamma2: float = 0.0):
+    """|Q S> Anderson model (one channel, or "2chQS" with Gamma1 = gamma and
+    Gamma2 = gamma2): forward sweep saving the DM-NRG shells (UpdateBefCut =
+    1, c_d), then the FDM density-matrix backward sweep and the c_d spectral
+    function.  site_dim defaults to 4 (16 for two channels).  Returns
+    (omega, A, rho_trace per shell)."""
     L = lib()
-    cfg = _Cfg(MODEL_1CHQS, nsites, ncutoff, lam, U, ed, gamma, 0.0, 0.0, nthreads, -1, 1)
+    if model not in ("1chQS", "2chQS"):
+        raise ValueError(f"DM-NRG is restated for 1chQS and 2chQS, not {model!r}")
+    two = model == "2chQS"
+    if site_dim is None:
+        site_dim = 16.0 if two else 4.0
+    cfg = _Cfg(MODEL_2CHQS if two else MODEL_1CHQS, nsites, ncutoff, lam, U, ed, gamma, gamma2 if two else 0.0,
+               0.0, nthreads, -1, 1)
     h = L.oracle_run(ctypes.byref(cfg))
     if not h:
         raise RuntimeError("oracle: " + L.oracle_last_error().decode())
@@ -272,12 +281,15 @@ _DM_D = ("basis_qn", "basis_en", "qn", "en", "evec", "cd_el")
 _DM_I = ("basis_bbe", "basis_itype", "basis_stcf", "bbe", "kept", "cd_map", "cd_mbe")
 
 
-def dm_shells(nsites: int, ncutoff: int, lam: float, U: float, ed: float, gamma: float, nthreads: int = 1):
-    """The DM-NRG shells of the one-channel |Q S> Anderson sweep (UpdateBefCut
-    = 1, c_d), one dict of arrays per shell (Abasis_N: basis_*; Acut_N: qn,
-    bbe, en, kept, evec; c_d: cd_*)."""
+def dm_shells(nsites: int, ncutoff: int, lam: float, U: float, ed: float, gamma: float, nthreads: int = 1,
+              model: str = "1chQS", gamma2: float = 0.0):
+    """The DM-NRG shells of the |Q S> Anderson sweep (one channel, or "2chQS"
+    with Gamma2 = gamma2; UpdateBefCut = 1, c_d), one dict of arrays per shell
+    (Abasis_N: basis_*; Acut_N: qn, bbe, en, kept, evec; c_d: cd_*)."""
     L = lib()
-    cfg = _Cfg(MODEL_1CHQS, nsites, ncutoff, lam, U, ed, gamma, 0.0, 0.0, nthreads, -1, 1)
+    two = model == "2chQS"
+    cfg = _Cfg(MODEL_2CHQS if two else MODEL_1CHQS, nsites, ncutoff, lam, U, ed, gamma, gamma2 if two else 0.0,
+               0.0, nthreads, -1, 1)
     h = L.oracle_run(ctypes.byref(cfg))
     if not h:
         raise RuntimeError("oracle: " + L.oracle_last_error().decode())

@@ -55,11 +55,14 @@ def test_dm_against_oracle_on_a_log_grid(engine):
     assert t["lehmann_pairs"] > 0 and t["lehmann_evals"] > 0
 
 
-def test_dm_call_order_and_model_errors(engine):
-    cfg = tg.SweepConfig(tg.MODEL_2CH_QS, 3, 40, 2.5, 0.3, -0.15, 0.01, 0.01, 0.0, 0)
+def test_dm_call_order_and_model_errors(engine, tmp_path):
+    cfg = tg.SweepConfig(tg.MODEL_1CH_QSZ, 3, 40, 2.5, 0.3, -0.15, 0.01, 0.0, 0.0, 0)
     import ctypes
     st = engine.L.nrg_sweep_run_dm(engine.h, ctypes.byref(cfg))
-    assert st == 1  # DM shells exist for the one-channel |Q S> model only
+    assert st == 1  # DM shells exist for the |Q S> models only
+    engine.sweep_dm(3, 40, 2.5, 0.3, -0.15, 0.01, model="2chQS", gamma2=0.01)
+    with pytest.raises(tg.NRGError):  # the reference's DM_NRG reads one-channel shells only
+        engine.dm_save_bin(str(tmp_path), "2chQSAnderson")
     engine.sweep_dm(6, 40, 2.5, 0.5, -0.25, 0.02)
     prm = engine.dm_params(nw=2)
     with pytest.raises(tg.NRGError) as e:  # Lehmann sums before the backward sweep
@@ -110,3 +113,42 @@ def test_dm_shells_saved_in_reference_layout(engine, tmp_path):
             lo, hi = s["cd_mbe"][2 * k], s["cd_mbe"][2 * k + 1] + 1
             a, r = m["MatEl"][lo:hi], s["cd_el"][lo:hi]
             assert abs(np.linalg.norm(a) - np.linalg.norm(r)) < 1e-10 * max(1.0, np.linalg.norm(r))
+
+
+def test_two_channel_all_kept_is_one_channel_with_summed_gamma(engine):
+    """The two-channel impurity couples to the even combination of the two
+    identical chains only.  With every state kept (4 x 16^3 states in the
+    last shell) A(omega) of 2chQS(Gamma1, Gamma2) equals 1chQS(Gamma1 +
+    Gamma2) to round-off: the two-channel c_d rule, the 16-state site algebra
+    and the last shell's Lehmann sum on the GPU against the one-channel path
+    that is pinned to the reference DM_NRG."""
+    om = np.concatenate([-np.logspace(0, -4, 40), np.logspace(-4, 0, 40)])
+    T = 3e-3
+    engine.sweep_dm(3, 100000, 2.5, 0.3, -0.15, 0.01, model="2chQS", gamma2=0.012)
+    prm = engine.dm_params(temp=T, bbroad=0.6)
+    assert prm.site_dim == 16.0
+    tr2 = engine.dm_backprop(prm)
+    _, A2 = engine.lehmann(prm, omegas=om)
+    engine.sweep_dm(3, 100000, 2.5, 0.3, -0.15, 0.022)
+    prm1 = engine.dm_params(temp=T, bbroad=0.6)
+    tr1 = engine.dm_backprop(prm1)
+    _, A1 = engine.lehmann(prm1, omegas=om)
+    assert np.abs(A2 - A1).max() < 1e-10 * np.abs(A1).max()
+    np.testing.assert_allclose(tr2, tr1, rtol=1e-10)
+
+
+def test_two_channel_dm_against_oracle(engine):
+    """Truncated two-channel shells (80 kept multiplets): the backward sweep
+    through the 16-state site and the FDM sum against the oracle's
+    restatement, at a temperature inside the chain."""
+    lam, ns, nc = 2.5, 6, 80
+    temp = 0.7 * lam ** (-(4 - 1) / 2.0) / 0.727
+    om = np.concatenate([-np.logspace(0, -4, 30), np.logspace(-4, 0, 30)])
+    o_om, o_A, o_tr = orc.dm_spectral(ns, nc, lam, 0.3, -0.15, 0.01, temp, 0.6, omegas=om, model="2chQS",
+                                      gamma2=0.012, nthreads=min(8, os.cpu_count() or 1))
+    engine.sweep_dm(ns, nc, lam, 0.3, -0.15, 0.01, model="2chQS", gamma2=0.012)
+    prm = engine.dm_params(temp=temp, bbroad=0.6)
+    tr = engine.dm_backprop(prm)
+    np.testing.assert_allclose(tr, o_tr, rtol=1e-10)
+    _, A = engine.lehmann(prm, omegas=om)
+    _close(A, o_A)

@@ -462,16 +462,26 @@ class Engine:
 
     # ---- DM-NRG spectral function ---------------------------------------
     def sweep_dm(self, nsites: int, ncutoff: int, lam: float, U: float, ed: float, gamma: float,
-                 degen_eps: float = 0.0) -> int:
-        """Forward sweep of the one-channel |Q S> Anderson model keeping the
-        DM-NRG shells on the device; returns the number of shells."""
-        cfg = SweepConfig(MODEL_1CH_QS, nsites, ncutoff, lam, U, ed, gamma, 0.0, degen_eps, PREC_FP64)
+                 degen_eps: float = 0.0, model: str = "1chQS", gamma2: float = 0.0) -> int:
+        """Forward sweep of the |Q S> Anderson model (model "1chQS", or "2chQS"
+        with Gamma1 = gamma and Gamma2 = gamma2) keeping the DM-NRG shells on
+        the device; returns the number of shells."""
+        if model not in ("1chQS", "2chQS"):
+            raise NRGError(f"DM-NRG shells are available for 1chQS and 2chQS, not {model!r}")
+        cfg = SweepConfig(MODELS[model], nsites, ncutoff, lam, U, ed, gamma, gamma2 if model == "2chQS" else 0.0,
+                          degen_eps, PREC_FP64)
         self._check(self.L.nrg_sweep_run_dm(self.h, ctypes.byref(cfg)))
+        self._dm_site_dim = 16.0 if model == "2chQS" else 4.0
         return int(self.L.nrg_dm_num_shells(self.h))
 
-    @staticmethod
-    def dm_params(temp: float = 0.0, mtemp: int = -1, betabar: float = 0.727, bbroad: float = 0.6,
-                  twindow: float = 2.0, broadtemp: float = 0.8, site_dim: float = 4.0, nw: int = 4) -> DmParams:
+    def dm_params(self, temp: float = 0.0, mtemp: int = -1, betabar: float = 0.727, bbroad: float = 0.6,
+                  twindow: float = 2.0, broadtemp: float = 0.8, site_dim: float | None = None,
+                  nw: int = 4) -> DmParams:
+        """DM_NRG's parameters; site_dim (states per Wilson site in the FDM
+        weights) defaults to that of the last sweep_dm: 4, or 16 for two
+        channels."""
+        if site_dim is None:
+            site_dim = getattr(self, "_dm_site_dim", 4.0)
         return DmParams(temp, mtemp, betabar, bbroad, twindow, broadtemp, site_dim, nw)
 
     def dm_backprop(self, prm: DmParams) -> np.ndarray:

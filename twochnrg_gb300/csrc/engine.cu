@@ -101,8 +101,10 @@ struct DmShell {
   int64_t zsize = 0;
   DevBuf Z, cdel;                      // eigenvectors (row = eigenvector) and c_d elements
   DevBuf rho;                          // reduced density matrix, dense blocks laid out like Z
-  DevBuf pairs;                        // Lehmann pairs: dE, W(omega >= 0), W(omega < 0)
-  int64_t npairs = 0;
+  DevBuf rec;                          // Lehmann records: (key, w) of the four lists
+  int64_t nrec[4] = {0, 0, 0, 0};
+  double* rkey[4] = {};
+  double* rw[4] = {};
 };
 
 struct IterResult {
@@ -127,6 +129,7 @@ struct nrg_ctx {
   // device buffers
   nrg::DevBuf meta, vmeta, H, d, e, tau, ev, en, flag, scal, Y, scratch, Z, Zt, T, partial, red, gpart, fde, e2, spl;
   nrg::DevBuf ops_a[6], ops_b[6], opptr;
+  nrg::DevBuf dmcnt, dmpart;            // Lehmann record counts / offsets, and partial sums
   cudaEvent_t ev_a[8];
   // concurrent whole-GPU tridiagonalizations: side streams, fork/join events,
   // per-stream scratch and the block lists
@@ -140,6 +143,7 @@ struct nrg_ctx {
   std::vector<int> out_bbe, out_bbe_bc, out_bbe_eig, out_stcf, out_map, out_mbe;
   // DM-NRG shells of the last nrg_sweep_run_dm, and the density matrices
   double dm_lambda = 0.0;
+  int dm_model = 0;  // ModelKind of the shells
   std::vector<std::unique_ptr<nrg::DmShell>> dm;
   bool dm_rho_valid = false;
   double dm_temp = 0.0;                // temperature the density matrices were built for
@@ -688,7 +692,7 @@ void plan_update(UpdatePlan& U, const ModelSpec& m, const Basis& B, const EigPla
                 GatherTerm G{};
                 G.job = jid; G.dst_base = p.offset + u; G.dst_stride = p.nsite; G.rows = p.count;
                 G.src_base = q.offset + v; G.src_stride = q.nsite; G.srows = q.count;
-                if (m.op_kind[o] == OP_IMPONLY || m.op_kind[o] == OP_CD_QS) {
+                if (m.op_kind[o] == OP_IMPONLY || m.op_kind[o] == OP_CD_QS || m.op_kind[o] == OP_CD_2CH) {
                   double g = 1.0;
                   if (m.op_kind[o] == OP_IMPONLY) {
                     if (tu_ != tv) continue;
@@ -772,8 +776,8 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
   if (cfg->model < 0 || cfg->model > 5) throw NrgError(NRG_ERR_ARG, "unknown model");
   if (chain && (cfg->model == NRG_MODEL_1CH_S || cfg->model == NRG_MODEL_1CH_SZ))
     throw NrgError(NRG_ERR_ARG, "the reference has no free-chain run for the superconducting-lead models");
-  if (dm && cfg->model != NRG_MODEL_1CH_QS)
-    throw NrgError(NRG_ERR_ARG, "DM-NRG shells are available for the one-channel |Q S> model");
+  if (dm && cfg->model != NRG_MODEL_1CH_QS && cfg->model != NRG_MODEL_2CH_QS)
+    throw NrgError(NRG_ERR_ARG, "DM-NRG shells are available for the |Q S> models (one and two channels)");
   if (cfg->nsites < 1 || cfg->ncutoff < 4 || !(cfg->lambda > 1.0)) throw NrgError(NRG_ERR_ARG, "bad sweep parameters");
   if (cfg->precision != NRG_PREC_FP64) throw NrgError(NRG_ERR_ARG, "unsupported precision");
   c->iters.clear();
@@ -788,14 +792,23 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
     const int nf = (S.m.kind == MODEL_1CHQS || S.m.kind == MODEL_1CHS) ? 1 : 2;
     S.m.op_kind.resize(nf); S.m.op_check.resize(nf); S.m.op_name.resize(nf); S.m.op_avg.resize(nf);
   }
-  if (dm) {
+  if (dm && S.m.kind == MODEL_1CHQS) {
     S.m.op_kind = {OP_F_QS, OP_CD_QS};
     S.m.op_check = {CHK_QS_CD, CHK_QS_CD};
     S.m.op_name = {"fN", "cdot1"};
     S.m.op_avg = {0, 0};
+  } else if (dm) {
+    // Two channels: f_N of both channels (they enter H_N) and c_d.
+    S.m.op_kind = {OP_F1_2CH, OP_F2_2CH, OP_CD_2CH};
+    S.m.op_check = {CHK_2CH_CD, CHK_2CH_CD, CHK_2CH_CD};
+    S.m.op_name = {"fNch1", "fNch2", "cdot1"};
+    S.m.op_avg = {0, 0, 0};
+  }
+  if (dm) {
     c->dm.clear();
     c->dm_rho_valid = false;
     c->dm_lambda = cfg->lambda;
+    c->dm_model = S.m.kind;
   }
   const ModelSpec& m = S.m;
   const double eps = cfg->degen_eps > 0 ? cfg->degen_eps : 1.0e-18;
@@ -827,7 +840,9 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
                                                  chain ? 0.0 : cfg->gamma2_or_B);
   if (chain_q) st.ops.resize(nops);
   if (dm) {
-    st.ops = {st.ops[0], st.ops[0]};  // c_d at H_{-1} is a copy of f (Main_SetH0.cpp:1958-1961)
+    // c_d at H_{-1} is a copy of f (Main_SetH0.cpp:1958-1961); f_ch1 = f_ch2 = d.
+    if (m.kind == MODEL_1CHQS) st.ops = {st.ops[0], st.ops[0]};
+    else st.ops = {st.ops[0], st.ops[1], st.ops[0]};
     c->dm_hm1_en = st.en;
   }
   S.kept.blk = st.blk;
@@ -1033,12 +1048,12 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
       sh->kept.resize(P.nstates);
       for (int g = 0; g < P.nstates; ++g) sh->kept[g] = R.en[g] <= R.ecut ? 1 : 0;
       sh->kept_src = K.src;
-      sh->cd = newops[1];
+      sh->cd = newops[nops_h];
       sh->zoff = P.yoff; sh->zsize = P.ysize;
       sh->Z.ensure(sizeof(double) * std::max<int64_t>(P.ysize, 1));
       CU(cudaMemcpyAsync(sh->Z.p, c->Z.p, sizeof(double) * P.ysize, cudaMemcpyDeviceToDevice, c->stream));
-      sh->cdel.ensure(sizeof(double) * std::max<int64_t>(newops[1].size, 1));
-      CU(cudaMemcpyAsync(sh->cdel.p, newptr[1], sizeof(double) * newops[1].size, cudaMemcpyDeviceToDevice,
+      sh->cdel.ensure(sizeof(double) * std::max<int64_t>(newops[nops_h].size, 1));
+      CU(cudaMemcpyAsync(sh->cdel.p, newptr[nops_h], sizeof(double) * newops[nops_h].size, cudaMemcpyDeviceToDevice,
                          c->stream));
       sh->basis = std::move(B);
       c->dm.push_back(std::move(sh));
@@ -1176,7 +1191,7 @@ void dm_backprop_impl(nrg_ctx* c, const nrg_dm_params* prm, double* rho_trace) {
     // Partial trace over the child states (DM_NRG_SetChildSt, SetChildSameType).
     const Basis& B1 = s1.basis;
     const int nbN = (int)sN.bsize.size();
-    const ModelSpec ms = make_model(MODEL_1CHQS);
+    const ModelSpec ms = make_model((ModelKind)c->dm_model);
     std::vector<std::vector<DmTraceTerm>> per(nbN);
     for (int nb1 = 0; nb1 < B1.blk.nblocks(); ++nb1) {
       const double Si = B1.blk.q(nb1, 1);
@@ -1282,30 +1297,24 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
   const int nw_ = (int)om.size();
   Timer tm(c);
   cudaEvent_t t0 = tm.start();
-  // Lehmann pairs of every shell.
-  std::vector<int64_t> shell_off(nsh + 1, 0);
-  for (int N = 0; N < nsh; ++N) {
-    const DmShell& s = *c->dm[N];
-    int64_t np = 0;
-    for (size_t k = 0; k < s.cd.bi.size(); ++k) np += (int64_t)s.bsize[s.cd.bi[k]] * s.bsize[s.cd.bj[k]];
-    shell_off[N + 1] = shell_off[N] + np;
-  }
-  const int64_t ptot = std::max<int64_t>(shell_off[nsh], 1);
-  c->ev.ensure(sizeof(double) * 3 * ptot);  // dE | Wp | Wn for all shells
-  double* dE = c->ev.as<double>();
-  double* Wp = dE + ptot;
-  double* Wn = Wp + ptot;
+  const double sqrt_pi = 1.7724538509055160273;
   const double beta_last = std::fabs(p.temp) < 1.e-20 ? 1.0e10 : p.betabar;
+  int64_t all_pairs = 0;
+  // Every shell's Lehmann records (FDM_SpecDens_M_STL / CalcSpecCosti_T_N
+  // weights, only the pairs whose term can be nonzero).
   for (int N = 0; N < nsh; ++N) {
     DmShell& s = *c->dm[N];
     const bool last = N == Nmax;
     std::vector<DmPair> pairs;
+    std::vector<DmChunk> chunks;
     GemmPlan g;
     int64_t poff = 0;
     std::vector<int> nk(s.bsize.size(), 0), nd(s.bsize.size(), 0);
     for (size_t b = 0; b < s.bsize.size(); ++b)
       for (int i = 0; i < s.bsize[b]; ++i) (s.kept[s.boff[b] + i] ? nk[b] : nd[b])++;
-    const int64_t pbytes = shell_off[N + 1] - shell_off[N];
+    int64_t pbytes = 0;
+    for (size_t k = 0; k < s.cd.bi.size(); ++k) pbytes += (int64_t)s.bsize[s.cd.bi[k]] * s.bsize[s.cd.bj[k]];
+    all_pairs += pbytes;
     c->Y.ensure(sizeof(double) * std::max<int64_t>(2 * pbytes, 1));
     double* P1 = c->Y.as<double>();
     double* P2 = P1 + pbytes;
@@ -1313,7 +1322,7 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
       const int b1 = s.cd.bi[k], b2 = s.cd.bj[k];
       DmPair P{};
       P.n1 = s.bsize[b1]; P.n2 = s.bsize[b2]; P.s1 = s.boff[b1]; P.s2 = s.boff[b2];
-      P.a_off = s.cd.off[k]; P.p_off = poff; P.out_off = shell_off[N] + poff;
+      P.a_off = s.cd.off[k]; P.p_off = poff;
       const double S1 = s.qn[2 * b1 + 1], S2 = s.qn[2 * b2 + 1];
       double cgf = 0.0;
       for (double Sz1 = -S1; Sz1 <= S1; Sz1 += 1.0) {
@@ -1327,17 +1336,26 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
         g.add(GemmJob{P.n1, P.n2, P.n1, 0, s.rho.as<double>() + s.zoff[b1], P.n1, Acd, P.n2, P1 + poff, P.n2});
         g.add(GemmJob{P.n1, P.n2, P.n2, 0, Acd, P.n2, s.rho.as<double>() + s.zoff[b2], P.n2, P2 + poff, P.n2});
       }
+      if ((int64_t)P.n1 * P.n2 > (int64_t)INT32_MAX) throw NrgError(NRG_ERR_SIZE, "c_d block pair too large");
+      if (last || !P.skip)
+        for (int64_t st = 0; st < (int64_t)P.n1 * P.n2; st += kPairChunk)
+          chunks.push_back(DmChunk{(int)pairs.size(), (int)st});
       pairs.push_back(P);
       poff += (int64_t)P.n1 * P.n2;
     }
+    for (int L = 0; L < 4; ++L) s.nrec[L] = 0;
+    if (chunks.empty()) continue;
     run_gemm_plan(c, g);
     Packer pk;
-    size_t o_p = pk.add(pairs), o_en = pk.add(s.en), o_kp = pk.add(s.kept);
+    size_t o_p = pk.add(pairs), o_c = pk.add(chunks), o_en = pk.add(s.en), o_kp = pk.add(s.kept);
     c->meta.ensure(pk.host.size() + 256);
     h2d(c, c->meta.p, pk.host.data(), pk.host.size());
     char* mb = c->meta.as<char>();
-    DmPairArgs a{};
-    a.pairs = (const DmPair*)(mb + o_p); a.cd = s.cdel.as<double>(); a.P1 = P1; a.P2 = P2;
+    const int nch = (int)chunks.size();
+    c->dmcnt.ensure(sizeof(int64_t) * (8 * (size_t)nch + 8));
+    DmRecArgs a{};
+    a.pairs = (const DmPair*)(mb + o_p); a.chunks = (const DmChunk*)(mb + o_c); a.nchunks = nch;
+    a.cd = s.cdel.as<double>(); a.P1 = P1; a.P2 = P2;
     a.en = (const double*)(mb + o_en); a.kept = (const unsigned char*)(mb + o_kp);
     a.last = last ? 1 : 0;
     a.beta_last = beta_last;
@@ -1348,8 +1366,28 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
           z += (2.0 * s.qn[2 * b + 1] + 1.0) * std::exp(-beta_last * s.en[i]);
       a.inv_z_last = 1.0 / z;
     }
-    a.dE = dE; a.Wp = Wp; a.Wn = Wn;
-    launch_dm_pairs(a, (int)pairs.size(), c->stream);
+    a.gauss_below = p.twindow * (p.temp / calc_dn(L, N));
+    a.inv_b = 1.0 / p.bbroad; a.inv_bt = 1.0 / p.broadtemp;
+    a.log_scale = 1.0 / (p.bbroad * sqrt_pi); a.gauss_scale = 1.0 / (p.broadtemp * sqrt_pi);
+    a.offsets = c->dmcnt.as<int64_t>();
+    a.totals = a.offsets + 4 * (size_t)nch;
+    a.counts = (int*)(a.totals + 8);
+    launch_dm_records(a, 0, c->stream);
+    c->launches += 2;
+    int64_t tot[4];
+    d2h(c, tot, a.totals, sizeof(tot));
+    CU(cudaStreamSynchronize(c->stream));
+    int64_t nrec = 0;
+    for (int L = 0; L < 4; ++L) nrec += tot[L];
+    s.rec.ensure(sizeof(double) * std::max<int64_t>(2 * nrec, 1));
+    double* r = s.rec.as<double>();
+    for (int L = 0; L < 4; ++L) {
+      s.nrec[L] = tot[L];
+      s.rkey[L] = a.key[L] = r;
+      s.rw[L] = a.w[L] = r + tot[L];
+      r += 2 * tot[L];
+    }
+    launch_dm_records(a, 1, c->stream);
     c->launches++;
     CU(cudaStreamSynchronize(c->stream));  // meta, vmeta and Y are reused by the next shell
   }
@@ -1365,24 +1403,71 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
     wfirst[k] = N0;
     wcount[k] = std::max(0, N1 - N0);
   }
-  std::vector<double> dn(nsh), tdn(nsh);
-  for (int N = 0; N < nsh; ++N) { dn[N] = calc_dn(L, N); tdn[N] = p.temp / dn[N]; }
+  // The record lists, the frequencies each one is summed against, the work
+  // items (list, record chunk, frequency tile) and the fold tables.
+  std::vector<std::vector<int>> oms(2 * (size_t)nsh);  // [shell][sign]: frequency indices, ascending
+  for (int k = 0; k < nw_; ++k)
+    for (int sl = 0; sl < wcount[k]; ++sl) oms[2 * (size_t)(wfirst[k] + sl) + (om[k] >= 0.0 ? 0 : 1)].push_back(k);
+  std::vector<LehList> lists;
+  std::vector<LehItem> items;
+  std::vector<int> omega_idx;
+  std::vector<int> list_of(4 * (size_t)nsh, -1);  // [shell][list L]
+  int64_t part = 0, evals = 0, nrec_all = 0;
+  for (int N = 0; N < nsh; ++N) {
+    const DmShell& s = *c->dm[N];
+    for (int Lk = 0; Lk < 4; ++Lk) {
+      const std::vector<int>& ks = oms[2 * (size_t)N + (Lk < 2 ? 0 : 1)];
+      nrec_all += s.nrec[Lk];
+      if (s.nrec[Lk] == 0 || ks.empty()) continue;
+      LehList li{};
+      li.key = s.rkey[Lk]; li.w = s.rw[Lk]; li.nrec = s.nrec[Lk]; li.shell = N; li.gauss = Lk & 1;
+      li.nomega = (int)ks.size(); li.omega_first = (int)omega_idx.size(); li.part_off = part;
+      omega_idx.insert(omega_idx.end(), ks.begin(), ks.end());
+      const int64_t nchk = (li.nrec + kRecChunk - 1) / kRecChunk;
+      const int ntile = (li.nomega + kOmegaTile - 1) / kOmegaTile;
+      part += nchk * li.nomega;
+      evals += li.nrec * li.nomega;
+      list_of[4 * (size_t)N + Lk] = (int)lists.size();
+      for (int64_t ch = 0; ch < nchk; ++ch)
+        for (int tl = 0; tl < ntile; ++tl) items.push_back(LehItem{(int)lists.size(), (int)ch, tl});
+      lists.push_back(li);
+    }
+  }
+  std::vector<int> fold_list((size_t)nw_ * window * 2, -1), fold_pos((size_t)nw_ * window * 2, 0);
+  for (int k = 0; k < nw_; ++k)
+    for (int sl = 0; sl < wcount[k]; ++sl) {
+      const int N = wfirst[k] + sl, sg = om[k] >= 0.0 ? 0 : 1;
+      const std::vector<int>& ks = oms[2 * (size_t)N + sg];
+      const int pos = (int)(std::lower_bound(ks.begin(), ks.end(), k) - ks.begin());
+      for (int gsn = 0; gsn < 2; ++gsn) {
+        const size_t fi = ((size_t)k * window + sl) * 2 + gsn;
+        fold_list[fi] = list_of[4 * (size_t)N + 2 * sg + gsn];
+        fold_pos[fi] = pos;
+      }
+    }
+  std::vector<double> dn(nsh), ldn(nsh), lom(nw_);
+  for (int N = 0; N < nsh; ++N) { dn[N] = calc_dn(L, N); ldn[N] = std::log(dn[N]); }
+  for (int k = 0; k < nw_; ++k) lom[k] = std::log(std::fabs(om[k]));
   Packer pk;
-  size_t o_om = pk.add(om), o_wf = pk.add(wfirst), o_wc = pk.add(wcount), o_so = pk.add(shell_off), o_dn = pk.add(dn),
-         o_td = pk.add(tdn);
+  size_t o_li = pk.add(lists), o_it = pk.add(items), o_oi = pk.add(omega_idx), o_om = pk.add(om), o_lo = pk.add(lom),
+         o_dn = pk.add(dn), o_ld = pk.add(ldn), o_wf = pk.add(wfirst), o_wc = pk.add(wcount), o_fl = pk.add(fold_list),
+         o_fp = pk.add(fold_pos);
   c->meta.ensure(pk.host.size() + 256);
   h2d(c, c->meta.p, pk.host.data(), pk.host.size());
   char* mb = c->meta.as<char>();
-  c->partial.ensure(sizeof(double) * std::max<size_t>((size_t)nw_ * window + nw_, 64 * 16));
+  c->dmpart.ensure(sizeof(double) * (size_t)(part + nw_ + 1));
   LehmannArgs la{};
-  la.nomega = nw_; la.omega = (const double*)(mb + o_om); la.win_first = (const int*)(mb + o_wf);
-  la.win_count = (const int*)(mb + o_wc); la.window = window; la.shell_off = (const int64_t*)(mb + o_so);
-  la.dE = dE; la.Wp = Wp; la.Wn = Wn; la.dn = (const double*)(mb + o_dn); la.tempdn = (const double*)(mb + o_td);
-  la.b = p.bbroad; la.twindow = p.twindow; la.broadtemp = p.broadtemp;
-  la.partial = c->partial.as<double>(); la.out = la.partial + (size_t)nw_ * window;
+  la.lists = (const LehList*)(mb + o_li); la.items = (const LehItem*)(mb + o_it); la.nitems = (int)items.size();
+  la.omega_idx = (const int*)(mb + o_oi); la.omega = (const double*)(mb + o_om); la.log_omega = (const double*)(mb + o_lo);
+  la.dn = (const double*)(mb + o_dn); la.log_dn = (const double*)(mb + o_ld);
+  la.inv_b = 1.0 / p.bbroad; la.b_quarter = p.bbroad / 4.0; la.inv_bt = 1.0 / p.broadtemp;
+  la.partial = c->dmpart.as<double>(); la.out = la.partial + part;
+  la.nomega = nw_; la.win_first = (const int*)(mb + o_wf); la.win_count = (const int*)(mb + o_wc); la.window = window;
+  la.fold_list = (const int*)(mb + o_fl); la.fold_pos = (const int*)(mb + o_fp);
+  if (items.size() > (size_t)INT32_MAX) throw NrgError(NRG_ERR_SIZE, "too many Lehmann work items");
   cudaEvent_t t1 = tm.start();
   launch_lehmann(la, c->stream);
-  c->launches += 2;
+  c->launches += la.nitems > 0 ? 2 : 1;
   tm.stop(t1, &c->timing.lehmann_ms);
   std::vector<double> A(nw_);
   d2h(c, A.data(), la.out, sizeof(double) * nw_);
@@ -1390,10 +1475,8 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
   CU(cudaStreamSynchronize(c->stream));
   check_flag(c);
   tm.collect();
-  int64_t evals = 0;
-  for (int k = 0; k < nw_; ++k)
-    for (int s = 0; s < wcount[k]; ++s) evals += shell_off[wfirst[k] + s + 1] - shell_off[wfirst[k] + s];
-  c->timing.lehmann_pairs = shell_off[nsh];
+  (void)all_pairs;
+  c->timing.lehmann_pairs = nrec_all;
   c->timing.lehmann_evals = evals;
   for (int k = 0; k < nw_; ++k) { omega_rhow[k] = om[k]; omega_rhow[nomega + k] = A[k]; }
   *nout = nw_;
@@ -1406,6 +1489,8 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
 void dm_save_bin_impl(nrg_ctx* c, const char* dir, const char* name) {
   if (c->dm.empty()) throw NrgError(NRG_ERR_STATE, "no DM-NRG shells: run nrg_sweep_run_dm first");
   if (!dir || !name) throw NrgError(NRG_ERR_ARG, "directory or name is NULL");
+  if (c->dm_model != MODEL_1CHQS)
+    throw NrgError(NRG_ERR_ARG, "the reference's DM_NRG reads one-channel |Q S> shells only (DM_NRG.cpp:292)");
   for (size_t N = 0; N < c->dm.size(); ++N) {
     const DmShell& s = *c->dm[N];
     const Basis& B = s.basis;

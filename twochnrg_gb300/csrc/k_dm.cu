@@ -8,10 +8,11 @@
 // split (FDM_SpecDens_M_STL, SpecFunc_allSTL.cpp:1253-2358).  Here the
 // rotations and the rho.A / A.rho products are one grouped FP64 GEMM launch
 // per shell, the partial trace is a gather over per-block term lists, and the
-// frequency dependence is isolated: every shell becomes a list of
-// (E_j - E_i, weight) pairs once, and the Lehmann kernel streams those pairs
-// for every frequency, with the log-Gaussian / Gaussian kernels of
-// BroadDelta.cpp evaluated on the fly.
+// frequency dependence is isolated: every shell becomes lists of
+// (E_j - E_i, weight) records once, keeping only the pairs whose term can be
+// nonzero, and the Lehmann kernel stages each chunk of records in shared
+// memory and sums it against a tile of frequencies, with the log-Gaussian /
+// Gaussian kernels of BroadDelta.cpp evaluated on the fly.
 #include "nrg_device.cuh"
 
 namespace nrg {
@@ -97,78 +98,206 @@ __global__ void __launch_bounds__(256) dm_trace_kernel(DmTraceArgs A) {
   }
 }
 
-// One CTA per block pair of c_d: the (E_j - E_i, weight) pairs.
-__global__ void __launch_bounds__(256) dm_pairs_kernel(DmPairArgs A) {
-  const DmPair P = A.pairs[blockIdx.x];
-  const int64_t n = (int64_t)P.n1 * P.n2;
-  for (int64_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
-    const int a = (int)(idx / P.n2), b = (int)(idx - (int64_t)a * P.n2);
-    const double m = A.cd[P.a_off + idx];
-    const double E1 = A.en[P.s1 + a], E2 = A.en[P.s2 + b];
-    double wp = 0.0, wn = 0.0;
-    if (A.last) {
-      const double sum12 = m * exp(-A.beta_last * E1) + exp(-A.beta_last * E2) * m;
-      wp = wn = P.cg * (sum12 * m) * A.inv_z_last;
-    } else if (!P.skip) {
-      const double w = P.cg * ((A.P1[P.p_off + idx] + A.P2[P.p_off + idx]) * m);
-      if (!A.kept[P.s2 + b]) wp = w;
-      if (!A.kept[P.s1 + a]) wn = w;
-    }
-    A.dE[P.out_off + idx] = E2 - E1;
-    A.Wp[P.out_off + idx] = wp;
-    A.Wn[P.out_off + idx] = wn;
+// The weights of pair idx of a c_d block pair: FDM_SpecDens_M_STL's
+// (rho A + A rho) A with the kept / discarded split, or on the last shell
+// CalcSpecCosti_T_N's Boltzmann weights.  Explicitly rounded (no FMA
+// contraction), so that the counting and the scattering pass, which both
+// call it, classify every pair alike.
+__device__ __forceinline__ void pair_value(const DmRecArgs& A, const DmPair& P, int64_t idx, double& dE,
+                                           double& wp, double& wn) {
+  const int a = (int)(idx / P.n2), b = (int)(idx - (int64_t)a * P.n2);
+  const double m = A.cd[P.a_off + idx];
+  const double E1 = A.en[P.s1 + a], E2 = A.en[P.s2 + b];
+  wp = 0.0; wn = 0.0;
+  if (A.last) {
+    const double sum12 = __dadd_rn(__dmul_rn(m, exp(-A.beta_last * E1)), __dmul_rn(exp(-A.beta_last * E2), m));
+    wp = wn = __dmul_rn(__dmul_rn(P.cg, __dmul_rn(sum12, m)), A.inv_z_last);
+  } else if (!P.skip) {
+    const double w = __dmul_rn(P.cg, __dmul_rn(__dadd_rn(A.P1[P.p_off + idx], A.P2[P.p_off + idx]), m));
+    if (!A.kept[P.s2 + b]) wp = w;
+    if (!A.kept[P.s1 + a]) wn = w;
   }
+  dE = E2 - E1;
 }
 
-// LogGaussDelta (BroadDelta.cpp:116-133), replaced by GaussDelta
-// (BroadDelta.cpp:96-106) inside the thermal window, as MijxBDeltaEij does.
-__device__ __forceinline__ double broad_delta(double om, double dE, double b, double tw, double bt, double tempdn) {
-  const double sqrt_pi = 1.7724538509055160273;
-  if (fabs(dE) < tw * tempdn) {
-    const double a1 = (om - dE) / bt;
-    return (1.0 / (bt * sqrt_pi)) * exp(-a1 * a1);
-  }
+// Bit L set: the pair's term is in list L (see DmRecArgs).
+__device__ __forceinline__ unsigned pair_lists(const DmRecArgs& A, double dE, double wp, double wn) {
+  const bool gauss = fabs(dE) < A.gauss_below;
   const double Ep = dE == 0.0 ? 1.0e-100 : dE;
-  if (om * Ep < 0.0) return 0.0;
-  const double a0 = 1.0 / (b * fabs(Ep) * sqrt_pi);
-  const double a1 = log(fabs(om / Ep)) / b;
-  const double x = a1 - b / 4.0;
-  return a0 * exp(-x * x);
+  unsigned f = 0u;
+  if (wp != 0.0) f |= gauss ? 2u : (Ep > 0.0 ? 1u : 0u);
+  if (wn != 0.0) f |= gauss ? 8u : (Ep < 0.0 ? 4u : 0u);
+  return f;
 }
 
-// grid (frequency, shell slot of its window): one shell's pairs per CTA.
+// pass 0: per chunk of kPairChunk pairs, how many go to each list.
+__global__ void __launch_bounds__(256) dm_count_kernel(DmRecArgs A) {
+  __shared__ int cnt[4];
+  const DmChunk C = A.chunks[blockIdx.x];
+  const DmPair P = A.pairs[C.pair];
+  const int64_t n = (int64_t)P.n1 * P.n2;
+  if (threadIdx.x < 4) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  int local[4] = {0, 0, 0, 0};
+  for (int i = threadIdx.x; i < kPairChunk; i += blockDim.x) {
+    const int64_t idx = (int64_t)C.start + i;
+    if (idx >= n) break;
+    double dE, wp, wn;
+    pair_value(A, P, idx, dE, wp, wn);
+    const unsigned f = pair_lists(A, dE, wp, wn);
+    for (int L = 0; L < 4; ++L) local[L] += (f >> L) & 1u;
+  }
+  for (int L = 0; L < 4; ++L) {
+    int v = local[L];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(&cnt[L], v);
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) A.counts[(int64_t)blockIdx.x * 4 + threadIdx.x] = cnt[threadIdx.x];
+}
+
+// Exclusive scan of the chunk counts of every list (one CTA of 1024).
+__global__ void __launch_bounds__(1024) dm_scan_kernel(DmRecArgs A) {
+  __shared__ int64_t part[1024];
+  const int T = blockDim.x, t = threadIdx.x;
+  const int per = (A.nchunks + T - 1) / T;
+  const int c0 = min(t * per, A.nchunks), c1 = min(c0 + per, A.nchunks);
+  for (int L = 0; L < 4; ++L) {
+    int64_t sum = 0;
+    for (int c = c0; c < c1; ++c) sum += A.counts[(int64_t)c * 4 + L];
+    part[t] = sum;
+    __syncthreads();
+    for (int o = 1; o < T; o <<= 1) {  // inclusive Hillis-Steele scan
+      const int64_t v = t >= o ? part[t - o] : 0;
+      __syncthreads();
+      part[t] += v;
+      __syncthreads();
+    }
+    int64_t run = part[t] - sum;
+    for (int c = c0; c < c1; ++c) {
+      A.offsets[(int64_t)c * 4 + L] = run;
+      run += A.counts[(int64_t)c * 4 + L];
+    }
+    if (t == T - 1) A.totals[L] = part[t];
+    __syncthreads();
+  }
+}
+
+// pass 1: the records, in pair order within every list.
+__global__ void __launch_bounds__(256) dm_scatter_kernel(DmRecArgs A) {
+  constexpr int NW = 8;
+  __shared__ int wtot[4][NW];
+  const DmChunk C = A.chunks[blockIdx.x];
+  const DmPair P = A.pairs[C.pair];
+  const int64_t n = (int64_t)P.n1 * P.n2;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int64_t run[4];
+  for (int L = 0; L < 4; ++L) run[L] = A.offsets[(int64_t)blockIdx.x * 4 + L];
+  for (int r = 0; r < kPairChunk; r += 256) {
+    const int64_t idx = (int64_t)C.start + r + threadIdx.x;
+    const bool in = (r + (int)threadIdx.x) < kPairChunk && idx < n;
+    double dE = 0.0, wp = 0.0, wn = 0.0;
+    if (in) pair_value(A, P, idx, dE, wp, wn);
+    const unsigned f = in ? pair_lists(A, dE, wp, wn) : 0u;
+    unsigned mask[4];
+    for (int L = 0; L < 4; ++L) {
+      mask[L] = __ballot_sync(0xffffffffu, (f >> L) & 1u);
+      if (lane == 0) wtot[L][warp] = __popc(mask[L]);
+    }
+    __syncthreads();
+    const unsigned lt = (1u << lane) - 1u;
+    for (int L = 0; L < 4; ++L) {
+      int before = 0, all = 0;
+      for (int w2 = 0; w2 < NW; ++w2) { before += w2 < warp ? wtot[L][w2] : 0; all += wtot[L][w2]; }
+      const int64_t pos = run[L] + before + __popc(mask[L] & lt);
+      if (((f >> L) & 1u) && pos < A.totals[L]) {
+        const double W = L < 2 ? wp : wn;
+        if (L == 0 || L == 2) {
+          const double aE = fabs(dE == 0.0 ? 1.0e-100 : dE);
+          A.key[L][pos] = log(aE) * A.inv_b;
+          A.w[L][pos] = W * A.log_scale / aE;
+        } else {
+          A.key[L][pos] = dE * A.inv_bt;
+          A.w[L][pos] = W * A.gauss_scale;
+        }
+      }
+      run[L] += all;
+    }
+    __syncthreads();
+  }
+}
+
+// One CTA per (list, chunk of kRecChunk records, tile of kOmegaTile
+// frequencies): the records are staged in shared memory once and every
+// warp sums them against 8 frequencies held in registers.
 __global__ void __launch_bounds__(256) lehmann_kernel(LehmannArgs A) {
-  __shared__ double red[8];
-  const int k = blockIdx.x, s = blockIdx.y;
-  double acc = 0.0;
-  int N = -1;
-  if (s < A.win_count[k]) {
-    N = A.win_first[k] + s;
-    const double dn = A.dn[N];
-    const double om = A.omega[k] / dn;
-    const double tempdn = A.tempdn[N];
-    const double* W = om >= 0.0 ? A.Wp : A.Wn;
-    for (int64_t p = A.shell_off[N] + threadIdx.x; p < A.shell_off[N + 1]; p += blockDim.x) {
-      const double w = W[p];
-      if (w != 0.0) acc += w * broad_delta(om, A.dE[p], A.b, A.twindow, A.broadtemp, tempdn);
+  constexpr int kStage = 2048, kPerWarp = 8;
+  __shared__ double sk[kStage], sw[kStage];
+  const LehItem it = A.items[blockIdx.x];
+  const LehList L = A.lists[it.list];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int j0 = it.tile * kOmegaTile + warp * kPerWarp;
+  double t[kPerWarp], acc[kPerWarp];
+  const double ldn = A.log_dn[L.shell], dn = A.dn[L.shell];
+#pragma unroll
+  for (int q = 0; q < kPerWarp; ++q) {
+    acc[q] = 0.0;
+    t[q] = 0.0;
+    const int j = j0 + q;
+    if (j < L.nomega) {
+      const int k = A.omega_idx[L.omega_first + j];
+      t[q] = L.gauss ? (A.omega[k] / dn) * A.inv_bt : (A.log_omega[k] - ldn) * A.inv_b - A.b_quarter;
     }
   }
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
-    A.partial[(int64_t)k * A.window + s] = N >= 0 ? t / A.dn[N] : 0.0;
+  const bool active = j0 < L.nomega;
+  const int64_t r0 = (int64_t)it.chunk * kRecChunk;
+  const int64_t r1 = min(r0 + (int64_t)kRecChunk, L.nrec);
+  for (int64_t base = r0; base < r1; base += kStage) {
+    const int n = (int)min((int64_t)kStage, r1 - base);
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) { sk[i] = L.key[base + i]; sw[i] = L.w[base + i]; }
+    __syncthreads();
+    if (!active) continue;
+    for (int i = lane; i < n; i += 32) {
+      const double kk = sk[i], ww = sw[i];
+#pragma unroll
+      for (int q = 0; q < kPerWarp; ++q) {
+        const double x = t[q] - kk;
+        acc[q] += ww * exp(-x * x);
+      }
+    }
+  }
+  if (!active) return;
+#pragma unroll
+  for (int q = 0; q < kPerWarp; ++q) {
+    double v = acc[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int j = j0 + q;
+    if (lane == 0 && j < L.nomega) A.partial[L.part_off + (int64_t)it.chunk * L.nomega + j] = v;
   }
 }
 
+// A(omega_k): the shells of its window in order, each shell's chunks in
+// order, divided by D_N (CalcSpecDM_NRG, SpecFuncClass.cpp:1827-1883).
 __global__ void lehmann_fold_kernel(LehmannArgs A) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= A.nomega) return;
-  double t = 0.0;
-  for (int s = 0; s < A.window; ++s) t += A.partial[(int64_t)k * A.window + s];
-  A.out[k] = t;
+  double tot = 0.0;
+  for (int s = 0; s < A.win_count[k]; ++s) {
+    const int N = A.win_first[k] + s;
+    double sh = 0.0;
+    for (int g = 0; g < 2; ++g) {
+      const int64_t fi = ((int64_t)k * A.window + s) * 2 + g;
+      const int li = A.fold_list[fi];
+      if (li < 0) continue;
+      const LehList L = A.lists[li];
+      const int pos = A.fold_pos[fi];
+      const int64_t nch = (L.nrec + kRecChunk - 1) / kRecChunk;
+      for (int64_t c = 0; c < nch; ++c) sh += A.partial[L.part_off + c * L.nomega + pos];
+    }
+    tot += sh / A.dn[N];
+  }
+  A.out[k] = tot;
 }
 
 }  // namespace
@@ -181,13 +310,19 @@ void launch_dm_trace(const DmTraceArgs& a, int nblocks, cudaStream_t s) {
   if (nblocks > 0) dm_trace_kernel<<<nblocks, 256, 0, s>>>(a);
 }
 
-void launch_dm_pairs(const DmPairArgs& a, int npairs_blocks, cudaStream_t s) {
-  if (npairs_blocks > 0) dm_pairs_kernel<<<npairs_blocks, 256, 0, s>>>(a);
+void launch_dm_records(const DmRecArgs& a, int pass, cudaStream_t s) {
+  if (a.nchunks <= 0) return;
+  if (pass == 0) {
+    dm_count_kernel<<<a.nchunks, 256, 0, s>>>(a);
+    dm_scan_kernel<<<1, 1024, 0, s>>>(a);
+  } else {
+    dm_scatter_kernel<<<a.nchunks, 256, 0, s>>>(a);
+  }
 }
 
 void launch_lehmann(const LehmannArgs& a, cudaStream_t s) {
   if (a.nomega <= 0) return;
-  lehmann_kernel<<<dim3(a.nomega, a.window), 256, 0, s>>>(a);
+  if (a.nitems > 0) lehmann_kernel<<<a.nitems, 256, 0, s>>>(a);
   lehmann_fold_kernel<<<(a.nomega + 127) / 128, 128, 0, s>>>(a);
 }
 

@@ -281,12 +281,25 @@ struct DmPair {           // one block pair (b1, b2) of c_d
   int s1, s2;             // first states of the blocks
   int64_t a_off;          // c_d block (n1 x n2) in cd
   int64_t p_off;          // rho1 . A and A . rho2 (each n1 x n2) in scratch
-  int64_t out_off;        // first Lehmann pair of this block pair
   double cg;              // sum_Sz CG^2 of the spectral sum
   int skip;               // both blocks without kept or without discarded states
 };
-struct DmPairArgs {
+// The Lehmann pairs of one shell as records of the broadened-delta sum.
+// A pair (i, j) of a c_d block pair has dE = E_j - E_i and the FDM weights
+// W+ (omega >= 0) and W- (omega < 0).  Only pairs whose term can be nonzero
+// are kept, in four lists: 0 (omega >= 0, log-Gaussian: W+ != 0, dE > 0),
+// 1 (omega >= 0, Gaussian: W+ != 0, |dE| < twindow T/D_N), 2 and 3 the same
+// for omega < 0 with W- and dE < 0.  Every list holds (key, w) with the
+// term w exp(-(t - key)^2): log-Gaussian key = ln|dE| / b, w = W / (b |dE|
+// sqrt(pi)), t = ln|omega/D_N| / b - b/4; Gaussian key = dE / bt, w = W /
+// (bt sqrt(pi)), t = (omega/D_N) / bt (LogGaussDelta / GaussDelta,
+// BroadDelta.cpp:96-133).  The dropped pairs contribute exactly 0.
+constexpr int kPairChunk = 1024;  // pairs per CTA of the record passes
+struct DmChunk { int pair, start; };
+struct DmRecArgs {
   const DmPair* pairs;
+  const DmChunk* chunks;
+  int nchunks;
   const double* cd;
   const double* P1;
   const double* P2;
@@ -294,27 +307,47 @@ struct DmPairArgs {
   const unsigned char* kept;
   int last;               // last shell: CalcSpecCosti_T_N weights
   double beta_last, inv_z_last;
-  double* dE;             // E(b2) - E(b1)
-  double* Wp;             // weight for omega >= 0
-  double* Wn;             // weight for omega < 0
+  double gauss_below;     // twindow * T / D_N
+  double inv_b, inv_bt, log_scale, gauss_scale;  // 1/b, 1/bt, 1/(b sqrt pi), 1/(bt sqrt pi)
+  int* counts;            // [nchunks][4]
+  int64_t* offsets;       // [nchunks][4], exclusive per list
+  int64_t* totals;        // [4]
+  double* key[4];
+  double* w[4];
 };
-void launch_dm_pairs(const DmPairArgs& a, int npairs_blocks, cudaStream_t s);
+void launch_dm_records(const DmRecArgs& a, int pass, cudaStream_t s);  // pass 0 count + scan, 1 scatter
 
-struct LehmannArgs {      // A(omega) = sum_N sum_p W_p BD(omega/D_N, dE_p) / D_N
-  int nomega;
+// One (shell, sign, branch) list of records and the frequencies whose
+// window holds the shell.
+constexpr int kRecChunk = 8192;   // records per CTA of the Lehmann kernel
+constexpr int kOmegaTile = 64;    // frequencies per CTA
+struct LehList {
+  const double* key;
+  const double* w;
+  int64_t nrec;
+  int shell, gauss;
+  int nomega, omega_first;  // frequencies: omega_idx[omega_first .. +nomega)
+  int64_t part_off;         // partial sums [chunk][nomega]
+};
+struct LehItem { int list, chunk, tile; };
+struct LehmannArgs {      // A(omega) = sum_N sum_records w exp(-(t - key)^2) / D_N
+  const LehList* lists;
+  const LehItem* items;
+  int nitems;
+  const int* omega_idx;
   const double* omega;
-  const int* win_first;   // first shell of each frequency's window
-  const int* win_count;   // shells in the window (<= window)
+  const double* log_omega;  // ln|omega|
+  const double* dn;         // D_N
+  const double* log_dn;     // ln D_N
+  double inv_b, b_quarter, inv_bt;
+  double* partial;
+  int nomega;
+  const int* win_first;     // first shell of each frequency's window
+  const int* win_count;     // shells in the window (<= window)
   int window;
-  const int64_t* shell_off;  // Lehmann pairs of shell N: [shell_off[N], shell_off[N+1])
-  const double* dE;
-  const double* Wp;
-  const double* Wn;
-  const double* dn;       // D_N
-  const double* tempdn;   // T / D_N
-  double b, twindow, broadtemp;
-  double* partial;        // [nomega * window], divided by D_N
-  double* out;            // [nomega]
+  const int* fold_list;     // [nomega][window][2]: list of (shell, branch) or -1
+  const int* fold_pos;      // the frequency's position in that list
+  double* out;              // [nomega]
 };
 void launch_lehmann(const LehmannArgs& a, cudaStream_t s);
 

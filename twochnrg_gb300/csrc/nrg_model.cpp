@@ -626,6 +626,39 @@ double op_site_factor(const ModelSpec& m, int op, double Si, double Sj, int ti, 
     }
     return f / norm;
   }
+  if (op == OP_CD_2CH) {
+    // The impurity d operator across the 16-state two-channel site.  The
+    // reference has no such rule (TwoChQS keeps no c_d); this is
+    // OneChQS_cd_MatEl's recoupling with the site multiplet left unchanged:
+    // t_i and t_j are members of one multiplet (TwoChQS_SpSm_table), the
+    // site member is the same on both sides, and the Fermi sign is (-1) to
+    // the site's fermion number Q + 2, as Q = 0 (one fermion) is for the
+    // one-channel site.
+    const TwoChTables& T = twoch();
+    if (T.spsm[ti][tj] == 0.0) return 0.0;
+    const int bi = m.site.block_of_state(ti), bj = m.site.block_of_state(tj);
+    const double Qt = ss.q(bi, 0), St = ss.q(bi, 1);
+    const double Scfi = Si - ss.q(bi, 2), Scfj = Sj - ss.q(bj, 2);
+    const double fermi = std::fabs(std::fmod(Qt, 2.0)) == 1.0 ? -1.0 : 1.0;
+    double sigma = Sj - Si;
+    double norm = cg(Si, Si, 0.5, sigma, Sj, Sj);
+    if (deq(norm, 0.0)) {
+      sigma = Si - Sj;
+      norm = cg(Si, Si, 0.5, sigma, Sj, Sj);
+      if (deq(norm, 0.0)) return 0.0;
+    }
+    double f = 0.0;
+    for (double Szcfj = -Scfj; Szcfj <= Scfj; Szcfj += 1.0) {
+      const double Szcfi = Szcfj - sigma;
+      const double Sztj = Sj - Szcfj, Szti = Si - Szcfi;
+      if (!deq(Szti, Sztj) || std::fabs(Sztj) > St + 1.0e-12) continue;
+      const double a0 = cg(Scfi, Szcfi, St, Szti, Si, Si);
+      const double a1 = cg(Scfj, Szcfj, St, Sztj, Sj, Sj);
+      const double a2 = cg(Scfi, Szcfi, 0.5, sigma, Scfj, Szcfj);
+      f += a0 * a1 * a2 * fermi;
+    }
+    return f / norm;
+  }
   if (op == OP_F_QS) {
     // OneChQS_fN_MatEl (OpMatRules.cpp:1167-1244).
     double qi[3] = {ss.q(ti, 0), ss.q(ti, 1), ss.q(ti, 2)}, qj[3] = {ss.q(tj, 0), ss.q(tj, 1), ss.q(tj, 2)};

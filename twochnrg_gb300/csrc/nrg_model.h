@@ -37,6 +37,7 @@ enum OpKind {
   OP_F_S = 8,       // OneChS_fN_MatEl       (OpMatRules.cpp:1555)
   OP_FUP_SZ = 9,    // OneChSz_fNup_MatEl    (OpMatRules.cpp:2016)
   OP_FDN_SZ = 10,   // OneChSz_fNdn_MatEl    (OpMatRules.cpp:2027)
+  OP_CD_2CH = 11,   // c_d across the two-channel site x old (OneChQS_cd_MatEl's recoupling)
 };
 // CheckForMatEl rule ids.
 enum CheckKind { CHK_DIAG = 1, CHK_QS_CD = 2, CHK_Q_CD = 3, CHK_2CH_CD = 4, CHK_S_CD = 5, CHK_SZ_UP = 6,
@@ -132,7 +133,7 @@ void build_hn_tables(const ModelSpec& m, const Basis& b, HNTables& t);
 
 // Site factor of an operator between two new-basis states, g(S_i, S_j, t_i,
 // t_j): for f-type operators the states came from the same old state; for
-// impurity operators (OP_IMPONLY, OP_CD_QS) g multiplies the old operator
+// impurity operators (OP_IMPONLY, OP_CD_QS, OP_CD_2CH) g multiplies the old operator
 // element between the states they came from.
 double op_site_factor(const ModelSpec& m, int op, double Si, double Sj, int ti, int tj);
 
