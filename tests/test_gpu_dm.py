@@ -152,3 +152,19 @@ def test_two_channel_dm_against_oracle(engine):
     np.testing.assert_allclose(tr, o_tr, rtol=1e-10)
     _, A = engine.lehmann(prm, omegas=om)
     _close(A, o_A)
+
+
+def test_dm_on_an_uneven_grid(engine):
+    """Frequencies not evenly spaced in ln|omega|: every tile takes the
+    direct exponentials instead of the recurrence along the tile."""
+    lam, ns = 2.5, 10
+    temp = 0.7 * lam ** (-(6 - 1) / 2.0) / 0.727
+    rng = np.random.default_rng(7)
+    x = np.sort(10.0 ** rng.uniform(-5, 0, 70))
+    om = np.concatenate([-x[::-1], x])
+    _, o_A, _ = orc.dm_spectral(ns, 60, lam, 0.4, -0.2, 0.015, temp, 0.6, omegas=om)
+    engine.sweep_dm(ns, 60, lam, 0.4, -0.2, 0.015)
+    prm = engine.dm_params(temp=temp, bbroad=0.6)
+    engine.dm_backprop(prm)
+    _, A = engine.lehmann(prm, omegas=om)
+    _close(A, o_A)

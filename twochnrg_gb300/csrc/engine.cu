@@ -101,10 +101,8 @@ struct DmShell {
   int64_t zsize = 0;
   DevBuf Z, cdel;                      // eigenvectors (row = eigenvector) and c_d elements
   DevBuf rho;                          // reduced density matrix, dense blocks laid out like Z
-  DevBuf rec;                          // Lehmann records: (key, w) of the four lists
+  DevBuf lpart;                        // Lehmann partial sums of this shell's record lists
   int64_t nrec[4] = {0, 0, 0, 0};
-  double* rkey[4] = {};
-  double* rw[4] = {};
 };
 
 struct IterResult {
@@ -129,7 +127,7 @@ struct nrg_ctx {
   // device buffers
   nrg::DevBuf meta, vmeta, H, d, e, tau, ev, en, flag, scal, Y, scratch, Z, Zt, T, partial, red, gpart, fde, e2, spl;
   nrg::DevBuf ops_a[6], ops_b[6], opptr;
-  nrg::DevBuf dmcnt, dmpart;            // Lehmann record counts / offsets, and partial sums
+  nrg::DevBuf dmcnt, dmrec, dmtab;     // Lehmann record counts / offsets, records, frequency tables
   cudaEvent_t ev_a[8];
   // concurrent whole-GPU tridiagonalizations: side streams, fork/join events,
   // per-stream scratch and the block lists
@@ -657,9 +655,13 @@ struct UpdatePlan {
 // (kept x n, row-major) and c->Zt (n x kept).  opblock maps a block of the
 // previous kept array (a segment's old_block) to the block the old operators
 // are stored by (NULL: the same block).
+//
+// kept_rows (DM-NRG shells, K = every state): per block of B its kept
+// states.  Operators other than c_d are then computed on the kept states only
+// (the next iteration reads nothing else), in the full layout.
 void plan_update(UpdatePlan& U, const ModelSpec& m, const Basis& B, const EigPlan& P, const Kept& K,
                  const std::vector<OpMeta>& oldops, const std::vector<int>* opblock = nullptr,
-                 const std::vector<int>* opsize = nullptr) {
+                 const std::vector<int>* opsize = nullptr, const std::vector<int>* kept_rows = nullptr) {
   auto ob = [&](int k) { return opblock ? (*opblock)[k] : k; };
   const int nops = (int)m.op_kind.size();
   U.newops.assign(nops, OpMeta());
@@ -670,11 +672,14 @@ void plan_update(UpdatePlan& U, const ModelSpec& m, const Basis& B, const EigPla
       for (int j = 0; j < nk; ++j) {
         if (!op_check(m.op_check[o], K.blk, i, j)) continue;
         const int bI = K.src[i], bJ = K.src[j];
+        const bool kept_only = kept_rows && m.op_kind[o] != OP_CD_QS && m.op_kind[o] != OP_CD_2CH;
         RotJob J{};
         J.ki = K.blk.size[i]; J.kj = K.blk.size[j]; J.nI = P.bsize[bI];
+        J.ldz = J.kj; J.ldo = J.kj;
         J.z_off = P.yoff[bI]; J.zt_off = P.yoff[bJ]; J.t_off = U.tsize; J.o_off = no.size; J.op = o;
         no.bi.push_back(i); no.bj.push_back(j); no.off.push_back(no.size);
         no.size += (int64_t)J.ki * J.kj;
+        if (kept_only) { J.ki = (*kept_rows)[bI]; J.kj = (*kept_rows)[bJ]; }
         U.tsize += (int64_t)J.nI * J.kj;
         const int jid = (int)U.jobs.size();
         U.jobs.push_back(J);
@@ -991,7 +996,8 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
       Kfull.blk = B.blk;
       for (int b = 0; b < nb; ++b) Kfull.src.push_back(b);
     }
-    plan_update(U, m, B, P, dm ? Kfull : K, S.ops, opblock.empty() ? nullptr : &opblock, &opsize);
+    plan_update(U, m, B, P, dm ? Kfull : K, S.ops, opblock.empty() ? nullptr : &opblock, &opsize,
+                dm ? &keptb : nullptr);
     std::vector<OpMeta>& newops = U.newops;
     const int nk = K.blk.nblocks();
     int nxt = 1 - S.cur;
@@ -1001,6 +1007,8 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
       b->ensure(sizeof(double) * std::max<int64_t>(newops[o].size, 1));
       newptr[o] = b->as<double>();
       oldptr[o] = S.opbuf(S.cur, o)->as<double>();
+      if (dm && m.op_kind[o] != OP_CD_QS && m.op_kind[o] != OP_CD_2CH)  // only the kept part is computed
+        CU(cudaMemsetAsync(newptr[o], 0, sizeof(double) * newops[o].size, c->stream));
     }
     Packer& up = U.up;
     U.o_old = up.add(oldptr); U.o_new = up.add(newptr);
@@ -1299,12 +1307,47 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
   cudaEvent_t t0 = tm.start();
   const double sqrt_pi = 1.7724538509055160273;
   const double beta_last = std::fabs(p.temp) < 1.e-20 ? 1.0e10 : p.betabar;
-  int64_t all_pairs = 0;
-  // Every shell's Lehmann records (FDM_SpecDens_M_STL / CalcSpecCosti_T_N
-  // weights, only the pairs whose term can be nonzero).
+  // Windows of shells per frequency (CalcNfromOmega, SpecFuncClass.cpp:41-49)
+  // and, per shell and sign, the frequencies whose window holds the shell.
+  const int window = 22;
+  std::vector<int> wfirst(nw_), wcount(nw_);
+  for (int k = 0; k < nw_; ++k) {
+    int iaux = (int)(2.0 * std::log(2.0 * std::fabs(om[k]) / hlf) / std::log(L));
+    iaux = 1 - iaux;
+    if (iaux < 0) iaux = 0;
+    const int N0 = iaux - 8 > 0 ? iaux - 8 : 0;
+    const int N1 = iaux + 14 < nsh ? iaux + 14 : nsh;
+    wfirst[k] = N0;
+    wcount[k] = std::max(0, N1 - N0);
+  }
+  std::vector<std::vector<int>> oms(2 * (size_t)nsh);  // [shell][sign]: frequency indices, ascending
+  for (int k = 0; k < nw_; ++k)
+    for (int sl = 0; sl < wcount[k]; ++sl) oms[2 * (size_t)(wfirst[k] + sl) + (om[k] >= 0.0 ? 0 : 1)].push_back(k);
+  std::vector<double> dn(nsh), ldn(nsh), lom(nw_);
+  for (int N = 0; N < nsh; ++N) { dn[N] = calc_dn(L, N); ldn[N] = std::log(dn[N]); }
+  for (int k = 0; k < nw_; ++k) lom[k] = std::log(std::fabs(om[k]));
+  Packer tab;
+  const size_t o_om = tab.add(om), o_lo = tab.add(lom), o_dn = tab.add(dn), o_ld = tab.add(ldn), o_wf = tab.add(wfirst),
+               o_wc = tab.add(wcount);
+  c->dmtab.ensure(tab.host.size() + 256);
+  h2d(c, c->dmtab.p, tab.host.data(), tab.host.size());
+  char* tb = c->dmtab.as<char>();
+  LehmannArgs la{};
+  la.omega = (const double*)(tb + o_om); la.log_omega = (const double*)(tb + o_lo);
+  la.dn = (const double*)(tb + o_dn); la.log_dn = (const double*)(tb + o_ld);
+  la.inv_b = 1.0 / p.bbroad; la.b_quarter = p.bbroad / 4.0; la.inv_bt = 1.0 / p.broadtemp;
+  la.nomega = nw_; la.win_first = (const int*)(tb + o_wf); la.win_count = (const int*)(tb + o_wc); la.window = window;
+  // Shell by shell: the Lehmann records (FDM_SpecDens_M_STL / CalcSpecCosti_T_N
+  // weights; only the pairs whose term can be nonzero), then their sums
+  // against every frequency whose window holds the shell, one partial sum
+  // per record chunk and frequency.  Only one shell's records exist at a time.
+  std::vector<LehList> lists;                      // every shell's lists (for the fold)
+  std::vector<int> list_of(4 * (size_t)nsh, -1);  // [shell][list L]
+  int64_t evals = 0, nrec_all = 0;
   for (int N = 0; N < nsh; ++N) {
     DmShell& s = *c->dm[N];
     const bool last = N == Nmax;
+    for (int Lk = 0; Lk < 4; ++Lk) s.nrec[Lk] = 0;
     std::vector<DmPair> pairs;
     std::vector<DmChunk> chunks;
     GemmPlan g;
@@ -1314,7 +1357,6 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
       for (int i = 0; i < s.bsize[b]; ++i) (s.kept[s.boff[b] + i] ? nk[b] : nd[b])++;
     int64_t pbytes = 0;
     for (size_t k = 0; k < s.cd.bi.size(); ++k) pbytes += (int64_t)s.bsize[s.cd.bi[k]] * s.bsize[s.cd.bj[k]];
-    all_pairs += pbytes;
     c->Y.ensure(sizeof(double) * std::max<int64_t>(2 * pbytes, 1));
     double* P1 = c->Y.as<double>();
     double* P2 = P1 + pbytes;
@@ -1343,7 +1385,6 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
       pairs.push_back(P);
       poff += (int64_t)P.n1 * P.n2;
     }
-    for (int L = 0; L < 4; ++L) s.nrec[L] = 0;
     if (chunks.empty()) continue;
     run_gemm_plan(c, g);
     Packer pk;
@@ -1366,7 +1407,7 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
           z += (2.0 * s.qn[2 * b + 1] + 1.0) * std::exp(-beta_last * s.en[i]);
       a.inv_z_last = 1.0 / z;
     }
-    a.gauss_below = p.twindow * (p.temp / calc_dn(L, N));
+    a.gauss_below = p.twindow * (p.temp / dn[N]);
     a.inv_b = 1.0 / p.bbroad; a.inv_bt = 1.0 / p.broadtemp;
     a.log_scale = 1.0 / (p.bbroad * sqrt_pi); a.gauss_scale = 1.0 / (p.broadtemp * sqrt_pi);
     a.offsets = c->dmcnt.as<int64_t>();
@@ -1378,104 +1419,110 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
     d2h(c, tot, a.totals, sizeof(tot));
     CU(cudaStreamSynchronize(c->stream));
     int64_t nrec = 0;
-    for (int L = 0; L < 4; ++L) nrec += tot[L];
-    s.rec.ensure(sizeof(double) * std::max<int64_t>(2 * nrec, 1));
-    double* r = s.rec.as<double>();
-    for (int L = 0; L < 4; ++L) {
-      s.nrec[L] = tot[L];
-      s.rkey[L] = a.key[L] = r;
-      s.rw[L] = a.w[L] = r + tot[L];
-      r += 2 * tot[L];
+    for (int Lk = 0; Lk < 4; ++Lk) nrec += tot[Lk];
+    c->dmrec.ensure(sizeof(double) * std::max<int64_t>(2 * nrec, 1));
+    double* r = c->dmrec.as<double>();
+    for (int Lk = 0; Lk < 4; ++Lk) {
+      s.nrec[Lk] = tot[Lk];
+      a.key[Lk] = r;
+      a.w[Lk] = r + tot[Lk];
+      r += 2 * tot[Lk];
     }
     launch_dm_records(a, 1, c->stream);
     c->launches++;
-    CU(cudaStreamSynchronize(c->stream));  // meta, vmeta and Y are reused by the next shell
-  }
-  // Windows of shells per frequency (CalcNfromOmega, SpecFuncClass.cpp:41-49).
-  const int window = 22;
-  std::vector<int> wfirst(nw_), wcount(nw_);
-  for (int k = 0; k < nw_; ++k) {
-    int iaux = (int)(2.0 * std::log(2.0 * std::fabs(om[k]) / hlf) / std::log(L));
-    iaux = 1 - iaux;
-    if (iaux < 0) iaux = 0;
-    const int N0 = iaux - 8 > 0 ? iaux - 8 : 0;
-    const int N1 = iaux + 14 < nsh ? iaux + 14 : nsh;
-    wfirst[k] = N0;
-    wcount[k] = std::max(0, N1 - N0);
-  }
-  // The record lists, the frequencies each one is summed against, the work
-  // items (list, record chunk, frequency tile) and the fold tables.
-  std::vector<std::vector<int>> oms(2 * (size_t)nsh);  // [shell][sign]: frequency indices, ascending
-  for (int k = 0; k < nw_; ++k)
-    for (int sl = 0; sl < wcount[k]; ++sl) oms[2 * (size_t)(wfirst[k] + sl) + (om[k] >= 0.0 ? 0 : 1)].push_back(k);
-  std::vector<LehList> lists;
-  std::vector<LehItem> items;
-  std::vector<int> omega_idx;
-  std::vector<int> list_of(4 * (size_t)nsh, -1);  // [shell][list L]
-  int64_t part = 0, evals = 0, nrec_all = 0;
-  for (int N = 0; N < nsh; ++N) {
-    const DmShell& s = *c->dm[N];
+    // This shell's lists, their frequencies and work items.
+    std::vector<LehList> sl;
+    std::vector<int> sl_kind;
+    std::vector<int64_t> sl_off;
+    std::vector<LehItem> items;
+    std::vector<int> omega_idx;
+    int64_t part = 0;
     for (int Lk = 0; Lk < 4; ++Lk) {
       const std::vector<int>& ks = oms[2 * (size_t)N + (Lk < 2 ? 0 : 1)];
       nrec_all += s.nrec[Lk];
       if (s.nrec[Lk] == 0 || ks.empty()) continue;
       LehList li{};
-      li.key = s.rkey[Lk]; li.w = s.rw[Lk]; li.nrec = s.nrec[Lk]; li.shell = N; li.gauss = Lk & 1;
-      li.nomega = (int)ks.size(); li.omega_first = (int)omega_idx.size(); li.part_off = part;
+      li.key = a.key[Lk]; li.w = a.w[Lk]; li.nrec = s.nrec[Lk]; li.shell = N; li.gauss = Lk & 1;
+      li.nomega = (int)ks.size(); li.omega_first = (int)omega_idx.size();
       omega_idx.insert(omega_idx.end(), ks.begin(), ks.end());
       const int64_t nchk = (li.nrec + kRecChunk - 1) / kRecChunk;
       const int ntile = (li.nomega + kOmegaTile - 1) / kOmegaTile;
       part += nchk * li.nomega;
       evals += li.nrec * li.nomega;
-      list_of[4 * (size_t)N + Lk] = (int)lists.size();
+      // Tiles of a log-Gaussian list whose frequencies are evenly spaced in
+      // ln|omega| (to 1e-12 of the step; the step at most 0.5 b) take the
+      // recurrence.
+      std::vector<double> tile_delta(ntile, 0.0);
+      if (!li.gauss)
+        for (int tl = 0; tl < ntile; ++tl) {
+          const int j0 = tl * kOmegaTile, j1 = std::min(li.nomega, j0 + kOmegaTile);
+          if (j1 - j0 < 2) continue;
+          const double d = (lom[ks[j1 - 1]] - lom[ks[j0]]) / (j1 - 1 - j0);
+          bool even = std::isfinite(d) && d != 0.0 && std::fabs(d) <= 0.5 * p.bbroad;
+          for (int j = j0; even && j + 1 < j1; ++j)
+            even = std::fabs((lom[ks[j + 1]] - lom[ks[j]]) - d) <= 1e-12 * std::fabs(d);
+          if (even) tile_delta[tl] = d / p.bbroad;
+        }
       for (int64_t ch = 0; ch < nchk; ++ch)
-        for (int tl = 0; tl < ntile; ++tl) items.push_back(LehItem{(int)lists.size(), (int)ch, tl});
-      lists.push_back(li);
+        for (int tl = 0; tl < ntile; ++tl) items.push_back(LehItem{(int)sl.size(), (int)ch, tl, tile_delta[tl]});
+      sl.push_back(li);
+      sl_kind.push_back(Lk);
+      sl_off.push_back(part - nchk * li.nomega);
     }
+    if (items.size() > (size_t)INT32_MAX) throw NrgError(NRG_ERR_SIZE, "too many Lehmann work items");
+    s.lpart.ensure(sizeof(double) * std::max<int64_t>(part, 1));
+    for (size_t q = 0; q < sl.size(); ++q) {
+      sl[q].part = s.lpart.as<double>() + sl_off[q];
+      list_of[4 * (size_t)N + sl_kind[q]] = (int)lists.size();
+      lists.push_back(sl[q]);
+    }
+    if (!items.empty()) {
+      Packer pl;
+      const size_t o_li = pl.add(sl), o_it = pl.add(items), o_oi = pl.add(omega_idx);
+      c->vmeta.ensure(pl.host.size() + 256);
+      h2d(c, c->vmeta.p, pl.host.data(), pl.host.size());
+      char* vb = c->vmeta.as<char>();
+      la.lists = (const LehList*)(vb + o_li); la.items = (const LehItem*)(vb + o_it); la.nitems = (int)items.size();
+      la.omega_idx = (const int*)(vb + o_oi);
+      cudaEvent_t t1 = tm.start();
+      launch_lehmann(la, c->stream);
+      c->launches++;
+      tm.stop(t1, &c->timing.lehmann_ms);
+    }
+    CU(cudaStreamSynchronize(c->stream));  // meta, vmeta, dmrec and Y are reused by the next shell
   }
+  // A(omega): every frequency's window shells in order.
   std::vector<int> fold_list((size_t)nw_ * window * 2, -1), fold_pos((size_t)nw_ * window * 2, 0);
   for (int k = 0; k < nw_; ++k)
-    for (int sl = 0; sl < wcount[k]; ++sl) {
-      const int N = wfirst[k] + sl, sg = om[k] >= 0.0 ? 0 : 1;
+    for (int sl2 = 0; sl2 < wcount[k]; ++sl2) {
+      const int N = wfirst[k] + sl2, sg = om[k] >= 0.0 ? 0 : 1;
       const std::vector<int>& ks = oms[2 * (size_t)N + sg];
       const int pos = (int)(std::lower_bound(ks.begin(), ks.end(), k) - ks.begin());
       for (int gsn = 0; gsn < 2; ++gsn) {
-        const size_t fi = ((size_t)k * window + sl) * 2 + gsn;
+        const size_t fi = ((size_t)k * window + sl2) * 2 + gsn;
         fold_list[fi] = list_of[4 * (size_t)N + 2 * sg + gsn];
         fold_pos[fi] = pos;
       }
     }
-  std::vector<double> dn(nsh), ldn(nsh), lom(nw_);
-  for (int N = 0; N < nsh; ++N) { dn[N] = calc_dn(L, N); ldn[N] = std::log(dn[N]); }
-  for (int k = 0; k < nw_; ++k) lom[k] = std::log(std::fabs(om[k]));
-  Packer pk;
-  size_t o_li = pk.add(lists), o_it = pk.add(items), o_oi = pk.add(omega_idx), o_om = pk.add(om), o_lo = pk.add(lom),
-         o_dn = pk.add(dn), o_ld = pk.add(ldn), o_wf = pk.add(wfirst), o_wc = pk.add(wcount), o_fl = pk.add(fold_list),
-         o_fp = pk.add(fold_pos);
-  c->meta.ensure(pk.host.size() + 256);
-  h2d(c, c->meta.p, pk.host.data(), pk.host.size());
-  char* mb = c->meta.as<char>();
-  c->dmpart.ensure(sizeof(double) * (size_t)(part + nw_ + 1));
-  LehmannArgs la{};
-  la.lists = (const LehList*)(mb + o_li); la.items = (const LehItem*)(mb + o_it); la.nitems = (int)items.size();
-  la.omega_idx = (const int*)(mb + o_oi); la.omega = (const double*)(mb + o_om); la.log_omega = (const double*)(mb + o_lo);
-  la.dn = (const double*)(mb + o_dn); la.log_dn = (const double*)(mb + o_ld);
-  la.inv_b = 1.0 / p.bbroad; la.b_quarter = p.bbroad / 4.0; la.inv_bt = 1.0 / p.broadtemp;
-  la.partial = c->dmpart.as<double>(); la.out = la.partial + part;
-  la.nomega = nw_; la.win_first = (const int*)(mb + o_wf); la.win_count = (const int*)(mb + o_wc); la.window = window;
-  la.fold_list = (const int*)(mb + o_fl); la.fold_pos = (const int*)(mb + o_fp);
-  if (items.size() > (size_t)INT32_MAX) throw NrgError(NRG_ERR_SIZE, "too many Lehmann work items");
-  cudaEvent_t t1 = tm.start();
-  launch_lehmann(la, c->stream);
-  c->launches += la.nitems > 0 ? 2 : 1;
-  tm.stop(t1, &c->timing.lehmann_ms);
+  Packer pf;
+  const size_t o_li = pf.add(lists), o_fl = pf.add(fold_list), o_fp = pf.add(fold_pos);
+  c->meta.ensure(pf.host.size() + 256);
+  h2d(c, c->meta.p, pf.host.data(), pf.host.size());
+  char* fb = c->meta.as<char>();
+  c->dmrec.ensure(sizeof(double) * std::max(nw_, 1));
+  la.lists = (const LehList*)(fb + o_li); la.items = nullptr; la.nitems = 0;
+  la.fold_list = (const int*)(fb + o_fl); la.fold_pos = (const int*)(fb + o_fp);
+  la.out = c->dmrec.as<double>();
+  cudaEvent_t t2 = tm.start();
+  launch_lehmann_fold(la, c->stream);
+  c->launches++;
+  tm.stop(t2, &c->timing.lehmann_ms);
   std::vector<double> A(nw_);
   d2h(c, A.data(), la.out, sizeof(double) * nw_);
   tm.stop(t0, &c->timing.dm_spectral_ms);
   CU(cudaStreamSynchronize(c->stream));
   check_flag(c);
   tm.collect();
-  (void)all_pairs;
   c->timing.lehmann_pairs = nrec_all;
   c->timing.lehmann_evals = evals;
   for (int k = 0; k < nw_; ++k) { omega_rhow[k] = om[k]; omega_rhow[nomega + k] = A[k]; }

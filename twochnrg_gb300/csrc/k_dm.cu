@@ -258,12 +258,28 @@ __global__ void __launch_bounds__(256) lehmann_kernel(LehmannArgs A) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) { sk[i] = L.key[base + i]; sw[i] = L.w[base + i]; }
     __syncthreads();
     if (!active) continue;
-    for (int i = lane; i < n; i += 32) {
-      const double kk = sk[i], ww = sw[i];
+    if (it.delta != 0.0) {
+      const double d = it.delta, c = exp(-2.0 * d * d);
+#pragma unroll 2
+      for (int i = lane; i < n; i += 32) {
+        const double ww = sw[i], x0 = t[0] - sk[i];
+        double g = exp(-x0 * x0), r = exp(-d * (2.0 * x0 + d));
+        acc[0] += ww * g;
 #pragma unroll
-      for (int q = 0; q < kPerWarp; ++q) {
-        const double x = t[q] - kk;
-        acc[q] += ww * exp(-x * x);
+        for (int q = 1; q < kPerWarp; ++q) {
+          g *= r;
+          r *= c;
+          acc[q] += ww * g;
+        }
+      }
+    } else {
+      for (int i = lane; i < n; i += 32) {
+        const double kk = sk[i], ww = sw[i];
+#pragma unroll
+        for (int q = 0; q < kPerWarp; ++q) {
+          const double x = t[q] - kk;
+          acc[q] += ww * exp(-x * x);
+        }
       }
     }
   }
@@ -273,7 +289,7 @@ __global__ void __launch_bounds__(256) lehmann_kernel(LehmannArgs A) {
     double v = acc[q];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     const int j = j0 + q;
-    if (lane == 0 && j < L.nomega) A.partial[L.part_off + (int64_t)it.chunk * L.nomega + j] = v;
+    if (lane == 0 && j < L.nomega) L.part[(int64_t)it.chunk * L.nomega + j] = v;
   }
 }
 
@@ -293,7 +309,7 @@ __global__ void lehmann_fold_kernel(LehmannArgs A) {
       const LehList L = A.lists[li];
       const int pos = A.fold_pos[fi];
       const int64_t nch = (L.nrec + kRecChunk - 1) / kRecChunk;
-      for (int64_t c = 0; c < nch; ++c) sh += A.partial[L.part_off + c * L.nomega + pos];
+      for (int64_t c = 0; c < nch; ++c) sh += L.part[c * L.nomega + pos];
     }
     tot += sh / A.dn[N];
   }
@@ -321,9 +337,11 @@ void launch_dm_records(const DmRecArgs& a, int pass, cudaStream_t s) {
 }
 
 void launch_lehmann(const LehmannArgs& a, cudaStream_t s) {
-  if (a.nomega <= 0) return;
   if (a.nitems > 0) lehmann_kernel<<<a.nitems, 256, 0, s>>>(a);
-  lehmann_fold_kernel<<<(a.nomega + 127) / 128, 128, 0, s>>>(a);
+}
+
+void launch_lehmann_fold(const LehmannArgs& a, cudaStream_t s) {
+  if (a.nomega > 0) lehmann_fold_kernel<<<(a.nomega + 127) / 128, 128, 0, s>>>(a);
 }
 
 }  // namespace nrg

@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(256) gather_kernel(UpdateArgs A) {
       for (int idx = threadIdx.x; idx < G.rows * kj; idx += blockDim.x) {
         const int a = idx / kj, c = idx - a * kj;
         double* dst = T + (int64_t)(G.dst_base + a * G.dst_stride) * kj + c;
-        *dst = fma(G.coef, Zt[(int64_t)(G.src_base + a * G.src_stride) * kj + c], *dst);
+        *dst = fma(G.coef, Zt[(int64_t)(G.src_base + a * G.src_stride) * J.ldz + c], *dst);
       }
     } else {
       const double* M = A.old_ops[G.op] + G.old_off;
@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(256) gather_kernel(UpdateArgs A) {
         double acc = 0.0;
         const double* Ma = M + (int64_t)a * G.old_ld;
         for (int bb = 0; bb < G.srows; ++bb)
-          acc = fma(Ma[bb], Zt[(int64_t)(G.src_base + bb * G.src_stride) * kj + c], acc);
+          acc = fma(Ma[bb], Zt[(int64_t)(G.src_base + bb * G.src_stride) * J.ldz + c], acc);
         double* dst = T + (int64_t)(G.dst_base + a * G.dst_stride) * kj + c;
         *dst = fma(G.coef, acc, *dst);
       }
@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(256) gemm_kernel(UpdateArgs A) {
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int c = n0 + tx + 16 * j;
-      if (c < N) O[(int64_t)r * N + c] = acc[i][j];
+      if (c < N) O[(int64_t)r * J.ldo + c] = acc[i][j];
     }
   }
 }
@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(256) imp_gemm_kernel(UpdateArgs A) {
       for (int idx = threadIdx.x; idx < TK * TN; idx += 256) {
         const int r = idx / TN, c = idx - r * TN;
         const int gr = k0 + r, gc = n0 + c;
-        Bs[r][c] = (gr < K && gc < N) ? Zt[(int64_t)(G.src_base + gr * G.src_stride) * N + gc] : 0.0;
+        Bs[r][c] = (gr < K && gc < N) ? Zt[(int64_t)(G.src_base + gr * G.src_stride) * J.ldz + gc] : 0.0;
       }
       __syncthreads();
 #pragma unroll

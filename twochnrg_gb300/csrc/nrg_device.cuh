@@ -191,8 +191,9 @@ struct GatherTerm {       // T[dst rows] += coef * M . Zt[src rows]
 };
 struct RotJob {           // O (ki x kj) = Z_I (ki x nI) . T (nI x kj)
   int ki, kj, nI;
+  int ldz, ldo;           // row strides of Zt_J and of O (>= kj: a leading part of each)
   int64_t z_off;          // Z_I (row-major ki x nI)
-  int64_t zt_off;         // Zt_J (row-major nJ x kj)
+  int64_t zt_off;         // Zt_J (row-major nJ x ldz)
   int64_t t_off;          // T scratch (nI x kj)
   int64_t o_off;          // output in the new operator's element array
   int op;                 // operator index
@@ -327,9 +328,13 @@ struct LehList {
   int64_t nrec;
   int shell, gauss;
   int nomega, omega_first;  // frequencies: omega_idx[omega_first .. +nomega)
-  int64_t part_off;         // partial sums [chunk][nomega]
+  double* part;             // partial sums [chunk][nomega]
 };
-struct LehItem { int list, chunk, tile; };
+// delta != 0: the tile's frequencies are evenly spaced in t by delta (a
+// log-spaced grid on a log-Gaussian list), and exp(-(t - key)^2) along the
+// 8 frequencies of a warp follows from two exponentials by the recurrence
+// g_{q+1} = g_q r_q, r_{q+1} = r_q exp(-2 delta^2).
+struct LehItem { int list, chunk, tile; double delta; };
 struct LehmannArgs {      // A(omega) = sum_N sum_records w exp(-(t - key)^2) / D_N
   const LehList* lists;
   const LehItem* items;
@@ -340,7 +345,6 @@ struct LehmannArgs {      // A(omega) = sum_N sum_records w exp(-(t - key)^2) / 
   const double* dn;         // D_N
   const double* log_dn;     // ln D_N
   double inv_b, b_quarter, inv_bt;
-  double* partial;
   int nomega;
   const int* win_first;     // first shell of each frequency's window
   const int* win_count;     // shells in the window (<= window)
@@ -349,6 +353,7 @@ struct LehmannArgs {      // A(omega) = sum_N sum_records w exp(-(t - key)^2) / 
   const int* fold_pos;      // the frequency's position in that list
   double* out;              // [nomega]
 };
-void launch_lehmann(const LehmannArgs& a, cudaStream_t s);
+void launch_lehmann(const LehmannArgs& a, cudaStream_t s);       // the items (one shell's lists)
+void launch_lehmann_fold(const LehmannArgs& a, cudaStream_t s);  // every list -> out
 
 }  // namespace nrg
