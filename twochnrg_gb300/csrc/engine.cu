@@ -101,6 +101,7 @@ struct DmShell {
   int64_t zsize = 0;
   DevBuf Z, cdel;                      // eigenvectors (row = eigenvector) and c_d elements
   DevBuf rho;                          // reduced density matrix, dense blocks laid out like Z
+  std::vector<int> rrows;              // per block: rho is zero beyond its leading rrows x rrows part
   DevBuf lpart;                        // Lehmann partial sums of this shell's record lists
   int64_t nrec[4] = {0, 0, 0, 0};
 };
@@ -1178,6 +1179,12 @@ void dm_backprop_impl(nrg_ctx* c, const nrg_dm_params* prm, double* rho_trace) {
     }
     s.rho.ensure(sizeof(double) * R.size());
     h2d(c, s.rho.p, R.data(), sizeof(double) * s.zsize);
+    s.rrows.assign(s.bsize.size(), 0);
+    for (size_t b = 0; b < s.bsize.size(); ++b) {
+      const int n = s.bsize[b];
+      for (int i = 0; i < n; ++i)
+        if (R[s.zoff[b] + (int64_t)i * n + i] != 0.0) s.rrows[b] = i + 1;
+    }
   }
   for (int N = Nmax - 1; N >= 0; --N) {
     DmShell& sN = *c->dm[N];
@@ -1188,11 +1195,15 @@ void dm_backprop_impl(nrg_ctx* c, const nrg_dm_params* prm, double* rho_trace) {
     double* Tm = c->T.as<double>();
     double* rot = (double*)((char*)c->T.p + ((zs + 255) & ~size_t(255)));
     GemmPlan g1, g2;
+    // rho_b is zero beyond its leading r x r part (kept x kept, then the
+    // discarded states whose Boltzmann weight is not 0), so T = rho Z has r
+    // nonzero rows and Z^T T sums over r of them: the same terms in the
+    // same order as the full products.
     for (size_t b = 0; b < s1.bsize.size(); ++b) {
-      const int n = s1.bsize[b];
+      const int n = s1.bsize[b], r = s1.rrows[b];
       const double* Z = s1.Z.as<double>() + s1.zoff[b];
-      g1.add(GemmJob{n, n, n, 0, s1.rho.as<double>() + s1.zoff[b], n, Z, n, Tm + s1.zoff[b], n});
-      g2.add(GemmJob{n, n, n, 1, Z, n, Tm + s1.zoff[b], n, rot + s1.zoff[b], n});
+      g1.add(GemmJob{r, n, r, 0, s1.rho.as<double>() + s1.zoff[b], n, Z, n, Tm + s1.zoff[b], n});
+      g2.add(GemmJob{n, n, r, 1, Z, n, Tm + s1.zoff[b], n, rot + s1.zoff[b], n});
     }
     run_gemm_plan(c, g1);
     run_gemm_plan(c, g2);
@@ -1242,6 +1253,17 @@ void dm_backprop_impl(nrg_ctx* c, const nrg_dm_params* prm, double* rho_trace) {
     ta.terms = (const DmTraceTerm*)(mb + o_t); ta.rot = rot; ta.en = (const double*)(mb + o_en);
     ta.kept = (const unsigned char*)(mb + o_kp); ta.beta = 1 / TempBar;
     ta.zdisc = ZTot / std::pow(p.site_dim, Nmax - N); ta.rho = sN.rho.as<double>();
+    // Nonzero rows of rho_N: the kept states, then the discarded ones whose
+    // exp(-beta E) may not underflow (beta E <= 800; exp gives 0 beyond
+    // 745.2), a prefix of each block as the energies ascend.
+    sN.rrows.assign(nbN, 0);
+    for (int b = 0; b < nbN; ++b) {
+      int r = nkept[b];
+      if (ta.zdisc != 0.0)
+        for (int i = nkept[b]; i < sN.bsize[b]; ++i)
+          if (ta.beta * sN.en[sN.boff[b] + i] <= 800.0) r = i + 1;
+      sN.rrows[b] = r;
+    }
     launch_dm_trace(ta, nbN, c->stream);
     c->launches++;
     CU(cudaStreamSynchronize(c->stream));  // meta and T are reused by the next shell
@@ -1373,10 +1395,13 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
       }
       P.cg = cgf;
       P.skip = ((nk[b1] == 0 && nk[b2] == 0) || (nd[b1] == 0 && nd[b2] == 0)) ? 1 : 0;
+      P.r1 = s.rrows[b1]; P.r2 = s.rrows[b2];
       if (!last && !P.skip) {
+        // rho A has r1 nonzero rows, A rho r2 nonzero columns (the rest is
+        // never read).
         const double* Acd = s.cdel.as<double>() + P.a_off;
-        g.add(GemmJob{P.n1, P.n2, P.n1, 0, s.rho.as<double>() + s.zoff[b1], P.n1, Acd, P.n2, P1 + poff, P.n2});
-        g.add(GemmJob{P.n1, P.n2, P.n2, 0, Acd, P.n2, s.rho.as<double>() + s.zoff[b2], P.n2, P2 + poff, P.n2});
+        g.add(GemmJob{P.r1, P.n2, P.r1, 0, s.rho.as<double>() + s.zoff[b1], P.n1, Acd, P.n2, P1 + poff, P.n2});
+        g.add(GemmJob{P.n1, P.r2, P.r2, 0, Acd, P.n2, s.rho.as<double>() + s.zoff[b2], P.n2, P2 + poff, P.n2});
       }
       if ((int64_t)P.n1 * P.n2 > (int64_t)INT32_MAX) throw NrgError(NRG_ERR_SIZE, "c_d block pair too large");
       if (last || !P.skip)

@@ -113,7 +113,8 @@ __device__ __forceinline__ void pair_value(const DmRecArgs& A, const DmPair& P, 
     const double sum12 = __dadd_rn(__dmul_rn(m, exp(-A.beta_last * E1)), __dmul_rn(exp(-A.beta_last * E2), m));
     wp = wn = __dmul_rn(__dmul_rn(P.cg, __dmul_rn(sum12, m)), A.inv_z_last);
   } else if (!P.skip) {
-    const double w = __dmul_rn(P.cg, __dmul_rn(__dadd_rn(A.P1[P.p_off + idx], A.P2[P.p_off + idx]), m));
+    const double p1 = a < P.r1 ? A.P1[P.p_off + idx] : 0.0, p2 = b < P.r2 ? A.P2[P.p_off + idx] : 0.0;
+    const double w = __dmul_rn(P.cg, __dmul_rn(__dadd_rn(p1, p2), m));
     if (!A.kept[P.s2 + b]) wp = w;
     if (!A.kept[P.s1 + a]) wn = w;
   }

@@ -284,6 +284,7 @@ struct DmPair {           // one block pair (b1, b2) of c_d
   int64_t p_off;          // rho1 . A and A . rho2 (each n1 x n2) in scratch
   double cg;              // sum_Sz CG^2 of the spectral sum
   int skip;               // both blocks without kept or without discarded states
+  int r1, r2;             // rho1 . A is zero beyond row r1, A . rho2 beyond column r2
 };
 // The Lehmann pairs of one shell as records of the broadened-delta sum.
 // A pair (i, j) of a c_d block pair has dE = E_j - E_i and the FDM weights
