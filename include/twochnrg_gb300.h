@@ -130,8 +130,8 @@ typedef struct {
   double dm_backprop_ms;  /* nrg_dm_backprop: rotations + partial traces        */
   double dm_spectral_ms;  /* nrg_lehmann: pair weights + Lehmann sums           */
   double lehmann_ms;      /* nrg_lehmann: the Lehmann-sum kernels alone         */
-  int64_t lehmann_pairs;  /* (E_j - E_i, weight) pairs over all shells          */
-  int64_t lehmann_evals;  /* pair x frequency evaluations of the broadened delta */
+  int64_t lehmann_pairs;  /* Lehmann pairs whose term can be nonzero, all shells */
+  int64_t lehmann_evals;  /* those pairs x the frequencies of their shell window */
   double vectors_ms;      /* inverse iteration + reorthogonalization            */
 } nrg_timing;
 

@@ -143,6 +143,7 @@ struct nrg_ctx {
   // DM-NRG shells of the last nrg_sweep_run_dm, and the density matrices
   double dm_lambda = 0.0;
   int dm_model = 0;  // ModelKind of the shells
+  bool shared_gpu = false;  // a batch worker: other contexts run beside this one
   std::vector<std::unique_ptr<nrg::DmShell>> dm;
   bool dm_rho_valid = false;
   double dm_temp = 0.0;                // temperature the density matrices were built for
@@ -261,10 +262,14 @@ void plan_blocks(EigPlan& P, const std::vector<int>& bsize) {
   P.hsize = h;
 }
 
-int choose_cluster(int maxn) {
+// Cluster size of the small-block tridiagonalization.  A context that shares
+// the GPU with others (the workers of nrg_sweep_batch) stays at 8 CTAs: the
+// 16-CTA clusters need a whole free GPC each and serialize against the other
+// contexts' kernels (256 batched solves: 40.2 s with 16, 35.0 s with 8).
+int choose_cluster(int maxn, bool shared_gpu) {
   const char* s = std::getenv("NRG_CLUSTER");
   if (s) return std::atoi(s);
-  return maxn >= 256 ? 16 : 8;
+  return (maxn >= 256 && !shared_gpu) ? 16 : 8;
 }
 
 // Blocks at least this large are tridiagonalized by a cooperative grid of
@@ -364,7 +369,7 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
     ts.order = d_order + nbig;
     ts.nblocks = nb - nbig;
     ts.maxn = std::max(maxs, 2);
-    int cluster = choose_cluster(maxs);
+    int cluster = choose_cluster(maxs, c->shared_gpu);
     int ncl = tridiag_max_clusters(cluster, ts.maxn);
     if (ncl <= 0) { cluster = 8; ncl = tridiag_max_clusters(cluster, ts.maxn); }
     if (ncl <= 0) throw NrgError(NRG_ERR_SIZE, "tridiagonalization does not fit on the device");
@@ -2392,6 +2397,7 @@ nrg_status nrg_sweep_batch(int device, int ninst, const nrg_sweep_config* cfgs, 
         if (g_batch_err.empty()) g_batch_err = "nrg_create failed in a batch worker";
         return;
       }
+      c->shared_gpu = nw > 1;
       for (int i; (i = next.fetch_add(1)) < ninst;) {
         st = nrg_sweep_run(c, &cfgs[i]);
         if (st != NRG_OK) {
