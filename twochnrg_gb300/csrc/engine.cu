@@ -2383,6 +2383,18 @@ nrg_status nrg_sweep_batch(int device, int ninst, const nrg_sweep_config* cfgs, 
     std::lock_guard<std::mutex> lock(g_batch_mu);
     g_batch_err.clear();
   }
+  // Largest instances first (kept count x iterations x site size): the
+  // workers' device buffers reach their final size on their first instance,
+  // so later instances do not reallocate (cudaFree waits for the whole
+  // device, every worker's kernels included), and the last instances to
+  // finish are short ones.
+  std::vector<int> order(ninst);
+  for (int i = 0; i < ninst; ++i) order[i] = i;
+  auto cost = [&](int i) {
+    const double site = cfgs[i].model == NRG_MODEL_2CH_QS ? 16.0 : 4.0;
+    return (double)cfgs[i].ncutoff * site * cfgs[i].nsites;
+  };
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost(a) > cost(b); });
   std::atomic<int> next(0);
   std::atomic<int> status(NRG_OK);
   std::vector<std::thread> th;
@@ -2398,7 +2410,8 @@ nrg_status nrg_sweep_batch(int device, int ninst, const nrg_sweep_config* cfgs, 
         return;
       }
       c->shared_gpu = nw > 1;
-      for (int i; (i = next.fetch_add(1)) < ninst;) {
+      for (int k; (k = next.fetch_add(1)) < ninst;) {
+        const int i = order[k];
         st = nrg_sweep_run(c, &cfgs[i]);
         if (st != NRG_OK) {
           status.store(st);
