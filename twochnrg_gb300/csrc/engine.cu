@@ -1480,7 +1480,8 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
       part += nchk * li.nomega;
       evals += li.nrec * li.nomega;
       // Tiles of a log-Gaussian list whose frequencies are evenly spaced in
-      // ln|omega| (to 1e-12 of the step; the step at most 0.5 b) take the
+      // ln|omega| (to 1e-12 of the step; the step at most 0.1 b, so that 16
+      // steps move the Gaussian's argument by at most 1.6) take the
       // recurrence.
       std::vector<double> tile_delta(ntile, 0.0);
       if (!li.gauss)
@@ -1488,7 +1489,7 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
           const int j0 = tl * kOmegaTile, j1 = std::min(li.nomega, j0 + kOmegaTile);
           if (j1 - j0 < 2) continue;
           const double d = (lom[ks[j1 - 1]] - lom[ks[j0]]) / (j1 - 1 - j0);
-          bool even = std::isfinite(d) && d != 0.0 && std::fabs(d) <= 0.5 * p.bbroad;
+          bool even = std::isfinite(d) && d != 0.0 && std::fabs(d) <= 0.1 * p.bbroad;
           for (int j = j0; even && j + 1 < j1; ++j)
             even = std::fabs((lom[ks[j + 1]] - lom[ks[j]]) - d) <= 1e-12 * std::fabs(d);
           if (even) tile_delta[tl] = d / p.bbroad;

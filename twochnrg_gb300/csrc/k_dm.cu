@@ -229,28 +229,33 @@ __global__ void __launch_bounds__(256) dm_scatter_kernel(DmRecArgs A) {
 }
 
 // One CTA per (list, chunk of kRecChunk records, tile of kOmegaTile
-// frequencies): the records are staged in shared memory once and every
-// warp sums them against 8 frequencies held in registers.
+// frequencies): the records are staged in shared memory once; warp w sums
+// the records of its half (w / 4) against the 16 frequencies of its quarter
+// of the tile (w % 4), held in registers, and the halves are added in
+// shared memory in a fixed order.
 __global__ void __launch_bounds__(256) lehmann_kernel(LehmannArgs A) {
-  constexpr int kStage = 2048, kPerWarp = 8;
-  __shared__ double sk[kStage], sw[kStage];
+  constexpr int kStage = 2048, kPerWarp = 16, kGroups = kOmegaTile / kPerWarp, kSplit = 8 / kGroups;
+  __shared__ double sk[kStage], sw[kStage], st[kOmegaTile], sred[8][kPerWarp];
   const LehItem it = A.items[blockIdx.x];
   const LehList L = A.lists[it.list];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int j0 = it.tile * kOmegaTile + warp * kPerWarp;
-  double t[kPerWarp], acc[kPerWarp];
+  const int grp = warp % kGroups, part = warp / kGroups;
+  const int jt = it.tile * kOmegaTile;
   const double ldn = A.log_dn[L.shell], dn = A.dn[L.shell];
-#pragma unroll
-  for (int q = 0; q < kPerWarp; ++q) {
-    acc[q] = 0.0;
-    t[q] = 0.0;
-    const int j = j0 + q;
+  if (threadIdx.x < kOmegaTile) {
+    const int j = jt + threadIdx.x;
+    double t = 0.0;
     if (j < L.nomega) {
       const int k = A.omega_idx[L.omega_first + j];
-      t[q] = L.gauss ? (A.omega[k] / dn) * A.inv_bt : (A.log_omega[k] - ldn) * A.inv_b - A.b_quarter;
+      t = L.gauss ? (A.omega[k] / dn) * A.inv_bt : (A.log_omega[k] - ldn) * A.inv_b - A.b_quarter;
     }
+    st[threadIdx.x] = t;
   }
+  const int j0 = jt + grp * kPerWarp;
   const bool active = j0 < L.nomega;
+  double acc[kPerWarp];
+#pragma unroll
+  for (int q = 0; q < kPerWarp; ++q) acc[q] = 0.0;
   const int64_t r0 = (int64_t)it.chunk * kRecChunk;
   const int64_t r1 = min(r0 + (int64_t)kRecChunk, L.nrec);
   for (int64_t base = r0; base < r1; base += kStage) {
@@ -259,11 +264,11 @@ __global__ void __launch_bounds__(256) lehmann_kernel(LehmannArgs A) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) { sk[i] = L.key[base + i]; sw[i] = L.w[base + i]; }
     __syncthreads();
     if (!active) continue;
+    const double* tq = st + grp * kPerWarp;
     if (it.delta != 0.0) {
-      const double d = it.delta, c = exp(-2.0 * d * d);
-#pragma unroll 2
-      for (int i = lane; i < n; i += 32) {
-        const double ww = sw[i], x0 = t[0] - sk[i];
+      const double d = it.delta, c = exp(-2.0 * d * d), t0 = tq[0];
+      for (int i = part * 32 + lane; i < n; i += 32 * kSplit) {
+        const double ww = sw[i], x0 = t0 - sk[i];
         double g = exp(-x0 * x0), r = exp(-d * (2.0 * x0 + d));
         acc[0] += ww * g;
 #pragma unroll
@@ -274,23 +279,38 @@ __global__ void __launch_bounds__(256) lehmann_kernel(LehmannArgs A) {
         }
       }
     } else {
-      for (int i = lane; i < n; i += 32) {
-        const double kk = sk[i], ww = sw[i];
+      // Eight frequencies per pass over the records (register pressure).
 #pragma unroll
-        for (int q = 0; q < kPerWarp; ++q) {
-          const double x = t[q] - kk;
-          acc[q] += ww * exp(-x * x);
+      for (int qb = 0; qb < kPerWarp; qb += 8) {
+        double a8[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int i = part * 32 + lane; i < n; i += 32 * kSplit) {
+          const double kk = sk[i], ww = sw[i];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const double x = tq[qb + q] - kk;
+            a8[q] += ww * exp(-x * x);
+          }
         }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc[qb + q] += a8[q];
       }
     }
   }
-  if (!active) return;
+  // Warp sums: lane q < kPerWarp ends with frequency q's.
+  double mine = 0.0;
 #pragma unroll
   for (int q = 0; q < kPerWarp; ++q) {
     double v = acc[q];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int j = j0 + q;
-    if (lane == 0 && j < L.nomega) L.part[(int64_t)it.chunk * L.nomega + j] = v;
+    if (lane == q) mine = v;
+  }
+  if (lane < kPerWarp) sred[warp][lane] = mine;
+  __syncthreads();
+  if (part == 0 && active && lane < kPerWarp) {
+    double v = 0.0;
+    for (int p = 0; p < kSplit; ++p) v += sred[grp + p * kGroups][lane];
+    const int j = j0 + lane;
+    if (j < L.nomega) L.part[(int64_t)it.chunk * L.nomega + j] = v;
   }
 }
 

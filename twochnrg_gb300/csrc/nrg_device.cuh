@@ -333,7 +333,7 @@ struct LehList {
 };
 // delta != 0: the tile's frequencies are evenly spaced in t by delta (a
 // log-spaced grid on a log-Gaussian list), and exp(-(t - key)^2) along the
-// 8 frequencies of a warp follows from two exponentials by the recurrence
+// 16 frequencies of a warp follows from two exponentials by the recurrence
 // g_{q+1} = g_q r_q, r_{q+1} = r_q exp(-2 delta^2).
 struct LehItem { int list, chunk, tile; double delta; };
 struct LehmannArgs {      // A(omega) = sum_N sum_records w exp(-(t - key)^2) / D_N
