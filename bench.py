@@ -108,7 +108,7 @@ def sum_n3(result) -> float:
     return float(sum(float((it.bsize.astype(float) ** 3).sum()) for it in result.iters))
 
 
-def cpu_sample(nthreads: int):
+def cpu_sample(nthreads: int, want_result: bool = False):
     """Time the oracle port (the reference's algorithm on the host cores)."""
     from oracle import oracle as orc
     t = time.perf_counter()
@@ -116,7 +116,30 @@ def cpu_sample(nthreads: int):
                 CPU_SAMPLE["U"], CPU_SAMPLE["ed"], CPU_SAMPLE["gamma1"], CPU_SAMPLE["gamma2_or_B"],
                 nthreads=nthreads, blas_threads=1)
     dt = time.perf_counter() - t
-    return dt, sum_n3(s)
+    return (dt, sum_n3(s), s) if want_result else (dt, sum_n3(s))
+
+
+def sweep_errors(gpu, ref) -> dict:
+    """Largest deviations of a GPU sweep from the oracle's on the same
+    inputs: block eigenvalues relative to each iteration's largest level,
+    the thermodynamics (beta, T, T chi, S at four temperatures) and the
+    operator averages (<n_d> first) relative to their size."""
+    import numpy as np
+    eig = thermo = tchi = opavg = nd = 0.0
+    for a, b in zip(gpu.iters, ref.iters):
+        scale = max(1.0, float(np.abs(b.en).max()))
+        eig = max(eig, float(np.abs(np.asarray(a.en) - np.asarray(b.en)).max()) / scale)
+        ta, tb = np.asarray(a.thermo, dtype=float).ravel(), np.asarray(b.thermo, dtype=float).ravel()
+        rel = np.abs(ta - tb) / np.maximum(np.abs(tb), 1e-300)
+        thermo = max(thermo, float(rel.max()))
+        tchi = max(tchi, float(rel.reshape(-1, 4)[:, 2].max()))
+        oa, ob = np.asarray(a.opavg, dtype=float), np.asarray(b.opavg, dtype=float)
+        if ob.size:
+            r = np.abs(oa - ob) / np.maximum(np.abs(ob), 1e-300)
+            opavg = max(opavg, float(r.max()))
+            nd = max(nd, float(r[0]))
+    return {"eigenvalues_rel_max": eig, "n_d_rel_max": nd, "T_chi_rel_max": tchi, "thermo_rel_max": thermo,
+            "opavg_rel_max": opavg, "iterations": min(len(gpu.iters), len(ref.iters))}
 
 
 # sum_b n_b^3 over the 50 iterations of the full workload, from the block
@@ -370,11 +393,17 @@ def main():
         "lehmann_bound": "fp64 (one exp per nonzero Lehmann record and frequency)"}
     if not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
-        dt, w_s = cpu_sample(cores)
+        dt, w_s, ref = cpu_sample(cores, want_result=True)
         line["cpu_baseline"] = {
             "value": dt * w_full / w_s, "unit": "s", "cores": cores, "kind": "port",
             "sample": (f"oracle port, same model/parameters with 600 kept and 8 iterations: {dt:.2f} s on "
                        f"{cores} threads, scaled by the sum n^3 ratio {w_full / w_s:.1f}")}
+        # The GPU sweep against the FP64 oracle on that sample.
+        C = CPU_SAMPLE
+        gs = eng.sweep(C["model"], C["nsites"], C["ncutoff"], C["lam"], C["U"], C["ed"], C["gamma1"],
+                      C["gamma2_or_B"])
+        line["accuracy"] = {"sweep": dict(sweep_errors(gs, ref), sample=(
+            "two-channel sweep, same model/parameters, 600 kept, 8 iterations, GPU against the FP64 oracle"))}
         cbs, cdt, cn = cpu_batch_sample(cores)
         line["batched"]["cpu_baseline"] = {
             "value": cbs, "unit": "solves/s", "cores": cores, "kind": "port",
@@ -384,9 +413,17 @@ def main():
         from oracle import oracle as orc
         g = gpu_dm(eng, DM_SAMPLE, DM_SAMPLE_NOMEGA)
         t = time.perf_counter()
-        orc.dm_spectral(DM_SAMPLE["nsites"], DM_SAMPLE["ncutoff"], DM_SAMPLE["lam"], DM_SAMPLE["U"],
-                        DM_SAMPLE["ed"], DM_SAMPLE["gamma"], DM_TEMP, DM_BROAD, omegas=dm_omegas(DM_SAMPLE_NOMEGA))
+        o_dm = orc.dm_spectral(DM_SAMPLE["nsites"], DM_SAMPLE["ncutoff"], DM_SAMPLE["lam"], DM_SAMPLE["U"],
+                               DM_SAMPLE["ed"], DM_SAMPLE["gamma"], DM_TEMP, DM_BROAD,
+                               omegas=dm_omegas(DM_SAMPLE_NOMEGA))
         cdm = (time.perf_counter() - t) * 1e3
+        import numpy as np
+        A_gpu, A_ref = np.asarray(g[6]), np.asarray(o_dm[1])
+        line.setdefault("accuracy", {})["dm_spectral"] = {
+            "A_rel_max": float((np.abs(A_gpu - A_ref) / np.maximum(np.abs(A_ref), 1e-300)).max()),
+            "A_abs_max_over_max_A": float(np.abs(A_gpu - A_ref).max() / np.abs(A_ref).max()),
+            "sample": (f"one-channel DM-NRG, {DM_SAMPLE['nsites']} iterations, {DM_SAMPLE['ncutoff']} kept, "
+                       f"{DM_SAMPLE_NOMEGA} frequencies, GPU against the FP64 oracle")}
         line["dm_spectral"]["cpu_baseline"] = {
             "value": cdm, "unit": "ms", "cores": 1, "kind": "port",
             "sample": (f"oracle port (single thread) on {DM_SAMPLE['nsites']} iterations, {DM_SAMPLE['ncutoff']} "
