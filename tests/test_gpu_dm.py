@@ -1,7 +1,9 @@
 """DM-NRG on the GPU (nrg_sweep_run_dm -> nrg_dm_backprop -> nrg_lehmann)
 against the reference DM_NRG's own A(omega) (tests/golden/dm_*.npz, made by
 tests/golden/make_dm_golden.py) and against the oracle on other temperatures
-and frequency grids.
+and frequency grids; the two-channel shells against the one-channel model
+with Gamma1 + Gamma2 (an exact identity with every state kept) and against
+the oracle's restatement.
 
 Tolerance: spectra within 1e-8 relative (the block eigenvectors come from a
 different eigensolver than LAPACK's, so agreement is at the eigenvector
