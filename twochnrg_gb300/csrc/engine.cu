@@ -263,13 +263,16 @@ void plan_blocks(EigPlan& P, const std::vector<int>& bsize) {
 }
 
 // Cluster size of the small-block tridiagonalization.  A context that shares
-// the GPU with others (the workers of nrg_sweep_batch) stays at 8 CTAs: the
-// 16-CTA clusters need a whole free GPC each and serialize against the other
-// contexts' kernels (256 batched solves: 40.2 s with 16, 35.0 s with 8).
+// the GPU with others (the workers of nrg_sweep_batch) uses 4 CTAs: large
+// clusters need whole free GPCs and serialize against the other contexts'
+// kernels, and a block's Householder steps wait on one barrier each however
+// many SMs share them (256 batched solves, 16 workers: 40.2 s with clusters
+// of 16 and 8, 35.0 s with 8, 28.9 s with 4, 36.2 s with 2).
 int choose_cluster(int maxn, bool shared_gpu) {
   const char* s = std::getenv("NRG_CLUSTER");
   if (s) return std::atoi(s);
-  return (maxn >= 256 && !shared_gpu) ? 16 : 8;
+  if (shared_gpu) return 4;
+  return maxn >= 256 ? 16 : 8;
 }
 
 // Blocks at least this large are tridiagonalized by a cooperative grid of
