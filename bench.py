@@ -45,6 +45,17 @@ CPU_SAMPLE = dict(model="2chQS", nsites=8, ncutoff=600, lam=2.5, U=0.3, ed=-0.15
 TRIDIAG_DRAM_BYTES_PER_FLOP = None
 
 
+def max_over_ranks(dist, *vals):
+    """Each value's maximum over the ranks (replicas only: the ranks share
+    nothing but this reduction and the barriers)."""
+    if dist is None:
+        return vals
+    import torch
+    t = torch.tensor(vals, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return tuple(float(x) for x in t)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -343,11 +354,7 @@ def main():
     ck = clocks.stop()
     value = statistics.mean(dev_ms) / 1e3
     e2e = statistics.mean(wall)
-    if dist:
-        import torch
-        t = torch.tensor([value, e2e], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        value, e2e = float(t[0]), float(t[1])
+    value, e2e = max_over_ranks(dist, value, e2e)
     if rank != 0:
         return
     T = tim[-1]
