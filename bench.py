@@ -40,9 +40,12 @@ WARMUP_NSITES = 6
 # dspev cost that dominates the CPU path).
 CPU_SAMPLE = dict(model="2chQS", nsites=8, ncutoff=600, lam=2.5, U=0.3, ed=-0.15, gamma1=0.01,
                   gamma2_or_B=0.01)
-# DRAM bytes per algorithmic FP64 flop of the tridiagonalization, from the
-# ncu capture summarised in profiles/tridiag_fp64_2chQS.md.
-TRIDIAG_DRAM_BYTES_PER_FLOP = None
+# DRAM traffic of the tridiagonalization, from the ncu capture summarised in
+# profiles/tridiag_fp64_2chQS.md: one n = 2400 block read 46 MB (its n^2
+# doubles, touched once; the rest of the passes hit L2) and wrote 5 MB.  The
+# traffic of a launch therefore scales with the n^2 of its blocks, not with
+# the flops: 8 B x n^2 x (1 + 5/46).
+TRIDIAG_DRAM_BYTES_PER_ELEMENT = 8.0 * (1.0 + 5.0 / 46.0)
 
 
 def max_over_ranks(dist, *vals):
@@ -117,6 +120,10 @@ class ClockSampler:
 
 def sum_n3(result) -> float:
     return float(sum(float((it.bsize.astype(float) ** 3).sum()) for it in result.iters))
+
+
+def sum_n2(result) -> float:
+    return float(sum(float((it.bsize.astype(float) ** 2).sum()) for it in result.iters))
 
 
 def cpu_sample(nthreads: int, want_result: bool = False):
@@ -361,8 +368,8 @@ def main():
     tri_ms = T["tridiag_ms"]
     achieved = T["tridiag_flops"] / (tri_ms * 1e-3) / 1e12
     traffic = None
-    if TRIDIAG_DRAM_BYTES_PER_FLOP is not None and T["tridiag_launches"]:
-        traffic = TRIDIAG_DRAM_BYTES_PER_FLOP * T["tridiag_flops"] / T["tridiag_launches"]
+    if T["tridiag_launches"]:
+        traffic = TRIDIAG_DRAM_BYTES_PER_ELEMENT * sum_n2(res) / T["tridiag_launches"]
     w_full = sum_n3(res)
     line = {
         "metric": "2ch NRG sweep s", "value": value, "unit": "s", "n_gpus": args.gpus,
