@@ -466,11 +466,14 @@ nrg_status nrg_dm_save_bin(nrg_ctx* ctx, const char* dir, const char* name);
  *   stream   cudaStream_t to run on (NULL = default stream); the call returns
  *            after the stream has reached the end of the solve
  * The solver's scratch is one fixed array of about 3.7 MB in device memory,
- * reserved when the library is loaded and kept by every GPU that loads it
- * until the process exits.  The first call on a device looks up the array's
- * device address with that device current; call on the device you want to
- * use.  All calls share the array: calls that overlap on the GPU (other host
- * threads, other streams) race and must not be issued. */
+ * kept by every GPU that loads it until the process exits.  Each call looks
+ * up the array's device address on the current device; call on the device
+ * you want to use.  CUDA loads the module that holds the array lazily, at its
+ * first use on a device, and that load can allocate device memory and
+ * synchronise: make one warm-up call per device before carving out device
+ * memory, or run the process with CUDA_MODULE_LOADING=EAGER.  All calls share
+ * the array: calls that overlap on the GPU (other host threads, other
+ * streams) race and must not be issued. */
 nrg_status nrg_diag_block_noalloc(int n, const double* a, double* eigvals, double* eigvecs, void* stream);
 
 #ifdef __cplusplus

@@ -2,11 +2,11 @@
 # Build the unmodified reference TwoChNRG NRG_main (and the reference-linked
 # golden-vector harness) from the read-only reference tree, for use as a test
 # oracle only.  Outputs go to oracle/_ref/ (git-ignored).  Needs the reference
-# tree (default /root/reference, override with REF_DIR) and scipy's bundled
+# tree (REF_DIR; unset, the directory "reference" beside the repository) and scipy's bundled
 # OpenBLAS for LAPACK/BLAS.  Nothing here is part of the product path.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF_DIR="${REF_DIR:-/root/reference}"
+REF_DIR="${REF_DIR:-$(cd "$HERE/../.." && pwd)/reference}"
 OUT="$HERE/_ref"
 OBJ="$OUT/obj"
 mkdir -p "$OBJ"

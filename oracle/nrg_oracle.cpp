@@ -1599,6 +1599,7 @@ struct OracleIter {
   std::vector<double> thermo;     // 4 x (beta, T, suscep, entropy)
   std::vector<double> opavg;      // CalcAvg operators over AeigCut
   std::vector<int> kept_bsize;    // AeigCut block sizes
+  double seconds = 0;             // wall time of this iteration
   // Optional capture of the DiagHN inputs/outputs for drop-in tests.
   std::vector<double> basis_qn, basis_en;
   std::vector<int> basis_bbe, basis_itype, basis_stcf;
@@ -1861,6 +1862,7 @@ void* oracle_run(const oracle_config* cfg) {
   }
   const int ien = nchan + 1;  // e_N's place in ParamsHN (NRG_main.cpp:272-276)
   for (int N = N0; N < cfg->nsites; ++N) {
+    const auto t_iter = std::chrono::steady_clock::now();
     OracleIter I;
     P[ien] = onsite(N);  // GetEn(Nsites) (NRG_main.cpp:198, 408-413)
     I.params = P;
@@ -1924,6 +1926,7 @@ void* oracle_run(const oracle_config* cfg) {
     // (NRG_main.cpp:414-419; NRGchainClass.cpp:187-202, z = 1)
     if (cfg->model == ORACLE_MODEL_1CHS || cfg->model == ORACLE_MODEL_1CHSZ)
       P[3] = std::pow(Lambda, 0.5 * (double)N) / HLF * cfg->delta_sc;
+    I.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_iter).count();
     R->it.push_back(std::move(I));
   }
   R->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -1947,6 +1950,7 @@ int oracle_iter_nstates(void* h, int n) { return (int)ITER(h, n).en.size(); }
 const double* oracle_iter_en(void* h, int n) { return ITER(h, n).en.data(); }
 double oracle_iter_emin(void* h, int n) { return ITER(h, n).emin; }
 double oracle_iter_ecut(void* h, int n) { return ITER(h, n).ecut; }
+double oracle_iter_seconds(void* h, int n) { return ITER(h, n).seconds; }
 int oracle_iter_nkept(void* h, int n) { return ITER(h, n).nkept; }
 const double* oracle_iter_thermo(void* h, int n) { return ITER(h, n).thermo.data(); }
 const double* oracle_iter_opavg(void* h, int n) { return ITER(h, n).opavg.data(); }

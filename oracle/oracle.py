@@ -72,7 +72,7 @@ def lib():
         L.oracle_cgordan.argtypes = [ctypes.c_double] * 6
         L.oracle_seconds.restype = ctypes.c_double
         L.oracle_op_name.restype = ctypes.c_char_p
-        for name in ("oracle_iter_emin", "oracle_iter_ecut"):
+        for name in ("oracle_iter_emin", "oracle_iter_ecut", "oracle_iter_seconds"):
             getattr(L, name).restype = ctypes.c_double
         for name in ("oracle_iter_qn", "oracle_iter_en", "oracle_iter_thermo", "oracle_iter_opavg",
                      "oracle_iter_params", "oracle_iter_H", "oracle_iter_basis_en", "oracle_opavg_m1"):
@@ -119,6 +119,7 @@ class Iteration:
     basis_itype: np.ndarray | None = None
     basis_stcf: np.ndarray | None = None
     basis_en: np.ndarray | None = None
+    seconds: float = 0.0    # wall time of the iteration
     # capture iteration only: every input/output of DiagHN, SetKept, CutStates
     # and UpdateMatrices by name (old_*, basis_*, eig_*, kept*, cut_*, new_*;
     # per-operator arrays end in .<operator index>)
@@ -181,7 +182,8 @@ def run(model: str, nsites: int, ncutoff: int, lam: float, U: float, ed: float, 
                 nkept=L.oracle_iter_nkept(h, n),
                 thermo=_arr(L.oracle_iter_thermo(h, n), 16, np.float64).reshape(4, 4),
                 opavg=_arr(L.oracle_iter_opavg(h, n), nops, np.float64),
-                kept_bsize=_arr(L.oracle_iter_kept_bsize(h, n), L.oracle_iter_nkeptblocks(h, n), np.int64))
+                kept_bsize=_arr(L.oracle_iter_kept_bsize(h, n), L.oracle_iter_nkeptblocks(h, n), np.int64),
+                seconds=L.oracle_iter_seconds(h, n))
             if n == capture_iter:
                 it.H = _arr(L.oracle_iter_H(h, n), L.oracle_iter_H_size(h, n), np.float64)
                 it.basis_itype = _arr(L.oracle_iter_basis_itype(h, n), ns, np.int64)

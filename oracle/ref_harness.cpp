@@ -21,6 +21,7 @@
 //                  TwoChQS_HN_MatEl with f_ch1 = f_ch2 = d; last arg = Gamma2
 // Output: line records "ITER", "BLK", "EN", "CUT", "THERMO", "OPAVG" (see
 // tests/golden/make_golden.py for the parser).
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -305,6 +306,7 @@ int main(int argc, char** argv) {
 
   ParamsHN[nchan + 1] = chain.GetEn(0);  // NRG_main.cpp:198, 272-273
   for (int N = 0; N < Nsites; ++N) {
+    const auto t_iter = std::chrono::steady_clock::now();
     double DN = HalfLambdaFactor * pow(Lambda, (-(N - 1) / 2.0));  // NRG_main.cpp:283
     BuildBasis(CommonQNs, totSpos, &AeigCut, &Abasis, &SingleSite, 0);
     HN.DiagHN(ParamsHN, &Abasis, &SingleSite, &Mats[0], &Aeig, false);
@@ -333,6 +335,10 @@ int main(int argc, char** argv) {
     printf("KEPTBLK %d", AeigCut.NumBlocks());
     for (int b = 0; b < AeigCut.NumBlocks(); ++b) printf(" %d", AeigCut.GetBlockSize(b));
     printf("\n");
+    // wall seconds of this iteration (the reference routines, one thread)
+    printf("TIME %d %.6f\n", N,
+           std::chrono::duration<double>(std::chrono::steady_clock::now() - t_iter).count());
+    fflush(stdout);
     for (int ich = 0; ich < nchan; ++ich) ParamsHN[ich + 1] = chain.GetChin(N);  // NRG_main.cpp:402-405
     if ((int)ParamsHN.size() > nchan + 2) ParamsHN[nchan + 1] = chain.GetEn(N + 1);  // NRG_main.cpp:408-413
     if (model == "1chS" || model == "1chSz")

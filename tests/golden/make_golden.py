@@ -22,7 +22,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 HARNESS = os.path.join(REPO, "oracle", "_ref", "ref_harness")
-REF = os.environ.get("REF_DIR", "/root/reference")
+# the reference tree: REF_DIR, else the directory "reference" beside the repository
+REF = os.environ.get("REF_DIR", os.path.join(os.path.dirname(REPO), "reference"))
 
 # name: (model, nsites, ncutoff, Lambda, U, ed, Gamma1, Gamma2|B[, Delta_SC])
 CASES = {

@@ -9,14 +9,18 @@
 // device pointers for the input matrix and the outputs, and every scratch
 // array of the eigensolver (the tridiagonalization workspace, the inverse-
 // iteration factors, the launch tables and the error word) lives in one
-// file-scope __device__ array of fixed size, reserved when the library is
-// loaded and held by every GPU that loads it until the process exits.
+// file-scope __device__ array of fixed size, held by every GPU that loads this
+// file's module until the process exits.
+//
+// CUDA loads modules lazily by default: the module holding the array (and the
+// eigensolver kernels') is loaded on a device at its first use there, which
+// can allocate device memory and synchronise.  A caller that must never see
+// that makes one warm-up call per device before it carves out its memory, or
+// runs the process with CUDA_MODULE_LOADING=EAGER.
 //
 // The kernels are the ones nrg_diag_blocks runs (k_tridiag.cu, k_tdeig.cu);
 // only the tables they read are generated on the device instead of uploaded.
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "../../include/twochnrg_gb300.h"
 #include "nrg_device.cuh"
@@ -94,9 +98,6 @@ __global__ void cluster_kernel(Layout L, int n) {
   for (int c = nc; c < n; ++c) { L.cl_block[c] = 0; L.cl_first[c] = 0; L.cl_count[c] = 0; }
 }
 
-std::mutex g_mu;
-void* g_addr[256];
-
 }  // namespace
 }  // namespace nrg
 
@@ -105,18 +106,14 @@ extern "C" nrg_status nrg_diag_block_noalloc(int n, const double* a, double* eig
   using namespace nrg;
   if (n < 1 || !a || !eigvals || !eigvecs) return NRG_ERR_ARG;
   if (n > NRG_NOALLOC_MAX_N) return NRG_ERR_SIZE;
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return NRG_ERR_CUDA;
-  double* base = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
-      void* p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return NRG_ERR_CUDA;
-      g_addr[dev] = p;
-    }
-    base = static_cast<double*>(g_addr[dev]);
-  }
+  // The array's device address on the current device, looked up on every
+  // call: a cached address would go stale if the module were reloaded (a
+  // device reset, another context), and the lookup allocates nothing once
+  // the module is loaded.
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return NRG_ERR_CUDA;
+  double* base = static_cast<double*>(p);
+  if (tridiag_max_clusters(8, n < 2 ? 2 : n) <= 0) return NRG_ERR_SIZE;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const Layout L = layout(base);
   const int bw = backtransform_warps(n);
@@ -131,12 +128,15 @@ extern "C" nrg_status nrg_diag_block_noalloc(int n, const double* a, double* eig
   ea.nblocks = 1; ea.bsize = L.bsize; ea.soff = L.soff; ea.d = L.d; ea.e = L.e; ea.ev = L.ev; ea.nstates = n;
   ea.flag = L.flag; ea.maxn = n; ea.fde = L.fde; ea.e2 = L.e2; ea.split = L.split;
   launch_bisect(ea, L.state_block, s);
+  if (cudaGetLastError() != cudaSuccess) return NRG_ERR_CUDA;
   cluster_kernel<<<1, 32, 0, s>>>(L, n);
+  if (cudaGetLastError() != cudaSuccess) return NRG_ERR_CUDA;
   InvIterArgs ia{};
   ia.nblocks = 1; ia.bsize = L.bsize; ia.soff = L.soff; ia.d = L.d; ia.e = L.e; ia.ev = L.ev; ia.nvec = L.nvec;
   ia.yoff = L.yoff; ia.Y = L.Y; ia.scratch = L.LU; ia.cl_block = L.cl_block; ia.cl_first = L.cl_first;
   ia.cl_count = L.cl_count; ia.nclusters = n; ia.flag = L.flag;
   launch_inviter(ia, L.vec_block, L.vec_index, n, s);
+  if (cudaGetLastError() != cudaSuccess) return NRG_ERR_CUDA;
   BackArgs ba{};
   ba.bsize = L.bsize; ba.hoff = L.hoff; ba.H_const = L.A; ba.soff = L.soff; ba.tau = L.tau; ba.nvec = L.nvec;
   ba.yoff = L.yoff; ba.Y = L.Y; ba.Z = eigvecs; ba.Zt = nullptr; ba.zoff = L.yoff; ba.maxn = n;
