@@ -9,10 +9,22 @@ needed between steps.
 
 Prints one JSON line (rank 0).  `value` is the sweep time in seconds measured
 with CUDA events on the engine's stream (mean over the timed steps, max over
-ranks); `e2e` is the host wall time of the same call including every
-host<->device copy of inputs and results.
+ranks) in the headline arithmetic (--precision, default mixed: the large
+blocks' Householder reduction blocked, its trailing updates as split-BF16
+products on the tensor cores); `e2e` is the host wall time of the same call
+including every host<->device copy of inputs and results.  The plain FP64
+form is timed once after the timed region ("fp64"), and both forms are
+checked against the reference's own outputs for the first five iterations
+at 3000 kept (tests/golden/cfg1_2chQS_n5_k3000.npz) and against each other
+over the whole sweep ("accuracy").
+
+The CPU baseline is the oracle port of the reference algorithm on the host
+cores over iterations 0-3 of the same workload -- iteration 3 is the first at
+the full 3000 kept multiplets -- measured iteration by iteration; the sweep
+total derived from it is labelled an estimate.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--precision mixed|fp64]
 """
 from __future__ import annotations
 
@@ -35,11 +47,15 @@ WORKLOAD_NAME = ("two-channel Anderson NRG sweep, (Q,S) basis: Lambda=2.5, U=0.3
 # Warm-up steps: the first 6 Wilson iterations of the same workload (they
 # reach the full block sizes, so every kernel, code path and buffer is hot).
 WARMUP_NSITES = 6
-# CPU sample: the same model and parameters with 600 kept multiplets, 8
-# iterations; scaled to the full sweep by the ratio of sum_b n_b^3 (the
-# dspev cost that dominates the CPU path).
-CPU_SAMPLE = dict(model="2chQS", nsites=8, ncutoff=600, lam=2.5, U=0.3, ed=-0.15, gamma1=0.01,
-                  gamma2_or_B=0.01)
+# CPU sample: iterations 0-3 of the workload itself.  Iterations 0-2 grow the
+# basis (35, 462, 6435 states); iteration 3 is the first at the full kept count
+# (about 45 600 states, blocks up to 4341), and every later iteration has
+# about the same size (44 600-47 700 states, largest block 4240-4651).
+CPU_ITERS = 4
+# The reference's own routines on one core, from the run that made the
+# fixture tests/golden/cfg1_2chQS_n5_k3000.npz (build container, x86):
+# seconds per iteration of the same workload.
+REF_FIXTURE = "cfg1_2chQS_n5_k3000"
 # DRAM traffic of the tridiagonalization, from the ncu capture summarised in
 # profiles/tridiag_fp64_2chQS.md: one n = 2400 block read 46 MB (its n^2
 # doubles, touched once; the rest of the passes hit L2) and wrote 5 MB.  The
@@ -126,25 +142,64 @@ def sum_n2(result) -> float:
     return float(sum(float((it.bsize.astype(float) ** 2).sum()) for it in result.iters))
 
 
-def cpu_sample(nthreads: int, want_result: bool = False):
-    """Time the oracle port (the reference's algorithm on the host cores)."""
+def cpu_sample(nthreads: int):
+    """The oracle port (the reference's algorithm: element-wise H_N, LAPACK
+    dspev per block, dgemm rotations) on iterations 0-3 of the workload, the
+    blocks of an iteration spread over `nthreads` host threads.  Returns the
+    wall time and the oracle's sweep (with its per-iteration seconds)."""
     from oracle import oracle as orc
+    W = WORKLOAD
     t = time.perf_counter()
-    s = orc.run(CPU_SAMPLE["model"], CPU_SAMPLE["nsites"], CPU_SAMPLE["ncutoff"], CPU_SAMPLE["lam"],
-                CPU_SAMPLE["U"], CPU_SAMPLE["ed"], CPU_SAMPLE["gamma1"], CPU_SAMPLE["gamma2_or_B"],
+    s = orc.run(W["model"], CPU_ITERS, W["ncutoff"], W["lam"], W["U"], W["ed"], W["gamma1"], W["gamma2_or_B"],
                 nthreads=nthreads, blas_threads=1)
-    dt = time.perf_counter() - t
-    return (dt, sum_n3(s), s) if want_result else (dt, sum_n3(s))
+    return time.perf_counter() - t, s
 
 
-def sweep_errors(gpu, ref) -> dict:
-    """Largest deviations of a GPU sweep from the oracle's on the same
-    inputs: block eigenvalues relative to each iteration's largest level,
-    the thermodynamics (beta, T, T chi, S at four temperatures) and the
-    operator averages (<n_d> first) relative to their size."""
+def sweep_estimate(per_iter_s, nsites: int) -> float:
+    """Sweep total from measured iterations: the measured ones plus, for each
+    later iteration, the last (full-size) one's time.  Later iterations have
+    the same kept count and 0.97-1.20 times its sum of n_b^3."""
+    return float(sum(per_iter_s) + (nsites - len(per_iter_s)) * per_iter_s[-1])
+
+
+def load_fixture(name: str):
+    """A reference fixture in the shape of a sweep result (tests/golden)."""
     import numpy as np
-    eig = thermo = tchi = opavg = nd = 0.0
-    for a, b in zip(gpu.iters, ref.iters):
+    g = np.load(os.path.join(ROOT, "tests", "golden", name + ".npz"))
+
+    class It:
+        pass
+
+    its = []
+    for n in range(int(g["niters"])):
+        it = It()
+        it.qn, it.bsize, it.en = g[f"qn_{n}"], g[f"bsize_{n}"], g[f"en_{n}"]
+        it.nkept, it.ecut = int(g[f"nkept_{n}"]), float(g[f"ecut_{n}"])
+        it.kept_bsize, it.thermo, it.opavg = g[f"kept_bsize_{n}"], g[f"thermo_{n}"], g[f"opavg_{n}"]
+        it.seconds = float(g[f"seconds_{n}"]) if f"seconds_{n}" in g else None
+        its.append(it)
+    return its
+
+
+def bookkeeping_exact(gpu_iters, ref_iters) -> bool:
+    import numpy as np
+    for a, b in zip(gpu_iters, ref_iters):
+        if not (np.array_equal(a.bsize, b.bsize) and a.nkept == b.nkept
+                and np.array_equal(a.kept_bsize, b.kept_bsize)):
+            return False
+    return True
+
+
+def sweep_errors(gpu_iters, ref_iters) -> dict:
+    """Largest deviations of a GPU sweep from a reference on the same
+    inputs: block eigenvalues relative to each iteration's largest level,
+    E_cut likewise, the thermodynamics (beta, T, T chi, S at four
+    temperatures) and the operator averages (<n_d> first) relative to their
+    size; and whether every integer of the block bookkeeping agrees."""
+    import numpy as np
+    eig = thermo = tchi = opavg = nd = ecut = 0.0
+    for a, b in zip(gpu_iters, ref_iters):
+        ecut = max(ecut, abs(a.ecut - b.ecut) / max(1.0, float(np.abs(b.en).max())))
         scale = max(1.0, float(np.abs(b.en).max()))
         eig = max(eig, float(np.abs(np.asarray(a.en) - np.asarray(b.en)).max()) / scale)
         ta, tb = np.asarray(a.thermo, dtype=float).ravel(), np.asarray(b.thermo, dtype=float).ravel()
@@ -156,43 +211,65 @@ def sweep_errors(gpu, ref) -> dict:
             r = np.abs(oa - ob) / np.maximum(np.abs(ob), 1e-300)
             opavg = max(opavg, float(r.max()))
             nd = max(nd, float(r[0]))
-    return {"eigenvalues_rel_max": eig, "n_d_rel_max": nd, "T_chi_rel_max": tchi, "thermo_rel_max": thermo,
-            "opavg_rel_max": opavg, "iterations": min(len(gpu.iters), len(ref.iters))}
-
-
-# sum_b n_b^3 over the 50 iterations of the full workload, from the block
-# sizes the sweep produces (identical on CPU and GPU: the bookkeeping is exact).
-def full_sum_n3_from(result) -> float:
-    return sum_n3(result)
+    return {"eigenvalues_rel_max": eig, "ecut_rel_max": ecut, "n_d_rel_max": nd, "T_chi_rel_max": tchi,
+            "thermo_rel_max": thermo, "opavg_rel_max": opavg,
+            "bookkeeping_exact": bookkeeping_exact(gpu_iters, ref_iters),
+            "iterations": min(len(gpu_iters), len(ref_iters))}
 
 
 def run_reference_arm(args, rank: int):
+    """The reference's algorithm on the host cores: the oracle port over
+    iterations 0-3 of the workload (3 = the first at 3000 kept), measured
+    iteration by iteration once; `value` is the sweep total derived from those
+    measurements (labelled an estimate).  The reference's own binaries are
+    built from its sources in the build container only (the sources are not
+    on the GPU host, and x86 binaries do not run on its Arm cores); the
+    fixture made there records the reference's own per-iteration seconds on
+    one core, reported beside the port's."""
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    steps = []
-    for _ in range(args.warmup):
-        cpu_sample(cores)
-    for _ in range(args.steps):
-        steps.append(cpu_sample(cores))
-    dt = statistics.mean(s[0] for s in steps)
-    w_sample = steps[0][1]
-    w_full = FULL_SUM_N3
-    value = dt * w_full / w_sample
-    sample = (f"oracle port of the reference sweep (same model/parameters, 600 kept, 8 iterations) "
-              f"timed at {dt:.2f} s on {cores} threads, scaled by sum n^3 ratio {w_full / w_sample:.1f}")
+    wall, s = cpu_sample(cores)
+    per = [it.seconds for it in s.iters]
+    value = sweep_estimate(per, WORKLOAD["nsites"])
     line = {"metric": "2ch NRG sweep s", "value": value, "unit": "s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
+            "steps": 1, "warmup": 0, "ms_per_step": value * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD_NAME, "parallelism": "host threads over blocks"},
-            "cpu_baseline": {"value": value, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
+            "config": {"workload": WORKLOAD_NAME, "parallelism": f"host threads over blocks ({cores})"},
+            "estimate": {"value_is": "sweep total estimated from measured iterations: iterations 0-3 as "
+                                     "measured plus 46 more at the measured time of iteration 3 (the first "
+                                     "at 3000 kept)",
+                         "measured_iterations": list(range(len(per))), "measured_s": per,
+                         "timed_region_s": wall,
+                         "passes": "the sample runs once: --steps/--warmup would repeat ~minutes of CPU work"},
+            "cpu_baseline": {"value": value, "unit": "s", "cores": cores, "kind": "port",
+                             "sample": (f"oracle port, iterations 0-3 of the workload measured "
+                                        f"({', '.join(f'{x:.2f}' for x in per)} s; {wall:.1f} s in all), "
+                                        "sweep total estimated as above")},
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    cbs, cdt, cn = cpu_batch_sample(cores)
+    ref = reference_seconds()
+    if ref:
+        line["reference_one_core"] = ref
+    cbs, cdt, cn, _ = cpu_batch_sample(cores)
     line["batched"] = {"metric": "batched solves/s", "value": cbs, "unit": "solves/s",
                        "instances": cn, "seconds": cdt, "workload": BATCH_NAME,
                        "sample": f"oracle port on the first {cn} of {BATCH_INSTANCES} instances, one per thread"}
     print(json.dumps(line), flush=True)
+
+
+def reference_seconds():
+    """The reference's own per-iteration seconds (one core, build container)
+    recorded in the full-size fixture."""
+    try:
+        its = load_fixture(REF_FIXTURE)
+    except (OSError, KeyError):
+        return None
+    sec = [it.seconds for it in its if it.seconds is not None]
+    if not sec:
+        return None
+    return {"iterations": list(range(len(sec))), "seconds": sec,
+            "where": "reference routines (oracle/ref_harness), one core of the build container (x86)"}
 
 
 BATCH_INSTANCES = 256
@@ -212,10 +289,27 @@ def cpu_batch_sample(cores: int):
     orc.lib()
     t = time.perf_counter()
     with ThreadPoolExecutor(max_workers=cores) as ex:
-        list(ex.map(lambda c: orc.run(c["model"], c["nsites"], c["ncutoff"], c["lam"], c["U"], c["ed"],
-                                      c["gamma1"], c["gamma2_or_B"], nthreads=1), inst))
+        res = list(ex.map(lambda c: orc.run(c["model"], c["nsites"], c["ncutoff"], c["lam"], c["U"], c["ed"],
+                                            c["gamma1"], c["gamma2_or_B"], nthreads=1), inst))
     dt = time.perf_counter() - t
-    return len(inst) / dt, dt, len(inst)
+    return len(inst) / dt, dt, len(inst), res
+
+
+def batch_errors(gpu, refs) -> dict:
+    """Errors of the GPU batch against the oracle on the instances the CPU
+    sample ran: <n_d> and T chi (CalcSuscep at the four temperatures of each
+    iteration) relative, and the kept counts."""
+    import numpy as np
+    nd = tchi = 0.0
+    nk_ok = True
+    for i, o in enumerate(refs):
+        for n, it in enumerate(o.iters):
+            nk_ok &= int(gpu.nkept[i, n]) == it.nkept
+            a, b = gpu.thermo[i, n][:, 2], np.asarray(it.thermo)[:, 2]
+            tchi = max(tchi, float((np.abs(a - b) / np.maximum(np.abs(b), 1e-300)).max()))
+            nd = max(nd, abs(float(gpu.opavg[i, n, 0]) - it.opavg[0]) / max(abs(it.opavg[0]), 1e-300))
+    return {"n_d_rel_max": nd, "T_chi_rel_max": tchi, "nkept_exact": bool(nk_ok), "instances": len(refs),
+            "iterations": 40}
 
 
 DM_WORKLOAD = dict(nsites=40, ncutoff=500, lam=2.5, U=0.5, ed=-0.25, gamma=0.02)
@@ -305,13 +399,7 @@ def gpu_batch(workers: int, device: int):
     inst = batched_qsz(BATCH_INSTANCES, seed=BATCH_SEED)
     tg.sweep_batch(inst[:workers], nworkers=workers, device=device)  # warm-up
     res = tg.sweep_batch(inst, nworkers=workers, device=device)
-    return BATCH_INSTANCES / res.seconds, res.seconds
-
-
-# Fixed by the workload: sum over the 50 iterations of n_b^3 for the block
-# structure the sweep produces (the bookkeeping is exact, so CPU and GPU agree;
-# the GPU arm reports the value it measured as "sum_n3").
-FULL_SUM_N3 = 1.6993633731293001e13
+    return BATCH_INSTANCES / res.seconds, res.seconds, res
 
 
 def main():
@@ -325,6 +413,8 @@ def main():
     ap.add_argument("--dm2ch", action="store_true",
                     help="only the two-channel DM-NRG spectral function (about 8 minutes and 190 GB at 3000 kept)")
     ap.add_argument("--dm2ch-ncutoff", type=int, default=DM2_WORKLOAD["ncutoff"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+                    help="arithmetic of the timed sweeps (the other form is timed once after them)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
@@ -337,12 +427,15 @@ def main():
     if ws > 1:
         import torch.distributed as dist  # replicas only: used for barriers and the max over ranks
         dist.init_process_group("gloo")
+    import numpy as np
     import twochnrg_gb300 as tg
     eng = tg.Engine(local)
     W = dict(WORKLOAD)
+    prec = tg.PREC_MIXED if args.precision == "mixed" else tg.PREC_FP64
+    other = tg.PREC_FP64 if prec == tg.PREC_MIXED else tg.PREC_MIXED
     warm = dict(W, nsites=WARMUP_NSITES)
     for _ in range(args.warmup):
-        eng.sweep(**warm, fetch=False)
+        eng.sweep(**warm, fetch=False, precision=prec)
     peak = eng.fp64_peak()
     if dist:
         dist.barrier()
@@ -353,7 +446,7 @@ def main():
     res = None
     for _ in range(args.steps):
         t = time.perf_counter()
-        res = eng.sweep(**W, fetch=True)
+        res = eng.sweep(**W, fetch=True, precision=prec)
         wall.append(time.perf_counter() - t)
         dev_ms.append(res.timing["device_ms"])
         tim.append(res.timing)
@@ -368,22 +461,27 @@ def main():
     tri_ms = T["tridiag_ms"]
     achieved = T["tridiag_flops"] / (tri_ms * 1e-3) / 1e12
     traffic = None
-    if T["tridiag_launches"]:
+    if T["tridiag_launches"] and prec == tg.PREC_FP64:
         traffic = TRIDIAG_DRAM_BYTES_PER_ELEMENT * sum_n2(res) / T["tridiag_launches"]
     w_full = sum_n3(res)
+    names = {tg.PREC_MIXED: "mixed", tg.PREC_FP64: "fp64"}
     line = {
         "metric": "2ch NRG sweep s", "value": value, "unit": "s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
-        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64+bf16 (split-BF16 tensor-core products, FP64 elsewhere)" if prec == tg.PREC_MIXED else "f64",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD_NAME, "parallelism": f"replicas x{args.gpus}",
+        "config": {"workload": WORKLOAD_NAME, "precision": names[prec], "parallelism": f"replicas x{args.gpus}",
                    "l2": "working set (H_N blocks ~0.8 GB per iteration) larger than L2; no flush",
                    "warmup_step": f"first {WARMUP_NSITES} iterations of the same workload"},
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(T["h2d_bytes"]),
                 "d2h_bytes_per_step": int(T["d2h_bytes"])},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "fp64", "kernel": "tridiag (Householder, FP64)", "achieved": achieved,
-                     "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+        "roofline": {"bound": "fp64", "kernel": ("Householder reduction, blocked: FP64 panels + tensor-core "
+                                                 "trailing products" if prec == tg.PREC_MIXED else
+                                                 "Householder reduction (FP64)"),
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "traffic": traffic,
                      "peak_source": "measured by bench.py: DFMA register loop on all SMs (FP64 has no "
                                     "entry in MEASURED_PEAKS.json)",
                      "algorithmic": "4/3 sum_b n_b^3 flops per iteration"},
@@ -391,9 +489,34 @@ def main():
         "phases_ms": {k: T[k] for k in ("assemble_ms", "tridiag_ms", "tridiag_eig_ms", "vectors_ms",
                                           "backtransform_ms", "cut_ms", "update_ms")},
         "sum_n3": w_full,
+        "gpu_iteration_ms": [round(it.device_ms, 3) for it in res.iters],
     }
+    # the other arithmetic, once, and the two forms against each other
+    r2 = eng.sweep(**W, fetch=True, precision=other)
+    line[names[other]] = {"value": r2.timing["device_ms"] / 1e3, "unit": "s",
+                          "e2e_s": r2.timing["total_ms"] / 1e3,
+                          "phases_ms": {k: r2.timing[k] for k in ("tridiag_ms", "tridiag_eig_ms", "vectors_ms",
+                                                                  "backtransform_ms", "update_ms")}}
+    mixed_s = value if prec == tg.PREC_MIXED else r2.timing["device_ms"] / 1e3
+    fp64_s = value if prec == tg.PREC_FP64 else r2.timing["device_ms"] / 1e3
+    line["mixed_vs_fp64"] = {"speedup": fp64_s / mixed_s, "mixed_s": mixed_s, "fp64_s": fp64_s}
+    rm, rf = (res, r2) if prec == tg.PREC_MIXED else (r2, res)
+    line["accuracy"] = {"mixed_vs_fp64_sweep": dict(sweep_errors(rm.iters, rf.iters),
+                                                    sample="whole 50-iteration sweep, mixed against FP64 GPU")}
+    # both forms against the reference's own outputs at 3000 kept
+    try:
+        ref_its = load_fixture(REF_FIXTURE)
+    except OSError:
+        ref_its = None
+    if ref_its:
+        for p, nm in ((tg.PREC_FP64, "fp64"), (tg.PREC_MIXED, "mixed")):
+            g = eng.sweep(**dict(W, nsites=len(ref_its)), fetch=True, precision=p)
+            line["accuracy"][f"sweep_full_{nm}"] = dict(
+                sweep_errors(g.iters, ref_its),
+                sample=f"iterations 0-{len(ref_its) - 1} of the workload at 3000 kept, GPU against the "
+                       "reference's own routines (fixture tests/golden/cfg1_2chQS_n5_k3000.npz)")
     # second half of the metric: batched independent solves per second
-    bs, bsec = gpu_batch(args.batch_workers, local)
+    bs, bsec, bres = gpu_batch(args.batch_workers, local)
     line["batched"] = {"metric": "batched solves/s", "value": bs * (ws if dist else 1), "unit": "solves/s",
                        "instances": BATCH_INSTANCES, "seconds": bsec, "workers": args.batch_workers,
                        "workload": BATCH_NAME, "timing": "host wall time of nrg_sweep_batch"}
@@ -407,21 +530,33 @@ def main():
         "lehmann_bound": "fp64 (one exp per nonzero Lehmann record and frequency)"}
     if not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
-        dt, w_s, ref = cpu_sample(cores, want_result=True)
+        cwall, cs = cpu_sample(cores)
+        per = [it.seconds for it in cs.iters]
+        est = sweep_estimate(per, W["nsites"])
+        gpu_first = [it.device_ms / 1e3 for it in res.iters[:len(per)]]
         line["cpu_baseline"] = {
-            "value": dt * w_full / w_s, "unit": "s", "cores": cores, "kind": "port",
-            "sample": (f"oracle port, same model/parameters with 600 kept and 8 iterations: {dt:.2f} s on "
-                       f"{cores} threads, scaled by the sum n^3 ratio {w_full / w_s:.1f}")}
-        # The GPU sweep against the FP64 oracle on that sample.
-        C = CPU_SAMPLE
-        gs = eng.sweep(C["model"], C["nsites"], C["ncutoff"], C["lam"], C["U"], C["ed"], C["gamma1"],
-                      C["gamma2_or_B"])
-        line["accuracy"] = {"sweep": dict(sweep_errors(gs, ref), sample=(
-            "two-channel sweep, same model/parameters, 600 kept, 8 iterations, GPU against the FP64 oracle"))}
-        cbs, cdt, cn = cpu_batch_sample(cores)
+            "value": est, "unit": "s", "cores": cores, "kind": "port",
+            "estimate": True,
+            "sample": (f"oracle port on iterations 0-{len(per) - 1} of the workload (iteration 3: the first at "
+                       f"3000 kept), measured per iteration: {', '.join(f'{x:.2f}' for x in per)} s; sweep total "
+                       f"estimated as those plus {W['nsites'] - len(per)} iterations at iteration 3's time"),
+            "measured_s": per, "timed_region_s": cwall,
+            "gpu_same_iterations_s": gpu_first,
+            "measured_ratio_same_iterations": sum(per) / max(sum(gpu_first), 1e-12),
+            "measured_ratio_full_size_iteration": per[-1] / max(gpu_first[-1], 1e-12)}
+        ref = reference_seconds()
+        if ref:
+            line["cpu_baseline"]["reference_one_core"] = ref
+        # the port's sample against the GPU on the same iterations (both forms above)
+        line["accuracy"]["port_vs_gpu_first_iterations"] = dict(
+            sweep_errors(res.iters[:len(cs.iters)], cs.iters),
+            sample=f"iterations 0-{len(per) - 1} at 3000 kept, GPU ({names[prec]}) against the oracle port")
+        cbs, cdt, cn, crefs = cpu_batch_sample(cores)
         line["batched"]["cpu_baseline"] = {
             "value": cbs, "unit": "solves/s", "cores": cores, "kind": "port",
             "sample": f"oracle port on the first {cn} instances, one per thread: {cdt:.2f} s"}
+        line["batched"]["accuracy"] = dict(batch_errors(bres, crefs),
+                                           sample=f"the first {cn} instances, GPU batch against the oracle")
         # DM-NRG: GPU and the oracle port on the same reduced case (the port
         # evaluates every frequency with dense products, as DM_NRG does)
         from oracle import oracle as orc
@@ -431,9 +566,8 @@ def main():
                                DM_SAMPLE["ed"], DM_SAMPLE["gamma"], DM_TEMP, DM_BROAD,
                                omegas=dm_omegas(DM_SAMPLE_NOMEGA))
         cdm = (time.perf_counter() - t) * 1e3
-        import numpy as np
         A_gpu, A_ref = np.asarray(g[6]), np.asarray(o_dm[1])
-        line.setdefault("accuracy", {})["dm_spectral"] = {
+        line["accuracy"]["dm_spectral"] = {
             "A_rel_max": float((np.abs(A_gpu - A_ref) / np.maximum(np.abs(A_ref), 1e-300)).max()),
             "A_abs_max_over_max_A": float(np.abs(A_gpu - A_ref).max() / np.abs(A_ref).max()),
             "sample": (f"one-channel DM-NRG, {DM_SAMPLE['nsites']} iterations, {DM_SAMPLE['ncutoff']} kept, "

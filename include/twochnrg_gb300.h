@@ -69,7 +69,12 @@ typedef enum {
 
 /* Arithmetic of the dense steps. */
 typedef enum {
-  NRG_PREC_FP64 = 0      /* plain FP64 everywhere */
+  NRG_PREC_FP64 = 0,     /* plain FP64 everywhere */
+  NRG_PREC_MIXED = 1     /* the large blocks' Householder reduction blocked by panels of 32
+                            columns, its trailing rank-64 updates as split-BF16 products on the
+                            tensor cores (6 slices, FP32 accumulation, FP64 recombination;
+                            error of order 2^-36 of the operands' magnitudes); everything
+                            else FP64 */
 } nrg_precision;
 
 typedef struct nrg_ctx nrg_ctx;
@@ -108,6 +113,8 @@ typedef struct {
   const double* opavg;     /* [nops] CalcOpAvg of the averaged operators at betabar */
   const double* params;    /* [4] ParamsHN used: Lambda, chi_1, chi_2 (0 if 1ch; Delta_N for
                               NRG_MODEL_1CH_S), eN */
+  double wall_ms;          /* host wall time of the iteration (table building, copies, kernels) */
+  double device_ms;        /* CUDA-event span of the iteration on the engine stream */
 } nrg_iteration;
 
 /* Phase timing of the last sweep (device time from CUDA events). */
@@ -169,6 +176,21 @@ nrg_status nrg_sweep_batch(int device, int ninst, const nrg_sweep_config* cfgs, 
 /* Measured FP64 FMA throughput of the device (TFLOP/s), from a register-only
  * DFMA loop over all SMs: the roofline denominator of the FP64 kernels. */
 nrg_status nrg_fp64_peak(nrg_ctx* ctx, double* tflops);
+
+/* FP64-accurate product on the tcgen05 tensor cores, the building block of
+ * the mixed-precision form: C (m x n) += alpha * A (m x k) * B (n x k)^T, all
+ * row-major FP64 DEVICE pointers with leading dimensions lda, ldb, ldc.  Each
+ * row of A and B is cut into `slices` BF16 fixed-point slices of 8 bits under
+ * a power-of-two row scale; the slice products accumulate in FP32 in tensor
+ * memory, without rounding for the three leading levels, and are summed in
+ * FP64.  The error is of order 2^-35 sqrt(k/64) |A_i| |B_j| per element with
+ * slices = 5 and 2^-36 with 6 (|A_i|: largest magnitude in row i).  The
+ * reference's dense products it stands for are the cblas_dgemm calls of
+ * UpdateMatrices (src/UpdateMatrices.cpp:481-494) and the Householder
+ * trailing updates inside dspev (src/NRGmatrixClass.cpp:645).  k <= 256,
+ * 1 <= slices <= 6; returns after the product is complete. */
+nrg_status nrg_gemm_f64_tensor(nrg_ctx* ctx, int m, int n, int k, double alpha, const double* A, int64_t lda,
+                               const double* B, int64_t ldb, double* C, int64_t ldc, int slices);
 
 /* ---- drop-in replacements --------------------------------------------- */
 

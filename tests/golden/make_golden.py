@@ -44,6 +44,13 @@ CASES = {
     "s_1chS_n12_k200": ("1chS", 12, 200, 2.5, 0.5, -0.25, 0.02, 0.0, 0.01),
     "sz_1chSz_n12_k200": ("1chSz", 12, 200, 2.5, 0.5, -0.25, 0.02, 1.0e-3, 0.01),
 }
+# The headline two-channel workload at its full kept count, first iterations
+# only (iteration 3 is the first at 3000 kept; each takes the reference
+# about ten minutes on one core).  Generated only when named on the command
+# line: python tests/golden/make_golden.py cfg1_2chQS_n5_k3000
+SLOW_CASES = {
+    "cfg1_2chQS_n5_k3000": ("2chQS", 5, 3000, 2.5, 0.3, -0.15, 0.01, 0.01),
+}
 
 
 def parse(text: str) -> dict:
@@ -76,6 +83,8 @@ def parse(text: str) -> dict:
             cur["opavg"] = [float(x) for x in t[3::2]]
         elif t[0] == "KEPTBLK":
             cur["kept_bsize"] = [int(x) for x in t[2:]]
+        elif t[0] == "TIME":
+            cur["seconds"] = float(t[2])
     out = {"opnames": np.array(names), "opavg_m1": np.array(opm1), "niters": len(it)}
     for n, c in enumerate(it):
         out[f"params_{n}"] = np.array(c["params"])
@@ -87,6 +96,8 @@ def parse(text: str) -> dict:
         out[f"thermo_{n}"] = np.array(c["thermo"])
         out[f"opavg_{n}"] = np.array(c["opavg"])
         out[f"kept_bsize_{n}"] = np.array(c["kept_bsize"])
+        if "seconds" in c:  # wall time of the iteration, reference routines on one thread
+            out[f"seconds_{n}"] = np.array(c["seconds"])
     return out
 
 
@@ -111,8 +122,8 @@ def main() -> None:
         sys.exit("build the reference first: bash oracle/build_ref.sh")
     np.savez_compressed(os.path.join(HERE, "run1_log.npz"), **run1_log())
     only = sys.argv[1:]
-    for name, case in CASES.items():
-        if only and name not in only:
+    for name, case in {**CASES, **SLOW_CASES}.items():
+        if (only and name not in only) or (not only and name in SLOW_CASES):
             continue
         model, ns, nc, lam, U, ed, g1, x = case[:8]
         args = [HARNESS, model, str(ns), str(nc), repr(lam), repr(U), repr(ed), repr(g1), repr(x)]

@@ -38,3 +38,29 @@ def test_batch_of_mixed_models():
         for n, it in enumerate(o.iters):
             assert res.nkept[i, n] == it.nkept
             np.testing.assert_allclose(res.thermo[i, n], it.thermo, rtol=1e-8, atol=1e-14)
+
+
+def test_batch_full_size_instances():
+    """Four instances of the batched workload itself (seed 2024: 40 iterations,
+    kept counts drawn from 200..1000), including its largest kept count, against
+    the oracle on host threads: kept counts exact; <n_d>, <S_z> and T chi (with
+    the CalcSuscep quirk of the reference, <S_z^2> without <S_z>^2) 1e-8."""
+    from concurrent.futures import ThreadPoolExecutor
+    allinst = batched_qsz(256, seed=2024)
+    pick = sorted(range(256), key=lambda i: allinst[i]["ncutoff"])
+    idx = [pick[0], pick[85], pick[170], pick[255]]
+    inst = [allinst[i] for i in idx]
+    res = tg.sweep_batch(inst, nworkers=4)
+
+    def oracle(c):
+        return orc.run(c["model"], c["nsites"], c["ncutoff"], c["lam"], c["U"], c["ed"], c["gamma1"],
+                       c["gamma2_or_B"], nthreads=2)
+
+    with ThreadPoolExecutor(max_workers=4) as ex:
+        refs = list(ex.map(oracle, inst))
+    for i, o in enumerate(refs):
+        assert len(o.iters) == 40
+        for n, it in enumerate(o.iters):
+            assert res.nkept[i, n] == it.nkept, f"instance {idx[i]} N={n}"
+            np.testing.assert_allclose(res.thermo[i, n], it.thermo, rtol=1e-8, atol=1e-14)
+            np.testing.assert_allclose(res.opavg[i, n, :len(it.opavg)], it.opavg, rtol=1e-8, atol=1e-12)

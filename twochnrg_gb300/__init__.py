@@ -23,6 +23,7 @@ MODEL_1CH_QS, MODEL_1CH_QSZ, MODEL_2CH_QS, MODEL_1CH_Q, MODEL_1CH_S, MODEL_1CH_S
 MODELS = {"1chQS": MODEL_1CH_QS, "1chQSz": MODEL_1CH_QSZ, "2chQS": MODEL_2CH_QS, "1chQ": MODEL_1CH_Q,
           "1chS": MODEL_1CH_S, "1chSz": MODEL_1CH_SZ}
 PREC_FP64 = 0
+PREC_MIXED = 1  # blocked reduction of the large blocks with tensor-core trailing products
 
 STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "out of memory", 4: "not converged",
           5: "size limit exceeded", 6: "block structures out of sync", 7: "device wait timed out",
@@ -49,7 +50,8 @@ class _Iteration(ctypes.Structure):
                 ("ecut", ctypes.c_double), ("nkept", ctypes.c_int), ("nkept_blocks", ctypes.c_int),
                 ("kept_block_size", ctypes.POINTER(ctypes.c_int)),
                 ("thermo", ctypes.POINTER(ctypes.c_double)), ("nops", ctypes.c_int),
-                ("opavg", ctypes.POINTER(ctypes.c_double)), ("params", ctypes.POINTER(ctypes.c_double))]
+                ("opavg", ctypes.POINTER(ctypes.c_double)), ("params", ctypes.POINTER(ctypes.c_double)),
+                ("wall_ms", ctypes.c_double), ("device_ms", ctypes.c_double)]
 
 
 class Timing(ctypes.Structure):
@@ -285,6 +287,12 @@ def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     _dp = ctypes.POINTER(ctypes.c_double)
     _ip = ctypes.POINTER(ctypes.c_int)
     L.nrg_diag_blocks.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp, _dp, _dp]
+    L.nrg_gemm_f64_tensor.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                      ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                      ctypes.c_void_p, ctypes.c_int64, ctypes.c_int]
+    L.cudaMalloc.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]
+    L.cudaFree.argtypes = [ctypes.c_void_p]
+    L.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
     L.nrg_diag_hn.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_int, ctypes.POINTER(_Blocks),
                               ctypes.c_int, ctypes.POINTER(_Matrix), ctypes.POINTER(_Basis), _dp, _dp, _dp]
     L.nrg_cut_states.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Blocks), _dp, _dp, ctypes.c_int,
@@ -323,6 +331,8 @@ class Iteration:
     thermo: np.ndarray
     opavg: np.ndarray
     kept_bsize: np.ndarray
+    wall_ms: float = 0.0     # host wall time of the iteration
+    device_ms: float = 0.0   # CUDA-event span of the iteration on the engine stream
 
 
 @dataclass
@@ -367,6 +377,34 @@ class Engine:
     @property
     def kernel_count(self) -> int:
         return int(self.L.nrg_kernel_count(self.h))
+
+    def gemm_f64_tensor(self, A, B, C, alpha: float = 1.0, slices: int = 6):
+        """C + alpha A B^T through nrg_gemm_f64_tensor (split-BF16 products on
+        the tensor cores); A (m, k), B (n, k), C (m, n) host arrays, copied to
+        and from device buffers allocated for the call.  Returns the new C."""
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        B = np.ascontiguousarray(B, dtype=np.float64)
+        C = np.array(C, dtype=np.float64, order="C", copy=True)
+        m, k = A.shape
+        n = B.shape[0]
+        L = self.L
+        bufs = []
+        try:
+            for arr in (A, B, C):
+                p = ctypes.c_void_p()
+                if L.cudaMalloc(ctypes.byref(p), max(arr.nbytes, 8)) != 0:
+                    raise NRGError(3, "cudaMalloc failed")
+                bufs.append(p)
+                if L.cudaMemcpy(p, arr.ctypes.data, arr.nbytes, 1) != 0:
+                    raise NRGError(2, "cudaMemcpy failed")
+            self._check(L.nrg_gemm_f64_tensor(self.h, m, n, k, float(alpha), bufs[0], k, bufs[1], k, bufs[2], n,
+                                              int(slices)))
+            if L.cudaMemcpy(C.ctypes.data, bufs[2], C.nbytes, 2) != 0:
+                raise NRGError(2, "cudaMemcpy failed")
+        finally:
+            for p in bufs:
+                L.cudaFree(p)
+        return C
 
     def diag_blocks(self, sizes, packed_upper):
         """DiagBlock for a batch of blocks in the reference's packed-upper
@@ -599,7 +637,8 @@ class Engine:
                 emin=it.emin, ecut=it.ecut, nkept=it.nkept,
                 thermo=_arr(it.thermo, 16, np.float64).reshape(4, 4),
                 opavg=_arr(it.opavg, it.nops, np.float64),
-                kept_bsize=_arr(it.kept_block_size, it.nkept_blocks, np.int64)))
+                kept_bsize=_arr(it.kept_block_size, it.nkept_blocks, np.int64),
+                wall_ms=it.wall_ms, device_ms=it.device_ms))
         return out
 
 

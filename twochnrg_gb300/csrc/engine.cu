@@ -111,6 +111,7 @@ struct IterResult {
   std::vector<int> bsize, kept_bsize;
   double emin = 0, ecut = 0;
   int nkept = 0;
+  double wall_ms = 0, device_ms = 0;  // host wall time and CUDA-event span of the iteration
 };
 
 }  // namespace nrg
@@ -129,6 +130,7 @@ struct nrg_ctx {
   nrg::DevBuf meta, vmeta, H, d, e, tau, ev, en, flag, scal, Y, scratch, Z, Zt, T, partial, red, gpart, fde, e2, spl;
   nrg::DevBuf ops_a[6], ops_b[6], opptr;
   nrg::DevBuf dmcnt, dmrec, dmtab;     // Lehmann record counts / offsets, records, frequency tables
+  nrg::DevBuf ozw;                     // split-BF16 slices and row scales of the tensor-core products
   cudaEvent_t ev_a[8];
   // concurrent whole-GPU tridiagonalizations: side streams, fork/join events,
   // per-stream scratch and the block lists
@@ -136,6 +138,10 @@ struct nrg_ctx {
   cudaStream_t aux[kMaxSplit] = {};
   cudaEvent_t fork = nullptr, join[kMaxSplit] = {};
   nrg::DevBuf gpart_k[kMaxSplit], gbig;
+  // mixed precision: per concurrent grid the blocked reduction's [V W], column
+  // and share scratch, and the tensor-core product's slices
+  nrg::DevBuf pvw[kMaxSplit], pcol[kMaxSplit], ppart[kMaxSplit], ozk[kMaxSplit];
+  int precision = NRG_PREC_FP64;
   // drop-in outputs (host, valid until the next call on the context)
   std::vector<double> out_en, out_qn, out_cut_en, out_vec, out_el;
   std::vector<unsigned char> out_kept, out_cut_kept;
@@ -233,6 +239,7 @@ void check_flag(nrg_ctx* c) {
   if (f & DEV_DEGEN_OVERFLOW) throw NrgError(NRG_ERR_SIZE, "too many near-degenerate levels for SetDegen");
   if (f & DEV_BAD_INPUT) throw NrgError(NRG_ERR_ARG, "non-finite value met in an eigenvalue solve");
   if (f & DEV_NOT_CONVERGED) throw NrgError(NRG_ERR_NOT_CONVERGED, "inverse iteration did not converge");
+  if (f & DEV_TIMEOUT) throw NrgError(NRG_ERR_TIMEOUT, "a tensor-core kernel's bounded wait gave up");
 }
 
 // ------------------------------------------------------------------ eigensolve
@@ -290,6 +297,13 @@ int big_block_threshold() {
 // each overlap those latencies.  Four grids of 38 SMs with blocks from 1800
 // states on measured fastest on the two-channel workload (1 to 8 grids and
 // thresholds 1500 to 3200 tried).
+// Mixed precision: blocks at least this large take the blocked reduction
+// with the tensor-core trailing product.
+int mixed_block_threshold() {
+  const char* s = std::getenv("NRG_MIXED_N");
+  return s ? std::atoi(s) : 1800;
+}
+
 int grid_split(int nbig) {
   const char* s = std::getenv("NRG_GRID_SPLIT");
   int k = s ? std::atoi(s) : 4;
@@ -306,13 +320,65 @@ int grid_split(int nbig) {
 // not held up.
 std::mutex g_coop_mu;
 
+// Panel width of the blocked reduction (mixed precision): the trailing
+// product has K = 2 nb.
+constexpr int kPanelNb = 32;
+constexpr int kOzSlices = 6;
+
+// Mixed precision: the large blocks of `blocks` tridiagonalized one after
+// the other on stream `s` by the blocked reduction, each panel of kPanelNb
+// columns on a cooperative grid of G CTAs (k_panel.cu) followed by the
+// trailing rank-2 kPanelNb update H[k1:, k1:] -= [V W] [W V]^T as an
+// FP64-accurate split-BF16 product on the tensor cores (k_ozaki.cu), limited
+// to G CTAs so that concurrent grids share the GPU evenly.
+void blocked_reduction(nrg_ctx* c, const EigPlan& P, const std::vector<int>& blocks, int slot, int G,
+                       cudaStream_t s) {
+  const int nb = kPanelNb, ld = 2 * kPanelNb;
+  int maxn = 3;
+  for (int b : blocks) maxn = std::max(maxn, P.bsize[b]);
+  c->pvw[slot].ensure(sizeof(double) * (size_t)maxn * ld);
+  c->pcol[slot].ensure(sizeof(double) * (2 * (size_t)maxn + 2 + (size_t)G * (ld + 2)));
+  c->ozk[slot].ensure(oz_work_bytes(maxn, maxn, ld, kOzSlices));
+  double* VW = c->pvw[slot].as<double>();
+  double* col = c->pcol[slot].as<double>();
+  double* ybuf = col + 2 * (size_t)maxn;
+  double* part = ybuf + 2;
+  for (int b : blocks) {
+    const int n = P.bsize[b];
+    double* H = c->H.as<double>() + P.hoff[b];
+    const int so = P.soff[b];
+    if (n < 3) throw NrgError(NRG_ERR_SIZE, "blocked reduction needs n >= 3");
+    if (panel_smem_bytes(n, 0, nb, G) > (size_t)max_dyn_smem())
+      throw NrgError(NRG_ERR_SIZE, "blocked reduction: block too large for shared memory");
+    for (int k0 = 0; k0 < n - 2; k0 += nb) {
+      const int k1 = std::min(k0 + nb, n - 2);
+      const bool last = k1 == n - 2;
+      CU(cudaMemsetAsync(VW, 0, sizeof(double) * (size_t)n * ld, s));
+      PanelArgs pa{};
+      pa.H = H; pa.n = n; pa.k0 = k0; pa.k1 = k1; pa.nb = nb; pa.last = last ? 1 : 0;
+      pa.d = c->d.as<double>() + so; pa.e = c->e.as<double>() + so; pa.tau = c->tau.as<double>() + so;
+      pa.VW = VW; pa.col = col; pa.part = part; pa.ybuf = ybuf;
+      CU(launch_panel(pa, G, s));
+      c->launches++; c->timing.tridiag_launches++;
+      if (last) break;
+      OzGemm g{};
+      g.C = H + (size_t)k1 * n + k1; g.ldc = n; g.m = n - k1; g.n = n - k1; g.K = ld; g.S = kOzSlices;
+      g.alpha = -1.0; g.A = VW + (size_t)k1 * ld; g.lda = ld; g.B = g.A; g.ldb = ld; g.b_swap = true;
+      g.work = c->ozk[slot].p; g.flag = c->flag.as<int>(); g.max_ctas = G;
+      CU(oz_gemm(g, s));
+      c->launches += 3;
+    }
+  }
+}
+
 // `order`: all blocks, largest first (host copy `order_h`); the big blocks
 // form its prefix.
 void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::vector<int>& order_h,
                             const int* d_order, const int* d_bsize, const int64_t* d_hoff, const int* d_soff,
                             const int* d_state_block) {
   const int nb = (int)P.bsize.size();
-  const int thr = big_block_threshold();
+  const bool mixed = c->precision == NRG_PREC_MIXED;
+  const int thr = mixed ? mixed_block_threshold() : big_block_threshold();
   int nbig = 0;
   while (nbig < nb && P.bsize[order_h[nbig]] >= thr) ++nbig;
   CU(cudaMemsetAsync(c->red.p, 0, sizeof(int), c->stream));
@@ -343,7 +409,25 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
       if (!c->join[k]) CU(cudaEventCreateWithFlags(&c->join[k], cudaEventDisableTiming));
   }
   cudaEvent_t t0 = tm.start();
-  if (K == 1) {
+  if (mixed && K >= 1) {
+    const int G = panel_max_grid();
+    if (G <= 0) throw NrgError(NRG_ERR_SIZE, "blocked tridiagonalization does not fit");
+    if (K == 1) {
+      std::vector<int> all(order_h.begin(), order_h.begin() + nbig);
+      blocked_reduction(c, P, all, 0, G, c->stream);
+      CU(cudaEventRecord(c->join[0], c->stream));
+    } else {
+      const int Gk = G / K;
+      if (!c->fork) CU(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
+      CU(cudaEventRecord(c->fork, c->stream));
+      for (int k = 0; k < K; ++k) {
+        if (!c->aux[k]) CU(cudaStreamCreateWithFlags(&c->aux[k], cudaStreamNonBlocking));
+        CU(cudaStreamWaitEvent(c->aux[k], c->fork, 0));
+        blocked_reduction(c, P, bins[k], k, Gk, c->aux[k]);
+        CU(cudaEventRecord(c->join[k], c->aux[k]));
+      }
+    }
+  } else if (K == 1) {
     const int G = tridiag_grid_size(ta.maxn);
     if (G <= 0) throw NrgError(NRG_ERR_SIZE, "whole-GPU tridiagonalization does not fit");
     c->gpart.ensure(sizeof(double) * tridiag_grid_work(ta.maxn, G));
@@ -793,7 +877,9 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
   if (dm && cfg->model != NRG_MODEL_1CH_QS && cfg->model != NRG_MODEL_2CH_QS)
     throw NrgError(NRG_ERR_ARG, "DM-NRG shells are available for the |Q S> models (one and two channels)");
   if (cfg->nsites < 1 || cfg->ncutoff < 4 || !(cfg->lambda > 1.0)) throw NrgError(NRG_ERR_ARG, "bad sweep parameters");
-  if (cfg->precision != NRG_PREC_FP64) throw NrgError(NRG_ERR_ARG, "unsupported precision");
+  if (cfg->precision != NRG_PREC_FP64 && cfg->precision != NRG_PREC_MIXED)
+    throw NrgError(NRG_ERR_ARG, "unsupported precision");
+  c->precision = cfg->precision;
   c->iters.clear();
   c->opavg_m1.clear();
   std::memset(&c->timing, 0, sizeof(c->timing));
@@ -914,7 +1000,13 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
   // N = 0 and as ScaleFactor(N-1) * Delta_SC = Lambda^((N-1)/2) / HLF *
   // Delta_SC after that (NRG_main.cpp:220-227, 276, 414-419).
   const bool sc = m.kind == MODEL_1CHS || m.kind == MODEL_1CHSZ;
+  cudaEvent_t it0, it1;
+  CU(cudaEventCreate(&it0));
+  CU(cudaEventCreate(&it1));
+  EvGuard itg{it0, it1};
   for (int N = N0; N < cfg->nsites; ++N) {
+    const auto t_iter = clock::now();
+    CU(cudaEventRecord(it0, c->stream));
     IterResult R;
     eN = onsite(N);
     const double delta = !sc ? 0.0 : (N == 0 ? cfg->delta_sc
@@ -1085,6 +1177,12 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
     S.ops = newops;
     S.cur = nxt;
     for (int ich = 0; ich < m.nchan; ++ich) chi[ich] = hop(N);
+    CU(cudaEventRecord(it1, c->stream));
+    CU(cudaEventSynchronize(it1));
+    float it_ms = 0.f;
+    CU(cudaEventElapsedTime(&it_ms, it0, it1));
+    R.device_ms = it_ms;
+    R.wall_ms = std::chrono::duration<double, std::milli>(clock::now() - t_iter).count();
     c->iters.push_back(std::move(R));
   }
   CU(cudaEventRecord(span1, c->stream));
@@ -2229,6 +2327,8 @@ nrg_status nrg_sweep_iteration(const nrg_ctx* ctx, int n, nrg_iteration* out) {
   out->nops = (int)R.opavg.size();
   out->opavg = R.opavg.data();
   out->params = R.params.data();
+  out->wall_ms = R.wall_ms;
+  out->device_ms = R.device_ms;
   return NRG_OK;
 }
 
@@ -2242,6 +2342,31 @@ nrg_status nrg_sweep_opavg_initial(const nrg_ctx* ctx, int* nops, const double**
 nrg_status nrg_sweep_timing(const nrg_ctx* ctx, nrg_timing* out) {
   if (!ctx || !out) return NRG_ERR_ARG;
   *out = ctx->timing;
+  return NRG_OK;
+}
+
+nrg_status nrg_gemm_f64_tensor(nrg_ctx* ctx, int m, int n, int k, double alpha, const double* A, int64_t lda,
+                               const double* B, int64_t ldb, double* C, int64_t ldc, int slices) {
+  if (!ctx) return NRG_ERR_ARG;
+  ctx->err.clear();
+  if (m < 0 || n < 0 || k < 0 || k > nrg::kOzMaxK || slices < 1 || slices > nrg::kOzMaxSlices) return NRG_ERR_ARG;
+  if ((m > 0 && (!A || lda < k)) || (n > 0 && (!B || ldb < k)) || (m > 0 && n > 0 && (!C || ldc < n)))
+    return NRG_ERR_ARG;
+  if (m == 0 || n == 0 || k == 0) return NRG_OK;
+  GUARD(ctx, {
+    using namespace nrg;
+    CU(cudaSetDevice(ctx->device));
+    ctx->flag.ensure(sizeof(int) * 4);
+    CU(cudaMemsetAsync(ctx->flag.p, 0, sizeof(int), ctx->stream));
+    ctx->ozw.ensure(oz_work_bytes(m, n, k, slices));
+    OzGemm g{};
+    g.C = C; g.ldc = ldc; g.m = m; g.n = n; g.K = k; g.S = slices; g.alpha = alpha;
+    g.A = A; g.lda = lda; g.B = B; g.ldb = ldb; g.work = ctx->ozw.p; g.flag = ctx->flag.as<int>();
+    CU(oz_gemm(g, ctx->stream));
+    ctx->launches += 3;
+    CU(cudaStreamSynchronize(ctx->stream));
+    check_flag(ctx);
+  });
   return NRG_OK;
 }
 

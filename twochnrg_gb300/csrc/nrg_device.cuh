@@ -24,8 +24,55 @@ enum DeviceFlag : int {
   DEV_SIZE = 1,           // a block exceeded a compiled / shared-memory limit
   DEV_NOT_CONVERGED = 2,  // inverse iteration did not converge
   DEV_BAD_INPUT = 4,      // NaN / Inf met in an input
-  DEV_DEGEN_OVERFLOW = 8  // too many near-zero levels for the SetDegen pass
+  DEV_DEGEN_OVERFLOW = 8, // too many near-zero levels for the SetDegen pass
+  DEV_TIMEOUT = 16        // a bounded wait on an mbarrier gave up
 };
+
+// ---------------------------------------------------------------- tensor-core products
+// C[i][j] += alpha * sum_k A[i][k] B[j][k] (FP64 in and out) on the tcgen05
+// tensor cores from split-BF16 slices (k_ozaki.cu); error of order 2^-36
+// |A_i| |B_j| with S = 6.  work: oz_work_bytes(m, n, K, S) bytes of device
+// scratch.  a_swap / b_swap read the operand's column (k + K/2) mod K.
+constexpr int kOzMaxK = 256;
+constexpr int kOzMaxSlices = 6;
+struct OzGemm {
+  double* C;
+  int64_t ldc;
+  int m, n, K, S;
+  double alpha;
+  const double* A;
+  int64_t lda;
+  const double* B;
+  int64_t ldb;
+  bool a_swap, b_swap;
+  void* work;
+  int* flag;
+  int max_ctas;  // 0: one CTA per SM
+};
+size_t oz_work_bytes(int m, int n, int K, int S);
+
+// One panel of the blocked Householder reduction of a large block (k_panel.cu):
+// steps j in [k0, k1) against the matrix as it was at the panel's start,
+// writing [V W] (n x 2nb, zeroed by the caller beforehand) for the trailing
+// product H[k1:, k1:] -= [V W] [W V]^T; with `last` (k1 == n - 2) also the
+// closing 2 x 2 block.
+struct PanelArgs {
+  double* H;      // the block, n x n row-major
+  int n, k0, k1, nb;
+  int last;
+  double* d;      // at the block's state offset
+  double* e;
+  double* tau;
+  double* VW;     // n x 2nb
+  double* col;    // 2n scratch
+  double* part;   // grid x (2nb + 2) scratch
+  double* ybuf;   // 2 scratch
+};
+size_t panel_smem_bytes(int n, int k0, int nb, int grid);
+cudaError_t launch_panel(const PanelArgs& a, int grid, cudaStream_t s);
+int panel_max_grid();
+size_t oz_smem_bytes(int S);
+cudaError_t oz_gemm(const OzGemm& p, cudaStream_t s);
 
 // ---------------------------------------------------------------- assembly
 // One H_N block (dense n x n row-major at hoff) per new (Q,S)/(Q,Sz) sector.
