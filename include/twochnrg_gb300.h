@@ -192,6 +192,10 @@ nrg_status nrg_fp64_peak(nrg_ctx* ctx, double* tflops);
 nrg_status nrg_gemm_f64_tensor(nrg_ctx* ctx, int m, int n, int k, double alpha, const double* A, int64_t lda,
                                const double* B, int64_t ldb, double* C, int64_t ldc, int slices);
 
+/* Arithmetic (nrg_precision) of the drop-in calls nrg_diag_blocks and
+ * nrg_diag_hn on this context; a sweep sets it from its configuration. */
+nrg_status nrg_set_precision(nrg_ctx* ctx, int precision);
+
 /* ---- drop-in replacements --------------------------------------------- */
 
 /* CNRGmatrix::DiagBlock replacement for a batch of blocks

@@ -2,8 +2,8 @@
 blocked Householder panels with their trailing updates as split-BF16
 products on the tensor cores.
 
-The threshold of the blocked path is lowered through NRG_MIXED_N so that
-these small workloads run through it.  Tolerances of the mixed form, as the
+The thresholds of the large-block paths are lowered through NRG_BIG_N and
+NRG_MIXED_N so that these small workloads run through the blocked path.  Tolerances of the mixed form, as the
 metric states them: block eigenvalues 1e-9 relative to the largest level of
 the iteration; thermodynamics and operator averages 1e-8 relative; every
 integer of the block bookkeeping exact.  Observed errors are ~1e-13.
@@ -57,6 +57,8 @@ def compare(gpu, ref):
 
 @pytest.fixture
 def blocked_everywhere(monkeypatch):
+    # every block from 48 states on is a "large" block, and takes the blocked path
+    monkeypatch.setenv("NRG_BIG_N", "48")
     monkeypatch.setenv("NRG_MIXED_N", "48")
 
 

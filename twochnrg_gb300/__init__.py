@@ -287,6 +287,7 @@ def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     _dp = ctypes.POINTER(ctypes.c_double)
     _ip = ctypes.POINTER(ctypes.c_int)
     L.nrg_diag_blocks.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp, _dp, _dp]
+    L.nrg_set_precision.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.nrg_gemm_f64_tensor.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                       ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                                       ctypes.c_void_p, ctypes.c_int64, ctypes.c_int]
@@ -377,6 +378,11 @@ class Engine:
     @property
     def kernel_count(self) -> int:
         return int(self.L.nrg_kernel_count(self.h))
+
+    def set_precision(self, precision: int) -> None:
+        """Arithmetic of diag_blocks / diag_hn on this context (PREC_FP64 or
+        PREC_MIXED); a sweep sets it from its own argument."""
+        self._check(self.L.nrg_set_precision(self.h, int(precision)))
 
     def gemm_f64_tensor(self, A, B, C, alpha: float = 1.0, slices: int = 6):
         """C + alpha A B^T through nrg_gemm_f64_tensor (split-BF16 products on

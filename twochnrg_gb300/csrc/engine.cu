@@ -298,7 +298,8 @@ int big_block_threshold() {
 // states on measured fastest on the two-channel workload (1 to 8 grids and
 // thresholds 1500 to 3200 tried).
 // Mixed precision: blocks at least this large take the blocked reduction
-// with the tensor-core trailing product.
+// with the tensor-core trailing product (the other large blocks the FP64
+// whole-grid kernel, the small ones the cluster kernel).
 int mixed_block_threshold() {
   const char* s = std::getenv("NRG_MIXED_N");
   return s ? std::atoi(s) : 1800;
@@ -378,7 +379,7 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
                             const int* d_state_block) {
   const int nb = (int)P.bsize.size();
   const bool mixed = c->precision == NRG_PREC_MIXED;
-  const int thr = mixed ? mixed_block_threshold() : big_block_threshold();
+  const int thr = big_block_threshold();
   int nbig = 0;
   while (nbig < nb && P.bsize[order_h[nbig]] >= thr) ++nbig;
   CU(cudaMemsetAsync(c->red.p, 0, sizeof(int), c->stream));
@@ -410,22 +411,40 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
   }
   cudaEvent_t t0 = tm.start();
   if (mixed && K >= 1) {
+    // Mixed precision: blocks from the mixed threshold on take the blocked
+    // reduction (FP64 panels + tensor-core trailing products); the other
+    // large blocks the FP64 whole-grid kernel, on the same stream before them.
     const int G = panel_max_grid();
-    if (G <= 0) throw NrgError(NRG_ERR_SIZE, "blocked tridiagonalization does not fit");
-    if (K == 1) {
-      std::vector<int> all(order_h.begin(), order_h.begin() + nbig);
-      blocked_reduction(c, P, all, 0, G, c->stream);
-      CU(cudaEventRecord(c->join[0], c->stream));
-    } else {
-      const int Gk = G / K;
-      if (!c->fork) CU(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
-      CU(cudaEventRecord(c->fork, c->stream));
-      for (int k = 0; k < K; ++k) {
+    const int Gfp = tridiag_grid_size(ta.maxn);
+    if (G <= 0 || Gfp <= 0) throw NrgError(NRG_ERR_SIZE, "blocked tridiagonalization does not fit");
+    const int mthr = mixed_block_threshold();
+    if (K == 1) bins[0].assign(order_h.begin(), order_h.begin() + nbig);
+    if (!c->fork) CU(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
+    CU(cudaEventRecord(c->fork, c->stream));
+    Packer pk;
+    std::vector<std::vector<int>> fp(K), bl(K);
+    size_t o_fp[nrg_ctx::kMaxSplit] = {};
+    for (int k = 0; k < K; ++k) {
+      for (int b : bins[k]) (P.bsize[b] >= mthr ? bl[k] : fp[k]).push_back(b);
+      o_fp[k] = pk.add(fp[k]);
+    }
+    c->gbig.ensure(pk.host.size() + 256);
+    h2d(c, c->gbig.p, pk.host.data(), pk.host.size());
+    for (int k = 0; k < K; ++k) {
+      cudaStream_t sk = c->stream;
+      if (K > 1) {
         if (!c->aux[k]) CU(cudaStreamCreateWithFlags(&c->aux[k], cudaStreamNonBlocking));
-        CU(cudaStreamWaitEvent(c->aux[k], c->fork, 0));
-        blocked_reduction(c, P, bins[k], k, Gk, c->aux[k]);
-        CU(cudaEventRecord(c->join[k], c->aux[k]));
+        sk = c->aux[k];
+        CU(cudaStreamWaitEvent(sk, c->fork, 0));
       }
+      if (!fp[k].empty()) {
+        c->gpart_k[k].ensure(sizeof(double) * tridiag_grid_work(ta.maxn, Gfp / K));
+        CU(launch_tridiag_grid(ta, (const int*)(c->gbig.as<char>() + o_fp[k]), (int)fp[k].size(),
+                               c->gpart_k[k].as<double>(), Gfp / K, sk));
+        c->launches++; c->timing.tridiag_launches++;
+      }
+      if (!bl[k].empty()) blocked_reduction(c, P, bl[k], k, G / K, sk);
+      CU(cudaEventRecord(c->join[k], sk));
     }
   } else if (K == 1) {
     const int G = tridiag_grid_size(ta.maxn);
@@ -2342,6 +2361,12 @@ nrg_status nrg_sweep_opavg_initial(const nrg_ctx* ctx, int* nops, const double**
 nrg_status nrg_sweep_timing(const nrg_ctx* ctx, nrg_timing* out) {
   if (!ctx || !out) return NRG_ERR_ARG;
   *out = ctx->timing;
+  return NRG_OK;
+}
+
+nrg_status nrg_set_precision(nrg_ctx* ctx, int precision) {
+  if (!ctx || (precision != NRG_PREC_FP64 && precision != NRG_PREC_MIXED)) return NRG_ERR_ARG;
+  ctx->precision = precision;
   return NRG_OK;
 }
 

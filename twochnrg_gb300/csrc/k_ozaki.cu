@@ -13,7 +13,13 @@
 // (exact for K <= 256: at level 2, 3 pairs x 256 x 2^14 x 2^-16 < 2^24 x
 // 2^-16) and 3 <= s + t < S together (its magnitude is below 2^-2 of the
 // leading level's unit, so FP32 rounds it at about 2^-25 of that unit); the
-// epilogue adds them in FP64 and applies alpha and the row scales.  With
+// epilogue joins them without FP64 arithmetic -- the first three are exact
+// integers in units of 1, 2^-8 and 2^-16, the fourth is rounded to units of
+// 2^-24 (below its own FP32 rounding), and the four are combined in one int64
+// -- then makes one conversion to FP64, applies the column's power-of-two
+// scale in the exponent field and the row's scale and alpha in the single
+// FMA into C: two FP64 operations per element, where the FP64 pipe is the
+// scarce resource of this GPU.  With
 // S = 6 (21 BF16 products per element pair) the dropped levels (below
 // 2^-48) and the rounding of the fourth accumulator (about 2^-39 per
 // addition) leave an error of order 2^-36 sqrt(K/64) |A_i| |B_j|; with S = 5,
@@ -135,13 +141,13 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
 }
 
-// One warp per row: the row's power-of-two scale and its S slices.  Rows at
+// One warp per row: the row's power-of-two scale 2^ex (ex stored) and its S slices.  Rows at
 // or past `rows` (padding up to the slab height) and columns at or past K
 // (padding to whole 64-column chunks) are written as zeros.  swap_halves
 // reads column (k + K/2) mod K instead of k: [W V] from a stored [V W].
 __global__ void oz_split_kernel(const double* __restrict__ X, int64_t ldx, int rows, int K, int kpad, int slab,
                                 int S, int swap_halves, __nv_bfloat16* __restrict__ out,
-                                double* __restrict__ scale) {
+                                int* __restrict__ scale_exp) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= slab) return;
@@ -152,7 +158,7 @@ __global__ void oz_split_kernel(const double* __restrict__ X, int64_t ldx, int r
   for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   int ex = 0;
   if (mx > 0.0) frexp(mx, &ex);  // mx = f 2^ex, f in [0.5, 1): |x| / 2^ex <= 1
-  if (lane == 0 && r < rows) scale[r] = mx > 0.0 ? ldexp(1.0, ex) : 1.0;
+  if (lane == 0 && r < rows) scale_exp[r] = mx > 0.0 ? ex : 0;
   const int half = K / 2;
   for (int k = lane; k < kpad; k += 32) {
     double x = 0.0;
@@ -177,8 +183,8 @@ struct OzArgs {
   int S;             // slices per operand
   int slab_a, slab_b;  // rows per slice slab of the A and B slice arrays
   double alpha;
-  const double* sa;  // row scales of A and B
-  const double* sb;
+  const int* ea;     // row scale exponents of A and B (row i scaled by 2^ea[i])
+  const int* eb;
   int tiles_n;
   int ntiles;
   int* flag;
@@ -259,7 +265,8 @@ __global__ void __launch_bounds__(128, 1) oz_gemm_kernel(const __grid_constant__
     // Epilogue: thread (warp w, lane l) owns row 32w + l of the tile.
     const int row = ti * kTile + warp * 32 + lane;
     const bool row_ok = row < g.m;
-    const double ra = row_ok ? g.alpha * g.sa[row] * 0x1p-14 : 0.0;
+    // alpha 2^(ea - 14 - 24): the slices' 2^-7 per operand and the 2^-24 unit of the joined sum
+    const double ra = row_ok ? g.alpha * ldexp(1.0, g.ea[row] - 38) : 0.0;
     double* crow = g.C + (int64_t)(row_ok ? row : 0) * g.ldc;
     for (int c0 = 0; c0 < kTile; c0 += 16) {
       float a0[16], a1[16], a2[16], a3[16];
@@ -273,8 +280,19 @@ __global__ void __launch_bounds__(128, 1) oz_gemm_kernel(const __grid_constant__
       for (int q = 0; q < 16; ++q) {
         const int col = tj * kTile + c0 + q;
         if (col < g.n) {
-          const double v = ((double)a0[q] + (double)a1[q]) + ((double)a2[q] + (double)a3[q]);
-          crow[col] = fma(ra * g.sb[col], v, crow[col]);
+          // levels 0, 1, 2 exact in units of 1, 2^-8, 2^-16; level 3 and up to 2^-24
+          long long T = (long long)__float2int_rn(a0[q]);
+          T = (T << 8) + __float2int_rn(a1[q] * 256.0f);
+          T = (T << 8) + __float2int_rn(a2[q] * 65536.0f);
+          T = (T << 8) + __float2int_rn(a3[q] * 16777216.0f);  // |T| < 2^47: exact in FP64
+          double v = (double)T;
+          const int ec = g.eb[col];
+          const long long bits = __double_as_longlong(v);
+          const int ne = (int)((bits >> 52) & 0x7FF) + ec;
+          if (T == 0) v = 0.0;
+          else if (ne > 0 && ne < 2047) v = __longlong_as_double(bits + ((long long)ec << 52));
+          else v = ldexp(v, ec);
+          crow[col] = fma(ra, v, crow[col]);
         }
       }
     }
@@ -341,8 +359,8 @@ cudaError_t oz_gemm(const OzGemm& p, cudaStream_t s) {
   __nv_bfloat16* slb = sla + (size_t)p.S * slab_a * kpad;
   size_t sl_bytes = (size_t)p.S * ((size_t)slab_a + slab_b) * kpad * 2;
   sl_bytes = (sl_bytes + 255) & ~size_t(255);
-  double* sca = reinterpret_cast<double*>(w + sl_bytes);
-  double* scb = sca + slab_a;
+  int* sca = reinterpret_cast<int*>(w + sl_bytes);
+  int* scb = sca + slab_a;
   // Slices of both operands (one warp per row).
   {
     const int rows_a = slab_a, rows_b = slab_b;
@@ -358,7 +376,7 @@ cudaError_t oz_gemm(const OzGemm& p, cudaStream_t s) {
     return cudaErrorInvalidValue;
   OzArgs g{};
   g.C = p.C; g.ldc = p.ldc; g.m = p.m; g.n = p.n; g.kchunks = kpad / kChunk; g.S = p.S;
-  g.slab_a = slab_a; g.slab_b = slab_b; g.alpha = p.alpha; g.sa = sca; g.sb = scb;
+  g.slab_a = slab_a; g.slab_b = slab_b; g.alpha = p.alpha; g.ea = sca; g.eb = scb;
   g.tiles_n = slab_b / kTile;
   g.ntiles = (slab_a / kTile) * g.tiles_n;
   g.flag = p.flag;

@@ -67,16 +67,16 @@ __host__ __device__ inline SmemLayout smem_layout(int n, int k0, int nb, int G) 
   SmemLayout L;
   const int m = n - k0;
   L.rows_per = (m + G - 1) / G;
-  L.nseg = 4;
+  L.nseg = 2;
   L.v = 0;
   L.vw = L.v + (size_t)n;
   L.y = L.vw + (size_t)L.rows_per * (2 * nb + 1);
   L.rowp = L.y + (size_t)L.rows_per;
-  L.cur = L.rowp + (size_t)L.rows_per * L.nseg;
+  L.cur = L.rowp + (size_t)L.rows_per * L.nseg * 33;
   L.nxt = L.cur + 2 * (size_t)nb;
   L.pq = L.nxt + 2 * (size_t)nb;
   L.red = L.pq + 2 * (size_t)nb + 2;
-  L.total = L.red + kWarps + 4;
+  L.total = L.red + kWarps + 8;
   return L;
 }
 
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(kThreads, 1) panel_kernel(PanelArgs A) {
   double* v = sm + L.v;        // v_j over [j+1, n)
   double* vw = sm + L.vw;      // own rows' [V W], rows_per x 2nb (row stride 2nb + 1: no bank conflicts)
   double* yl = sm + L.y;       // own rows' y
-  double* rowp = sm + L.rowp;  // (row, segment) partial sums of H v
+  double* rowp = sm + L.rowp;  // (row, segment) lane partial sums of H v, 33 apart
   double* cur = sm + L.cur;    // row j of [V W] for the column correction
   double* nxt = sm + L.nxt;    // row j+1 of [V W], formed during step j
   double* pq = sm + L.pq;      // W^T v (l < i), V^T v (nb + l), v^T y (2nb)
@@ -100,16 +100,15 @@ __global__ void __launch_bounds__(kThreads, 1) panel_kernel(PanelArgs A) {
   double* H = A.H;
   // [V W] rows of this panel start at zero
   for (int x = tid; x < L.rows_per * lds; x += kThreads) vw[x] = 0.0;
-  for (int x = tid; x < 2 * nb; x += kThreads) nxt[x] = 0.0;
+  for (int x = tid; x < 2 * nb; x += kThreads) cur[x] = 0.0;
   __syncthreads();
   double* part = A.part;  // [G][2nb + 2]
   for (int j = k0; j < A.k1; ++j) {
     const int i = j - k0;
     const int par = i & 1;
     double* col = A.col + (size_t)par * n;
-    // row j of [V W]: entries l < i (the last one formed by every CTA at step j-1)
-    for (int x = tid; x < 2 * nb; x += kThreads) cur[x] = nxt[x];
-    __syncthreads();
+    // cur: row j of [V W], entries l < i (the last one formed by every CTA
+    // at step j-1, in what was nxt then)
     // Phase 1: own pieces of column j of the corrected matrix, and norm shares.
     double s = 0.0;
     for (int r = max(r0, j) + tid; r < r1; r += kThreads) {
@@ -122,16 +121,23 @@ __global__ void __launch_bounds__(kThreads, 1) panel_kernel(PanelArgs A) {
     s = block_sum(s, red);
     if (tid == 0) __stcg(part + (size_t)rank * (ld + 2) + ld + 1, s);
     grid.sync();  // (A)
-    // Phase 2: the Householder vector of column j, in full in every CTA.
-    if (tid < 32) {
+    // Phase 2: the Householder vector of column j, in full in every CTA.  The
+    // column pieces and the norm shares are fetched in one round trip.
+    for (int c = j + tid; c < n; c += kThreads) v[c] = __ldcg(col + c);
+    if (tid == 0) {
       double t = 0.0;
-      for (int q = lane; q < G; q += 32) t += __ldcg(part + (size_t)q * (ld + 2) + ld + 1);
-      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-      if (lane == 0) red[kWarps + 1] = t;
+      for (int q0 = 0; q0 < G; q0 += 8) {
+        double sh[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) sh[u] = q0 + u < G ? __ldcg(part + (size_t)(q0 + u) * (ld + 2) + ld + 1) : 0.0;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) t += sh[u];
+      }
+      red[kWarps + 1] = t;
     }
     __syncthreads();
     const double nrm2 = red[kWarps + 1];
-    const double dj = __ldcg(col + j), alpha = __ldcg(col + j + 1);
+    const double dj = v[j], alpha = v[j + 1];
     double tau, beta, scal;
     if (nrm2 == 0.0) {
       tau = 0.0; beta = alpha; scal = 0.0;
@@ -140,7 +146,8 @@ __global__ void __launch_bounds__(kThreads, 1) panel_kernel(PanelArgs A) {
       tau = (beta - alpha) / beta;
       scal = 1.0 / (alpha - beta);
     }
-    for (int c = j + 1 + tid; c < n; c += kThreads) v[c] = (c == j + 1) ? 1.0 : __ldcg(col + c) * scal;
+    __syncthreads();
+    for (int c = j + 1 + tid; c < n; c += kThreads) v[c] = (c == j + 1) ? 1.0 : v[c] * scal;
     if (rank == 0 && tid == 0) { A.d[j] = dj; A.e[j] = beta; A.tau[j] = tau; }
     __syncthreads();
     // v_j into row j of the block (no CTA reads row j again), own share of
@@ -161,22 +168,34 @@ __global__ void __launch_bounds__(kThreads, 1) panel_kernel(PanelArgs A) {
       const int r = ra + rr;
       const int cb = j + 1 + sg * seglen, ce = min(n, cb + seglen);
       const double* Hr = H + (size_t)r * n;
+      // eight independent loads in flight per lane: the row streams from L2
+      // or HBM and the FP64 pipe, not the load latency, must set the pace
       double acc0 = 0.0, acc1 = 0.0;
-      int c = cb + lane;
-      for (; c + 32 < ce; c += 64) {
-        acc0 = fma(__ldcg(Hr + c), v[c], acc0);
-        acc1 = fma(__ldcg(Hr + c + 32), v[c + 32], acc1);
+      for (int c = cb + lane; c < ce; c += 8 * 32) {
+        double h[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) h[u] = c + 32 * u < ce ? __ldcg(Hr + c + 32 * u) : 0.0;
+#pragma unroll
+        for (int u = 0; u < 8; u += 2) {
+          acc0 = fma(h[u], c + 32 * u < ce ? v[c + 32 * u] : 0.0, acc0);
+          acc1 = fma(h[u + 1], c + 32 * (u + 1) < ce ? v[c + 32 * (u + 1)] : 0.0, acc1);
+        }
       }
-      if (c < ce) acc0 = fma(__ldcg(Hr + c), v[c], acc0);
-      acc0 += acc1;
-      for (int o = 16; o > 0; o >>= 1) acc0 += __shfl_xor_sync(0xffffffffu, acc0, o);
-      if (lane == 0) rowp[rr * S + sg] = acc0;
+      // lane partials to shared memory: one thread per row adds them (32
+      // additions per item instead of a warp-wide shuffle tree's 160)
+      rowp[(size_t)(rr * S + sg) * 33 + lane] = acc0 + acc1;
     }
     __syncthreads();
     double yv = 0.0;
     for (int rr = tid; rr < nr; rr += kThreads) {
       double y = 0.0;
-      for (int sg = 0; sg < S; ++sg) y += rowp[rr * S + sg];
+      for (int sg = 0; sg < S; ++sg) {
+        const double* pr = rowp + (size_t)(rr * S + sg) * 33;
+        double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+#pragma unroll
+        for (int q = 0; q < 32; q += 4) { t0 += pr[q]; t1 += pr[q + 1]; t2 += pr[q + 2]; t3 += pr[q + 3]; }
+        y += (t0 + t1) + (t2 + t3);
+      }
       yl[ra - r0 + rr] = y;
       yv = fma(y, v[ra + rr], yv);
       if (ra + rr == j + 1) __stcg(A.ybuf + par, y);
@@ -192,18 +211,36 @@ __global__ void __launch_bounds__(kThreads, 1) panel_kernel(PanelArgs A) {
     }
     if (tid == 0) __stcg(part + (size_t)rank * (ld + 2) + ld, yv);
     grid.sync();  // (B)
-    // Phase 3: sums of the shares, own rows of w, and row j+1's new W entry.
-    for (int x = tid; x < 2 * nb + 1; x += kThreads) {
-      const bool used = x == ld ? true : (x < nb ? x < i : x - nb < i);
+    // Phase 3: sums of the shares, own rows of w, and row j+1's new W entry;
+    // the shares, row j+1 of [V W] (entries l < i, from the owners' earlier
+    // writes) and y(j+1) are fetched in one round trip.
+    for (int x = tid; x < 2 * nb; x += kThreads) {
+      const int l = x < nb ? x : x - nb;
+      nxt[x] = l < i ? __ldcg(A.VW + (size_t)(j + 1) * ld + x) : 0.0;
+    }
+    if (tid == kThreads - 1) red[kWarps + 2] = __ldcg(A.ybuf + par);
+    // a thread per value (2i + 1 of them) adds the G shares, loaded eight at a time
+    for (int xx = tid; xx < 2 * i + 1; xx += kThreads) {
+      const int x = xx == 2 * i ? ld : (xx < i ? xx : nb + (xx - i));
       double t = 0.0;
-      if (used)
-        for (int q = 0; q < G; ++q) t += __ldcg(part + (size_t)q * (ld + 2) + (x == ld ? ld : x));
-      pq[x == ld ? ld : x] = t;
+      for (int q0 = 0; q0 < G; q0 += 8) {
+        double sh[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) sh[u] = q0 + u < G ? __ldcg(part + (size_t)(q0 + u) * (ld + 2) + x) : 0.0;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) t += sh[u];
+      }
+      pq[x] = t;
     }
     __syncthreads();
-    double pp = 0.0;
-    for (int l = 0; l < i; ++l) pp = fma(pq[l], pq[nb + l], pp);
-    const double yvt = pq[ld] - 2.0 * pp;  // v^T (A_now v)
+    if (warp == 0) {  // v^T (A_now v) = y.v - 2 (W^T v).(V^T v), formed once
+      double t = 0.0;
+      for (int l = lane; l < i; l += 32) t = fma(pq[l], pq[nb + l], t);
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (lane == 0) red[kWarps + 3] = pq[ld] - 2.0 * t;
+    }
+    __syncthreads();
+    const double yvt = red[kWarps + 3];
     const double h = 0.5 * tau * tau * yvt;
     for (int rr = tid; rr < nr; rr += kThreads) {
       const int r = ra + rr;
@@ -214,26 +251,17 @@ __global__ void __launch_bounds__(kThreads, 1) panel_kernel(PanelArgs A) {
       vr[nb + i] = w;
       A.VW[(size_t)r * ld + nb + i] = w;
     }
-    // row j+1 of [V W] for the next column: entries l < i from the owners'
-    // earlier writes, l = i formed here (v_j(j+1) = 1)
-    if (j + 1 < n) {
-      const double yj1 = __ldcg(A.ybuf + par);
+    if (warp == 0) {
       double t = 0.0;
-      for (int l = 0; l < i; ++l) {
-        const double vl = __ldcg(A.VW + (size_t)(j + 1) * ld + l);
-        const double wl = __ldcg(A.VW + (size_t)(j + 1) * ld + nb + l);
-        t = fma(-vl, pq[l], fma(-wl, pq[nb + l], t));
-      }
-      __syncthreads();
-      for (int x = tid; x < 2 * nb; x += kThreads) {
-        const int l = x < nb ? x : x - nb;
-        double val = 0.0;
-        if (l < i) val = __ldcg(A.VW + (size_t)(j + 1) * ld + x);
-        else if (l == i) val = x < nb ? 1.0 : fma(tau, yj1 + t, -h);
-        nxt[x] = val;
+      for (int l = lane; l < i; l += 32) t = fma(-nxt[l], pq[l], fma(-nxt[nb + l], pq[nb + l], t));
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (lane == 0) {
+        nxt[i] = 1.0;
+        nxt[nb + i] = fma(tau, red[kWarps + 2] + t, -h);
       }
     }
     __syncthreads();
+    double* sw = cur; cur = nxt; nxt = sw;
   }
   if (A.last) {
     // closing 2 x 2 block with the whole panel's correction
