@@ -477,6 +477,18 @@ nrg_status nrg_write_code_pars(const char* dir, double lambda, int nsites, const
  * plus ThisCodePars.dat: the reference's DM_NRG can then run on them. */
 nrg_status nrg_dm_save_bin(nrg_ctx* ctx, const char* dir, const char* name);
 
+/* The inverse of nrg_dm_save_bin: shells 0 .. nshells-1 (nshells <= 0: the
+ * Nsitesmax of ThisCodePars.dat) of a one-channel |Q S> NRG_main run saved
+ * with the spectral density switched on (calcdens = 1), read from dir in the
+ * reference's layout -- what DM_NRG reads (DM_NRG.cpp:163-298;
+ * CNRGarray::ReadBinInStream NRGarrayClass.cpp:886-958,
+ * CNRGbasisarray::ReadBin :2005-2078, CNRGmatrix::ReadBin
+ * NRGmatrixClass.cpp:1016-1082) -- into the context's DM-NRG state, so that
+ * nrg_dm_backprop and nrg_lehmann run on them.  Each shell's basis must be
+ * what BuildBasis makes of the previous shell's kept states (else
+ * NRG_ERR_SYNC); Lambda comes from ThisCodePars.dat. */
+nrg_status nrg_dm_load_bin(nrg_ctx* ctx, const char* dir, const char* name, int nshells);
+
 /* Largest block nrg_diag_block_noalloc accepts. */
 #define NRG_NOALLOC_MAX_N 256
 

@@ -170,3 +170,69 @@ def test_dm_on_an_uneven_grid(engine):
     engine.dm_backprop(prm)
     _, A = engine.lehmann(prm, omegas=om)
     _close(A, o_A)
+
+
+def _write_oracle_shells(d, nsites, ncut, lam, U, ed, G, name="1chQSAnderson"):
+    shells = orc.dm_shells(nsites, ncut, lam, U, ed, G)
+    for N, s in enumerate(shells):
+        tg.write_dm_shell(str(d), name, N, s)
+    tg.write_code_pars(str(d), lam, nsites, name)
+
+
+def test_dm_from_snapshot_files(tmp_path):
+    """The backward sweep and spectral function started from .bin snapshots in
+    the reference's layout (as the reference's NRG_main writes them: the
+    writer's files equal NRG_main's byte for byte, tests/test_binfile.py)
+    instead of a GPU forward sweep, against the oracle's DM-NRG on the same
+    shells."""
+    lam, ns, nc, U, ed, G = 2.5, 12, 80, 0.4, -0.2, 0.015
+    _write_oracle_shells(tmp_path, ns, nc, lam, U, ed, G)
+    temp = 0.7 * lam ** (-(8 - 1) / 2.0) / 0.727
+    om = np.concatenate([-np.logspace(0, -5, 60), np.logspace(-5, 0, 60)])
+    _, o_A, o_tr = orc.dm_spectral(ns, nc, lam, U, ed, G, temp, 0.6, omegas=om)
+    e = tg.Engine(0)
+    try:
+        assert e.dm_load_bin(str(tmp_path), "1chQSAnderson") == ns
+        prm = e.dm_params(temp=temp, bbroad=0.6)
+        np.testing.assert_allclose(e.dm_backprop(prm), o_tr, rtol=1e-10)
+        _, A = e.lehmann(prm, omegas=om)
+        _close(A, o_A)
+    finally:
+        e.close()
+
+
+def test_dm_snapshot_round_trip(engine, tmp_path):
+    """GPU forward sweep -> dm_save_bin -> dm_load_bin on a fresh context:
+    the same spectral function."""
+    engine.sweep_dm(10, 60, 2.5, 0.5, -0.25, 0.02)
+    prm = engine.dm_params(mtemp=6, bbroad=0.6, nw=4)
+    engine.dm_backprop(prm)
+    om, A = engine.lehmann(prm)
+    engine.dm_save_bin(str(tmp_path), "rt")
+    e = tg.Engine(0)
+    try:
+        assert e.dm_load_bin(str(tmp_path), "rt") == 10
+        p2 = e.dm_params(mtemp=6, bbroad=0.6, nw=4)
+        e.dm_backprop(p2)
+        om2, A2 = e.lehmann(p2)
+        np.testing.assert_array_equal(om2, om)
+        np.testing.assert_allclose(A2, A, rtol=1e-12, atol=1e-14 * float(np.abs(A).max()))
+    finally:
+        e.close()
+
+
+def test_dm_snapshot_mismatch_is_rejected(engine, tmp_path):
+    """A shell whose basis is not what BuildBasis makes of the previous
+    shell's kept states (here: shell 2 of another kept count) is refused."""
+    a, b = tmp_path / "a", tmp_path / "b"
+    a.mkdir(); b.mkdir()
+    _write_oracle_shells(a, 4, 40, 2.5, 0.5, -0.25, 0.02)
+    _write_oracle_shells(b, 4, 20, 2.5, 0.5, -0.25, 0.02)
+    import shutil
+    for k in ("Abasis", "Acut", "Mat0"):
+        shutil.copy(b / f"{k}_1chQSAnderson_N2.bin", a / f"{k}_1chQSAnderson_N2.bin")
+    with pytest.raises(tg.NRGError) as ei:
+        engine.dm_load_bin(str(a), "1chQSAnderson")
+    assert ei.value.status == 6  # NRG_ERR_SYNC
+    with pytest.raises(tg.NRGError):
+        engine.dm_load_bin(str(tmp_path / "missing"), "1chQSAnderson")

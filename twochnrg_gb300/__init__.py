@@ -288,6 +288,7 @@ def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     _ip = ctypes.POINTER(ctypes.c_int)
     L.nrg_diag_blocks.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp, _dp, _dp]
     L.nrg_set_precision.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.nrg_dm_load_bin.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int]
     L.nrg_gemm_f64_tensor.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                       ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                                       ctypes.c_void_p, ctypes.c_int64, ctypes.c_int]
@@ -556,6 +557,13 @@ class Engine:
     def dm_save_bin(self, directory: str, name: str) -> None:
         """The DM-NRG shells as the reference's .bin files plus ThisCodePars.dat."""
         self._check(self.L.nrg_dm_save_bin(self.h, directory.encode(), name.encode()))
+
+    def dm_load_bin(self, directory: str, name: str, nshells: int = 0) -> int:
+        """DM-NRG shells from the reference's .bin files (NRG_main with the
+        spectral density on, or dm_save_bin) and ThisCodePars.dat; afterwards
+        dm_backprop and lehmann run on them.  Returns the number of shells."""
+        self._check(self.L.nrg_dm_load_bin(self.h, directory.encode(), name.encode(), int(nshells)))
+        return int(self.L.nrg_dm_num_shells(self.h))
 
     def timing(self) -> dict:
         t = Timing()

@@ -17,12 +17,15 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
 #include <fstream>
 #include <iomanip>
+#include <iterator>
 #include <string>
 #include <vector>
 
 #include "../../include/twochnrg_gb300.h"
+#include "nrg_model.h"
 
 namespace {
 
@@ -69,7 +72,89 @@ std::string path_of(const char* dir, const char* what, const char* name, int n) 
   return std::string(dir) + "/" + what + "_" + name + "_N" + std::to_string(n) + ".bin";
 }
 
+// Reader of the same layout (the inverse of Out): every count is checked
+// against the bytes left, so a truncated or foreign file fails cleanly.
+struct In {
+  std::vector<char> b;
+  size_t pos = 0;
+  bool ok = true;
+  bool need(size_t k) { if (!ok || pos + k > b.size()) ok = false; return ok; }
+  int32_t i32() { int32_t v = 0; if (need(4)) { std::memcpy(&v, b.data() + pos, 4); pos += 4; } return v; }
+  double f64() { double v = 0; if (need(8)) { std::memcpy(&v, b.data() + pos, 8); pos += 8; } return v; }
+  bool b8() { bool v = false; if (need(1)) { v = b[pos] != 0; pos += 1; } return v; }
+  int32_t count(size_t elem) {
+    const int32_t n = i32();
+    if (n < 0 || !need((size_t)n * elem)) { ok = false; return 0; }
+    return n;
+  }
+  void dvec(std::vector<double>& v) {
+    const int32_t n = count(8);
+    v.resize(n);
+    if (n) { std::memcpy(v.data(), b.data() + pos, 8 * (size_t)n); pos += 8 * (size_t)n; }
+  }
+  void ivec(std::vector<int>& v) {
+    const int32_t n = count(4);
+    v.resize(n);
+    for (int32_t k = 0; k < n; ++k) v[k] = i32();
+  }
+  void bvec(std::vector<unsigned char>& v) {
+    const int32_t n = count(1);
+    v.resize(n);
+    for (int32_t k = 0; k < n; ++k) v[k] = b8() ? 1 : 0;
+  }
+  void skip(size_t elem) { const int32_t n = count(elem); pos += (size_t)n * elem; }
+};
+
 }  // namespace
+
+namespace nrg {
+
+// CNRGarray::ReadBin / CNRGbasisarray::ReadBin / CNRGmatrix::ReadBin
+// (NRGarrayClass.cpp:886-958, 2005-2078; NRGmatrixClass.cpp:1016-1082):
+// the fields in SaveBin's order; complex parts and the fields NRG_main
+// leaves empty are skipped.  kind: 0 CNRGarray, 1 CNRGbasisarray, 2 CNRGmatrix.
+bool read_bin_file(const std::string& path, int kind, BinShellFile& f, std::string& err) {
+  std::ifstream is(path, std::ios::in | std::ios::binary);
+  if (!is) { err = "cannot open " + path; return false; }
+  In in;
+  in.b.assign(std::istreambuf_iterator<char>(is), std::istreambuf_iterator<char>());
+  f.nshell = in.i32();
+  f.nqn = in.i32();
+  in.dvec(f.qn);
+  in.dvec(f.en);
+  in.dvec(f.evec);
+  in.skip(16);              // cEigVec
+  in.ivec(f.bbe);
+  in.skip(4);               // iDegen
+  in.bvec(f.kept);
+  f.totalS = in.b8();
+  in.ivec(f.sqnumbers);
+  if (kind == 1) {
+    in.ivec(f.itype);
+    in.ivec(f.stcf);
+    in.ivec(f.bbe_bc);
+    in.ivec(f.bbe_eig);
+    in.i32();               // NQNumbers_stcf
+    in.skip(8);             // StCameFromQNumbers
+  } else if (kind == 2) {
+    in.dvec(f.mat_el);
+    in.skip(16);            // MatElCplx
+    in.ivec(f.map);
+    in.ivec(f.mbe);
+    in.b8(); in.b8(); in.b8();  // NeedOld, UpperTriangular, IsComplex
+    in.f64();               // WignerEckartL
+  }
+  if (!in.ok || in.pos != in.b.size()) { err = "malformed or truncated snapshot " + path; return false; }
+  if (f.nqn <= 0 || f.qn.size() % (size_t)f.nqn != 0 || f.bbe.size() != 2 * (f.qn.size() / f.nqn)) {
+    err = "inconsistent block structure in " + path;
+    return false;
+  }
+  return true;
+}
+
+std::string bin_path(const char* dir, const char* what, const char* name, int n) { return path_of(dir, what, name, n); }
+
+}  // namespace nrg
 
 extern "C" {
 

@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -1749,6 +1750,128 @@ void dm_save_bin_impl(nrg_ctx* c, const char* dir, const char* name) {
   if (st != NRG_OK) throw NrgError(st, std::string("cannot write ThisCodePars.dat into ") + dir);
 }
 
+// The DM-NRG shells from .bin snapshots in the reference's layout, as
+// DM_NRG reads them (DM_NRG.cpp:163-298 with CNRGarray::ReadBinInStream,
+// NRGarrayClass.cpp:886-958; CNRGbasisarray::ReadBin, :2005-2078;
+// CNRGmatrix::ReadBin, NRGmatrixClass.cpp:1016-1082): Lambda from
+// ThisCodePars.dat, then per shell N Abasis_N, Acut_N and Mat0_N (c_d).  The
+// device needs each shell's BuildBasis segments, which the files do not
+// hold: they are rebuilt from the previous shell's kept blocks (H_{-1}'s for
+// shell 0) and the rebuilt basis must equal the file's -- sectors, block
+// sizes, iType and StCameFrom -- or the call returns NRG_ERR_SYNC.
+void dm_load_bin_impl(nrg_ctx* c, const char* dir, const char* name, int nshells) {
+  if (!dir || !name) throw NrgError(NRG_ERR_ARG, "directory or name is NULL");
+  double lambda = 0.0;
+  int nsites0 = 0, nmax = 0;
+  {
+    std::ifstream pars(std::string(dir) + "/ThisCodePars.dat");
+    if (!(pars >> lambda >> nsites0 >> nmax)) throw NrgError(NRG_ERR_ARG, std::string("cannot read ") + dir +
+                                                                      "/ThisCodePars.dat");
+  }
+  if (!(lambda > 1.0)) throw NrgError(NRG_ERR_ARG, "ThisCodePars.dat: Lambda must exceed 1");
+  if (nshells <= 0) nshells = nmax;
+  if (nshells <= 0) throw NrgError(NRG_ERR_ARG, "no shells to load");
+  ModelSpec m = make_model(MODEL_1CHQS);
+  StartState st = make_start(m, lambda, 0.0, 0.0, 0.0);
+  // the device words the backward sweep and the spectral function use (a
+  // fresh context has run no sweep that would have made them)
+  c->flag.ensure(sizeof(int) * 4);
+  CU(cudaMemsetAsync(c->flag.p, 0, sizeof(int), c->stream));
+  c->scal.ensure(sizeof(double) * 32);
+  c->partial.ensure(sizeof(double) * 64 * 16);
+  c->opptr.ensure(sizeof(double*) * 32);
+  c->dm.clear();
+  c->dm_rho_valid = false;
+  c->dm_lambda = lambda;
+  c->dm_model = MODEL_1CHQS;
+  c->dm_hm1_en.assign(st.en.size(), 0.0);
+  BlockArray prev = st.blk;                        // the kept array shell N was built from
+  std::vector<int> prev_full_off = st.blk.offset;  // where each kept block starts in the previous full array
+  for (int N = 0; N < nshells; ++N) {
+    BinShellFile fb, fa, fm;
+    std::string err;
+    if (!read_bin_file(bin_path(dir, "Abasis", name, N), 1, fb, err) ||
+        !read_bin_file(bin_path(dir, "Acut", name, N), 1, fa, err) ||
+        !read_bin_file(bin_path(dir, "Mat0", name, N), 2, fm, err))
+      throw NrgError(NRG_ERR_ARG, err);
+    if (fb.nqn != 2 || fa.nqn != 2 || fm.nqn != 2 || fb.nshell != N || fa.nshell != N)
+      throw NrgError(NRG_ERR_ARG, "snapshot of shell " + std::to_string(N) + " is not a one-channel |Q S> shell N");
+    Basis B;
+    build_basis(m, prev, B);
+    const int nb = B.blk.nblocks(), ns = B.blk.nstates();
+    bool same = (int)fb.qn.size() == 2 * nb && (int)fb.itype.size() == ns && (int)fb.stcf.size() == ns &&
+                (int)fb.en.size() == ns;
+    for (int b = 0; same && b < nb; ++b)
+      same = fb.qn[2 * b] == B.blk.q(b, 0) && fb.qn[2 * b + 1] == B.blk.q(b, 1) &&
+             fb.bbe[2 * b] == B.blk.offset[b] && fb.bbe[2 * b + 1] == B.blk.offset[b] + B.blk.size[b] - 1;
+    for (int b = 0; same && b < nb; ++b)
+      for (int i = 0; same && i < B.blk.size[b]; ++i) {
+        const int g = B.blk.offset[b] + i;
+        const Segment& sg = B.seg[b][B.seg_of[g]];
+        same = fb.itype[g] == B.itype[g] && fb.stcf[g] == prev_full_off[sg.old_block] + B.a_of[g];
+      }
+    if (!same)
+      throw NrgError(NRG_ERR_SYNC, "Abasis of shell " + std::to_string(N) +
+                                       " is not what BuildBasis makes of the previous shell's kept states");
+    if (N == 0)
+      for (int g = 0; g < ns; ++g) c->dm_hm1_en[fb.stcf[g]] = fb.en[g];
+    // Acut_N: the blocks of H_N, energies, Kept, all eigenvectors
+    if (fa.qn != fb.qn || fa.bbe != fb.bbe || (int)fa.en.size() != ns || (int)fa.kept.size() != ns)
+      throw NrgError(NRG_ERR_SYNC, "Acut of shell " + std::to_string(N) + " does not match its Abasis");
+    auto sh = std::make_unique<DmShell>();
+    sh->bsize = B.blk.size; sh->boff = B.blk.offset; sh->qn = B.blk.qn;
+    sh->en = fa.en; sh->kept = fa.kept;
+    int64_t z = 0;
+    for (int b = 0; b < nb; ++b) {
+      const int n = B.blk.size[b];
+      if ((int)fa.bbe_eig.size() != 2 * nb || fa.bbe_eig[2 * b] != z || fa.bbe_eig[2 * b + 1] != z + (int64_t)n * n - 1)
+        throw NrgError(NRG_ERR_SYNC, "eigenvector layout of shell " + std::to_string(N) + " is not n x n per block");
+      sh->zoff.push_back(z);
+      z += (int64_t)n * n;
+    }
+    if ((int64_t)fa.evec.size() != z) throw NrgError(NRG_ERR_SYNC, "eigenvector count of shell " + std::to_string(N));
+    sh->zsize = z;
+    // kept blocks (Kept is a prefix of each block: CutStates keeps the levels up to E_cut)
+    BlockArray kept;
+    kept.nqn = 2;
+    std::vector<int> kept_full_off;
+    for (int b = 0; b < nb; ++b) {
+      int k = 0;
+      while (k < B.blk.size[b] && fa.kept[B.blk.offset[b] + k]) ++k;
+      for (int x = k; x < B.blk.size[b]; ++x)
+        if (fa.kept[B.blk.offset[b] + x]) throw NrgError(NRG_ERR_SYNC, "Kept is not a prefix of its block");
+      if (k == 0) continue;
+      kept.push(&B.blk.qn[2 * b], k);
+      sh->kept_src.push_back(b);
+      kept_full_off.push_back(B.blk.offset[b]);
+    }
+    // c_d: MatBlockMap / MatBlockBegEnd over the blocks of H_N
+    const int nmb = (int)fm.map.size() / 2;
+    if ((int)fm.mbe.size() != 2 * nmb || fm.qn != fa.qn || fm.bbe != fa.bbe)
+      throw NrgError(NRG_ERR_SYNC, "Mat0 of shell " + std::to_string(N) + " is not synced with Acut");
+    int64_t nel = 0;
+    for (int k = 0; k < nmb; ++k) {
+      const int bi = fm.map[2 * k], bj = fm.map[2 * k + 1];
+      if (bi < 0 || bi >= nb || bj < 0 || bj >= nb ||
+          fm.mbe[2 * k + 1] - fm.mbe[2 * k] + 1 != B.blk.size[bi] * B.blk.size[bj])
+        throw NrgError(NRG_ERR_SYNC, "c_d block table of shell " + std::to_string(N));
+      sh->cd.bi.push_back(bi); sh->cd.bj.push_back(bj); sh->cd.off.push_back(fm.mbe[2 * k]);
+      nel = std::max<int64_t>(nel, (int64_t)fm.mbe[2 * k + 1] + 1);
+    }
+    if ((int64_t)fm.mat_el.size() < nel) throw NrgError(NRG_ERR_SYNC, "c_d elements of shell " + std::to_string(N));
+    sh->cd.size = nel;
+    sh->Z.ensure(sizeof(double) * std::max<int64_t>(z, 1));
+    h2d(c, sh->Z.p, fa.evec.data(), sizeof(double) * z);
+    sh->cdel.ensure(sizeof(double) * std::max<int64_t>(nel, 1));
+    h2d(c, sh->cdel.p, fm.mat_el.data(), sizeof(double) * nel);
+    CU(cudaStreamSynchronize(c->stream));
+    sh->basis = std::move(B);
+    c->dm.push_back(std::move(sh));
+    prev = kept;
+    prev_full_off = kept_full_off;
+  }
+}
+
 // DiagBlock for a batch of blocks given in the reference's packed upper
 // storage: same device pipeline as the sweep, all eigenvectors kept.
 // ------------------------------------------------------------ thermodynamics
@@ -2513,6 +2636,16 @@ nrg_status nrg_lehmann(nrg_ctx* ctx, const nrg_dm_params* prm, int nomega, const
     CU(cudaSetDevice(ctx->device));
     std::memset(&ctx->timing, 0, sizeof(ctx->timing));
     lehmann_impl(ctx, prm, nomega, omegas, omega_rhow, nout);
+  });
+  return NRG_OK;
+}
+
+nrg_status nrg_dm_load_bin(nrg_ctx* ctx, const char* dir, const char* name, int nshells) {
+  if (!ctx) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    dm_load_bin_impl(ctx, dir, name, nshells);
   });
   return NRG_OK;
 }

@@ -120,6 +120,19 @@ StartState make_chain_start(const ModelSpec& m, double lambda);
 // BuildBasis (BuildBasis.cpp:8-432) from a kept array.
 void build_basis(const ModelSpec& m, const BlockArray& kept, Basis& out);
 
+// One .bin snapshot in the reference's SaveBin layout (binfile.cpp): the
+// CNRGarray fields, the CNRGbasisarray ones (kind 1) or the CNRGmatrix ones
+// (kind 2).
+struct BinShellFile {
+  int nshell = 0, nqn = 0;
+  bool totalS = false;
+  std::vector<double> qn, en, evec, mat_el;
+  std::vector<int> bbe, sqnumbers, itype, stcf, bbe_bc, bbe_eig, map, mbe;
+  std::vector<unsigned char> kept;
+};
+bool read_bin_file(const std::string& path, int kind, BinShellFile& f, std::string& err);
+std::string bin_path(const char* dir, const char* what, const char* name, int n);
+
 // Coefficient tables for H_N assembly, per new block:
 //   coef[((ti*NT + tj)*nchan*nsigma + ch*nsigma + s)*2 + dir]
 // dir 0: the old operator is read as (stcf_i, stcf_j); dir 1: as (stcf_j,
