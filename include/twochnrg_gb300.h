@@ -192,6 +192,44 @@ nrg_status nrg_fp64_peak(nrg_ctx* ctx, double* tflops);
 nrg_status nrg_gemm_f64_tensor(nrg_ctx* ctx, int m, int n, int k, double alpha, const double* A, int64_t lda,
                                const double* B, int64_t ldb, double* C, int64_t ldc, int slices);
 
+/* ---- derivatives: a forward / backward pair ------------------------------
+ * The reference has no derivative code; its CalcOpAvg averages of the
+ * operators dH/dp (n_d for eps_d, (n_d^2 - n_d)/2 for U, -S_z for B;
+ * src/CalcOpAvg.cpp:13-84, CodeHandler_ModelSwitch.cpp:748-780) are the
+ * Hellmann-Feynman values these derivatives meet for the ground-state energy.
+ *
+ * nrg_grad_forward runs the sweep of cfg (NRG_MODEL_1CH_QS or
+ * NRG_MODEL_1CH_QSZ, FP64) and, at its kept-state set, the derivatives of
+ * every iteration's reported values with respect to p = (eps_d, U, Gamma1,
+ * B) (B is cfg->gamma2_or_B).  They come from tangents carried through each
+ * step on the device: the assembly of dH_N from the previous tangents, the
+ * eigenvalue and kept-eigenvector derivatives from first-order perturbation
+ * theory with every eigenvector of the block (no coupling between levels
+ * closer than 1e-10 of the block's scale: inside a degenerate multiplet the
+ * eigenvectors are not determined and do not couple), the operator rotation
+ * differentiated, and the thermodynamic and average sums differentiated.
+ * Forward tangents carry the four directions beside the primal iteration by
+ * iteration, so no eigenvectors are stored between iterations (nothing to
+ * checkpoint).  The iterations stay readable with nrg_sweep_iteration. */
+typedef struct {
+  int nsites;              /* iterations */
+  int nparams;             /* 4: eps_d, U, Gamma1, B */
+  int nops;                /* averaged operators, as nrg_iteration.opavg */
+  const double* d_thermo;  /* [(n*nparams + k)*16 + v]: d thermo[v] of iteration n / d p_k */
+  const double* d_opavg;   /* [(n*nparams + k)*nops + o] */
+  const double* d_emin;    /* [n*nparams + k]: d emin (the raw lowest level) / d p_k */
+  const double* egs;       /* [n] absolute ground-state energy sum_{M<=n} D_M emin_M */
+  const double* d_egs;     /* [n*nparams + k] */
+} nrg_grad;
+nrg_status nrg_grad_forward(nrg_ctx* ctx, const nrg_sweep_config* cfg, nrg_grad* out);
+
+/* Vector-Jacobian product of the last nrg_grad_forward: grad[k] =
+ * sum over iterations n of g_thermo[n*16+v] d thermo[v]/dp_k + g_opavg[n*nops+o]
+ * d opavg[o]/dp_k + g_egs[n] d egs/dp_k; any of the three weight arrays may
+ * be NULL.  NRG_ERR_STATE without a preceding forward. */
+nrg_status nrg_grad_backward(nrg_ctx* ctx, const double* g_thermo, const double* g_opavg, const double* g_egs,
+                             double* grad);
+
 /* Arithmetic (nrg_precision) of the drop-in calls nrg_diag_blocks and
  * nrg_diag_hn on this context; a sweep sets it from its configuration. */
 nrg_status nrg_set_precision(nrg_ctx* ctx, int precision);

@@ -54,6 +54,25 @@ class _Iteration(ctypes.Structure):
                 ("wall_ms", ctypes.c_double), ("device_ms", ctypes.c_double)]
 
 
+class _Grad(ctypes.Structure):
+    _fields_ = [("nsites", ctypes.c_int), ("nparams", ctypes.c_int), ("nops", ctypes.c_int),
+                ("d_thermo", ctypes.POINTER(ctypes.c_double)), ("d_opavg", ctypes.POINTER(ctypes.c_double)),
+                ("d_emin", ctypes.POINTER(ctypes.c_double)), ("egs", ctypes.POINTER(ctypes.c_double)),
+                ("d_egs", ctypes.POINTER(ctypes.c_double))]
+
+
+@dataclass
+class GradResult:
+    """nrg_grad_forward: the sweep and the derivatives of its reported values
+    with respect to (eps_d, U, Gamma1, B), parameter on the second axis."""
+    sweep: "SweepResult"
+    d_thermo: np.ndarray   # (nsites, 4, 4, 4): d thermo (beta, T, T chi, S at 4 temperatures)
+    d_opavg: np.ndarray    # (nsites, 4, nops)
+    d_emin: np.ndarray     # (nsites, 4)
+    egs: np.ndarray        # (nsites,) absolute ground-state energy
+    d_egs: np.ndarray      # (nsites, 4)
+
+
 class Timing(ctypes.Structure):
     _fields_ = [("total_ms", ctypes.c_double), ("assemble_ms", ctypes.c_double),
                 ("tridiag_ms", ctypes.c_double), ("tridiag_eig_ms", ctypes.c_double),
@@ -288,6 +307,9 @@ def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     _ip = ctypes.POINTER(ctypes.c_int)
     L.nrg_diag_blocks.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp, _dp, _dp]
     L.nrg_set_precision.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.nrg_grad_forward.argtypes = [ctypes.c_void_p, ctypes.POINTER(SweepConfig), ctypes.POINTER(_Grad)]
+    L.nrg_grad_backward.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.POINTER(ctypes.c_double)]
     L.nrg_dm_load_bin.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int]
     L.nrg_gemm_f64_tensor.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                       ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
@@ -625,6 +647,38 @@ class Engine:
         self._check(self.L.nrg_sweep_run(self.h, ctypes.byref(cfg)))
         return self._fetch(fetch)
 
+    def grad_forward(self, model: str, nsites: int, ncutoff: int, lam: float, U: float, ed: float,
+                     gamma1: float, B: float = 0.0, degen_eps: float = 0.0) -> GradResult:
+        """nrg_grad_forward: the sweep of the one-channel Anderson model ("1chQS"
+        or "1chQSz") and the derivatives of every iteration's reported values
+        with respect to (eps_d, U, Gamma1, B) at its kept-state set."""
+        cfg = SweepConfig(MODELS[model], nsites, ncutoff, lam, U, ed, gamma1, B, degen_eps, PREC_FP64, 0.0)
+        g = _Grad()
+        self._check(self.L.nrg_grad_forward(self.h, ctypes.byref(cfg), ctypes.byref(g)))
+        n, k, no = g.nsites, g.nparams, g.nops
+        return GradResult(self._fetch(True), _arr(g.d_thermo, n * k * 16, np.float64).reshape(n, k, 4, 4),
+                          _arr(g.d_opavg, n * k * no, np.float64).reshape(n, k, no),
+                          _arr(g.d_emin, n * k, np.float64).reshape(n, k), _arr(g.egs, n, np.float64),
+                          _arr(g.d_egs, n * k, np.float64).reshape(n, k))
+
+    def grad_backward(self, g_thermo=None, g_opavg=None, g_egs=None) -> np.ndarray:
+        """nrg_grad_backward: the gradient of sum(g_thermo * thermo) +
+        sum(g_opavg * opavg) + sum(g_egs * egs) over the iterations of the last
+        grad_forward, with respect to (eps_d, U, Gamma1, B)."""
+        keep = []
+
+        def ptr(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            keep.append(a)
+            return a.ctypes.data_as(ctypes.c_void_p)
+
+        out = np.zeros(4)
+        self._check(self.L.nrg_grad_backward(self.h, ptr(g_thermo), ptr(g_opavg), ptr(g_egs),
+                                             out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out
+
     def fetch(self) -> SweepResult:
         """The iterations of the last sweep on this context."""
         return self._fetch(True)
@@ -687,5 +741,5 @@ def sweep_batch(instances, nworkers: int = 16, device: int = 0, precision: int =
     return BatchResult(thermo.reshape(n, max_sites, 4, 4), opavg, nkept, sec.value)
 
 
-__all__ = ["Engine", "NRGError", "SweepResult", "Iteration", "BatchResult", "load_library", "sweep_batch",
+__all__ = ["Engine", "NRGError", "SweepResult", "Iteration", "BatchResult", "GradResult", "load_library", "sweep_batch",
            "MODELS"]

@@ -19,7 +19,7 @@ LIB = os.path.join(OUT_DIR, "libtwochnrg_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["engine.cu", "k_assemble.cu", "k_tridiag.cu", "k_tdeig.cu", "k_cut.cu", "k_update.cu",
-              "k_dm.cu", "k_ozaki.cu", "k_panel.cu", "noalloc.cu"]
+              "k_dm.cu", "k_ozaki.cu", "k_panel.cu", "k_tangent.cu", "noalloc.cu"]
 CXX_SOURCES = ["nrg_model.cpp", "binfile.cpp", "thermofile.cpp", "chain.cpp"]
 
 

@@ -117,8 +117,14 @@ struct IterResult {
 
 }  // namespace nrg
 
+namespace nrg { namespace { struct TangentState; } }
+
 struct nrg_ctx {
   int device = 0;
+  // derivatives of the last nrg_grad_forward: the tangent pass's state and
+  // the absolute ground-state energy per iteration with its tangents
+  nrg::TangentState* tan = nullptr;
+  std::vector<double> grad_egs, grad_degs, grad_demin;
   cudaStream_t stream = nullptr;
   std::string err;
   int64_t launches = 0;
@@ -303,7 +309,7 @@ int big_block_threshold() {
 // whole-grid kernel, the small ones the cluster kernel).
 int mixed_block_threshold() {
   const char* s = std::getenv("NRG_MIXED_N");
-  return s ? std::atoi(s) : 1800;
+  return s ? std::atoi(s) : 2200;  // measured best on the two-channel sweep (1800-4200 tried)
 }
 
 int grid_split(int nbig) {
@@ -419,7 +425,26 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
     const int Gfp = tridiag_grid_size(ta.maxn);
     if (G <= 0 || Gfp <= 0) throw NrgError(NRG_ERR_SIZE, "blocked tridiagonalization does not fit");
     const int mthr = mixed_block_threshold();
-    if (K == 1) bins[0].assign(order_h.begin(), order_h.begin() + nbig);
+    // Deal the large blocks to the K streams by their cost on the path they
+    // take (greedy, largest first): per column, the FP64 kernel does three
+    // FMAs per trailing element and pays ~16 us of barrier and vector work,
+    // the blocked panel one FMA and ~50 us (two grid barriers); in FMA units
+    // of a quarter of the GPU (about 1.3e11 FMA/s), 2.1e6 and 6.6e6 per column.
+    auto cost = [&](int n) {
+      const double n3 = (double)n * n * n;
+      return n >= mthr ? n3 / 3.0 + 6.6e6 * n : n3 + 2.1e6 * n;
+    };
+    {
+      std::vector<int> big(order_h.begin(), order_h.begin() + nbig);
+      std::stable_sort(big.begin(), big.end(), [&](int x, int y) { return cost(P.bsize[x]) > cost(P.bsize[y]); });
+      std::vector<double> load(K, 0.0);
+      for (auto& bk : bins) bk.clear();
+      for (int b : big) {
+        const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        bins[k].push_back(b);
+        load[k] += cost(P.bsize[b]);
+      }
+    }
     if (!c->fork) CU(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
     CU(cudaEventRecord(c->fork, c->stream));
     Packer pk;
@@ -502,6 +527,11 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
   ea.e2 = c->e2.as<double>();
   c->spl.ensure(std::max(P.nstates, 1));
   ea.split = c->spl.as<unsigned char>();
+  // mixed precision: the tensor-core trailing updates leave residues of order
+  // 2^-36 of the block's scale where the FP64 reduction leaves round-off, so
+  // the tridiagonal falls apart at that level (an eigenvalue moves by at most
+  // that much, inside the mixed form's 1e-9)
+  ea.split_eps = mixed ? 0x1p-34 : 0.0;
   cudaEvent_t t1 = tm.start();
   launch_bisect(ea, d_state_block, c->stream);
   c->launches += 3;  // FP32 copies, levels, ordering
@@ -853,12 +883,26 @@ void plan_update(UpdatePlan& U, const ModelSpec& m, const Basis& B, const EigPla
   U.o_jobs = U.up.add(U.jobs); U.o_tj = U.up.add(U.tjob); U.o_tm = U.up.add(U.tmn);
 }
 
-void launch_update_plan(nrg_ctx* c, Timer& tm, UpdatePlan& U) {
+// Substitutions for a run of an update plan with other inputs (the tangent
+// pass): eigenvector rows Z and columns Zt, device tables of old and new
+// operator pointers, and whether the site-operator (identity-on-old) terms
+// take part.
+struct UpdateInputs {
+  const double* Z = nullptr;
+  const double* Zt = nullptr;
+  const double* const* old_tab = nullptr;
+  double* const* new_tab = nullptr;
+  bool site_terms = true;
+};
+
+void launch_update_plan(nrg_ctx* c, Timer& tm, UpdatePlan& U, const UpdateInputs* sub = nullptr) {
   cudaEvent_t tu = tm.start();
   const size_t tbytes = sizeof(double) * std::max<int64_t>(U.tsize, 1);
-  c->T.ensure(tbytes + U.up.host.size() + 512);
-  U.ub = c->T.as<char>() + ((tbytes + 255) & ~size_t(255));
-  h2d(c, U.ub, U.up.host.data(), U.up.host.size());
+  if (!sub) {
+    c->T.ensure(tbytes + U.up.host.size() + 512);
+    U.ub = c->T.as<char>() + ((tbytes + 255) & ~size_t(255));
+    h2d(c, U.ub, U.up.host.data(), U.up.host.size());
+  }
   CU(cudaMemsetAsync(c->T.p, 0, tbytes, c->stream));
   char* ub = U.ub;
   UpdateArgs ua{};
@@ -866,6 +910,10 @@ void launch_update_plan(nrg_ctx* c, Timer& tm, UpdatePlan& U) {
   ua.group_count = (const int*)(ub + U.o_gc); ua.ngroups = (int)U.gfirst.size(); ua.jobs = (const RotJob*)(ub + U.o_jobs);
   ua.Z = c->Z.as<double>(); ua.Zt = c->Zt.as<double>(); ua.T = c->T.as<double>();
   ua.old_ops = (const double* const*)(ub + U.o_old); ua.new_ops = (double* const*)(ub + U.o_new);
+  if (sub) {
+    ua.Z = sub->Z; ua.Zt = sub->Zt; ua.old_ops = sub->old_tab; ua.new_ops = sub->new_tab;
+    if (!sub->site_terms) ua.ngroups = 0;
+  }
   ua.tile_job = (const int*)(ub + U.o_tj); ua.tile_mn = (const int*)(ub + U.o_tm); ua.ntiles = (int)U.tjob.size();
   ua.terms1 = (const GatherTerm*)(ub + U.o_t1); ua.group1_first = (const int*)(ub + U.o_g1f);
   ua.group1_count = (const int*)(ub + U.o_g1c); ua.tile1_group = (const int*)(ub + U.o_t1g);
@@ -876,6 +924,46 @@ void launch_update_plan(nrg_ctx* c, Timer& tm, UpdatePlan& U) {
   for (const RotJob& J : U.jobs) c->timing.update_flops += 2.0 * J.ki * (double)J.nI * J.kj;
   tm.stop(tu, &c->timing.update_ms);
 }
+
+// Grouped FP64 GEMM jobs (gemm_jobs_kernel): one 64 x 64 tile per CTA.
+struct GemmPlan {
+  std::vector<GemmJob> jobs;
+  std::vector<int> tjob, tmn;
+  void add(const GemmJob& J) {
+    const int id = (int)jobs.size();
+    jobs.push_back(J);
+    for (int mt = 0; mt * 64 < J.m; ++mt)
+      for (int nt = 0; nt * 64 < J.n; ++nt) { tjob.push_back(id); tmn.push_back((mt << 16) | nt); }
+  }
+};
+
+void run_gemm_plan(nrg_ctx* c, const GemmPlan& G) {
+  if (G.jobs.empty()) return;
+  Packer pk;
+  size_t oj = pk.add(G.jobs), ot = pk.add(G.tjob), om = pk.add(G.tmn);
+  c->vmeta.ensure(pk.host.size() + 256);
+  h2d(c, c->vmeta.p, pk.host.data(), pk.host.size());
+  char* b = c->vmeta.as<char>();
+  launch_gemm_jobs((const GemmJob*)(b + oj), (const int*)(b + ot), (const int*)(b + om), (int)G.tjob.size(), c->stream);
+  c->launches++;
+}
+
+// The tangent pass of nrg_grad_forward: for each of the four parameters
+// (eps_d, U, Gamma, B) the tangents of the kept energies and of the
+// operators, carried from iteration to iteration beside the primal sweep
+// (ping-pong buffers like the primal operators), the scratch of the
+// eigen-derivatives, and the per-iteration results.
+struct TangentState {
+  static constexpr int NP = 4;
+  double params[NP] = {0, 0, 0, 0};     // eps_d, U, Gamma, B of the sweep
+  DevBuf dEk[NP][2], dops[NP][2][6];
+  DevBuf deold, dH, T1, dHt, C, dZ, dZt, dlam, dEall, tmp[3][6], gscaled[6], tabs, part, out;
+  // per iteration n and parameter k (index n * NP + k): tangents of the
+  // thermodynamic values (the 16 of nrg_iteration.thermo), of the operator
+  // averages, and of the raw lowest level (lambda_min, before SetE0zero)
+  std::vector<double> dthermo, dopavg, dlmin;
+  int nops = 0;
+};
 
 // dm: NRG_main with the spectral density switched on (calcdens = 1,
 // UpdateBefCut = 1; CodeHandler_ModelSwitch.cpp:162-176, NRG_main.cpp:334-396):
@@ -888,7 +976,8 @@ void launch_update_plan(nrg_ctx* c, Timer& tm, UpdatePlan& U) {
 // 940-1000): H_0 is the first site alone (Nsites0 = 1), its thermodynamics
 // are taken before the loop at D_0 (NRG_main.cpp:242-255), and iteration N =
 // 1 .. nsites-1 adds site N with hopping chi_{N-1}.  Only f_N is carried.
-void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool chain = false) {
+void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool chain = false,
+               TangentState* tan = nullptr) {
   using clock = std::chrono::steady_clock;
   auto t_begin = clock::now();
   if (cfg->model < 0 || cfg->model > 5) throw NrgError(NRG_ERR_ARG, "unknown model");
@@ -987,6 +1076,32 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
       c->opavg_m1.push_back(opavg_host(st.blk, st.en, diag, m.totalS, betabar));
     }
   }
+
+  // Tangents at H_{-1}: its levels are linear in eps_d, U and B (no shift is
+  // applied to them), its operators do not depend on the parameters, and
+  // Gamma enters through chi_{-1} at iteration 0.
+  const bool fullvec = dm || tan;
+  if (tan) {
+    if (chain || dm || (m.kind != MODEL_1CHQS && m.kind != MODEL_1CHQSZ))
+      throw NrgError(NRG_ERR_ARG, "derivatives are built for the one-channel |Q S> and |Q Sz> Anderson sweeps");
+    const StartState s0 = make_start(m, lambda, 0.0, 0.0, 0.0);
+    const StartState sd[3] = {make_start(m, lambda, 0.0, 1.0, 0.0), make_start(m, lambda, 1.0, 0.0, 0.0),
+                              make_start(m, lambda, 0.0, 0.0, 1.0)};
+    tan->params[0] = cfg->ed; tan->params[1] = cfg->U; tan->params[2] = cfg->gamma1; tan->params[3] = cfg->gamma2_or_B;
+    tan->dthermo.clear(); tan->dopavg.clear(); tan->dlmin.clear();
+    for (int p = 0; p < TangentState::NP; ++p) {
+      std::vector<double> de(st.en.size(), 0.0);
+      if (p != 2)
+        for (size_t k = 0; k < de.size(); ++k) de[k] = sd[p == 3 ? 2 : p].en[k] - s0.en[k];
+      tan->dEk[p][0].ensure(sizeof(double) * std::max<size_t>(de.size(), 1));
+      h2d(c, tan->dEk[p][0].p, de.data(), sizeof(double) * de.size());
+      for (int o = 0; o < nops; ++o) {
+        tan->dops[p][0][o].ensure(sizeof(double) * std::max<int64_t>(S.ops[o].size, 1));
+        CU(cudaMemsetAsync(tan->dops[p][0][o].p, 0, sizeof(double) * std::max<int64_t>(S.ops[o].size, 1), c->stream));
+      }
+    }
+  }
+  int tcur = 0;  // which tangent ping-pong buffer holds the current tangents
 
   // The chain: Wilson's (SetChainWilson: e_N = 0) or the caller's
   // (nrg_set_chain); iteration N uses hop(N-1) (chi_{-1} at N = 0) and
@@ -1107,18 +1222,18 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
     for (int x : K.blk.size) R.kept_bsize.push_back(x);
     // ---------------- kept eigenvectors
     P.nvec.assign(nb, 0);
-    for (int b = 0; b < nb; ++b) P.nvec[b] = dm ? P.bsize[b] : keptb[b];
+    for (int b = 0; b < nb; ++b) P.nvec[b] = fullvec ? P.bsize[b] : keptb[b];
     // eigenvalues for clustering: shifted energies have the same gaps
     run_vectors(c, tm, P, R.en, aa.bsize, aa.hoff, aa.bstate);
     // ---------------- UpdateMatrices
     UpdatePlan U;
-    Kept Kfull;  // UpdateBefCut: rotate into every state of H_N
-    if (dm) {
+    Kept Kfull;  // UpdateBefCut (and the tangent pass): the layout of every state of H_N
+    if (fullvec) {
       Kfull.blk = B.blk;
       for (int b = 0; b < nb; ++b) Kfull.src.push_back(b);
     }
-    plan_update(U, m, B, P, dm ? Kfull : K, S.ops, opblock.empty() ? nullptr : &opblock, &opsize,
-                dm ? &keptb : nullptr);
+    plan_update(U, m, B, P, fullvec ? Kfull : K, S.ops, opblock.empty() ? nullptr : &opblock, &opsize,
+                fullvec ? &keptb : nullptr);
     std::vector<OpMeta>& newops = U.newops;
     const int nk = K.blk.nblocks();
     int nxt = 1 - S.cur;
@@ -1128,7 +1243,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
       b->ensure(sizeof(double) * std::max<int64_t>(newops[o].size, 1));
       newptr[o] = b->as<double>();
       oldptr[o] = S.opbuf(S.cur, o)->as<double>();
-      if (dm && m.op_kind[o] != OP_CD_QS && m.op_kind[o] != OP_CD_2CH)  // only the kept part is computed
+      if (fullvec && m.op_kind[o] != OP_CD_QS && m.op_kind[o] != OP_CD_2CH)  // only the kept part is computed
         CU(cudaMemsetAsync(newptr[o], 0, sizeof(double) * newops[o].size, c->stream));
     }
     Packer& up = U.up;
@@ -1143,16 +1258,23 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
     std::vector<const double*> avgptr;
     for (int o : avg_ops) {
       avgptr.push_back(newptr[o]);
-      for (int i = 0; i < nk; ++i) { int k = newops[o].find(i, i); diag_off.push_back(k >= 0 ? newops[o].off[k] : -1); }
+      for (int i = 0; i < nk; ++i) {  // full layout: the kept block's own block of H_N
+        const int bi = fullvec ? K.src[i] : i;
+        const int k = newops[o].find(bi, bi);
+        diag_off.push_back(k >= 0 ? newops[o].off[k] : -1);
+      }
     }
+    std::vector<int> kld(nk);  // row stride of each kept block's diagonal operator block
+    for (int i = 0; i < nk; ++i) kld[i] = fullvec ? P.bsize[K.src[i]] : K.blk.size[i];
     size_t o_ksb = up.add(kstate_block), o_ksz = up.add(ksz), o_koff = up.add(koff), o_doff = up.add(diag_off),
-           o_avp = up.add(avgptr), o_kq = up.add(K.blk.qn);
+           o_avp = up.add(avgptr), o_kq = up.add(K.blk.qn), o_kld = up.add(kld);
     launch_update_plan(c, tm, U);
     char* ub = U.ub;
     // ---------------- CalcStuff: operator averages over the kept states
     cudaEvent_t to = tm.start();
     OpDiagArgs od{};
     od.nblocks = nk; od.ksize = (const int*)(ub + o_ksz); od.koff = (const int*)(ub + o_koff);
+    od.kld = (const int*)(ub + o_kld);
     od.ken = (const double*)(ub + o_ken); od.bq = (const double*)(ub + o_kq); od.totalS = m.totalS ? 1 : 0;
     od.beta = betabar; od.nops = (int)avg_ops.size(); od.ops = (const double* const*)(ub + o_avp);
     od.diag_off = (const int64_t*)(ub + o_doff); od.out = c->scal.as<double>() + 24;
@@ -1170,6 +1292,157 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
       if (!(std::fabs(Zk) < 1.e-20)) s = s / Zk;
       R.opavg.push_back(s);
     }
+    // ---------------- tangents of this iteration (nrg_grad_forward)
+    if (tan) {
+      TangentState& TS = *tan;
+      const int NP = TangentState::NP;
+      TS.nops = (int)avg_ops.size();
+      // host tables: kept states, coupling-matrix offsets, pointer tables
+      std::vector<int> kept_state;
+      for (int i = 0; i < nk; ++i)
+        for (int x = 0; x < K.blk.size[i]; ++x) kept_state.push_back(P.soff[K.src[i]] + x);
+      std::vector<int64_t> coff(nb);
+      int64_t csz = 0;
+      for (int b = 0; b < nb; ++b) { coff[b] = csz; csz += (int64_t)P.bsize[b] * keptb[b]; }
+      int gs = 0;
+      for (int g = 1; g < P.nstates; ++g) if (R.en[g] < R.en[gs]) gs = g;
+      const int nkept = (int)kept_state.size();
+      TS.deold.ensure(sizeof(double) * std::max(P.nstates, 1));
+      for (DevBuf* b : {&TS.dH, &TS.T1, &TS.dHt}) b->ensure(sizeof(double) * std::max<int64_t>(P.hsize, 1));
+      TS.C.ensure(sizeof(double) * std::max<int64_t>(csz, 1));
+      TS.dZ.ensure(sizeof(double) * std::max<int64_t>(P.ysize, 1));
+      TS.dZt.ensure(sizeof(double) * std::max<int64_t>(P.ysize, 1));
+      TS.dlam.ensure(sizeof(double) * std::max(P.nstates, 1));
+      TS.dEall.ensure(sizeof(double) * std::max(P.nstates, 1));
+      for (int r = 0; r < 3; ++r)
+        for (int o = 0; o < nops; ++o) TS.tmp[r][o].ensure(sizeof(double) * std::max<int64_t>(newops[o].size, 1));
+      for (int p = 0; p < NP; ++p) {
+        TS.dEk[p][1 - tcur].ensure(sizeof(double) * std::max(nkept, 1));
+        for (int o = 0; o < nops; ++o)
+          TS.dops[p][1 - tcur][o].ensure(sizeof(double) * std::max<int64_t>(newops[o].size, 1));
+      }
+      // iteration 0, Gamma: chi_{-1} is proportional to sqrt(Gamma), so the
+      // coupling's tangent is the primal coupling over 2 Gamma
+      const bool gamma_term = N == 0 && !(std::fabs(cfg->gamma1) == 0.0);
+      if (gamma_term)
+        for (int o = 0; o < nops_h; ++o) {
+          TS.gscaled[o].ensure(sizeof(double) * std::max<int64_t>(S.ops[o].size, 1));
+          launch_tan_scale(S.opbuf(S.cur, o)->as<double>(), 0.5 / cfg->gamma1, S.ops[o].size,
+                           TS.gscaled[o].as<double>(), c->stream);
+        }
+      // pointer tables: per parameter the tangent old operators (8) and new
+      // ones (8), then the three rotation outputs (8 each), the Gamma-scaled
+      // couplings (8), and per parameter the averaged operators' tangents (8)
+      std::vector<const double*> ptrs;
+      for (int p = 0; p < NP; ++p) {
+        for (int o = 0; o < 8; ++o) ptrs.push_back(o < nops ? TS.dops[p][tcur][o].as<double>() : nullptr);
+        for (int o = 0; o < 8; ++o) ptrs.push_back(o < nops ? TS.dops[p][1 - tcur][o].as<double>() : nullptr);
+      }
+      for (int r = 0; r < 3; ++r)
+        for (int o = 0; o < 8; ++o) ptrs.push_back(o < nops ? TS.tmp[r][o].as<double>() : nullptr);
+      for (int o = 0; o < 8; ++o) ptrs.push_back(gamma_term && o < nops_h ? TS.gscaled[o].as<double>() : nullptr);
+      for (int p = 0; p < NP; ++p)
+        for (int k = 0; k < 8; ++k)
+          ptrs.push_back(k < (int)avg_ops.size() ? TS.dops[p][1 - tcur][avg_ops[k]].as<double>() : nullptr);
+      Packer tp;
+      const size_t o_ptr = tp.add(ptrs), o_kst = tp.add(kept_state), o_coff = tp.add(coff), o_nkeep = tp.add(keptb),
+                   o_stcf = tp.add(B.stcf);
+      TS.tabs.ensure(tp.host.size() + 256);
+      h2d(c, TS.tabs.p, tp.host.data(), tp.host.size());
+      char* tb = TS.tabs.as<char>();
+      const double* const* dptr = (const double* const*)(tb + o_ptr);
+      auto tab_old = [&](int p) { return dptr + 16 * p; };
+      auto tab_tmp = [&](int r) { return dptr + 16 * NP + 8 * r; };
+      const double* const* tab_gamma = dptr + 16 * NP + 24;
+      auto tab_avg = [&](int p) { return dptr + 16 * NP + 32 + 8 * p; };
+      // the eigen-derivative GEMMs of every block (the same for all parameters)
+      GemmPlan G1, G2, G3, G4;
+      for (int b = 0; b < nb; ++b) {
+        const int n = P.bsize[b], kb = keptb[b];
+        const int64_t h = P.hoff[b], y = P.yoff[b];
+        double* Zb = c->Z.as<double>() + y;
+        double* Ztb = c->Zt.as<double>() + y;
+        G1.add(GemmJob{n, n, n, 0, TS.dH.as<double>() + h, n, Ztb, n, TS.T1.as<double>() + h, n});
+        G2.add(GemmJob{n, n, n, 0, Zb, n, TS.T1.as<double>() + h, n, TS.dHt.as<double>() + h, n});
+        if (kb == 0) continue;
+        G3.add(GemmJob{n, kb, n, 0, Ztb, n, TS.C.as<double>() + coff[b], kb, TS.dZt.as<double>() + y, n});
+        G4.add(GemmJob{kb, n, n, 1, TS.C.as<double>() + coff[b], kb, Zb, n, TS.dZ.as<double>() + y, n});
+      }
+      TS.part.ensure(sizeof(double) * tan_partial_doubles());
+      TS.out.ensure(sizeof(double) * TanSumArgs::kMaxOut * NP + 64);
+      std::vector<double> sums((size_t)TanSumArgs::kMaxOut * NP), dl(NP);
+      for (int p = 0; p < NP; ++p) {
+        // dH_N: the assembly on the tangents of the old energies and operators
+        launch_tan_gather(TS.dEk[p][tcur].as<double>(), (const int*)(tb + o_stcf), P.nstates, TS.deold.as<double>(),
+                          c->stream);
+        AssembleArgs a2 = aa;
+        a2.H = TS.dH.as<double>(); a2.st_eold = TS.deold.as<double>(); a2.eN = 0.0;
+        a2.ops = (gamma_term && p == 2) ? tab_gamma : tab_old(p);
+        launch_assemble(a2, P.nstates, (const int*)(mb + o_sb), (const int*)(mb + AT.o_ri), c->stream);
+        run_gemm_plan(c, G1);
+        run_gemm_plan(c, G2);
+        TanEigArgs te{};
+        te.bsize = aa.bsize; te.soff = aa.bstate; te.hoff = aa.hoff; te.dHt = TS.dHt.as<double>();
+        te.ev = c->ev.as<double>(); te.nkeep = (const int*)(tb + o_nkeep); te.coff = (const int64_t*)(tb + o_coff);
+        te.C = TS.C.as<double>(); te.dlam = TS.dlam.as<double>(); te.degen_tol = 1e-10;
+        launch_tan_eig(te, nb, c->stream);
+        run_gemm_plan(c, G3);
+        run_gemm_plan(c, G4);
+        launch_tan_shift(TS.dlam.as<double>(), P.nstates, gs, TS.dEall.as<double>(), (const int*)(tb + o_kst), nkept,
+                         TS.dEk[p][1 - tcur].as<double>(), c->stream);
+        // dO_new = dZ_I F Z_J^T + Z_I F dZ_J^T + Z_I dF Z_J^T
+        for (int r = 0; r < 3; ++r)
+          for (int o = 0; o < nops; ++o)
+            CU(cudaMemsetAsync(TS.tmp[r][o].p, 0, sizeof(double) * newops[o].size, c->stream));
+        const double* const* old_primal = (const double* const*)(ub + U.o_old);
+        UpdateInputs u1{TS.dZ.as<double>(), c->Zt.as<double>(), old_primal, (double* const*)tab_tmp(0), true};
+        UpdateInputs u2{c->Z.as<double>(), TS.dZt.as<double>(), old_primal, (double* const*)tab_tmp(1), true};
+        UpdateInputs u3{c->Z.as<double>(), c->Zt.as<double>(), tab_old(p), (double* const*)tab_tmp(2), false};
+        launch_update_plan(c, tm, U, &u1);
+        launch_update_plan(c, tm, U, &u2);
+        launch_update_plan(c, tm, U, &u3);
+        for (int o = 0; o < nops; ++o)
+          launch_tan_axpy3(TS.tmp[0][o].as<double>(), TS.tmp[1][o].as<double>(), TS.tmp[2][o].as<double>(), 1.0,
+                           newops[o].size, TS.dops[p][1 - tcur][o].as<double>(), c->stream);
+        // weighted sums of the thermodynamics and operator-average tangents
+        TanSumArgs ts{};
+        ts.nstates = P.nstates; ts.state_block = (const int*)(mb + o_sb); ts.bq = (const double*)(mb + o_bq);
+        ts.en = c->en.as<double>(); ts.dE = TS.dEall.as<double>(); ts.totalS = m.totalS ? 1 : 0;
+        for (int t = 0; t < 4; ++t) ts.beta[t] = betas[t];
+        ts.nkept = nkept; ts.nkblocks = nk; ts.kstate_block = (const int*)(ub + o_ksb); ts.koff = (const int*)(ub + o_koff);
+        ts.kld = (const int*)(ub + o_kld); ts.kbq = (const double*)(ub + o_kq); ts.ken = (const double*)(ub + o_ken);
+        ts.dEk = TS.dEk[p][1 - tcur].as<double>(); ts.betabar = betabar; ts.nops = (int)avg_ops.size();
+        ts.ops = (const double* const*)(ub + o_avp); ts.dops = tab_avg(p); ts.diag_off = (const int64_t*)(ub + o_doff);
+        launch_tan_sums(ts, TS.part.as<double>(), TS.out.as<double>() + (size_t)p * TanSumArgs::kMaxOut, c->stream);
+        d2h(c, &dl[p], TS.dlam.as<double>() + gs, sizeof(double));
+        c->launches += 14;
+      }
+      d2h(c, sums.data(), TS.out.p, sizeof(double) * sums.size());
+      CU(cudaStreamSynchronize(c->stream));
+      check_flag(c);
+      tm.collect();
+      // derivatives of the reported values from the sums (CalcSuscep,
+      // CalcEntropy and CalcOpAvg differentiated: d e^{-beta E} = -beta e^{-beta E} dE)
+      for (int p = 0; p < NP; ++p) {
+        const double* q = sums.data() + (size_t)p * TanSumArgs::kMaxOut;
+        for (int t = 0; t < 4; ++t) {
+          const double Z = scal[8 + 3 * t], s1 = scal[8 + 3 * t + 1], sE = scal[8 + 3 * t + 2], b = betas[t];
+          const double dZ = -b * q[3 * t], ds1 = -b * q[3 * t + 1], dsE = q[3 * t] - b * q[3 * t + 2];
+          TS.dthermo.push_back(0.0);                                         // beta
+          TS.dthermo.push_back(0.0);                                         // T
+          TS.dthermo.push_back(ds1 / Z - s1 * dZ / (Z * Z));                 // T chi
+          TS.dthermo.push_back(b * (dsE / Z - sE * dZ / (Z * Z)) + dZ / Z);  // S
+        }
+        const double Zk = avg[avg_ops.size()];
+        const double dZk = -betabar * q[TanSumArgs::kMaxOut - 1];
+        for (size_t k = 0; k < avg_ops.size(); ++k) {
+          const double SO = avg[k], dSO = q[12 + 2 * k] - betabar * q[12 + 2 * k + 1];
+          TS.dopavg.push_back(std::fabs(Zk) < 1.e-20 ? 0.0 : dSO / Zk - SO * dZk / (Zk * Zk));
+        }
+        TS.dlmin.push_back(dl[p]);
+      }
+      tcur = 1 - tcur;
+    }
     // ---------------- DM-NRG shell (SaveArrays, NRGcodehandlerClass.cpp:887-932)
     if (dm) {
       auto sh = std::make_unique<DmShell>();
@@ -1186,6 +1459,9 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
                          c->stream));
       sh->basis = std::move(B);
       c->dm.push_back(std::move(sh));
+      opsize = P.bsize;
+      opblock = K.src;
+    } else if (tan) {  // operators stay in the full layout (kept part computed)
       opsize = P.bsize;
       opblock = K.src;
     } else {
@@ -1212,6 +1488,32 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
   c->timing.device_ms = span_ms;
   c->timing.kernel_launches = c->launches - launches0;
   c->timing.total_ms = std::chrono::duration<double, std::milli>(clock::now() - t_begin).count();
+}
+
+// nrg_grad_forward: the sweep with the tangent pass, then the absolute
+// ground-state energy sum_{M<=N} D_M E_min,M (H_N is built from energies
+// already shifted by the earlier E_min and rescaled, so the shifts add up in
+// absolute units) and its tangents.
+void grad_forward_impl(nrg_ctx* c, const nrg_sweep_config* cfg) {
+  if (!c->tan) c->tan = new TangentState();
+  sweep_run(c, cfg, false, false, c->tan);
+  const int NP = TangentState::NP;
+  const int ni = (int)c->iters.size();
+  const double lambda = cfg->lambda, HLF = 0.5 * (1.0 + 1.0 / lambda);
+  c->grad_egs.assign(ni, 0.0);
+  c->grad_degs.assign((size_t)ni * NP, 0.0);
+  c->grad_demin = c->tan->dlmin;
+  double e = 0.0;
+  std::vector<double> de(NP, 0.0);
+  for (int n = 0; n < ni; ++n) {
+    const double DN = HLF * std::pow(lambda, (-(n - 1) / 2.0));
+    e += DN * c->iters[n].emin;
+    c->grad_egs[n] = e;
+    for (int k = 0; k < NP; ++k) {
+      de[k] += DN * c->tan->dlmin[(size_t)n * NP + k];
+      c->grad_degs[(size_t)n * NP + k] = de[k];
+    }
+  }
 }
 
 // ------------------------------------------------------------------ DM-NRG
@@ -1258,27 +1560,6 @@ double dm_partition(const DmShell& s, double beta, bool disc_only) {
   return sum;
 }
 
-struct GemmPlan {
-  std::vector<GemmJob> jobs;
-  std::vector<int> tjob, tmn;
-  void add(const GemmJob& J) {
-    const int id = (int)jobs.size();
-    jobs.push_back(J);
-    for (int mt = 0; mt * 64 < J.m; ++mt)
-      for (int nt = 0; nt * 64 < J.n; ++nt) { tjob.push_back(id); tmn.push_back((mt << 16) | nt); }
-  }
-};
-
-void run_gemm_plan(nrg_ctx* c, const GemmPlan& G) {
-  if (G.jobs.empty()) return;
-  Packer pk;
-  size_t oj = pk.add(G.jobs), ot = pk.add(G.tjob), om = pk.add(G.tmn);
-  c->vmeta.ensure(pk.host.size() + 256);
-  h2d(c, c->vmeta.p, pk.host.data(), pk.host.size());
-  char* b = c->vmeta.as<char>();
-  launch_gemm_jobs((const GemmJob*)(b + oj), (const int*)(b + ot), (const int*)(b + om), (int)G.tjob.size(), c->stream);
-  c->launches++;
-}
 
 // DM_NRG_SetRhoNmax + (RotateMatrix, DM_NRG_CalcRhoN_withSU2) per shell, FDM.
 void dm_backprop_impl(nrg_ctx* c, const nrg_dm_params* prm, double* rho_trace) {
@@ -2427,6 +2708,8 @@ void nrg_destroy(nrg_ctx* ctx) {
   }
   if (ctx->fork) cudaEventDestroy(ctx->fork);
   cudaStreamDestroy(ctx->stream);
+  delete ctx->tan;
+  ctx->tan = nullptr;
   nrg_ctx* chain = ctx->chain_ctx;
   delete ctx;
   nrg_destroy(chain);
@@ -2484,6 +2767,49 @@ nrg_status nrg_sweep_opavg_initial(const nrg_ctx* ctx, int* nops, const double**
 nrg_status nrg_sweep_timing(const nrg_ctx* ctx, nrg_timing* out) {
   if (!ctx || !out) return NRG_ERR_ARG;
   *out = ctx->timing;
+  return NRG_OK;
+}
+
+nrg_status nrg_grad_forward(nrg_ctx* ctx, const nrg_sweep_config* cfg, nrg_grad* out) {
+  if (!ctx || !cfg || !out) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    grad_forward_impl(ctx, cfg);
+  });
+  const nrg::TangentState& T = *ctx->tan;
+  out->nsites = (int)ctx->iters.size();
+  out->nparams = nrg::TangentState::NP;
+  out->nops = T.nops;
+  out->d_thermo = T.dthermo.data();
+  out->d_opavg = T.dopavg.data();
+  out->d_emin = ctx->grad_demin.data();
+  out->egs = ctx->grad_egs.data();
+  out->d_egs = ctx->grad_degs.data();
+  return NRG_OK;
+}
+
+nrg_status nrg_grad_backward(nrg_ctx* ctx, const double* g_thermo, const double* g_opavg, const double* g_egs,
+                             double* grad) {
+  if (!ctx || !grad) return NRG_ERR_ARG;
+  if (!ctx->tan || ctx->grad_egs.size() != ctx->iters.size()) {
+    ctx->err = "nrg_grad_backward needs a preceding nrg_grad_forward on the context";
+    return NRG_ERR_STATE;
+  }
+  const nrg::TangentState& T = *ctx->tan;
+  const int NP = nrg::TangentState::NP, ni = (int)ctx->iters.size(), no = T.nops;
+  for (int k = 0; k < NP; ++k) {
+    double g = 0.0;
+    for (int n = 0; n < ni; ++n) {
+      const size_t r = (size_t)n * NP + k;
+      if (g_thermo)
+        for (int v = 0; v < 16; ++v) g += g_thermo[(size_t)n * 16 + v] * T.dthermo[r * 16 + v];
+      if (g_opavg)
+        for (int o = 0; o < no; ++o) g += g_opavg[(size_t)n * no + o] * T.dopavg[r * no + o];
+      if (g_egs) g += g_egs[n] * ctx->grad_degs[r];
+    }
+    grad[k] = g;
+  }
   return NRG_OK;
 }
 

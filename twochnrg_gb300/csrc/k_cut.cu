@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(kRedThreads) opdiag_partial_kernel(OpDiagArgs 
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nk; i += gridDim.x * blockDim.x) {
     const int b = kstate_block[i];
     const int x = i - A.koff[b];
-    const int kb = A.ksize[b];
+    const int kb = A.kld ? A.kld[b] : A.ksize[b];
     const double deg = A.totalS ? 2.0 * A.bq[2 * b + 1] + 1.0 : 1.0;
     const double w = exp(-A.beta * A.ken[i]);
     for (int o = 0; o < A.nops; ++o) {

@@ -152,6 +152,7 @@ struct TdEigArgs {
   float* fde;            // scratch [2*nstates]: FP32 copies of d and e for the FP32 bracket
   double* e2;            // scratch [nstates]: e^2
   unsigned char* split;  // scratch [nstates]: e_i negligible (the pieces' ends)
+  double split_eps;      // relative size below which e_i counts as zero (<= 0: FP64's unit round-off)
 };
 void launch_bisect(const TdEigArgs& a, const int* state_block, cudaStream_t s);
 
@@ -273,6 +274,7 @@ void launch_update(const UpdateArgs& a, cudaStream_t s);
 struct OpDiagArgs {       // Boltzmann sums of diagonal elements over kept states
   int nblocks;
   const int* ksize;       // kept states per block
+  const int* kld;         // row stride of the block's diagonal operator block (NULL: ksize)
   const int* koff;        // kept state offsets
   const double* ken;      // kept energies
   const double* bq;
@@ -285,6 +287,51 @@ struct OpDiagArgs {       // Boltzmann sums of diagonal elements over kept state
 };
 void launch_opdiag(const OpDiagArgs& a, const int* kstate_block, int nk, double* partial, cudaStream_t s);
 int reduce_partial_count();
+
+// ---------------------------------------------------------------- tangents (k_tangent.cu)
+struct TanEigArgs {      // per block: dlambda = diag(dH~), C = dH~_kl / (lambda_l - lambda_k)
+  const int* bsize;
+  const int* soff;
+  const int64_t* hoff;   // dH~ per block, n x n at hoff
+  const double* dHt;
+  const double* ev;      // levels, ascending per block
+  const int* nkeep;      // kept eigenvectors per block (columns of C)
+  const int64_t* coff;   // C per block, n x nkeep row-major
+  double* C;
+  double* dlam;          // per state
+  double degen_tol;      // relative gap below which two levels do not couple
+};
+void launch_tan_eig(const TanEigArgs& a, int nblocks, cudaStream_t s);
+void launch_tan_shift(const double* dlam, int nstates, int gs, double* dE_all, const int* kept_state, int nkept,
+                      double* dE_kept, cudaStream_t s);
+void launch_tan_gather(const double* dE_kept_old, const int* stcf, int n, double* out, cudaStream_t s);
+void launch_tan_axpy3(const double* a, const double* b, const double* c, double scale, int64_t n, double* out,
+                      cudaStream_t s);
+void launch_tan_scale(const double* a, double scale, int64_t n, double* out, cudaStream_t s);
+struct TanSumArgs {      // weighted sums of the thermodynamics and operator-average tangents
+  static constexpr int kMaxOut = 24;  // 12 thermo sums, 2 per operator (<= 5), the last: sum deg w dE (kept)
+  int nstates;
+  const int* state_block;
+  const double* bq;      // block quantum numbers (Q, S or Sz)
+  const double* en;      // shifted energies
+  const double* dE;      // their tangents
+  int totalS;
+  double beta[4];
+  int nkept, nkblocks;
+  const int* kstate_block;
+  const int* koff;
+  const int* kld;        // row stride of each kept block's diagonal operator block
+  const double* kbq;
+  const double* ken;
+  const double* dEk;
+  double betabar;
+  int nops;
+  const double* const* ops;   // averaged operators (primal) and their tangents
+  const double* const* dops;
+  const int64_t* diag_off;    // [nops * nkblocks]
+};
+size_t tan_partial_doubles();
+void launch_tan_sums(const TanSumArgs& a, double* partial, double* out, cudaStream_t s);
 
 // ---------------------------------------------------------------- DM-NRG
 struct GemmJob {          // C (m x n) = op(A) (m x k) . B (k x n), row-major, FP64
