@@ -66,3 +66,19 @@ def test_clebsch_gordan_known_values():
     assert abs(cg(0.5, -0.5, 0.5, 0.5, 0.0, 0.0) + np.sqrt(0.5)) < 1e-15
     assert abs(cg(1.0, 1.0, 0.5, -0.5, 0.5, 0.5) - np.sqrt(2.0 / 3.0)) < 1e-15
     assert cg(1.0, 1.0, 1.0, 1.0, 1.0, 1.0) == 0.0
+
+
+def test_oracle_matches_reference_full_size_start():
+    """The headline workload (two channels, 3000 kept): the oracle's first
+    three iterations against the reference's own (fixture made by the
+    reference routines; iterations 3-4 at full size are checked on the GPU
+    and by the bench's CPU sample, minutes each on one core)."""
+    g = np.load(os.path.join(GOLD, "cfg1_2chQS_n5_k3000.npz"))
+    o = orc.run("2chQS", 3, 3000, 2.5, 0.3, -0.15, 0.01, 0.01, nthreads=min(8, os.cpu_count() or 1))
+    for n, it in enumerate(o.iters):
+        np.testing.assert_array_equal(it.bsize, g[f"bsize_{n}"])
+        assert it.nkept == int(g[f"nkept_{n}"])
+        np.testing.assert_array_equal(it.kept_bsize, g[f"kept_bsize_{n}"])
+        np.testing.assert_allclose(it.en, g[f"en_{n}"], rtol=0, atol=1e-12 * max(1.0, np.abs(it.en).max()))
+        np.testing.assert_allclose(it.thermo, g[f"thermo_{n}"], rtol=1e-12)
+        np.testing.assert_allclose(it.opavg, g[f"opavg_{n}"], rtol=1e-12, atol=1e-14)
