@@ -527,11 +527,6 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
   ea.e2 = c->e2.as<double>();
   c->spl.ensure(std::max(P.nstates, 1));
   ea.split = c->spl.as<unsigned char>();
-  // mixed precision: the tensor-core trailing updates leave residues of order
-  // 2^-36 of the block's scale where the FP64 reduction leaves round-off, so
-  // the tridiagonal falls apart at that level (an eigenvalue moves by at most
-  // that much, inside the mixed form's 1e-9)
-  ea.split_eps = mixed ? 0x1p-34 : 0.0;
   cudaEvent_t t1 = tm.start();
   launch_bisect(ea, d_state_block, c->stream);
   c->launches += 3;  // FP32 copies, levels, ordering

@@ -110,9 +110,9 @@ __device__ __forceinline__ double pair_step(double S1, double S2, bool above, in
 // e_i is negligible next to its diagonal neighbours (the splitting test of
 // LAPACK's tridiagonal solvers): the block then falls apart into unreduced
 // pieces whose eigenvalues are simple.
-__device__ __forceinline__ bool split_at(const double* d, const double* e, int i, double eps) {
+__device__ __forceinline__ bool split_at(const double* d, const double* e, int i) {
   const double ei = e[i];
-  return ei * ei <= (eps * eps) * fabs(d[i] * d[i + 1]) || ei == 0.0;
+  return ei * ei <= (kEps * kEps) * fabs(d[i] * d[i + 1]) || ei == 0.0;
 }
 
 // One thread per diagonal position k of each tridiagonal block: the piece
@@ -482,19 +482,19 @@ __global__ void __launch_bounds__(kBackWarps * 32) backtransform_kernel(BackArgs
 // FP32 copies of d and e for the FP32 bracket, e^2 for the FP64 passes, and
 // the splitting test at every position (the last state of a block has e = 0).
 __global__ void prep_levels_kernel(const double* d, const double* e, float* out, double* e2, unsigned char* spl,
-                                   int n, double eps) {
+                                   int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     out[i] = (float)d[i];
     out[n + i] = (float)e[i];
     e2[i] = e[i] * e[i];
-    spl[i] = (i + 1 < n) ? (split_at(d, e, i, eps) ? 1 : 0) : 1;
+    spl[i] = (i + 1 < n) ? (split_at(d, e, i) ? 1 : 0) : 1;
   }
 }
 
 void launch_bisect(const TdEigArgs& a, const int* state_block, cudaStream_t s) {
   if (a.nstates <= 0) return;
   prep_levels_kernel<<<(a.nstates + 255) / 256 < 1024 ? (a.nstates + 255) / 256 : 1024, 256, 0, s>>>(
-      a.d, a.e, a.fde, a.e2, a.split, a.nstates, a.split_eps > 0.0 ? a.split_eps : kEps);
+      a.d, a.e, a.fde, a.e2, a.split, a.nstates);
   // One warp per CTA: the long-running threads of the largest blocks then
   // spread over all SMs instead of crowding a few.
   bisect_kernel<<<(a.nstates + 31) / 32, 32, 0, s>>>(a, state_block);

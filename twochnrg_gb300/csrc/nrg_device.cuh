@@ -152,7 +152,6 @@ struct TdEigArgs {
   float* fde;            // scratch [2*nstates]: FP32 copies of d and e for the FP32 bracket
   double* e2;            // scratch [nstates]: e^2
   unsigned char* split;  // scratch [nstates]: e_i negligible (the pieces' ends)
-  double split_eps;      // relative size below which e_i counts as zero (<= 0: FP64's unit round-off)
 };
 void launch_bisect(const TdEigArgs& a, const int* state_block, cudaStream_t s);
 
