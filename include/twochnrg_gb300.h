@@ -398,6 +398,112 @@ nrg_status nrg_dm_backprop(nrg_ctx* ctx, const nrg_dm_params* prm, double* rho_t
 nrg_status nrg_lehmann(nrg_ctx* ctx, const nrg_dm_params* prm, int nomega, const double* omegas, double* omega_rhow,
                        int* nout);
 
+/* ---- model plug-in -----------------------------------------------------
+ * A model supplied by the caller, without rebuilding the engine: the
+ * reference's per-model function pointers of CNRGmatrix (CalcHNMatEl,
+ * CalcMatEl, CheckForMatEl; include/NRGclasses.hpp:612-634, assigned per
+ * model in src/CodeHandler_ModelSwitch.cpp:131-640), its SetSingleSite and
+ * its H_{-1} set-up, as tables and callbacks.  The engine calls the
+ * callbacks on the host while it builds each iteration's tables (once per
+ * distinct argument set; results are cached for the sweep) and assembles
+ * H_N and updates the operators on the device from those tables.
+ *
+ * H_N element between new states i (site type t_i, from old state a_i) and j
+ * (t_j, a_j), i < j, with O_o the old operators entering H_N and
+ * c(o, dir) = hn_coef(user, S, t_i, t_j, channel, sigma, dir) for the block's
+ * second quantum number S (the rule is taken for (t_i, t_j) and read as
+ * O(a_i, a_j), dir 0, or -- when that element is below 1e-20 in magnitude --
+ * as O(a_j, a_i), dir 1, as the reference's HN rules do):
+ *   NRG_HN_ONE_OP      (chi_1 O_0) c(0)                         one operator
+ *   NRG_HN_SPIN_SUM    (sum_{s=0,1} c(s) O_s) chi_1             O_0, O_1 (channel 0, sigma s)
+ *   NRG_HN_CHANNEL_SUM sum_{ch=0,1} [(chi_ch O_ch) c(ch,0) + (chi_ch O_ch) c(ch,1)]
+ * with IEEE products and sums in that order (the reference's evaluation
+ * orders of OneChQS_HN_MatEl, OneChQSz_HN_MatEl and TwoChQS_HN_MatEl).  The
+ * diagonal is sqrt(Lambda) E_old(a_i), plus e_N (Q_site(t_i) + 1) with
+ * `onsite`.
+ *
+ * Operators (the first hn_ops -- 1 for NRG_HN_ONE_OP, else 2 -- enter H_N):
+ *   NRG_OP_SITE           acts on the new site (f_N): F(i, j) = op_factor(user,
+ *                         o, S_i, S_j, t_i, t_j) between states of the same old state
+ *   NRG_OP_IMPURITY       an old operator recoupled across the site (c_d):
+ *                         F(i, j) = op_factor(...) O_old(a_i, a_j)
+ *   NRG_OP_IMPURITY_DIAG  an old operator times the site identity (n_d, S_z):
+ *                         F(i, j) = [t_i == t_j] O_old(a_i, a_j); op_factor is not called
+ * and the new O(i, j) blocks are kept only for block pairs with
+ * op_check(user, o, qn_i, qn_j) != 0 (qn: the two quantum numbers of each
+ * kept block).  op_avg[o] = 1 reports <O_o> per iteration (CalcOpAvg).
+ *
+ * Site basis: site_nblocks blocks of site_bsize states with site_nqn
+ * quantum numbers: (Q, S, S_z) with total_spin (SU(2) multiplets; BuildBasis
+ * couples S_old and S_site by the triangle rule), else (Q, S_z) added.
+ * Types t are the site states in block order.
+ *
+ * H_{-1}: start_nblocks kept blocks (Q, S or S_z), their sizes and levels
+ * (in units of Lambda (1 + 1/Lambda)/2, as the reference's *_SetAnderson_Hm1
+ * leave them), and per operator start_npairs[o] block pairs
+ * (start_pairs: bi, bj per pair, all operators concatenated) with their
+ * dense row-major blocks concatenated in start_el.
+ *
+ * nrg_sweep_run_model runs the sweep of nrg_sweep_run with this model
+ * (cfg->model is ignored; gamma1 and, with two channels, gamma2_or_B give
+ * chi_{-1}); results through nrg_sweep_iteration.  The superconducting-lead
+ * pairing term, DM-NRG shells, the free chain and derivatives are available
+ * for the built-in models only.  A callback returning a non-finite value, a
+ * malformed description or a basis with no states returns NRG_ERR_ARG. */
+typedef double (*nrg_hn_coef_fn)(void* user, double s_block, int ti, int tj, int channel, int sigma, int dir);
+typedef double (*nrg_op_factor_fn)(void* user, int op, double s_i, double s_j, int ti, int tj);
+typedef int (*nrg_op_check_fn)(void* user, int op, const double* qn_i, const double* qn_j);
+
+enum { NRG_HN_ONE_OP = 0, NRG_HN_SPIN_SUM = 1, NRG_HN_CHANNEL_SUM = 2 };
+enum { NRG_OP_SITE = 0, NRG_OP_IMPURITY = 1, NRG_OP_IMPURITY_DIAG = 2 };
+
+typedef struct {
+  int total_spin;
+  int site_nqn;              /* 3 with total_spin (Q, S, S_z), else 2 (Q, S_z) */
+  int site_nblocks;
+  const double* site_qn;     /* [site_nblocks * site_nqn] */
+  const int* site_bsize;     /* [site_nblocks] */
+  int hn_form;               /* NRG_HN_* */
+  int onsite;                /* 1: the diagonal adds e_N (Q_site + 1) */
+  nrg_hn_coef_fn hn_coef;
+  int nops;                  /* 1 .. 8 */
+  const int* op_class;       /* [nops] NRG_OP_* */
+  const int* op_avg;         /* [nops] 1: <O> reported */
+  nrg_op_factor_fn op_factor;
+  nrg_op_check_fn op_check;
+  int start_nblocks;
+  const double* start_qn;    /* [2 * start_nblocks] */
+  const int* start_bsize;    /* [start_nblocks] */
+  const double* start_en;    /* [sum of start_bsize] */
+  const int* start_npairs;   /* [nops] */
+  const int* start_pairs;    /* [2 * sum of start_npairs] */
+  const double* start_el;    /* the pairs' blocks */
+  void* user;                /* passed to every callback */
+} nrg_model_desc;
+
+nrg_status nrg_sweep_run_model(nrg_ctx* ctx, const nrg_sweep_config* cfg, const nrg_model_desc* model);
+
+/* The tables the device assembly and operator update read, built on the host
+ * (no device needed) for a built-in model (desc NULL, model = nrg_model) or
+ * a described one (desc non-NULL, model ignored):
+ *   nrg_model_hn_table  coefficient table of a block of second quantum
+ *                       number s_block: entry ((ti ntypes + tj) nchan nsigma +
+ *                       channel nsigma + sigma) 2 + dir; *n receives its length
+ *                       (ntypes^2 nchan nsigma 2), written when cap >= *n
+ *   nrg_model_op_factor site factor of operator op (F between site types ti,
+ *                       tj in blocks of spin s_i, s_j); 1/0 for n_d-like operators
+ *   nrg_model_op_check  CheckForMatEl of operator op between kept blocks of
+ *                       quantum numbers qn_i, qn_j (two each); *out 0 or 1 */
+nrg_status nrg_model_hn_table(int model, const nrg_model_desc* desc, double s_block, double* coef, int cap, int* n);
+nrg_status nrg_model_op_factor(int model, const nrg_model_desc* desc, int op, double s_i, double s_j, int ti, int tj,
+                               double* out);
+nrg_status nrg_model_op_check(int model, const nrg_model_desc* desc, int op, const double* qn_i,
+                              const double* qn_j, int* out);
+
+/* Clebsch-Gordan coefficient <j1 m1; j2 m2 | j m> (the reference's CGordan,
+ * src/CGordan.cpp:34-120), for plug-in rules; 0 outside the triangle. */
+double nrg_clebsch(double j1, double m1, double j2, double m2, double j, double m);
+
 /* ---- thermodynamics with the free-chain subtraction --------------------
  * The reference computes the impurity T chi and S in two NRG_main runs
  * (calcdens = 3, then 2): the free Wilson chain first, written to

@@ -1,0 +1,98 @@
+"""Models supplied through the plug-in boundary (nrg_sweep_run_model): the
+built-in one-channel models restated in Python (plugin_models.py) must pass
+the same parity tests as the built-in ones -- the reference's golden
+fixtures with the tolerances of test_gpu_sweep.py -- and give the built-in
+sweep's results bit for bit (their tables are identical)."""
+import os
+
+import numpy as np
+import pytest
+
+import plugin_models as pm
+import twochnrg_gb300 as tg
+from test_gpu_sweep import GOLD, compare
+
+pytestmark = pytest.mark.gpu
+
+
+def _fixture(name):
+    g = np.load(os.path.join(GOLD, name + ".npz"))
+
+    class Ref:
+        iters = []
+
+    for n in range(int(g["niters"])):
+        class It:
+            pass
+        it = It()
+        it.qn, it.bsize, it.en = g[f"qn_{n}"], g[f"bsize_{n}"], g[f"en_{n}"]
+        it.nkept, it.ecut = int(g[f"nkept_{n}"]), float(g[f"ecut_{n}"])
+        it.kept_bsize, it.thermo, it.opavg = g[f"kept_bsize_{n}"], g[f"thermo_{n}"], g[f"opavg_{n}"]
+        Ref.iters.append(it)
+    return g["config"], Ref
+
+
+def _same(a, b):
+    assert len(a.iters) == len(b.iters)
+    for x, y in zip(a.iters, b.iters):
+        np.testing.assert_array_equal(x.qn, y.qn)
+        np.testing.assert_array_equal(x.bsize, y.bsize)
+        np.testing.assert_array_equal(x.en, y.en)
+        np.testing.assert_array_equal(x.kept_bsize, y.kept_bsize)
+        np.testing.assert_array_equal(x.thermo, y.thermo)
+        np.testing.assert_array_equal(x.opavg, y.opavg)
+        assert x.nkept == y.nkept and x.ecut == y.ecut and x.emin == y.emin
+
+
+def test_plugin_qs_matches_reference_fixture(engine):
+    cfg, ref = _fixture("cfg0_1chQS_n40_k500")
+    model, ns, nc, lam, U, ed, g1, _ = cfg[:8]
+    assert str(model) == "1chQS"
+    plug = pm.one_channel_qs(float(U), float(ed), float(lam))
+    r = engine.sweep_model(plug, int(ns), int(nc), float(lam), float(g1))
+    compare(r, ref, "1chQS")
+    b = engine.sweep("1chQS", int(ns), int(nc), float(lam), float(U), float(ed), float(g1))
+    _same(r, b)
+
+
+def test_plugin_qsz_matches_reference_fixture(engine):
+    cfg, ref = _fixture("qsz_1chQSz_n14_k300")
+    model, ns, nc, lam, U, ed, g1, B = cfg[:8]
+    assert str(model) == "1chQSz"
+    plug = pm.one_channel_qsz(float(U), float(ed), float(B), float(lam))
+    r = engine.sweep_model(plug, int(ns), int(nc), float(lam), float(g1))
+    compare(r, ref, "1chQSz")
+    b = engine.sweep("1chQSz", int(ns), int(nc), float(lam), float(U), float(ed), float(g1), float(B))
+    _same(r, b)
+
+
+def test_plugin_mixed_precision(engine, monkeypatch):
+    """The plug-in model through the mixed form (large-block thresholds
+    lowered so the blocked reduction runs) against the FP64 built-in."""
+    monkeypatch.setenv("NRG_BIG_N", "48")
+    monkeypatch.setenv("NRG_MIXED_N", "48")
+    plug = pm.one_channel_qs(0.5, -0.25, 2.5)
+    r = engine.sweep_model(plug, 12, 300, 2.5, 0.02, precision=tg.PREC_MIXED)
+    b = engine.sweep("1chQS", 12, 300, 2.5, 0.5, -0.25, 0.02)
+    for x, y in zip(r.iters, b.iters):
+        np.testing.assert_array_equal(x.bsize, y.bsize)
+        assert x.nkept == y.nkept
+        assert np.max(np.abs(x.en - y.en)) < 1e-9 * max(1.0, float(np.max(np.abs(y.en))))
+
+
+def test_plugin_errors(engine):
+    plug = pm.one_channel_qs(0.5, -0.25, 2.5)
+    bad = pm.one_channel_qs(0.5, -0.25, 2.5)
+    bad.hn_form = 7
+    with pytest.raises(tg.NRGError):
+        engine.sweep_model(bad, 4, 50, 2.5, 0.02)
+
+    def boom(*a):
+        raise ValueError("rule failed")
+    bad = pm.one_channel_qs(0.5, -0.25, 2.5)
+    bad.hn_coef = boom
+    with pytest.raises(ValueError, match="rule failed"):
+        engine.sweep_model(bad, 4, 50, 2.5, 0.02)
+    # the context stays usable
+    r = engine.sweep_model(plug, 4, 50, 2.5, 0.02)
+    assert len(r.iters) == 4

@@ -279,6 +279,153 @@ class ThermoResult:
         return out
 
 
+# ---- model plug-in (nrg_model_desc) -----------------------------------------
+HN_ONE_OP, HN_SPIN_SUM, HN_CHANNEL_SUM = 0, 1, 2
+OP_SITE, OP_IMPURITY, OP_IMPURITY_DIAG = 0, 1, 2
+_HN_COEF_FN = ctypes.CFUNCTYPE(ctypes.c_double, ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                               ctypes.c_int, ctypes.c_int, ctypes.c_int)
+_OP_FACTOR_FN = ctypes.CFUNCTYPE(ctypes.c_double, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                 ctypes.c_int, ctypes.c_int)
+_OP_CHECK_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                ctypes.POINTER(ctypes.c_double))
+
+
+class _ModelDesc(ctypes.Structure):
+    _fields_ = [("total_spin", ctypes.c_int), ("site_nqn", ctypes.c_int), ("site_nblocks", ctypes.c_int),
+                ("site_qn", ctypes.POINTER(ctypes.c_double)), ("site_bsize", ctypes.POINTER(ctypes.c_int)),
+                ("hn_form", ctypes.c_int), ("onsite", ctypes.c_int), ("hn_coef", _HN_COEF_FN),
+                ("nops", ctypes.c_int), ("op_class", ctypes.POINTER(ctypes.c_int)),
+                ("op_avg", ctypes.POINTER(ctypes.c_int)), ("op_factor", _OP_FACTOR_FN),
+                ("op_check", _OP_CHECK_FN), ("start_nblocks", ctypes.c_int),
+                ("start_qn", ctypes.POINTER(ctypes.c_double)), ("start_bsize", ctypes.POINTER(ctypes.c_int)),
+                ("start_en", ctypes.POINTER(ctypes.c_double)), ("start_npairs", ctypes.POINTER(ctypes.c_int)),
+                ("start_pairs", ctypes.POINTER(ctypes.c_int)), ("start_el", ctypes.POINTER(ctypes.c_double)),
+                ("user", ctypes.c_void_p)]
+
+
+@dataclass
+class ModelPlugin:
+    """A model supplied from Python through nrg_sweep_run_model: the
+    reference's CalcHNMatEl / CalcMatEl / CheckForMatEl rules
+    (include/NRGclasses.hpp:612-634) as callables, its single-site basis and
+    its H_{-1} set-up.
+
+    hn_coef(S, ti, tj, channel, sigma, dir) -> float
+    op_factor(op, S_i, S_j, ti, tj) -> float          (NRG_OP_SITE / NRG_OP_IMPURITY)
+    op_check(op, qn_i, qn_j) -> bool                   (qn: (Q, S or S_z) of a kept block)
+    start_ops[o]: list of (bi, bj, dense block) of operator o at H_{-1}."""
+    total_spin: bool
+    site_qn: list
+    site_bsize: list
+    hn_form: int
+    onsite: bool
+    hn_coef: object
+    op_class: list
+    op_avg: list
+    op_factor: object
+    op_check: object
+    start_qn: list
+    start_bsize: list
+    start_en: list
+    start_ops: list
+
+    def _desc(self, keep: list, errors: list) -> "_ModelDesc":
+        def guard(fn, bad):
+            def call(*a):
+                try:
+                    return fn(*a)
+                except BaseException as e:  # surfaced after the sweep returns
+                    errors.append(e)
+                    return bad
+            return call
+
+        def dbl(v):
+            a = np.ascontiguousarray(v, dtype=np.float64).ravel()
+            keep.append(a)
+            return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+        def ints(v):
+            a = np.ascontiguousarray(v, dtype=np.int32).ravel()
+            keep.append(a)
+            return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+        d = _ModelDesc()
+        d.total_spin = 1 if self.total_spin else 0
+        d.site_nqn = 3 if self.total_spin else 2
+        d.site_nblocks = len(self.site_bsize)
+        d.site_qn = dbl(self.site_qn)
+        d.site_bsize = ints(self.site_bsize)
+        d.hn_form = self.hn_form
+        d.onsite = 1 if self.onsite else 0
+        hc = guard(lambda u, S, ti, tj, ch, sg, dr: float(self.hn_coef(S, ti, tj, ch, sg, dr)), float("nan"))
+        of = guard(lambda u, o, si, sj, ti, tj: float(self.op_factor(o, si, sj, ti, tj)), float("nan"))
+        oc = guard(lambda u, o, qi, qj: 1 if self.op_check(o, (qi[0], qi[1]), (qj[0], qj[1])) else 0, 0)
+        d.hn_coef = _HN_COEF_FN(hc)
+        d.op_factor = _OP_FACTOR_FN(of)
+        d.op_check = _OP_CHECK_FN(oc)
+        keep.extend([d.hn_coef, d.op_factor, d.op_check])
+        d.nops = len(self.op_class)
+        d.op_class = ints(self.op_class)
+        d.op_avg = ints(self.op_avg)
+        d.start_nblocks = len(self.start_bsize)
+        d.start_qn = dbl(self.start_qn)
+        d.start_bsize = ints(self.start_bsize)
+        d.start_en = dbl(self.start_en)
+        d.start_npairs = ints([len(p) for p in self.start_ops])
+        d.start_pairs = ints([[bi, bj] for p in self.start_ops for bi, bj, _ in p] or [0])
+        d.start_el = dbl(np.concatenate([np.asarray(b, dtype=np.float64).ravel()
+                                         for p in self.start_ops for _, _, b in p] or [np.zeros(1)]))
+        return d
+
+
+_dp_ = ctypes.POINTER(ctypes.c_double)
+
+
+class ModelTables:
+    """The host tables of a model (nrg_model_hn_table / nrg_model_op_factor /
+    nrg_model_op_check): a built-in model by name or a ModelPlugin.  Needs no
+    device."""
+
+    def __init__(self, model):
+        self.L = load_library()
+        self._keep, self._errors = [], []
+        if isinstance(model, ModelPlugin):
+            self.model, self.desc = -1, ctypes.byref(model._desc(self._keep, self._errors))
+        else:
+            self.model, self.desc = MODELS[model], None
+
+    def _call(self, st):
+        if self._errors:
+            raise self._errors.pop(0)
+        if st != 0:
+            raise NRGError(st, STATUS.get(st, "error"))
+
+    def hn_table(self, s_block: float) -> np.ndarray:
+        n = ctypes.c_int()
+        self._call(self.L.nrg_model_hn_table(self.model, self.desc, s_block, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value)
+        self._call(self.L.nrg_model_hn_table(self.model, self.desc, s_block,
+                                             out.ctypes.data_as(_dp_), n.value, ctypes.byref(n)))
+        return out
+
+    def op_factor(self, op: int, s_i: float, s_j: float, ti: int, tj: int) -> float:
+        v = ctypes.c_double()
+        self._call(self.L.nrg_model_op_factor(self.model, self.desc, op, s_i, s_j, ti, tj, ctypes.byref(v)))
+        return v.value
+
+    def op_check(self, op: int, qn_i, qn_j) -> bool:
+        a = (ctypes.c_double * 2)(*qn_i)
+        b = (ctypes.c_double * 2)(*qn_j)
+        v = ctypes.c_int()
+        self._call(self.L.nrg_model_op_check(self.model, self.desc, op, a, b, ctypes.byref(v)))
+        return bool(v.value)
+
+
+def clebsch(j1: float, m1: float, j2: float, m2: float, j: float, m: float) -> float:
+    """nrg_clebsch: <j1 m1; j2 m2 | j m> as the engine computes it."""
+    return load_library().nrg_clebsch(j1, m1, j2, m2, j, m)
+
+
 def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     """Load the engine library; raise if it is not built (no fallback)."""
     global _lib
@@ -297,6 +444,15 @@ def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     L.nrg_kernel_count.argtypes = [ctypes.c_void_p]
     L.nrg_kernel_count.restype = ctypes.c_int64
     L.nrg_sweep_run.argtypes = [ctypes.c_void_p, ctypes.POINTER(SweepConfig)]
+    L.nrg_sweep_run_model.argtypes = [ctypes.c_void_p, ctypes.POINTER(SweepConfig), ctypes.POINTER(_ModelDesc)]
+    L.nrg_model_hn_table.argtypes = [ctypes.c_int, ctypes.POINTER(_ModelDesc), ctypes.c_double, _dp_, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_int)]
+    L.nrg_model_op_factor.argtypes = [ctypes.c_int, ctypes.POINTER(_ModelDesc), ctypes.c_int, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp_]
+    L.nrg_model_op_check.argtypes = [ctypes.c_int, ctypes.POINTER(_ModelDesc), ctypes.c_int, _dp_, _dp_,
+                                     ctypes.POINTER(ctypes.c_int)]
+    L.nrg_clebsch.argtypes = [ctypes.c_double] * 6
+    L.nrg_clebsch.restype = ctypes.c_double
     L.nrg_sweep_num_iterations.argtypes = [ctypes.c_void_p]
     L.nrg_sweep_iteration.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(_Iteration)]
     L.nrg_sweep_opavg_initial.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
@@ -645,6 +801,20 @@ class Engine:
         cfg = SweepConfig(MODELS[model], nsites, ncutoff, lam, U, ed, gamma1, gamma2_or_B,
                           degen_eps, precision, delta_sc)
         self._check(self.L.nrg_sweep_run(self.h, ctypes.byref(cfg)))
+        return self._fetch(fetch)
+
+    def sweep_model(self, plugin: ModelPlugin, nsites: int, ncutoff: int, lam: float, gamma1: float,
+                    gamma2: float = 0.0, degen_eps: float = 0.0, precision: int = PREC_FP64,
+                    fetch: bool = True) -> SweepResult:
+        """One sweep of a caller-described model (nrg_sweep_run_model);
+        gamma1 (and gamma2 with two channels) give chi_{-1}."""
+        cfg = SweepConfig(-1, nsites, ncutoff, lam, 0.0, 0.0, gamma1, gamma2, degen_eps, precision, 0.0)
+        keep, errors = [], []
+        desc = plugin._desc(keep, errors)
+        st = self.L.nrg_sweep_run_model(self.h, ctypes.byref(cfg), ctypes.byref(desc))
+        if errors:
+            raise errors[0]
+        self._check(st)
         return self._fetch(fetch)
 
     def grad_forward(self, model: str, nsites: int, ncutoff: int, lam: float, U: float, ed: float,

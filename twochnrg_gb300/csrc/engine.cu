@@ -760,9 +760,7 @@ AsmTables prepare_assembly(nrg_ctx* c, const ModelSpec& m, const Basis& B, const
   aa.pair_fwd = (const int64_t*)(mb + o_pf); aa.pair_fwd_ld = (const int*)(mb + o_pfl);
   aa.pair_bwd = (const int64_t*)(mb + o_pbw); aa.pair_bwd_ld = (const int*)(mb + o_pbl);
   aa.coef = (const double*)(mb + o_coef); aa.ntypes = tabs.ntypes; aa.nchan = tabs.nchan; aa.nsigma = tabs.nsigma;
-  // OneChQ_HN_MatEl is OneChQSz_HN_MatEl without the e_N term (zero on the
-  // flat band): the same device arithmetic
-  aa.nops_h = nops_h; aa.model = m.kind == MODEL_1CHQ ? (int)MODEL_1CHQSZ : (int)m.kind; aa.ops = (const double* const*)c->opptr.p;
+  aa.nops_h = nops_h; aa.model = m.hn_form; aa.onsite = m.onsite ? 1 : 0; aa.ops = (const double* const*)c->opptr.p;
   aa.sqrt_lambda = std::sqrt(lambda); aa.eN = eN; aa.chi[0] = chi[0]; aa.chi[1] = chi[1];
   aa.site_q = (const double*)(mb + o_sq); aa.H = c->H.as<double>();
   aa.sc_pair = (const double*)(mb + o_scp); aa.hc_switch = (const int*)(mb + o_hcs);
@@ -808,9 +806,10 @@ void plan_update(UpdatePlan& U, const ModelSpec& m, const Basis& B, const EigPla
     OpMeta& no = U.newops[o];
     for (int i = 0; i < nk; ++i)
       for (int j = 0; j < nk; ++j) {
-        if (!op_check(m.op_check[o], K.blk, i, j)) continue;
+        if (!op_check(m, m.op_check[o], K.blk, i, j)) continue;
         const int bI = K.src[i], bJ = K.src[j];
-        const bool kept_only = kept_rows && m.op_kind[o] != OP_CD_QS && m.op_kind[o] != OP_CD_2CH;
+        const bool cd_like = m.op_kind[o] == OP_CD_QS || m.op_kind[o] == OP_CD_2CH || m.op_kind[o] >= OP_PLUGIN_IMP;
+        const bool kept_only = kept_rows && !cd_like;
         RotJob J{};
         J.ki = K.blk.size[i]; J.kj = K.blk.size[j]; J.nI = P.bsize[bI];
         J.ldz = J.kj; J.ldo = J.kj;
@@ -835,7 +834,7 @@ void plan_update(UpdatePlan& U, const ModelSpec& m, const Basis& B, const EigPla
                 GatherTerm G{};
                 G.job = jid; G.dst_base = p.offset + u; G.dst_stride = p.nsite; G.rows = p.count;
                 G.src_base = q.offset + v; G.src_stride = q.nsite; G.srows = q.count;
-                if (m.op_kind[o] == OP_IMPONLY || m.op_kind[o] == OP_CD_QS || m.op_kind[o] == OP_CD_2CH) {
+                if (m.op_kind[o] == OP_IMPONLY || cd_like) {
                   double g = 1.0;
                   if (m.op_kind[o] == OP_IMPONLY) {
                     if (tu_ != tv) continue;
@@ -971,11 +970,16 @@ struct TangentState {
 // 940-1000): H_0 is the first site alone (Nsites0 = 1), its thermodynamics
 // are taken before the loop at D_0 (NRG_main.cpp:242-255), and iteration N =
 // 1 .. nsites-1 adds site N with hopping chi_{N-1}.  Only f_N is carried.
+//
+// ext: a caller-described model (nrg_sweep_run_model); cfg->model is then
+// ignored.
 void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool chain = false,
-               TangentState* tan = nullptr) {
+               TangentState* tan = nullptr, const nrg_model_desc* ext = nullptr) {
   using clock = std::chrono::steady_clock;
   auto t_begin = clock::now();
-  if (cfg->model < 0 || cfg->model > 5) throw NrgError(NRG_ERR_ARG, "unknown model");
+  if (ext && (dm || chain || tan))
+    throw NrgError(NRG_ERR_ARG, "DM-NRG shells, the free chain and derivatives are built for the built-in models");
+  if (!ext && (cfg->model < 0 || cfg->model > 5)) throw NrgError(NRG_ERR_ARG, "unknown model");
   if (chain && (cfg->model == NRG_MODEL_1CH_S || cfg->model == NRG_MODEL_1CH_SZ))
     throw NrgError(NRG_ERR_ARG, "the reference has no free-chain run for the superconducting-lead models");
   if (dm && cfg->model != NRG_MODEL_1CH_QS && cfg->model != NRG_MODEL_2CH_QS)
@@ -990,7 +994,15 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
   const int64_t launches0 = c->launches;
   Sweep S;
   S.c = c;
-  S.m = make_model((ModelKind)cfg->model);
+  if (ext) {
+    try {
+      S.m = make_plugin_model(*ext);
+    } catch (const std::invalid_argument& e) {
+      throw NrgError(NRG_ERR_ARG, e.what());
+    }
+  } else {
+    S.m = make_model((ModelKind)cfg->model);
+  }
   S.cfg = *cfg;
   if (chain) {
     const int nf = (S.m.kind == MODEL_1CHQS || S.m.kind == MODEL_1CHS) ? 1 : 2;
@@ -1020,7 +1032,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
   const double HLF = 0.5 * (1.0 + 1.0 / lambda);
   const double betabar = 0.727;
   const int nops = (int)m.op_kind.size();
-  const int nops_h = (m.kind == MODEL_1CHQS || m.kind == MODEL_1CHS) ? 1 : 2;  // old operators entering H_N
+  const int nops_h = m.nops_h;  // old operators entering H_N
   Timer tm(c);
   cudaEvent_t span0, span1;
   CU(cudaEventCreate(&span0));
@@ -1039,9 +1051,15 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
   // Gamma = 0): a decoupled four-state impurity beside the chain from site 0
   // on (Nsites0 = 0); its ln 4 is CNRGthermo::dImpValue.
   const bool chain_q = chain && m.kind == MODEL_1CHQ;
-  StartState st = chain && !chain_q ? make_chain_start(m, lambda)
-                                    : make_start(m, lambda, chain ? 0.0 : cfg->U, chain ? 0.0 : cfg->ed,
-                                                 chain ? 0.0 : cfg->gamma2_or_B);
+  StartState st;
+  try {
+    st = ext ? make_plugin_start(m)
+         : chain && !chain_q ? make_chain_start(m, lambda)
+                             : make_start(m, lambda, chain ? 0.0 : cfg->U, chain ? 0.0 : cfg->ed,
+                                          chain ? 0.0 : cfg->gamma2_or_B);
+  } catch (const std::invalid_argument& e) {
+    throw NrgError(NRG_ERR_ARG, e.what());
+  }
   if (chain_q) st.ops.resize(nops);
   if (dm) {
     // c_d at H_{-1} is a copy of f (Main_SetH0.cpp:1958-1961); f_ch1 = f_ch2 = d.
@@ -2359,7 +2377,7 @@ void diag_hn_impl(nrg_ctx* c, int model, const double* params, int nparams, cons
   if (nparams > m.nchan + 2 && params[m.nchan + 2] != 0.0)
     throw NrgError(NRG_ERR_ARG, "superconducting leads (Delta_SC != 0) are not supported");
   if (!(params[0] > 1.0)) throw NrgError(NRG_ERR_ARG, "Lambda must exceed 1");
-  const int nops_h = m.kind == MODEL_1CHQS ? 1 : 2;
+  const int nops_h = m.nops_h;
   if (nops < nops_h || !ops) throw NrgError(NRG_ERR_ARG, "the model's f operators are required");
   if (!en_out || !evec_out) throw NrgError(NRG_ERR_ARG, "output arrays are NULL");
   std::memset(&c->timing, 0, sizeof(c->timing));
@@ -2726,6 +2744,79 @@ nrg_status nrg_sweep_run(nrg_ctx* ctx, const nrg_sweep_config* cfg) {
     sweep_run(ctx, cfg);
   });
   return NRG_OK;
+}
+
+nrg_status nrg_sweep_run_model(nrg_ctx* ctx, const nrg_sweep_config* cfg, const nrg_model_desc* model) {
+  if (!ctx || !cfg || !model) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    sweep_run(ctx, cfg, false, false, nullptr, model);
+  });
+  return NRG_OK;
+}
+
+namespace {
+nrg::ModelSpec host_model(int model, const nrg_model_desc* desc) {
+  if (desc) return nrg::make_plugin_model(*desc);
+  if (model < 0 || model > 5) throw std::invalid_argument("unknown model");
+  return nrg::make_model((nrg::ModelKind)model);
+}
+}  // namespace
+
+nrg_status nrg_model_hn_table(int model, const nrg_model_desc* desc, double s_block, double* coef, int cap, int* n) {
+  if (!n) return NRG_ERR_ARG;
+  try {
+    const nrg::ModelSpec m = host_model(model, desc);
+    nrg::Basis B;
+    B.blk.nqn = 2;
+    const double q[2] = {0.0, s_block};
+    B.blk.push(q, 1);
+    nrg::HNTables t;
+    nrg::build_hn_tables(m, B, t);
+    *n = (int)t.coef.size();
+    if (coef && cap >= *n) std::copy(t.coef.begin(), t.coef.end(), coef);
+  } catch (const std::exception&) {
+    return NRG_ERR_ARG;
+  }
+  return NRG_OK;
+}
+
+nrg_status nrg_model_op_factor(int model, const nrg_model_desc* desc, int op, double s_i, double s_j, int ti, int tj,
+                               double* out) {
+  if (!out) return NRG_ERR_ARG;
+  try {
+    const nrg::ModelSpec m = host_model(model, desc);
+    if (op < 0 || op >= (int)m.op_kind.size() || ti < 0 || tj < 0 || ti >= m.site.nstates || tj >= m.site.nstates)
+      return NRG_ERR_ARG;
+    const int k = m.op_kind[op];
+    *out = k == nrg::OP_IMPONLY ? (ti == tj ? 1.0 : 0.0) : nrg::op_site_factor(m, k, s_i, s_j, ti, tj);
+  } catch (const std::exception&) {
+    return NRG_ERR_ARG;
+  }
+  return NRG_OK;
+}
+
+nrg_status nrg_model_op_check(int model, const nrg_model_desc* desc, int op, const double* qn_i, const double* qn_j,
+                              int* out) {
+  if (!out || !qn_i || !qn_j) return NRG_ERR_ARG;
+  try {
+    const nrg::ModelSpec m = host_model(model, desc);
+    if (op < 0 || op >= (int)m.op_check.size()) return NRG_ERR_ARG;
+    nrg::BlockArray a;
+    a.nqn = 2;
+    a.push(qn_i, 1);
+    a.push(qn_j, 1);
+    const bool same = qn_i[0] == qn_j[0] && qn_i[1] == qn_j[1];  // one kept block: Diag_check holds
+    *out = nrg::op_check(m, m.op_check[op], a, 0, same ? 0 : 1) ? 1 : 0;
+  } catch (const std::exception&) {
+    return NRG_ERR_ARG;
+  }
+  return NRG_OK;
+}
+
+double nrg_clebsch(double j1, double m1, double j2, double m2, double j, double m) {
+  return nrg::clebsch(j1, m1, j2, m2, j, m);
 }
 
 int nrg_sweep_num_iterations(const nrg_ctx* ctx) { return ctx ? (int)ctx->iters.size() : 0; }

@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(256) assemble_kernel(AssembleArgs A, const int
     double v;
     if (i == j) {
       v = __dmul_rn(A.sqrt_lambda, A.st_eold[gi]);
-      if (A.model != 2) v = __dadd_rn(v, __dmul_rn(A.eN, __dadd_rn(A.site_q[A.st_type[gi]], 1.0)));
+      if (A.onsite) v = __dadd_rn(v, __dmul_rn(A.eN, __dadd_rn(A.site_q[A.st_type[gi]], 1.0)));
     } else {
       const int p = A.st_seg[gi], q = A.st_seg[gj];
       const int ai = A.st_a[gi], aj = A.st_a[gj];

@@ -98,7 +98,8 @@ struct AssembleArgs {
   const double* coef;        // [nblocks * per_block]
   int ntypes, nchan, nsigma;
   int nops_h;                // old operators entering H_N (pair-table stride)
-  int model;                 // ModelKind
+  int model;                 // element arithmetic: ModelKind of the rule it follows
+  int onsite;                // the diagonal adds e_N (site charge + 1)
   const double* const* ops;  // [nops_h] old operator element arrays
   double sqrt_lambda, eN;
   double chi[2];

@@ -214,7 +214,92 @@ ModelSpec make_model(ModelKind kind) {
     throw std::runtime_error("unknown model");
   }
   for (int k : m.op_kind) m.op_avg.push_back(k == OP_IMPONLY ? 1 : 0);
+  // Old operators entering H_N and the element arithmetic of the assembly:
+  // OneChQ_HN_MatEl is OneChQSz_HN_MatEl without the e_N term (zero on the
+  // flat band), the same arithmetic.
+  m.nops_h = (kind == MODEL_1CHQS || kind == MODEL_1CHS) ? 1 : 2;
+  m.hn_form = kind == MODEL_1CHQ ? (int)MODEL_1CHQSZ : (int)kind;
+  m.onsite = kind != MODEL_2CHQS;
   return m;
+}
+
+namespace {
+void plugin_fail(const char* what) { throw std::invalid_argument(std::string("model description: ") + what); }
+}  // namespace
+
+ModelSpec make_plugin_model(const nrg_model_desc& d) {
+  if (d.total_spin != 0 && d.total_spin != 1) plugin_fail("total_spin must be 0 or 1");
+  if (d.site_nqn != (d.total_spin ? 3 : 2)) plugin_fail("site_nqn must be 3 with total_spin, else 2");
+  if (d.site_nblocks < 1 || !d.site_qn || !d.site_bsize) plugin_fail("no site blocks");
+  if (d.hn_form < NRG_HN_ONE_OP || d.hn_form > NRG_HN_CHANNEL_SUM) plugin_fail("unknown hn_form");
+  if (!d.hn_coef || !d.op_check) plugin_fail("hn_coef and op_check are required");
+  const int hn_ops = d.hn_form == NRG_HN_ONE_OP ? 1 : 2;
+  if (d.nops < hn_ops || d.nops > 8 || !d.op_class) plugin_fail("nops must cover the operators entering H_N (at most 8)");
+  ModelSpec m;
+  m.kind = MODEL_PLUGIN;
+  m.site.blk.nqn = d.site_nqn;
+  for (int b = 0; b < d.site_nblocks; ++b) {
+    if (d.site_bsize[b] < 1) plugin_fail("empty site block");
+    m.site.blk.push(d.site_qn + (size_t)b * d.site_nqn, d.site_bsize[b]);
+    m.site.nstates += d.site_bsize[b];
+  }
+  m.totalS = d.total_spin == 1;
+  m.nchan = d.hn_form == NRG_HN_CHANNEL_SUM ? 2 : 1;
+  m.nsigma = d.hn_form == NRG_HN_ONE_OP ? 1 : 2;
+  m.nops_h = hn_ops;
+  m.hn_form = d.hn_form == NRG_HN_ONE_OP ? (int)MODEL_1CHQS
+              : d.hn_form == NRG_HN_SPIN_SUM ? (int)MODEL_1CHQSZ : (int)MODEL_2CHQS;
+  m.onsite = d.onsite != 0;
+  for (int o = 0; o < d.nops; ++o) {
+    const int cls = d.op_class[o];
+    if (cls == NRG_OP_SITE) m.op_kind.push_back(OP_PLUGIN_SITE + o);
+    else if (cls == NRG_OP_IMPURITY) m.op_kind.push_back(OP_PLUGIN_IMP + o);
+    else if (cls == NRG_OP_IMPURITY_DIAG) m.op_kind.push_back(OP_IMPONLY);
+    else plugin_fail("unknown op_class");
+    if (cls != NRG_OP_IMPURITY_DIAG && !d.op_factor) plugin_fail("op_factor is required");
+    m.op_check.push_back(CHK_PLUGIN + o);
+    m.op_name.push_back("op" + std::to_string(o));
+    m.op_avg.push_back(d.op_avg && d.op_avg[o] ? 1 : 0);
+  }
+  m.ext = &d;
+  m.cache = std::make_shared<PluginCache>();
+  return m;
+}
+
+StartState make_plugin_start(const ModelSpec& m) {
+  const nrg_model_desc& d = *m.ext;
+  if (d.start_nblocks < 1 || !d.start_qn || !d.start_bsize || !d.start_en || !d.start_npairs)
+    plugin_fail("no H_{-1} blocks");
+  StartState s;
+  s.blk.nqn = 2;
+  for (int b = 0; b < d.start_nblocks; ++b) {
+    if (d.start_bsize[b] < 1) plugin_fail("empty H_{-1} block");
+    s.blk.push(d.start_qn + 2 * (size_t)b, d.start_bsize[b]);
+  }
+  s.en.assign(d.start_en, d.start_en + s.blk.nstates());
+  for (double e : s.en)
+    if (!std::isfinite(e)) plugin_fail("non-finite H_{-1} level");
+  size_t pr = 0;
+  int64_t el = 0;
+  for (int o = 0; o < d.nops; ++o) {
+    OpBlocks ob;
+    if (d.start_npairs[o] < 0) plugin_fail("negative pair count");
+    if (d.start_npairs[o] > 0 && (!d.start_pairs || !d.start_el)) plugin_fail("missing H_{-1} operator blocks");
+    for (int k = 0; k < d.start_npairs[o]; ++k, ++pr) {
+      const int i = d.start_pairs[2 * pr], j = d.start_pairs[2 * pr + 1];
+      if (i < 0 || j < 0 || i >= d.start_nblocks || j >= d.start_nblocks) plugin_fail("H_{-1} operator block out of range");
+      const int64_t n = (int64_t)d.start_bsize[i] * d.start_bsize[j];
+      ob.bi.push_back(i); ob.bj.push_back(j); ob.off.push_back((int64_t)ob.el.size());
+      for (int64_t x = 0; x < n; ++x) {
+        const double v = d.start_el[el + x];
+        if (!std::isfinite(v)) plugin_fail("non-finite H_{-1} operator element");
+        ob.el.push_back(v);
+      }
+      el += n;
+    }
+    s.ops.push_back(std::move(ob));
+  }
+  return s;
 }
 
 namespace {
@@ -351,7 +436,7 @@ StartState make_chain_start(const ModelSpec& m, double lambda) {
     OpBlocks f;
     for (int i = 0; i < B.blk.nblocks(); ++i)
       for (int j = 0; j < B.blk.nblocks(); ++j) {
-        if (!op_check(m.op_check[o], B.blk, i, j)) continue;
+        if (!op_check(m, m.op_check[o], B.blk, i, j)) continue;
         f.bi.push_back(i); f.bj.push_back(j); f.off.push_back((int64_t)f.el.size());
         for (int a = B.blk.offset[i]; a < B.blk.offset[i] + B.blk.size[i]; ++a)
           for (int b = B.blk.offset[j]; b < B.blk.offset[j] + B.blk.size[j]; ++b)
@@ -527,7 +612,15 @@ void build_hn_tables(const ModelSpec& m, const Basis& b, HNTables& t) {
     for (int ti = 0; ti < NT; ++ti)
       for (int tj = 0; tj < NT; ++tj) {
         size_t base = ((size_t)ti * NT + tj) * t.nchan * t.nsigma;
-        if (m.kind == MODEL_1CHQS) {
+        if (m.kind == MODEL_PLUGIN) {
+          for (int ch = 0; ch < t.nchan; ++ch)
+            for (int s = 0; s < t.nsigma; ++s)
+              for (int dir = 0; dir < 2; ++dir) {
+                const double v = m.ext->hn_coef(m.ext->user, Si, ti, tj, ch, s, dir);
+                if (!std::isfinite(v)) plugin_fail("hn_coef returned a non-finite value");
+                c[(base + (size_t)ch * t.nsigma + s) * 2 + dir] = v;
+              }
+        } else if (m.kind == MODEL_1CHQS) {
           c[base * 2 + 0] = hn_coef_1chQS(m.site, Si, ti, tj);
           c[base * 2 + 1] = hn_coef_1chQS(m.site, Si, tj, ti);
         } else if (m.kind == MODEL_1CHS) {
@@ -573,6 +666,16 @@ bool hc_switch_1chSz(int sigma, int ti, int tj) { return fd_onechS(sigma, ti, tj
 
 double op_site_factor(const ModelSpec& m, int op, double Si, double Sj, int ti, int tj) {
   const BlockArray& ss = m.site.blk;
+  if (op >= OP_PLUGIN_SITE) {
+    const int o = op >= OP_PLUGIN_IMP ? op - OP_PLUGIN_IMP : op - OP_PLUGIN_SITE;
+    const auto key = std::make_tuple(o, Si, Sj, ti, tj);
+    auto it = m.cache->factor.find(key);
+    if (it != m.cache->factor.end()) return it->second;
+    const double v = m.ext->op_factor(m.ext->user, o, Si, Sj, ti, tj);
+    if (!std::isfinite(v)) plugin_fail("op_factor returned a non-finite value");
+    m.cache->factor.emplace(key, v);
+    return v;
+  }
   if (op == OP_F_S) {
     // OneChS_fN_MatEl (OpMatRules.cpp:1555-1654), with its site lookups.
     auto q = [&](int t, int k) { return ss.q(m.site.block_of_state(t), k); };
@@ -707,7 +810,17 @@ double op_site_factor(const ModelSpec& m, int op, double Si, double Sj, int ti, 
   return 0.0;
 }
 
-bool op_check(int chk, const BlockArray& a, int i, int j) {
+bool op_check(const ModelSpec& m, int chk, const BlockArray& a, int i, int j) {
+  if (chk >= CHK_PLUGIN) {
+    const int o = chk - CHK_PLUGIN;
+    const auto key = std::make_tuple(o, a.q(i, 0), a.q(i, 1), a.q(j, 0), a.q(j, 1));
+    auto it = m.cache->check.find(key);
+    if (it != m.cache->check.end()) return it->second;
+    const double qi[2] = {a.q(i, 0), a.q(i, 1)}, qj[2] = {a.q(j, 0), a.q(j, 1)};
+    const bool v = m.ext->op_check(m.ext->user, o, qi, qj) != 0;
+    m.cache->check.emplace(key, v);
+    return v;
+  }
   // OneChS_cd_check (OpMatRules.cpp:172, S in the second slot here),
   // Diag_check (OpMatRules.cpp:12), OneChQS_cd_check (:106), OneChQ_cd_check
   // (:92), TwoChQS_cd_check (TwoChQS_OpMatRules.cpp:16).

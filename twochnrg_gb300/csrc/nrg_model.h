@@ -10,8 +10,12 @@
 #include <array>
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <string>
+#include <tuple>
 #include <vector>
+
+#include "../../include/twochnrg_gb300.h"
 
 namespace nrg {
 
@@ -23,7 +27,9 @@ namespace nrg {
 // its blocks carry a constant 0 in the charge slot and S in the second, so
 // that every SU(2) rule reads S where it does for (Q,S).
 // MODEL_1CHSZ (SymNo 8) is its |Sz> form with a Zeeman field: blocks (0, Sz).
-enum ModelKind { MODEL_1CHQS = 0, MODEL_1CHQSZ = 1, MODEL_2CHQS = 2, MODEL_1CHQ = 3, MODEL_1CHS = 4, MODEL_1CHSZ = 5 };
+// MODEL_PLUGIN: a model described by the caller (nrg_model_desc).
+enum ModelKind { MODEL_1CHQS = 0, MODEL_1CHQSZ = 1, MODEL_2CHQS = 2, MODEL_1CHQ = 3, MODEL_1CHS = 4, MODEL_1CHSZ = 5,
+                 MODEL_PLUGIN = 6 };
 
 // Operator rule ids (how the operator acts on a new site; see build_op_terms).
 enum OpKind {
@@ -38,10 +44,16 @@ enum OpKind {
   OP_FUP_SZ = 9,    // OneChSz_fNup_MatEl    (OpMatRules.cpp:2016)
   OP_FDN_SZ = 10,   // OneChSz_fNdn_MatEl    (OpMatRules.cpp:2027)
   OP_CD_2CH = 11,   // c_d across the two-channel site x old (OneChQS_cd_MatEl's recoupling)
+  // Plug-in operators: OP_PLUGIN_SITE + o acts on the new site (like f_N),
+  // OP_PLUGIN_IMP + o is an old operator recoupled across the site (like
+  // c_d); the factor is the caller's op_factor for operator o.
+  OP_PLUGIN_SITE = 1000,
+  OP_PLUGIN_IMP = 2000,
 };
 // CheckForMatEl rule ids.
+// CHK_PLUGIN + o: the caller's op_check for operator o.
 enum CheckKind { CHK_DIAG = 1, CHK_QS_CD = 2, CHK_Q_CD = 3, CHK_2CH_CD = 4, CHK_S_CD = 5, CHK_SZ_UP = 6,
-                 CHK_SZ_DN = 7 };
+                 CHK_SZ_DN = 7, CHK_PLUGIN = 1000 };
 
 // Block-structured array: the common part of CNRGarray / CNRGbasisarray
 // (include/NRGclasses.hpp:47-349).
@@ -85,18 +97,34 @@ struct Basis {
   std::vector<int> a_of;      // old state index inside the old block
 };
 
+// Callback results of a plug-in model, memoised for one sweep (the
+// callbacks are pure functions of their arguments).
+struct PluginCache {
+  std::map<std::tuple<int, double, double, int, int>, double> factor;
+  std::map<std::tuple<int, double, double, double, double>, bool> check;
+};
+
 struct ModelSpec {
   ModelKind kind;
   Site site;
   bool totalS;           // SU(2) multiplet basis
   int nchan;             // Wilson channels
   int nsigma;            // spin components summed in H_N (QSz: 2)
+  int nops_h = 1;        // old operators entering H_N (the first ones)
+  int hn_form = 0;       // element arithmetic of the assembly (AssembleArgs::model)
+  bool onsite = true;    // the diagonal adds e_N (Q_site + 1)
   std::vector<int> op_kind, op_check;
   std::vector<std::string> op_name;
   std::vector<char> op_avg;  // CalcAvg operators
+  const nrg_model_desc* ext = nullptr;  // MODEL_PLUGIN: the caller's description
+  std::shared_ptr<PluginCache> cache;
 };
 
 ModelSpec make_model(ModelKind kind);
+// A caller-described model (nrg_model_desc): checked, its site basis and
+// operator rules taken over.  Throws std::invalid_argument on a malformed
+// description.
+ModelSpec make_plugin_model(const nrg_model_desc& d);
 
 // Initial impurity data (H_{-1}): kept array with energies and operators in
 // dense per-block-pair form (reference MatBlockMap order).
@@ -112,6 +140,8 @@ struct StartState {
   std::vector<OpBlocks> ops;
 };
 StartState make_start(const ModelSpec& m, double lambda, double U, double ed, double B);
+// H_{-1} of a plug-in model, from its description.
+StartState make_plugin_start(const ModelSpec& m);
 // Free-chain start-up (calcdens = 3, CodeHandler_ModelSwitch.cpp:377-420,
 // 667-720, 940-1000): the first Wilson site alone at zero energy (flat band,
 // e_0 = 0) with only the channel operators f_N that enter H_N.
@@ -161,7 +191,7 @@ bool hc_switch_1chS(int ti, int tj);
 // the old operator is read backwards also when OneChS_fd_table(sigma, t_i,
 // t_j) vanishes.
 bool hc_switch_1chSz(int sigma, int ti, int tj);
-bool op_check(int chk, const BlockArray& kept, int i, int j);
+bool op_check(const ModelSpec& m, int chk, const BlockArray& kept, int i, int j);
 
 // Clebsch-Gordan <J1 M1; J2 M2 | J M>  (CGordan.cpp:34-120).
 double clebsch(double J1, double M1, double J2, double M2, double J, double M);
