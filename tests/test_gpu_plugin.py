@@ -66,6 +66,17 @@ def test_plugin_qsz_matches_reference_fixture(engine):
     _same(r, b)
 
 
+def test_plugin_two_channel_matches_reference_fixture(engine):
+    cfg, ref = _fixture("cfg1_2chQS_n8_k300")
+    model, ns, nc, lam, U, ed, g1, g2 = cfg[:8]
+    assert str(model) == "2chQS"
+    plug = pm.two_channel_qs(float(U), float(ed), float(lam))
+    r = engine.sweep_model(plug, int(ns), int(nc), float(lam), float(g1), float(g2))
+    compare(r, ref, "2chQS")
+    b = engine.sweep("2chQS", int(ns), int(nc), float(lam), float(U), float(ed), float(g1), float(g2))
+    _same(r, b)
+
+
 def test_plugin_mixed_precision(engine, monkeypatch):
     """The plug-in model through the mixed form (large-block thresholds
     lowered so the blocked reduction runs) against the FP64 built-in."""

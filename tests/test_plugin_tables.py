@@ -8,23 +8,25 @@ import pytest
 import plugin_models as pm
 import twochnrg_gb300 as tg
 
-CASES = [("1chQS", lambda: pm.one_channel_qs(0.5, -0.25, 2.5)),
-         ("1chQSz", lambda: pm.one_channel_qsz(0.5, -0.25, 1e-3, 2.5))]
+CASES = [("1chQS", lambda: pm.one_channel_qs(0.5, -0.25, 2.5), 4, 4),
+         ("1chQSz", lambda: pm.one_channel_qsz(0.5, -0.25, 1e-3, 2.5), 4, 4),
+         ("2chQS", lambda: pm.two_channel_qs(0.3, -0.15, 2.5), 16, 5)]
 QN = [(-1.0, 0.0), (0.0, 0.5), (1.0, 0.0), (0.0, -0.5), (2.0, 0.5), (1.0, 1.0), (-2.0, 1.5)]
 
 
-@pytest.mark.parametrize("name,make", CASES, ids=[c[0] for c in CASES])
-def test_tables_equal_builtin(name, make):
+@pytest.mark.parametrize("name,make,ntypes,nops", CASES, ids=[c[0] for c in CASES])
+def test_tables_equal_builtin(name, make, ntypes, nops):
     a, b = tg.ModelTables(name), tg.ModelTables(make())
     for S in np.arange(0.0, 8.5, 0.5):
         ta, tb = a.hn_table(S), b.hn_table(S)
-        assert ta.shape == tb.shape and ta.size > 0
+        per_pair = {"1chQS": 2, "1chQSz": 4, "2chQS": 8}[name]  # 2 nchan nsigma
+        assert ta.shape == tb.shape and ta.size == ntypes * ntypes * per_pair
         np.testing.assert_array_equal(ta, tb)
-    for o in range(4):
-        for Si in np.arange(0.0, 4.0, 0.5):
-            for Sj in np.arange(0.0, 4.0, 0.5):
-                for ti in range(4):
-                    for tj in range(4):
+    for o in range(nops):
+        for Si in np.arange(0.0, 3.0 if ntypes > 4 else 4.0, 0.5):
+            for Sj in np.arange(0.0, 3.0 if ntypes > 4 else 4.0, 0.5):
+                for ti in range(ntypes):
+                    for tj in range(ntypes):
                         assert a.op_factor(o, Si, Sj, ti, tj) == b.op_factor(o, Si, Sj, ti, tj)
         for qi in QN:
             for qj in QN:
