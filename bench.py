@@ -9,11 +9,12 @@ needed between steps.
 
 Prints one JSON line (rank 0).  `value` is the sweep time in seconds measured
 with CUDA events on the engine's stream (mean over the timed steps, max over
-ranks) in the headline arithmetic (--precision, default mixed: the large
-blocks' Householder reduction blocked, its trailing updates as split-BF16
-products on the tensor cores); `e2e` is the host wall time of the same call
-including every host<->device copy of inputs and results.  The plain FP64
-form is timed once after the timed region ("fp64"), and both forms are
+ranks) in the headline arithmetic (--precision, default fp64, the faster
+form on this workload; "mixed": the largest blocks' Householder reduction
+blocked, its trailing updates as split-BF16 products on the tensor cores);
+`e2e` is the host wall time of the same call including every host<->device
+copy of inputs and results.  The other form is timed once after the timed
+region, and both forms are
 checked against the reference's own outputs for the first five iterations
 at 3000 kept (tests/golden/cfg1_2chQS_n5_k3000.npz) and against each other
 over the whole sweep ("accuracy").
@@ -413,7 +414,7 @@ def main():
     ap.add_argument("--dm2ch", action="store_true",
                     help="only the two-channel DM-NRG spectral function (about 8 minutes and 190 GB at 3000 kept)")
     ap.add_argument("--dm2ch-ncutoff", type=int, default=DM2_WORKLOAD["ncutoff"])
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+    ap.add_argument("--precision", default="fp64", choices=["mixed", "fp64"],
                     help="arithmetic of the timed sweeps (the other form is timed once after them)")
     args = ap.parse_args()
     ws, rank, local = dist_env()

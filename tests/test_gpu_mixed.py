@@ -83,8 +83,8 @@ def test_mixed_matches_oracle_two_channel(engine, blocked_everywhere, monkeypatc
 
 def test_mixed_default_threshold_agrees_with_fp64(engine):
     # the default threshold on a sweep whose largest blocks pass it
-    case = ("2chQS", 4, 2200, 2.5, 0.3, -0.15, 0.01, 0.01)
+    case = ("2chQS", 4, 3000, 2.5, 0.3, -0.15, 0.01, 0.01)
     a = engine.sweep(*case)
     b = engine.sweep(*case, precision=tg.PREC_MIXED)
-    assert max(int(it.bsize.max()) for it in a.iters) >= 2600
+    assert max(int(it.bsize.max()) for it in a.iters) >= 4200
     compare(b, a)

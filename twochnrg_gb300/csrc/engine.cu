@@ -309,7 +309,11 @@ int big_block_threshold() {
 // whole-grid kernel, the small ones the cluster kernel).
 int mixed_block_threshold() {
   const char* s = std::getenv("NRG_MIXED_N");
-  return s ? std::atoi(s) : 2200;  // measured best on the two-channel sweep (1800-4200 tried)
+  // With the lower-triangle FP64 grid kernel the blocked path pays off only
+  // for the largest blocks: per full-size iteration of the two-channel sweep
+  // at 3000 kept, thresholds 2600 / 3000 / 3400 / 3800 / 4200 gave 1.42 /
+  // 1.33 / 1.38 / 1.21 / 1.06 s against 1.04 s for FP64.
+  return s ? std::atoi(s) : 4200;
 }
 
 int grid_split(int nbig) {
@@ -426,13 +430,14 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
     if (G <= 0 || Gfp <= 0) throw NrgError(NRG_ERR_SIZE, "blocked tridiagonalization does not fit");
     const int mthr = mixed_block_threshold();
     // Deal the large blocks to the K streams by their cost on the path they
-    // take (greedy, largest first): per column, the FP64 kernel does three
-    // FMAs per trailing element and pays ~16 us of barrier and vector work,
-    // the blocked panel one FMA and ~50 us (two grid barriers); in FMA units
-    // of a quarter of the GPU (about 1.3e11 FMA/s), 2.1e6 and 6.6e6 per column.
+    // take (greedy, largest first): per column, the FP64 kernel does two
+    // FMAs per trailing element of the lower triangle and pays ~21 us of
+    // barriers and vector work, the blocked panel one FMA per element of the
+    // full trailing matrix and ~50 us; in FMA units of a quarter of the GPU
+    // (about 1.3e11 FMA/s), 2.8e6 and 6.6e6 per column.
     auto cost = [&](int n) {
       const double n3 = (double)n * n * n;
-      return n >= mthr ? n3 / 3.0 + 6.6e6 * n : n3 + 2.1e6 * n;
+      return n >= mthr ? n3 / 3.0 + 6.6e6 * n : 2.0 * n3 / 3.0 + 2.8e6 * n;
     };
     {
       std::vector<int> big(order_h.begin(), order_h.begin() + nbig);

@@ -208,15 +208,43 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
 }
 
 // Whole-GPU variant for the largest blocks: every CTA of a cooperative grid
-// works on the same block and owns a contiguous range of its rows.  Per
-// Householder step each CTA applies the pending rank-2 update to its rows and
-// forms their complete entries of y = tau A v (the rows hold both triangles),
-// writes them and its share of y.v to global memory, and after ONE grid
-// barrier every CTA reads y and the shares and forms w.  y and the shares are
-// double-buffered by step parity: a CTA that runs ahead into the next step
-// writes the other buffer, and cannot run two steps ahead past the barrier.
-// Same outputs as tridiag_kernel.
-constexpr int kSeg = 4;  // column segments per row: warps work on (row, segment) items
+// works on the same block.  It touches the LOWER triangle only, so each
+// Householder step costs 4 FMA per stored element (2 for the pending rank-2
+// update, 1 for each of the two products a_rc v_c and a_rc v_r of y = A v):
+// 2/3 n^3 FMA per block, the algorithmic count, against n^3 for a full-storage
+// update (2 FMA per element of both triangles plus one for the row product).
+//
+// Per step j (trailing rows j+1..n-1, m of them):
+//  * The rows form tiles of kRowTile rows, dealt to the CTAs in the order
+//    g, 2G-1-g, 2G+g, 4G-1-g, ... so that every CTA gets short and long rows
+//    alike (equal work, and no CTA holds a tall narrow triangle whose first
+//    strip would be a long chain of dependent loads for one warp).  A row
+//    tile is cut into strips of 32 columns; strip s belongs to the same warp
+//    of the CTA in every row tile (a snake over the warps), so the column
+//    sums of y (lane = column, accumulated over the tile's rows in
+//    registers, then into the CTA's column array) need no synchronisation
+//    inside the CTA.  The row sums go through a per-warp shared tile read
+//    transposed (lane = row), so they also accumulate by FMA.
+//  * Each CTA publishes its column sums (G x m) and its warps' row sums (one
+//    value per warp and row of its tiles); grid barrier 1.
+//  * Columns are dealt evenly to the CTAs, which add the shares in a fixed
+//    order (the warps' row sums, then the CTAs' column sums) into
+//    y = tau A v and their part of y.v; grid barrier 2; every CTA forms w.
+//  * Column j+1 of the updated matrix is captured during the sweep (the
+//    element in column j+1 of each row), double-buffered by step parity: it
+//    is row j+1 of the next step.
+// The upper triangle is free storage: row j receives v_j (v_j[j+1] = 1) in
+// columns j+1..n-1 for the back-transformation, as in tridiag_kernel.
+// Every sum has a fixed order, so all CTAs hold bitwise identical vectors
+// and the result does not depend on timing.
+constexpr int kRowTile = 8;
+constexpr int kTileLd = 33;  // padded row of a warp's transpose tile
+constexpr int kTileDoubles = (kRowTile + 1) * kTileLd;  // + one row for v of the strip's columns
+
+__host__ __device__ constexpr size_t grid_smem_doubles(int maxn) {
+  return 4 * (size_t)maxn + (size_t)kWarps * kTileDoubles + kWarps + 4;
+}
+__host__ __device__ constexpr size_t grid_smem_bytes(int maxn) { return sizeof(double) * grid_smem_doubles(maxn); }
 
 __global__ void __launch_bounds__(kThreads, 1) tridiag_grid_kernel(TridiagArgs A, const int* big, int nbig,
                                                                   double* work) {
@@ -228,34 +256,47 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_grid_kernel(TridiagArgs A
   double* V0 = sm;
   double* V1 = sm + maxn;
   double* W = sm + 2 * maxn;
-  double* rowp = sm + 3 * maxn;  // (row, segment) partial sums, up to 2 maxn
-  double* red = sm + 5 * maxn;
+  double* CA = sm + 3 * maxn;  // this CTA's column sums, indexed by column
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  double* tl = sm + 4 * (size_t)maxn + (size_t)warp * kTileDoubles;
+  double* red = sm + 4 * (size_t)maxn + (size_t)kWarps * kTileDoubles;
+  double* part = work;                              // G x maxn column sums
+  double* rpart = work + (size_t)G * maxn;          // kWarps x maxn row sums
+  double* colb = rpart + (size_t)kWarps * maxn;     // 2 x maxn captured column
+  double* ybuf = colb + 2 * (size_t)maxn;           // maxn
+  double* dpart = ybuf + maxn;                      // G
   for (int qb = 0; qb < nbig; ++qb) {
     const int b = big[qb];
     const int n = A.bsize[b];
     double* H = A.H + A.hoff[b];
     const int so = A.soff[b];
-    if (n > maxn) {
-      if (rank == 0 && tid == 0) atomicOr(A.flag, DEV_SIZE);
+    if (n > maxn || n < 2) {
+      if (rank == 0 && tid == 0) {
+        if (n > maxn) atomicOr(A.flag, DEV_SIZE);
+        else if (n == 1) { A.d[so] = H[0]; A.e[so] = 0.0; A.tau[so] = 0.0; }
+      }
       continue;
     }
     double* vnew = V0;
     double* vold = V1;
     bool have_old = false;
-    int par = 0;
     for (int j = 0; j + 2 < n; ++j) {
+      const int m = n - j - 1;
+      // Row j of A^(j): row 0 of the input, later the column captured in the
+      // previous sweep; the pending update applied.  Also the row
+      // boundaries and the cleared column sums of this step.
+      const double* src = j == 0 ? H : colb + (size_t)((j - 1) & 1) * maxn;
+      double s = 0.0;
       for (int c = j + tid; c < n; c += kThreads) {
-        double a = __ldcg(H + (int64_t)j * n + c);
+        double a = __ldcg(src + c);
         if (have_old) a = fma(-vold[j], W[c], fma(-W[j], vold[c], a));
         vnew[c] = a;
+        if (c >= j + 2) s = fma(a, a, s);
       }
       if (have_old && rank == 0)
         for (int c = j + tid; c < n; c += kThreads) H[(int64_t)(j - 1) * n + c] = vold[c];
-      __syncthreads();
-      double s = 0.0;
-      for (int c = j + 2 + tid; c < n; c += kThreads) s = fma(vnew[c], vnew[c], s);
-      s = block_sum(s, red);
+      s = block_sum(s, red);  // synchronises: vnew visible
+      for (int c = j + 1 + tid; c < n; c += kThreads) CA[c] = 0.0;
       const double dj = vnew[j], alpha = vnew[j + 1];
       double tau, beta, scal;
       if (s == 0.0) {
@@ -269,61 +310,130 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_grid_kernel(TridiagArgs A
       for (int c = j + 1 + tid; c < n; c += kThreads) vnew[c] = (c == j + 1) ? 1.0 : vnew[c] * scal;
       if (rank == 0 && tid == 0) { A.d[so + j] = dj; A.e[so + j] = beta; A.tau[so + j] = tau; }
       __syncthreads();
-      const int m = n - j - 1;
-      const int rows_per = (m + G - 1) / G;
-      const int r0 = j + 1 + rank * rows_per;
-      const int nr = max(0, min(n, r0 + rows_per) - r0);
-      int S = kSeg;
-      while (S > 1 && rows_per * S > 2 * maxn) S >>= 1;
-      const int seglen = (((m + S - 1) / S) + 31) & ~31;
-      for (int it = warp; it < nr * S; it += kWarps) {
-        const int rr = it / S, sg = it - rr * S;
-        const int r = r0 + rr;
-        const int cb = j + 1 + sg * seglen, ce = min(n, cb + seglen);
-        double* Hr = H + (int64_t)r * n;
-        double acc = 0.0;
-        if (have_old) {
-          const double vr = vold[r], wr = W[r];
-          for (int c = cb + lane; c < ce; c += 32) {
-            double a = __ldcg(Hr + c);
-            a = fma(-vr, W[c], fma(-wr, vold[c], a));
-            __stcg(Hr + c, a);
-            acc = fma(a, vnew[c], acc);
-          }
-        } else {
-          for (int c = cb + lane; c < ce; c += 32) acc = fma(__ldcg(Hr + c), vnew[c], acc);
+
+      // The sweep over this CTA's rows: tiles of kRowTile rows x 32 columns.
+      double* cnext = colb + (size_t)(j & 1) * maxn;
+      const int ntiles = (m + kRowTile - 1) / kRowTile;
+      for (int q = 0;; ++q) {
+        // row tiles dealt g, 2G-1-g, 2G+g, 4G-1-g, ...: short and long rows alike
+        const int tt = (q >> 1) * 2 * G + ((q & 1) ? 2 * G - 1 - rank : rank);
+        if (tt >= ntiles) {
+          if ((q >> 1) * 2 * G >= ntiles) break;
+          continue;
         }
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) rowp[rr * S + sg] = acc;
+        const int t0 = j + 1 + tt * kRowTile, t1 = min(n, t0 + kRowTile);
+        const int ns = (t1 - 1 - j + 31) >> 5;  // strips covering columns j+1 .. t1-1
+        double P = 0.0;  // lane: row t0 + (lane % kRowTile), columns of its lane group
+        // strip st belongs to warp st % 32 < 16 ? st % 32 : 31 - st % 32 in every
+        // row tile (a snake over the warps: the strips' heights fall to the right)
+        for (int k = 0; k < 2 * ns; ++k) {
+          const int st = (k >> 1) * 32 + ((k & 1) ? 31 - warp : warp);
+          if (st >= ns) {
+            if ((k >> 1) * 32 >= ns) break;
+            continue;
+          }
+          const int c = j + 1 + st * 32 + lane;
+          const bool okc = c < t1;
+          double vc = 0.0, wc = 0.0, vn = 0.0;
+          if (okc) {
+            vn = vnew[c];
+            if (have_old) { vc = vold[c]; wc = W[c]; }
+          }
+          double a[kRowTile];
+#pragma unroll
+          for (int rr = 0; rr < kRowTile; ++rr) {
+            const int r = t0 + rr;
+            a[rr] = (okc && r < t1 && c <= r) ? __ldcg(H + (int64_t)r * n + c) : 0.0;
+          }
+          double acc = 0.0;
+#pragma unroll
+          for (int rr = 0; rr < kRowTile; ++rr) {
+            const int r = t0 + rr;
+            const bool ok = okc && r < t1 && c <= r;
+            double x = a[rr];
+            if (ok) {
+              if (have_old) {
+                x = fma(-vold[r], wc, fma(-W[r], vc, x));
+                __stcg(H + (int64_t)r * n + c, x);
+              }
+              if (c == j + 1) __stcg(cnext + r, x);
+              if (c < r) acc = fma(x, vnew[r], acc);
+            }
+            tl[rr * kTileLd + lane] = ok ? x : 0.0;
+          }
+          tl[kRowTile * kTileLd + lane] = vn;
+          if (okc) CA[c] += acc;
+          __syncwarp();
+          {
+            // lane: row rr of the tile, columns q*kGroup .. q*kGroup+kGroup-1 of
+            // the strip (32 / kRowTile lane groups share the 32 columns)
+            constexpr int kGroup = 32 / (32 / kRowTile);
+            const int rr = lane % kRowTile, q = lane / kRowTile;
+            const double* trow = tl + rr * kTileLd + q * kGroup;
+            const double* tv = tl + kRowTile * kTileLd + q * kGroup;
+#pragma unroll
+            for (int k = 0; k < kGroup; ++k) P = fma(trow[k], tv[k], P);
+          }
+          __syncwarp();
+        }
+#pragma unroll
+        for (int o = kRowTile; o < 32; o <<= 1) P += __shfl_xor_sync(0xffffffffu, P, o);
+        if (lane < kRowTile && t0 + lane < t1) __stcg(rpart + (size_t)warp * maxn + t0 + lane, P);
       }
       __syncthreads();
-      double* yb = work + (int64_t)par * maxn;
-      double* db = work + 2 * (int64_t)maxn + par * G;
-      double dpart = 0.0;
-      for (int rr = tid; rr < nr; rr += kThreads) {
-        double y = 0.0;
-        for (int sg = 0; sg < S; ++sg) y += rowp[rr * S + sg];
-        y *= tau;
-        __stcg(yb + r0 + rr, y);
-        dpart = fma(y, vnew[r0 + rr], dpart);
-      }
-      dpart = block_sum(dpart, red);
-      if (tid == 0) __stcg(db + rank, dpart);
+      for (int c = j + 1 + tid; c < n; c += kThreads) __stcg(part + (size_t)rank * maxn + c, CA[c]);
       grid.sync();
-      double dt = 0.0;
+
+      // y = tau A v over this CTA's even share of the columns, in a fixed order.
+      const int chunk = (m + G - 1) / G;
+      const int q0 = j + 1 + rank * chunk, q1 = min(n, q0 + chunk);
+      // Eight threads per column, each over every eighth share, so that the
+      // loads of a column are in flight together; then a shuffle tree.
+      double dp = 0.0;
+      for (int cb = q0; cb < q1; cb += kThreads / 8) {
+        const int c = cb + (tid >> 3), sub = tid & 7;
+        double y = 0.0;
+        if (c < q1) {
+          // all of a thread's loads issued before the first add (8 per round)
+          double v[8];
+#pragma unroll
+          for (int k = 0; k < kWarps / 8; ++k) v[k] = __ldcg(rpart + (size_t)(sub + 8 * k) * maxn + c);
+#pragma unroll
+          for (int k = 0; k < kWarps / 8; ++k) y += v[k];
+          for (int g0 = sub; g0 < G; g0 += 64) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              const int g = g0 + 8 * k;
+              v[k] = g < G ? __ldcg(part + (size_t)g * maxn + c) : 0.0;
+            }
+#pragma unroll
+            for (int k = 0; k < 8; ++k) y += v[k];
+          }
+        }
+        y += __shfl_xor_sync(0xffffffffu, y, 1);
+        y += __shfl_xor_sync(0xffffffffu, y, 2);
+        y += __shfl_xor_sync(0xffffffffu, y, 4);
+        if (c < q1 && sub == 0) {
+          y *= tau;
+          __stcg(ybuf + c, y);
+          dp = fma(y, vnew[c], dp);
+        }
+      }
+      dp = block_sum(dp, red);
+      if (tid == 0) __stcg(dpart + rank, dp);
+      grid.sync();
       if (tid < 32) {
-        for (int q = lane; q < G; q += 32) dt += __ldcg(db + q);
+        double dt = 0.0;
+        for (int q = lane; q < G; q += 32) dt += __ldcg(dpart + q);
         for (int o = 16; o > 0; o >>= 1) dt += __shfl_xor_sync(0xffffffffu, dt, o);
         if (lane == 0) red[kWarps + 1] = dt;
       }
       __syncthreads();
-      dt = red[kWarps + 1];
-      const double h = 0.5 * tau * dt;
-      for (int c = j + 1 + tid; c < n; c += kThreads) W[c] = fma(-h, vnew[c], __ldcg(yb + c));
+      const double h = 0.5 * tau * red[kWarps + 1];
+      for (int c = j + 1 + tid; c < n; c += kThreads) W[c] = fma(-h, vnew[c], __ldcg(ybuf + c));
       __syncthreads();
       double* t = vnew; vnew = vold; vold = t;
       have_old = true;
-      par ^= 1;
     }
     if (rank == 0) {
       if (have_old)
@@ -340,14 +450,15 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_grid_kernel(TridiagArgs A
         A.d[so + j + 1] = a11; A.e[so + j + 1] = 0.0; A.tau[so + j + 1] = 0.0;
       }
     }
-    grid.sync();  // the next block's phase 1 must not race the last writes
+    grid.sync();  // the next block's first reads must not race the last writes
   }
 }
 
 }  // namespace
 
 int tridiag_grid_size(int maxn) {
-  size_t smem = sizeof(double) * (5 * (size_t)maxn + kWarps + 4) + 16;
+  const size_t smem = grid_smem_bytes(maxn);
+  if (smem > (size_t)max_dyn_smem()) return 0;
   if (cudaFuncSetAttribute(tridiag_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()) !=
       cudaSuccess)
     return 0;
@@ -359,11 +470,14 @@ int tridiag_grid_size(int maxn) {
   return per_sm >= 1 ? sms : 0;  // one CTA per SM
 }
 
-size_t tridiag_grid_work(int maxn, int grid) { return 2 * (size_t)maxn + 2 * (size_t)grid + 64; }
+size_t tridiag_grid_work(int maxn, int grid) {
+  return ((size_t)grid + kWarps + 4) * (size_t)maxn + (size_t)grid + 64;
+}
 
 cudaError_t launch_tridiag_grid(const TridiagArgs& a, const int* big, int nbig, double* work, int grid,
                                 cudaStream_t s) {
-  size_t smem = sizeof(double) * (5 * (size_t)a.maxn + kWarps + 4) + 16;
+  const size_t smem = grid_smem_bytes(a.maxn);
+  if (smem > (size_t)max_dyn_smem() || grid < 1) return cudaErrorInvalidValue;
   cudaError_t err =
       cudaFuncSetAttribute(tridiag_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem());
   if (err != cudaSuccess) return err;
