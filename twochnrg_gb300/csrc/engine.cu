@@ -52,10 +52,12 @@ struct DevBuf {
   void* p = nullptr;
   size_t cap = 0;
   ~DevBuf() { if (p) cudaFree(p); }
+  // Grows by at least half the current capacity, so that a sweep whose
+  // sizes creep up reallocates rarely (cudaFree synchronises the device).
   void ensure(size_t bytes) {
     if (bytes <= cap) return;
+    const size_t want = std::max(bytes, cap + cap / 2);
     if (p) { CU(cudaFree(p)); p = nullptr; cap = 0; }
-    size_t want = std::max(bytes, cap + cap / 2);
     CU(cudaMalloc(&p, want));
     cap = want;
   }

@@ -1,23 +1,29 @@
 // Batched Householder tridiagonalization of all H_N blocks of one iteration
-// in a single persistent launch (FP64).
+// (FP64).
 //
 // This is the first half of the reference's per-block LAPACK dspev call
 // (CNRGmatrix::DiagBlock, NRGmatrixClass.cpp:638-656), re-designed for the
-// GB300: one thread-block CLUSTER owns one H_N block at a time and pulls the
-// next block (largest first) from a global work counter.  The CTAs of the
-// cluster split the trailing matrix by rows; per Householder step they make
-// one pass over their rows that applies the previous step's rank-2 update and
-// accumulates their share of the symmetric product A v in shared memory; the
-// shares are summed through distributed shared memory after one hardware
-// cluster barrier.  The matrix lives in HBM/L2 (full storage, both
-// triangles kept symmetric); each step touches every trailing element once.
+// GB300.  Both kernels work on the LOWER triangle of each block only: per
+// Householder step a stored element a_rc (c <= r) takes the pending rank-2
+// update (2 FMA), is written back, and contributes to y = A v twice, a_rc v_c
+// to row r and a_rc v_r to column c (2 FMA) -- 2/3 n^3 FMA per block, the
+// algorithmic count (a full-storage update does n^3).  The shared sweep is
+// lower_sweep below; the kernels differ in who cooperates on a block:
+//   tridiag_kernel       one thread-block CLUSTER per block (blocks pulled
+//                        largest first from a work counter); the CTAs' shares
+//                        of y are summed through distributed shared memory
+//                        after one hardware cluster barrier per step;
+//   tridiag_grid_kernel  every CTA of a cooperative grid on the same block
+//                        (the largest blocks), two grid barriers per step.
 //
 // Outputs: d (diagonal), e (sub-diagonal), tau (reflector scalars) at the
 // block's state offset, and the Householder vector v_j (v_j[j+1] = 1) in row j
-// of the block's matrix, columns j+1..n-1, for the back-transformation.
+// of the block's matrix, columns j+1..n-1 (the upper triangle, free storage),
+// for the back-transformation.
 //
-// There are no spin waits: the only synchronisation is barrier.cluster, which
-// every CTA of a cluster reaches the same number of times.
+// There are no spin waits: the only synchronisation is barrier.cluster and
+// the cooperative grid barrier, which every CTA reaches the same number of
+// times.
 #include <cooperative_groups.h>
 
 #include "nrg_device.cuh"
@@ -49,20 +55,125 @@ __device__ double block_sum(double v, double* red) {
   return red[kWarps];
 }
 
+constexpr int kRowTile = 8;
+constexpr int kTileLd = 33;  // padded row of a warp's transpose tile
+constexpr int kTileDoubles = (kRowTile + 1) * kTileLd;  // + one row for v of the strip's columns
+
+__host__ __device__ constexpr size_t grid_smem_doubles(int maxn) {
+  return 4 * (size_t)maxn + (size_t)kWarps * kTileDoubles + kWarps + 4;
+}
+__host__ __device__ constexpr size_t grid_smem_bytes(int maxn) { return sizeof(double) * grid_smem_doubles(maxn); }
+
+// One Householder step's sweep over the trailing lower triangle of part
+// `rank` of `parts` (the CTAs of a grid or of a cluster): rows j+1..n-1 in
+// tiles of kRowTile rows dealt rank, 2 parts-1-rank, 2 parts+rank, ...; strips
+// of 32 columns snaked over the warps (strip s to the same warp in every
+// tile).  Each stored element a_rc (c <= r) gets the pending rank-2 update
+// (vold, W; have_old), is written back, adds a_rc v_r to the column sum CA[c]
+// (c < r; the CTA's own array, one warp per column) and a_rc v_c to the row
+// sum of r.  Per row tile, row_sink(k, t0, t1, P) receives the warp's row
+// sums (lane l < kRowTile: row t0 + l; k counts this part's tiles) and
+// capture(r, x) the updated element of column j+1 of every row.
+template <class RowSink, class Capture>
+__device__ __forceinline__ void lower_sweep(double* H, int n, int j, int parts, int rank, bool have_old,
+                                            const double* vnew, const double* vold, const double* W, double* CA,
+                                            double* tl, RowSink row_sink, Capture capture) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int m = n - j - 1;
+  const int ntiles = (m + kRowTile - 1) / kRowTile;
+  int k_own = 0;
+  for (int q = 0;; ++q) {
+    // row tiles dealt g, 2G-1-g, 2G+g, 4G-1-g, ...: short and long rows alike
+    const int tt = (q >> 1) * 2 * parts + ((q & 1) ? 2 * parts - 1 - rank : rank);
+    if (tt >= ntiles) {
+      if ((q >> 1) * 2 * parts >= ntiles) break;
+      continue;
+    }
+    const int t0 = j + 1 + tt * kRowTile, t1 = min(n, t0 + kRowTile);
+    const int ns = (t1 - 1 - j + 31) >> 5;  // strips covering columns j+1 .. t1-1
+    double P = 0.0;  // lane: row t0 + (lane % kRowTile), columns of its lane group
+    // strip st belongs to warp st % 32 < 16 ? st % 32 : 31 - st % 32 in every
+    // row tile (a snake over the warps: the strips' heights fall to the right)
+    for (int ks = 0; ks < 2 * ns; ++ks) {
+      const int st = (ks >> 1) * 32 + ((ks & 1) ? 31 - warp : warp);
+      if (st >= ns) {
+        if ((ks >> 1) * 32 >= ns) break;
+        continue;
+      }
+      const int c = j + 1 + st * 32 + lane;
+      const bool okc = c < t1;
+      double vc = 0.0, wc = 0.0, vn = 0.0;
+      if (okc) {
+        vn = vnew[c];
+        if (have_old) { vc = vold[c]; wc = W[c]; }
+      }
+      double a[kRowTile];
+#pragma unroll
+      for (int rr = 0; rr < kRowTile; ++rr) {
+        const int r = t0 + rr;
+        a[rr] = (okc && r < t1 && c <= r) ? __ldcg(H + (int64_t)r * n + c) : 0.0;
+      }
+      double acc = 0.0;
+#pragma unroll
+      for (int rr = 0; rr < kRowTile; ++rr) {
+        const int r = t0 + rr;
+        const bool ok = okc && r < t1 && c <= r;
+        double x = a[rr];
+        if (ok) {
+          if (have_old) {
+            x = fma(-vold[r], wc, fma(-W[r], vc, x));
+            __stcg(H + (int64_t)r * n + c, x);
+          }
+          if (c == j + 1) capture(r, x);
+          if (c < r) acc = fma(x, vnew[r], acc);
+        }
+        tl[rr * kTileLd + lane] = ok ? x : 0.0;
+      }
+      tl[kRowTile * kTileLd + lane] = vn;
+      if (okc) CA[c] += acc;
+      __syncwarp();
+      {
+        // lane: row rr of the tile, columns g*kGroup .. g*kGroup+kGroup-1 of
+        // the strip (32 / kRowTile lane groups share the 32 columns)
+        constexpr int kGroup = 32 / (32 / kRowTile);
+        const int rr = lane % kRowTile, g = lane / kRowTile;
+        const double* trow = tl + rr * kTileLd + g * kGroup;
+        const double* tv = tl + kRowTile * kTileLd + g * kGroup;
+#pragma unroll
+        for (int x = 0; x < kGroup; ++x) P = fma(trow[x], tv[x], P);
+      }
+      __syncwarp();
+    }
+#pragma unroll
+    for (int o = kRowTile; o < 32; o <<= 1) P += __shfl_xor_sync(0xffffffffu, P, o);
+    row_sink(k_own, t0, t1, P);
+    ++k_own;
+  }
+}
+
+// Rows of the trailing matrix a CTA of a cluster of `cluster` CTAs can own
+// (row tiles dealt as in lower_sweep), for its row-sum buffer.
+__host__ __device__ constexpr int cluster_own_rows(int maxn, int cluster) {
+  return kRowTile * (((maxn + kRowTile - 1) / kRowTile + cluster - 1) / cluster + 1);
+}
+
 __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
   extern __shared__ double sm[];
   cg::cluster_group cl = cg::this_cluster();
   const int CL = (int)cl.num_blocks();
   const int rank = (int)cl.block_rank();
   const int maxn = A.maxn;
+  const int own_max = cluster_own_rows(maxn, CL);
   double* V0 = sm;
   double* V1 = sm + maxn;
   double* W = sm + 2 * maxn;
   double* Y0 = sm + 3 * maxn;
   double* Y1 = sm + 4 * maxn;
-  double* red = sm + 5 * maxn;  // kWarps + 1 doubles
-  int* sblk = (int*)(red + kWarps + 2);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  double* tl = sm + 5 * (size_t)maxn + (size_t)warp * kTileDoubles;
+  double* rowp = sm + 5 * (size_t)maxn + (size_t)kWarps * kTileDoubles;  // kWarps x own_max
+  double* red = rowp + (size_t)kWarps * own_max;  // kWarps + 2 doubles
+  int* sblk = (int*)(red + kWarps + 2);
 
   for (;;) {
     if (rank == 0 && tid == 0) *sblk = atomicAdd(A.queue, 1);
@@ -86,7 +197,9 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
     double* vold = V1;
     bool have_old = false;
     for (int j = 0; j + 2 < n; ++j) {
-      // Phase 1: row j of A^(j) (pending rank-2 update applied) -> x.
+      // Phase 1: row j of A^(j) -> vnew.  Row 0 is the input's; row j > 0
+      // holds column j as the previous sweep captured it (updated through
+      // step j-2) in its upper part; the pending update is applied here.
       double s = 0.0;
       for (int c = j + tid; c < n; c += kThreads) {
         double a = __ldcg(H + (int64_t)j * n + c);
@@ -94,8 +207,6 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
         vnew[c] = a;
         if (c >= j + 2) s = fma(a, a, s);
       }
-      if (have_old && rank == 0)
-        for (int c = j + tid; c < n; c += kThreads) H[(int64_t)(j - 1) * n + c] = vold[c];
       s = block_sum(s, red);
       const double dj = vnew[j], alpha = vnew[j + 1];
       double tau, beta, scal;
@@ -107,59 +218,39 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
         scal = 1.0 / (alpha - beta);
       }
       __syncthreads();
-      for (int c = j + 1 + tid; c < n; c += kThreads) vnew[c] = (c == j + 1) ? 1.0 : vnew[c] * scal;
+      // v_{j-1} into row j-1 (its upper part was last read at step j-1)
+      if (have_old && rank == 0)
+        for (int c = j + tid; c < n; c += kThreads) H[(int64_t)(j - 1) * n + c] = vold[c];
+      double* yp = (j & 1) ? Y1 : Y0;
+      for (int c = j + 1 + tid; c < n; c += kThreads) {
+        vnew[c] = (c == j + 1) ? 1.0 : vnew[c] * scal;
+        yp[c] = 0.0;
+      }
       if (rank == 0 && tid == 0) { A.d[so + j] = dj; A.e[so + j] = beta; A.tau[so + j] = tau; }
       __syncthreads();
 
-      // Phase 2: this CTA's rows of the trailing block: apply the pending
-      // update, store, and accumulate column sums of A^(j) v_j.
-      const int m = n - j - 1;
-      const int rows_per = (m + CL - 1) / CL;
-      const int r0 = j + 1 + rank * rows_per;
-      const int r1 = min(n, r0 + rows_per);
-      double* yp = (j & 1) ? Y1 : Y0;
-      const int nchunks = (m + 63) / 64;
-      for (int chk = warp; chk < nchunks; chk += kWarps) {
-        const int c0 = j + 1 + chk * 64 + lane;
-        const int c1 = c0 + 32;
-        const bool ok0 = c0 < n, ok1 = c1 < n;
-        double vo0 = 0.0, wo0 = 0.0, vo1 = 0.0, wo1 = 0.0;
-        if (have_old) {
-          if (ok0) { vo0 = vold[c0]; wo0 = W[c0]; }
-          if (ok1) { vo1 = vold[c1]; wo1 = W[c1]; }
+      // Phase 2: this CTA's row tiles of the trailing lower triangle: the
+      // pending update, column sums of y into its share yp, row sums per
+      // warp; column j+1 captured into the upper part of row j+1.
+      lower_sweep(H, n, j, CL, rank, have_old, vnew, vold, W, yp, tl,
+                  [&](int k, int, int, double P) {
+                    if (lane < kRowTile) rowp[(size_t)warp * own_max + k * kRowTile + lane] = P;
+                  },
+                  [&](int r, double x) { __stcg(H + (int64_t)(j + 1) * n + r, x); });
+      __syncthreads();
+      {
+        // the warps' row sums of the CTA's own rows into its share
+        const int m = n - j - 1;
+        const int ntiles = (m + kRowTile - 1) / kRowTile;
+        for (int idx = tid; idx < own_max; idx += kThreads) {
+          const int k = idx / kRowTile, rr = idx - k * kRowTile;
+          const int tt = (k >> 1) * 2 * CL + ((k & 1) ? 2 * CL - 1 - rank : rank);
+          const int r = j + 1 + tt * kRowTile + rr;
+          if (tt >= ntiles || r >= n) continue;
+          double v = 0.0;
+          for (int w = 0; w < kWarps; ++w) v += rowp[(size_t)w * own_max + idx];
+          yp[r] += v;
         }
-        double acc0 = 0.0, acc1 = 0.0;
-        int r = r0;
-        for (; r + 1 < r1; r += 2) {  // two rows in flight
-          const double* Ha = H + (int64_t)r * n;
-          const double* Hb = Ha + n;
-          double a0 = ok0 ? __ldcg(Ha + c0) : 0.0, a1 = ok1 ? __ldcg(Ha + c1) : 0.0;
-          double b0 = ok0 ? __ldcg(Hb + c0) : 0.0, b1 = ok1 ? __ldcg(Hb + c1) : 0.0;
-          if (have_old) {
-            const double vra = vold[r], wra = W[r], vrb = vold[r + 1], wrb = W[r + 1];
-            a0 = fma(-vra, wo0, fma(-wra, vo0, a0)); a1 = fma(-vra, wo1, fma(-wra, vo1, a1));
-            b0 = fma(-vrb, wo0, fma(-wrb, vo0, b0)); b1 = fma(-vrb, wo1, fma(-wrb, vo1, b1));
-            if (ok0) { __stcg((double*)Ha + c0, a0); __stcg((double*)Hb + c0, b0); }
-            if (ok1) { __stcg((double*)Ha + c1, a1); __stcg((double*)Hb + c1, b1); }
-          }
-          const double va = vnew[r], vb = vnew[r + 1];
-          acc0 = fma(a0, va, acc0); acc1 = fma(a1, va, acc1);
-          acc0 = fma(b0, vb, acc0); acc1 = fma(b1, vb, acc1);
-        }
-        if (r < r1) {
-          const double* Ha = H + (int64_t)r * n;
-          double a0 = ok0 ? __ldcg(Ha + c0) : 0.0, a1 = ok1 ? __ldcg(Ha + c1) : 0.0;
-          if (have_old) {
-            const double vra = vold[r], wra = W[r];
-            a0 = fma(-vra, wo0, fma(-wra, vo0, a0)); a1 = fma(-vra, wo1, fma(-wra, vo1, a1));
-            if (ok0) __stcg((double*)Ha + c0, a0);
-            if (ok1) __stcg((double*)Ha + c1, a1);
-          }
-          const double va = vnew[r];
-          acc0 = fma(a0, va, acc0); acc1 = fma(a1, va, acc1);
-        }
-        if (ok0) yp[c0] = acc0;
-        if (ok1) yp[c1] = acc1;
       }
       cl.sync();
 
@@ -188,7 +279,7 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
       double* t = vnew; vnew = vold; vold = t;
       have_old = true;
     }
-    // Last 2x2 block with the pending update, and the last reflector.
+    // Last 2x2 block (lower triangle) with the pending update, and the last reflector.
     if (rank == 0) {
       if (have_old)
         for (int c = n - 2 + tid; c < n; c += kThreads) H[(int64_t)(n - 3) * n + c] = vold[c];
@@ -237,15 +328,6 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
 // columns j+1..n-1 for the back-transformation, as in tridiag_kernel.
 // Every sum has a fixed order, so all CTAs hold bitwise identical vectors
 // and the result does not depend on timing.
-constexpr int kRowTile = 8;
-constexpr int kTileLd = 33;  // padded row of a warp's transpose tile
-constexpr int kTileDoubles = (kRowTile + 1) * kTileLd;  // + one row for v of the strip's columns
-
-__host__ __device__ constexpr size_t grid_smem_doubles(int maxn) {
-  return 4 * (size_t)maxn + (size_t)kWarps * kTileDoubles + kWarps + 4;
-}
-__host__ __device__ constexpr size_t grid_smem_bytes(int maxn) { return sizeof(double) * grid_smem_doubles(maxn); }
-
 __global__ void __launch_bounds__(kThreads, 1) tridiag_grid_kernel(TridiagArgs A, const int* big, int nbig,
                                                                   double* work) {
   extern __shared__ double sm[];
@@ -311,75 +393,13 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_grid_kernel(TridiagArgs A
       if (rank == 0 && tid == 0) { A.d[so + j] = dj; A.e[so + j] = beta; A.tau[so + j] = tau; }
       __syncthreads();
 
-      // The sweep over this CTA's rows: tiles of kRowTile rows x 32 columns.
+      // The sweep over this CTA's row tiles; row sums to rpart, column j+1 to colb.
       double* cnext = colb + (size_t)(j & 1) * maxn;
-      const int ntiles = (m + kRowTile - 1) / kRowTile;
-      for (int q = 0;; ++q) {
-        // row tiles dealt g, 2G-1-g, 2G+g, 4G-1-g, ...: short and long rows alike
-        const int tt = (q >> 1) * 2 * G + ((q & 1) ? 2 * G - 1 - rank : rank);
-        if (tt >= ntiles) {
-          if ((q >> 1) * 2 * G >= ntiles) break;
-          continue;
-        }
-        const int t0 = j + 1 + tt * kRowTile, t1 = min(n, t0 + kRowTile);
-        const int ns = (t1 - 1 - j + 31) >> 5;  // strips covering columns j+1 .. t1-1
-        double P = 0.0;  // lane: row t0 + (lane % kRowTile), columns of its lane group
-        // strip st belongs to warp st % 32 < 16 ? st % 32 : 31 - st % 32 in every
-        // row tile (a snake over the warps: the strips' heights fall to the right)
-        for (int k = 0; k < 2 * ns; ++k) {
-          const int st = (k >> 1) * 32 + ((k & 1) ? 31 - warp : warp);
-          if (st >= ns) {
-            if ((k >> 1) * 32 >= ns) break;
-            continue;
-          }
-          const int c = j + 1 + st * 32 + lane;
-          const bool okc = c < t1;
-          double vc = 0.0, wc = 0.0, vn = 0.0;
-          if (okc) {
-            vn = vnew[c];
-            if (have_old) { vc = vold[c]; wc = W[c]; }
-          }
-          double a[kRowTile];
-#pragma unroll
-          for (int rr = 0; rr < kRowTile; ++rr) {
-            const int r = t0 + rr;
-            a[rr] = (okc && r < t1 && c <= r) ? __ldcg(H + (int64_t)r * n + c) : 0.0;
-          }
-          double acc = 0.0;
-#pragma unroll
-          for (int rr = 0; rr < kRowTile; ++rr) {
-            const int r = t0 + rr;
-            const bool ok = okc && r < t1 && c <= r;
-            double x = a[rr];
-            if (ok) {
-              if (have_old) {
-                x = fma(-vold[r], wc, fma(-W[r], vc, x));
-                __stcg(H + (int64_t)r * n + c, x);
-              }
-              if (c == j + 1) __stcg(cnext + r, x);
-              if (c < r) acc = fma(x, vnew[r], acc);
-            }
-            tl[rr * kTileLd + lane] = ok ? x : 0.0;
-          }
-          tl[kRowTile * kTileLd + lane] = vn;
-          if (okc) CA[c] += acc;
-          __syncwarp();
-          {
-            // lane: row rr of the tile, columns q*kGroup .. q*kGroup+kGroup-1 of
-            // the strip (32 / kRowTile lane groups share the 32 columns)
-            constexpr int kGroup = 32 / (32 / kRowTile);
-            const int rr = lane % kRowTile, q = lane / kRowTile;
-            const double* trow = tl + rr * kTileLd + q * kGroup;
-            const double* tv = tl + kRowTile * kTileLd + q * kGroup;
-#pragma unroll
-            for (int k = 0; k < kGroup; ++k) P = fma(trow[k], tv[k], P);
-          }
-          __syncwarp();
-        }
-#pragma unroll
-        for (int o = kRowTile; o < 32; o <<= 1) P += __shfl_xor_sync(0xffffffffu, P, o);
-        if (lane < kRowTile && t0 + lane < t1) __stcg(rpart + (size_t)warp * maxn + t0 + lane, P);
-      }
+      lower_sweep(H, n, j, G, rank, have_old, vnew, vold, W, CA, tl,
+                  [&](int, int t0, int t1, double P) {
+                    if (lane < kRowTile && t0 + lane < t1) __stcg(rpart + (size_t)warp * maxn + t0 + lane, P);
+                  },
+                  [&](int r, double x) { __stcg(cnext + r, x); });
       __syncthreads();
       for (int c = j + 1 + tid; c < n; c += kThreads) __stcg(part + (size_t)rank * maxn + c, CA[c]);
       grid.sync();
@@ -486,12 +506,14 @@ cudaError_t launch_tridiag_grid(const TridiagArgs& a, const int* big, int nbig, 
   return cudaLaunchCooperativeKernel((const void*)tridiag_grid_kernel, dim3(grid), dim3(kThreads), args, smem, s);
 }
 
-size_t tridiag_smem_bytes(int maxn) {
-  return sizeof(double) * (5 * (size_t)maxn + kWarps + 4) + 16;
+size_t tridiag_smem_bytes(int maxn, int cluster) {
+  return sizeof(double) * (5 * (size_t)maxn + (size_t)kWarps * kTileDoubles +
+                           (size_t)kWarps * cluster_own_rows(maxn, cluster) + kWarps + 2) + 16;
 }
 
 cudaError_t launch_tridiag(const TridiagArgs& a, int cluster, int nclusters, cudaStream_t s) {
-  size_t smem = tridiag_smem_bytes(a.maxn);
+  size_t smem = tridiag_smem_bytes(a.maxn, cluster);
+  if (smem > (size_t)max_dyn_smem()) return cudaErrorInvalidValue;
   cudaError_t err = cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem());
   if (err != cudaSuccess) return err;
   if (cluster > 8) {
@@ -514,7 +536,8 @@ cudaError_t launch_tridiag(const TridiagArgs& a, int cluster, int nclusters, cud
 }
 
 int tridiag_max_clusters(int cluster, int maxn) {
-  size_t smem = tridiag_smem_bytes(maxn);
+  size_t smem = tridiag_smem_bytes(maxn, cluster);
+  if (smem > (size_t)max_dyn_smem()) return 0;
   if (cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()) != cudaSuccess)
     return 0;
   if (cluster > 8) cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);

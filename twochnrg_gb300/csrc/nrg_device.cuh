@@ -131,7 +131,7 @@ struct TridiagArgs {
   int maxn;
 };
 cudaError_t launch_tridiag(const TridiagArgs& a, int cluster, int nclusters, cudaStream_t s);
-size_t tridiag_smem_bytes(int maxn);
+size_t tridiag_smem_bytes(int maxn, int cluster);
 int tridiag_max_clusters(int cluster, int maxn);
 // Whole-GPU cooperative variant for the largest blocks (processed in turn).
 int tridiag_grid_size(int maxn);
