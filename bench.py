@@ -58,11 +58,11 @@ CPU_ITERS = 4
 # seconds per iteration of the same workload.
 REF_FIXTURE = "cfg1_2chQS_n5_k3000"
 # DRAM traffic of the tridiagonalization, from the ncu capture summarised in
-# profiles/tridiag_fp64_2chQS.md: one n = 2400 block read 46 MB (its n^2
-# doubles, touched once; the rest of the passes hit L2) and wrote 5 MB.  The
-# traffic of a launch therefore scales with the n^2 of its blocks, not with
-# the flops: 8 B x n^2 x (1 + 5/46).
-TRIDIAG_DRAM_BYTES_PER_ELEMENT = 8.0 * (1.0 + 5.0 / 46.0)
+# profiles/tridiag_fp64_2chQS.md: one n = 2400 block read 23.3 MB (its lower
+# triangle, n^2/2 doubles, touched once; the rest of the passes hit L2) and
+# wrote 4.4 MB.  The traffic of a launch therefore scales with the n^2 of its
+# blocks, not with the flops: 4 B x n^2 x (1 + 4.4/23.3).
+TRIDIAG_DRAM_BYTES_PER_ELEMENT = 4.0 * (1.0 + 4.4 / 23.3)
 
 
 def max_over_ranks(dist, *vals):
@@ -410,7 +410,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--batch-workers", type=int, default=16)
+    ap.add_argument("--batch-workers", type=int, default=8)
     ap.add_argument("--dm2ch", action="store_true",
                     help="only the two-channel DM-NRG spectral function (about 8 minutes and 190 GB at 3000 kept)")
     ap.add_argument("--dm2ch-ncutoff", type=int, default=DM2_WORKLOAD["ncutoff"])
@@ -435,8 +435,11 @@ def main():
     prec = tg.PREC_MIXED if args.precision == "mixed" else tg.PREC_FP64
     other = tg.PREC_FP64 if prec == tg.PREC_MIXED else tg.PREC_MIXED
     warm = dict(W, nsites=WARMUP_NSITES)
-    for _ in range(args.warmup):
-        eng.sweep(**warm, fetch=False, precision=prec)
+    for i in range(args.warmup):
+        # the first warm-up step is the whole sweep, so that every device buffer
+        # has reached its final size before the timed steps (a buffer that grows
+        # is freed and reallocated, and cudaFree synchronises the device)
+        eng.sweep(**(W if i == 0 else warm), fetch=False, precision=prec)
     peak = eng.fp64_peak()
     if dist:
         dist.barrier()
@@ -474,7 +477,7 @@ def main():
         "data": "synthetic",
         "config": {"workload": WORKLOAD_NAME, "precision": names[prec], "parallelism": f"replicas x{args.gpus}",
                    "l2": "working set (H_N blocks ~0.8 GB per iteration) larger than L2; no flush",
-                   "warmup_step": f"first {WARMUP_NSITES} iterations of the same workload"},
+                   "warmup_step": f"the whole sweep once, then its first {WARMUP_NSITES} iterations"},
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(T["h2d_bytes"]),
                 "d2h_bytes_per_step": int(T["d2h_bytes"])},
         "gpu_launches": int(launches),

@@ -888,7 +888,7 @@ class BatchResult:
     seconds: float
 
 
-def sweep_batch(instances, nworkers: int = 16, device: int = 0, precision: int = PREC_FP64) -> BatchResult:
+def sweep_batch(instances, nworkers: int = 8, device: int = 0, precision: int = PREC_FP64) -> BatchResult:
     """Run independent sweeps (dicts with the Engine.sweep keywords) on one
     GPU through nrg_sweep_batch."""
     L = load_library()

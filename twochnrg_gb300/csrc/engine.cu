@@ -350,9 +350,12 @@ void blocked_reduction(nrg_ctx* c, const EigPlan& P, const std::vector<int>& blo
   const int nb = kPanelNb, ld = 2 * kPanelNb;
   int maxn = 3;
   for (int b : blocks) maxn = std::max(maxn, P.bsize[b]);
-  c->pvw[slot].ensure(sizeof(double) * (size_t)maxn * ld);
-  c->pcol[slot].ensure(sizeof(double) * (2 * (size_t)maxn + 2 + (size_t)G * (ld + 2)));
-  c->ozk[slot].ensure(oz_work_bytes(maxn, maxn, ld, kOzSlices));
+  // sized for the next multiple of 1024 states: the largest block creeps up
+  // over a sweep, and a reallocation synchronises the device
+  const size_t nres = ((size_t)maxn + 1023) / 1024 * 1024;
+  c->pvw[slot].ensure(sizeof(double) * nres * ld);
+  c->pcol[slot].ensure(sizeof(double) * (2 * nres + 2 + (size_t)G * (ld + 2)));
+  c->ozk[slot].ensure(oz_work_bytes((int)nres, (int)nres, ld, kOzSlices));
   double* VW = c->pvw[slot].as<double>();
   double* col = c->pcol[slot].as<double>();
   double* ybuf = col + 2 * (size_t)maxn;
