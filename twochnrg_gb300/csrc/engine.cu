@@ -291,6 +291,15 @@ int choose_cluster(int maxn, bool shared_gpu) {
   return maxn >= 256 ? 16 : 8;
 }
 
+// Threads per CTA of the cluster kernel: 256 (two CTAs per SM) for the
+// workers of nrg_sweep_batch, whose small latency-bound blocks gain from more
+// of them in flight, else 512.
+int cluster_threads(bool shared_gpu) {
+  const char* s = std::getenv("NRG_CLUSTER_THREADS");
+  if (s) return std::atoi(s) == 256 ? 256 : 512;
+  return shared_gpu ? 256 : 512;
+}
+
 // Blocks at least this large are tridiagonalized by a cooperative grid of
 // many SMs (one block after the other per grid); smaller ones by one
 // thread-block cluster each.
@@ -512,11 +521,12 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
     ts.nblocks = nb - nbig;
     ts.maxn = std::max(maxs, 2);
     int cluster = choose_cluster(maxs, c->shared_gpu);
-    int ncl = tridiag_max_clusters(cluster, ts.maxn);
-    if (ncl <= 0) { cluster = 8; ncl = tridiag_max_clusters(cluster, ts.maxn); }
+    int threads = cluster_threads(c->shared_gpu);
+    int ncl = tridiag_max_clusters(cluster, ts.maxn, threads);
+    if (ncl <= 0) { cluster = 8; threads = 512; ncl = tridiag_max_clusters(cluster, ts.maxn, threads); }
     if (ncl <= 0) throw NrgError(NRG_ERR_SIZE, "tridiagonalization does not fit on the device");
     ncl = std::min(ncl, nb - nbig);
-    CU(launch_tridiag(ts, cluster, ncl, c->stream));
+    CU(launch_tridiag(ts, cluster, ncl, c->stream, threads));
     c->launches++; c->timing.tridiag_launches++;
   }
   for (int k = 0; K > 1 && k < K; ++k) CU(cudaStreamWaitEvent(c->stream, c->join[k], 0));

@@ -40,6 +40,7 @@ constexpr int kWarps = kThreads / 32;
 // Deterministic block-wide sum (same tree in every CTA of the cluster): a
 // shuffle tree per warp, then one over the warp sums (FP64 latency is long,
 // so no serial chains).
+template <int NW = kWarps>
 __device__ double block_sum(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -47,12 +48,12 @@ __device__ double block_sum(double v, double* red) {
   if (lane == 0) red[warp] = v;
   __syncthreads();
   if (warp == 0) {
-    double t = lane < kWarps ? red[lane] : 0.0;
+    double t = lane < NW ? red[lane] : 0.0;
     for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-    if (lane == 0) red[kWarps] = t;
+    if (lane == 0) red[NW] = t;
   }
   __syncthreads();
-  return red[kWarps];
+  return red[NW];
 }
 
 constexpr int kRowTile = 8;
@@ -67,14 +68,14 @@ __host__ __device__ constexpr size_t grid_smem_bytes(int maxn) { return sizeof(d
 // One Householder step's sweep over the trailing lower triangle of part
 // `rank` of `parts` (the CTAs of a grid or of a cluster): rows j+1..n-1 in
 // tiles of kRowTile rows dealt rank, 2 parts-1-rank, 2 parts+rank, ...; strips
-// of 32 columns snaked over the warps (strip s to the same warp in every
+// of 32 columns snaked over the NW warps (strip s to the same warp in every
 // tile).  Each stored element a_rc (c <= r) gets the pending rank-2 update
 // (vold, W; have_old), is written back, adds a_rc v_r to the column sum CA[c]
 // (c < r; the CTA's own array, one warp per column) and a_rc v_c to the row
 // sum of r.  Per row tile, row_sink(k, t0, t1, P) receives the warp's row
 // sums (lane l < kRowTile: row t0 + l; k counts this part's tiles) and
 // capture(r, x) the updated element of column j+1 of every row.
-template <class RowSink, class Capture>
+template <int NW, class RowSink, class Capture>
 __device__ __forceinline__ void lower_sweep(double* H, int n, int j, int parts, int rank, bool have_old,
                                             const double* vnew, const double* vold, const double* W, double* CA,
                                             double* tl, RowSink row_sink, Capture capture) {
@@ -92,12 +93,13 @@ __device__ __forceinline__ void lower_sweep(double* H, int n, int j, int parts, 
     const int t0 = j + 1 + tt * kRowTile, t1 = min(n, t0 + kRowTile);
     const int ns = (t1 - 1 - j + 31) >> 5;  // strips covering columns j+1 .. t1-1
     double P = 0.0;  // lane: row t0 + (lane % kRowTile), columns of its lane group
-    // strip st belongs to warp st % 32 < 16 ? st % 32 : 31 - st % 32 in every
-    // row tile (a snake over the warps: the strips' heights fall to the right)
+    // strip st belongs to warp st % 2NW < NW ? st % 2NW : 2NW-1 - st % 2NW in
+    // every row tile (a snake over the NW warps: the strips' heights fall to
+    // the right)
     for (int ks = 0; ks < 2 * ns; ++ks) {
-      const int st = (ks >> 1) * 32 + ((ks & 1) ? 31 - warp : warp);
+      const int st = (ks >> 1) * 2 * NW + ((ks & 1) ? 2 * NW - 1 - warp : warp);
       if (st >= ns) {
-        if ((ks >> 1) * 32 >= ns) break;
+        if ((ks >> 1) * 2 * NW >= ns) break;
         continue;
       }
       const int c = j + 1 + st * 32 + lane;
@@ -157,7 +159,12 @@ __host__ __device__ constexpr int cluster_own_rows(int maxn, int cluster) {
   return kRowTile * (((maxn + kRowTile - 1) / kRowTile + cluster - 1) / cluster + 1);
 }
 
-__global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
+// NT threads per CTA: 512 (one CTA per SM) when the sweep has the GPU to
+// itself, 256 (two per SM) for concurrent batch workers, whose small blocks
+// are latency-bound: twice as many blocks in flight.
+template <int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) tridiag_kernel(TridiagArgs A) {
+  constexpr int NW = NT / 32;
   extern __shared__ double sm[];
   cg::cluster_group cl = cg::this_cluster();
   const int CL = (int)cl.num_blocks();
@@ -171,9 +178,9 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
   double* Y1 = sm + 4 * maxn;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   double* tl = sm + 5 * (size_t)maxn + (size_t)warp * kTileDoubles;
-  double* rowp = sm + 5 * (size_t)maxn + (size_t)kWarps * kTileDoubles;  // kWarps x own_max
-  double* red = rowp + (size_t)kWarps * own_max;  // kWarps + 2 doubles
-  int* sblk = (int*)(red + kWarps + 2);
+  double* rowp = sm + 5 * (size_t)maxn + (size_t)NW * kTileDoubles;  // NW x own_max
+  double* red = rowp + (size_t)NW * own_max;  // NW + 2 doubles
+  int* sblk = (int*)(red + NW + 2);
 
   for (;;) {
     if (rank == 0 && tid == 0) *sblk = atomicAdd(A.queue, 1);
@@ -201,13 +208,13 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
       // holds column j as the previous sweep captured it (updated through
       // step j-2) in its upper part; the pending update is applied here.
       double s = 0.0;
-      for (int c = j + tid; c < n; c += kThreads) {
+      for (int c = j + tid; c < n; c += NT) {
         double a = __ldcg(H + (int64_t)j * n + c);
         if (have_old) a = fma(-vold[j], W[c], fma(-W[j], vold[c], a));
         vnew[c] = a;
         if (c >= j + 2) s = fma(a, a, s);
       }
-      s = block_sum(s, red);
+      s = block_sum<NW>(s, red);
       const double dj = vnew[j], alpha = vnew[j + 1];
       double tau, beta, scal;
       if (s == 0.0) {
@@ -220,9 +227,9 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
       __syncthreads();
       // v_{j-1} into row j-1 (its upper part was last read at step j-1)
       if (have_old && rank == 0)
-        for (int c = j + tid; c < n; c += kThreads) H[(int64_t)(j - 1) * n + c] = vold[c];
+        for (int c = j + tid; c < n; c += NT) H[(int64_t)(j - 1) * n + c] = vold[c];
       double* yp = (j & 1) ? Y1 : Y0;
-      for (int c = j + 1 + tid; c < n; c += kThreads) {
+      for (int c = j + 1 + tid; c < n; c += NT) {
         vnew[c] = (c == j + 1) ? 1.0 : vnew[c] * scal;
         yp[c] = 0.0;
       }
@@ -232,7 +239,7 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
       // Phase 2: this CTA's row tiles of the trailing lower triangle: the
       // pending update, column sums of y into its share yp, row sums per
       // warp; column j+1 captured into the upper part of row j+1.
-      lower_sweep(H, n, j, CL, rank, have_old, vnew, vold, W, yp, tl,
+      lower_sweep<NW>(H, n, j, CL, rank, have_old, vnew, vold, W, yp, tl,
                   [&](int k, int, int, double P) {
                     if (lane < kRowTile) rowp[(size_t)warp * own_max + k * kRowTile + lane] = P;
                   },
@@ -242,13 +249,13 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
         // the warps' row sums of the CTA's own rows into its share
         const int m = n - j - 1;
         const int ntiles = (m + kRowTile - 1) / kRowTile;
-        for (int idx = tid; idx < own_max; idx += kThreads) {
+        for (int idx = tid; idx < own_max; idx += NT) {
           const int k = idx / kRowTile, rr = idx - k * kRowTile;
           const int tt = (k >> 1) * 2 * CL + ((k & 1) ? 2 * CL - 1 - rank : rank);
           const int r = j + 1 + tt * kRowTile + rr;
           if (tt >= ntiles || r >= n) continue;
           double v = 0.0;
-          for (int w = 0; w < kWarps; ++w) v += rowp[(size_t)w * own_max + idx];
+          for (int w = 0; w < NW; ++w) v += rowp[(size_t)w * own_max + idx];
           yp[r] += v;
         }
       }
@@ -259,7 +266,7 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
         const double* rem[16];
 #pragma unroll
         for (int q = 0; q < 16; ++q) rem[q] = q < CL ? cl.map_shared_rank(yp, q) : yp;
-        for (int c = j + 1 + tid; c < n; c += kThreads) {
+        for (int c = j + 1 + tid; c < n; c += NT) {
           double sh[16];
 #pragma unroll
           for (int q = 0; q < 16; ++q) sh[q] = q < CL ? rem[q][c] : 0.0;  // all loads in flight
@@ -271,10 +278,10 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
       }
       __syncthreads();
       double dt = 0.0;
-      for (int c = j + 1 + tid; c < n; c += kThreads) dt = fma(W[c], vnew[c], dt);
-      dt = block_sum(dt, red);
+      for (int c = j + 1 + tid; c < n; c += NT) dt = fma(W[c], vnew[c], dt);
+      dt = block_sum<NW>(dt, red);
       const double h = 0.5 * tau * dt;
-      for (int c = j + 1 + tid; c < n; c += kThreads) W[c] = fma(-h, vnew[c], W[c]);
+      for (int c = j + 1 + tid; c < n; c += NT) W[c] = fma(-h, vnew[c], W[c]);
       __syncthreads();
       double* t = vnew; vnew = vold; vold = t;
       have_old = true;
@@ -282,7 +289,7 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_kernel(TridiagArgs A) {
     // Last 2x2 block (lower triangle) with the pending update, and the last reflector.
     if (rank == 0) {
       if (have_old)
-        for (int c = n - 2 + tid; c < n; c += kThreads) H[(int64_t)(n - 3) * n + c] = vold[c];
+        for (int c = n - 2 + tid; c < n; c += NT) H[(int64_t)(n - 3) * n + c] = vold[c];
       if (tid == 0) {
         const int j = n - 2;
         double a00 = H[(int64_t)j * n + j], a10 = H[(int64_t)(j + 1) * n + j], a11 = H[(int64_t)(j + 1) * n + j + 1];
@@ -395,7 +402,7 @@ __global__ void __launch_bounds__(kThreads, 1) tridiag_grid_kernel(TridiagArgs A
 
       // The sweep over this CTA's row tiles; row sums to rpart, column j+1 to colb.
       double* cnext = colb + (size_t)(j & 1) * maxn;
-      lower_sweep(H, n, j, G, rank, have_old, vnew, vold, W, CA, tl,
+      lower_sweep<kWarps>(H, n, j, G, rank, have_old, vnew, vold, W, CA, tl,
                   [&](int, int t0, int t1, double P) {
                     if (lane < kRowTile && t0 + lane < t1) __stcg(rpart + (size_t)warp * maxn + t0 + lane, P);
                   },
@@ -506,54 +513,60 @@ cudaError_t launch_tridiag_grid(const TridiagArgs& a, const int* big, int nbig, 
   return cudaLaunchCooperativeKernel((const void*)tridiag_grid_kernel, dim3(grid), dim3(kThreads), args, smem, s);
 }
 
-size_t tridiag_smem_bytes(int maxn, int cluster) {
-  return sizeof(double) * (5 * (size_t)maxn + (size_t)kWarps * kTileDoubles +
-                           (size_t)kWarps * cluster_own_rows(maxn, cluster) + kWarps + 2) + 16;
+size_t tridiag_smem_bytes(int maxn, int cluster, int threads) {
+  const size_t nw = (size_t)threads / 32;
+  return sizeof(double) * (5 * (size_t)maxn + nw * kTileDoubles + nw * cluster_own_rows(maxn, cluster) + nw + 2) + 16;
 }
 
-cudaError_t launch_tridiag(const TridiagArgs& a, int cluster, int nclusters, cudaStream_t s) {
-  size_t smem = tridiag_smem_bytes(a.maxn, cluster);
-  if (smem > (size_t)max_dyn_smem()) return cudaErrorInvalidValue;
-  cudaError_t err = cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem());
-  if (err != cudaSuccess) return err;
-  if (cluster > 8) {
-    err = cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (err != cudaSuccess) return err;
-  }
+namespace {
+const void* cluster_kernel(int threads) {
+  return threads == 256 ? (const void*)tridiag_kernel<256> : (const void*)tridiag_kernel<512>;
+}
+
+cudaLaunchConfig_t cluster_config(int cluster, int nclusters, int threads, size_t smem, cudaLaunchAttribute* attr) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(cluster * nclusters), 1, 1);
-  cfg.blockDim = dim3(kThreads, 1, 1);
+  cfg.blockDim = dim3((unsigned)threads, 1, 1);
   cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = (unsigned)cluster;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, tridiag_kernel, a);
+  return cfg;
 }
 
-int tridiag_max_clusters(int cluster, int maxn) {
-  size_t smem = tridiag_smem_bytes(maxn, cluster);
-  if (smem > (size_t)max_dyn_smem()) return 0;
-  if (cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()) != cudaSuccess)
-    return 0;
-  if (cluster > 8) cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)cluster, 1, 1);
-  cfg.blockDim = dim3(kThreads, 1, 1);
-  cfg.dynamicSmemBytes = smem;
+cudaError_t cluster_attributes(int cluster, int threads) {
+  const void* k = cluster_kernel(threads);
+  cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem());
+  if (err == cudaSuccess && cluster > 8) err = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  return err;
+}
+}  // namespace
+
+cudaError_t launch_tridiag(const TridiagArgs& a, int cluster, int nclusters, cudaStream_t s, int threads) {
+  if (threads != 256 && threads != 512) return cudaErrorInvalidValue;
+  const size_t smem = tridiag_smem_bytes(a.maxn, cluster, threads);
+  if (smem > (size_t)max_dyn_smem()) return cudaErrorInvalidValue;
+  cudaError_t err = cluster_attributes(cluster, threads);
+  if (err != cudaSuccess) return err;
   cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = (unsigned)cluster;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cudaLaunchConfig_t cfg = cluster_config(cluster, nclusters, threads, smem, attr);
+  cfg.stream = s;
+  if (threads == 256) return cudaLaunchKernelEx(&cfg, tridiag_kernel<256>, a);
+  return cudaLaunchKernelEx(&cfg, tridiag_kernel<512>, a);
+}
+
+int tridiag_max_clusters(int cluster, int maxn, int threads) {
+  if (threads != 256 && threads != 512) return 0;
+  const size_t smem = tridiag_smem_bytes(maxn, cluster, threads);
+  if (smem > (size_t)max_dyn_smem()) return 0;
+  if (cluster_attributes(cluster, threads) != cudaSuccess) return 0;
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = cluster_config(cluster, 1, threads, smem, attr);
   int nc = 0;
-  if (cudaOccupancyMaxActiveClusters(&nc, tridiag_kernel, &cfg) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveClusters(&nc, cluster_kernel(threads), &cfg) != cudaSuccess) return 0;
   return nc;
 }
 

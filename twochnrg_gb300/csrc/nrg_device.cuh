@@ -130,9 +130,10 @@ struct TridiagArgs {
   int* flag;
   int maxn;
 };
-cudaError_t launch_tridiag(const TridiagArgs& a, int cluster, int nclusters, cudaStream_t s);
-size_t tridiag_smem_bytes(int maxn, int cluster);
-int tridiag_max_clusters(int cluster, int maxn);
+// threads: 512 (one CTA per SM) or 256 (two per SM, for concurrent contexts).
+cudaError_t launch_tridiag(const TridiagArgs& a, int cluster, int nclusters, cudaStream_t s, int threads = 512);
+size_t tridiag_smem_bytes(int maxn, int cluster, int threads = 512);
+int tridiag_max_clusters(int cluster, int maxn, int threads = 512);
 // Whole-GPU cooperative variant for the largest blocks (processed in turn).
 int tridiag_grid_size(int maxn);
 // work: tridiag_grid_work(maxn, grid) doubles of device memory.
