@@ -70,6 +70,29 @@ def test_large_block_whole_gpu_path(engine, monkeypatch):
     _check_block(A, ws[0], Zs[0], wr, Zr)
 
 
+@pytest.mark.parametrize("path", ["grid", "cluster256"])
+def test_lower_triangle_kernels_on_ragged_sizes(engine, monkeypatch, path):
+    """Both Householder kernels work on the lower triangle in tiles of 8 rows
+    by 32 columns: sizes around the tile edges (2 and 3: no full step; 8, 9,
+    31 to 34, 65) through the whole-grid kernel (threshold lowered to 2) and
+    through the cluster kernel's 256-thread form."""
+    rng = np.random.default_rng(21)
+    if path == "grid":
+        monkeypatch.setenv("NRG_BIG_N", "2")
+    else:
+        monkeypatch.setenv("NRG_CLUSTER_THREADS", path[len("cluster"):])
+        monkeypatch.setenv("NRG_CLUSTER", "4")
+    sizes = [2, 3, 8, 9, 31, 32, 33, 34, 65, 257]
+    mats = []
+    for n in sizes:
+        X = rng.standard_normal((n, n))
+        mats.append((X + X.T) / np.sqrt(n))
+    ws, Zs = engine.diag_blocks(sizes, np.concatenate([orc.pack_upper(A) for A in mats]))
+    for A, w, Z in zip(mats, ws, Zs):
+        wr, Zr = orc.diag_block(orc.pack_upper(A), A.shape[0])
+        _check_block(A, w, Z, wr, Zr)
+
+
 @pytest.mark.parametrize("split", ["1", "2", "3"])
 def test_concurrent_grids_path(engine, monkeypatch, split):
     """Several large blocks dealt to concurrent cooperative grids, next to

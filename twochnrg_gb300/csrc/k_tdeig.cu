@@ -201,13 +201,22 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
   for (int it = 0; it < 200 && !done; ++it) {
     if (hi - lo <= fmax(2.0 * kEps * fmax(fabs(lo), fabs(hi)), floor_w)) break;
     if (it >= 16) newton = false;  // a model step that has not converged by now: bisect
+    if (!newton) {
+      // plain bisection needs the count alone (about half the FP64 work of a
+      // pass with the derivative sums)
+      const int c = sturm_count(d, e2, n, x, pivmin);
+      if (c > k) hi = x; else lo = x;
+      x = 0.5 * (lo + hi);
+      v = x;
+      continue;
+    }
     double S1, S2;
     const int c = sturm_sums(d, e2, n, x, pivmin, &S1, &S2);
     if (c > k) hi = x; else lo = x;
     const bool above = c <= k;
     const double step = pair_step(S1, S2, above, above ? k - c : c - 1 - k);
     double xn = 0.5 * (lo + hi);
-    if (newton && isfinite(step)) {
+    if (isfinite(step)) {
       // round-off floor of the recurrence: a few ulps of the spectral radius
       const double small = 4.0 * kEps * fabs(x) + 16.0 * kEps * tnorm;
       if (fabs(step) <= small) {
