@@ -222,7 +222,11 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
       if (fabs(step) <= small) {
         // converged: accept only if the k-th level is within reach of x + step;
         // the count at x already settles the side x is on
-        const double xc = x + step, del = 2.0 * fabs(step) + small;
+        // A group of levels split only by round-off (the two-channel
+        // spectrum's channel partners and free-chain combinations) is accepted
+        // as resolved at 64 ulps of the spectral radius, about the accuracy
+        // LAPACK's solvers give such a group.
+        const double xc = x + step, del = fmax(2.0 * fabs(step) + small, 64.0 * kEps * tnorm);
         bool ok;
         if (unique && xc >= lo && xc <= hi) ok = true;
         else if (above && step >= 0.0) ok = sturm_count(d, e2, n, xc + del, pivmin) > k;
