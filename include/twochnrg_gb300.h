@@ -483,6 +483,18 @@ typedef struct {
 
 nrg_status nrg_sweep_run_model(nrg_ctx* ctx, const nrg_sweep_config* cfg, const nrg_model_desc* model);
 
+/* nrg_diag_hn and nrg_update_ops (below) for a described model: the per-call-
+ * site drop-ins of DiagHN and UpdateMatrices, where the reference calls
+ * CalcHNMatEl, CalcMatEl and CheckForMatEl.  params_hn as for nrg_diag_hn
+ * (one chi per channel of the description); ops / old_ops hold the
+ * description's operators in its order (the first hn_ops enter H_N). */
+nrg_status nrg_diag_hn_model(nrg_ctx* ctx, const nrg_model_desc* model, const double* params_hn, int nparams,
+                             const nrg_blocks* old_kept, int nops, const nrg_matrix* ops, const nrg_basis* abasis,
+                             double* en, double* eigvec, double* emin);
+nrg_status nrg_update_ops_model(nrg_ctx* ctx, const nrg_model_desc* model, const nrg_blocks* old_kept,
+                                const nrg_basis* abasis, const nrg_eigcut* acut, int nops, const nrg_matrix* old_ops,
+                                nrg_matrix* new_ops);
+
 /* The tables the device assembly and operator update read, built on the host
  * (no device needed) for a built-in model (desc NULL, model = nrg_model) or
  * a described one (desc non-NULL, model ignored):

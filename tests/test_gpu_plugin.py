@@ -107,3 +107,46 @@ def test_plugin_errors(engine):
     # the context stays usable
     r = engine.sweep_model(plug, 4, 50, 2.5, 0.02)
     assert len(r.iters) == 4
+
+
+# The per-call-site drop-ins (DiagHN and UpdateMatrices, where the reference
+# calls CalcHNMatEl / CalcMatEl / CheckForMatEl) with the plug-in models: the
+# results equal the built-in models' bit for bit on the oracle's captured
+# iteration inputs.
+STEP_CASES = [
+    ("1chQS", 6, 80, 2.5, 0.5, -0.25, 0.02, 0.0, 4),
+    ("1chQSz", 6, 70, 2.5, 0.4, -0.2, 0.015, 1e-3, 3),
+    ("2chQS", 4, 60, 2.5, 0.3, -0.15, 0.01, 0.01, 2),
+]
+
+
+def _plugin_for(model, U, ed, x, lam):
+    if model == "1chQS":
+        return pm.one_channel_qs(U, ed, lam)
+    if model == "1chQSz":
+        return pm.one_channel_qsz(U, ed, x, lam)
+    return pm.two_channel_qs(U, ed, lam)
+
+
+@pytest.mark.parametrize("case", STEP_CASES, ids=[f"{c[0]}-N{c[8]}" for c in STEP_CASES])
+def test_plugin_per_call_site(engine, case):
+    from oracle import oracle as orc
+    model, ns, nc, lam, U, ed, g1, x, n = case
+    it = orc.run(model, ns, nc, lam, U, ed, g1, x, capture_iter=n).iters[n]
+    cap = it.cap
+    plug = _plugin_for(model, U, ed, x, lam)
+    ops = [(cap[f"old_map.{o}"], cap[f"old_mbe.{o}"], cap[f"old_el.{o}"]) for o in range(cap["nmats"])]
+    basis = (cap["basis_qn"], cap["basis_bbe"], cap["basis_itype"], cap["basis_stcf"], cap["basis_en"])
+    a = engine.diag_hn(model, cap["params"], cap["old_qn"], cap["old_bbe"], ops, *basis)
+    b = engine.diag_hn(plug, cap["params"], cap["old_qn"], cap["old_bbe"], ops, *basis)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+    assert a[2] == b[2]
+    args = (cap["old_qn"], cap["old_bbe"], *basis, cap["cut_qn"], cap["cut_bbe"], cap["cut_bbe_eig"],
+            cap["cut_evec"], ops)
+    na, nb = engine.update_ops(model, *args), engine.update_ops(plug, *args)
+    assert len(na) == len(nb)
+    for (m1, e1, v1), (m2, e2, v2) in zip(na, nb):
+        np.testing.assert_array_equal(m1, m2)
+        np.testing.assert_array_equal(e1, e2)
+        np.testing.assert_array_equal(v1, v2)

@@ -475,6 +475,12 @@ def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     L.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
     L.nrg_diag_hn.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_int, ctypes.POINTER(_Blocks),
                               ctypes.c_int, ctypes.POINTER(_Matrix), ctypes.POINTER(_Basis), _dp, _dp, _dp]
+    L.nrg_diag_hn_model.argtypes = [ctypes.c_void_p, ctypes.POINTER(_ModelDesc), _dp, ctypes.c_int,
+                                    ctypes.POINTER(_Blocks), ctypes.c_int, ctypes.POINTER(_Matrix),
+                                    ctypes.POINTER(_Basis), _dp, _dp, _dp]
+    L.nrg_update_ops_model.argtypes = [ctypes.c_void_p, ctypes.POINTER(_ModelDesc), ctypes.POINTER(_Blocks),
+                                       ctypes.POINTER(_Basis), ctypes.POINTER(_EigCut), ctypes.c_int,
+                                       ctypes.POINTER(_Matrix), ctypes.POINTER(_Matrix)]
     L.nrg_cut_states.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Blocks), _dp, _dp, ctypes.c_int,
                                  ctypes.c_double, ctypes.POINTER(_CutResult)]
     L.nrg_update_ops.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(_Blocks), ctypes.POINTER(_Basis),
@@ -618,8 +624,9 @@ class Engine:
     # bbe [2*nblocks] inclusive BlockBegEnd, operators as (MatBlockMap,
     # MatBlockBegEnd, MatEl) triples in the model's operator order.
 
-    def diag_hn(self, model: str, params, old_qn, old_bbe, ops, basis_qn, basis_bbe, itype, stcf, basis_en):
-        """CNRGmatrix::DiagHN + SetE0zero.  Returns (en, eigvec, emin): en the
+    def diag_hn(self, model, params, old_qn, old_bbe, ops, basis_qn, basis_bbe, itype, stcf, basis_en):
+        """CNRGmatrix::DiagHN + SetE0zero for a built-in model (its name) or a
+        ModelPlugin (nrg_diag_hn_model).  Returns (en, eigvec, emin): en the
         E_min-shifted eigenvalues (ascending per block), eigvec the
         block-concatenated n x n matrices (row k = eigenvector k)."""
         k = _Keep()
@@ -632,9 +639,19 @@ class Engine:
         en = np.empty(int(sizes.sum()), dtype=np.float64)
         vec = np.empty(int((sizes ** 2).sum()), dtype=np.float64)
         emin = ctypes.c_double()
-        self._check(self.L.nrg_diag_hn(self.h, MODELS[model], params.ctypes.data_as(_DP), len(params),
-                                       ctypes.byref(old), len(ops), mats, ctypes.byref(basis),
-                                       en.ctypes.data_as(_DP), vec.ctypes.data_as(_DP), ctypes.byref(emin)))
+        if isinstance(model, ModelPlugin):
+            keep, errors = [], []
+            desc = model._desc(keep, errors)
+            st = self.L.nrg_diag_hn_model(self.h, ctypes.byref(desc), params.ctypes.data_as(_DP), len(params),
+                                          ctypes.byref(old), len(ops), mats, ctypes.byref(basis),
+                                          en.ctypes.data_as(_DP), vec.ctypes.data_as(_DP), ctypes.byref(emin))
+            if errors:
+                raise errors[0]
+            self._check(st)
+        else:
+            self._check(self.L.nrg_diag_hn(self.h, MODELS[model], params.ctypes.data_as(_DP), len(params),
+                                           ctypes.byref(old), len(ops), mats, ctypes.byref(basis),
+                                           en.ctypes.data_as(_DP), vec.ctypes.data_as(_DP), ctypes.byref(emin)))
         return en, vec, emin.value
 
     def cut_states(self, qn, bbe, en, eigvec, ncutoff: int, degen_eps: float = 0.0) -> dict:
@@ -663,9 +680,10 @@ class Engine:
             out["eigvec"] = _arr(c.eigvec, int(bbe_eig[-1] + 1) if nb else 0, np.float64)
         return out
 
-    def update_ops(self, model: str, old_qn, old_bbe, basis_qn, basis_bbe, itype, stcf, basis_en,
+    def update_ops(self, model, old_qn, old_bbe, basis_qn, basis_bbe, itype, stcf, basis_en,
                    cut_qn, cut_bbe, cut_bbe_eig, cut_eigvec, ops):
-        """UpdateMatrices for all of the model's operators.  Returns the new
+        """UpdateMatrices for all of the model's operators, a built-in model
+        (its name) or a ModelPlugin (nrg_update_ops_model).  Returns the new
         operators as (MatBlockMap, MatBlockBegEnd, MatEl) triples."""
         k = _Keep()
         old = k.blocks(old_qn, old_bbe)
@@ -673,8 +691,17 @@ class Engine:
         cut = _EigCut(k.blocks(cut_qn, cut_bbe), None, k.i(cut_bbe_eig), None, None, None, k.d(cut_eigvec))
         mats = (_Matrix * len(ops))(*[k.matrix(m) for m in ops])
         new = (_Matrix * len(ops))()
-        self._check(self.L.nrg_update_ops(self.h, MODELS[model], ctypes.byref(old), ctypes.byref(basis),
-                                          ctypes.byref(cut), len(ops), mats, new))
+        if isinstance(model, ModelPlugin):
+            keep, errors = [], []
+            desc = model._desc(keep, errors)
+            st = self.L.nrg_update_ops_model(self.h, ctypes.byref(desc), ctypes.byref(old), ctypes.byref(basis),
+                                             ctypes.byref(cut), len(ops), mats, new)
+            if errors:
+                raise errors[0]
+            self._check(st)
+        else:
+            self._check(self.L.nrg_update_ops(self.h, MODELS[model], ctypes.byref(old), ctypes.byref(basis),
+                                              ctypes.byref(cut), len(ops), mats, new))
         res = []
         for m in new:
             nmb = m.nmatblocks

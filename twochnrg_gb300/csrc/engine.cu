@@ -2343,7 +2343,15 @@ BlockArray blocks_from_abi(const nrg_blocks* b, const char* what) {
   return a;
 }
 
-ModelSpec model_from_abi(int model) {
+// A built-in model of the per-call-site drop-ins, or a caller's description.
+ModelSpec model_from_abi(int model, const nrg_model_desc* desc = nullptr) {
+  if (desc) {
+    try {
+      return make_plugin_model(*desc);
+    } catch (const std::invalid_argument& e) {
+      throw NrgError(NRG_ERR_ARG, e.what());
+    }
+  }
   if (model < 0 || model > 2) throw NrgError(NRG_ERR_ARG, "unknown model");
   return make_model((ModelKind)model);
 }
@@ -2391,8 +2399,9 @@ OpMeta op_from_abi(const nrg_matrix& M, const BlockArray& blk, int64_t* nel) {
 
 // DiagHN + SetE0zero for a caller-given basis (all eigenvectors).
 void diag_hn_impl(nrg_ctx* c, int model, const double* params, int nparams, const nrg_blocks* old_kept, int nops,
-                  const nrg_matrix* ops, const nrg_basis* abasis, double* en_out, double* evec_out, double* emin_out) {
-  const ModelSpec m = model_from_abi(model);
+                  const nrg_matrix* ops, const nrg_basis* abasis, double* en_out, double* evec_out, double* emin_out,
+                  const nrg_model_desc* desc = nullptr) {
+  const ModelSpec m = model_from_abi(model, desc);
   if (!params || nparams < m.nchan + 2) throw NrgError(NRG_ERR_ARG, "ParamsHN needs Lambda, chi per channel and e_N");
   if (nparams > m.nchan + 2 && params[m.nchan + 2] != 0.0)
     throw NrgError(NRG_ERR_ARG, "superconducting leads (Delta_SC != 0) are not supported");
@@ -2544,8 +2553,8 @@ void cut_states_impl(nrg_ctx* c, const nrg_blocks* aeig, const double* en, const
 // UpdateMatrices for a caller-given AeigCut (kept rows of the eigenvectors
 // uploaded as Z and Z^T) and old operators.
 void update_ops_impl(nrg_ctx* c, int model, const nrg_blocks* old_kept, const nrg_basis* abasis, const nrg_eigcut* acut,
-                     int nops, const nrg_matrix* old_ops, nrg_matrix* new_ops) {
-  const ModelSpec m = model_from_abi(model);
+                     int nops, const nrg_matrix* old_ops, nrg_matrix* new_ops, const nrg_model_desc* desc = nullptr) {
+  const ModelSpec m = model_from_abi(model, desc);
   if (nops != (int)m.op_kind.size() || !old_ops || !new_ops)
     throw NrgError(NRG_ERR_ARG, "nops must equal the model's operator count");
   if (!acut) throw NrgError(NRG_ERR_ARG, "acut is NULL");
@@ -2991,6 +3000,30 @@ nrg_status nrg_update_ops(nrg_ctx* ctx, int model, const nrg_blocks* old_kept, c
   GUARD(ctx, {
     CU(cudaSetDevice(ctx->device));
     update_ops_impl(ctx, model, old_kept, abasis, acut, nops, old_ops, new_ops);
+  });
+  return NRG_OK;
+}
+
+nrg_status nrg_diag_hn_model(nrg_ctx* ctx, const nrg_model_desc* model, const double* params_hn, int nparams,
+                             const nrg_blocks* old_kept, int nops, const nrg_matrix* ops, const nrg_basis* abasis,
+                             double* en, double* eigvec, double* emin) {
+  if (!ctx || !model) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    diag_hn_impl(ctx, -1, params_hn, nparams, old_kept, nops, ops, abasis, en, eigvec, emin, model);
+  });
+  return NRG_OK;
+}
+
+nrg_status nrg_update_ops_model(nrg_ctx* ctx, const nrg_model_desc* model, const nrg_blocks* old_kept,
+                                const nrg_basis* abasis, const nrg_eigcut* acut, int nops, const nrg_matrix* old_ops,
+                                nrg_matrix* new_ops) {
+  if (!ctx || !model) return NRG_ERR_ARG;
+  ctx->err.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    update_ops_impl(ctx, -1, old_kept, abasis, acut, nops, old_ops, new_ops, model);
   });
   return NRG_OK;
 }
