@@ -547,6 +547,7 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
   ea.e2 = c->e2.as<double>();
   c->spl.ensure(std::max(P.nstates, 1));
   ea.split = c->spl.as<unsigned char>();
+  ea.mixed_n = mixed ? std::max(thr, mixed_block_threshold()) : 0;
   cudaEvent_t t1 = tm.start();
   launch_bisect(ea, d_state_block, c->stream);
   c->launches += 3;  // FP32 copies, levels, ordering

@@ -225,8 +225,11 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
         // A group of levels split only by round-off (the two-channel
         // spectrum's channel partners and free-chain combinations) is accepted
         // as resolved at 64 ulps of the spectral radius, about the accuracy
-        // LAPACK's solvers give such a group.
-        const double xc = x + step, del = fmax(2.0 * fabs(step) + small, 64.0 * kEps * tnorm);
+        // LAPACK's solvers give such a group; for a block reduced in mixed
+        // precision, whose reduction leaves the levels about 2^-36 of the
+        // block's scale apart from H's, at 2^-40 of the spectral radius.
+        const double gtol = (A.mixed_n > 0 && nb >= A.mixed_n) ? 0x1p-40 : 64.0 * kEps;
+        const double xc = x + step, del = fmax(2.0 * fabs(step) + small, gtol * tnorm);
         bool ok;
         if (unique && xc >= lo && xc <= hi) ok = true;
         else if (above && step >= 0.0) ok = sturm_count(d, e2, n, xc + del, pivmin) > k;

@@ -154,6 +154,8 @@ struct TdEigArgs {
   float* fde;            // scratch [2*nstates]: FP32 copies of d and e for the FP32 bracket
   double* e2;            // scratch [nstates]: e^2
   unsigned char* split;  // scratch [nstates]: e_i negligible (the pieces' ends)
+  int mixed_n;           // blocks of at least this many states were reduced in mixed
+                         // precision (their levels carry its ~2^-36 error); <= 0: none
 };
 void launch_bisect(const TdEigArgs& a, const int* state_block, cudaStream_t s);
 
