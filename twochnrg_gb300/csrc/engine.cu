@@ -397,6 +397,52 @@ void blocked_reduction(nrg_ctx* c, const EigPlan& P, const std::vector<int>& blo
   }
 }
 
+// Deals blocks (largest cost first) to K bins: longest-processing-time
+// greedy, then single moves and pairwise swaps out of the most loaded bin
+// while they lower its load (a few passes; the bins' order within is kept
+// largest first).
+std::vector<std::vector<int>> deal_by_cost(const std::vector<int>& blocks, const std::vector<double>& cost, int K) {
+  std::vector<std::vector<int>> bins(K);
+  std::vector<double> load(K, 0.0);
+  std::vector<int> idx(blocks.size());
+  for (size_t i = 0; i < idx.size(); ++i) idx[i] = (int)i;
+  std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+  std::vector<int> where(blocks.size());
+  for (int i : idx) {
+    const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    where[i] = k;
+    load[k] += cost[i];
+  }
+  for (int pass = 0; pass < 8; ++pass) {
+    const int hk = (int)(std::max_element(load.begin(), load.end()) - load.begin());
+    double best = load[hk];
+    int bi = -1, bj = -1, bk = -1;  // move i to bk, or swap i and j
+    for (size_t i = 0; i < blocks.size(); ++i) {
+      if (where[i] != hk) continue;
+      for (int k = 0; k < K; ++k) {
+        if (k == hk) continue;
+        const double m = std::max(load[hk] - cost[i], load[k] + cost[i]);
+        if (m < best - 1e-9 * best) { best = m; bi = (int)i; bj = -1; bk = k; }
+        for (size_t j = 0; j < blocks.size(); ++j) {
+          if (where[j] != k || cost[j] >= cost[i]) continue;
+          const double d = cost[i] - cost[j];
+          const double sw = std::max(load[hk] - d, load[k] + d);
+          if (sw < best - 1e-9 * best) { best = sw; bi = (int)i; bj = (int)j; bk = k; }
+        }
+      }
+    }
+    if (bi < 0) break;
+    if (bj < 0) {
+      load[hk] -= cost[bi]; load[bk] += cost[bi]; where[bi] = bk;
+    } else {
+      const double d = cost[bi] - cost[bj];
+      load[hk] -= d; load[bk] += d; where[bi] = bk; where[bj] = hk;
+    }
+  }
+  for (int i : idx) bins[where[i]].push_back(blocks[i]);
+  return bins;
+}
+
 // `order`: all blocks, largest first (host copy `order_h`); the big blocks
 // form its prefix.
 void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::vector<int>& order_h,
@@ -418,14 +464,13 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
   if (K > 1) {  // deal the large blocks by cost and upload the lists before the fork
     // the lower-triangle grid kernel: 2/3 n^3 FMA plus ~21 us of barriers and
     // vector work per column (2.8e6 FMA of a quarter of the GPU)
-    std::vector<double> load(K, 0.0);
+    std::vector<int> big(order_h.begin(), order_h.begin() + nbig);
+    std::vector<double> cst(nbig);
     for (int q = 0; q < nbig; ++q) {
-      const int b = order_h[q];
-      const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-      bins[k].push_back(b);
-      const double n = (double)P.bsize[b];
-      load[k] += 2.0 * n * n * n / 3.0 + 2.8e6 * n;
+      const double n = (double)P.bsize[big[q]];
+      cst[q] = 2.0 * n * n * n / 3.0 + 2.8e6 * n;
     }
+    bins = deal_by_cost(big, cst, K);
     Packer pk;
     for (int k = 0; k < K; ++k) o_bins[k] = pk.add(bins[k]);
     c->gbig.ensure(pk.host.size() + 256);
@@ -458,14 +503,9 @@ void run_tridiag_and_bisect(nrg_ctx* c, Timer& tm, const EigPlan& P, const std::
     };
     {
       std::vector<int> big(order_h.begin(), order_h.begin() + nbig);
-      std::stable_sort(big.begin(), big.end(), [&](int x, int y) { return cost(P.bsize[x]) > cost(P.bsize[y]); });
-      std::vector<double> load(K, 0.0);
-      for (auto& bk : bins) bk.clear();
-      for (int b : big) {
-        const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        bins[k].push_back(b);
-        load[k] += cost(P.bsize[b]);
-      }
+      std::vector<double> cst(nbig);
+      for (int q = 0; q < nbig; ++q) cst[q] = cost(P.bsize[big[q]]);
+      bins = deal_by_cost(big, cst, K);
     }
     if (!c->fork) CU(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
     CU(cudaEventRecord(c->fork, c->stream));
