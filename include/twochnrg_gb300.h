@@ -70,11 +70,11 @@ typedef enum {
 /* Arithmetic of the dense steps. */
 typedef enum {
   NRG_PREC_FP64 = 0,     /* plain FP64 everywhere */
-  NRG_PREC_MIXED = 1     /* the large blocks' Householder reduction blocked by panels of 32
-                            columns, its trailing rank-64 updates as split-BF16 products on the
-                            tensor cores (6 slices, FP32 accumulation, FP64 recombination;
-                            error of order 2^-36 of the operands' magnitudes); everything
-                            else FP64 */
+  NRG_PREC_MIXED = 1     /* the largest blocks' Householder reduction (from 4200 states on;
+                            NRG_MIXED_N overrides) blocked by panels of 32 columns, its
+                            trailing rank-64 updates as split-BF16 products on the tensor
+                            cores (6 slices, FP32 accumulation, FP64 recombination; error of
+                            order 2^-36 of the operands' magnitudes); everything else FP64 */
 } nrg_precision;
 
 typedef struct nrg_ctx nrg_ctx;
