@@ -159,6 +159,7 @@ struct nrg_ctx {
   double dm_lambda = 0.0;
   int dm_model = 0;  // ModelKind of the shells
   bool shared_gpu = false;  // a batch worker: other contexts run beside this one
+  cudaEvent_t bsync = nullptr;  // blocking-sync event of stream_wait
   std::vector<std::unique_ptr<nrg::DmShell>> dm;
   bool dm_rho_valid = false;
   double dm_temp = 0.0;                // temperature the density matrices were built for
@@ -239,6 +240,20 @@ void d2h(nrg_ctx* c, void* dst, const void* src, size_t bytes) {
   if (!bytes) return;
   CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
   c->timing.d2h_bytes += (int64_t)bytes;
+}
+
+// Waits for the context's stream.  A batch worker (shared_gpu) sleeps in the
+// wait (an event with cudaEventBlockingSync) instead of spinning, so that
+// many workers do not take the host cores from each other's table
+// building; a context alone on the GPU spins, for the shortest wake-up.
+void stream_wait(nrg_ctx* c) {
+  if (!c->shared_gpu) {
+    CU(cudaStreamSynchronize(c->stream));
+    return;
+  }
+  if (!c->bsync) CU(cudaEventCreateWithFlags(&c->bsync, cudaEventBlockingSync | cudaEventDisableTiming));
+  CU(cudaEventRecord(c->bsync, c->stream));
+  CU(cudaEventSynchronize(c->bsync));
 }
 
 void check_flag(nrg_ctx* c) {
@@ -1214,7 +1229,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
   const bool sc = m.kind == MODEL_1CHS || m.kind == MODEL_1CHSZ;
   cudaEvent_t it0, it1;
   CU(cudaEventCreate(&it0));
-  CU(cudaEventCreate(&it1));
+  CU(cudaEventCreateWithFlags(&it1, c->shared_gpu ? cudaEventBlockingSync : cudaEventDefault));
   EvGuard itg{it0, it1};
   for (int N = N0; N < cfg->nsites; ++N) {
     const auto t_iter = clock::now();
@@ -1275,7 +1290,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
     d2h(c, keptb.data(), bs.kept, sizeof(int) * nb);
     d2h(c, R.en.data(), c->en.p, sizeof(double) * P.nstates);
     tm.stop(tc, &c->timing.cut_ms);
-    CU(cudaStreamSynchronize(c->stream));
+    stream_wait(c);
     check_flag(c);
     R.emin = scal[0]; R.ecut = scal[1]; R.nkept = (int)scal[2];
     R.qn = B.blk.qn; R.bsize = P.bsize;
@@ -1360,7 +1375,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
     std::vector<double> avg(8);
     d2h(c, avg.data(), c->scal.as<double>() + 24, sizeof(double) * 8);
     tm.stop(to, &c->timing.cut_ms);
-    CU(cudaStreamSynchronize(c->stream));
+    stream_wait(c);
     check_flag(c);
     tm.collect();
     const double Zk = avg[avg_ops.size()];
@@ -2793,6 +2808,7 @@ void nrg_destroy(nrg_ctx* ctx) {
     if (ctx->join[k]) cudaEventDestroy(ctx->join[k]);
   }
   if (ctx->fork) cudaEventDestroy(ctx->fork);
+  if (ctx->bsync) cudaEventDestroy(ctx->bsync);
   cudaStreamDestroy(ctx->stream);
   delete ctx->tan;
   ctx->tan = nullptr;
