@@ -169,7 +169,9 @@ nrg_status nrg_sweep_timing(const nrg_ctx* ctx, nrg_timing* out);
  *   thermo[(i*max_sites + n)*16 .. +16]  as nrg_iteration.thermo,
  *   opavg [(i*max_sites + n)*4  .. +4]   CalcOpAvg values (unused slots 0),
  *   nkept [i*max_sites + n]              states with E <= Ecut.
- * *seconds receives the wall time of the whole batch. */
+ * *seconds receives the wall time of the whole batch.  Eight workers
+ * measured best on a GB300 with 16 host cores; the workers' small blocks use
+ * the cluster Householder kernel's two-CTAs-per-SM form. */
 nrg_status nrg_sweep_batch(int device, int ninst, const nrg_sweep_config* cfgs, int nworkers, int max_sites,
                            double* thermo, double* opavg, int* nkept, double* seconds);
 
