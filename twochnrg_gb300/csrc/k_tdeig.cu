@@ -231,7 +231,11 @@ __global__ void bisect_kernel(TdEigArgs A, const int* state_block) {
         const double gtol = (A.mixed_n > 0 && nb >= A.mixed_n) ? 0x1p-40 : 64.0 * kEps;
         const double xc = x + step, del = fmax(2.0 * fabs(step) + small, gtol * tnorm);
         bool ok;
-        if (unique && xc >= lo && xc <= hi) ok = true;
+        // The bracket holding the k-th level alone settles it, provided x is
+        // near a root (|f'/f| large): a small step also comes out at a
+        // stationary point of f between two levels (S1 = 0), which the
+        // bracket can hold too; there the Sturm counts decide.
+        if (unique && xc >= lo && xc <= hi && fabs(S1) * small >= 1.0) ok = true;
         else if (above && step >= 0.0) ok = sturm_count(d, e2, n, xc + del, pivmin) > k;
         else if (!above && step <= 0.0) ok = sturm_count(d, e2, n, xc - del, pivmin) <= k;
         else ok = sturm_count(d, e2, n, xc - del, pivmin) <= k && sturm_count(d, e2, n, xc + del, pivmin) > k;
