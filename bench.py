@@ -159,7 +159,8 @@ def cpu_sample(nthreads: int):
 def sweep_estimate(per_iter_s, nsites: int) -> float:
     """Sweep total from measured iterations: the measured ones plus, for each
     later iteration, the last (full-size) one's time.  Later iterations have
-    the same kept count and 0.97-1.20 times its sum of n_b^3."""
+    the same kept count and 0.94-1.26 times its sum of n_b^3 (the GPU's own
+    full-size iterations take 0.94-1.25 times iteration 3's time)."""
     return float(sum(per_iter_s) + (nsites - len(per_iter_s)) * per_iter_s[-1])
 
 
