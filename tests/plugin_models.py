@@ -277,3 +277,40 @@ def two_channel_qs(U, ed, lam):
         start_en=[0.5 * U / scale, (ed + 0.5 * U) / scale, (2.0 * ed + 1.5 * U) / scale],
         start_ops=[fop, fop, _start_ops_diag(3, n), _start_ops_diag(3, [x * x for x in n]),
                    _start_ops_diag(3, [S * (S + 1.0) for _, S in blocks])])
+
+
+def one_channel_q(U, ed, lam):
+    """One-channel Anderson model in the charge-only |Q> basis (SymNo 3): blocks
+    carry (Q, 0); the site's Q = 0 block holds |up> and |dn>."""
+    site = [(-1.0, 0.0), (0.0, 0.0), (1.0, 0.0)]  # CNRGCodeHandler::SetSingleSite, SymNo 3
+    sizes = [1, 2, 1]
+    qtype = [-1.0, 0.0, 0.0, 1.0]  # Q of the types |0>, |up>, |dn>, |up dn>
+
+    def hn_coef(S, ti, tj, ch, sg, dr):
+        # OneChQ_HN_MatEl (OpMatRules.cpp:1065-1147), OneChQSz_HN_MatEl's arithmetic
+        sigma = 1 if sg == 0 else -1
+        sign = lambda t: -1.0 if _deq(qtype[t], 0.0) else 1.0  # noqa: E731
+        return sign(tj) * _fd(sigma, ti, tj) if dr == 0 else sign(ti) * _fd(sigma, tj, ti)
+
+    def op_factor(o, Si, Sj, ti, tj):  # OneChQ_fN_MatEl (OpMatRules.cpp:1003-1033)
+        return _fd(1 if o == 0 else -1, tj, ti)
+
+    def op_check(o, qi, qj):
+        if o < 2:  # OneChQ_cd_check (OpMatRules.cpp:92)
+            return _deq(qj[0], qi[0] + 1.0)
+        return qi == qj
+
+    # OneChQ_SetAnderson_Hm1 (Main/Main_SetH0.cpp:217-352): the Q = 0 block two-fold
+    scale = lam * 0.5 * (1.0 + 1.0 / lam)
+    blocks = [(-1.0, 0.0), (0.0, 0.0), (1.0, 0.0)]
+    return tg.ModelPlugin(
+        total_spin=False, site_qn=site, site_bsize=sizes, hn_form=tg.HN_SPIN_SUM, onsite=True,
+        hn_coef=hn_coef, op_class=[tg.OP_SITE, tg.OP_SITE, tg.OP_IMPURITY_DIAG, tg.OP_IMPURITY_DIAG],
+        op_avg=[0, 0, 1, 1], op_factor=op_factor, op_check=op_check,
+        start_qn=blocks, start_bsize=[1, 2, 1],
+        start_en=[0.5 * U / scale, (ed + 0.5 * U) / scale, (ed + 0.5 * U) / scale, (2.0 * ed + 1.5 * U) / scale],
+        start_ops=[[(0, 1, np.array([[1.0, 0.0]])), (1, 2, np.array([[0.0], [1.0]]))],
+                   [(0, 1, np.array([[0.0, 1.0]])), (1, 2, np.array([[-1.0], [0.0]]))],
+                   [(0, 0, np.array([[0.0]])), (1, 1, np.array([[0.5, 0.0], [0.0, -0.5]])), (2, 2, np.array([[0.0]]))],
+                   [(0, 0, np.array([[0.0]])), (1, 1, np.array([[0.25, 0.0], [0.0, 0.25]])),
+                    (2, 2, np.array([[0.0]]))]])

@@ -77,6 +77,17 @@ def test_plugin_two_channel_matches_reference_fixture(engine):
     _same(r, b)
 
 
+def test_plugin_q_matches_reference_fixture(engine):
+    cfg, ref = _fixture("q_1chQ_n12_k200")
+    model, ns, nc, lam, U, ed, g1, _ = cfg[:8]
+    assert str(model) == "1chQ"
+    plug = pm.one_channel_q(float(U), float(ed), float(lam))
+    r = engine.sweep_model(plug, int(ns), int(nc), float(lam), float(g1))
+    compare(r, ref, "1chQ")
+    b = engine.sweep("1chQ", int(ns), int(nc), float(lam), float(U), float(ed), float(g1))
+    _same(r, b)
+
+
 def test_plugin_mixed_precision(engine, monkeypatch):
     """The plug-in model through the mixed form (large-block thresholds
     lowered so the blocked reduction runs) against the FP64 built-in."""

@@ -10,7 +10,8 @@ import twochnrg_gb300 as tg
 
 CASES = [("1chQS", lambda: pm.one_channel_qs(0.5, -0.25, 2.5), 4, 4),
          ("1chQSz", lambda: pm.one_channel_qsz(0.5, -0.25, 1e-3, 2.5), 4, 4),
-         ("2chQS", lambda: pm.two_channel_qs(0.3, -0.15, 2.5), 16, 5)]
+         ("2chQS", lambda: pm.two_channel_qs(0.3, -0.15, 2.5), 16, 5),
+         ("1chQ", lambda: pm.one_channel_q(0.4, -0.2, 2.5), 4, 4)]
 QN = [(-1.0, 0.0), (0.0, 0.5), (1.0, 0.0), (0.0, -0.5), (2.0, 0.5), (1.0, 1.0), (-2.0, 1.5)]
 
 
@@ -19,7 +20,7 @@ def test_tables_equal_builtin(name, make, ntypes, nops):
     a, b = tg.ModelTables(name), tg.ModelTables(make())
     for S in np.arange(0.0, 8.5, 0.5):
         ta, tb = a.hn_table(S), b.hn_table(S)
-        per_pair = {"1chQS": 2, "1chQSz": 4, "2chQS": 8}[name]  # 2 nchan nsigma
+        per_pair = {"1chQS": 2, "1chQSz": 4, "2chQS": 8, "1chQ": 4}[name]  # 2 nchan nsigma
         assert ta.shape == tb.shape and ta.size == ntypes * ntypes * per_pair
         np.testing.assert_array_equal(ta, tb)
     for o in range(nops):
