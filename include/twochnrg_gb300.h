@@ -400,6 +400,30 @@ nrg_status nrg_dm_backprop(nrg_ctx* ctx, const nrg_dm_params* prm, double* rho_t
 nrg_status nrg_lehmann(nrg_ctx* ctx, const nrg_dm_params* prm, int nomega, const double* omegas, double* omega_rhow,
                        int* nout);
 
+/* ---- derivatives of A(omega) ---------------------------------------------
+ * The reference has no derivative code (see nrg_grad_forward).
+ * nrg_grad_forward_dm runs the sweep of nrg_sweep_run_dm (NRG_MODEL_1CH_QS,
+ * FP64) with the tangent pass of nrg_grad_forward (out as there).  Each
+ * shell keeps, per parameter p = (eps_d, U, Gamma1, B), the tangents of its
+ * energies, of every eigenvector (all states, as the DM-NRG rotations and
+ * c_d use them all; no coupling inside a degenerate level) and of c_d.
+ * nrg_dm_backprop on those shells also carries the four tangents of the
+ * density matrices: d rho~ = Z^T (d rho Z + rho dZ) + dZ^T rho Z, the same
+ * partial trace, and the Boltzmann weights differentiated with d ln ZTot.
+ * nrg_lehmann_grad then returns what nrg_lehmann returns and d_rhow[k *
+ * nomega + j] = d A(omega_j) / d p_k (k < 4; d_rhow holds 4 * nomega), from
+ * d(rho A) = d rho A + rho dA, d(A rho) = dA rho + A d rho, the records'
+ * weight and energy tangents and the broadening kernels differentiated.
+ * These are the derivatives at the forward sweep's kept-state set and at the
+ * undisplaced parameters' choice between the log-Gaussian and the Gaussian
+ * kernel for every pair.  B does not enter the |Q S> model: its row is 0.
+ * nrg_lehmann_grad_backward: grad[k] = sum_j g_rhow[j] d A(omega_j) / d p_k
+ * over the *nout frequencies of the last nrg_lehmann_grad. */
+nrg_status nrg_grad_forward_dm(nrg_ctx* ctx, const nrg_sweep_config* cfg, nrg_grad* out);
+nrg_status nrg_lehmann_grad(nrg_ctx* ctx, const nrg_dm_params* prm, int nomega, const double* omegas,
+                            double* omega_rhow, double* d_rhow, int* nout);
+nrg_status nrg_lehmann_grad_backward(nrg_ctx* ctx, const double* g_rhow, double* grad);
+
 /* ---- model plug-in -----------------------------------------------------
  * A model supplied by the caller, without rebuilding the engine: the
  * reference's per-model function pointers of CNRGmatrix (CalcHNMatEl,

@@ -490,6 +490,9 @@ def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
     L.nrg_dm_num_shells.argtypes = [ctypes.c_void_p]
     L.nrg_dm_backprop.argtypes = [ctypes.c_void_p, ctypes.POINTER(DmParams), _dp]
     L.nrg_lehmann.argtypes = [ctypes.c_void_p, ctypes.POINTER(DmParams), ctypes.c_int, _dp, _dp, _ip]
+    L.nrg_grad_forward_dm.argtypes = [ctypes.c_void_p, ctypes.POINTER(SweepConfig), ctypes.POINTER(_Grad)]
+    L.nrg_lehmann_grad.argtypes = [ctypes.c_void_p, ctypes.POINTER(DmParams), ctypes.c_int, _dp, _dp, _dp, _ip]
+    L.nrg_lehmann_grad_backward.argtypes = [ctypes.c_void_p, _dp, _dp]
     L.nrg_write_dm_shell.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(DmShell)]
     L.nrg_write_code_pars.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_int, ctypes.c_char_p]
     L.nrg_dm_save_bin.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]
@@ -758,6 +761,52 @@ class Engine:
                                        ctypes.byref(nout)))
         n = nout.value
         return out[:n].copy(), out[cap:cap + n].copy()
+
+    def grad_forward_dm(self, nsites: int, ncutoff: int, lam: float, U: float, ed: float, gamma: float,
+                        degen_eps: float = 0.0) -> GradResult:
+        """nrg_grad_forward_dm: sweep_dm of the one-channel |Q S> model with the
+        tangent pass; afterwards dm_backprop also builds the density matrices'
+        tangents and lehmann_grad gives d A(omega) / d (eps_d, U, Gamma, B)."""
+        cfg = SweepConfig(MODELS["1chQS"], nsites, ncutoff, lam, U, ed, gamma, 0.0, degen_eps, PREC_FP64, 0.0)
+        g = _Grad()
+        self._check(self.L.nrg_grad_forward_dm(self.h, ctypes.byref(cfg), ctypes.byref(g)))
+        self._dm_site_dim = 4.0
+        n, k, no = g.nsites, g.nparams, g.nops
+        return GradResult(self._fetch(True), _arr(g.d_thermo, n * k * 16, np.float64).reshape(n, k, 4, 4),
+                          _arr(g.d_opavg, n * k * no, np.float64).reshape(n, k, no),
+                          _arr(g.d_emin, n * k, np.float64).reshape(n, k), _arr(g.egs, n, np.float64),
+                          _arr(g.d_egs, n * k, np.float64).reshape(n, k))
+
+    def lehmann_grad(self, prm: DmParams, omegas=None, capacity: int = 0):
+        """nrg_lehmann_grad after grad_forward_dm and dm_backprop: returns
+        (omega, A, dA) with dA[k, j] = d A(omega_j) / d p_k, p = (eps_d, U,
+        Gamma, B)."""
+        n_sh = int(self.L.nrg_dm_num_shells(self.h))
+        if omegas is None:
+            cap = capacity or 2 * prm.nw * n_sh + 8
+            om_ptr = None
+        else:
+            om = np.ascontiguousarray(omegas, dtype=np.float64)
+            cap = len(om)
+            om_ptr = om.ctypes.data_as(_DP)
+        out = np.zeros(2 * max(cap, 1))
+        dout = np.zeros(4 * max(cap, 1))
+        nout = ctypes.c_int(0)
+        self._check(self.L.nrg_lehmann_grad(self.h, ctypes.byref(prm), cap, om_ptr, out.ctypes.data_as(_DP),
+                                            dout.ctypes.data_as(_DP), ctypes.byref(nout)))
+        n = nout.value
+        self._lehmann_grad_n = n
+        return out[:n].copy(), out[cap:cap + n].copy(), dout.reshape(4, max(cap, 1))[:, :n].copy()
+
+    def lehmann_grad_backward(self, g_rhow) -> np.ndarray:
+        """nrg_lehmann_grad_backward: sum_j g_rhow[j] d A(omega_j) / d p over the
+        frequencies of the last lehmann_grad."""
+        g = np.ascontiguousarray(g_rhow, dtype=np.float64)
+        if g.shape != (getattr(self, "_lehmann_grad_n", -1),):
+            raise ValueError("g_rhow must hold one weight per frequency of the last lehmann_grad")
+        out = np.zeros(4)
+        self._check(self.L.nrg_lehmann_grad_backward(self.h, g.ctypes.data_as(_DP), out.ctypes.data_as(_DP)))
+        return out
 
     def dm_save_bin(self, directory: str, name: str) -> None:
         """The DM-NRG shells as the reference's .bin files plus ThisCodePars.dat."""

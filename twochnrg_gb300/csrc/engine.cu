@@ -89,6 +89,8 @@ struct OpMeta {
   }
 };
 
+struct DmTan { static constexpr int NP = 4; };  // parameter directions of the DM-NRG tangents
+
 // One Wilson shell as the DM-NRG backward sweep needs it (what NRG_main
 // saves with UpdateBefCut = 1: Abasis_N, the uncut eigen-array Acut_N and
 // c_d in it), kept on the device between the forward and backward sweeps.
@@ -107,6 +109,12 @@ struct DmShell {
   std::vector<int> rrows;              // per block: rho is zero beyond its leading rrows x rrows part
   DevBuf lpart;                        // Lehmann partial sums of this shell's record lists
   int64_t nrec[4] = {0, 0, 0, 0};
+  // Tangents along the four parameters (eps_d, U, Gamma, B) of
+  // nrg_grad_forward_dm; ntan = 0 without them.
+  int ntan = 0;
+  std::vector<double> den;             // [p * nstates + i]: d en
+  DevBuf dZ[4], dcd[4], drho[4];       // d Z (rows, the layout of Z), d c_d, d rho (the layout of rho)
+  DevBuf ltpart;                       // tangent Lehmann partial sums, [p][the layout of lpart]
 };
 
 struct IterResult {
@@ -139,6 +147,7 @@ struct nrg_ctx {
   nrg::DevBuf meta, vmeta, H, d, e, tau, ev, en, flag, scal, Y, scratch, Z, Zt, T, partial, red, gpart, fde, e2, spl;
   nrg::DevBuf ops_a[6], ops_b[6], opptr;
   nrg::DevBuf dmcnt, dmrec, dmtab;     // Lehmann record counts / offsets, records, frequency tables
+  nrg::DevBuf dmtmeta;                 // work items of the tangent Lehmann sums
   nrg::DevBuf ozw;                     // split-BF16 slices and row scales of the tensor-core products
   cudaEvent_t ev_a[8];
   // concurrent whole-GPU tridiagonalizations: side streams, fork/join events,
@@ -162,6 +171,9 @@ struct nrg_ctx {
   cudaEvent_t bsync = nullptr;  // blocking-sync event of stream_wait
   std::vector<std::unique_ptr<nrg::DmShell>> dm;
   bool dm_rho_valid = false;
+  bool dm_drho_valid = false;          // the density matrices' tangents are built too
+  nrg::DevBuf dmtan;                   // scratch of the tangent rotations and rho.A products
+  std::vector<double> dm_drhow;        // [p][omega]: d A / d p of the last nrg_lehmann_grad
   double dm_temp = 0.0;                // temperature the density matrices were built for
   std::vector<double> dm_hm1_en;       // H_{-1} energies (what shell 0's basis came from)
   // thermodynamics with the free-chain subtraction (nrg_thermo_run): the
@@ -1102,6 +1114,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
   if (dm) {
     c->dm.clear();
     c->dm_rho_valid = false;
+    c->dm_drho_valid = false;
     c->dm_lambda = cfg->lambda;
     c->dm_model = S.m.kind;
   }
@@ -1174,8 +1187,10 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
   // Gamma enters through chi_{-1} at iteration 0.
   const bool fullvec = dm || tan;
   if (tan) {
-    if (chain || dm || (m.kind != MODEL_1CHQS && m.kind != MODEL_1CHQSZ))
-      throw NrgError(NRG_ERR_ARG, "derivatives are built for the one-channel |Q S> and |Q Sz> Anderson sweeps");
+    if (chain || (m.kind != MODEL_1CHQS && m.kind != MODEL_1CHQSZ) || (dm && m.kind != MODEL_1CHQS))
+      throw NrgError(NRG_ERR_ARG,
+                     "derivatives are built for the one-channel |Q S> and |Q Sz> Anderson sweeps "
+                     "(with DM-NRG shells: |Q S>)");
     const StartState s0 = make_start(m, lambda, 0.0, 0.0, 0.0);
     const StartState sd[3] = {make_start(m, lambda, 0.0, 1.0, 0.0), make_start(m, lambda, 1.0, 0.0, 0.0),
                               make_start(m, lambda, 0.0, 0.0, 1.0)};
@@ -1385,6 +1400,8 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
       R.opavg.push_back(s);
     }
     // ---------------- tangents of this iteration (nrg_grad_forward)
+    std::unique_ptr<DmShell> shp;
+    if (dm) shp = std::make_unique<DmShell>();
     if (tan) {
       TangentState& TS = *tan;
       const int NP = TangentState::NP;
@@ -1393,9 +1410,12 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
       std::vector<int> kept_state;
       for (int i = 0; i < nk; ++i)
         for (int x = 0; x < K.blk.size[i]; ++x) kept_state.push_back(P.soff[K.src[i]] + x);
+      // Eigenvector tangents: of the kept states; of every state when the
+      // shell is kept for DM-NRG (its rotations and c_d use them all).
+      const std::vector<int>& ccols = dm ? P.bsize : keptb;
       std::vector<int64_t> coff(nb);
       int64_t csz = 0;
-      for (int b = 0; b < nb; ++b) { coff[b] = csz; csz += (int64_t)P.bsize[b] * keptb[b]; }
+      for (int b = 0; b < nb; ++b) { coff[b] = csz; csz += (int64_t)P.bsize[b] * ccols[b]; }
       int gs = 0;
       for (int g = 1; g < P.nstates; ++g) if (R.en[g] < R.en[gs]) gs = g;
       const int nkept = (int)kept_state.size();
@@ -1437,7 +1457,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
         for (int k = 0; k < 8; ++k)
           ptrs.push_back(k < (int)avg_ops.size() ? TS.dops[p][1 - tcur][avg_ops[k]].as<double>() : nullptr);
       Packer tp;
-      const size_t o_ptr = tp.add(ptrs), o_kst = tp.add(kept_state), o_coff = tp.add(coff), o_nkeep = tp.add(keptb),
+      const size_t o_ptr = tp.add(ptrs), o_kst = tp.add(kept_state), o_coff = tp.add(coff), o_nkeep = tp.add(ccols),
                    o_stcf = tp.add(B.stcf);
       TS.tabs.ensure(tp.host.size() + 256);
       h2d(c, TS.tabs.p, tp.host.data(), tp.host.size());
@@ -1450,7 +1470,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
       // the eigen-derivative GEMMs of every block (the same for all parameters)
       GemmPlan G1, G2, G3, G4;
       for (int b = 0; b < nb; ++b) {
-        const int n = P.bsize[b], kb = keptb[b];
+        const int n = P.bsize[b], kb = ccols[b];
         const int64_t h = P.hoff[b], y = P.yoff[b];
         double* Zb = c->Z.as<double>() + y;
         double* Ztb = c->Zt.as<double>() + y;
@@ -1463,6 +1483,10 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
       TS.part.ensure(sizeof(double) * tan_partial_doubles());
       TS.out.ensure(sizeof(double) * TanSumArgs::kMaxOut * NP + 64);
       std::vector<double> sums((size_t)TanSumArgs::kMaxOut * NP), dl(NP);
+      if (dm) {
+        shp->ntan = NP;
+        shp->den.assign((size_t)NP * P.nstates, 0.0);
+      }
       for (int p = 0; p < NP; ++p) {
         // dH_N: the assembly on the tangents of the old energies and operators
         launch_tan_gather(TS.dEk[p][tcur].as<double>(), (const int*)(tb + o_stcf), P.nstates, TS.deold.as<double>(),
@@ -1482,6 +1506,11 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
         run_gemm_plan(c, G4);
         launch_tan_shift(TS.dlam.as<double>(), P.nstates, gs, TS.dEall.as<double>(), (const int*)(tb + o_kst), nkept,
                          TS.dEk[p][1 - tcur].as<double>(), c->stream);
+        if (dm) {  // the shell's tangents: every eigenvector's and every energy's
+          shp->dZ[p].ensure(sizeof(double) * std::max<int64_t>(P.ysize, 1));
+          CU(cudaMemcpyAsync(shp->dZ[p].p, TS.dZ.p, sizeof(double) * P.ysize, cudaMemcpyDeviceToDevice, c->stream));
+          d2h(c, shp->den.data() + (size_t)p * P.nstates, TS.dEall.p, sizeof(double) * P.nstates);
+        }
         // dO_new = dZ_I F Z_J^T + Z_I F dZ_J^T + Z_I dF Z_J^T
         for (int r = 0; r < 3; ++r)
           for (int o = 0; o < nops; ++o)
@@ -1496,6 +1525,12 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
         for (int o = 0; o < nops; ++o)
           launch_tan_axpy3(TS.tmp[0][o].as<double>(), TS.tmp[1][o].as<double>(), TS.tmp[2][o].as<double>(), 1.0,
                            newops[o].size, TS.dops[p][1 - tcur][o].as<double>(), c->stream);
+        if (dm) {
+          const int64_t ncd = newops[nops_h].size;
+          shp->dcd[p].ensure(sizeof(double) * std::max<int64_t>(ncd, 1));
+          CU(cudaMemcpyAsync(shp->dcd[p].p, TS.dops[p][1 - tcur][nops_h].p, sizeof(double) * ncd,
+                             cudaMemcpyDeviceToDevice, c->stream));
+        }
         // weighted sums of the thermodynamics and operator-average tangents
         TanSumArgs ts{};
         ts.nstates = P.nstates; ts.state_block = (const int*)(mb + o_sb); ts.bq = (const double*)(mb + o_bq);
@@ -1537,7 +1572,7 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
     }
     // ---------------- DM-NRG shell (SaveArrays, NRGcodehandlerClass.cpp:887-932)
     if (dm) {
-      auto sh = std::make_unique<DmShell>();
+      std::unique_ptr<DmShell> sh = std::move(shp);
       sh->bsize = P.bsize; sh->boff = P.soff; sh->qn = B.blk.qn; sh->en = R.en;
       sh->kept.resize(P.nstates);
       for (int g = 0; g < P.nstates; ++g) sh->kept[g] = R.en[g] <= R.ecut ? 1 : 0;
@@ -1586,9 +1621,13 @@ void sweep_run(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false, bool ch
 // ground-state energy sum_{M<=N} D_M E_min,M (H_N is built from energies
 // already shifted by the earlier E_min and rescaled, so the shifts add up in
 // absolute units) and its tangents.
-void grad_forward_impl(nrg_ctx* c, const nrg_sweep_config* cfg) {
+//
+// dm: the sweep keeps the DM-NRG shells (nrg_sweep_run_dm) with their
+// tangents (nrg_grad_forward_dm).
+void grad_forward_impl(nrg_ctx* c, const nrg_sweep_config* cfg, bool dm = false) {
   if (!c->tan) c->tan = new TangentState();
-  sweep_run(c, cfg, false, false, c->tan);
+  c->dm_drhow.clear();
+  sweep_run(c, cfg, dm, false, c->tan);
   const int NP = TangentState::NP;
   const int ni = (int)c->iters.size();
   const double lambda = cfg->lambda, HLF = 0.5 * (1.0 + 1.0 / lambda);
@@ -1653,6 +1692,18 @@ double dm_partition(const DmShell& s, double beta, bool disc_only) {
 }
 
 
+// The tangent of dm_partition along parameter k of the shells' tangents.
+double dm_partition_tangent(const DmShell& s, double beta, bool disc_only, int k) {
+  const double* dE = s.den.data() + (size_t)k * s.en.size();
+  double sum = 0.0;
+  for (size_t b = 0; b < s.bsize.size(); ++b) {
+    const double Si = s.qn[2 * b + 1];
+    for (int i = s.boff[b]; i < s.boff[b] + s.bsize[b]; ++i)
+      if (!disc_only || !s.kept[i]) sum += (2.0 * Si + 1.0) * (-beta * dE[i]) * std::exp(-beta * s.en[i]);
+  }
+  return sum;
+}
+
 // DM_NRG_SetRhoNmax + (RotateMatrix, DM_NRG_CalcRhoN_withSU2) per shell, FDM.
 void dm_backprop_impl(nrg_ctx* c, const nrg_dm_params* prm, double* rho_trace) {
   if (c->dm.empty()) throw NrgError(NRG_ERR_STATE, "no DM-NRG shells: run nrg_sweep_run_dm first");
@@ -1667,6 +1718,22 @@ void dm_backprop_impl(nrg_ctx* c, const nrg_dm_params* prm, double* rho_trace) {
   for (int N = Nmax - 1; N >= 0; --N) {
     TempBar = p.temp / calc_dn(L, N - 1);
     ZTot += dm_partition(*c->dm[N], 1.0 / TempBar, true) * std::pow(p.site_dim, Nmax - N);
+  }
+  // Tangents (shells of nrg_grad_forward_dm): d ln ZTot per parameter, with
+  // d exp(-beta E) = -beta dE exp(-beta E).
+  bool tg = true;
+  for (const auto& sp : c->dm) tg = tg && sp->ntan == DmTan::NP;
+  double dlogz[DmTan::NP] = {0.0, 0.0, 0.0, 0.0};
+  if (tg) {
+    for (int k = 0; k < DmTan::NP; ++k) {
+      TempBar = p.temp / calc_dn(L, Nmax - 1);
+      double dz = dm_partition_tangent(*c->dm[Nmax], 1.0 / TempBar, false, k);
+      for (int N = Nmax - 1; N >= 0; --N) {
+        TempBar = p.temp / calc_dn(L, N - 1);
+        dz += dm_partition_tangent(*c->dm[N], 1.0 / TempBar, true, k) * std::pow(p.site_dim, Nmax - N);
+      }
+      dlogz[k] = dz / ZTot;
+    }
   }
   {  // SetRhoNmax (DM_NRG_SetRhoNmax.cpp:9-126): diagonal Boltzmann weights.
     DmShell& s = *c->dm[Nmax];
@@ -1683,6 +1750,19 @@ void dm_backprop_impl(nrg_ctx* c, const nrg_dm_params* prm, double* rho_trace) {
       const int n = s.bsize[b];
       for (int i = 0; i < n; ++i)
         if (R[s.zoff[b] + (int64_t)i * n + i] != 0.0) s.rrows[b] = i + 1;
+    }
+    for (int k = 0; tg && k < DmTan::NP; ++k) {  // d rho = rho (-beta dE - d ln ZTot)
+      std::vector<double> dR((size_t)std::max<int64_t>(s.zsize, 1), 0.0);
+      const double* dE = s.den.data() + (size_t)k * s.en.size();
+      for (size_t b = 0; b < s.bsize.size(); ++b) {
+        const int n = s.bsize[b];
+        for (int i = 0; i < n; ++i) {
+          const int64_t q = s.zoff[b] + (int64_t)i * n + i;
+          dR[q] = R[q] * (-beta * dE[s.boff[b] + i] - dlogz[k]);
+        }
+      }
+      s.drho[k].ensure(sizeof(double) * dR.size());
+      h2d(c, s.drho[k].p, dR.data(), sizeof(double) * s.zsize);
     }
   }
   for (int N = Nmax - 1; N >= 0; --N) {
@@ -1706,6 +1786,28 @@ void dm_backprop_impl(nrg_ctx* c, const nrg_dm_params* prm, double* rho_trace) {
     }
     run_gemm_plan(c, g1);
     run_gemm_plan(c, g2);
+    // Tangents: d rho~ = Z^T (d rho Z + rho dZ) + dZ^T (rho Z), per parameter.
+    const size_t zsa = (zs + 255) & ~size_t(255);
+    double* U0 = nullptr;
+    if (tg) {
+      c->dmtan.ensure(2 * DmTan::NP * zsa);
+      U0 = c->dmtan.as<double>();
+      auto Uk = [&](int k) { return (double*)((char*)U0 + k * zsa); };
+      auto Rk = [&](int k) { return (double*)((char*)U0 + (DmTan::NP + k) * zsa); };
+      GemmPlan h[4];
+      for (int k = 0; k < DmTan::NP; ++k)
+        for (size_t b = 0; b < s1.bsize.size(); ++b) {
+          const int n = s1.bsize[b], r = s1.rrows[b];
+          const int64_t o = s1.zoff[b];
+          const double* Z = s1.Z.as<double>() + o;
+          const double* dZ = s1.dZ[k].as<double>() + o;
+          h[0].add(GemmJob{r, n, r, 0, s1.drho[k].as<double>() + o, n, Z, n, Uk(k) + o, n});
+          h[1].add(GemmJob{r, n, r, 0, s1.rho.as<double>() + o, n, dZ, n, Uk(k) + o, n, 1});
+          h[2].add(GemmJob{n, n, r, 1, Z, n, Uk(k) + o, n, Rk(k) + o, n});
+          h[3].add(GemmJob{n, n, r, 1, dZ, n, Tm + o, n, Rk(k) + o, n, 1});
+        }
+      for (int q = 0; q < 4; ++q) run_gemm_plan(c, h[q]);
+    }
     // Partial trace over the child states (DM_NRG_SetChildSt, SetChildSameType).
     const Basis& B1 = s1.basis;
     const int nbN = (int)sN.bsize.size();
@@ -1740,7 +1842,7 @@ void dm_backprop_impl(nrg_ctx* c, const nrg_dm_params* prm, double* rho_trace) {
     Packer pk;
     size_t o_bs = pk.add(sN.bsize), o_so = pk.add(sN.boff), o_ro = pk.add(sN.zoff), o_nk = pk.add(nkept),
            o_tf = pk.add(tfirst), o_tc = pk.add(tcount), o_t = pk.add(terms), o_en = pk.add(sN.en),
-           o_kp = pk.add(sN.kept);
+           o_kp = pk.add(sN.kept), o_den = tg ? pk.add(sN.den) : 0;
     c->meta.ensure(pk.host.size() + 256);
     h2d(c, c->meta.p, pk.host.data(), pk.host.size());
     char* mb = c->meta.as<char>();
@@ -1765,6 +1867,16 @@ void dm_backprop_impl(nrg_ctx* c, const nrg_dm_params* prm, double* rho_trace) {
     }
     launch_dm_trace(ta, nbN, c->stream);
     c->launches++;
+    for (int k = 0; tg && k < DmTan::NP; ++k) {
+      DmTraceArgs tt = ta;
+      tt.rot = (const double*)((char*)U0 + (DmTan::NP + k) * zsa);
+      tt.dE = (const double*)(mb + o_den) + (size_t)k * sN.en.size();
+      tt.dlogz = dlogz[k];
+      sN.drho[k].ensure(sizeof(double) * std::max<int64_t>(sN.zsize, 1));
+      tt.rho = sN.drho[k].as<double>();
+      launch_dm_trace(tt, nbN, c->stream);
+      c->launches++;
+    }
     CU(cudaStreamSynchronize(c->stream));  // meta and T are reused by the next shell
   }
   tm.stop(t0, &c->timing.dm_backprop_ms);
@@ -1772,6 +1884,7 @@ void dm_backprop_impl(nrg_ctx* c, const nrg_dm_params* prm, double* rho_trace) {
   check_flag(c);
   tm.collect();
   c->dm_rho_valid = true;
+  c->dm_drho_valid = tg;
   c->dm_temp = p.temp;
   if (rho_trace) {
     for (int N = 0; N < nsh; ++N) {
@@ -1808,9 +1921,19 @@ std::vector<double> dm_grid(double L, int nsh, int nw) {
 
 // CalcSpecDM_NRG (SpecFuncClass.cpp:1827-1883) with FDM_SpecDens_M_STL /
 // CalcSpecCosti_T_N for every shell of the window, for all frequencies.
+//
+// d_rhow != NULL (nrg_lehmann_grad): the same sums differentiated along the
+// four parameter directions of the shells' tangents, d_rhow[k * nomega + j].
+// Per shell: d(rho A) = d rho A + rho dA and d(A rho) = dA rho + A d rho
+// (grouped GEMMs), the records' tangents beside the records, and the
+// Lehmann kernel over them.
 void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double* omegas, double* omega_rhow,
-                  int* nout) {
+                  int* nout, double* d_rhow = nullptr) {
   if (!c->dm_rho_valid) throw NrgError(NRG_ERR_STATE, "no density matrices: run nrg_dm_backprop first");
+  const bool tg = d_rhow != nullptr;
+  constexpr int NP = DmTan::NP;
+  if (tg && !c->dm_drho_valid)
+    throw NrgError(NRG_ERR_STATE, "no density-matrix tangents: run nrg_grad_forward_dm, then nrg_dm_backprop");
   if (!omega_rhow || !nout || nomega < 0) throw NrgError(NRG_ERR_ARG, "bad output arguments");
   const int nsh = (int)c->dm.size(), Nmax = nsh - 1;
   const double L = c->dm_lambda, hlf = 0.5 * (1.0 + (1.0 / L));
@@ -1863,6 +1986,7 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
   // against every frequency whose window holds the shell, one partial sum
   // per record chunk and frequency.  Only one shell's records exist at a time.
   std::vector<LehList> lists;                      // every shell's lists (for the fold)
+  std::vector<LehList> tlists[NP];                 // their tangent lists (parts only are read by the fold)
   std::vector<int> list_of(4 * (size_t)nsh, -1);  // [shell][list L]
   int64_t evals = 0, nrec_all = 0;
   for (int N = 0; N < nsh; ++N) {
@@ -1881,6 +2005,14 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
     c->Y.ensure(sizeof(double) * std::max<int64_t>(2 * pbytes, 1));
     double* P1 = c->Y.as<double>();
     double* P2 = P1 + pbytes;
+    // tangents: d(rho A) of parameter k at X1 + k pbytes, d(A rho) at X2 + k pbytes
+    double *X1 = nullptr, *X2 = nullptr;
+    GemmPlan gt0, gt1;
+    if (tg) {
+      c->dmtan.ensure(sizeof(double) * std::max<int64_t>(2 * NP * pbytes, 1));
+      X1 = c->dmtan.as<double>();
+      X2 = X1 + NP * pbytes;
+    }
     for (size_t k = 0; k < s.cd.bi.size(); ++k) {
       const int b1 = s.cd.bi[k], b2 = s.cd.bj[k];
       DmPair P{};
@@ -1899,8 +2031,21 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
         // rho A has r1 nonzero rows, A rho r2 nonzero columns (the rest is
         // never read).
         const double* Acd = s.cdel.as<double>() + P.a_off;
-        g.add(GemmJob{P.r1, P.n2, P.r1, 0, s.rho.as<double>() + s.zoff[b1], P.n1, Acd, P.n2, P1 + poff, P.n2});
-        g.add(GemmJob{P.n1, P.r2, P.r2, 0, Acd, P.n2, s.rho.as<double>() + s.zoff[b2], P.n2, P2 + poff, P.n2});
+        const double* rho1 = s.rho.as<double>() + s.zoff[b1];
+        const double* rho2 = s.rho.as<double>() + s.zoff[b2];
+        g.add(GemmJob{P.r1, P.n2, P.r1, 0, rho1, P.n1, Acd, P.n2, P1 + poff, P.n2});
+        g.add(GemmJob{P.n1, P.r2, P.r2, 0, Acd, P.n2, rho2, P.n2, P2 + poff, P.n2});
+        for (int k = 0; tg && k < NP; ++k) {
+          const double* dA = s.dcd[k].as<double>() + P.a_off;
+          const double* drho1 = s.drho[k].as<double>() + s.zoff[b1];
+          const double* drho2 = s.drho[k].as<double>() + s.zoff[b2];
+          double* x1 = X1 + k * pbytes + poff;
+          double* x2 = X2 + k * pbytes + poff;
+          gt0.add(GemmJob{P.r1, P.n2, P.r1, 0, drho1, P.n1, Acd, P.n2, x1, P.n2});
+          gt1.add(GemmJob{P.r1, P.n2, P.r1, 0, rho1, P.n1, dA, P.n2, x1, P.n2, 1});
+          gt0.add(GemmJob{P.n1, P.r2, P.r2, 0, dA, P.n2, rho2, P.n2, x2, P.n2});
+          gt1.add(GemmJob{P.n1, P.r2, P.r2, 0, Acd, P.n2, drho2, P.n2, x2, P.n2, 1});
+        }
       }
       if ((int64_t)P.n1 * P.n2 > (int64_t)INT32_MAX) throw NrgError(NRG_ERR_SIZE, "c_d block pair too large");
       if (last || !P.skip)
@@ -1911,8 +2056,11 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
     }
     if (chunks.empty()) continue;
     run_gemm_plan(c, g);
+    run_gemm_plan(c, gt0);
+    run_gemm_plan(c, gt1);
     Packer pk;
-    size_t o_p = pk.add(pairs), o_c = pk.add(chunks), o_en = pk.add(s.en), o_kp = pk.add(s.kept);
+    size_t o_p = pk.add(pairs), o_c = pk.add(chunks), o_en = pk.add(s.en), o_kp = pk.add(s.kept),
+           o_den = tg ? pk.add(s.den) : 0;
     c->meta.ensure(pk.host.size() + 256);
     h2d(c, c->meta.p, pk.host.data(), pk.host.size());
     char* mb = c->meta.as<char>();
@@ -1930,6 +2078,14 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
         for (int i = s.boff[b]; i < s.boff[b] + s.bsize[b]; ++i)
           z += (2.0 * s.qn[2 * b + 1] + 1.0) * std::exp(-beta_last * s.en[i]);
       a.inv_z_last = 1.0 / z;
+      for (int k = 0; tg && k < NP; ++k) a.dlogz_last[k] = dm_partition_tangent(s, beta_last, false, k) / z;
+    }
+    if (tg) {
+      a.ntan = NP;
+      a.dP1 = X1; a.dP2 = X2; a.pstride = pbytes;
+      for (int k = 0; k < NP; ++k) a.dcd[k] = s.dcd[k].as<double>();
+      a.dE = (const double*)(mb + o_den);
+      a.nstates = (int)s.en.size();
     }
     a.gauss_below = p.twindow * (p.temp / dn[N]);
     a.inv_b = 1.0 / p.bbroad; a.inv_bt = 1.0 / p.broadtemp;
@@ -1944,13 +2100,18 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
     CU(cudaStreamSynchronize(c->stream));
     int64_t nrec = 0;
     for (int Lk = 0; Lk < 4; ++Lk) nrec += tot[Lk];
-    c->dmrec.ensure(sizeof(double) * std::max<int64_t>(2 * nrec, 1));
+    const int per_rec = tg ? 2 + 2 * NP : 2;  // key, w (and per parameter d w, 2 w d key)
+    c->dmrec.ensure(sizeof(double) * std::max<int64_t>(per_rec * nrec, 1));
     double* r = c->dmrec.as<double>();
     for (int Lk = 0; Lk < 4; ++Lk) {
       s.nrec[Lk] = tot[Lk];
       a.key[Lk] = r;
       a.w[Lk] = r + tot[Lk];
-      r += 2 * tot[Lk];
+      if (tg) {
+        a.tw[Lk] = r + 2 * tot[Lk];
+        a.tg[Lk] = r + (2 + NP) * tot[Lk];
+      }
+      r += per_rec * tot[Lk];
     }
     launch_dm_records(a, 1, c->stream);
     c->launches++;
@@ -1996,6 +2157,18 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
     }
     if (items.size() > (size_t)INT32_MAX) throw NrgError(NRG_ERR_SIZE, "too many Lehmann work items");
     s.lpart.ensure(sizeof(double) * std::max<int64_t>(part, 1));
+    if (tg) s.ltpart.ensure(sizeof(double) * std::max<int64_t>(NP * part, 1));
+    std::vector<LehList> stl;  // this shell's tangent lists, parameter major
+    for (int k = 0; tg && k < NP; ++k)
+      for (size_t q = 0; q < sl.size(); ++q) {
+        LehList t = sl[q];
+        const int Lk = sl_kind[q];
+        t.w = a.tw[Lk] + k * tot[Lk];
+        t.g = a.tg[Lk] + k * tot[Lk];
+        t.part = s.ltpart.as<double>() + k * part + sl_off[q];
+        stl.push_back(t);
+        tlists[k].push_back(t);
+      }
     for (size_t q = 0; q < sl.size(); ++q) {
       sl[q].part = s.lpart.as<double>() + sl_off[q];
       list_of[4 * (size_t)N + sl_kind[q]] = (int)lists.size();
@@ -2013,6 +2186,25 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
       launch_lehmann(la, c->stream);
       c->launches++;
       tm.stop(t1, &c->timing.lehmann_ms);
+      if (tg) {  // the same items over the tangent lists of every parameter
+        std::vector<LehItem> titems;
+        for (int k = 0; k < NP; ++k)
+          for (LehItem it : items) {
+            it.list += k * (int)sl.size();
+            titems.push_back(it);
+          }
+        if (titems.size() > (size_t)INT32_MAX) throw NrgError(NRG_ERR_SIZE, "too many Lehmann work items");
+        Packer pt;
+        const size_t o_tl = pt.add(stl), o_ti = pt.add(titems), o_to = pt.add(omega_idx);
+        c->dmtmeta.ensure(pt.host.size() + 256);
+        h2d(c, c->dmtmeta.p, pt.host.data(), pt.host.size());
+        char* tb2 = c->dmtmeta.as<char>();
+        LehmannArgs lt = la;
+        lt.lists = (const LehList*)(tb2 + o_tl); lt.items = (const LehItem*)(tb2 + o_ti);
+        lt.nitems = (int)titems.size(); lt.omega_idx = (const int*)(tb2 + o_to);
+        launch_lehmann_tangent(lt, c->stream);
+        c->launches++;
+      }
     }
     CU(cudaStreamSynchronize(c->stream));  // meta, vmeta, dmrec and Y are reused by the next shell
   }
@@ -2031,19 +2223,29 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
     }
   Packer pf;
   const size_t o_li = pf.add(lists), o_fl = pf.add(fold_list), o_fp = pf.add(fold_pos);
+  size_t o_tli[NP] = {0, 0, 0, 0};
+  for (int k = 0; tg && k < NP; ++k) o_tli[k] = pf.add(tlists[k]);
   c->meta.ensure(pf.host.size() + 256);
   h2d(c, c->meta.p, pf.host.data(), pf.host.size());
   char* fb = c->meta.as<char>();
-  c->dmrec.ensure(sizeof(double) * std::max(nw_, 1));
+  const int nout_sets = tg ? 1 + NP : 1;
+  c->dmrec.ensure(sizeof(double) * std::max(nout_sets * nw_, 1));
   la.lists = (const LehList*)(fb + o_li); la.items = nullptr; la.nitems = 0;
   la.fold_list = (const int*)(fb + o_fl); la.fold_pos = (const int*)(fb + o_fp);
   la.out = c->dmrec.as<double>();
   cudaEvent_t t2 = tm.start();
   launch_lehmann_fold(la, c->stream);
   c->launches++;
+  for (int k = 0; tg && k < NP; ++k) {  // the tangent lists have the primal lists' order
+    LehmannArgs lf = la;
+    lf.lists = (const LehList*)(fb + o_tli[k]);
+    lf.out = c->dmrec.as<double>() + (size_t)(1 + k) * nw_;
+    launch_lehmann_fold(lf, c->stream);
+    c->launches++;
+  }
   tm.stop(t2, &c->timing.lehmann_ms);
-  std::vector<double> A(nw_);
-  d2h(c, A.data(), la.out, sizeof(double) * nw_);
+  std::vector<double> A((size_t)nout_sets * nw_);
+  d2h(c, A.data(), la.out, sizeof(double) * nout_sets * nw_);
   tm.stop(t0, &c->timing.dm_spectral_ms);
   CU(cudaStreamSynchronize(c->stream));
   check_flag(c);
@@ -2051,6 +2253,14 @@ void lehmann_impl(nrg_ctx* c, const nrg_dm_params* prm, int nomega, const double
   c->timing.lehmann_pairs = nrec_all;
   c->timing.lehmann_evals = evals;
   for (int k = 0; k < nw_; ++k) { omega_rhow[k] = om[k]; omega_rhow[nomega + k] = A[k]; }
+  if (tg) {
+    c->dm_drhow.assign((size_t)NP * nw_, 0.0);
+    for (int k = 0; k < NP; ++k)
+      for (int j = 0; j < nw_; ++j) {
+        d_rhow[(size_t)k * nomega + j] = A[(size_t)(1 + k) * nw_ + j];
+        c->dm_drhow[(size_t)k * nw_ + j] = A[(size_t)(1 + k) * nw_ + j];
+      }
+  }
   *nout = nw_;
 }
 
@@ -2155,6 +2365,7 @@ void dm_load_bin_impl(nrg_ctx* c, const char* dir, const char* name, int nshells
   c->opptr.ensure(sizeof(double*) * 32);
   c->dm.clear();
   c->dm_rho_valid = false;
+  c->dm_drho_valid = false;
   c->dm_lambda = lambda;
   c->dm_model = MODEL_1CHQS;
   c->dm_hm1_en.assign(st.en.size(), 0.0);
@@ -2945,12 +3156,13 @@ nrg_status nrg_sweep_timing(const nrg_ctx* ctx, nrg_timing* out) {
   return NRG_OK;
 }
 
-nrg_status nrg_grad_forward(nrg_ctx* ctx, const nrg_sweep_config* cfg, nrg_grad* out) {
+namespace {
+nrg_status grad_forward_abi(nrg_ctx* ctx, const nrg_sweep_config* cfg, nrg_grad* out, bool dm) {
   if (!ctx || !cfg || !out) return NRG_ERR_ARG;
   ctx->err.clear();
   GUARD(ctx, {
     CU(cudaSetDevice(ctx->device));
-    grad_forward_impl(ctx, cfg);
+    grad_forward_impl(ctx, cfg, dm);
   });
   const nrg::TangentState& T = *ctx->tan;
   out->nsites = (int)ctx->iters.size();
@@ -2961,6 +3173,35 @@ nrg_status nrg_grad_forward(nrg_ctx* ctx, const nrg_sweep_config* cfg, nrg_grad*
   out->d_emin = ctx->grad_demin.data();
   out->egs = ctx->grad_egs.data();
   out->d_egs = ctx->grad_degs.data();
+  return NRG_OK;
+}
+}  // namespace
+
+nrg_status nrg_grad_forward(nrg_ctx* ctx, const nrg_sweep_config* cfg, nrg_grad* out) {
+  return grad_forward_abi(ctx, cfg, out, false);
+}
+
+nrg_status nrg_grad_forward_dm(nrg_ctx* ctx, const nrg_sweep_config* cfg, nrg_grad* out) {
+  if (cfg && cfg->model != NRG_MODEL_1CH_QS) {
+    if (ctx) ctx->err = "nrg_grad_forward_dm: DM-NRG tangents are built for NRG_MODEL_1CH_QS";
+    return NRG_ERR_ARG;
+  }
+  return grad_forward_abi(ctx, cfg, out, true);
+}
+
+nrg_status nrg_lehmann_grad_backward(nrg_ctx* ctx, const double* g_rhow, double* grad) {
+  if (!ctx || !g_rhow || !grad) return NRG_ERR_ARG;
+  if (ctx->dm_drhow.empty()) {
+    ctx->err = "nrg_lehmann_grad_backward needs a preceding nrg_lehmann_grad on the context";
+    return NRG_ERR_STATE;
+  }
+  const int NP = nrg::DmTan::NP;
+  const size_t nw = ctx->dm_drhow.size() / NP;
+  for (int k = 0; k < NP; ++k) {
+    double g = 0.0;
+    for (size_t j = 0; j < nw; ++j) g += g_rhow[j] * ctx->dm_drhow[(size_t)k * nw + j];
+    grad[k] = g;
+  }
   return NRG_OK;
 }
 
@@ -3161,6 +3402,19 @@ nrg_status nrg_lehmann(nrg_ctx* ctx, const nrg_dm_params* prm, int nomega, const
     CU(cudaSetDevice(ctx->device));
     std::memset(&ctx->timing, 0, sizeof(ctx->timing));
     lehmann_impl(ctx, prm, nomega, omegas, omega_rhow, nout);
+  });
+  return NRG_OK;
+}
+
+nrg_status nrg_lehmann_grad(nrg_ctx* ctx, const nrg_dm_params* prm, int nomega, const double* omegas,
+                            double* omega_rhow, double* d_rhow, int* nout) {
+  if (!ctx || !d_rhow) return NRG_ERR_ARG;
+  ctx->err.clear();
+  ctx->dm_drhow.clear();
+  GUARD(ctx, {
+    CU(cudaSetDevice(ctx->device));
+    std::memset(&ctx->timing, 0, sizeof(ctx->timing));
+    lehmann_impl(ctx, prm, nomega, omegas, omega_rhow, nout, d_rhow);
   });
   return NRG_OK;
 }

@@ -68,7 +68,10 @@ __global__ void __launch_bounds__(256) gemm_jobs_kernel(const GemmJob* jobs, con
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int c = n0 + tx + 16 * j;
-      if (c < J.n) J.C[(int64_t)r * J.ldc + c] = acc[i][j];
+      if (c < J.n) {
+        double* o = J.C + (int64_t)r * J.ldc + c;
+        *o = J.accum ? *o + acc[i][j] : acc[i][j];
+      }
     }
   }
 }
@@ -93,7 +96,10 @@ __global__ void __launch_bounds__(256) dm_trace_kernel(DmTraceArgs A) {
           v += T.cg * A.rot[T.rot_off + (int64_t)(T.base + ii * T.stride) * T.nb + T.base + jj * T.stride];
       }
     }
-    if (i == j && !A.kept[s0 + i] && A.zdisc != 0.0) v = exp(-A.beta * A.en[s0 + i]) / A.zdisc;
+    if (i == j && !A.kept[s0 + i] && A.zdisc != 0.0) {
+      const double e = exp(-A.beta * A.en[s0 + i]) / A.zdisc;
+      v = A.dE ? e * (-A.beta * A.dE[s0 + i] - A.dlogz) : e;
+    }
     R[idx] = v;
   }
 }
@@ -119,6 +125,32 @@ __device__ __forceinline__ void pair_value(const DmRecArgs& A, const DmPair& P, 
     if (!A.kept[P.s1 + a]) wn = w;
   }
   dE = E2 - E1;
+}
+
+// pair_value differentiated along direction p: d(E_j - E_i) and the
+// tangents of W+ and W- (the same kept / discarded split).
+__device__ __forceinline__ void pair_tangent(const DmRecArgs& A, const DmPair& P, int64_t idx, int p, double& ddE,
+                                             double& dwp, double& dwn) {
+  const int a = (int)(idx / P.n2), b = (int)(idx - (int64_t)a * P.n2);
+  const double m = A.cd[P.a_off + idx], dm = A.dcd[p][P.a_off + idx];
+  const double* dE = A.dE + (int64_t)p * A.nstates;
+  const double dE1 = dE[P.s1 + a], dE2 = dE[P.s2 + b];
+  dwp = 0.0; dwn = 0.0;
+  if (A.last) {
+    const double e1 = exp(-A.beta_last * A.en[P.s1 + a]), e2 = exp(-A.beta_last * A.en[P.s2 + b]);
+    const double s12 = (e1 + e2) * m;
+    const double ds12 = (e1 + e2) * dm - A.beta_last * (e1 * dE1 + e2 * dE2) * m;
+    const double w = P.cg * s12 * m * A.inv_z_last;
+    dwp = dwn = P.cg * (ds12 * m + s12 * dm) * A.inv_z_last - w * A.dlogz_last[p];
+  } else if (!P.skip) {
+    const int64_t q = (int64_t)p * A.pstride + P.p_off + idx;
+    const double p1 = a < P.r1 ? A.P1[P.p_off + idx] : 0.0, p2 = b < P.r2 ? A.P2[P.p_off + idx] : 0.0;
+    const double dp1 = a < P.r1 ? A.dP1[q] : 0.0, dp2 = b < P.r2 ? A.dP2[q] : 0.0;
+    const double dw = P.cg * ((dp1 + dp2) * m + (p1 + p2) * dm);
+    if (!A.kept[P.s2 + b]) dwp = dw;
+    if (!A.kept[P.s1 + a]) dwn = dw;
+  }
+  ddE = dE2 - dE1;
 }
 
 // Bit L set: the pair's term is in list L (see DmRecArgs).
@@ -184,7 +216,9 @@ __global__ void __launch_bounds__(1024) dm_scan_kernel(DmRecArgs A) {
   }
 }
 
-// pass 1: the records, in pair order within every list.
+// pass 1: the records, in pair order within every list (TAN: and their
+// tangents).
+template <bool TAN>
 __global__ void __launch_bounds__(256) dm_scatter_kernel(DmRecArgs A) {
   constexpr int NW = 8;
   __shared__ int wtot[4][NW];
@@ -200,6 +234,12 @@ __global__ void __launch_bounds__(256) dm_scatter_kernel(DmRecArgs A) {
     double dE = 0.0, wp = 0.0, wn = 0.0;
     if (in) pair_value(A, P, idx, dE, wp, wn);
     const unsigned f = in ? pair_lists(A, dE, wp, wn) : 0u;
+    double tdd[4] = {0.0, 0.0, 0.0, 0.0}, twp[4] = {0.0, 0.0, 0.0, 0.0}, twn[4] = {0.0, 0.0, 0.0, 0.0};
+    if (TAN) {
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+        if (f && p < A.ntan) pair_tangent(A, P, idx, p, tdd[p], twp[p], twn[p]);
+    }
     unsigned mask[4];
     for (int L = 0; L < 4; ++L) {
       mask[L] = __ballot_sync(0xffffffffu, (f >> L) & 1u);
@@ -220,6 +260,27 @@ __global__ void __launch_bounds__(256) dm_scatter_kernel(DmRecArgs A) {
         } else {
           A.key[L][pos] = dE * A.inv_bt;
           A.w[L][pos] = W * A.gauss_scale;
+        }
+        // tangents: log-Gaussian w = W c / |dE|, key = ln|dE| / b;
+        // Gaussian w = W c, key = dE / bt
+        const int64_t T = A.totals[L];
+#pragma unroll
+        for (int p = 0; p < (TAN ? 4 : 0); ++p) {
+          if (p >= A.ntan) break;
+          const double dW = L < 2 ? twp[p] : twn[p];
+          double tw, tg;
+          if (L == 0 || L == 2) {
+            const double aE = fabs(dE == 0.0 ? 1.0e-100 : dE);
+            const double daE = (dE < 0.0 ? -1.0 : 1.0) * tdd[p];
+            const double w = W * A.log_scale / aE;
+            tw = dW * A.log_scale / aE - w * daE / aE;
+            tg = 2.0 * w * (daE / aE) * A.inv_b;
+          } else {
+            tw = dW * A.gauss_scale;
+            tg = 2.0 * (W * A.gauss_scale) * tdd[p] * A.inv_bt;
+          }
+          A.tw[L][p * T + pos] = tw;
+          A.tg[L][p * T + pos] = tg;
         }
       }
       run[L] += all;
@@ -314,6 +375,93 @@ __global__ void __launch_bounds__(256) lehmann_kernel(LehmannArgs A) {
   }
 }
 
+// lehmann_kernel over the tangent of every record: the term's tangent is
+// (d w + g x) exp(-x^2), x = t - key, with g = 2 w d key.
+__global__ void __launch_bounds__(256) lehmann_tangent_kernel(LehmannArgs A) {
+  constexpr int kStage = 1024, kPerWarp = 16, kGroups = kOmegaTile / kPerWarp, kSplit = 8 / kGroups;
+  __shared__ double sk[kStage], sw[kStage], sg[kStage], st[kOmegaTile], sred[8][kPerWarp];
+  const LehItem it = A.items[blockIdx.x];
+  const LehList L = A.lists[it.list];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int grp = warp % kGroups, part = warp / kGroups;
+  const int jt = it.tile * kOmegaTile;
+  const double ldn = A.log_dn[L.shell], dn = A.dn[L.shell];
+  if (threadIdx.x < kOmegaTile) {
+    const int j = jt + threadIdx.x;
+    double t = 0.0;
+    if (j < L.nomega) {
+      const int k = A.omega_idx[L.omega_first + j];
+      t = L.gauss ? (A.omega[k] / dn) * A.inv_bt : (A.log_omega[k] - ldn) * A.inv_b - A.b_quarter;
+    }
+    st[threadIdx.x] = t;
+  }
+  const int j0 = jt + grp * kPerWarp;
+  const bool active = j0 < L.nomega;
+  double acc[kPerWarp];
+#pragma unroll
+  for (int q = 0; q < kPerWarp; ++q) acc[q] = 0.0;
+  const int64_t r0 = (int64_t)it.chunk * kRecChunk;
+  const int64_t r1 = min(r0 + (int64_t)kRecChunk, L.nrec);
+  for (int64_t base = r0; base < r1; base += kStage) {
+    const int n = (int)min((int64_t)kStage, r1 - base);
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      sk[i] = L.key[base + i];
+      sw[i] = L.w[base + i];
+      sg[i] = L.g[base + i];
+    }
+    __syncthreads();
+    if (!active) continue;
+    const double* tq = st + grp * kPerWarp;
+    if (it.delta != 0.0) {
+      const double d = it.delta, c = exp(-2.0 * d * d), t0 = tq[0];
+      for (int i = part * 32 + lane; i < n; i += 32 * kSplit) {
+        const double ww = sw[i], gg = sg[i];
+        double x = t0 - sk[i];
+        double g = exp(-x * x), r = exp(-d * (2.0 * x + d));
+        acc[0] += (ww + gg * x) * g;
+#pragma unroll
+        for (int q = 1; q < kPerWarp; ++q) {
+          g *= r;
+          r *= c;
+          x += d;
+          acc[q] += (ww + gg * x) * g;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int qb = 0; qb < kPerWarp; qb += 8) {
+        double a8[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int i = part * 32 + lane; i < n; i += 32 * kSplit) {
+          const double kk = sk[i], ww = sw[i], gg = sg[i];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const double x = tq[qb + q] - kk;
+            a8[q] += (ww + gg * x) * exp(-x * x);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc[qb + q] += a8[q];
+      }
+    }
+  }
+  double mine = 0.0;
+#pragma unroll
+  for (int q = 0; q < kPerWarp; ++q) {
+    double v = acc[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == q) mine = v;
+  }
+  if (lane < kPerWarp) sred[warp][lane] = mine;
+  __syncthreads();
+  if (part == 0 && active && lane < kPerWarp) {
+    double v = 0.0;
+    for (int p = 0; p < kSplit; ++p) v += sred[grp + p * kGroups][lane];
+    const int j = j0 + lane;
+    if (j < L.nomega) L.part[(int64_t)it.chunk * L.nomega + j] = v;
+  }
+}
+
 // A(omega_k): the shells of its window in order, each shell's chunks in
 // order, divided by D_N (CalcSpecDM_NRG, SpecFuncClass.cpp:1827-1883).
 __global__ void lehmann_fold_kernel(LehmannArgs A) {
@@ -353,12 +501,17 @@ void launch_dm_records(const DmRecArgs& a, int pass, cudaStream_t s) {
     dm_count_kernel<<<a.nchunks, 256, 0, s>>>(a);
     dm_scan_kernel<<<1, 1024, 0, s>>>(a);
   } else {
-    dm_scatter_kernel<<<a.nchunks, 256, 0, s>>>(a);
+    if (a.ntan > 0) dm_scatter_kernel<true><<<a.nchunks, 256, 0, s>>>(a);
+    else dm_scatter_kernel<false><<<a.nchunks, 256, 0, s>>>(a);
   }
 }
 
 void launch_lehmann(const LehmannArgs& a, cudaStream_t s) {
   if (a.nitems > 0) lehmann_kernel<<<a.nitems, 256, 0, s>>>(a);
+}
+
+void launch_lehmann_tangent(const LehmannArgs& a, cudaStream_t s) {
+  if (a.nitems > 0) lehmann_tangent_kernel<<<a.nitems, 256, 0, s>>>(a);
 }
 
 void launch_lehmann_fold(const LehmannArgs& a, cudaStream_t s) {

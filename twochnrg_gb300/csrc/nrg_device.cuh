@@ -346,6 +346,7 @@ struct GemmJob {          // C (m x n) = op(A) (m x k) . B (k x n), row-major, F
   int ldb;
   double* C;
   int ldc;
+  int accum;              // 1: C += op(A) . B (after the launches that write C before)
 };
 // One 64x64 tile of C per CTA: tile t belongs to job tile_job[t] at
 // (tile_mn[t] >> 16, tile_mn[t] & 0xffff).
@@ -371,6 +372,11 @@ struct DmTraceArgs {      // DM_NRG_CalcRhoN_withSU2 for all blocks of shell N
   double beta;            // FDM diagonal of discarded states: exp(-beta E) / zdisc
   double zdisc;
   double* rho;
+  // Tangent form (dE != NULL): rot is the rotated tangent, and a discarded
+  // state's diagonal is d[exp(-beta E) / zdisc] = exp(-beta E) / zdisc
+  // (-beta dE - dlogz), dlogz = d ln zdisc.
+  const double* dE;
+  double dlogz;
 };
 void launch_dm_trace(const DmTraceArgs& a, int nblocks, cudaStream_t s);
 
@@ -413,6 +419,23 @@ struct DmRecArgs {
   int64_t* totals;        // [4]
   double* key[4];
   double* w[4];
+  // Tangents along ntan (0 or 4) parameter directions, written by the
+  // scatter pass beside each record: d(rho A) and d(A rho) of direction p at
+  // dP1 / dP2 + p * pstride (the layout of P1 / P2), c_d's tangent dcd[p],
+  // the energies' tangents at dE + p * nstates, d ln Z of the last shell.
+  // Record q of list L gets tw[L][p * totals[L] + q] = d w and
+  // tg[L][p * totals[L] + q] = 2 w d key, so that the term's tangent is
+  // (d w + 2 w d key x) exp(-x^2), x = t - key.
+  int ntan;
+  const double* dP1;
+  const double* dP2;
+  int64_t pstride;
+  const double* dcd[4];
+  const double* dE;
+  int nstates;
+  double dlogz_last[4];
+  double* tw[4];
+  double* tg[4];
 };
 void launch_dm_records(const DmRecArgs& a, int pass, cudaStream_t s);  // pass 0 count + scan, 1 scatter
 
@@ -427,6 +450,7 @@ struct LehList {
   int shell, gauss;
   int nomega, omega_first;  // frequencies: omega_idx[omega_first .. +nomega)
   double* part;             // partial sums [chunk][nomega]
+  const double* g;          // tangent lists: 2 w d key per record (w holds d w)
 };
 // delta != 0: the tile's frequencies are evenly spaced in t by delta (a
 // log-spaced grid on a log-Gaussian list), and exp(-(t - key)^2) along the
@@ -452,6 +476,8 @@ struct LehmannArgs {      // A(omega) = sum_N sum_records w exp(-(t - key)^2) / 
   double* out;              // [nomega]
 };
 void launch_lehmann(const LehmannArgs& a, cudaStream_t s);       // the items (one shell's lists)
+// The same items over tangent lists: sum (d w + g x) exp(-x^2), x = t - key.
+void launch_lehmann_tangent(const LehmannArgs& a, cudaStream_t s);
 void launch_lehmann_fold(const LehmannArgs& a, cudaStream_t s);  // every list -> out
 
 }  // namespace nrg
