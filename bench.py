@@ -349,6 +349,117 @@ def gpu_dm(eng, W, nomega):
     return fwd, back, t["dm_spectral_ms"], t["lehmann_ms"], t["lehmann_pairs"], t["lehmann_evals"], A
 
 
+# The derivatives (--grad): d/d(eps_d, U, Gamma, B) of the one-channel
+# Anderson model at Lambda=2.5, U=0.4, eps_d=-0.2, Gamma=0.015, B=1e-6, 1000
+# kept, 45 iterations: <n_d> and T chi (four temperatures per iteration, 180
+# from 1e-10 to 1) from the (Q,Sz) sweep, which carries the field, and
+# A(omega) on 512 frequencies from the (Q,S) DM-NRG (T = 1e-8, b = 0.6), in
+# which B does not enter.
+GRAD_WORKLOAD = dict(nsites=45, ncutoff=1000, lam=2.5, U=0.4, ed=-0.2, gamma=0.015, B=1e-6)
+GRAD_NOMEGA = 512
+GRAD_NAME = ("derivatives of <n_d>, T chi(T) and A(omega) with respect to (eps_d, U, Gamma, B), one-channel "
+             "Anderson: Lambda=2.5, U=0.4, ed=-0.2, Gamma=0.015, B=1e-6, 45 iterations, 1000 kept; (Q,Sz) sweep "
+             "for <n_d> and T chi, (Q,S) DM-NRG (FDM, T=1e-8, b=0.6) for A(omega) on 512 frequencies "
+             "+-logspace(-10, 0, 256)")
+
+
+def fd_error(an, fd, floor=1e-3):
+    """max |analytic - central difference| over max(max |fd|, floor)."""
+    import numpy as np
+    return float(np.abs(an - fd).max() / max(float(np.abs(fd).max()), floor))
+
+
+def run_grad(args, rank: int, local: int) -> None:
+    """The derivatives of the fifth configuration with their cost against
+    the plain runs, checked against central differences of the GPU runs
+    (step 1e-5 |p|; 1e-7 for B) and against the Hellmann-Feynman averages of
+    the last iteration."""
+    import numpy as np
+    import torch
+    import twochnrg_gb300 as tg
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    eng = tg.Engine(local)
+    W = GRAD_WORKLOAD
+    args_qsz = ("1chQSz", W["nsites"], W["ncutoff"], W["lam"], W["U"], W["ed"], W["gamma"], W["B"])
+    k0 = eng.kernel_count
+    t0 = time.perf_counter()
+    g = eng.grad_forward(*args_qsz)
+    grad_ms = eng.timing()["device_ms"]
+    grad_wall = time.perf_counter() - t0
+    launches = eng.kernel_count - k0
+    eng.sweep(*args_qsz, fetch=False)
+    plain_ms = eng.timing()["device_ms"]
+    params = [W["ed"], W["U"], W["gamma"], W["B"]]
+    names = ["eps_d", "U", "Gamma", "B"]
+    fd_sweep = {}
+    for k in range(4):
+        h = 1e-7 if k == 3 else 1e-5 * abs(params[k])
+        pp, pm = list(params), list(params)
+        pp[k] += h
+        pm[k] -= h
+        rp = eng.sweep("1chQSz", W["nsites"], W["ncutoff"], W["lam"], pp[1], pp[0], pp[2], pp[3])
+        rm = eng.sweep("1chQSz", W["nsites"], W["ncutoff"], W["lam"], pm[1], pm[0], pm[2], pm[3])
+        # the derivatives are those of a fixed kept set: compare the
+        # iterations before the first one at which a displaced sweep keeps
+        # another set
+        n = 0
+        for a, b, c in zip(rp.iters, rm.iters, g.sweep.iters):
+            if not (np.array_equal(a.kept_bsize, c.kept_bsize) and np.array_equal(b.kept_bsize, c.kept_bsize)):
+                break
+            n += 1
+        fd_t = np.array([(a.thermo[:, 2] - b.thermo[:, 2]) / (2 * h) for a, b in zip(rp.iters[:n], rm.iters[:n])])
+        fd_n = np.array([(a.opavg[0] - b.opavg[0]) / (2 * h) for a, b in zip(rp.iters[:n], rm.iters[:n])])
+        fd_sweep[names[k]] = {"step": h, "iterations_compared": n,
+                              "tchi_rel_err": fd_error(g.d_thermo[:n, k, :, 2], fd_t) if n else None,
+                              "nd_rel_err": fd_error(g.d_opavg[:n, k, 0], fd_n) if n else None,
+                              "max_abs_dtchi": float(np.abs(fd_t).max()) if n else None,
+                              "tchi_abs_err_by_iteration": [float(f"{x:.3g}") for x in
+                                                            np.abs(g.d_thermo[:n, k, :, 2] - fd_t).max(axis=1)]}
+    last = g.sweep.iters[-1]
+    hf = {"dEgs_deps_d": float(g.d_egs[-1, 0]), "nd": float(last.opavg[0]),
+          "dEgs_dB": float(g.d_egs[-1, 3]), "Szdot": float(last.opavg[1])}
+    # A(omega): forward sweep with tangents, backward sweep, Lehmann sums
+    om = dm_omegas(GRAD_NOMEGA)
+    t1 = time.perf_counter()
+    eng.grad_forward_dm(W["nsites"], W["ncutoff"], W["lam"], W["U"], W["ed"], W["gamma"])
+    dm_fwd = eng.timing()["device_ms"]
+    prm = eng.dm_params(temp=DM_TEMP, bbroad=DM_BROAD)
+    eng.dm_backprop(prm)
+    dm_back = eng.timing()["dm_backprop_ms"]
+    _, A, dA = eng.lehmann_grad(prm, omegas=om)
+    dm_spec = eng.timing()["dm_spectral_ms"]
+    dm_wall = time.perf_counter() - t1
+    plain = gpu_dm(eng, dict(nsites=W["nsites"], ncutoff=W["ncutoff"], lam=W["lam"], U=W["U"], ed=W["ed"],
+                             gamma=W["gamma"]), GRAD_NOMEGA)
+    kept0 = [it.kept_bsize for it in eng.fetch().iters]
+    fd_dm = {}
+    for k in range(3):
+        h = 1e-5 * abs(params[k])
+        out, same = [], True
+        for sgn in (1, -1):
+            q = list(params)
+            q[k] += sgn * h
+            out.append(gpu_dm(eng, dict(nsites=W["nsites"], ncutoff=W["ncutoff"], lam=W["lam"], U=q[1], ed=q[0],
+                                        gamma=q[2]), GRAD_NOMEGA)[-1])
+            same = same and all(np.array_equal(a.kept_bsize, b) for a, b in zip(eng.fetch().iters, kept0))
+        fd = (out[0] - out[1]) / (2 * h)
+        fd_dm[names[k]] = {"step": h, "kept_sets_equal": bool(same), "rel_err": fd_error(dA[k], fd, 0.0),
+                           "max_abs_dA": float(np.abs(fd).max())}
+    line = {"metric": "derivatives of the sweep observables and of A(omega)", "value": (grad_ms + dm_fwd + dm_back
+            + dm_spec) * 1e-3, "unit": "s", "higher_is_better": False, "n_gpus": 1, "dtype": "f64",
+            "data": "synthetic (flat band Wilson chain)", "config": {"workload": GRAD_NAME},
+            "sweep_grad_s": grad_ms * 1e-3, "sweep_plain_s": plain_ms * 1e-3, "sweep_grad_wall_s": grad_wall,
+            "dm_grad_forward_s": dm_fwd * 1e-3, "dm_grad_backprop_s": dm_back * 1e-3,
+            "dm_grad_spectral_s": dm_spec * 1e-3, "dm_grad_wall_s": dm_wall,
+            "dm_plain_s": (plain[0] + plain[1] + plain[2]) * 1e-3,
+            "fd_sweep": fd_sweep, "fd_spectral": fd_dm, "hellmann_feynman_last_iteration": hf,
+            "sweep_grad_launches": launches}
+    print(json.dumps(line), flush=True)
+    eng.close()
+
+
 def run_dm2ch(args, rank: int, local: int) -> None:
     """One pass of the two-channel DM-NRG spectral function: forward sweep
     keeping the shells, density-matrix backward sweep, Lehmann sums.  The
@@ -415,6 +526,8 @@ def main():
     ap.add_argument("--dm2ch", action="store_true",
                     help="only the two-channel DM-NRG spectral function (about 8 minutes and 190 GB at 3000 kept)")
     ap.add_argument("--dm2ch-ncutoff", type=int, default=DM2_WORKLOAD["ncutoff"])
+    ap.add_argument("--grad", action="store_true",
+                    help="the derivatives (sweep observables and A(omega)) with their checks, one JSON line")
     ap.add_argument("--precision", default="fp64", choices=["mixed", "fp64"],
                     help="arithmetic of the timed sweeps (the other form is timed once after them)")
     args = ap.parse_args()
@@ -424,6 +537,9 @@ def main():
         return
     if args.dm2ch:
         run_dm2ch(args, rank, local)
+        return
+    if args.grad:
+        run_grad(args, rank, local)
         return
     dist = None
     if ws > 1:
