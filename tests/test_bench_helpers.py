@@ -44,3 +44,12 @@ def test_traffic_scaling():
 
     assert bench.sum_n2(R) == 2 * (9 + 16)
     assert bench.sum_n3(R) == 2 * (27 + 64)
+
+
+def test_fd_error():
+    an = np.array([1.0, 2.0, -3.0])
+    fd = np.array([1.0, 2.0, -3.0 + 3e-6])
+    assert abs(bench.fd_error(an, fd) - 1e-6) < 1e-12
+    # derivatives that vanish: the error is taken against the floor
+    assert abs(bench.fd_error(np.zeros(2), np.array([1e-9, -2e-9])) - 2e-6) < 1e-18
+    assert bench.fd_error(np.zeros(2), np.array([1e-9, -2e-9]), 0.0) == 1.0
