@@ -99,3 +99,32 @@ def test_dA_needs_the_tangent_shells(engine):
     cfg = tg.SweepConfig(tg.MODELS["2chQS"], ns, nc, lam, U, ed, G, G, 0.0, tg.PREC_FP64, 0.0)
     g = tg._Grad()
     assert engine.L.nrg_grad_forward_dm(engine.h, tg.ctypes.byref(cfg), tg.ctypes.byref(g)) == 1  # NRG_ERR_ARG
+
+
+def test_dA_matches_differences_of_the_oracle(engine):
+    """The same derivatives against central differences of the oracle's
+    DM-NRG (the reference's algorithm restated on the CPU), on a log grid at
+    T = D_8 / betabar."""
+    from oracle import oracle as orc
+    ns, nc, lam, U, ed, G = 12, 80, 2.5, 0.4, -0.15, 0.015
+    temp = 0.7 * lam ** (-(8 - 1) / 2.0) / 0.727
+    om = np.concatenate([-np.logspace(0, -5, 40), np.logspace(-5, 0, 40)])
+    engine.grad_forward_dm(ns, nc, lam, U, ed, G)
+    prm = engine.dm_params(temp=temp, bbroad=0.6)
+    engine.dm_backprop(prm)
+    _, A, dA = engine.lehmann_grad(prm, omegas=om)
+    params = [ed, U, G]
+    failures = []
+    for k in range(3):
+        h = 1e-5 * abs(params[k])
+        out = []
+        for sgn in (1, -1):
+            p = list(params)
+            p[k] += sgn * h
+            out.append(orc.dm_spectral(ns, nc, lam, p[1], p[0], p[2], temp, 0.6, omegas=om)[1])
+        fd = (out[0] - out[1]) / (2 * h)
+        err = np.abs(dA[k] - fd)
+        scale = np.abs(fd).max()
+        if (err > 1e-6 * scale + 1e-6 * np.abs(fd)).any():
+            failures.append(f"parameter {k}: max |analytic - fd| {err.max():.3e}, max |fd| {scale:.3e}")
+    assert not failures, "; ".join(failures)

@@ -63,6 +63,34 @@ def test_grad_matches_central_differences(engine, case):
     assert not failures, "; ".join(failures)
 
 
+def test_grad_matches_differences_of_the_oracle(engine):
+    """The asymmetric (Q,Sz) case against central differences of the oracle's
+    sweep (the reference's algorithm restated on the CPU)."""
+    from oracle import oracle as orc
+    case = CASES[0]
+    model, ns, nc, lam, U, ed, G, B = case
+    g = engine.grad_forward(*case)
+    params = [ed, U, G, B]
+    failures = []
+    for k in range(4):
+        h = 1e-6 if k == 3 else 1e-5 * abs(params[k])
+        runs = []
+        for sgn in (1, -1):
+            p = list(params)
+            p[k] += sgn * h
+            runs.append(orc.run(model, ns, nc, lam, p[1], p[0], p[2], p[3]))
+        assert all(a.nkept == b.nkept == c.nkept for a, b, c in zip(runs[0].iters, runs[1].iters, g.sweep.iters))
+        fd_t = np.array([(a.thermo[:, 2:] - b.thermo[:, 2:]) / (2 * h) for a, b in zip(runs[0].iters, runs[1].iters)])
+        fd_o = np.array([(a.opavg - b.opavg) / (2 * h) for a, b in zip(runs[0].iters, runs[1].iters)])
+        rel = 1e-5 if k == 3 else 1e-6
+        for what, fd, an in (("thermo", fd_t, g.d_thermo[:, k, :, 2:]), ("opavg", fd_o, g.d_opavg[:, k])):
+            scale = max(np.abs(fd).max(), 1e-3)
+            if (np.abs(an - fd) > rel * np.abs(fd) + rel * scale).any():
+                failures.append(f"parameter {k} {what}: max |analytic - fd| {np.abs(an - fd).max():.3e}, "
+                                f"max |fd| {np.abs(fd).max():.3e}")
+    assert not failures, "; ".join(failures)
+
+
 def test_backward_is_the_jacobian_contraction(engine):
     case = CASES[0]
     g = engine.grad_forward(*case)
