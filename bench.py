@@ -369,17 +369,13 @@ def fd_error(an, fd, floor=1e-3):
     return float(np.abs(an - fd).max() / max(float(np.abs(fd).max()), floor))
 
 
-def run_grad(args, rank: int, local: int) -> None:
+def gpu_grad(local: int) -> dict:
     """The derivatives of the fifth configuration with their cost against
     the plain runs, checked against central differences of the GPU runs
     (step 1e-5 |p|; 1e-7 for B) and against the Hellmann-Feynman averages of
-    the last iteration."""
+    the last iteration.  Runs on its own context, closed afterwards."""
     import numpy as np
-    import torch
     import twochnrg_gb300 as tg
-    if rank != 0:
-        return
-    torch.cuda.set_device(local)
     eng = tg.Engine(local)
     W = GRAD_WORKLOAD
     args_qsz = ("1chQSz", W["nsites"], W["ncutoff"], W["lam"], W["U"], W["ed"], W["gamma"], W["B"])
@@ -447,17 +443,29 @@ def run_grad(args, rank: int, local: int) -> None:
         fd = (out[0] - out[1]) / (2 * h)
         fd_dm[names[k]] = {"step": h, "kept_sets_equal": bool(same), "rel_err": fd_error(dA[k], fd, 0.0),
                            "max_abs_dA": float(np.abs(fd).max())}
-    line = {"metric": "derivatives of the sweep observables and of A(omega)", "value": (grad_ms + dm_fwd + dm_back
-            + dm_spec) * 1e-3, "unit": "s", "higher_is_better": False, "n_gpus": 1, "dtype": "f64",
-            "data": "synthetic (flat band Wilson chain)", "config": {"workload": GRAD_NAME},
+    eng.close()
+    return {"workload": GRAD_NAME, "unit": "s",
+            "total_s": (grad_ms + dm_fwd + dm_back + dm_spec) * 1e-3,
             "sweep_grad_s": grad_ms * 1e-3, "sweep_plain_s": plain_ms * 1e-3, "sweep_grad_wall_s": grad_wall,
             "dm_grad_forward_s": dm_fwd * 1e-3, "dm_grad_backprop_s": dm_back * 1e-3,
             "dm_grad_spectral_s": dm_spec * 1e-3, "dm_grad_wall_s": dm_wall,
             "dm_plain_s": (plain[0] + plain[1] + plain[2]) * 1e-3,
             "fd_sweep": fd_sweep, "fd_spectral": fd_dm, "hellmann_feynman_last_iteration": hf,
             "sweep_grad_launches": launches}
+
+
+def run_grad(args, rank: int, local: int) -> None:
+    """gpu_grad as its own JSON line."""
+    import torch
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    d = gpu_grad(local)
+    line = {"metric": "derivatives of the sweep observables and of A(omega)", "value": d.pop("total_s"),
+            "unit": d.pop("unit"), "higher_is_better": False, "n_gpus": 1, "dtype": "f64",
+            "data": "synthetic (flat band Wilson chain)", "config": {"workload": d.pop("workload")}}
+    line.update(d)
     print(json.dumps(line), flush=True)
-    eng.close()
 
 
 def run_dm2ch(args, rank: int, local: int) -> None:
@@ -698,6 +706,13 @@ def main():
             "sample": (f"oracle port (single thread) on {DM_SAMPLE['nsites']} iterations, {DM_SAMPLE['ncutoff']} "
                        f"kept, {DM_SAMPLE_NOMEGA} frequencies, same T and b; GPU on that case: "
                        f"{g[0] + g[1] + g[2]:.1f} ms")}
+    if not dist:
+        # the derivatives (fifth configuration) on a context of their own;
+        # a failure there is reported in the line, not raised
+        try:
+            line["derivatives"] = gpu_grad(local)
+        except Exception as e:  # noqa: BLE001
+            line["derivatives"] = {"error": f"{type(e).__name__}: {e}"}
     print(json.dumps(line), flush=True)
     eng.close()
     if dist:
