@@ -341,7 +341,9 @@ int big_block_threshold() {
 // trips of the Householder vector and y), so independent blocks on fewer SMs
 // each overlap those latencies.  Four grids of 38 SMs with blocks from 1800
 // states on measured fastest on the two-channel workload (1 to 8 grids and
-// thresholds 1500 to 3200 tried).
+// thresholds 1500 to 3200 tried), and again with the lower-triangle kernels:
+// iterations 3-7 at 3000 kept took 4.83 s, against 4.89 / 4.90 s for
+// thresholds 1400 / 2400, 5.34 / 5.36 / 5.74 s for 3 / 5 / 6 grids.
 // Mixed precision: blocks at least this large take the blocked reduction
 // with the tensor-core trailing product (the other large blocks the FP64
 // whole-grid kernel, the small ones the cluster kernel).
