@@ -413,6 +413,14 @@ def gpu_grad(local: int) -> dict:
                               "max_abs_dtchi": float(np.abs(fd_t).max()) if n else None,
                               "tchi_abs_err_by_iteration": [float(f"{x:.3g}") for x in
                                                             np.abs(g.d_thermo[:n, k, :, 2] - fd_t).max(axis=1)]}
+    # T chi and its derivatives on 64 temperatures log-spaced over [1e-10, 1e-2]
+    # (the sweep's own temperatures reach down to about 3e-9 in 45 iterations;
+    # below that the entries are null)
+    temps = np.logspace(-10, -2, 64)
+    tchi64, dtchi64 = g.tchi_on(temps)
+    nul = lambda a: [None if not np.isfinite(x) else float(x) for x in a]  # noqa: E731
+    tchi_grid = {"T": temps.tolist(), "tchi": nul(tchi64), "d_tchi": [nul(r) for r in dtchi64],
+                 "covered": int(np.isfinite(tchi64).sum())}
     last = g.sweep.iters[-1]
     hf = {"dEgs_deps_d": float(g.d_egs[-1, 0]), "nd": float(last.opavg[0]),
           "dEgs_dB": float(g.d_egs[-1, 3]), "Szdot": float(last.opavg[1])}
@@ -451,6 +459,7 @@ def gpu_grad(local: int) -> dict:
             "dm_grad_spectral_s": dm_spec * 1e-3, "dm_grad_wall_s": dm_wall,
             "dm_plain_s": (plain[0] + plain[1] + plain[2]) * 1e-3,
             "fd_sweep": fd_sweep, "fd_spectral": fd_dm, "hellmann_feynman_last_iteration": hf,
+            "tchi_64T": tchi_grid,
             "sweep_grad_launches": launches}
 
 

@@ -53,3 +53,31 @@ def test_fd_error():
     # derivatives that vanish: the error is taken against the floor
     assert abs(bench.fd_error(np.zeros(2), np.array([1e-9, -2e-9])) - 2e-6) < 1e-18
     assert bench.fd_error(np.zeros(2), np.array([1e-9, -2e-9]), 0.0) == 1.0
+
+
+def test_tchi_on_a_temperature_grid():
+    import twochnrg_gb300 as tg
+    lam, betabar, n = 2.5, 0.727, 6
+    its = []
+    for N in range(n):
+        DN = 0.5 * (1 + 1 / lam) * lam ** (-(N - 1) / 2.0)
+        betas = betabar * lam ** ((np.arange(1, 5) - 4) / 8.0)
+        th = np.zeros((4, 4))
+        th[:, 0], th[:, 1] = betas, DN / betas
+        th[:, 2] = 0.25 + 0.1 * np.log(th[:, 1])  # linear in ln T: interpolated exactly
+        its.append(tg.Iteration(params=np.zeros(4), qn=np.zeros((0, 2)), bsize=np.zeros(0, np.int64),
+                                en=np.zeros(0), emin=0.0, ecut=0.0, nkept=0, thermo=th, opavg=np.zeros(0),
+                                kept_bsize=np.zeros(0, np.int64)))
+    dth = np.zeros((n, 4, 4, 4))
+    for k in range(4):
+        dth[:, k, :, 2] = np.array([it.thermo[:, 2] for it in its]) * (k + 1)
+    g = tg.GradResult(tg.SweepResult(iters=its), dth, np.zeros((n, 4, 0)), np.zeros((n, 4)), np.zeros(n),
+                      np.zeros((n, 4)))
+    T = np.array([it.thermo[:, 1] for it in its]).ravel()
+    temps = np.array([T.min() / 2, T.min() * 1.3, np.sqrt(T.min() * T.max()), T.max() / 1.1, T.max() * 2])
+    tchi, dt = g.tchi_on(temps)
+    want = 0.25 + 0.1 * np.log(temps)
+    assert np.isnan(tchi[0]) and np.isnan(tchi[-1]) and np.isnan(dt[:, 0]).all()
+    np.testing.assert_allclose(tchi[1:-1], want[1:-1], rtol=1e-12)
+    for k in range(4):
+        np.testing.assert_allclose(dt[k, 1:-1], (k + 1) * want[1:-1], rtol=1e-12)

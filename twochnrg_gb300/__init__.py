@@ -72,6 +72,27 @@ class GradResult:
     egs: np.ndarray        # (nsites,) absolute ground-state energy
     d_egs: np.ndarray      # (nsites, 4)
 
+    def tchi_on(self, temps):
+        """T chi and d T chi / d p at the temperatures `temps`, linear in ln T
+        between the sweep's own temperatures (four per iteration, strictly
+        decreasing along the sweep); the derivatives are interpolated alike,
+        the interpolation being linear in the values.  The free chain's part
+        of T chi does not depend on the parameters, so d T chi is also the
+        derivative of the impurity's T chi.  Temperatures outside the sweep's
+        range get NaN.  Returns (tchi (m,), d_tchi (4, m))."""
+        T = np.array([it.thermo[:, 1] for it in self.sweep.iters]).ravel()
+        v = np.array([it.thermo[:, 2] for it in self.sweep.iters]).ravel()
+        d = self.d_thermo[:, :, :, 2].transpose(1, 0, 2).reshape(self.d_thermo.shape[1], -1)
+        o = np.argsort(T)
+        lt = np.log(T[o])
+        x = np.log(np.asarray(temps, dtype=np.float64))
+        out = (x < lt[0]) | (x > lt[-1])
+        tchi = np.interp(x, lt, v[o])
+        dt = np.array([np.interp(x, lt, dk[o]) for dk in d])
+        tchi[out] = np.nan
+        dt[:, out] = np.nan
+        return tchi, dt
+
 
 class Timing(ctypes.Structure):
     _fields_ = [("total_ms", ctypes.c_double), ("assemble_ms", ctypes.c_double),
